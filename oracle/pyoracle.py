@@ -1,0 +1,294 @@
+"""ctypes view of the CPU restatement in oracle/liboracle.so.
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by ``__graft_entry__.smoke()`` and by
+the benchmark's CPU-baseline leg, as the checker.  The product package never
+imports it.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+
+OR_RNG_MT19937, OR_RNG_PHILOX = 0, 1
+OR_PREC_REF64, OR_PREC_GPU32 = 0, 1
+OR_PSI_RBM, OR_PSI_DEEP, OR_PSI_PAIR = 0, 1, 2
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_up = C.POINTER(C.c_uint)
+_u64p = C.POINTER(C.c_uint64)
+
+
+class _Op(C.Structure):
+    _fields_ = [("S", C.c_int), ("L", C.c_int), ("coef", _dp), ("types", _ip), ("idx", _ip)]
+
+
+class _Psi(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int), ("N", C.c_int), ("prefactor", C.c_double),
+        ("M", C.c_int), ("b", _dp), ("W", _dp),
+        ("num_layers", C.c_int), ("size", C.c_int * 3), ("conn", C.c_int * 3),
+        ("lhs_conn", _up * 3), ("lhs_w", _dp * 3), ("bias", _dp * 3), ("final_w", _dp),
+        ("lhs_w_im", _dp * 3), ("bias_im", _dp * 3), ("final_w_im", _dp),
+        ("translational_invariance", C.c_int),
+    ]
+
+
+class _McCfg(C.Structure):
+    _fields_ = [
+        ("total_chains", C.c_int), ("chain_begin", C.c_int), ("num_chains", C.c_int),
+        ("samples_per_chain", C.c_int), ("num_sweeps", C.c_int), ("num_therm", C.c_int),
+        ("rng", C.c_int), ("seed", C.c_uint64), ("prec", C.c_int),
+        ("fast_sweep_tries", C.c_int), ("total_z", C.c_int), ("sector", C.c_int),
+    ]
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(os.path.join(HERE, "oracle.c")):
+            build()
+        L = C.CDLL(LIB_PATH)
+        L.or_philox_word.restype = C.c_uint32
+        L.or_philox_word.argtypes = [C.c_uint64, C.c_uint32, C.c_uint64]
+        L.or_lc_re_f32.restype = C.c_float
+        L.or_lc_re_f32.argtypes = [C.c_float, C.c_float]
+        L.or_expf_det.restype = C.c_float
+        L.or_expf_det.argtypes = [C.c_float]
+        L.or_exact_norm.restype = C.c_double
+        L.or_exact_hsd.restype = C.c_double
+        L.or_samples_hsd.restype = C.c_double
+        L.or_num_params.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _c128(a):
+    return np.ascontiguousarray(np.asarray(a, np.complex128))
+
+
+def _ptr(a, t=_dp):
+    return a.ctypes.data_as(t)
+
+
+class Op:
+    """Reference operator table (coefficients [S], pauli types / indices [S, L])."""
+
+    def __init__(self, coef, types, idx):
+        self.coef = _c128(coef)
+        self.types = np.ascontiguousarray(types, np.int32)
+        self.idx = np.ascontiguousarray(idx, np.int32)
+        self.c = _Op(len(self.coef), self.types.shape[1], _ptr(self.coef.view(np.float64)),
+                     _ptr(self.types, _ip), _ptr(self.idx, _ip))
+
+
+class RBM:
+    def __init__(self, b, W, prefactor=1.0):
+        self.b = _c128(b)
+        self.W = _c128(W)
+        self.N, self.M = self.W.shape
+        self.c = _Psi()
+        self.c.kind = OR_PSI_RBM
+        self.c.N = self.N
+        self.c.M = self.M
+        self.c.prefactor = prefactor
+        self.c.b = _ptr(self.b.view(np.float64))
+        self.c.W = _ptr(self.W.view(np.float64))
+
+    @property
+    def num_params(self):
+        return 2 * self.N + self.M + self.N * self.M
+
+
+class Deep:
+    """PsiDeep (pair=False) or PsiPair (pair=True) from complex per-layer arrays."""
+
+    def __init__(self, N, biases, connections, weights, final_weights, prefactor=1.0, pair=False,
+                 translational_invariance=False):
+        self.N = N
+        self.keep = []
+        self.c = _Psi()
+        self.c.kind = OR_PSI_PAIR if pair else OR_PSI_DEEP
+        self.c.N = N
+        self.c.prefactor = prefactor
+        self.c.num_layers = len(biases)
+        self.c.translational_invariance = int(translational_invariance)
+
+        def hold(a):
+            self.keep.append(a)
+            return a
+
+        for l, (b, cn, w) in enumerate(zip(biases, connections, weights)):
+            cn = hold(np.ascontiguousarray(cn, np.uint32))
+            self.c.size[l] = len(b)
+            self.c.conn[l] = cn.shape[0]
+            self.c.lhs_conn[l] = _ptr(cn, _up)
+            if pair:
+                self.c.lhs_w[l] = _ptr(hold(np.ascontiguousarray(np.real(w), np.float64)))
+                self.c.bias[l] = _ptr(hold(np.ascontiguousarray(np.real(b), np.float64)))
+                self.c.lhs_w_im[l] = _ptr(hold(np.ascontiguousarray(np.imag(w), np.float64)))
+                self.c.bias_im[l] = _ptr(hold(np.ascontiguousarray(np.imag(b), np.float64)))
+            else:
+                self.c.lhs_w[l] = _ptr(hold(_c128(w)).view(np.float64))
+                self.c.bias[l] = _ptr(hold(_c128(b)).view(np.float64))
+        if pair:
+            self.c.final_w = _ptr(hold(np.ascontiguousarray(np.real(final_weights), np.float64)))
+            self.c.final_w_im = _ptr(hold(np.ascontiguousarray(np.imag(final_weights), np.float64)))
+        else:
+            self.c.final_w = _ptr(hold(_c128(final_weights)).view(np.float64))
+
+    @property
+    def num_params(self):
+        return lib().or_num_params(C.byref(self.c))
+
+
+def nwords(N):
+    return (N + 63) // 64
+
+
+def spins_array(configs, N):
+    """uint64 bitsets [count, nwords] from python ints or a uint64 array."""
+    nw = nwords(N)
+    out = np.zeros((len(configs), nw), np.uint64)
+    for t, c in enumerate(configs):
+        c = int(c)
+        for k in range(nw):
+            out[t, k] = (c >> (64 * k)) & 0xFFFFFFFFFFFFFFFF
+    return out
+
+
+def log_psi(psi, spins):
+    out = np.zeros(2)
+    s = np.ascontiguousarray(spins, np.uint64)
+    lib().or_log_psi(C.byref(psi.c), _ptr(s, _u64p), _ptr(out))
+    return complex(out[0], out[1])
+
+
+def O_k(psi, spins):
+    P = psi.num_params
+    out = np.zeros(2 * P)
+    s = np.ascontiguousarray(spins, np.uint64)
+    lib().or_O_k(C.byref(psi.c), _ptr(s, _u64p), _ptr(out))
+    return out.view(np.complex128)
+
+
+def local_energy(psi, op, spins, lp=None):
+    s = np.ascontiguousarray(spins, np.uint64)
+    if lp is None:
+        lp = log_psi(psi, s)
+    lpa = np.array([lp.real, lp.imag])
+    out = np.zeros(2)
+    lib().or_local_energy(C.byref(psi.c), C.byref(op.c), _ptr(s, _u64p), _ptr(lpa), _ptr(out))
+    return complex(out[0], out[1])
+
+
+def exact_norm(psi):
+    return lib().or_exact_norm(C.byref(psi.c))
+
+
+def psi_vector(psi):
+    out = np.zeros(2 << psi.N)
+    lib().or_psi_vector(C.byref(psi.c), _ptr(out))
+    return out.view(np.complex128)
+
+
+def exact_fluctuation(psi, op):
+    E = np.zeros(2)
+    sig = C.c_double()
+    lib().or_exact_fluctuation(C.byref(psi.c), C.byref(op.c), _ptr(E), C.byref(sig))
+    return sig.value, complex(E[0], E[1])
+
+
+def exact_gradient(psi, op):
+    P = psi.num_params
+    g = np.zeros(2 * P)
+    E = np.zeros(2)
+    lib().or_exact_gradient(C.byref(psi.c), C.byref(op.c), _ptr(g), _ptr(E))
+    return g.view(np.complex128), complex(E[0], E[1])
+
+
+def exact_hsd(psi, psi_prime, op, is_unitary, nu=1.0, gradient=True):
+    P = psi_prime.num_params
+    g = np.zeros(2 * P) if gradient else None
+    d = lib().or_exact_hsd(C.byref(psi.c), C.byref(psi_prime.c), C.byref(op.c), int(is_unitary),
+                           C.c_double(nu), _ptr(g) if gradient else None)
+    return (g.view(np.complex128) if gradient else None), d
+
+
+def samples_gradient(psi, op, spins):
+    s = np.ascontiguousarray(spins, np.uint64)
+    P = psi.num_params
+    g = np.zeros(2 * P)
+    E = np.zeros(2)
+    lib().or_samples_gradient(C.byref(psi.c), C.byref(op.c), len(s), _ptr(s, _u64p), _ptr(g), _ptr(E))
+    return g.view(np.complex128), complex(E[0], E[1])
+
+
+def samples_hsd(psi, psi_prime, op, is_unitary, spins, nu=1.0, gradient=True):
+    s = np.ascontiguousarray(spins, np.uint64)
+    P = psi_prime.num_params
+    g = np.zeros(2 * P) if gradient else None
+    d = lib().or_samples_hsd(C.byref(psi.c), C.byref(psi_prime.c), C.byref(op.c), int(is_unitary), len(s),
+                             _ptr(s, _u64p), C.c_double(nu), _ptr(g) if gradient else None)
+    return (g.view(np.complex128) if gradient else None), d
+
+
+def mc_run(psi, op, num_chains, samples_per_chain, num_sweeps, num_therm, rng=OR_RNG_PHILOX, seed=0,
+           prec=OR_PREC_GPU32, chain_begin=0, total_chains=None, total_z=False, sector=0, fast_sweep_tries=0,
+           want_eloc=True):
+    """Runs chains and returns (spins [samples, chains, nwords], log_psi, eloc, accepts, rejects)."""
+    nw = nwords(psi.N)
+    cfg = _McCfg(total_chains or num_chains, chain_begin, num_chains, samples_per_chain, num_sweeps, num_therm,
+                 rng, seed, prec, fast_sweep_tries, int(total_z), sector)
+    spins = np.zeros((samples_per_chain, num_chains, nw), np.uint64)
+    lp = np.zeros((samples_per_chain, num_chains, 2))
+    el = np.zeros((samples_per_chain, num_chains, 2))
+    acc = np.zeros(num_chains, np.uint64)
+    rej = np.zeros(num_chains, np.uint64)
+    r = lib().or_mc_run(C.byref(psi.c), C.byref(op.c) if op is not None else None, C.byref(cfg),
+                        _ptr(spins, _u64p), _ptr(lp), _ptr(el) if (want_eloc and op is not None) else None,
+                        _ptr(acc, _u64p), _ptr(rej, _u64p))
+    if r != 0:
+        raise ValueError("oracle mc_run: unsupported configuration")
+    return (spins, lp.view(np.complex128)[..., 0], el.view(np.complex128)[..., 0], acc, rej)
+
+
+def logcosh(z):
+    out = np.zeros(2)
+    lib().or_logcosh(C.c_double(z.real), C.c_double(z.imag), _ptr(out))
+    return complex(out[0], out[1])
+
+
+def tanh(z):
+    out = np.zeros(2)
+    lib().or_tanh(C.c_double(z.real), C.c_double(z.imag), _ptr(out))
+    return complex(out[0], out[1])
+
+
+def philox_word(seed, walker, index):
+    return lib().or_philox_word(seed, walker, index)
+
+
+def mt_words(seed, count):
+    out = np.zeros(count, np.uint32)
+    lib().or_mt_words(C.c_uint32(seed), count, _ptr(out, C.POINTER(C.c_uint32)))
+    return out
+
+
+def expf_det(x):
+    return lib().or_expf_det(C.c_float(x))
+
+
+def lc_re_f32(x, y):
+    return lib().or_lc_re_f32(C.c_float(x), C.c_float(y))
