@@ -1,0 +1,206 @@
+/*
+ * rbmg — C ABI of the GB300 implementation of RBMonGPU's variational hot path.
+ *
+ * Plain C: opaque handles, host pointers and sizes, int status codes.  Complex
+ * numbers are interleaved (re, im) doubles, exactly the memory layout of
+ * numpy.complex128 / std::complex<double>.  Spin configurations are bitsets of
+ * ceil(N/64) uint64 words, bit i set <=> s_i = +1 (reference include/Spins.h:125-129).
+ *
+ * Every call is synchronous: results are on the host when it returns, as in the
+ * reference.  Handles are not thread-safe (the reference's objects are not either).
+ *
+ * Each declaration names the reference interface it replaces (paths relative to
+ * the RBMonGPU source tree; the Python names are those of pyRBMonGPU/main.cpp).
+ */
+#ifndef RBMG_H
+#define RBMG_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define RBMG_API __attribute__((visibility("default")))
+#else
+#define RBMG_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes: the reference throws std::runtime_error / calls exit
+ * (include/types.h:40-48, 83-97); here every failure is returned. */
+#define RBMG_OK 0
+#define RBMG_EINVAL 1        /* bad argument or shape */
+#define RBMG_ENOMEM 2        /* device allocation failed */
+#define RBMG_ECUDA 3         /* CUDA runtime error (message in rbmg_last_error) */
+#define RBMG_ETIMEOUT 4      /* a bounded device wait gave up */
+#define RBMG_ENAN 5          /* non-finite parameters or results */
+#define RBMG_EUNSUPPORTED 6  /* combination not provided (mirrors a missing reference instantiation) */
+
+typedef struct rbmg_psi rbmg_psi;
+typedef struct rbmg_operator rbmg_operator;
+typedef struct rbmg_ensemble rbmg_ensemble;
+
+/* last error message of the calling thread */
+RBMG_API const char* rbmg_last_error(void);
+/* library version string */
+RBMG_API const char* rbmg_version(void);
+
+/* setDevice (source/RBMonGPU.cu:7-9, pyRBMonGPU/main.cpp:611) */
+RBMG_API int rbmg_set_device(int device);
+/* start_profiling / stop_profiling (source/RBMonGPU.cu:11-17) */
+RBMG_API int rbmg_profiler_start(void);
+RBMG_API int rbmg_profiler_stop(void);
+
+/* activation_function (pyRBMonGPU/main.cpp:607-609): the reference's rational
+ * log-cosh, include/quantum_state/psi_functions.hpp:49-57, evaluated in FP64. */
+RBMG_API int rbmg_activation(double re, double im, double* out /* [2] */);
+
+/* ---------------------------------------------------------------- Psi (RBM)
+ * Psi(alpha, beta, b, W, prefactor, free_quantum_axis, gpu)
+ * (include/quantum_state/Psi.hpp:361-378, pyRBMonGPU/main.cpp:50-59).
+ * alpha, beta: [N] real; b: [M] complex; W: [N, M] complex row-major.
+ * Like the reference (include/quantum_state/PsiBase.hpp:239-249) beta is
+ * initialised from alpha.  free_quantum_axis != 0 returns RBMG_EUNSUPPORTED. */
+RBMG_API int rbmg_psi_create(int N, int M, const double* alpha, const double* beta, const double* b, const double* W,
+                    double prefactor, int free_quantum_axis, rbmg_psi** out);
+
+/* PsiDeep(alpha, beta, b_list, connections_list, W_list, final_weights, prefactor,
+ * free_quantum_axis, gpu) (include/quantum_state/PsiDeep.hpp:339-400,
+ * pyRBMonGPU/main.cpp:97-108) and, with pair != 0, PsiPair(...) with the same
+ * arguments (include/quantum_state/PsiPair.hpp:166-205, main.cpp:138-149).
+ * Layer l has sizes[l] units and conns[l] inputs per unit; connections[l] is
+ * [conns[l], sizes[l]] uint32, biases[l] [sizes[l]] complex, weights[l]
+ * [conns[l], sizes[l]] complex, final_weights [sizes[L-1]] complex. */
+RBMG_API int rbmg_psi_deep_create(int N, int num_layers, const int* sizes, const int* conns,
+                         const uint32_t* const* connections, const double* const* biases,
+                         const double* const* weights, const double* final_weights, const double* alpha,
+                         const double* beta, double prefactor, int free_quantum_axis, int pair, rbmg_psi** out);
+
+/* Psi.copy() / PsiDeep.copy() (source/quantum_state/Psi.cu:17-29); all fields are
+ * copied, including the O_k length the reference's copy drops. */
+RBMG_API int rbmg_psi_copy(const rbmg_psi* psi, rbmg_psi** out);
+RBMG_API int rbmg_psi_destroy(rbmg_psi* psi);
+
+/* psi kind: 0 Psi, 1 PsiDeep, 2 PsiPair */
+RBMG_API int rbmg_psi_kind(const rbmg_psi* psi, int* kind);
+/* N, M (RBM) or width (deep), num_params (Psi.hpp:372, PsiDeep.cu:34-66) */
+RBMG_API int rbmg_psi_shape(const rbmg_psi* psi, int* N, int* M, int* num_params);
+/* params getter / setter, layout [alpha(N), beta(N), ...] (Psi.cu:71-92, PsiDeep.cu:120-177,
+ * PsiPair.cu:34-76); values cross as complex128, the device holds complex64. */
+RBMG_API int rbmg_psi_get_params(const rbmg_psi* psi, double* params /* [2 P] */);
+RBMG_API int rbmg_psi_set_params(rbmg_psi* psi, const double* params /* [2 P] */);
+RBMG_API int rbmg_psi_get_prefactor(const rbmg_psi* psi, double* prefactor);
+RBMG_API int rbmg_psi_set_prefactor(rbmg_psi* psi, double prefactor);
+/* PsiDeep.translational_invariance (pyRBMonGPU/main.cpp:111) */
+RBMG_API int rbmg_psi_set_translational_invariance(rbmg_psi* psi, int on);
+
+/* log psi(s) for a batch of configurations (Psi::log_psi_s_std, source/quantum_state/Psi.cu:57-58),
+ * without the prefactor; out [2 count]. */
+RBMG_API int rbmg_psi_log_psi(const rbmg_psi* psi, int count, const uint64_t* spins, double* out);
+
+/* Psi.vector: psi over all 2^N basis states, index = bit pattern
+ * (source/network_functions/PsiVector.cu:13-51); out [2 * 2^N]. */
+RBMG_API int rbmg_psi_vector(const rbmg_psi* psi, double* out);
+
+/* psi.norm(exact_summation) = sqrt(sum_s prefactor^2 |psi(s)|^2)
+ * (source/network_functions/PsiNorm.cu:13-44), via an FP64 log-sum-exp. */
+RBMG_API int rbmg_psi_norm(const rbmg_psi* psi, rbmg_ensemble* exact_summation, double* norm);
+
+/* psi_O_k_vector(psi, spins) (source/network_functions/PsiOkVector.cu:9-44); entries [0, 2N) are 0. */
+RBMG_API int rbmg_psi_O_k_vector(const rbmg_psi* psi, const uint64_t* spins, double* out /* [2 P] */);
+
+/* ---------------------------------------------------------------- Operator
+ * Operator(coefficients[S], pauli_types[S, L], pauli_indices[S, L], gpu)
+ * (include/operator/Operator.hpp:394-409, pyRBMonGPU/main.cpp:240-245): types
+ * 0 = I, 1 = X, 2 = Y, 3 = Z; an index of -1 ends a string. */
+RBMG_API int rbmg_operator_create(int num_strings, int max_string_length, const double* coefficients, const int* pauli_types,
+                         const int* pauli_indices, rbmg_operator** out);
+RBMG_API int rbmg_operator_destroy(rbmg_operator* op);
+/* num_strings, max_string_length, coefficients / pauli_types / pauli_indices getters (main.cpp:252-256) */
+RBMG_API int rbmg_operator_shape(const rbmg_operator* op, int* num_strings, int* max_string_length);
+RBMG_API int rbmg_operator_tables(const rbmg_operator* op, double* coefficients, int* pauli_types, int* pauli_indices);
+
+/* ---------------------------------------------------------------- ensembles
+ * MonteCarloLoop(num_samples, num_sweeps, num_thermalization_sweeps, num_markov_chains, gpu)
+ * (source/spin_ensembles/MonteCarloLoop.cu:20-42, pyRBMonGPU/main.cpp:276-284).
+ * Each chain is a Philox4x32-10 stream keyed by `seed`; num_samples must be a
+ * multiple of num_markov_chains (MonteCarloLoop.cu:78). */
+RBMG_API int rbmg_mc_create(uint32_t num_samples, uint32_t num_sweeps, uint32_t num_thermalization_sweeps,
+                   uint32_t num_markov_chains, uint64_t seed, rbmg_ensemble** out);
+/* MonteCarloLoop(MonteCarloLoop&) (MonteCarloLoop.cu:44-66): same settings, fresh streams */
+RBMG_API int rbmg_mc_copy(const rbmg_ensemble* other, rbmg_ensemble** out);
+/* set_total_z_symmetry / set_fast_sweep (include/spin_ensembles/MonteCarloLoop.hpp:283-291) */
+RBMG_API int rbmg_mc_set_total_z_symmetry(rbmg_ensemble* mc, int sector);
+RBMG_API int rbmg_mc_set_fast_sweep(rbmg_ensemble* mc, uint32_t num_tries);
+/* acceptance counters of the last sampling call (MonteCarloLoop.hpp:215-219), summed
+ * over chains; per_chain_accepts may be NULL or [num_markov_chains]. */
+RBMG_API int rbmg_mc_acceptance(const rbmg_ensemble* mc, uint64_t* accepts, uint64_t* proposals, uint64_t* per_chain_accepts);
+
+/* ExactSummation(N, gpu) (source/spin_ensembles/ExactSummation.cu:16-24, main.cpp:288-291) */
+RBMG_API int rbmg_exact_create(uint32_t num_spins, rbmg_ensemble** out);
+/* ExactSummation.set_total_z_symmetry (ExactSummation.cu:26-45) */
+RBMG_API int rbmg_exact_set_total_z_symmetry(rbmg_ensemble* exact, int sector);
+
+/* num_steps (main.cpp:281, 291) */
+RBMG_API int rbmg_ensemble_num_steps(const rbmg_ensemble* ens, uint64_t* num_steps);
+RBMG_API int rbmg_ensemble_destroy(rbmg_ensemble* ens);
+
+/* Runs the ensemble's foreach (MonteCarloLoop.hpp:294-339) and records, per sample
+ * index (step * chains + chain), the configuration, log psi and local energy.
+ * spins [num_steps * nwords], log_psi / eloc [2 * num_steps]; any may be NULL;
+ * eloc needs op.  (Extension: the reference exposes this only to C++ lambdas.) */
+RBMG_API int rbmg_ensemble_samples(rbmg_ensemble* ens, const rbmg_psi* psi, const rbmg_operator* op, uint64_t* spins,
+                          double* log_psi, double* eloc);
+
+/* ---------------------------------------------------------------- ExpectationValue
+ * (source/network_functions/ExpectationValue.cu, pyRBMonGPU/main.cpp:295-339) */
+/* __call__(psi, operator, ensemble) -> <O>                        (:17-73)  */
+RBMG_API int rbmg_ev_value(const rbmg_psi* psi, const rbmg_operator* op, rbmg_ensemble* ens, double* value /* [2] */);
+/* __call__(psi, [operators], ensemble) -> [<O_i>]                 (:448-518) */
+RBMG_API int rbmg_ev_values(const rbmg_psi* psi, const rbmg_operator* const* ops, int num_ops, rbmg_ensemble* ens,
+                   double* values /* [2 num_ops] */);
+/* fluctuation -> (sigma, <O>)                                     (:130-175) */
+RBMG_API int rbmg_ev_fluctuation(const rbmg_psi* psi, const rbmg_operator* op, rbmg_ensemble* ens, double* sigma,
+                        double* value /* [2] */);
+/* gradient -> (grad[P], <O>), grad_k = <E O_k*> + conj<E_k> - 2 <E> <O_k*>   (:177-256) */
+RBMG_API int rbmg_ev_gradient(const rbmg_psi* psi, const rbmg_operator* op, rbmg_ensemble* ens, double* grad /* [2P] */,
+                     double* value /* [2] */);
+
+/* ---------------------------------------------------------------- HilbertSpaceDistance
+ * (source/network_functions/HilbertSpaceDistance.cu:14-269, HilbertSpaceDistance_PsiPair.cu:99-169,
+ * pyRBMonGPU/main.cpp:342-418).  The ensemble samples psi. */
+RBMG_API int rbmg_hsd_distance(const rbmg_psi* psi, const rbmg_psi* psi_prime, const rbmg_operator* op, int is_unitary,
+                      rbmg_ensemble* ens, double* distance);
+RBMG_API int rbmg_hsd_gradient(const rbmg_psi* psi, const rbmg_psi* psi_prime, const rbmg_operator* op, int is_unitary,
+                      rbmg_ensemble* ens, float nu, double* grad /* [2 P'] */, double* distance);
+
+/* ---------------------------------------------------------------- persistent chains
+ * Extension without a reference counterpart: the reference's foreach re-draws and
+ * re-thermalises its chains on every call (include/spin_ensembles/MonteCarloLoop.hpp:79-105);
+ * a chain handle keeps the walkers' configurations and Philox positions on the device
+ * between calls, for long runs measured sweep by sweep (autocorrelation times).
+ * The step is the reference's MonteCarloLoop step (MonteCarloLoop.hpp:153-256). */
+typedef struct rbmg_chain rbmg_chain;
+RBMG_API int rbmg_chain_create(const rbmg_psi* psi, uint32_t num_walkers, uint64_t seed, rbmg_chain** out);
+RBMG_API int rbmg_chain_destroy(rbmg_chain* chain);
+/* Runs n_sweeps sweeps (N proposals each) of every walker; after every
+ * `measure_every`-th sweep the local energies of all walkers are written to
+ * d_eloc_out, a DEVICE array of double2 [n_sweeps / measure_every][num_walkers]
+ * (NULL: no measurement).  `stream` is a cudaStream_t (NULL: the library's stream);
+ * the call returns without synchronising. */
+RBMG_API int rbmg_chain_sweep_async(rbmg_chain* chain, const rbmg_psi* psi, const rbmg_operator* op, int n_sweeps,
+                                    int measure_every, void* d_eloc_out, void* stream);
+/* host copies of the walkers' configurations [num_walkers * nwords] and acceptance counters */
+RBMG_API int rbmg_chain_state(const rbmg_chain* chain, uint64_t* spins, uint64_t* accepts, uint64_t* proposals);
+/* the library's CUDA stream of the calling thread, as a cudaStream_t */
+RBMG_API int rbmg_stream(void** stream);
+
+/* FP32 FMA throughput of the current device in TFLOP/s (a probe kernel of `iters`
+ * x 128 independent FMAs per thread), the roofline denominator of the sampler. */
+RBMG_API int rbmg_probe_fp32_tflops(int iters, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

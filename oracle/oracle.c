@@ -168,18 +168,20 @@ static void rng_spins(rng_t* r, int N, uint64_t* s) {
     spins_mask(s, N);
 }
 
-/* include/random.h:60-79 (int shifts as in the reference, valid for n < 32). */
+/* include/random.h:60-79.  The reference shifts an int (valid for n < 32); the same
+ * steps with 64-bit masks, identical for n < 32 and defined up to n = 64. */
 static uint64_t rng_n_over_k(rng_t* r, unsigned n, unsigned k) {
+    const uint64_t mask = n >= 64 ? ~(uint64_t)0 : (((uint64_t)1 << n) - 1u);
     uint64_t w = rng_u32(r);
     w |= (uint64_t)rng_u32(r) << 32;
-    uint64_t result = w & (uint64_t)((1 << n) - 1);
+    uint64_t result = w & mask;
     int diff = (int)k - (int)__builtin_popcountll(result);
     while (diff != 0) {
         uint64_t w2 = rng_u32(r);
         w2 |= (uint64_t)rng_u32(r) << 32;
         unsigned pos = (unsigned)(w2 % n);
-        while (((result & (uint64_t)(1 << pos)) != 0) == (diff > 0)) pos = (pos + 1) % n;
-        result ^= (uint64_t)(1 << pos);
+        while (((result >> pos) & 1u) == (uint64_t)(diff > 0)) pos = (pos + 1) % n;
+        result ^= (uint64_t)1 << pos;
         if (diff > 0) diff--; else diff++;
     }
     return result;
@@ -1035,7 +1037,12 @@ int or_mc_run(const or_psi* psi, const or_op* op, const or_mc_cfg* cfg,
             c.tr_i = c.tr_r + mpad32(M);
             c.tre = c.tr_i + mpad32(M);
         }
-        chain_init_spins(&c);
+        if (cfg->state_spins && cfg->resume) {
+            memcpy(c.s, cfg->state_spins + (size_t)cc * nw, sizeof(uint64_t) * nw);
+            c.rng.index = cfg->state_rng[cc];
+        } else {
+            chain_init_spins(&c);
+        }
         const int fast = cfg->fast_sweep_tries > 0;
         if (cfg->prec == OR_PREC_REF64) {
             if (M > 0) for (int j = 0; j < M; j++) c.theta[j] = rbm_angle(psi, j, c.s);
@@ -1074,6 +1081,10 @@ int or_mc_run(const or_psi* psi, const or_op* op, const or_mc_cfg* cfg,
         }
         if (accepts) accepts[cc] = c.acc;
         if (rejects) rejects[cc] = c.rej;
+        if (cfg->state_spins) {
+            memcpy(cfg->state_spins + (size_t)cc * nw, c.s, sizeof(uint64_t) * nw);
+            cfg->state_rng[cc] = c.rng.index;
+        }
         free(c.theta);
         free(c.th_r);
     }

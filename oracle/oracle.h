@@ -119,6 +119,12 @@ typedef struct {
     int fast_sweep_tries;   /* 0 = single-spin sweeps */
     int total_z;            /* 1 = S_z-conserving pair updates */
     int sector;
+    /* optional persistent state of the chains (Philox streams only): when state_spins is
+     * set and resume != 0 the chains continue from these configurations and stream
+     * positions instead of drawing fresh starts; both are updated on return */
+    uint64_t* state_spins;   /* [num_chains][nwords] */
+    uint64_t* state_rng;     /* [num_chains] next Philox word */
+    int resume;
 } or_mc_cfg;
 
 int or_mc_run(const or_psi* psi, const or_op* op, const or_mc_cfg* cfg,

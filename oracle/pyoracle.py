@@ -44,6 +44,7 @@ class _McCfg(C.Structure):
         ("samples_per_chain", C.c_int), ("num_sweeps", C.c_int), ("num_therm", C.c_int),
         ("rng", C.c_int), ("seed", C.c_uint64), ("prec", C.c_int),
         ("fast_sweep_tries", C.c_int), ("total_z", C.c_int), ("sector", C.c_int),
+        ("state_spins", _u64p), ("state_rng", _u64p), ("resume", C.c_int),
     ]
 
 
@@ -246,11 +247,18 @@ def samples_hsd(psi, psi_prime, op, is_unitary, spins, nu=1.0, gradient=True):
 
 def mc_run(psi, op, num_chains, samples_per_chain, num_sweeps, num_therm, rng=OR_RNG_PHILOX, seed=0,
            prec=OR_PREC_GPU32, chain_begin=0, total_chains=None, total_z=False, sector=0, fast_sweep_tries=0,
-           want_eloc=True):
-    """Runs chains and returns (spins [samples, chains, nwords], log_psi, eloc, accepts, rejects)."""
+           want_eloc=True, state=None):
+    """Runs chains and returns (spins [samples, chains, nwords], log_psi, eloc, accepts, rejects).
+    state: optional (spins [chains, nwords] uint64, rng [chains] uint64, resume flag list) carried
+    between calls."""
     nw = nwords(psi.N)
     cfg = _McCfg(total_chains or num_chains, chain_begin, num_chains, samples_per_chain, num_sweeps, num_therm,
                  rng, seed, prec, fast_sweep_tries, int(total_z), sector)
+    if state is not None:
+        cfg.state_spins = _ptr(state[0], _u64p)
+        cfg.state_rng = _ptr(state[1], _u64p)
+        cfg.resume = int(state[2][0])
+        state[2][0] = 1
     spins = np.zeros((samples_per_chain, num_chains, nw), np.uint64)
     lp = np.zeros((samples_per_chain, num_chains, 2))
     el = np.zeros((samples_per_chain, num_chains, 2))

@@ -1,0 +1,663 @@
+"""Python classes with the names, arguments and results of RBMonGPU's pybind11 module
+(pyRBMonGPU/main.cpp:45-614) and its Python veneer (pyRBMonGPU/Psi.py, PsiDeep.py,
+PsiPair.py), implemented over the C ABI of include/rbmg.h.
+
+Every computation runs in the CUDA library; the ``gpu`` arguments are accepted for
+signature compatibility only.
+"""
+import ctypes as C
+import json
+import math
+
+import numpy as np
+
+from ._lib import RbmgError, call, lib
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_u64p = C.POINTER(C.c_uint64)
+
+
+def _c128(a):
+    return np.ascontiguousarray(np.asarray(a, dtype=np.complex128))
+
+
+def _f64(a):
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+
+
+def _p(a, t=_dp):
+    return a.ctypes.data_as(t)
+
+
+def _handle():
+    return C.c_void_p()
+
+
+def nwords(N):
+    return (N + 63) // 64
+
+
+def spins_to_words(spins, N):
+    """Accepts a Spins, a python int bit pattern, or a uint64 word array."""
+    if isinstance(spins, Spins):
+        return spins.words()
+    if isinstance(spins, (int, np.integer)):
+        v = int(spins)
+        return np.array([(v >> (64 * k)) & 0xFFFFFFFFFFFFFFFF for k in range(nwords(N))], np.uint64)
+    w = np.ascontiguousarray(np.asarray(spins, dtype=np.uint64)).reshape(-1)
+    if w.size != nwords(N):
+        raise ValueError("spin configuration has the wrong number of words")
+    return w
+
+
+# --------------------------------------------------------------------- helpers
+def setDevice(device):
+    call("rbmg_set_device", int(device))
+
+
+def start_profiling():
+    call("rbmg_profiler_start")
+
+
+def stop_profiling():
+    call("rbmg_profiler_stop")
+
+
+def activation_function(z):
+    """The reference's rational log-cosh (include/quantum_state/psi_functions.hpp:49-57)."""
+    z = complex(z)
+    out = np.zeros(2)
+    call("rbmg_activation", z.real, z.imag, _p(out))
+    return complex(out[0], out[1])
+
+
+class Spins:
+    """Bit-packed spin configuration: bit i set <=> s_i = +1 (include/Spins.h:222-333)."""
+
+    def __init__(self, configuration, num_spins):
+        self.N = int(num_spins)
+        mask = (1 << self.N) - 1
+        self.configuration = int(configuration) & mask
+
+    def array(self, num_spins=None):
+        n = self.N if num_spins is None else num_spins
+        return np.array([1.0 if (self.configuration >> i) & 1 else -1.0 for i in range(n)])
+
+    def flip(self, position):
+        return Spins(self.configuration ^ (1 << position), self.N)
+
+    def rotate_left(self, shift, N):
+        c = self.configuration
+        return Spins(((c << shift) | (c >> (N - shift))) & ((1 << N) - 1), N)
+
+    def hamming_distance(self, other):
+        return bin(self.configuration ^ other.configuration).count("1")
+
+    def words(self):
+        return spins_to_words(self.configuration, self.N)
+
+
+# --------------------------------------------------------------------- states
+class _PsiBase:
+    _h = None
+
+    def __del__(self):
+        h, self._h = self._h, None
+        if h is not None and lib is not None:
+            try:
+                lib().rbmg_psi_destroy(h)
+            except Exception:
+                pass
+
+    @property
+    def N(self):
+        n = C.c_int()
+        call("rbmg_psi_shape", self._h, C.byref(n), None, None)
+        return n.value
+
+    @property
+    def num_params(self):
+        p = C.c_int()
+        call("rbmg_psi_shape", self._h, None, None, C.byref(p))
+        return p.value
+
+    @property
+    def params(self):
+        out = np.zeros(self.num_params, np.complex128)
+        call("rbmg_psi_get_params", self._h, _p(out.view(np.float64)))
+        return out
+
+    @params.setter
+    def params(self, new_params):
+        v = _c128(new_params)
+        if v.size != self.num_params:
+            raise ValueError("params has the wrong length")
+        call("rbmg_psi_set_params", self._h, _p(v.view(np.float64)))
+
+    @property
+    def prefactor(self):
+        v = C.c_double()
+        call("rbmg_psi_get_prefactor", self._h, C.byref(v))
+        return v.value
+
+    @prefactor.setter
+    def prefactor(self, value):
+        call("rbmg_psi_set_prefactor", self._h, float(value))
+
+    @property
+    def alpha(self):
+        return self.params[: self.N].real.copy()
+
+    @property
+    def beta(self):
+        return self.params[self.N: 2 * self.N].real.copy()
+
+    @property
+    def gpu(self):
+        return True
+
+    @property
+    def free_quantum_axis(self):
+        return False
+
+    def _vector(self):
+        out = np.zeros(1 << self.N, np.complex128)
+        call("rbmg_psi_vector", self._h, _p(out.view(np.float64)))
+        return out
+
+    @property
+    def vector(self):
+        # alpha / beta rotations of pyRBMonGPU/Psi.py:88-100 need QuantumExpression; with the
+        # free quantum axis unsupported they are zero and the vector is the plain amplitude list
+        return self._vector()
+
+    def norm(self, exact_summation):
+        v = C.c_double()
+        call("rbmg_psi_norm", self._h, exact_summation._h, C.byref(v))
+        return v.value
+
+    def normalize(self, exact_summation):
+        """pyRBMonGPU/Psi.py:54-55 (PsiDeep.py:55-57 resets the prefactor to 1 first)."""
+        if isinstance(self, PsiDeep):
+            self.prefactor = 1.0
+        self.prefactor = self.prefactor / self.norm(exact_summation)
+
+    def copy(self):
+        h = _handle()
+        call("rbmg_psi_copy", self._h, C.byref(h))
+        obj = object.__new__(type(self))
+        obj.__dict__.update(self.__dict__)
+        obj._h = h
+        return obj
+
+    def __pos__(self):
+        return self.copy()
+
+    def log_psi_s(self, spins):
+        w = spins_to_words(spins, self.N)
+        out = np.zeros(2)
+        call("rbmg_psi_log_psi", self._h, 1, _p(w, _u64p), _p(out))
+        return complex(out[0], out[1])
+
+    def log_psi_batch(self, spins_words):
+        w = np.ascontiguousarray(spins_words, np.uint64).reshape(-1, nwords(self.N))
+        out = np.zeros(2 * len(w))
+        call("rbmg_psi_log_psi", self._h, len(w), _p(w, _u64p), _p(out))
+        return out.view(np.complex128)
+
+
+class Psi(_PsiBase):
+    """Complex RBM: Psi(alpha, beta, b, W, prefactor, free_quantum_axis, gpu)
+    (include/quantum_state/Psi.hpp:361-378)."""
+
+    def __init__(self, alpha, beta, b, W, prefactor=1.0, free_quantum_axis=False, gpu=True):
+        b = _c128(b)
+        W = _c128(W)
+        N, M = W.shape
+        if b.shape != (M,):
+            raise ValueError("b must have M entries")
+        alpha = _f64(alpha) if alpha is not None else np.zeros(N)
+        beta = _f64(beta) if beta is not None else np.zeros(N)
+        h = _handle()
+        call("rbmg_psi_create", N, M, _p(alpha), _p(beta), _p(b.view(np.float64)), _p(W.view(np.float64)),
+             float(prefactor), int(bool(free_quantum_axis)), C.byref(h))
+        self._h = h
+
+    @property
+    def M(self):
+        m = C.c_int()
+        call("rbmg_psi_shape", self._h, None, C.byref(m), None)
+        return m.value
+
+    @property
+    def num_angles(self):
+        return self.M
+
+    @property
+    def b(self):
+        N, M = self.N, self.M
+        return self.params[2 * N: 2 * N + M].copy()
+
+    @b.setter
+    def b(self, value):
+        p = self.params
+        N, M = self.N, self.M
+        p[2 * N: 2 * N + M] = _c128(value)
+        self.params = p
+
+    @property
+    def W(self):
+        N, M = self.N, self.M
+        return self.params[2 * N + M:].reshape(N, M).copy()
+
+    @W.setter
+    def W(self, value):
+        p = self.params
+        N, M = self.N, self.M
+        p[2 * N + M:] = _c128(value).reshape(-1)
+        self.params = p
+
+    def to_json(self):
+        """pyRBMonGPU/Psi.py:8-22"""
+        def cplx(a):
+            a = np.asarray(a)
+            return {"real": a.real.tolist(), "imag": a.imag.tolist()}
+        return {"type": "Psi", "alpha": self.alpha.tolist(), "beta": self.beta.tolist(), "b": cplx(self.b),
+                "W": cplx(self.W), "prefactor": self.prefactor}
+
+    @staticmethod
+    def from_json(obj, gpu=True):
+        def arr(v):
+            if isinstance(v, dict):
+                return np.asarray(v["real"]) + 1j * np.asarray(v["imag"])
+            return np.asarray(v)
+        return Psi(arr(obj["alpha"]).real, arr(obj["beta"]).real, arr(obj["b"]), arr(obj["W"]), obj["prefactor"],
+                   False, gpu)
+
+
+class PsiDeep(_PsiBase):
+    """Sparse feed-forward net (include/quantum_state/PsiDeep.hpp:339-400):
+    PsiDeep(alpha, beta, b_list, connections_list, W_list, final_weights, prefactor,
+    free_quantum_axis, gpu).  PsiPair subclasses it with two real nets."""
+
+    _pair = 0
+
+    def __init__(self, alpha, beta, b, connections, W, final_weights, prefactor=1.0, free_quantum_axis=False,
+                 gpu=True):
+        bl = [_c128(x) for x in b]
+        cl = [np.ascontiguousarray(np.asarray(c), dtype=np.uint32) for c in connections]
+        wl = [_c128(w) for w in W]
+        fw = _c128(final_weights)
+        L = len(bl)
+        N = len(np.asarray(alpha)) if alpha is not None else int(max(int(cl[0].max()) + 1, 1))
+        sizes = (C.c_int * L)(*[len(x) for x in bl])
+        conns = (C.c_int * L)(*[c.shape[0] for c in cl])
+        for l in range(L):
+            if cl[l].shape != (conns[l], sizes[l]) or wl[l].shape != (conns[l], sizes[l]):
+                raise ValueError(f"layer {l}: connections and weights must be [connectivity, size]")
+        cptr = (C.POINTER(C.c_uint32) * L)(*[c.ctypes.data_as(C.POINTER(C.c_uint32)) for c in cl])
+        bptr = (_dp * L)(*[_p(x.view(np.float64)) for x in bl])
+        wptr = (_dp * L)(*[_p(x.view(np.float64)) for x in wl])
+        alpha = _f64(alpha) if alpha is not None else np.zeros(N)
+        beta = _f64(beta) if beta is not None else np.zeros(N)
+        h = _handle()
+        call("rbmg_psi_deep_create", N, L, sizes, conns, cptr, bptr, wptr, _p(fw.view(np.float64)), _p(alpha),
+             _p(beta), float(prefactor), int(bool(free_quantum_axis)), self._pair, C.byref(h))
+        self._h = h
+        self._shapes = [(int(conns[l]), int(sizes[l])) for l in range(L)]
+        self._connections = [c.copy() for c in cl]
+        self._ti = False
+
+    @property
+    def translational_invariance(self):
+        return self._ti
+
+    @translational_invariance.setter
+    def translational_invariance(self, on):
+        call("rbmg_psi_set_translational_invariance", self._h, int(bool(on)))
+        self._ti = bool(on)
+
+    def _split(self):
+        p = self.params[2 * self.N:]
+        out, k = [], 0
+        for conn, size in self._shapes:
+            b = p[k: k + size]
+            k += size
+            w = p[k: k + conn * size].reshape(conn, size)
+            k += conn * size
+            out.append((b, w))
+        return out, p[k:]
+
+    @property
+    def b(self):
+        return [b.copy() for b, _ in self._split()[0]]
+
+    @property
+    def W(self):
+        return [w.copy() for _, w in self._split()[0]]
+
+    @property
+    def connections(self):
+        return [c.copy() for c in self._connections]
+
+    @property
+    def final_weights(self):
+        return self._split()[1].copy()
+
+    @property
+    def first_layer_params_slice(self):
+        conn, size = self._shapes[0]
+        return slice(2 * self.N, 2 * self.N + conn * size + size)
+
+
+class PsiPair(PsiDeep):
+    """Two real PsiDeep nets for Re / Im log psi (include/quantum_state/PsiPair.hpp:166-205)."""
+
+    _pair = 1
+
+
+# --------------------------------------------------------------------- operator
+class Operator:
+    """Pauli-string sum as the reference's padded table (include/operator/Operator.hpp:394-409).
+
+    Operator(coefficients[S], pauli_types[S, L], pauli_indices[S, L], gpu); types 0=I 1=X 2=Y 3=Z,
+    index -1 ends a string.  An object with a ``to_table()`` method returning the same three
+    arrays is accepted in place of the tables (the reference's PauliExpression overload).
+    """
+
+    def __init__(self, coefficients, pauli_types=None, pauli_indices=None, gpu=True):
+        if pauli_types is None or isinstance(pauli_types, bool):
+            coefficients, pauli_types, pauli_indices = coefficients.to_table()
+        coef = _c128(coefficients).reshape(-1)
+        types = np.ascontiguousarray(np.asarray(pauli_types), dtype=np.int32)
+        idx = np.ascontiguousarray(np.asarray(pauli_indices), dtype=np.int32)
+        if types.ndim != 2 or types.shape != idx.shape or types.shape[0] != coef.size:
+            raise ValueError("pauli_types / pauli_indices must be [num_strings, max_string_length]")
+        h = _handle()
+        call("rbmg_operator_create", types.shape[0], types.shape[1], _p(coef.view(np.float64)), _p(types, _ip),
+             _p(idx, _ip), C.byref(h))
+        self._h = h
+
+    def __del__(self):
+        h, self._h = getattr(self, "_h", None), None
+        if h is not None:
+            try:
+                lib().rbmg_operator_destroy(h)
+            except Exception:
+                pass
+
+    def _shape(self):
+        s, l = C.c_int(), C.c_int()
+        call("rbmg_operator_shape", self._h, C.byref(s), C.byref(l))
+        return s.value, l.value
+
+    @property
+    def num_strings(self):
+        return self._shape()[0]
+
+    @property
+    def max_string_length(self):
+        return self._shape()[1]
+
+    def _tables(self):
+        S, L = self._shape()
+        c = np.zeros(S, np.complex128)
+        t = np.zeros((S, L), np.int32)
+        i = np.zeros((S, L), np.int32)
+        call("rbmg_operator_tables", self._h, _p(c.view(np.float64)), _p(t, _ip), _p(i, _ip))
+        return c, t, i
+
+    @property
+    def coefficients(self):
+        return self._tables()[0]
+
+    @property
+    def pauli_types(self):
+        return self._tables()[1]
+
+    @property
+    def pauli_indices(self):
+        return self._tables()[2]
+
+    @property
+    def gpu(self):
+        return True
+
+
+# --------------------------------------------------------------------- ensembles
+class _Ensemble:
+    _h = None
+
+    def __del__(self):
+        h, self._h = self._h, None
+        if h is not None:
+            try:
+                lib().rbmg_ensemble_destroy(h)
+            except Exception:
+                pass
+
+    @property
+    def num_steps(self):
+        n = C.c_uint64()
+        call("rbmg_ensemble_num_steps", self._h, C.byref(n))
+        return n.value
+
+    def samples(self, psi, operator=None):
+        """(spins words [num_steps, nwords], log psi [num_steps], E_loc or None) of one foreach pass."""
+        n = self.num_steps
+        nw = nwords(psi.N)
+        sp = np.zeros((n, nw), np.uint64)
+        lp = np.zeros(2 * n)
+        el = np.zeros(2 * n) if operator is not None else None
+        call("rbmg_ensemble_samples", self._h, psi._h, operator._h if operator is not None else None,
+             _p(sp, _u64p), _p(lp), _p(el) if el is not None else None)
+        return sp, lp.view(np.complex128), (el.view(np.complex128) if el is not None else None)
+
+
+class MonteCarloLoop(_Ensemble):
+    """MonteCarloLoop(num_samples, num_sweeps, num_thermalization_sweeps, num_markov_chains, gpu)
+    (source/spin_ensembles/MonteCarloLoop.cu:20-42); ``seed`` keys the chains' Philox streams."""
+
+    def __init__(self, num_samples, num_sweeps=1, num_thermalization_sweeps=0, num_markov_chains=1, gpu=True,
+                 seed=0):
+        h = _handle()
+        if isinstance(num_samples, MonteCarloLoop):   # MonteCarloLoop(MonteCarloLoop&)
+            call("rbmg_mc_copy", num_samples._h, C.byref(h))
+        else:
+            call("rbmg_mc_create", int(num_samples), int(num_sweeps), int(num_thermalization_sweeps),
+                 int(num_markov_chains), int(seed), C.byref(h))
+        self._h = h
+
+    def set_total_z_symmetry(self, sector):
+        call("rbmg_mc_set_total_z_symmetry", self._h, int(sector))
+
+    def set_fast_sweep(self, num_tries):
+        call("rbmg_mc_set_fast_sweep", self._h, int(num_tries))
+
+    def acceptance(self):
+        a, p = C.c_uint64(), C.c_uint64()
+        call("rbmg_mc_acceptance", self._h, C.byref(a), C.byref(p), None)
+        return a.value, p.value
+
+    @property
+    def acceptance_rate(self):
+        a, p = self.acceptance()
+        return float(a) / float(p) if p else float("nan")
+
+
+class ExactSummation(_Ensemble):
+    """ExactSummation(N, gpu) (source/spin_ensembles/ExactSummation.cu:16-45)."""
+
+    def __init__(self, num_spins, gpu=True):
+        h = _handle()
+        call("rbmg_exact_create", int(num_spins), C.byref(h))
+        self._h = h
+
+    def set_total_z_symmetry(self, sector):
+        call("rbmg_exact_set_total_z_symmetry", self._h, int(sector))
+
+
+# --------------------------------------------------------------------- reductions
+class ExpectationValue:
+    """source/network_functions/ExpectationValue.cu (pyRBMonGPU/main.cpp:295-339)."""
+
+    def __init__(self, gpu=True):
+        self.gpu = gpu
+
+    def __call__(self, psi, operator_, spin_ensemble):
+        if isinstance(operator_, (list, tuple)):
+            ops = (C.c_void_p * len(operator_))(*[o._h for o in operator_])
+            out = np.zeros(2 * len(operator_))
+            call("rbmg_ev_values", psi._h, ops, len(operator_), spin_ensemble._h, _p(out))
+            return list(out.view(np.complex128))
+        out = np.zeros(2)
+        call("rbmg_ev_value", psi._h, operator_._h, spin_ensemble._h, _p(out))
+        return complex(out[0], out[1])
+
+    def fluctuation(self, psi, operator_, spin_ensemble):
+        sig = C.c_double()
+        out = np.zeros(2)
+        call("rbmg_ev_fluctuation", psi._h, operator_._h, spin_ensemble._h, C.byref(sig), _p(out))
+        return sig.value, complex(out[0], out[1])
+
+    def gradient(self, psi, operator_, spin_ensemble):
+        g = np.zeros(psi.num_params, np.complex128)
+        out = np.zeros(2)
+        call("rbmg_ev_gradient", psi._h, operator_._h, spin_ensemble._h, _p(g.view(np.float64)), _p(out))
+        return g, complex(out[0], out[1])
+
+
+class HilbertSpaceDistance:
+    """source/network_functions/HilbertSpaceDistance.cu (pyRBMonGPU/main.cpp:342-418)."""
+
+    def __init__(self, N, num_params, gpu=True):
+        self.N = N
+        self.num_params = num_params
+
+    def __call__(self, psi, psi_prime, operator_, is_unitary, spin_ensemble):
+        d = C.c_double()
+        call("rbmg_hsd_distance", psi._h, psi_prime._h, operator_._h, int(bool(is_unitary)), spin_ensemble._h,
+             C.byref(d))
+        return d.value
+
+    def gradient(self, psi, psi_prime, operator_, is_unitary, spin_ensemble, nu=1.0):
+        g = np.zeros(psi_prime.num_params, np.complex128)
+        d = C.c_double()
+        call("rbmg_hsd_gradient", psi._h, psi_prime._h, operator_._h, int(bool(is_unitary)), spin_ensemble._h,
+             C.c_float(nu), _p(g.view(np.float64)), C.byref(d))
+        return g, d.value
+
+
+def psi_O_k_vector(psi, spins):
+    """source/network_functions/PsiOkVector.cu:9-44 (entries [0, 2N) are zero)."""
+    w = spins_to_words(spins, psi.N)
+    out = np.zeros(psi.num_params, np.complex128)
+    call("rbmg_psi_O_k_vector", psi._h, _p(w, _u64p), _p(out.view(np.float64)))
+    return out
+
+
+# --------------------------------------------------------------------- persistent chains
+class Chain:
+    """Walkers whose configurations and Philox positions stay on the device between
+    calls (extension: the reference's foreach restarts its chains every call)."""
+
+    def __init__(self, psi, num_walkers, seed=0):
+        h = _handle()
+        call("rbmg_chain_create", psi._h, int(num_walkers), int(seed), C.byref(h))
+        self._h = h
+        self.num_walkers = int(num_walkers)
+        self.N = psi.N
+        self._host = None
+
+    def __del__(self):
+        h, self._h = getattr(self, "_h", None), None
+        if h is not None:
+            try:
+                lib().rbmg_chain_destroy(h)
+            except Exception:
+                pass
+
+    def sweep_async(self, psi, operator_=None, n_sweeps=1, measure_every=1, d_eloc=0, stream=None):
+        """Device-level call: d_eloc is a device address of double2 [n_sweeps // measure_every][walkers]."""
+        call("rbmg_chain_sweep_async", self._h, psi._h, operator_._h if operator_ is not None else None,
+             int(n_sweeps), int(measure_every), C.c_void_p(d_eloc) if d_eloc else None,
+             C.c_void_p(stream) if stream else None)
+
+    def state(self):
+        sp = np.zeros((self.num_walkers, nwords(self.N)), np.uint64)
+        a, p = C.c_uint64(), C.c_uint64()
+        call("rbmg_chain_state", self._h, _p(sp, _u64p), C.byref(a), C.byref(p))
+        return sp, a.value, p.value
+
+
+def library_stream():
+    """The library's CUDA stream of the calling thread (a cudaStream_t as int)."""
+    st = C.c_void_p()
+    call("rbmg_stream", C.byref(st))
+    return st.value or 0
+
+
+# --------------------------------------------------------------------- factories
+def real_noise(shape, rng=np.random):
+    return 2 * rng.random_sample(shape) - 1
+
+
+def complex_noise(shape, rng=np.random):
+    return real_noise(shape, rng) + 1j * real_noise(shape, rng)
+
+
+def new_neural_network(N, M, initial_value=(0.01 + 1j * math.pi / 4), alpha=0, beta=0, free_quantum_axis=False,
+                       noise=1e-6, gpu=True):
+    """pyRBMonGPU/new_neural_network.py:29-50"""
+    if isinstance(alpha, (int, float)):
+        alpha = alpha * np.ones(N)
+    if isinstance(beta, (int, float)):
+        beta = beta * np.ones(N)
+    b = noise * complex_noise(M)
+    W = noise * complex_noise((N, M))
+    for r in range(M // N):
+        W[:, r * N:(r + 1) * N] += initial_value * np.diag(np.ones(N))
+    return Psi(alpha, beta, b, W, 1, free_quantum_axis, gpu)
+
+
+def new_deep_neural_network(N, M, C_, initial_value=(0.01 + 1j * math.pi / 4), alpha=0, beta=0,
+                            free_quantum_axis=False, noise=1e-4, gpu=True, pair=False, noise_modulation="auto",
+                            final_weights=10):
+    """pyRBMonGPU/new_neural_network.py:53-153 (1D networks)."""
+    for n, m, c in zip([N] + M[:-1], M, C_):
+        assert (m * c) % n == 0
+        assert c <= n
+    if isinstance(alpha, (float, int)):
+        alpha = alpha * np.ones(N)
+    if isinstance(beta, (float, int)):
+        beta = beta * np.ones(N)
+    b = [noise * complex_noise(m) for m in M]
+    w = noise * complex_noise((C_[0], M[0]))
+    w[C_[0] // 2, :] += initial_value
+    W = [w]
+    if noise_modulation == "auto":
+        noise_modulation = [math.sqrt(6 / (c + next_c)) for c, next_c in zip(C_[1:], C_[2:] + [1])]
+    for c, m, next_c, nm in zip(C_[1:], M[1:], C_[2:] + [1], noise_modulation):
+        W.append(nm * math.sqrt(6 / (c + next_c)) * real_noise((c, m)) + noise * complex_noise((c, m)))
+
+    def delta_func(n, m, c):
+        if m > n:
+            return 1
+        if n % m == 0:
+            return n // m
+        return c
+
+    connections = []
+    for n, m, c in zip([N] + M[:-1], M, C_):
+        d = delta_func(n, m, c)
+        connections.append(np.array([[(j * d + i) % n for j in range(m)] for i in range(c)]))
+    if isinstance(final_weights, (float, int)):
+        final_weights = final_weights * np.ones(M[-1])
+    cls = PsiPair if pair else PsiDeep
+    return cls(alpha, beta, b, connections, W, final_weights, 1.0, free_quantum_axis, gpu)
+
+
+__all__ = ["Chain", "library_stream", "Psi", "PsiDeep", "PsiPair", "Operator", "Spins", "MonteCarloLoop", "ExactSummation",
+           "ExpectationValue", "HilbertSpaceDistance", "psi_O_k_vector", "activation_function", "setDevice",
+           "start_profiling", "stop_profiling", "new_neural_network", "new_deep_neural_network", "RbmgError"]

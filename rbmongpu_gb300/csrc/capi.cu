@@ -1,0 +1,1370 @@
+// C ABI of the library (include/rbmg.h): handles, the ensembles' sample streams
+// and the estimators of ExpectationValue / HilbertSpaceDistance, orchestrating the
+// CUDA kernels of rbm_impl.cuh, deep.cu and reduce_kernels.cu.
+#include <algorithm>
+#include <cmath>
+#include <functional>
+#include <memory>
+
+#include <cuda_profiler_api.h>
+
+#include "host.h"
+#include "rbm64.h"
+#include "reduce.h"
+
+namespace rbmg {
+
+// ---------------------------------------------------------------- errors
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* where) {
+    g_last_error = std::string(where) + ": " + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? RBMG_ENOMEM : RBMG_ECUDA;
+}
+
+cudaStream_t stream() {
+    static thread_local cudaStream_t st = nullptr;
+    static thread_local int st_dev = -1;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (!st || st_dev != dev) {
+        cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+        st_dev = dev;
+    }
+    return st;
+}
+
+// deep.cu
+int deep_upload(rbmg_psi* psi);
+int deep_log_psi(const rbmg_psi* psi, int count, const uint64_t* d_spins, uint64_t enum_base, int enumerate,
+                 double2* d_out, cudaStream_t st);
+
+// ---------------------------------------------------------------- workspace
+// Grow-only scratch buffers shared by all calls on this thread's device.
+struct Workspace {
+    DevBuf sample_spins, eloc, logpsi, logpsi_p, T, U, X, Tp, weights, coef1, coef2, coef3, omega, pr, nn;
+    DevBuf partial, block_scratch, sums, acc_O, acc_EO, acc_Ek, acc_wO, acc_pO, block_max, zsum;
+};
+
+static Workspace& ws() {
+    static thread_local Workspace w;
+    return w;
+}
+
+static int nwords_of(int N) { return (N + 63) / 64; }
+
+}  // namespace rbmg
+
+using namespace rbmg;
+
+int rbmg_psi::num_params() const {
+    if (kind == 0) return 2 * N + M + N * M;
+    int P = 2 * N;
+    for (const auto& l : layers) P += l.size + l.conn * l.size;
+    return P + (layers.empty() ? 0 : layers.back().size);
+}
+
+uint64_t rbmg_ensemble::num_steps() const {
+    if (kind == 0) return num_samples;
+    if (exact_total_z) return allowed.size();
+    return 1ull << num_spins;
+}
+
+// ====================================================================== misc
+extern "C" const char* rbmg_last_error(void) { return g_last_error.c_str(); }
+extern "C" const char* rbmg_version(void) { return "rbmg 0.1 (sm_103a)"; }
+
+extern "C" int rbmg_set_device(int device) {
+    RBMG_CK(cudaSetDevice(device));
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_profiler_start(void) {
+    RBMG_CK(cudaProfilerStart());
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_profiler_stop(void) {
+    RBMG_CK(cudaProfilerStop());
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_activation(double re, double im, double* out) {
+    if (!out) return fail(RBMG_EINVAL, "activation: null output");
+    // include/quantum_state/psi_functions.hpp:49-57 in FP64
+    const cplx z(re, im);
+    const double sign = re > 0.0 ? 1.0 : -1.0;
+    const cplx den = 9.19376335670885 + z * (sign * 10.2180213465 + z * (7.771429504240965 + z * (sign * 3.746646023906276 + z)));
+    const cplx r = sign * 0.9003320053750442 * z + (5.49914721954 - sign * 2.16564366435 * z) / den - 0.598139;
+    out[0] = r.real();
+    out[1] = r.imag();
+    return RBMG_OK;
+}
+
+// ====================================================================== Psi
+static int rbm_upload(rbmg_psi* p) {
+    for (const auto& v : p->b)
+        if (!std::isfinite(v.real()) || !std::isfinite(v.imag())) return fail(RBMG_ENAN, "Psi: non-finite b");
+    for (const auto& v : p->W)
+        if (!std::isfinite(v.real()) || !std::isfinite(v.imag())) return fail(RBMG_ENAN, "Psi: non-finite W");
+    std::vector<float2> hb(p->Mpad, make_float2(0.f, 0.f)), hW(static_cast<size_t>(p->N) * p->Mpad,
+                                                               make_float2(0.f, 0.f));
+    for (int j = 0; j < p->M; j++) hb[j] = make_float2(float(p->b[j].real()), float(p->b[j].imag()));
+    for (int i = 0; i < p->N; i++)
+        for (int j = 0; j < p->M; j++) {
+            const cplx w = p->W[static_cast<size_t>(i) * p->M + j];
+            hW[static_cast<size_t>(i) * p->Mpad + j] = make_float2(float(w.real()), float(w.imag()));
+        }
+    RBMG_CK(p->db.ensure(hb.size() * sizeof(float2)));
+    RBMG_CK(p->dW.ensure(hW.size() * sizeof(float2)));
+    RBMG_CK(cudaMemcpyAsync(p->db.p, hb.data(), hb.size() * sizeof(float2), cudaMemcpyHostToDevice, stream()));
+    RBMG_CK(cudaMemcpyAsync(p->dW.p, hW.data(), hW.size() * sizeof(float2), cudaMemcpyHostToDevice, stream()));
+    RBMG_CK(cudaStreamSynchronize(stream()));
+    p->f64_valid = false;
+    return RBMG_OK;
+}
+
+// FP64 parameter copies for the Hilbert-space distance pass, uploaded on first use
+static int rbm_upload64(const rbmg_psi* p) {
+    if (p->f64_valid) return RBMG_OK;
+    RBMG_CK(p->db64.ensure(sizeof(cplx) * p->M));
+    RBMG_CK(p->dW64.ensure(sizeof(cplx) * p->W.size()));
+    RBMG_CK(cudaMemcpyAsync(p->db64.p, p->b.data(), sizeof(cplx) * p->M, cudaMemcpyHostToDevice, stream()));
+    RBMG_CK(cudaMemcpyAsync(p->dW64.p, p->W.data(), sizeof(cplx) * p->W.size(), cudaMemcpyHostToDevice, stream()));
+    RBMG_CK(cudaStreamSynchronize(stream()));
+    p->f64_valid = true;
+    return RBMG_OK;
+}
+
+static Rbm64 rbm64(const rbmg_psi* p) { return Rbm64{p->N, p->M, p->dW64.as<double2>(), p->db64.as<double2>()}; }
+
+extern "C" int rbmg_psi_create(int N, int M, const double* alpha, const double* beta, const double* b,
+                               const double* W, double prefactor, int free_quantum_axis, rbmg_psi** out) {
+    (void)beta;
+    if (!out || N <= 0 || M <= 0 || !b || !W) return fail(RBMG_EINVAL, "Psi: bad arguments");
+    if (N > 64 * kMaxWords) return fail(RBMG_EINVAL, "Psi: N exceeds 256 spins");
+    if (free_quantum_axis) return fail(RBMG_EUNSUPPORTED, "Psi: free_quantum_axis is not provided");
+    const int K = rbm_lanes_k(M);
+    if (K < 0) return fail(RBMG_EINVAL, "Psi: M exceeds the largest instantiated hidden layer (576)");
+    auto p = std::make_unique<rbmg_psi>();
+    p->kind = 0;
+    p->N = N;
+    p->M = M;
+    p->Mpad = 32 * K;
+    p->prefactor = prefactor;
+    p->alpha.assign(N, 0.0);
+    if (alpha) p->alpha.assign(alpha, alpha + N);
+    p->beta = p->alpha;   // include/quantum_state/PsiBase.hpp:246: beta_array(alpha)
+    p->b.resize(M);
+    p->W.resize(static_cast<size_t>(N) * M);
+    std::memcpy(p->b.data(), b, sizeof(cplx) * M);
+    std::memcpy(p->W.data(), W, sizeof(cplx) * N * M);
+    const int r = rbm_upload(p.get());
+    if (r != RBMG_OK) return r;
+    *out = p.release();
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_psi_deep_create(int N, int num_layers, const int* sizes, const int* conns,
+                                    const uint32_t* const* connections, const double* const* biases,
+                                    const double* const* weights, const double* final_weights, const double* alpha,
+                                    const double* beta, double prefactor, int free_quantum_axis, int pair,
+                                    rbmg_psi** out) {
+    (void)beta;
+    if (!out || N <= 0 || num_layers <= 0 || num_layers > 3 || !sizes || !conns || !connections || !biases ||
+        !weights || !final_weights)
+        return fail(RBMG_EINVAL, "PsiDeep: bad arguments");
+    if (N > 64 * kMaxWords) return fail(RBMG_EINVAL, "PsiDeep: N exceeds 256 spins");
+    if (free_quantum_axis) return fail(RBMG_EUNSUPPORTED, "PsiDeep: free_quantum_axis is not provided");
+    auto p = std::make_unique<rbmg_psi>();
+    p->kind = pair ? 2 : 1;
+    p->N = N;
+    p->prefactor = prefactor;
+    p->alpha.assign(N, 0.0);
+    if (alpha) p->alpha.assign(alpha, alpha + N);
+    p->beta = p->alpha;
+    int prev = N;
+    p->width = N;
+    for (int l = 0; l < num_layers; l++) {
+        DeepLayerHost L;
+        L.size = sizes[l];
+        L.conn = conns[l];
+        if (L.size <= 0 || L.conn <= 0) return fail(RBMG_EINVAL, "PsiDeep: empty layer");
+        L.connections.assign(connections[l], connections[l] + static_cast<size_t>(L.conn) * L.size);
+        for (uint32_t c : L.connections)
+            if (static_cast<int>(c) >= prev) return fail(RBMG_EINVAL, "PsiDeep: connection index out of range");
+        L.biases.resize(L.size);
+        std::memcpy(L.biases.data(), biases[l], sizeof(cplx) * L.size);
+        L.weights.resize(static_cast<size_t>(L.conn) * L.size);
+        std::memcpy(L.weights.data(), weights[l], sizeof(cplx) * L.conn * L.size);
+        p->width = std::max(p->width, L.size);
+        prev = L.size;
+        p->layers.push_back(std::move(L));
+    }
+    p->final_weights.resize(prev);
+    std::memcpy(p->final_weights.data(), final_weights, sizeof(cplx) * prev);
+    const int r = deep_upload(p.get());
+    if (r != RBMG_OK) return r;
+    *out = p.release();
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_psi_copy(const rbmg_psi* psi, rbmg_psi** out) {
+    if (!psi || !out) return fail(RBMG_EINVAL, "copy: null handle");
+    auto p = std::make_unique<rbmg_psi>();
+    p->kind = psi->kind;
+    p->N = psi->N;
+    p->prefactor = psi->prefactor;
+    p->alpha = psi->alpha;
+    p->beta = psi->beta;
+    p->M = psi->M;
+    p->Mpad = psi->Mpad;
+    p->b = psi->b;
+    p->W = psi->W;
+    p->layers = psi->layers;
+    p->final_weights = psi->final_weights;
+    p->translational_invariance = psi->translational_invariance;
+    p->width = psi->width;
+    const int r = p->kind == 0 ? rbm_upload(p.get()) : deep_upload(p.get());
+    if (r != RBMG_OK) return r;
+    *out = p.release();
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_psi_destroy(rbmg_psi* psi) {
+    delete psi;
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_psi_kind(const rbmg_psi* psi, int* kind) {
+    if (!psi || !kind) return fail(RBMG_EINVAL, "kind: null");
+    *kind = psi->kind;
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_psi_shape(const rbmg_psi* psi, int* N, int* M, int* num_params) {
+    if (!psi) return fail(RBMG_EINVAL, "shape: null handle");
+    if (N) *N = psi->N;
+    if (M) *M = psi->kind == 0 ? psi->M : psi->width;
+    if (num_params) *num_params = psi->num_params();
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_psi_get_params(const rbmg_psi* psi, double* params) {
+    if (!psi || !params) return fail(RBMG_EINVAL, "get_params: null");
+    cplx* out = reinterpret_cast<cplx*>(params);
+    const int N = psi->N;
+    for (int i = 0; i < N; i++) {
+        out[i] = cplx(psi->alpha[i], 0.0);
+        out[N + i] = cplx(psi->beta[i], 0.0);
+    }
+    size_t k = 2 * N;
+    if (psi->kind == 0) {      // source/quantum_state/Psi.cu:71-78
+        for (const auto& v : psi->b) out[k++] = v;
+        for (const auto& v : psi->W) out[k++] = v;
+    } else {                   // source/quantum_state/PsiDeep.cu:120-140
+        for (const auto& L : psi->layers) {
+            for (const auto& v : L.biases) out[k++] = v;
+            for (const auto& v : L.weights) out[k++] = v;
+        }
+        for (const auto& v : psi->final_weights) out[k++] = v;
+    }
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_psi_set_params(rbmg_psi* psi, const double* params) {
+    if (!psi || !params) return fail(RBMG_EINVAL, "set_params: null");
+    const cplx* in = reinterpret_cast<const cplx*>(params);
+    const int N = psi->N;
+    const int P = psi->num_params();
+    for (int k = 0; k < P; k++)
+        if (!std::isfinite(in[k].real()) || !std::isfinite(in[k].imag())) return fail(RBMG_ENAN, "set_params: non-finite");
+    for (int i = 0; i < N; i++) {
+        psi->alpha[i] = in[i].real();
+        psi->beta[i] = in[N + i].real();
+    }
+    size_t k = 2 * N;
+    if (psi->kind == 0) {      // source/quantum_state/Psi.cu:80-92
+        for (auto& v : psi->b) v = in[k++];
+        for (auto& v : psi->W) v = in[k++];
+        return rbm_upload(psi);
+    }
+    for (auto& L : psi->layers) {   // source/quantum_state/PsiDeep.cu:143-177 (PsiPair.cu:55-76 splits re/im)
+        for (auto& v : L.biases) v = in[k++];
+        for (auto& v : L.weights) v = in[k++];
+    }
+    for (auto& v : psi->final_weights) v = in[k++];
+    return deep_upload(psi);
+}
+
+extern "C" int rbmg_psi_get_prefactor(const rbmg_psi* psi, double* prefactor) {
+    if (!psi || !prefactor) return fail(RBMG_EINVAL, "prefactor: null");
+    *prefactor = psi->prefactor;
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_psi_set_prefactor(rbmg_psi* psi, double prefactor) {
+    if (!psi) return fail(RBMG_EINVAL, "prefactor: null");
+    psi->prefactor = prefactor;
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_psi_set_translational_invariance(rbmg_psi* psi, int on) {
+    if (!psi) return fail(RBMG_EINVAL, "translational_invariance: null");
+    if (psi->kind == 0) return fail(RBMG_EINVAL, "translational_invariance: PsiDeep only");
+    if (on && psi->N > 64) return fail(RBMG_EUNSUPPORTED, "translational_invariance: N <= 64 (Spins.h:280-285)");
+    psi->translational_invariance = on ? 1 : 0;
+    return RBMG_OK;
+}
+
+// ====================================================================== Operator
+// Compact form of the padded table (include/operator/Operator.hpp:45-88): X flips,
+// Y flips and multiplies by -i s_i, Z multiplies by s_i, with the ORIGINAL spins.
+static int op_compile(rbmg_operator* op) {
+    op->ypow.assign(op->S, 0);
+    op->nflip.assign(op->S, 0);
+    op->flip_off.assign(op->S, 0);
+    op->offdiag_slot.assign(op->S, -1);
+    op->zmask.assign(static_cast<size_t>(op->S) * kMaxWords, 0);
+    op->flip_sites.clear();
+    op->num_offdiag = 0;
+    op->max_site = -1;
+    for (int n = 0; n < op->S; n++) {
+        uint64_t flips[kMaxWords] = {0, 0, 0, 0};
+        int yp = 0;
+        for (int c = 0; c < op->L; c++) {
+            const int i = op->idx[static_cast<size_t>(n) * op->L + c];
+            if (i < 0) break;
+            if (i >= 64 * kMaxWords) return fail(RBMG_EINVAL, "Operator: site index exceeds 256");
+            const int t = op->types[static_cast<size_t>(n) * op->L + c];
+            if (t < 0 || t > 3) return fail(RBMG_EINVAL, "Operator: pauli type must be 0..3");
+            op->max_site = std::max(op->max_site, i);
+            const uint64_t bit = 1ull << (i & 63);
+            if (t == 1 || t == 2) flips[i >> 6] ^= bit;
+            if (t == 2 || t == 3) op->zmask[static_cast<size_t>(n) * kMaxWords + (i >> 6)] ^= bit;
+            if (t == 2) yp++;
+        }
+        op->ypow[n] = yp & 3;
+        op->flip_off[n] = static_cast<int>(op->flip_sites.size());
+        for (int w = 0; w < kMaxWords; w++)
+            for (int bpos = 0; bpos < 64; bpos++)
+                if ((flips[w] >> bpos) & 1ull) op->flip_sites.push_back(64 * w + bpos);
+        op->nflip[n] = static_cast<int>(op->flip_sites.size()) - op->flip_off[n];
+        if (op->nflip[n] > 0) op->offdiag_slot[n] = op->num_offdiag++;
+    }
+    if (op->flip_sites.empty()) op->flip_sites.push_back(0);
+    auto up = [](DevBuf& d, const void* h, size_t bytes) -> cudaError_t {
+        cudaError_t e = d.ensure(std::max<size_t>(bytes, 16));
+        if (e != cudaSuccess) return e;
+        return cudaMemcpy(d.p, h, bytes, cudaMemcpyHostToDevice);
+    };
+    RBMG_CK(up(op->d_coef, op->coef.data(), sizeof(cplx) * op->S));
+    RBMG_CK(up(op->d_ypow, op->ypow.data(), sizeof(int) * op->S));
+    RBMG_CK(up(op->d_zmask, op->zmask.data(), sizeof(uint64_t) * op->zmask.size()));
+    RBMG_CK(up(op->d_nflip, op->nflip.data(), sizeof(int) * op->S));
+    RBMG_CK(up(op->d_flip_off, op->flip_off.data(), sizeof(int) * op->S));
+    RBMG_CK(up(op->d_flip_sites, op->flip_sites.data(), sizeof(int) * op->flip_sites.size()));
+    RBMG_CK(up(op->d_slot, op->offdiag_slot.data(), sizeof(int) * op->S));
+    return RBMG_OK;
+}
+
+// per-site lists of off-diagonal slots flipping that site, for the E_k term
+static int op_site_lists(rbmg_operator* op, int N) {
+    if (op->site_ptr_N == N) return RBMG_OK;
+    std::vector<std::vector<int>> per(N);
+    for (int n = 0; n < op->S; n++) {
+        if (op->offdiag_slot[n] < 0) continue;
+        for (int q = 0; q < op->nflip[n]; q++) {
+            const int site = op->flip_sites[op->flip_off[n] + q];
+            if (site < N) per[site].push_back(op->offdiag_slot[n]);
+        }
+    }
+    op->site_ptr.assign(N + 1, 0);
+    op->site_slots.clear();
+    for (int i = 0; i < N; i++) {
+        op->site_ptr[i] = static_cast<int>(op->site_slots.size());
+        op->site_slots.insert(op->site_slots.end(), per[i].begin(), per[i].end());
+    }
+    op->site_ptr[N] = static_cast<int>(op->site_slots.size());
+    if (op->site_slots.empty()) op->site_slots.push_back(0);
+    RBMG_CK(op->d_site_ptr.ensure(sizeof(int) * (N + 1)));
+    RBMG_CK(op->d_site_slots.ensure(sizeof(int) * op->site_slots.size()));
+    RBMG_CK(cudaMemcpy(op->d_site_ptr.p, op->site_ptr.data(), sizeof(int) * (N + 1), cudaMemcpyHostToDevice));
+    RBMG_CK(cudaMemcpy(op->d_site_slots.p, op->site_slots.data(), sizeof(int) * op->site_slots.size(),
+                       cudaMemcpyHostToDevice));
+    op->site_ptr_N = N;
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_operator_create(int num_strings, int max_string_length, const double* coefficients,
+                                    const int* pauli_types, const int* pauli_indices, rbmg_operator** out) {
+    if (!out || num_strings <= 0 || max_string_length <= 0 || !coefficients || !pauli_types || !pauli_indices)
+        return fail(RBMG_EINVAL, "Operator: bad arguments");
+    auto op = std::make_unique<rbmg_operator>();
+    op->S = num_strings;
+    op->L = max_string_length;
+    op->coef.resize(num_strings);
+    std::memcpy(op->coef.data(), coefficients, sizeof(cplx) * num_strings);
+    for (const auto& c : op->coef)
+        if (!std::isfinite(c.real()) || !std::isfinite(c.imag())) return fail(RBMG_ENAN, "Operator: non-finite coefficient");
+    const size_t cells = static_cast<size_t>(num_strings) * max_string_length;
+    op->types.assign(pauli_types, pauli_types + cells);
+    op->idx.assign(pauli_indices, pauli_indices + cells);
+    const int r = op_compile(op.get());
+    if (r != RBMG_OK) return r;
+    *out = op.release();
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_operator_destroy(rbmg_operator* op) {
+    delete op;
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_operator_shape(const rbmg_operator* op, int* num_strings, int* max_string_length) {
+    if (!op) return fail(RBMG_EINVAL, "operator: null");
+    if (num_strings) *num_strings = op->S;
+    if (max_string_length) *max_string_length = op->L;
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_operator_tables(const rbmg_operator* op, double* coefficients, int* pauli_types,
+                                    int* pauli_indices) {
+    if (!op) return fail(RBMG_EINVAL, "operator: null");
+    if (coefficients) std::memcpy(coefficients, op->coef.data(), sizeof(cplx) * op->S);
+    if (pauli_types) std::memcpy(pauli_types, op->types.data(), sizeof(int) * op->types.size());
+    if (pauli_indices) std::memcpy(pauli_indices, op->idx.data(), sizeof(int) * op->idx.size());
+    return RBMG_OK;
+}
+
+// ====================================================================== ensembles
+extern "C" int rbmg_mc_create(uint32_t num_samples, uint32_t num_sweeps, uint32_t num_therm, uint32_t num_chains,
+                              uint64_t seed, rbmg_ensemble** out) {
+    if (!out || num_chains == 0 || num_samples == 0 || num_sweeps == 0)
+        return fail(RBMG_EINVAL, "MonteCarloLoop: zero samples, sweeps or chains");
+    if (num_samples % num_chains != 0)   // source/spin_ensembles/MonteCarloLoop.cu:78
+        return fail(RBMG_EINVAL, "MonteCarloLoop: num_samples must be a multiple of num_markov_chains");
+    auto e = std::make_unique<rbmg_ensemble>();
+    e->kind = 0;
+    e->num_samples = num_samples;
+    e->num_sweeps = num_sweeps;
+    e->num_therm = num_therm;
+    e->num_chains = num_chains;
+    e->seed = seed;
+    RBMG_CK(e->rng_index.ensure(sizeof(uint64_t) * num_chains));
+    RBMG_CK(cudaMemset(e->rng_index.p, 0, sizeof(uint64_t) * num_chains));
+    RBMG_CK(e->accepts.ensure(sizeof(unsigned long long) * num_chains));
+    RBMG_CK(e->proposals.ensure(sizeof(unsigned long long) * num_chains));
+    e->last_accepts.assign(num_chains, 0);
+    e->last_proposals.assign(num_chains, 0);
+    *out = e.release();
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_mc_copy(const rbmg_ensemble* o, rbmg_ensemble** out) {
+    if (!o || o->kind != 0) return fail(RBMG_EINVAL, "MonteCarloLoop copy: not a MonteCarloLoop");
+    int r = rbmg_mc_create(o->num_samples, o->num_sweeps, o->num_therm, o->num_chains, o->seed, out);
+    if (r != RBMG_OK) return r;
+    (*out)->total_z = o->total_z;
+    (*out)->sector = o->sector;
+    (*out)->fast_sweep_tries = o->fast_sweep_tries;
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_mc_set_total_z_symmetry(rbmg_ensemble* mc, int sector) {
+    if (!mc || mc->kind != 0) return fail(RBMG_EINVAL, "set_total_z_symmetry: not a MonteCarloLoop");
+    mc->total_z = 1;
+    mc->sector = sector;
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_mc_set_fast_sweep(rbmg_ensemble* mc, uint32_t num_tries) {
+    if (!mc || mc->kind != 0) return fail(RBMG_EINVAL, "set_fast_sweep: not a MonteCarloLoop");
+    mc->fast_sweep_tries = num_tries;
+    return fail(RBMG_EUNSUPPORTED, "set_fast_sweep: multi-spin masks are not provided by this build");
+}
+
+extern "C" int rbmg_mc_acceptance(const rbmg_ensemble* mc, uint64_t* accepts, uint64_t* proposals,
+                                  uint64_t* per_chain) {
+    if (!mc || mc->kind != 0) return fail(RBMG_EINVAL, "acceptance: not a MonteCarloLoop");
+    uint64_t a = 0, p = 0;
+    for (size_t c = 0; c < mc->last_accepts.size(); c++) {
+        a += mc->last_accepts[c];
+        p += mc->last_proposals[c];
+        if (per_chain) per_chain[c] = mc->last_accepts[c];
+    }
+    if (accepts) *accepts = a;
+    if (proposals) *proposals = p;
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_exact_create(uint32_t num_spins, rbmg_ensemble** out) {
+    if (!out || num_spins == 0 || num_spins > 30) return fail(RBMG_EINVAL, "ExactSummation: 1 <= N <= 30");
+    auto e = std::make_unique<rbmg_ensemble>();
+    e->kind = 1;
+    e->num_spins = num_spins;
+    *out = e.release();
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_exact_set_total_z_symmetry(rbmg_ensemble* ex, int sector) {
+    if (!ex || ex->kind != 1) return fail(RBMG_EINVAL, "set_total_z_symmetry: not an ExactSummation");
+    // source/spin_ensembles/ExactSummation.cu:26-45
+    ex->allowed.clear();
+    const uint64_t dim = 1ull << ex->num_spins;
+    for (uint64_t x = 0; x < dim; x++) {
+        const int tz = 2 * __builtin_popcountll(x) - static_cast<int>(ex->num_spins);
+        if (tz == sector) ex->allowed.push_back(x);
+    }
+    ex->exact_total_z = 1;
+    RBMG_CK(ex->d_allowed.ensure(sizeof(uint64_t) * std::max<size_t>(1, ex->allowed.size())));
+    if (!ex->allowed.empty())
+        RBMG_CK(cudaMemcpy(ex->d_allowed.p, ex->allowed.data(), sizeof(uint64_t) * ex->allowed.size(),
+                           cudaMemcpyHostToDevice));
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_ensemble_num_steps(const rbmg_ensemble* ens, uint64_t* n) {
+    if (!ens || !n) return fail(RBMG_EINVAL, "num_steps: null");
+    *n = ens->num_steps();
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_ensemble_destroy(rbmg_ensemble* ens) {
+    delete ens;
+    return RBMG_OK;
+}
+
+// ====================================================================== sample streams
+namespace rbmg {
+
+// One chunk of samples: spins on the device (or basis indices when enumerate),
+// per-sample weights (null = equal weights) and, for MC, the sampler's log psi / E_loc.
+struct Chunk {
+    int count = 0;
+    const uint64_t* spins = nullptr;
+    int enumerate = 0;
+    uint64_t enum_base = 0;
+    const double* weights = nullptr;
+    const double2* eloc = nullptr;      // filled by the sampler when requested
+};
+
+struct StreamResult {
+    double norm_factor = 1.0;   // reference weight scale: sum_s prefactor^2 |psi|^2 (exact) or 1/num_samples (MC)
+    double log_norm = 0.0;      // log of sum_s prefactor^2 |psi|^2 (exact)
+};
+
+static int psi_log_psi_dev(const rbmg_psi* psi, int count, const uint64_t* d_spins, uint64_t enum_base,
+                           int enumerate, double2* d_out) {
+    if (psi->kind == 0) {
+        EstLaunch L{};
+        L.count = count;
+        L.enum_base = enum_base;
+        L.spins = d_spins;
+        L.flags = EST_LOGPSI | (enumerate ? EST_ENUMERATE : 0);
+        L.logpsi = d_out;
+        RBMG_CK(launch_rbm_estimate(psi->rbm_dev(), nullptr, nullptr, L, stream()));
+        return RBMG_OK;
+    }
+    return deep_log_psi(psi, count, d_spins, enum_base, enumerate, d_out, stream());
+}
+
+constexpr int kExactChunk = 1 << 16;
+
+// MonteCarloLoop::foreach (include/spin_ensembles/MonteCarloLoop.hpp:294-339): every call
+// re-draws the start configurations and thermalises; the chains' Philox streams continue.
+static int mc_stream(rbmg_ensemble* e, const rbmg_psi* psi, const rbmg_operator* op, bool want_eloc,
+                     size_t max_chunk_samples, const std::function<int(const Chunk&)>& fn) {
+    if (psi->kind != 0) return fail(RBMG_EUNSUPPORTED, "MonteCarloLoop: PsiDeep / PsiPair chains are sampled by deep.cu");
+    if (e->fast_sweep_tries) return fail(RBMG_EUNSUPPORTED, "fast sweep is not provided");
+    if (e->total_z && psi->N > 64) return fail(RBMG_EUNSUPPORTED, "total_z symmetry needs N <= 64");
+    const int nw = nwords_of(psi->N);
+    const int B = static_cast<int>(e->num_chains);
+    const int steps = static_cast<int>(e->num_samples / e->num_chains);
+    RBMG_CK(e->spins.ensure(sizeof(uint64_t) * nw * B));
+    e->spins_words = nw;
+    RBMG_CK(cudaMemsetAsync(e->accepts.p, 0, sizeof(unsigned long long) * B, stream()));
+    RBMG_CK(cudaMemsetAsync(e->proposals.p, 0, sizeof(unsigned long long) * B, stream()));
+    Workspace& W = ws();
+    const int rows_per_chunk = static_cast<int>(std::max<size_t>(1, std::min<size_t>(steps, max_chunk_samples / B)));
+    RBMG_CK(W.sample_spins.ensure(sizeof(uint64_t) * nw * B * rows_per_chunk));
+    if (want_eloc) RBMG_CK(W.eloc.ensure(sizeof(double2) * B * rows_per_chunk));
+    OpDev od;
+    if (op) od = op->dev();
+    bool first = true;
+    for (int row0 = 0; row0 < steps; row0 += rows_per_chunk) {
+        const int rows = std::min(rows_per_chunk, steps - row0);
+        McLaunch L{};
+        L.B = B;
+        L.walker_base = 0;
+        L.seed = e->seed;
+        L.spins = e->spins.as<uint64_t>();
+        L.rng_index = e->rng_index.as<uint64_t>();
+        L.init = first ? 1 : 0;
+        L.total_z = e->total_z;
+        L.sector = e->sector;
+        L.n_therm = first ? static_cast<int>(e->num_therm) : 0;
+        L.n_samples = rows;
+        L.sweeps_per_sample = static_cast<int>(e->num_sweeps);
+        L.sample_base = 0;
+        L.sample_spins = W.sample_spins.as<uint64_t>();
+        L.eloc = want_eloc ? W.eloc.as<double2>() : nullptr;
+        L.accepts = e->accepts.as<unsigned long long>();
+        L.proposals = e->proposals.as<unsigned long long>();
+        RBMG_CK(launch_rbm_mc(psi->rbm_dev(), op ? &od : nullptr, L, stream()));
+        first = false;
+        Chunk c;
+        c.count = rows * B;
+        c.spins = W.sample_spins.as<uint64_t>();
+        c.eloc = want_eloc ? W.eloc.as<double2>() : nullptr;
+        const int r = fn(c);
+        if (r != RBMG_OK) return r;
+    }
+    std::vector<unsigned long long> a(B), p(B);
+    RBMG_CK(cudaMemcpyAsync(a.data(), e->accepts.p, sizeof(unsigned long long) * B, cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaMemcpyAsync(p.data(), e->proposals.p, sizeof(unsigned long long) * B, cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaStreamSynchronize(stream()));
+    e->last_accepts.assign(a.begin(), a.end());
+    e->last_proposals.assign(p.begin(), p.end());
+    return RBMG_OK;
+}
+
+// ExactSummation::foreach (include/spin_ensembles/ExactSummation.hpp:36-84): weights
+// prefactor^2 |psi(s)|^2, computed as w_s = exp(2 Re log psi_s - L) (L = FP64
+// log-sum-exp over the basis) times the returned norm factor exp(2 log prefactor + L).
+static int exact_stream(rbmg_ensemble* e, const rbmg_psi* psi, StreamResult* res,
+                        const std::function<int(const Chunk&)>& fn) {
+    if (static_cast<int>(e->num_spins) != psi->N) return fail(RBMG_EINVAL, "ExactSummation: N does not match psi");
+    const uint64_t total = e->num_steps();
+    if (total == 0) return fail(RBMG_EINVAL, "ExactSummation: empty sector");
+    Workspace& W = ws();
+    RBMG_CK(W.logpsi.ensure(sizeof(double2) * total));
+    RBMG_CK(W.weights.ensure(sizeof(double) * total));
+    const int enumerate = e->exact_total_z ? 0 : 1;
+    const uint64_t* sp = e->exact_total_z ? e->d_allowed.as<uint64_t>() : nullptr;
+    for (uint64_t base = 0; base < total; base += kExactChunk) {
+        const int cnt = static_cast<int>(std::min<uint64_t>(kExactChunk, total - base));
+        const int r = psi_log_psi_dev(psi, cnt, sp ? sp + base : nullptr, base, enumerate,
+                                      W.logpsi.as<double2>() + base);
+        if (r != RBMG_OK) return r;
+    }
+    // FP64 log-sum-exp of 2 Re log psi
+    RBMG_CK(W.block_max.ensure(sizeof(double) * kSumBlocks));
+    int blocks = 0;
+    RBMG_CK(launch_max_re2(static_cast<int>(total), W.logpsi.as<double2>(), W.block_max.as<double>(), &blocks, stream()));
+    std::vector<double> bm(blocks);
+    RBMG_CK(cudaMemcpyAsync(bm.data(), W.block_max.p, sizeof(double) * blocks, cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaStreamSynchronize(stream()));
+    const double mx = *std::max_element(bm.begin(), bm.end());
+    if (!std::isfinite(mx)) return fail(RBMG_ENAN, "ExactSummation: non-finite log psi");
+    RBMG_CK(launch_exp_weights(static_cast<int>(total), W.logpsi.as<double2>(), mx, W.weights.as<double>(), stream()));
+    RBMG_CK(W.block_scratch.ensure(sizeof(double2) * kSumBlocks * kMaxSeries));
+    RBMG_CK(W.zsum.ensure(sizeof(double2) * kMaxSeries));
+    RBMG_CK(cudaMemsetAsync(W.zsum.p, 0, sizeof(double2) * kMaxSeries, stream()));
+    // sum of the weights (its own accumulator: the caller's sums are already armed)
+    RBMG_CK(W.coef1.ensure(sizeof(double2) * total));
+    RBMG_CK(launch_coef(static_cast<int>(total), W.weights.as<double>(), nullptr, 1.0, W.coef1.as<double2>(), stream()));
+    SeriesSet set{};
+    set.n = 1;
+    set.v[0] = W.coef1.as<double2>();
+    RBMG_CK(launch_weighted_sums(static_cast<int>(total), nullptr, set, W.block_scratch.as<double2>(),
+                                 W.zsum.as<double2>(), stream()));
+    double2 z;
+    RBMG_CK(cudaMemcpyAsync(&z, W.zsum.p, sizeof(double2), cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaStreamSynchronize(stream()));
+    const double logZ = mx + std::log(z.x);
+    // normalised weights w_s = |psi_s|^2 / Z
+    RBMG_CK(launch_exp_weights(static_cast<int>(total), W.logpsi.as<double2>(), logZ, W.weights.as<double>(), stream()));
+    res->log_norm = 2.0 * std::log(psi->prefactor) + logZ;
+    res->norm_factor = std::exp(res->log_norm);
+    for (uint64_t base = 0; base < total; base += kExactChunk) {
+        Chunk c;
+        c.count = static_cast<int>(std::min<uint64_t>(kExactChunk, total - base));
+        c.enumerate = enumerate;
+        c.enum_base = base;
+        c.spins = sp ? sp + base : nullptr;
+        c.weights = W.weights.as<double>() + base;
+        const int r = fn(c);
+        if (r != RBMG_OK) return r;
+    }
+    return RBMG_OK;
+}
+
+}  // namespace rbmg
+
+extern "C" int rbmg_psi_norm(const rbmg_psi* psi, rbmg_ensemble* ex, double* norm) {
+    if (!psi || !ex || !norm) return fail(RBMG_EINVAL, "norm: null");
+    if (ex->kind != 1) return fail(RBMG_EINVAL, "norm: needs an ExactSummation");
+    StreamResult res;
+    const int r = exact_stream(ex, psi, &res, [](const Chunk&) { return RBMG_OK; });
+    if (r != RBMG_OK) return r;
+    *norm = std::exp(0.5 * res.log_norm);
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_psi_log_psi(const rbmg_psi* psi, int count, const uint64_t* spins, double* out) {
+    if (!psi || count < 0 || (count > 0 && (!spins || !out))) return fail(RBMG_EINVAL, "log_psi: bad arguments");
+    if (count == 0) return RBMG_OK;
+    const int nw = nwords_of(psi->N);
+    Workspace& W = ws();
+    RBMG_CK(W.sample_spins.ensure(sizeof(uint64_t) * nw * count));
+    RBMG_CK(W.logpsi_p.ensure(sizeof(double2) * count));
+    RBMG_CK(cudaMemcpyAsync(W.sample_spins.p, spins, sizeof(uint64_t) * nw * count, cudaMemcpyHostToDevice, stream()));
+    const int r = psi_log_psi_dev(psi, count, W.sample_spins.as<uint64_t>(), 0, 0, W.logpsi_p.as<double2>());
+    if (r != RBMG_OK) return r;
+    RBMG_CK(cudaMemcpyAsync(out, W.logpsi_p.p, sizeof(double2) * count, cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaStreamSynchronize(stream()));
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_psi_vector(const rbmg_psi* psi, double* out) {
+    if (!psi || !out) return fail(RBMG_EINVAL, "vector: null");
+    if (psi->N > 30) return fail(RBMG_EINVAL, "vector: N <= 30");
+    const uint64_t dim = 1ull << psi->N;
+    Workspace& W = ws();
+    RBMG_CK(W.logpsi.ensure(sizeof(double2) * dim));
+    for (uint64_t base = 0; base < dim; base += kExactChunk) {
+        const int cnt = static_cast<int>(std::min<uint64_t>(kExactChunk, dim - base));
+        const int r = psi_log_psi_dev(psi, cnt, nullptr, base, 1, W.logpsi.as<double2>() + base);
+        if (r != RBMG_OK) return r;
+    }
+    std::vector<double2> lp(dim);
+    RBMG_CK(cudaMemcpyAsync(lp.data(), W.logpsi.p, sizeof(double2) * dim, cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaStreamSynchronize(stream()));
+    const double lpf = std::log(psi->prefactor);   // PsiVector.cu:23-39: exp(log prefactor + log psi)
+    cplx* o = reinterpret_cast<cplx*>(out);
+    for (uint64_t x = 0; x < dim; x++) o[x] = std::exp(cplx(lpf + lp[x].x, lp[x].y));
+    return RBMG_OK;
+}
+
+// ====================================================================== estimators
+namespace rbmg {
+
+struct Sums {
+    cplx E{0, 0};
+    double E2 = 0.0;
+};
+
+int deep_gradient_chunk(const rbmg_psi* psi, const rbmg_operator* op, const Chunk& c, double2 e_shift,
+                        double2* d_eloc, double2* acc_O, double2* acc_EO, double2* acc_Ek, double2* coef1,
+                        double2* coef2, cudaStream_t st);
+int deep_eloc_chunk(const rbmg_psi* psi, const rbmg_operator* op, const Chunk& c, double2* d_eloc, cudaStream_t st);
+int deep_stream(rbmg_ensemble* e, const rbmg_psi* psi, const rbmg_operator* op, bool want_eloc,
+                size_t max_chunk_samples, const std::function<int(const Chunk&)>& fn);
+
+// local energies of one chunk into W.eloc (unless the sampler already produced them)
+static int chunk_eloc(const rbmg_psi* psi, const rbmg_operator* op, const Chunk& c, const double2** out) {
+    if (c.eloc) {
+        *out = c.eloc;
+        return RBMG_OK;
+    }
+    Workspace& W = ws();
+    RBMG_CK(W.eloc.ensure(sizeof(double2) * c.count));
+    if (psi->kind != 0) {
+        const int r = deep_eloc_chunk(psi, op, c, W.eloc.as<double2>(), stream());
+        if (r != RBMG_OK) return r;
+        *out = W.eloc.as<double2>();
+        return RBMG_OK;
+    }
+    EstLaunch L{};
+    L.count = c.count;
+    L.enum_base = c.enum_base;
+    L.spins = c.spins;
+    L.flags = EST_ELOC | (c.enumerate ? EST_ENUMERATE : 0);
+    L.eloc = W.eloc.as<double2>();
+    const OpDev od = op->dev();
+    RBMG_CK(launch_rbm_estimate(psi->rbm_dev(), &od, nullptr, L, stream()));
+    *out = W.eloc.as<double2>();
+    return RBMG_OK;
+}
+
+// weighted mean of a per-sample complex series over one chunk (sum w v / sum w)
+static int chunk_mean(const Chunk& c, const double2* v, cplx* out) {
+    Workspace& W = ws();
+    RBMG_CK(W.coef3.ensure(sizeof(double2) * c.count));
+    RBMG_CK(launch_coef(c.count, c.weights, nullptr, 1.0, W.coef3.as<double2>(), stream()));
+    RBMG_CK(W.zsum.ensure(sizeof(double2) * kMaxSeries));
+    RBMG_CK(W.block_scratch.ensure(sizeof(double2) * kSumBlocks * kMaxSeries));
+    RBMG_CK(cudaMemsetAsync(W.zsum.p, 0, sizeof(double2) * kMaxSeries, stream()));
+    SeriesSet set{};
+    set.n = 2;
+    set.v[0] = v;
+    set.v[1] = W.coef3.as<double2>();   // the weights themselves, summed with unit weight below
+    RBMG_CK(launch_weighted_sums(c.count, c.weights, set, W.block_scratch.as<double2>(), W.zsum.as<double2>(),
+                                 stream()));
+    double2 m[2];
+    RBMG_CK(cudaMemcpyAsync(m, W.zsum.p, sizeof(m), cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaStreamSynchronize(stream()));
+    // m[1] = sum w * w when weighted; the weight total needs the plain sum: recompute it
+    double wtot = static_cast<double>(c.count);
+    if (c.weights) {
+        SeriesSet s1{};
+        s1.n = 1;
+        s1.v[0] = W.coef3.as<double2>();
+        RBMG_CK(cudaMemsetAsync(W.zsum.p, 0, sizeof(double2) * kMaxSeries, stream()));
+        RBMG_CK(launch_weighted_sums(c.count, nullptr, s1, W.block_scratch.as<double2>(), W.zsum.as<double2>(),
+                                     stream()));
+        double2 t;
+        RBMG_CK(cudaMemcpyAsync(&t, W.zsum.p, sizeof(t), cudaMemcpyDeviceToHost, stream()));
+        RBMG_CK(cudaStreamSynchronize(stream()));
+        wtot = t.x;
+    }
+    *out = wtot > 0.0 ? cplx(m[0].x, m[0].y) / wtot : cplx(0.0, 0.0);
+    return RBMG_OK;
+}
+
+static int run_stream(rbmg_ensemble* ens, const rbmg_psi* psi, const rbmg_operator* op, bool sampler_eloc,
+                      size_t max_chunk, StreamResult* res, const std::function<int(const Chunk&)>& fn) {
+    if (ens->kind == 1) return exact_stream(ens, psi, res, fn);
+    res->norm_factor = 1.0 / static_cast<double>(ens->num_samples);
+    if (psi->kind != 0) return deep_stream(ens, psi, op, sampler_eloc, max_chunk, fn);
+    return mc_stream(ens, psi, op, sampler_eloc, max_chunk, fn);
+}
+
+// <E> and <|E|^2> with reference weights
+static int energy_sums(const rbmg_psi* psi, const rbmg_operator* op, rbmg_ensemble* ens, Sums* out) {
+    Workspace& W = ws();
+    RBMG_CK(W.sums.ensure(sizeof(double2) * kMaxSeries));
+    RBMG_CK(W.block_scratch.ensure(sizeof(double2) * kSumBlocks * kMaxSeries));
+    RBMG_CK(cudaMemsetAsync(W.sums.p, 0, sizeof(double2) * kMaxSeries, stream()));
+    StreamResult res;
+    int r = run_stream(ens, psi, op, true, size_t(1) << 22, &res, [&](const Chunk& c) -> int {
+        const double2* e = nullptr;
+        int rr = chunk_eloc(psi, op, c, &e);
+        if (rr != RBMG_OK) return rr;
+        RBMG_CK(W.coef2.ensure(sizeof(double2) * c.count));
+        RBMG_CK(launch_abs2(c.count, e, W.coef2.as<double2>(), stream()));
+        SeriesSet set{};
+        set.n = 2;
+        set.v[0] = e;
+        set.v[1] = W.coef2.as<double2>();
+        RBMG_CK(launch_weighted_sums(c.count, c.weights, set, W.block_scratch.as<double2>(), W.sums.as<double2>(),
+                                     stream()));
+        return RBMG_OK;
+    });
+    if (r != RBMG_OK) return r;
+    double2 s[2];
+    RBMG_CK(cudaMemcpyAsync(s, W.sums.p, sizeof(s), cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaStreamSynchronize(stream()));
+    out->E = cplx(s[0].x, s[0].y) * res.norm_factor;
+    out->E2 = s[1].x * res.norm_factor;
+    if (!std::isfinite(out->E.real()) || !std::isfinite(out->E.imag())) return fail(RBMG_ENAN, "non-finite energy");
+    return RBMG_OK;
+}
+
+static int check_pair(const rbmg_psi* psi, const rbmg_operator* op, const rbmg_ensemble* ens) {
+    if (!psi || !ens) return fail(RBMG_EINVAL, "null handle");
+    if (op && op->max_site >= psi->N) return fail(RBMG_EINVAL, "operator acts on a site >= N");
+    if (ens->kind == 1 && static_cast<int>(ens->num_spins) != psi->N)
+        return fail(RBMG_EINVAL, "ExactSummation size does not match psi");
+    return RBMG_OK;
+}
+
+}  // namespace rbmg
+
+extern "C" int rbmg_ev_value(const rbmg_psi* psi, const rbmg_operator* op, rbmg_ensemble* ens, double* value) {
+    if (!op || !value) return fail(RBMG_EINVAL, "ev: null");
+    int r = check_pair(psi, op, ens);
+    if (r != RBMG_OK) return r;
+    Sums s;
+    r = energy_sums(psi, op, ens, &s);
+    if (r != RBMG_OK) return r;
+    value[0] = s.E.real();
+    value[1] = s.E.imag();
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_ev_values(const rbmg_psi* psi, const rbmg_operator* const* ops, int num_ops, rbmg_ensemble* ens,
+                              double* values) {
+    if (!ops || num_ops < 0 || (num_ops > 0 && !values)) return fail(RBMG_EINVAL, "ev list: bad arguments");
+    // one ensemble pass per operator: MC draws continue their streams as the
+    // reference's single pass would not; for ExactSummation the result is identical.
+    for (int q = 0; q < num_ops; q++) {
+        const int r = rbmg_ev_value(psi, ops[q], ens, values + 2 * q);
+        if (r != RBMG_OK) return r;
+    }
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_ev_fluctuation(const rbmg_psi* psi, const rbmg_operator* op, rbmg_ensemble* ens, double* sigma,
+                                   double* value) {
+    if (!op || !sigma || !value) return fail(RBMG_EINVAL, "fluctuation: null");
+    int r = check_pair(psi, op, ens);
+    if (r != RBMG_OK) return r;
+    Sums s;
+    r = energy_sums(psi, op, ens, &s);
+    if (r != RBMG_OK) return r;
+    *sigma = std::sqrt(s.E2 - std::norm(s.E));   // ExpectationValue.cu:171-174
+    value[0] = s.E.real();
+    value[1] = s.E.imag();
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_ev_gradient(const rbmg_psi* psi, const rbmg_operator* op, rbmg_ensemble* ens, double* grad,
+                                double* value) {
+    if (!op || !grad || !value) return fail(RBMG_EINVAL, "gradient: null");
+    int r = check_pair(psi, op, ens);
+    if (r != RBMG_OK) return r;
+    const int N = psi->N, P = psi->num_params();
+    const int nw = nwords_of(N);
+    Workspace& W = ws();
+    const size_t ok_len = static_cast<size_t>(P - 2 * N);   // O_k entries the accumulators hold
+    RBMG_CK(W.acc_O.ensure(sizeof(double2) * ok_len));
+    RBMG_CK(W.acc_EO.ensure(sizeof(double2) * ok_len));
+    RBMG_CK(W.acc_Ek.ensure(sizeof(double2) * ok_len));
+    RBMG_CK(cudaMemsetAsync(W.acc_O.p, 0, sizeof(double2) * ok_len, stream()));
+    RBMG_CK(cudaMemsetAsync(W.acc_EO.p, 0, sizeof(double2) * ok_len, stream()));
+    RBMG_CK(cudaMemsetAsync(W.acc_Ek.p, 0, sizeof(double2) * ok_len, stream()));
+    RBMG_CK(W.sums.ensure(sizeof(double2) * kMaxSeries));
+    RBMG_CK(W.block_scratch.ensure(sizeof(double2) * kSumBlocks * kMaxSeries));
+    RBMG_CK(cudaMemsetAsync(W.sums.p, 0, sizeof(double2) * kMaxSeries, stream()));
+    constexpr int kSplits = 64;
+    size_t per_sample = 0;
+    if (psi->kind == 0) {
+        r = op_site_lists(const_cast<rbmg_operator*>(op), N);
+        if (r != RBMG_OK) return r;
+        per_sample = sizeof(float2) * psi->Mpad * (2 + op->num_offdiag) + 64;
+        RBMG_CK(W.partial.ensure(sizeof(double2) * kSplits * (1 + N) * psi->M));
+    }
+    const size_t max_chunk = psi->kind == 0 ? std::max<size_t>(256, (size_t(512) << 20) / per_sample) : 4096;
+    // The sums are centred on E0, the mean local energy of the first chunk:
+    // EO' = sum w (E - E0) O*, Ek' = sum w (E_k - E0 O), so that FP32 partial sums keep
+    // the small covariance the gradient is made of (see the formula below).
+    cplx E0(0.0, 0.0);
+    bool have_shift = false;
+    StreamResult res;
+    r = run_stream(ens, psi, op, false, max_chunk, &res, [&](const Chunk& c) -> int {
+        RBMG_CK(W.eloc.ensure(sizeof(double2) * c.count));
+        if (psi->kind != 0) {
+            if (!have_shift) {
+                const double2* e0 = nullptr;
+                const int rr0 = chunk_eloc(psi, op, c, &e0);
+                if (rr0 != RBMG_OK) return rr0;
+                const int rr1 = chunk_mean(c, e0, &E0);
+                if (rr1 != RBMG_OK) return rr1;
+                have_shift = true;
+            }
+            RBMG_CK(W.coef1.ensure(sizeof(double2) * c.count));
+            RBMG_CK(W.coef2.ensure(sizeof(double2) * c.count));
+            const int rr = deep_gradient_chunk(psi, op, c, make_double2(E0.real(), E0.imag()), W.eloc.as<double2>(),
+                                               W.acc_O.as<double2>(), W.acc_EO.as<double2>(), W.acc_Ek.as<double2>(),
+                                               W.coef1.as<double2>(), W.coef2.as<double2>(), stream());
+            if (rr != RBMG_OK) return rr;
+        } else {
+            const OpDev od = op->dev();
+            if (!have_shift) {
+                const double2* e0 = nullptr;
+                const int rr0 = chunk_eloc(psi, op, c, &e0);
+                if (rr0 != RBMG_OK) return rr0;
+                const int rr1 = chunk_mean(c, e0, &E0);
+                if (rr1 != RBMG_OK) return rr1;
+                have_shift = true;
+            }
+            RBMG_CK(W.T.ensure(sizeof(float2) * c.count * psi->Mpad));
+            RBMG_CK(W.U.ensure(sizeof(float2) * c.count * psi->Mpad));
+            RBMG_CK(W.X.ensure(sizeof(float2) * std::max<size_t>(1, size_t(c.count) * op->num_offdiag * psi->Mpad)));
+            EstLaunch L{};
+            L.count = c.count;
+            L.enum_base = c.enum_base;
+            L.spins = c.spins;
+            L.flags = EST_ELOC | EST_GRADVEC | (c.enumerate ? EST_ENUMERATE : 0);
+            L.eloc = W.eloc.as<double2>();
+            L.T = W.T.as<float2>();
+            L.U = W.U.as<float2>();
+            L.X = W.X.as<float2>();
+            L.e_shift = make_double2(E0.real(), E0.imag());
+            RBMG_CK(launch_rbm_estimate(psi->rbm_dev(), &od, nullptr, L, stream()));
+            RBMG_CK(W.coef1.ensure(sizeof(double2) * c.count));
+            RBMG_CK(W.coef2.ensure(sizeof(double2) * c.count));
+            RBMG_CK(launch_coef(c.count, c.weights, nullptr, 1.0, W.coef1.as<double2>(), stream()));
+            RBMG_CK(launch_coef(c.count, c.weights, W.eloc.as<double2>(), 1.0, W.coef2.as<double2>(), stream(),
+                                make_double2(E0.real(), E0.imag())));
+            double2* part = W.partial.as<double2>();
+            RBMG_CK(launch_outer_reduce(c.count, N, nw, psi->M, c.spins, c.enum_base, c.enumerate,
+                                        W.coef1.as<double2>(), W.T.as<float2>(), psi->Mpad, 0,
+                                        W.acc_O.as<double2>(), part, kSplits, stream()));
+            RBMG_CK(launch_outer_reduce(c.count, N, nw, psi->M, c.spins, c.enum_base, c.enumerate,
+                                        W.coef2.as<double2>(), W.T.as<float2>(), psi->Mpad, 1,
+                                        W.acc_EO.as<double2>(), part, kSplits, stream()));
+            RBMG_CK(launch_outer_reduce(c.count, N, nw, psi->M, c.spins, c.enum_base, c.enumerate,
+                                        W.coef1.as<double2>(), W.U.as<float2>(), psi->Mpad, 0,
+                                        W.acc_Ek.as<double2>(), part, kSplits, stream()));
+            RBMG_CK(launch_vterm_reduce(c.count, N, nw, psi->M, psi->Mpad, c.spins, c.enum_base, c.enumerate,
+                                        c.weights, W.X.as<float2>(), op->num_offdiag, op->d_site_ptr.as<int>(),
+                                        op->d_site_slots.as<int>(), W.acc_Ek.as<double2>(), part, kSplits,
+                                        stream()));
+        }
+        SeriesSet set{};
+        set.n = 1;
+        set.v[0] = W.eloc.as<double2>();
+        RBMG_CK(launch_weighted_sums(c.count, c.weights, set, W.block_scratch.as<double2>(), W.sums.as<double2>(),
+                                     stream()));
+        return RBMG_OK;
+    });
+    if (r != RBMG_OK) return r;
+    std::vector<double2> O(ok_len), EO(ok_len), Ek(ok_len);
+    double2 Es;
+    RBMG_CK(cudaMemcpyAsync(O.data(), W.acc_O.p, sizeof(double2) * ok_len, cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaMemcpyAsync(EO.data(), W.acc_EO.p, sizeof(double2) * ok_len, cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaMemcpyAsync(Ek.data(), W.acc_Ek.p, sizeof(double2) * ok_len, cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaMemcpyAsync(&Es, W.sums.p, sizeof(double2), cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaStreamSynchronize(stream()));
+    // ExpectationValue.cu:243-253: grad = <E O*> + conj<E_k> - 2 <E> <O*>.  With the centred
+    // sums <E O*> = EO' + E0 conj<O> and <E_k> = Ek' + E0 <O>, so
+    // grad = EO' + conj(Ek') + (E0 + conj(E0) - 2 <E>) conj<O>.
+    const double f = res.norm_factor;
+    const cplx E = cplx(Es.x, Es.y) * f;
+    const cplx shift_sum = E0 + std::conj(E0) - 2.0 * E;
+    cplx* g = reinterpret_cast<cplx*>(grad);
+    for (int k = 0; k < 2 * N; k++) g[k] = 0.0;
+    for (size_t k = 0; k < ok_len; k++) {
+        const cplx o = cplx(O[k].x, O[k].y) * f, eo = cplx(EO[k].x, EO[k].y) * f, ek = cplx(Ek[k].x, Ek[k].y) * f;
+        g[2 * N + k] = eo + std::conj(ek) + shift_sum * std::conj(o);
+    }
+    value[0] = E.real();
+    value[1] = E.imag();
+    return RBMG_OK;
+}
+
+// ====================================================================== HSD
+namespace rbmg {
+int deep_hsd64_chunk(const rbmg_psi* psi, const rbmg_psi* pp, const rbmg_operator* op, const Chunk& c,
+                     double2* d_eloc, double2* d_dlp, cudaStream_t st);
+int deep_hsd_okreduce(const rbmg_psi* pp, int pair_part, int count, const uint64_t* d_spins, uint64_t enum_base,
+                      int enumerate, const double2* d_coef, double2* acc, cudaStream_t st);
+}  // namespace rbmg
+
+// Hilbert-space distance and its gradient w.r.t. psi' (HilbertSpaceDistance.cu:14-269).
+// Stage 1 streams the ensemble of psi and computes, in FP64, omega_s, ratio_s and
+// norm_s per sample, keeping the samples; stage 2 forms the gradient numerator as
+//   u'_k v - u v'_k = sum_s w_s conj(O_k(s)) B_s,  B_s = conj(<omega>) omega_s v - u <norm> ratio_s,
+// an exact rewrite in which the nearly cancelling terms are combined per sample in
+// FP64 before the FP32 O_k reduction.  PsiPair uses the two-pass real / imaginary
+// form of HilbertSpaceDistance_PsiPair.cu:99-169, each pass drawing its own samples.
+extern "C" int rbmg_hsd_gradient(const rbmg_psi* psi, const rbmg_psi* pp, const rbmg_operator* op, int is_unitary,
+                                 rbmg_ensemble* ens, float nu, double* grad, double* distance) {
+    if (!pp || !op || !distance) return fail(RBMG_EINVAL, "hsd: null");
+    int r = check_pair(psi, op, ens);
+    if (r != RBMG_OK) return r;
+    if (pp->N != psi->N) return fail(RBMG_EINVAL, "hsd: psi and psi_prime differ in N");
+    if (psi->kind != pp->kind) return fail(RBMG_EUNSUPPORTED, "hsd: psi and psi_prime must be of the same kind");
+    if (psi->kind == 0 && pp->M != psi->M) return fail(RBMG_EUNSUPPORTED, "hsd: psi and psi_prime need the same M");
+    const bool want_grad = grad != nullptr;
+    const int N = pp->N, P = pp->num_params();
+    const int nw = nwords_of(N);
+    const size_t ok_len = static_cast<size_t>(P - 2 * N);
+    Workspace& W = ws();
+    constexpr int kSplits = 64;
+    const int passes = (pp->kind == 2 && want_grad) ? 2 : 1;
+    const uint64_t total = ens->num_steps();
+    std::vector<cplx> gout(P, 0.0);
+    double dist = 0.0;
+    const OpDev od = op->dev();
+    if (psi->kind == 0) {
+        r = rbm_upload64(psi);
+        if (r == RBMG_OK) r = rbm_upload64(pp);
+        if (r != RBMG_OK) return r;
+    }
+    for (int pass = 0; pass < passes; pass++) {
+        // ---- stage 1
+        RBMG_CK(W.omega.ensure(sizeof(double2) * total));
+        RBMG_CK(W.pr.ensure(sizeof(double2) * total));
+        RBMG_CK(W.nn.ensure(sizeof(double2) * total));
+        RBMG_CK(W.coef3.ensure(sizeof(double) * total));      // weights of all samples
+        RBMG_CK(W.Tp.ensure(sizeof(uint64_t) * nw * total));   // spins of all samples
+        RBMG_CK(W.sums.ensure(sizeof(double2) * kMaxSeries));
+        RBMG_CK(W.block_scratch.ensure(sizeof(double2) * kSumBlocks * kMaxSeries));
+        RBMG_CK(cudaMemsetAsync(W.sums.p, 0, sizeof(double2) * kMaxSeries, stream()));
+        uint64_t* all_spins = W.Tp.as<uint64_t>();
+        double* all_w = W.coef3.as<double>();
+        bool weighted = false, enumerated = false;
+        uint64_t offset = 0;
+        StreamResult res;
+        r = run_stream(ens, psi, op, false, size_t(1) << 20, &res, [&](const Chunk& c) -> int {
+            RBMG_CK(W.eloc.ensure(sizeof(double2) * c.count));
+            RBMG_CK(W.logpsi_p.ensure(sizeof(double2) * c.count));
+            if (psi->kind == 0) {
+                Hsd64Launch L{};
+                L.count = c.count;
+                L.enum_base = c.enum_base;
+                L.enumerate = c.enumerate;
+                L.spins = c.spins;
+                L.eloc = W.eloc.as<double2>();
+                L.dlogpsi = W.logpsi_p.as<double2>();
+                RBMG_CK(launch_rbm_hsd64(rbm64(psi), rbm64(pp), od, L, stream()));
+            } else {
+                const int rr = deep_hsd64_chunk(psi, pp, op, c, W.eloc.as<double2>(), W.logpsi_p.as<double2>(),
+                                                stream());
+                if (rr != RBMG_OK) return rr;
+            }
+            RBMG_CK(launch_hsd_terms64(c.count, W.eloc.as<double2>(), W.logpsi_p.as<double2>(), is_unitary,
+                                       W.omega.as<double2>() + offset, W.pr.as<double2>() + offset,
+                                       W.nn.as<double2>() + offset, stream()));
+            if (c.spins) {
+                RBMG_CK(cudaMemcpyAsync(all_spins + offset * nw, c.spins, sizeof(uint64_t) * nw * c.count,
+                                        cudaMemcpyDeviceToDevice, stream()));
+            } else {
+                enumerated = true;
+            }
+            if (c.weights) {
+                weighted = true;
+                RBMG_CK(cudaMemcpyAsync(all_w + offset, c.weights, sizeof(double) * c.count, cudaMemcpyDeviceToDevice,
+                                        stream()));
+            }
+            offset += c.count;
+            return RBMG_OK;
+        });
+        if (r != RBMG_OK) return r;
+        const int count = static_cast<int>(offset);
+        SeriesSet set{};
+        set.n = 3;
+        set.v[0] = W.omega.as<double2>();
+        set.v[1] = W.pr.as<double2>();
+        set.v[2] = W.nn.as<double2>();
+        RBMG_CK(launch_weighted_sums(count, weighted ? all_w : nullptr, set, W.block_scratch.as<double2>(),
+                                     W.sums.as<double2>(), stream()));
+        double2 s3[3];
+        RBMG_CK(cudaMemcpyAsync(s3, W.sums.p, sizeof(s3), cudaMemcpyDeviceToHost, stream()));
+        RBMG_CK(cudaStreamSynchronize(stream()));
+        const double f = res.norm_factor;
+        const cplx omega = cplx(s3[0].x, s3[0].y) * f;
+        const double pr = s3[1].x * f, nn = s3[2].x * f;
+        const double u = std::norm(omega);   // HilbertSpaceDistance.cu:216-220, 248-250
+        const double v = nn * pr;
+        dist = std::sqrt(1.0 - u / v);
+        if (!want_grad) break;
+        // ---- stage 2: sum_s w_s c_s O_k(s) over the kept samples
+        const int mode = passes == 1 ? 0 : (pass == 0 ? 1 : 2);
+        RBMG_CK(W.coef1.ensure(sizeof(double2) * count));
+        RBMG_CK(launch_hsd_coef(count, weighted ? all_w : nullptr, W.omega.as<double2>(), W.pr.as<double2>(),
+                                make_double2(omega.real(), -omega.imag()), v, u, nn, mode, W.coef1.as<double2>(),
+                                stream()));
+        RBMG_CK(W.acc_wO.ensure(sizeof(double2) * ok_len));
+        RBMG_CK(cudaMemsetAsync(W.acc_wO.p, 0, sizeof(double2) * ok_len, stream()));
+        const uint64_t* sp = enumerated ? (ens->exact_total_z ? ens->d_allowed.as<uint64_t>() : nullptr) : all_spins;
+        const int enumerate = (enumerated && !ens->exact_total_z) ? 1 : 0;
+        if (pp->kind == 0) {
+            RBMG_CK(W.partial.ensure(sizeof(double2) * kSplits * (1 + N) * pp->M));
+            const int chunk = std::max(1024, static_cast<int>((size_t(256) << 20) / (sizeof(float2) * pp->Mpad)));
+            RBMG_CK(W.T.ensure(sizeof(float2) * std::min(chunk, count) * pp->Mpad));
+            RBMG_CK(W.logpsi.ensure(sizeof(double2) * std::min(chunk, count)));
+            const RbmDev pd = pp->rbm_dev();
+            for (int base = 0; base < count; base += chunk) {
+                const int cnt = std::min(chunk, count - base);
+                EstLaunch L{};
+                L.count = cnt;
+                L.enum_base = static_cast<uint64_t>(base);
+                L.spins = sp ? sp + static_cast<size_t>(base) * nw : nullptr;
+                L.flags = EST_PRIME | (enumerate ? EST_ENUMERATE : 0);
+                L.logpsi_prime = W.logpsi.as<double2>();
+                L.Tp = W.T.as<float2>();
+                RBMG_CK(launch_rbm_estimate(pd, nullptr, &pd, L, stream()));
+                RBMG_CK(launch_outer_reduce(cnt, N, nw, pp->M, L.spins, L.enum_base, enumerate,
+                                            W.coef1.as<double2>() + base, W.T.as<float2>(), pp->Mpad, 1,
+                                            W.acc_wO.as<double2>(), W.partial.as<double2>(), kSplits, stream()));
+            }
+        } else {
+            const int rr = deep_hsd_okreduce(pp, passes == 2 ? pass : -1, count, sp, 0, enumerate,
+                                             W.coef1.as<double2>(), W.acc_wO.as<double2>(), stream());
+            if (rr != RBMG_OK) return rr;
+        }
+        std::vector<double2> acc(ok_len);
+        RBMG_CK(cudaMemcpyAsync(acc.data(), W.acc_wO.p, sizeof(double2) * ok_len, cudaMemcpyDeviceToHost, stream()));
+        RBMG_CK(cudaStreamSynchronize(stream()));
+        if (mode == 0) {          // HilbertSpaceDistance.cu:253-263
+            const double pf = std::pow(dist, static_cast<double>(nu));
+            for (size_t k = 0; k < ok_len; k++) gout[2 * N + k] = -(cplx(acc[k].x, acc[k].y) * f) / (v * v) / pf;
+        } else if (mode == 1) {   // HilbertSpaceDistance_PsiPair.cu:121-133
+            for (size_t k = 0; k < ok_len; k++) gout[2 * N + k] = cplx(-(acc[k].x * f) / (v * v) / dist, 0.0);
+        } else {                  // HilbertSpaceDistance_PsiPair.cu:153-163
+            for (size_t k = 0; k < ok_len; k++) gout[2 * N + k] += cplx(0.0, -(acc[k].x * f) / v / dist);
+        }
+    }
+    *distance = dist;
+    if (want_grad) std::memcpy(grad, gout.data(), sizeof(cplx) * P);
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_hsd_distance(const rbmg_psi* psi, const rbmg_psi* pp, const rbmg_operator* op, int is_unitary,
+                                 rbmg_ensemble* ens, double* distance) {
+    return rbmg_hsd_gradient(psi, pp, op, is_unitary, ens, 1.0f, nullptr, distance);
+}
+
+// ====================================================================== samples / O_k
+extern "C" int rbmg_ensemble_samples(rbmg_ensemble* ens, const rbmg_psi* psi, const rbmg_operator* op,
+                                     uint64_t* spins, double* log_psi, double* eloc) {
+    int r = check_pair(psi, op, ens);
+    if (r != RBMG_OK) return r;
+    if (eloc && !op) return fail(RBMG_EINVAL, "samples: local energies need an operator");
+    const int nw = nwords_of(psi->N);
+    Workspace& W = ws();
+    uint64_t offset = 0;
+    StreamResult res;
+    r = run_stream(ens, psi, op, eloc != nullptr, size_t(1) << 22, &res, [&](const Chunk& c) -> int {
+        if (spins) {
+            if (c.spins) {
+                RBMG_CK(cudaMemcpyAsync(spins + offset * nw, c.spins, sizeof(uint64_t) * nw * c.count,
+                                        cudaMemcpyDeviceToHost, stream()));
+            } else {
+                for (int t = 0; t < c.count; t++) {
+                    spins[(offset + t) * nw] = c.enum_base + t;
+                    for (int k = 1; k < nw; k++) spins[(offset + t) * nw + k] = 0;
+                }
+            }
+        }
+        if (log_psi) {
+            RBMG_CK(W.logpsi_p.ensure(sizeof(double2) * c.count));
+            const int rr = psi_log_psi_dev(psi, c.count, c.spins, c.enum_base, c.enumerate, W.logpsi_p.as<double2>());
+            if (rr != RBMG_OK) return rr;
+            RBMG_CK(cudaMemcpyAsync(log_psi + 2 * offset, W.logpsi_p.p, sizeof(double2) * c.count,
+                                    cudaMemcpyDeviceToHost, stream()));
+        }
+        if (eloc) {
+            const double2* e = nullptr;
+            const int rr = chunk_eloc(psi, op, c, &e);
+            if (rr != RBMG_OK) return rr;
+            RBMG_CK(cudaMemcpyAsync(eloc + 2 * offset, e, sizeof(double2) * c.count, cudaMemcpyDeviceToHost, stream()));
+        }
+        RBMG_CK(cudaStreamSynchronize(stream()));
+        offset += c.count;
+        return RBMG_OK;
+    });
+    return r;
+}
+
+namespace rbmg {
+int deep_ok_vector(const rbmg_psi* psi, const uint64_t* d_spins, double2* d_out, cudaStream_t st);
+}  // namespace rbmg
+
+extern "C" int rbmg_psi_O_k_vector(const rbmg_psi* psi, const uint64_t* spins, double* out) {
+    if (!psi || !spins || !out) return fail(RBMG_EINVAL, "O_k_vector: null");
+    const int N = psi->N, P = psi->num_params();
+    const int nw = nwords_of(N);
+    Workspace& W = ws();
+    RBMG_CK(W.sample_spins.ensure(sizeof(uint64_t) * nw));
+    RBMG_CK(cudaMemcpyAsync(W.sample_spins.p, spins, sizeof(uint64_t) * nw, cudaMemcpyHostToDevice, stream()));
+    cplx* o = reinterpret_cast<cplx*>(out);
+    for (int k = 0; k < P; k++) o[k] = 0.0;
+    if (psi->kind == 0) {
+        RBMG_CK(W.Tp.ensure(sizeof(float2) * psi->Mpad));
+        RBMG_CK(W.logpsi_p.ensure(sizeof(double2)));
+        EstLaunch L{};
+        L.count = 1;
+        L.spins = W.sample_spins.as<uint64_t>();
+        L.flags = EST_PRIME;    // psi itself as psi': writes tanh(theta) into Tp
+        L.logpsi_prime = W.logpsi_p.as<double2>();
+        L.Tp = W.Tp.as<float2>();
+        const RbmDev d = psi->rbm_dev();
+        RBMG_CK(launch_rbm_estimate(d, nullptr, &d, L, stream()));
+        std::vector<float2> T(psi->Mpad);
+        RBMG_CK(cudaMemcpyAsync(T.data(), W.Tp.p, sizeof(float2) * psi->Mpad, cudaMemcpyDeviceToHost, stream()));
+        RBMG_CK(cudaStreamSynchronize(stream()));
+        const int M = psi->M;   // Psi.hpp:165-178
+        for (int j = 0; j < M; j++) {
+            const cplx t(T[j].x, T[j].y);
+            o[2 * N + j] = t;
+            for (int i = 0; i < N; i++) {
+                const bool up = (spins[i >> 6] >> (i & 63)) & 1ull;
+                o[2 * N + M + static_cast<size_t>(i) * M + j] = up ? t : -t;
+            }
+        }
+        return RBMG_OK;
+    }
+    RBMG_CK(W.acc_O.ensure(sizeof(double2) * P));
+    const int r = deep_ok_vector(psi, W.sample_spins.as<uint64_t>(), W.acc_O.as<double2>(), stream());
+    if (r != RBMG_OK) return r;
+    RBMG_CK(cudaMemcpyAsync(out + 4 * N, W.acc_O.p, sizeof(double2) * (P - 2 * N), cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaStreamSynchronize(stream()));
+    return RBMG_OK;
+}
+
+// ====================================================================== persistent chains
+struct rbmg_chain {
+    int N = 0, nw = 0;
+    uint32_t walkers = 0;
+    uint64_t seed = 0;
+    DevBuf spins, rng_index, accepts, proposals;
+    bool initialised = false;
+};
+
+extern "C" int rbmg_stream(void** st) {
+    if (!st) return fail(RBMG_EINVAL, "stream: null");
+    *st = static_cast<void*>(stream());
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_chain_create(const rbmg_psi* psi, uint32_t num_walkers, uint64_t seed, rbmg_chain** out) {
+    if (!psi || !out || num_walkers == 0) return fail(RBMG_EINVAL, "chain: bad arguments");
+    if (psi->kind != 0) return fail(RBMG_EUNSUPPORTED, "chain: complex RBM only");
+    auto c = std::make_unique<rbmg_chain>();
+    c->N = psi->N;
+    c->nw = nwords_of(psi->N);
+    c->walkers = num_walkers;
+    c->seed = seed;
+    RBMG_CK(c->spins.ensure(sizeof(uint64_t) * c->nw * num_walkers));
+    RBMG_CK(c->rng_index.ensure(sizeof(uint64_t) * num_walkers));
+    RBMG_CK(c->accepts.ensure(sizeof(unsigned long long) * num_walkers));
+    RBMG_CK(c->proposals.ensure(sizeof(unsigned long long) * num_walkers));
+    RBMG_CK(cudaMemset(c->rng_index.p, 0, sizeof(uint64_t) * num_walkers));
+    RBMG_CK(cudaMemset(c->accepts.p, 0, sizeof(unsigned long long) * num_walkers));
+    RBMG_CK(cudaMemset(c->proposals.p, 0, sizeof(unsigned long long) * num_walkers));
+    *out = c.release();
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_chain_destroy(rbmg_chain* c) {
+    delete c;
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_chain_sweep_async(rbmg_chain* c, const rbmg_psi* psi, const rbmg_operator* op, int n_sweeps,
+                                      int measure_every, void* d_eloc_out, void* st) {
+    if (!c || !psi || n_sweeps < 0) return fail(RBMG_EINVAL, "chain sweep: bad arguments");
+    if (psi->kind != 0 || psi->N != c->N) return fail(RBMG_EINVAL, "chain sweep: psi does not match the chain");
+    if (d_eloc_out && (!op || measure_every <= 0)) return fail(RBMG_EINVAL, "chain sweep: measurement needs op");
+    if (op && op->max_site >= psi->N) return fail(RBMG_EINVAL, "chain sweep: operator acts on a site >= N");
+    if (n_sweeps == 0) return RBMG_OK;
+    const int every = d_eloc_out ? measure_every : n_sweeps;
+    McLaunch L{};
+    L.B = static_cast<int>(c->walkers);
+    L.walker_base = 0;
+    L.seed = c->seed;
+    L.spins = c->spins.as<uint64_t>();
+    L.rng_index = c->rng_index.as<uint64_t>();
+    L.init = c->initialised ? 0 : 1;
+    L.n_therm = d_eloc_out ? n_sweeps % every : n_sweeps;
+    L.n_samples = d_eloc_out ? n_sweeps / every : 0;
+    L.sweeps_per_sample = every;
+    L.eloc = static_cast<double2*>(d_eloc_out);
+    L.accepts = c->accepts.as<unsigned long long>();
+    L.proposals = c->proposals.as<unsigned long long>();
+    OpDev od;
+    if (op) od = op->dev();
+    RBMG_CK(launch_rbm_mc(psi->rbm_dev(), op ? &od : nullptr, L, st ? static_cast<cudaStream_t>(st) : stream()));
+    c->initialised = true;
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_chain_state(const rbmg_chain* c, uint64_t* spins, uint64_t* accepts, uint64_t* proposals) {
+    if (!c) return fail(RBMG_EINVAL, "chain state: null");
+    RBMG_CK(cudaDeviceSynchronize());
+    if (spins) RBMG_CK(cudaMemcpy(spins, c->spins.p, sizeof(uint64_t) * c->nw * c->walkers, cudaMemcpyDeviceToHost));
+    std::vector<unsigned long long> a(c->walkers), p(c->walkers);
+    RBMG_CK(cudaMemcpy(a.data(), c->accepts.p, sizeof(unsigned long long) * c->walkers, cudaMemcpyDeviceToHost));
+    RBMG_CK(cudaMemcpy(p.data(), c->proposals.p, sizeof(unsigned long long) * c->walkers, cudaMemcpyDeviceToHost));
+    uint64_t sa = 0, sp = 0;
+    for (uint32_t w = 0; w < c->walkers; w++) {
+        sa += a[w];
+        sp += p[w];
+    }
+    if (accepts) *accepts = sa;
+    if (proposals) *proposals = sp;
+    return RBMG_OK;
+}

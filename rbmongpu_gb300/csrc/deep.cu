@@ -1,0 +1,832 @@
+// PsiDeep / PsiPair kernels (include/quantum_state/PsiDeep.hpp:89-293, PsiPair.hpp:36-119).
+//
+// One CTA per configuration: thread j owns unit j of the layer being evaluated;
+// the layer's inputs, angles and activations live in shared memory; weights are read
+// coalesced over j ([connectivity][size] layout, as the reference stores them).
+// The backward pass gathers over the rhs connection lists compiled on the host in
+// the reference's order (source/quantum_state/PsiDeep.cu:85-117).
+#include <algorithm>
+#include <functional>
+#include <memory>
+
+#include "device_math.cuh"
+#include "host.h"
+#include "reduce.h"
+
+namespace rbmg {
+
+struct Chunk {
+    int count = 0;
+    const uint64_t* spins = nullptr;
+    int enumerate = 0;
+    uint64_t enum_base = 0;
+    const double* weights = nullptr;
+    const double2* eloc = nullptr;
+};
+
+namespace {
+
+// ---------------------------------------------------------------- complex helpers
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+template <typename V> __device__ __forceinline__ V czero();
+template <> __device__ __forceinline__ float2 czero<float2>() { return make_float2(0.f, 0.f); }
+template <> __device__ __forceinline__ double2 czero<double2>() { return make_double2(0.0, 0.0); }
+template <typename V> __device__ __forceinline__ V creal(double x);
+template <> __device__ __forceinline__ float2 creal<float2>(double x) { return make_float2(float(x), 0.f); }
+template <> __device__ __forceinline__ double2 creal<double2>(double x) { return make_double2(x, 0.0); }
+
+__device__ __forceinline__ double2 lc64(double2 z) {
+    const double s = z.x > 0.0 ? 1.0 : -1.0;
+    double2 t = make_double2(s * 3.746646023906276 + z.x, z.y);
+    t = cmul(z, t); t.x += 7.771429504240965;
+    t = cmul(z, t); t.x += s * 10.2180213465;
+    t = cmul(z, t); t.x += 9.19376335670885;
+    const double2 num = make_double2(5.49914721954 - s * 2.16564366435 * z.x, -s * 2.16564366435 * z.y);
+    const double den = t.x * t.x + t.y * t.y;
+    return make_double2(s * 0.9003320053750442 * z.x + (num.x * t.x + num.y * t.y) / den - 0.598139,
+                        s * 0.9003320053750442 * z.y + (num.y * t.x - num.x * t.y) / den);
+}
+
+// activation: the reference's rational log-cosh for complex nets, ReLU for the real
+// nets of a PsiPair (include/quantum_state/psi_functions.hpp:118-125)
+template <bool REAL> __device__ __forceinline__ float2 act(float2 a) {
+    return REAL ? make_float2(a.x > 0.f ? a.x : 0.f, 0.f) : lc_c(a.x, a.y);
+}
+template <bool REAL> __device__ __forceinline__ double2 act(double2 a) {
+    return REAL ? make_double2(a.x > 0.0 ? a.x : 0.0, 0.0) : lc64(a);
+}
+// derivative: my_tanh for complex nets, 1 for the real nets (psi_functions.hpp:127-136)
+template <bool REAL> __device__ __forceinline__ float2 dact(float2 a) {
+    return REAL ? make_float2(1.f, 0.f) : tanh_c(a.x, a.y);
+}
+
+template <typename V> struct W_of;
+template <> struct W_of<float2> {
+    static __device__ __forceinline__ const float2* w(const DeepNetDev& n, int l) { return n.w[l]; }
+    static __device__ __forceinline__ const float2* b(const DeepNetDev& n, int l) { return n.b[l]; }
+    static __device__ __forceinline__ const float2* fw(const DeepNetDev& n) { return n.fw; }
+};
+template <> struct W_of<double2> {
+    static __device__ __forceinline__ const double2* w(const DeepNetDev& n, int l) { return n.w64[l]; }
+    static __device__ __forceinline__ const double2* b(const DeepNetDev& n, int l) { return n.b64[l]; }
+    static __device__ __forceinline__ const double2* fw(const DeepNetDev& n) { return n.fw64; }
+};
+
+// deterministic block sum of one complex value per thread; all threads receive it
+template <typename V>
+__device__ __forceinline__ V block_sum(V v, V* red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, off);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, off);
+    }
+    __syncthreads();
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    V t = czero<V>();
+    for (int q = 0; q < nwarps; q++) t = cadd(t, red[q]);
+    return t;
+}
+
+__device__ __forceinline__ bool bit_up(const uint64_t* s, int i) { return (s[i >> 6] >> (i & 63)) & 1ull; }
+
+// shared-memory layout of one configuration's evaluation
+template <typename V>
+struct Work {
+    V* in;        // [width]
+    V* out;       // [width]
+    V* angles;    // [units] or null
+    V* acts;      // [units] or null
+    V* red;       // [32]
+    uint64_t* s;  // [kMaxWords] spins being evaluated
+};
+
+// forward pass (PsiDeep.hpp:89-133) of one net on the spins in w.s; returns
+// sum_j act_j * final_w_j; with STORE keeps every angle and activation
+template <typename V, bool REAL, bool STORE>
+__device__ V forward_once(const DeepNetDev& net, const uint64_t* s, Work<V>& w) {
+    const int t = threadIdx.x;
+    if (t < net.N) w.in[t] = creal<V>(bit_up(s, t) ? 1.0 : -1.0);
+    __syncthreads();
+    V* in = w.in;
+    V* out = w.out;
+    for (int l = 0; l < net.L; l++) {
+        const int size = net.size[l], conn = net.conn[l];
+        if (t < size) {
+            const V* wl = W_of<V>::w(net, l);
+            const int* ci = net.cidx[l];
+            V a = czero<V>();
+            for (int c = 0; c < conn; c++) a = cadd(a, cmul(wl[c * size + t], in[ci[c * size + t]]));
+            a = cadd(a, W_of<V>::b(net, l)[t]);
+            const V y = act<REAL>(a);
+            if (STORE) {
+                w.angles[net.begin_angle[l] + t] = a;
+                w.acts[net.begin_angle[l] + t] = y;
+            }
+            out[t] = y;
+        }
+        __syncthreads();
+        V* tmp = in;
+        in = out;
+        out = tmp;
+    }
+    const int last = net.size[net.L - 1];
+    V term = czero<V>();
+    if (t < last) term = cmul(in[t], W_of<V>::fw(net)[t]);
+    return block_sum(term, w.red);
+}
+
+// log psi of one net with optional translational averaging (PsiDeep.hpp:135-169)
+template <typename V, bool REAL>
+__device__ V net_log_psi(const DeepNetDev& net, const uint64_t* s, Work<V>& w, uint64_t* shifted) {
+    if (!net.ti) return forward_once<V, REAL, false>(net, s, w);
+    V r = czero<V>();
+    for (int shift = 0; shift < net.N; shift++) {
+        __syncthreads();
+        if (threadIdx.x == 0) {   // Spins_t<1>::rotate_left (include/Spins.h:280-285)
+            const uint64_t x = s[0];
+            uint64_t y = shift == 0 ? x : ((x << shift) | (x >> (net.N - shift)));
+            if (net.N < 64) y &= (1ull << net.N) - 1ull;
+            shifted[0] = y;
+        }
+        __syncthreads();
+        r = cadd(r, forward_once<V, REAL, false>(net, shifted, w));
+    }
+    const double inv = 1.0 / net.N;
+    r.x *= inv;
+    r.y *= inv;
+    return r;
+}
+
+// log psi of the state: one complex net, or (Re, Im) from the two real nets of a PsiPair
+template <typename V>
+__device__ V state_log_psi(const DeepNetDev& n0, const DeepNetDev& n1, int pair, const uint64_t* s, Work<V>& w,
+                           uint64_t* shifted) {
+    if (!pair) return net_log_psi<V, false>(n0, s, w, shifted);
+    const V re = net_log_psi<V, true>(n0, s, w, shifted);
+    const V im = net_log_psi<V, true>(n1, s, w, shifted);
+    V r;
+    r.x = re.x;
+    r.y = im.x;
+    return r;
+}
+
+// reverse pass (PsiDeep.hpp:214-293) after forward_once<STORE>; emit(k, value) with k
+// counted from the first O_k entry (parameter index - 2N)
+template <bool REAL, typename Emit>
+__device__ void backward(const DeepNetDev& net, const uint64_t* s, Work<float2>& w, float2 log_psi, Emit emit) {
+    const int t = threadIdx.x;
+    const int L = net.L;
+    float2* cur = w.in;
+    float2* nxt = w.out;
+    for (int l = L - 1; l >= 0; l--) {
+        const int size = net.size[l];
+        float2 d = make_float2(0.f, 0.f);
+        if (t < size) {
+            const float2 ang = w.angles[net.begin_angle[l] + t];
+            if (l == L - 1) {
+                d = cmul(net.fw[t], dact<REAL>(ang));
+            } else {
+                const int nsize = net.size[l + 1];
+                float2 acc = make_float2(0.f, 0.f);
+                for (int e = net.rptr[l][t]; e < net.rptr[l][t + 1]; e++) {
+                    const int q = net.rq[l][e];
+                    acc = cadd(acc, cmul(net.w[l + 1][q], nxt[q % nsize]));
+                }
+                d = cmul(acc, dact<REAL>(ang));
+            }
+        }
+        __syncthreads();
+        if (t < size) {
+            cur[t] = d;
+            const int base = net.begin_params[l];
+            emit(base + t, d);
+            const int conn = net.conn[l];
+            for (int c = 0; c < conn; c++) {
+                const int src = net.cidx[l][c * size + t];
+                const float2 in = l == 0 ? make_float2(bit_up(s, src) ? 1.f : -1.f, 0.f)
+                                         : w.acts[net.begin_angle[l - 1] + src];
+                emit(base + size + c * size + t, cmul(d, in));
+            }
+        }
+        __syncthreads();
+        float2* tmp = cur;
+        cur = nxt;
+        nxt = tmp;
+    }
+    // final weights: log psi * activation of the last layer (PsiDeep.hpp:285-292)
+    const int last = net.size[L - 1];
+    if (t < last) emit(net.P - 2 * net.N - last + t, cmul(log_psi, w.acts[net.begin_angle[L - 1] + t]));
+    __syncthreads();
+}
+
+template <typename V>
+__device__ Work<V> carve(void* base, const DeepNetDev& net, bool store) {
+    Work<V> w;
+    V* p = static_cast<V*>(base);
+    const int width = net.width;
+    w.red = p;
+    p += 32;
+    w.in = p;
+    p += width;
+    w.out = p;
+    p += width;
+    w.angles = store ? p : nullptr;
+    if (store) p += net.units;
+    w.acts = store ? p : nullptr;
+    if (store) p += net.units;
+    w.s = reinterpret_cast<uint64_t*>(p);
+    return w;
+}
+
+__device__ __forceinline__ void load_config(const uint64_t* spins, uint64_t enum_base, int enumerate, long t, int N,
+                                            uint64_t* s) {
+    const int nw = (N + 63) / 64;
+    if (threadIdx.x < kMaxWords) {
+        uint64_t v = 0;
+        if (enumerate) {
+            if (threadIdx.x == 0) {
+                v = enum_base + static_cast<uint64_t>(t);
+                if (N < 64) v &= (1ull << N) - 1ull;
+            }
+        } else if (static_cast<int>(threadIdx.x) < nw) {
+            v = spins[t * nw + threadIdx.x];
+        }
+        s[threadIdx.x] = v;
+    }
+    __syncthreads();
+}
+
+// string n applied to s: flipped configuration into sp, returns coef * phase (Operator.hpp:45-88)
+__device__ double2 apply_string(const OpDev& op, int n, const uint64_t* s, uint64_t* sp) {
+    int parity = 0;
+    for (int k = 0; k < kMaxWords; k++) parity += __popcll(op.zmask[n * kMaxWords + k] & ~s[k]);
+    const double sg = (parity & 1) ? -1.0 : 1.0;
+    const double2 c = op.coef[n];
+    const int yp = op.ypow[n] & 3;
+    double2 r = yp == 0 ? c : (yp == 1 ? make_double2(c.y, -c.x) : (yp == 2 ? make_double2(-c.x, -c.y)
+                                                                            : make_double2(-c.y, c.x)));
+    __syncthreads();
+    if (threadIdx.x < kMaxWords) {
+        uint64_t v = s[threadIdx.x];
+        for (int q = 0; q < op.nflip[n]; q++) {
+            const int site = op.flip_sites[op.flip_off[n] + q];
+            if ((site >> 6) == static_cast<int>(threadIdx.x)) v ^= 1ull << (site & 63);
+        }
+        sp[threadIdx.x] = v;
+    }
+    __syncthreads();
+    return make_double2(sg * r.x, sg * r.y);
+}
+
+// ---------------------------------------------------------------- kernels
+template <typename V>
+__global__ void deep_logpsi_kernel(DeepNetDev n0, DeepNetDev n1, int pair, int count, const uint64_t* spins,
+                                   uint64_t enum_base, int enumerate, double2* out) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    Work<V> w = carve<V>(smem, n0, false);
+    uint64_t* shifted = w.s + kMaxWords;
+    const long t = blockIdx.x;
+    if (t >= count) return;
+    load_config(spins, enum_base, enum_base >= 0 && enumerate, t, n0.N, w.s);
+    const V lp = state_log_psi<V>(n0, n1, pair, w.s, w, shifted);
+    if (threadIdx.x == 0) out[t] = make_double2(lp.x, lp.y);
+}
+
+// local energy (Operator.hpp:90-115); FP32 or FP64 evaluation; with PRIME also
+// log psi'(s) - log psi(s) for the Hilbert-space distance
+template <typename V, bool PRIME>
+__global__ void deep_eloc_kernel(DeepNetDev n0, DeepNetDev n1, int pair, DeepNetDev p0, DeepNetDev p1, OpDev op,
+                                 int count, const uint64_t* spins, uint64_t enum_base, int enumerate, double2* eloc,
+                                 double2* dlp) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    Work<V> w = carve<V>(smem, n0.width >= p0.width ? n0 : p0, false);
+    uint64_t* sp = w.s + kMaxWords;
+    uint64_t* shifted = sp + kMaxWords;
+    const long t = blockIdx.x;
+    if (t >= count) return;
+    load_config(spins, enum_base, enumerate, t, n0.N, w.s);
+    const V lp = state_log_psi<V>(n0, n1, pair, w.s, w, shifted);
+    double er = 0.0, ei = 0.0;
+    for (int n = 0; n < op.S; n++) {
+        const double2 cf = apply_string(op, n, w.s, sp);
+        if (op.nflip[n] == 0) {
+            er += cf.x;
+            ei += cf.y;
+            continue;
+        }
+        const V lq = state_log_psi<V>(n0, n1, pair, sp, w, shifted);
+        const double dr = static_cast<double>(lq.x) - static_cast<double>(lp.x);
+        const double di = static_cast<double>(lq.y) - static_cast<double>(lp.y);
+        const double m = exp(dr);
+        const double xr = m * cos(di), xi = m * sin(di);
+        er += cf.x * xr - cf.y * xi;
+        ei += cf.x * xi + cf.y * xr;
+    }
+    double2 d = make_double2(0.0, 0.0);
+    if (PRIME) {
+        const V lq = state_log_psi<V>(p0, p1, pair, w.s, w, shifted);
+        d = make_double2(static_cast<double>(lq.x) - static_cast<double>(lp.x),
+                         static_cast<double>(lq.y) - static_cast<double>(lp.y));
+    }
+    if (threadIdx.x == 0) {
+        if (eloc) eloc[t] = make_double2(er, ei);
+        if (PRIME) dlp[t] = d;
+    }
+}
+
+// O_k rows [count][P - 2N] of one net (complex, or a real PsiPair net stored as (x, 0))
+template <bool REAL>
+__global__ void deep_ok_kernel(DeepNetDev net, int count, const uint64_t* spins, uint64_t enum_base, int enumerate,
+                               float2* rows, long ld) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    Work<float2> w = carve<float2>(smem, net, true);
+    const long t = blockIdx.x;
+    if (t >= count) return;
+    load_config(spins, enum_base, enumerate, t, net.N, w.s);
+    const float2 lp = forward_once<float2, REAL, true>(net, w.s, w);
+    float2* row = rows + t * ld;
+    backward<REAL>(net, w.s, w, lp, [&](int k, float2 v) { row[k] = v; });
+}
+
+// per sample: E_loc, O_k(s) row, and the centred E_k row
+//   Ek[s] = (E_diag - E0) O(s) + sum_{off-diagonal n} e_n O(s'_n)
+// (Operator.hpp:145-179 with the shift of the gradient estimator)
+__global__ void deep_grad_kernel(DeepNetDev net, OpDev op, int count, const uint64_t* spins, uint64_t enum_base,
+                                 int enumerate, double2 e_shift, double2* eloc, float2* Orows, float2* Ekrows,
+                                 long ld) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    Work<float2> w = carve<float2>(smem, net, true);
+    uint64_t* sp = w.s + kMaxWords;
+    const long t = blockIdx.x;
+    if (t >= count) return;
+    load_config(spins, enum_base, enumerate, t, net.N, w.s);
+    float2* orow = Orows + t * ld;
+    float2* erow = Ekrows + t * ld;
+    const float2 lp = forward_once<float2, false, true>(net, w.s, w);
+    backward<false>(net, w.s, w, lp, [&](int k, float2 v) { orow[k] = v; });
+    // diagonal part first
+    double dr_ = 0.0, di_ = 0.0;
+    for (int n = 0; n < op.S; n++) {
+        if (op.nflip[n] != 0) continue;
+        const double2 cf = apply_string(op, n, w.s, sp);
+        dr_ += cf.x;
+        di_ += cf.y;
+    }
+    double er = dr_, ei = di_;
+    {
+        const float2 c = make_float2(static_cast<float>(dr_ - e_shift.x), static_cast<float>(di_ - e_shift.y));
+        const int P = net.P - 2 * net.N;
+        for (int k = threadIdx.x; k < P; k += blockDim.x) erow[k] = cmul(c, orow[k]);
+    }
+    __syncthreads();
+    for (int n = 0; n < op.S; n++) {
+        if (op.nflip[n] == 0) continue;
+        const double2 cf = apply_string(op, n, w.s, sp);
+        const float2 lq = forward_once<float2, false, true>(net, sp, w);
+        const double dr = static_cast<double>(lq.x) - lp.x, di = static_cast<double>(lq.y) - lp.y;
+        const double m = exp(dr);
+        const double xr = m * cos(di), xi = m * sin(di);
+        const double e_r = cf.x * xr - cf.y * xi, e_i = cf.x * xi + cf.y * xr;
+        er += e_r;
+        ei += e_i;
+        const float2 e = make_float2(static_cast<float>(e_r), static_cast<float>(e_i));
+        backward<false>(net, sp, w, lq, [&](int k, float2 v) { erow[k] = cadd(erow[k], cmul(e, v)); });
+    }
+    if (threadIdx.x == 0) eloc[t] = make_double2(er, ei);
+}
+
+// out[k] += sum_s c[s] f(A[s][k]) over count samples, f = conj if conj_a
+__global__ void col_reduce_kernel(int count, int P, const double2* __restrict__ c, const float2* __restrict__ A,
+                                  long ld, int conj_a, double2* __restrict__ partial, int per_split) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const long s0 = static_cast<long>(blockIdx.y) * per_split;
+    const long s1 = min(static_cast<long>(count), s0 + per_split);
+    double2 acc = make_double2(0.0, 0.0);
+    if (k < P) {
+        float2 part = make_float2(0.f, 0.f);
+        int n = 0;
+        for (long s = s0; s < s1; s++) {
+            float2 a = A[s * ld + k];
+            if (conj_a) a.y = -a.y;
+            const double2 cc = c[s];
+            const float2 cf = make_float2(static_cast<float>(cc.x), static_cast<float>(cc.y));
+            part = cadd(part, cmul(cf, a));
+            if (++n == 32) {
+                acc.x += part.x;
+                acc.y += part.y;
+                part = make_float2(0.f, 0.f);
+                n = 0;
+            }
+        }
+        acc.x += part.x;
+        acc.y += part.y;
+        partial[static_cast<long>(blockIdx.y) * P + k] = acc;
+    }
+}
+
+__global__ void col_finish_kernel(int P, int splits, const double2* __restrict__ partial, double2* out) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= P) return;
+    double2 a = make_double2(0.0, 0.0);
+    for (int z = 0; z < splits; z++) {
+        a.x += partial[static_cast<long>(z) * P + k].x;
+        a.y += partial[static_cast<long>(z) * P + k].y;
+    }
+    out[k].x += a.x;
+    out[k].y += a.y;
+}
+
+// Metropolis for PsiDeep / PsiPair: one CTA per walker, full forward pass per proposal
+// (PsiDeep.hpp:191-194: angles are not updated incrementally).
+__global__ void deep_mc_kernel(DeepNetDev n0, DeepNetDev n1, int pair, McLaunch L) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    Work<float2> w = carve<float2>(smem, n0, false);
+    uint64_t* sp = w.s + kMaxWords;
+    uint64_t* shifted = sp + kMaxWords;
+    const int walker = blockIdx.x;
+    if (walker >= L.B) return;
+    const int N = n0.N, nw = (N + 63) / 64;
+    WalkerRng rng;
+    rng.init(L.seed, L.walker_base + static_cast<uint32_t>(walker), L.rng_index[walker]);
+    // every thread draws the same words, so all threads agree without a broadcast
+    uint64_t s[kMaxWords] = {0, 0, 0, 0};
+    if (L.init) {
+        for (int k = 0; k < nw; k++) {
+            const uint64_t lo = rng.next();
+            const uint64_t hi = rng.next();
+            s[k] = lo | (hi << 32);
+        }
+        if (N / 64 < nw) s[N / 64] &= (1ull << (N % 64)) - 1ull;
+    } else {
+        for (int k = 0; k < nw; k++) s[k] = L.spins[static_cast<long>(walker) * nw + k];
+    }
+    if (threadIdx.x < kMaxWords) w.s[threadIdx.x] = s[threadIdx.x];
+    __syncthreads();
+    float lpr = state_log_psi<float2>(n0, n1, pair, w.s, w, shifted).x;
+    unsigned long long acc = 0, props = 0;
+    const int total = L.n_therm + L.n_samples * L.sweeps_per_sample;
+    int sample = 0;
+    for (int sw = 0; sw < total; sw++) {
+        for (int p = 0; p < N; p++) {
+            const int site = static_cast<int>(rng.next() % static_cast<uint32_t>(N));
+            __syncthreads();
+            if (threadIdx.x < kMaxWords) {
+                uint64_t v = w.s[threadIdx.x];
+                if ((site >> 6) == static_cast<int>(threadIdx.x)) v ^= 1ull << (site & 63);
+                sp[threadIdx.x] = v;
+            }
+            __syncthreads();
+            const float nl = state_log_psi<float2>(n0, n1, pair, sp, w, shifted).x;
+            const float delta = nl - lpr;
+            bool accept = delta > 0.0f;
+            if (!accept) accept = rng.uniform() <= expf_det(2.0f * delta);
+            __syncthreads();
+            if (accept) {
+                if (threadIdx.x < kMaxWords) w.s[threadIdx.x] = sp[threadIdx.x];
+                lpr = nl;
+                acc++;
+            }
+            props++;
+            __syncthreads();
+        }
+        const int done = sw + 1 - L.n_therm;
+        if (done > 0 && done % L.sweeps_per_sample == 0) {
+            const long row = static_cast<long>(L.sample_base + sample) * L.B + walker;
+            if (L.sample_spins && threadIdx.x < nw) L.sample_spins[row * nw + threadIdx.x] = w.s[threadIdx.x];
+            sample++;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < nw) L.spins[static_cast<long>(walker) * nw + threadIdx.x] = w.s[threadIdx.x];
+    if (threadIdx.x == 0) {
+        L.rng_index[walker] = rng.index;
+        L.accepts[walker] += acc;
+        L.proposals[walker] += props;
+    }
+}
+
+int threads_for(const DeepNetDev& n) {
+    const int width = std::max(n.width, n.N);
+    return std::min(1024, std::max(32, (width + 31) / 32 * 32));
+}
+
+size_t smem_for(const DeepNetDev& n, size_t vbytes, bool store) {
+    return vbytes * (32 + 2 * n.width + (store ? 2 * n.units : 0)) + sizeof(uint64_t) * 4 * kMaxWords;
+}
+
+template <typename K>
+cudaError_t set_smem(K kernel, size_t bytes) {
+    if (bytes <= 48 * 1024) return cudaSuccess;
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- host side
+struct DeepHost {
+    std::vector<std::unique_ptr<DevBuf>> bufs;
+    DeepNetDev net[2];
+};
+
+static std::vector<std::unique_ptr<DeepHost>>& deep_registry() {
+    static std::vector<std::unique_ptr<DeepHost>> r;
+    return r;
+}
+
+template <typename T>
+static cudaError_t upload(DeepHost* h, const std::vector<T>& v, const T** out) {
+    auto b = std::make_unique<DevBuf>();
+    cudaError_t e = b->ensure(std::max<size_t>(16, sizeof(T) * v.size()));
+    if (e != cudaSuccess) return e;
+    if (!v.empty()) e = cudaMemcpy(b->p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice);
+    *out = static_cast<const T*>(b->p);
+    h->bufs.push_back(std::move(b));
+    return e;
+}
+
+// Device copy of the net(s): part 0 = complex net (PsiDeep) or real part (PsiPair), 1 = imaginary part.
+int deep_upload(rbmg_psi* psi) {
+    auto h = std::make_unique<DeepHost>();
+    const int nets = psi->kind == 2 ? 2 : 1;
+    const int L = static_cast<int>(psi->layers.size());
+    for (int part = 0; part < nets; part++) {
+        DeepNetDev& d = h->net[part];
+        d = DeepNetDev{};
+        d.N = psi->N;
+        d.L = L;
+        d.real_net = psi->kind == 2;
+        d.ti = psi->translational_invariance;
+        d.P = psi->num_params();
+        d.width = psi->width;
+        int k = 2 * psi->N, a = 0;
+        for (int l = 0; l < L; l++) {
+            const auto& Ly = psi->layers[l];
+            d.size[l] = Ly.size;
+            d.conn[l] = Ly.conn;
+            d.begin_params[l] = k - 2 * psi->N;
+            d.begin_angle[l] = a;
+            k += Ly.size + Ly.conn * Ly.size;
+            a += Ly.size;
+            auto pick = [&](const cplx& z) -> cplx {
+                if (psi->kind != 2) return z;
+                return part == 0 ? cplx(z.real(), 0.0) : cplx(z.imag(), 0.0);
+            };
+            std::vector<float2> w32(Ly.weights.size()), b32(Ly.biases.size());
+            std::vector<double2> w64(Ly.weights.size()), b64(Ly.biases.size());
+            for (size_t q = 0; q < Ly.weights.size(); q++) {
+                const cplx z = pick(Ly.weights[q]);
+                w32[q] = make_float2(float(z.real()), float(z.imag()));
+                w64[q] = make_double2(z.real(), z.imag());
+            }
+            for (size_t q = 0; q < Ly.biases.size(); q++) {
+                const cplx z = pick(Ly.biases[q]);
+                b32[q] = make_float2(float(z.real()), float(z.imag()));
+                b64[q] = make_double2(z.real(), z.imag());
+            }
+            std::vector<int> ci(Ly.connections.begin(), Ly.connections.end());
+            RBMG_CK(upload(h.get(), w32, &d.w[l]));
+            RBMG_CK(upload(h.get(), b32, &d.b[l]));
+            RBMG_CK(upload(h.get(), w64, &d.w64[l]));
+            RBMG_CK(upload(h.get(), b64, &d.b64[l]));
+            RBMG_CK(upload(h.get(), ci, &d.cidx[l]));
+        }
+        d.units = a;
+        // rhs lists of layer l from the lhs connections of layer l+1, in the order of
+        // source/quantum_state/PsiDeep.cu:101-111 (next unit j ascending, connection c inner)
+        for (int l = 0; l + 1 < L; l++) {
+            const auto& Nx = psi->layers[l + 1];
+            const int size = psi->layers[l].size;
+            std::vector<std::vector<int>> lists(size);
+            for (int j = 0; j < Nx.size; j++)
+                for (int c = 0; c < Nx.conn; c++) lists[Nx.connections[c * Nx.size + j]].push_back(c * Nx.size + j);
+            std::vector<int> ptr(size + 1, 0), q;
+            for (int i = 0; i < size; i++) {
+                ptr[i] = static_cast<int>(q.size());
+                q.insert(q.end(), lists[i].begin(), lists[i].end());
+            }
+            ptr[size] = static_cast<int>(q.size());
+            RBMG_CK(upload(h.get(), ptr, &d.rptr[l]));
+            RBMG_CK(upload(h.get(), q, &d.rq[l]));
+        }
+        std::vector<float2> f32(psi->final_weights.size());
+        std::vector<double2> f64(psi->final_weights.size());
+        for (size_t q = 0; q < f32.size(); q++) {
+            const cplx z = psi->kind != 2 ? psi->final_weights[q]
+                                          : (part == 0 ? cplx(psi->final_weights[q].real(), 0.0)
+                                                       : cplx(psi->final_weights[q].imag(), 0.0));
+            f32[q] = make_float2(float(z.real()), float(z.imag()));
+            f64[q] = make_double2(z.real(), z.imag());
+        }
+        RBMG_CK(upload(h.get(), f32, &d.fw));
+        RBMG_CK(upload(h.get(), f64, &d.fw64));
+    }
+    if (nets == 1) h->net[1] = h->net[0];
+    psi->deep_dev[0] = h->net[0];
+    psi->deep_dev[1] = h->net[1];
+    psi->deep_host = std::shared_ptr<void>(h.release(), [](void* p) { delete static_cast<DeepHost*>(p); });
+    return RBMG_OK;
+}
+
+static DeepNetDev net_of(const rbmg_psi* psi, int part) {
+    DeepNetDev d = psi->deep_dev[part];
+    d.ti = psi->translational_invariance;
+    return d;
+}
+
+int deep_log_psi(const rbmg_psi* psi, int count, const uint64_t* d_spins, uint64_t enum_base, int enumerate,
+                 double2* d_out, cudaStream_t st) {
+    if (count <= 0) return RBMG_OK;
+    const DeepNetDev n0 = net_of(psi, 0), n1 = net_of(psi, 1);
+    const size_t sm = smem_for(n0, sizeof(float2), false);
+    RBMG_CK(set_smem(deep_logpsi_kernel<float2>, sm));
+    deep_logpsi_kernel<float2><<<count, threads_for(n0), sm, st>>>(n0, n1, psi->kind == 2, count, d_spins, enum_base,
+                                                                   enumerate, d_out);
+    RBMG_CK(cudaGetLastError());
+    return RBMG_OK;
+}
+
+int deep_eloc_chunk(const rbmg_psi* psi, const rbmg_operator* op, const Chunk& c, double2* d_eloc, cudaStream_t st) {
+    if (c.count <= 0) return RBMG_OK;
+    const DeepNetDev n0 = net_of(psi, 0), n1 = net_of(psi, 1);
+    const size_t sm = smem_for(n0, sizeof(float2), false);
+    RBMG_CK(set_smem(deep_eloc_kernel<float2, false>, sm));
+    deep_eloc_kernel<float2, false><<<c.count, threads_for(n0), sm, st>>>(n0, n1, psi->kind == 2, n0, n1, op->dev(),
+                                                                         c.count, c.spins, c.enum_base, c.enumerate,
+                                                                         d_eloc, nullptr);
+    RBMG_CK(cudaGetLastError());
+    return RBMG_OK;
+}
+
+int deep_hsd64_chunk(const rbmg_psi* psi, const rbmg_psi* pp, const rbmg_operator* op, const Chunk& c,
+                     double2* d_eloc, double2* d_dlp, cudaStream_t st) {
+    if (c.count <= 0) return RBMG_OK;
+    if (pp->width != psi->width || pp->layers.size() != psi->layers.size())
+        return fail(RBMG_EUNSUPPORTED, "hsd: psi and psi_prime need the same layer shapes");
+    const DeepNetDev n0 = net_of(psi, 0), n1 = net_of(psi, 1), q0 = net_of(pp, 0), q1 = net_of(pp, 1);
+    const size_t sm = smem_for(n0, sizeof(double2), false) + 2 * sizeof(uint64_t) * kMaxWords;
+    RBMG_CK(set_smem(deep_eloc_kernel<double2, true>, sm));
+    deep_eloc_kernel<double2, true><<<c.count, threads_for(n0), sm, st>>>(n0, n1, psi->kind == 2, q0, q1, op->dev(),
+                                                                         c.count, c.spins, c.enum_base, c.enumerate,
+                                                                         d_eloc, d_dlp);
+    RBMG_CK(cudaGetLastError());
+    return RBMG_OK;
+}
+
+static DevBuf& rows_buf(int which) {
+    static thread_local DevBuf b[3];
+    return b[which];
+}
+
+static int col_reduce(int count, int P, const double2* c, const float2* A, long ld, int conj_a, double2* out,
+                      cudaStream_t st) {
+    if (count <= 0) return RBMG_OK;
+    const int per_split = std::max(64, (count + 63) / 64);
+    const int splits = (count + per_split - 1) / per_split;
+    DevBuf& part = rows_buf(2);
+    RBMG_CK(part.ensure(sizeof(double2) * static_cast<size_t>(splits) * P));
+    const dim3 grid((P + 255) / 256, splits);
+    col_reduce_kernel<<<grid, 256, 0, st>>>(count, P, c, A, ld, conj_a, part.as<double2>(), per_split);
+    col_finish_kernel<<<(P + 255) / 256, 256, 0, st>>>(P, splits, part.as<double2>(), out);
+    RBMG_CK(cudaGetLastError());
+    return RBMG_OK;
+}
+
+int deep_hsd_okreduce(const rbmg_psi* pp, int pair_part, int count, const uint64_t* d_spins, uint64_t enum_base,
+                      int enumerate, const double2* d_coef, double2* acc, cudaStream_t st) {
+    const DeepNetDev net = net_of(pp, pair_part == 1 ? 1 : 0);
+    const int P = net.P - 2 * net.N;
+    const int chunk = std::max(1, static_cast<int>((size_t(256) << 20) / (sizeof(float2) * P)));
+    DevBuf& rows = rows_buf(0);
+    RBMG_CK(rows.ensure(sizeof(float2) * static_cast<size_t>(std::min(chunk, count)) * P));
+    const size_t sm = smem_for(net, sizeof(float2), true);
+    for (int base = 0; base < count; base += chunk) {
+        const int cnt = std::min(chunk, count - base);
+        const uint64_t* sp = d_spins ? d_spins + static_cast<size_t>(base) * ((net.N + 63) / 64) : nullptr;
+        if (pp->kind == 2) {
+            RBMG_CK(set_smem(deep_ok_kernel<true>, sm));
+            deep_ok_kernel<true><<<cnt, threads_for(net), sm, st>>>(net, cnt, sp, enum_base + base, enumerate,
+                                                                    rows.as<float2>(), P);
+        } else {
+            RBMG_CK(set_smem(deep_ok_kernel<false>, sm));
+            deep_ok_kernel<false><<<cnt, threads_for(net), sm, st>>>(net, cnt, sp, enum_base + base, enumerate,
+                                                                     rows.as<float2>(), P);
+        }
+        RBMG_CK(cudaGetLastError());
+        // real O_k (PsiPair) multiply the real or complex coefficient; complex O_k enter conjugated
+        const int r = col_reduce(cnt, P, d_coef + base, rows.as<float2>(), P, pp->kind == 2 ? 0 : 1, acc, st);
+        if (r != RBMG_OK) return r;
+    }
+    return RBMG_OK;
+}
+
+int deep_ok_vector(const rbmg_psi* psi, const uint64_t* d_spins, double2* d_out, cudaStream_t st) {
+    if (psi->kind == 2) return fail(RBMG_EUNSUPPORTED, "psi_O_k_vector: not defined for PsiPair (PsiPair.hpp:73-76)");
+    const DeepNetDev net = net_of(psi, 0);
+    const int P = net.P - 2 * net.N;
+    DevBuf& rows = rows_buf(0);
+    RBMG_CK(rows.ensure(sizeof(float2) * P));
+    const size_t sm = smem_for(net, sizeof(float2), true);
+    RBMG_CK(set_smem(deep_ok_kernel<false>, sm));
+    deep_ok_kernel<false><<<1, threads_for(net), sm, st>>>(net, 1, d_spins, 0, 0, rows.as<float2>(), P);
+    RBMG_CK(cudaGetLastError());
+    RBMG_CK(cudaMemsetAsync(d_out, 0, sizeof(double2) * P, st));
+    DevBuf& one = rows_buf(1);
+    RBMG_CK(one.ensure(sizeof(double2)));
+    const double2 h1 = make_double2(1.0, 0.0);
+    RBMG_CK(cudaMemcpyAsync(one.p, &h1, sizeof(double2), cudaMemcpyHostToDevice, st));
+    return col_reduce(1, P, one.as<double2>(), rows.as<float2>(), P, 0, d_out, st);
+}
+
+int deep_gradient_chunk(const rbmg_psi* psi, const rbmg_operator* op, const Chunk& c, double2 e_shift,
+                        double2* d_eloc, double2* acc_O, double2* acc_EO, double2* acc_Ek, double2* coef1,
+                        double2* coef2, cudaStream_t st) {
+    if (psi->kind == 2) return fail(RBMG_EUNSUPPORTED, "gradient: not instantiated for PsiPair (ExpectationValue.cu:553)");
+    const DeepNetDev net = net_of(psi, 0);
+    const int P = net.P - 2 * net.N;
+    const int chunk = std::max(1, static_cast<int>((size_t(384) << 20) / (2 * sizeof(float2) * P)));
+    DevBuf& orows = rows_buf(0);
+    DevBuf& erows = rows_buf(1);
+    RBMG_CK(orows.ensure(sizeof(float2) * static_cast<size_t>(std::min(chunk, c.count)) * P));
+    RBMG_CK(erows.ensure(sizeof(float2) * static_cast<size_t>(std::min(chunk, c.count)) * P));
+    const size_t sm = smem_for(net, sizeof(float2), true) + sizeof(uint64_t) * kMaxWords;
+    RBMG_CK(set_smem(deep_grad_kernel, sm));
+    RBMG_CK(launch_coef(c.count, c.weights, nullptr, 1.0, coef1, st));
+    for (int base = 0; base < c.count; base += chunk) {
+        const int cnt = std::min(chunk, c.count - base);
+        const uint64_t* sp = c.spins ? c.spins + static_cast<size_t>(base) * ((net.N + 63) / 64) : nullptr;
+        deep_grad_kernel<<<cnt, threads_for(net), sm, st>>>(net, op->dev(), cnt, sp, c.enum_base + base, c.enumerate,
+                                                            e_shift, d_eloc + base, orows.as<float2>(),
+                                                            erows.as<float2>(), P);
+        RBMG_CK(cudaGetLastError());
+        RBMG_CK(launch_coef(cnt, c.weights ? c.weights + base : nullptr, d_eloc + base, 1.0, coef2 + base, st,
+                            e_shift));
+        int r = col_reduce(cnt, P, coef1 + base, orows.as<float2>(), P, 0, acc_O, st);
+        if (r == RBMG_OK) r = col_reduce(cnt, P, coef2 + base, orows.as<float2>(), P, 1, acc_EO, st);
+        if (r == RBMG_OK) r = col_reduce(cnt, P, coef1 + base, erows.as<float2>(), P, 0, acc_Ek, st);
+        if (r != RBMG_OK) return r;
+    }
+    return RBMG_OK;
+}
+
+// MonteCarloLoop::foreach for PsiDeep / PsiPair (MonteCarloLoop.hpp:294-339)
+int deep_stream(rbmg_ensemble* e, const rbmg_psi* psi, const rbmg_operator* op, bool want_eloc,
+                size_t max_chunk_samples, const std::function<int(const Chunk&)>& fn) {
+    (void)op;
+    (void)want_eloc;
+    if (e->fast_sweep_tries || e->total_z)
+        return fail(RBMG_EUNSUPPORTED, "PsiDeep chains: fast sweep / S_z symmetry are not provided");
+    const int nw = (psi->N + 63) / 64;
+    const int B = static_cast<int>(e->num_chains);
+    const int steps = static_cast<int>(e->num_samples / e->num_chains);
+    RBMG_CK(e->spins.ensure(sizeof(uint64_t) * nw * B));
+    RBMG_CK(cudaMemsetAsync(e->accepts.p, 0, sizeof(unsigned long long) * B, stream()));
+    RBMG_CK(cudaMemsetAsync(e->proposals.p, 0, sizeof(unsigned long long) * B, stream()));
+    static thread_local DevBuf samples;
+    const int rows_per_chunk = static_cast<int>(std::max<size_t>(1, std::min<size_t>(steps, max_chunk_samples / B)));
+    RBMG_CK(samples.ensure(sizeof(uint64_t) * nw * B * rows_per_chunk));
+    const DeepNetDev n0 = net_of(psi, 0), n1 = net_of(psi, 1);
+    const size_t sm = smem_for(n0, sizeof(float2), false);
+    RBMG_CK(set_smem(deep_mc_kernel, sm));
+    bool first = true;
+    for (int row0 = 0; row0 < steps; row0 += rows_per_chunk) {
+        const int rows = std::min(rows_per_chunk, steps - row0);
+        McLaunch L{};
+        L.B = B;
+        L.seed = e->seed;
+        L.spins = e->spins.as<uint64_t>();
+        L.rng_index = e->rng_index.as<uint64_t>();
+        L.init = first ? 1 : 0;
+        L.n_therm = first ? static_cast<int>(e->num_therm) : 0;
+        L.n_samples = rows;
+        L.sweeps_per_sample = static_cast<int>(e->num_sweeps);
+        L.sample_spins = samples.as<uint64_t>();
+        L.accepts = e->accepts.as<unsigned long long>();
+        L.proposals = e->proposals.as<unsigned long long>();
+        deep_mc_kernel<<<B, threads_for(n0), sm, stream()>>>(n0, n1, psi->kind == 2, L);
+        RBMG_CK(cudaGetLastError());
+        first = false;
+        Chunk c;
+        c.count = rows * B;
+        c.spins = samples.as<uint64_t>();
+        const int r = fn(c);
+        if (r != RBMG_OK) return r;
+    }
+    std::vector<unsigned long long> a(B), p(B);
+    RBMG_CK(cudaMemcpyAsync(a.data(), e->accepts.p, sizeof(unsigned long long) * B, cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaMemcpyAsync(p.data(), e->proposals.p, sizeof(unsigned long long) * B, cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaStreamSynchronize(stream()));
+    e->last_accepts.assign(a.begin(), a.end());
+    e->last_proposals.assign(p.begin(), p.end());
+    return RBMG_OK;
+}
+
+}  // namespace rbmg

@@ -1,0 +1,137 @@
+// Host-side objects behind the C ABI handles, shared by capi.cu and deep.cu.
+#pragma once
+
+#include <complex>
+#include <cstdint>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/rbmg.h"
+#include "kernels.h"
+
+namespace rbmg {
+
+using cplx = std::complex<double>;
+
+void set_error(const std::string& msg);
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* where);
+
+#define RBMG_CK(call)                                                    \
+    do {                                                                 \
+        cudaError_t e__ = (call);                                        \
+        if (e__ != cudaSuccess) return ::rbmg::cuda_fail(e__, #call);    \
+    } while (0)
+
+// grow-only device buffer
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    cudaError_t ensure(size_t n) {
+        if (n <= bytes) return cudaSuccess;
+        release();
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e != cudaSuccess) { p = nullptr; return e; }
+        bytes = n;
+        return cudaSuccess;
+    }
+    template <typename T>
+    T* as() const { return static_cast<T*>(p); }
+};
+
+cudaStream_t stream();
+
+struct DeepLayerHost {
+    int size = 0, conn = 0;
+    std::vector<uint32_t> connections;   // [conn][size]
+    std::vector<cplx> biases;            // [size]
+    std::vector<cplx> weights;           // [conn][size]
+};
+
+struct DeepDev;   // deep.cu
+
+}  // namespace rbmg
+
+struct rbmg_psi {
+    int kind = 0;     // 0 RBM, 1 PsiDeep, 2 PsiPair
+    int N = 0;
+    double prefactor = 1.0;
+    std::vector<double> alpha, beta;
+    // RBM
+    int M = 0, Mpad = 0;
+    std::vector<rbmg::cplx> b, W;
+    rbmg::DevBuf dW, db;
+    mutable rbmg::DevBuf dW64, db64;   // FP64 copies for the Hilbert-space distance pass, uploaded on use
+    mutable bool f64_valid = false;
+    // deep / pair
+    std::vector<rbmg::DeepLayerHost> layers;
+    std::vector<rbmg::cplx> final_weights;
+    int translational_invariance = 0;
+    rbmg::DeepNetDev deep_dev[2] = {};     // device nets (deep.cu): complex net, or PsiPair real / imaginary
+    std::shared_ptr<void> deep_host;       // owner of the device buffers behind deep_dev
+    int width = 0;
+
+    int num_params() const;
+    rbmg::RbmDev rbm_dev() const {
+        return rbmg::RbmDev{N, M, Mpad, static_cast<const float2*>(dW.p), static_cast<const float2*>(db.p)};
+    }
+};
+
+struct rbmg_operator {
+    int S = 0, L = 0;
+    std::vector<rbmg::cplx> coef;
+    std::vector<int> types, idx;
+    // compact form
+    std::vector<int> ypow, nflip, flip_off, flip_sites, offdiag_slot;
+    std::vector<uint64_t> zmask;
+    int num_offdiag = 0;
+    int max_site = -1;
+    rbmg::DevBuf d_coef, d_ypow, d_zmask, d_nflip, d_flip_off, d_flip_sites, d_slot;
+    // per-site CSR of the off-diagonal slots whose string flips the site (E_k term)
+    std::vector<int> site_ptr, site_slots;
+    rbmg::DevBuf d_site_ptr, d_site_slots;
+    int site_ptr_N = -1;
+    rbmg::OpDev dev() const {
+        return rbmg::OpDev{S,
+                           d_coef.as<double2>(),
+                           d_ypow.as<int>(),
+                           d_zmask.as<uint64_t>(),
+                           d_nflip.as<int>(),
+                           d_flip_off.as<int>(),
+                           d_flip_sites.as<int>(),
+                           d_slot.as<int>(),
+                           num_offdiag};
+    }
+};
+
+struct rbmg_ensemble {
+    int kind = 0;   // 0 MonteCarloLoop, 1 ExactSummation
+    // MonteCarloLoop
+    uint32_t num_samples = 0, num_sweeps = 1, num_therm = 0, num_chains = 1;
+    uint64_t seed = 0;
+    int total_z = 0, sector = 0;
+    uint32_t fast_sweep_tries = 0;
+    rbmg::DevBuf spins, rng_index, accepts, proposals;
+    int spins_words = 0;
+    std::vector<uint64_t> last_accepts, last_proposals;
+    // ExactSummation
+    uint32_t num_spins = 0;
+    int exact_total_z = 0;
+    std::vector<uint64_t> allowed;          // sector configurations
+    rbmg::DevBuf d_allowed;
+
+    uint64_t num_steps() const;
+};

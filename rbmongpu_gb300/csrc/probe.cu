@@ -1,0 +1,54 @@
+// FP32 FMA throughput probe: the denominator of the sampler's roofline (the sampler
+// is bound by the FP32 pipe, whose peak the driver's measured-peaks file does not list).
+#include <cuda_runtime.h>
+
+#include "host.h"
+
+namespace rbmg {
+namespace {
+
+__global__ void fma_probe_kernel(float* out, int iters, float a, float b) {
+    float x0 = threadIdx.x * 1e-7f, x1 = x0 + 1.f, x2 = x0 + 2.f, x3 = x0 + 3.f;
+    float x4 = x0 + 4.f, x5 = x0 + 5.f, x6 = x0 + 6.f, x7 = x0 + 7.f;
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int u = 0; u < 16; u++) {
+            x0 = fmaf(x0, a, b); x1 = fmaf(x1, a, b); x2 = fmaf(x2, a, b); x3 = fmaf(x3, a, b);
+            x4 = fmaf(x4, a, b); x5 = fmaf(x5, a, b); x6 = fmaf(x6, a, b); x7 = fmaf(x7, a, b);
+        }
+    }
+    const float s = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
+    if (s == 123.456f) out[threadIdx.x] = s;   // keeps the chains alive, never true in practice
+}
+
+}  // namespace
+}  // namespace rbmg
+
+using namespace rbmg;
+
+extern "C" int rbmg_probe_fp32_tflops(int iters, double* tflops) {
+    if (!tflops || iters <= 0) return fail(RBMG_EINVAL, "probe: bad arguments");
+    int dev = 0, sms = 0;
+    RBMG_CK(cudaGetDevice(&dev));
+    RBMG_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    float* out = nullptr;
+    RBMG_CK(cudaMalloc(&out, 1024 * sizeof(float)));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int blocks = sms * 8, threads = 256;
+    fma_probe_kernel<<<blocks, threads, 0, stream()>>>(out, iters / 4, 0.9999f, 1e-4f);   // warm-up
+    cudaEventRecord(e0, stream());
+    fma_probe_kernel<<<blocks, threads, 0, stream()>>>(out, iters, 0.9999f, 1e-4f);
+    cudaEventRecord(e1, stream());
+    cudaError_t err = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    if (err != cudaSuccess) return cuda_fail(err, "probe");
+    const double flops = 2.0 * 8 * 16 * static_cast<double>(iters) * blocks * threads;
+    *tflops = flops / (ms * 1e-3) / 1e12;
+    return RBMG_OK;
+}

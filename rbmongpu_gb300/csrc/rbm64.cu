@@ -1,0 +1,215 @@
+// FP64 per-sample pass for the Hilbert-space distance of complex RBMs.
+//
+// The distance between nearby states is a difference of nearly equal averages
+// (d^2 = 1 - |<omega>|^2 / (<norm><ratio>) is ~1e-6 for the perturbed copies the
+// reference tests), so the per-sample terms omega_s = exp(conj(log psi'_s - log psi_s)) E_s
+// and ratio_s are computed here in FP64, from FP64 copies of the parameters,
+// with log psi' - log psi summed angle by angle as differences.  One warp per sample,
+// angles and activations of the warp's sample in shared memory.
+#include <cuda_runtime.h>
+
+#include "kernels.h"
+#include "rbm64.h"
+
+namespace rbmg {
+
+namespace {
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// include/quantum_state/psi_functions.hpp:49-57 in FP64
+__device__ __forceinline__ double2 lc64(double2 z) {
+    const double s = z.x > 0.0 ? 1.0 : -1.0;
+    double2 t = make_double2(s * 3.746646023906276 + z.x, z.y);
+    t = cmul(z, t);
+    t.x += 7.771429504240965;
+    t = cmul(z, t);
+    t.x += s * 10.2180213465;
+    t = cmul(z, t);
+    t.x += 9.19376335670885;
+    const double2 num = make_double2(5.49914721954 - s * 2.16564366435 * z.x, -s * 2.16564366435 * z.y);
+    const double den = t.x * t.x + t.y * t.y;
+    const double qr = (num.x * t.x + num.y * t.y) / den, qi = (num.y * t.x - num.x * t.y) / den;
+    return make_double2(s * 0.9003320053750442 * z.x + qr - 0.598139, s * 0.9003320053750442 * z.y + qi);
+}
+
+__device__ __forceinline__ double2 warp_sum64(double2 v) {
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, off);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, off);
+    }
+    return v;
+}
+
+__device__ __forceinline__ bool spin_up(const uint64_t* s, int i) { return (s[i >> 6] >> (i & 63)) & 1ull; }
+
+// shared memory per warp: theta[M], f[M] (double2 each)
+__global__ void rbm_hsd64_kernel(Rbm64 P, Rbm64 PP, OpDev op, Hsd64Launch L) {
+    extern __shared__ double2 smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const long t = static_cast<long>(blockIdx.x) * kWarpsPerBlock + warp;
+    if (t >= L.count) return;
+    const int M = P.M, N = P.N;
+    double2* th = smem + static_cast<long>(warp) * 2 * M;
+    double2* f = th + M;
+    uint64_t s[kMaxWords] = {0, 0, 0, 0};
+    const int nw = (N + 63) / 64;
+    if (L.enumerate) {
+        const uint64_t idx = L.enum_base + static_cast<uint64_t>(t);
+        s[0] = N >= 64 ? idx : (idx & ((1ull << N) - 1ull));
+    } else {
+        for (int k = 0; k < nw; k++) s[k] = L.spins[t * nw + k];
+    }
+    double2 lp = make_double2(0.0, 0.0);
+    for (int j = lane; j < M; j += 32) {
+        double2 a = P.b[j];
+        for (int i = 0; i < N; i++) {
+            const double2 w = P.W[static_cast<long>(i) * M + j];
+            if (spin_up(s, i)) { a.x += w.x; a.y += w.y; }
+            else { a.x -= w.x; a.y -= w.y; }
+        }
+        th[j] = a;
+        f[j] = lc64(a);
+        lp.x += f[j].x;
+        lp.y += f[j].y;
+    }
+    lp = warp_sum64(lp);
+    __syncwarp();
+    // local energy (include/operator/Operator.hpp:90-115) with per-angle differences
+    double er = 0.0, ei = 0.0;
+    for (int n = 0; n < op.S; n++) {
+        int parity = 0;
+        for (int k = 0; k < nw; k++) parity += __popcll(op.zmask[n * kMaxWords + k] & ~s[k]);
+        const double sg = (parity & 1) ? -1.0 : 1.0;
+        const double2 c0 = op.coef[n];
+        const int yp = op.ypow[n] & 3;
+        double2 cf = yp == 0 ? c0 : (yp == 1 ? make_double2(c0.y, -c0.x) : (yp == 2 ? make_double2(-c0.x, -c0.y)
+                                                                                  : make_double2(-c0.y, c0.x)));
+        cf.x *= sg;
+        cf.y *= sg;
+        const int nf = op.nflip[n];
+        if (nf == 0) {
+            er += cf.x;
+            ei += cf.y;
+            continue;
+        }
+        const int off = op.flip_off[n];
+        double2 d = make_double2(0.0, 0.0);
+        for (int j = lane; j < M; j += 32) {
+            double2 a = th[j];
+            for (int q = 0; q < nf; q++) {
+                const int site = op.flip_sites[off + q];
+                const double2 w = P.W[static_cast<long>(site) * M + j];
+                const double two_s = spin_up(s, site) ? -2.0 : 2.0;
+                a.x += two_s * w.x;
+                a.y += two_s * w.y;
+            }
+            const double2 g = lc64(a);
+            d.x += g.x - f[j].x;
+            d.y += g.y - f[j].y;
+        }
+        d = warp_sum64(d);
+        const double m = exp(d.x);
+        const double2 x = make_double2(m * cos(d.y), m * sin(d.y));
+        er += cf.x * x.x - cf.y * x.y;
+        ei += cf.x * x.y + cf.y * x.x;
+    }
+    // log psi'(s) - log psi(s), angle by angle
+    double2 dl = make_double2(0.0, 0.0);
+    for (int j = lane; j < M; j += 32) {
+        double2 a = PP.b[j];
+        for (int i = 0; i < N; i++) {
+            const double2 w = PP.W[static_cast<long>(i) * M + j];
+            if (spin_up(s, i)) { a.x += w.x; a.y += w.y; }
+            else { a.x -= w.x; a.y -= w.y; }
+        }
+        const double2 g = lc64(a);
+        dl.x += g.x - f[j].x;
+        dl.y += g.y - f[j].y;
+    }
+    dl = warp_sum64(dl);
+    if (lane == 0) {
+        if (L.eloc) L.eloc[t] = make_double2(er, ei);
+        if (L.logpsi) L.logpsi[t] = lp;
+        L.dlogpsi[t] = dl;
+    }
+}
+
+__global__ void hsd_terms64_kernel(int count, const double2* __restrict__ eloc, const double2* __restrict__ dl,
+                                   int is_unitary, double2* omega, double2* pr, double2* nn) {
+    for (long s = blockIdx.x * 256L + threadIdx.x; s < count; s += static_cast<long>(gridDim.x) * 256) {
+        const double2 e = eloc[s];
+        const double dr = dl[s].x, di = -dl[s].y;   // conj(log psi' - log psi)
+        double2 om;
+        double n;
+        if (is_unitary) {   // source/network_functions/HilbertSpaceDistance.cu:88-94
+            const double m = exp(dr);
+            const double ar = m * cos(di), ai = m * sin(di);
+            om = make_double2(ar * e.x - ai * e.y, ar * e.y + ai * e.x);
+            n = e.x * e.x + e.y * e.y;
+        } else {            // :95-101
+            const double m = exp(e.x + dr);
+            om = make_double2(m * cos(e.y + di), m * sin(e.y + di));
+            n = exp(2.0 * e.x);
+        }
+        omega[s] = om;
+        pr[s] = make_double2(exp(2.0 * dl[s].x), 0.0);   // :102
+        nn[s] = make_double2(n, 0.0);
+    }
+}
+
+// per-sample gradient coefficients w_s * B_s (see capi.cu, rbmg_hsd_gradient)
+__global__ void hsd_coef_kernel(int count, const double* __restrict__ w, const double2* __restrict__ omega,
+                                const double2* __restrict__ pr, double2 conj_omega_bar, double v, double u,
+                                double nn_bar, int mode, double2* c) {
+    for (long s = blockIdx.x * 256L + threadIdx.x; s < count; s += static_cast<long>(gridDim.x) * 256) {
+        const double ws = w ? w[s] : 1.0;
+        const double2 om = omega[s];
+        const double2 a = cmul(conj_omega_bar, om);
+        double2 r;
+        if (mode == 2) {
+            r = make_double2(a.y, 0.0);                                  // Im(conj(<omega>) omega_s)
+        } else {
+            r = make_double2(a.x * v - u * nn_bar * pr[s].x, a.y * v);   // B_s
+            if (mode == 1) r.y = 0.0;                                     // Re B_s
+        }
+        c[s] = make_double2(ws * r.x, ws * r.y);
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_rbm_hsd64(const Rbm64& P, const Rbm64& PP, const OpDev& op, const Hsd64Launch& L,
+                             cudaStream_t st) {
+    if (L.count <= 0) return cudaSuccess;
+    const size_t smem = sizeof(double2) * 2 * P.M * kWarpsPerBlock;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(rbm_hsd64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             static_cast<int>(smem));
+        if (e != cudaSuccess) return e;
+    }
+    rbm_hsd64_kernel<<<(L.count + kWarpsPerBlock - 1) / kWarpsPerBlock, 32 * kWarpsPerBlock, smem, st>>>(P, PP, op, L);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_hsd_terms64(int count, const double2* eloc, const double2* dl, int is_unitary, double2* omega,
+                               double2* pr, double2* nn, cudaStream_t st) {
+    if (count <= 0) return cudaSuccess;
+    hsd_terms64_kernel<<<static_cast<int>(std::min(1024L, (count + 255L) / 256)), 256, 0, st>>>(
+        count, eloc, dl, is_unitary, omega, pr, nn);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_hsd_coef(int count, const double* w, const double2* omega, const double2* pr,
+                            double2 conj_omega_bar, double v, double u, double nn_bar, int mode, double2* c,
+                            cudaStream_t st) {
+    if (count <= 0) return cudaSuccess;
+    hsd_coef_kernel<<<static_cast<int>(std::min(1024L, (count + 255L) / 256)), 256, 0, st>>>(
+        count, w, omega, pr, conj_omega_bar, v, u, nn_bar, mode, c);
+    return cudaGetLastError();
+}
+
+}  // namespace rbmg

@@ -1,0 +1,37 @@
+// FP64 per-sample pass of the Hilbert-space distance (rbm64.cu).
+#pragma once
+
+#include <algorithm>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "kernels.h"
+
+namespace rbmg {
+
+struct Rbm64 {
+    int N, M;
+    const double2* W;   // [N][M]
+    const double2* b;   // [M]
+};
+
+struct Hsd64Launch {
+    int count;
+    uint64_t enum_base;
+    int enumerate;
+    const uint64_t* spins;
+    double2* eloc;      // [count] local energy of the operator under psi, or null
+    double2* logpsi;    // [count] log psi, or null
+    double2* dlogpsi;   // [count] log psi' - log psi
+};
+
+cudaError_t launch_rbm_hsd64(const Rbm64& P, const Rbm64& PP, const OpDev& op, const Hsd64Launch& L,
+                             cudaStream_t st);
+cudaError_t launch_hsd_terms64(int count, const double2* eloc, const double2* dl, int is_unitary, double2* omega,
+                               double2* pr, double2* nn, cudaStream_t st);
+// mode 0: w B_s, mode 1: w Re B_s, mode 2: w Im(conj(<omega>) omega_s)
+cudaError_t launch_hsd_coef(int count, const double* w, const double2* omega, const double2* pr,
+                            double2 conj_omega_bar, double v, double u, double nn_bar, int mode, double2* c,
+                            cudaStream_t st);
+
+}  // namespace rbmg

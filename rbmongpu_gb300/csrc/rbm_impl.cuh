@@ -1,0 +1,399 @@
+// Complex-RBM kernels: Metropolis sampler and per-sample estimator pass.
+//
+// Layout: one warp per walker (or per configuration).  Lane l owns hidden units
+// j = l + 32 k, k < K, and keeps their angles theta_j and Re f(theta_j) in
+// registers for the whole chain; W rows are read coalesced (one float2 per lane
+// per k) from global memory through L1/L2.  This file is included by the rbm_k*.cu
+// translation units, each instantiating one K.
+#pragma once
+
+#include "device_math.cuh"
+#include "kernels.h"
+
+namespace rbmg {
+
+// angles from scratch: theta_j = b_j, then theta_j +/-= W_ij for i = 0..N-1 in order
+// (include/quantum_state/Psi.hpp:43-53)
+template <int K, int NW>
+__device__ __forceinline__ void rbm_refresh(const RbmDev& P, const Spins<NW>& s, float (&tr)[K], float (&ti)[K],
+                                            int lane) {
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        const float2 b = __ldg(P.b + lane + 32 * k);
+        tr[k] = b.x;
+        ti[k] = b.y;
+    }
+    const float2* row = P.W + lane;
+    for (int i = 0; i < P.N; i++, row += P.Mpad) {
+        const float sg = s.up(i) ? 1.0f : -1.0f;
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const float2 w = __ldg(row + 32 * k);
+            tr[k] = __fadd_rn(tr[k], sg * w.x);
+            ti[k] = __fadd_rn(ti[k], sg * w.y);
+        }
+    }
+}
+
+template <int NW>
+__device__ __forceinline__ void draw_spins(WalkerRng& rng, int N, Spins<NW>& s) {
+#pragma unroll
+    for (int k = 0; k < NW; k++) {
+        const uint64_t lo = rng.next();
+        const uint64_t hi = rng.next();
+        s.w[k] = lo | (hi << 32);
+    }
+    if (N / 64 < NW) s.w[N / 64] &= (1ull << (N % 64)) - 1ull;
+}
+
+// include/random.h:60-79 with 64-bit masks (single word, N <= 64)
+__device__ __forceinline__ uint64_t draw_n_over_k(WalkerRng& rng, unsigned n, unsigned k) {
+    const uint64_t mask = n >= 64 ? ~0ull : ((1ull << n) - 1ull);
+    uint64_t w = rng.next();
+    w |= static_cast<uint64_t>(rng.next()) << 32;
+    uint64_t result = w & mask;
+    int diff = static_cast<int>(k) - __popcll(result);
+    while (diff != 0) {
+        uint64_t w2 = rng.next();
+        w2 |= static_cast<uint64_t>(rng.next()) << 32;
+        unsigned pos = static_cast<unsigned>(w2 % n);
+        for (unsigned guard = 0; ((result >> pos) & 1u) == static_cast<uint64_t>(diff > 0) && guard < 64; guard++)
+            pos = (pos + 1) % n;
+        result ^= 1ull << pos;
+        diff += diff > 0 ? -1 : 1;
+    }
+    return result;
+}
+
+// One Metropolis proposal (include/spin_ensembles/MonteCarloLoop.hpp:153-256): flip
+// site `u32 % N` (and a partner with the same new spin under S_z symmetry), update the
+// angles of the trial state, accept if Delta > 0 or u <= exp(2 Delta), u drawn only
+// when Delta <= 0.
+template <int K, int NW>
+__device__ __forceinline__ bool rbm_mh_step(const RbmDev& P, Spins<NW>& s, float (&tr)[K], float (&ti)[K],
+                                            float (&re)[K], WalkerRng& rng, int lane, int total_z) {
+    const int N = P.N;
+    int sites[2];
+    int ns = 1;
+    sites[0] = static_cast<int>(rng.next() % static_cast<uint32_t>(N));
+    if (total_z) {
+        const bool first_new = !s.up(sites[0]);
+        int sec = sites[0];
+        for (int guard = 0; guard < (1 << 20); guard++) {
+            const int c = static_cast<int>(rng.next() % static_cast<uint32_t>(N));
+            const bool v = c == sites[0] ? first_new : s.up(c);
+            if (v == first_new) { sec = c; break; }
+        }
+        sites[1] = sec;
+        ns = 2;
+    }
+    float nr[K], ni[K], nre[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) { nr[k] = tr[k]; ni[k] = ti[k]; }
+    Spins<NW> s2 = s;
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+        if (q >= ns) break;
+        const int site = q == 0 ? sites[0] : sites[1];
+        s2.flip(site);
+        const float two_s = s2.up(site) ? 2.0f : -2.0f;
+        const float2* row = P.W + static_cast<long>(site) * P.Mpad + lane;
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const float2 w = __ldg(row + 32 * k);
+            nr[k] = __fmaf_rn(two_s, w.x, nr[k]);
+            ni[k] = __fmaf_rn(two_s, w.y, ni[k]);
+        }
+    }
+    float part = 0.0f;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        nre[k] = lc_re(nr[k], ni[k]);
+        part = __fadd_rn(part, __fsub_rn(nre[k], re[k]));
+    }
+    const float delta = warp_sum_xor(part);
+    bool accept = delta > 0.0f;
+    if (!accept) accept = rng.uniform() <= expf_det(__fmul_rn(2.0f, delta));
+    if (accept) {
+        s = s2;
+#pragma unroll
+        for (int k = 0; k < K; k++) { tr[k] = nr[k]; ti[k] = ni[k]; re[k] = nre[k]; }
+    }
+    return accept;
+}
+
+// sign * (-i)^ypow of string n for the current (original) spins
+template <int NW>
+__device__ __forceinline__ double2 string_factor(const OpDev& op, int n, const Spins<NW>& s) {
+    int parity = 0;
+#pragma unroll
+    for (int k = 0; k < NW; k++) parity += __popcll(op.zmask[n * kMaxWords + k] & ~s.w[k]);
+    const double sg = (parity & 1) ? -1.0 : 1.0;
+    const double2 c = op.coef[n];
+    const int yp = op.ypow[n] & 3;
+    // c * (-i)^yp * sg
+    double2 r;
+    if (yp == 0) r = make_double2(c.x, c.y);
+    else if (yp == 1) r = make_double2(c.y, -c.x);
+    else if (yp == 2) r = make_double2(-c.x, -c.y);
+    else r = make_double2(-c.y, c.x);
+    return make_double2(sg * r.x, sg * r.y);
+}
+
+// Local energy E_loc(s) = sum_n coef_n phase_n exp(log psi(s'_n) - log psi(s))
+// (include/operator/Operator.hpp:90-115).  Diagonal strings contribute coef * phase
+// exactly.  With GRAD, also accumulates U_j = sum_n e_n tanh(theta'_nj) (the E_k term,
+// Operator.hpp:145-179) and stores X[slot][j] = e_n tanh(theta'_nj) per off-diagonal string.
+template <bool GRAD, int K, int NW>
+__device__ __forceinline__ double2 rbm_local_energy(const RbmDev& P, const OpDev& op, const Spins<NW>& s,
+                                                    const float (&tr)[K], const float (&ti)[K],
+                                                    const float2 (&f)[K], const float2 (&T)[K], float2 (&U)[K],
+                                                    float2* X, int lane) {
+    double er = 0.0, ei = 0.0;
+    if (GRAD) {
+#pragma unroll
+        for (int k = 0; k < K; k++) U[k] = make_float2(0.0f, 0.0f);
+    }
+    for (int n = 0; n < op.S; n++) {
+        const double2 cf = string_factor(op, n, s);
+        const int nf = op.nflip[n];
+        if (nf == 0) {
+            er += cf.x;
+            ei += cf.y;
+            if (GRAD) {
+                const float ex = static_cast<float>(cf.x), ey = static_cast<float>(cf.y);
+#pragma unroll
+                for (int k = 0; k < K; k++) {
+                    U[k].x += ex * T[k].x - ey * T[k].y;
+                    U[k].y += ex * T[k].y + ey * T[k].x;
+                }
+            }
+            continue;
+        }
+        float nr[K], ni[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) { nr[k] = tr[k]; ni[k] = ti[k]; }
+        const int off = op.flip_off[n];
+        for (int q = 0; q < nf; q++) {
+            const int site = op.flip_sites[off + q];
+            const float two_s = s.up(site) ? -2.0f : 2.0f;   // new spin = -old
+            const float2* row = P.W + static_cast<long>(site) * P.Mpad + lane;
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                const float2 w = __ldg(row + 32 * k);
+                nr[k] = fmaf(two_s, w.x, nr[k]);
+                ni[k] = fmaf(two_s, w.y, ni[k]);
+            }
+        }
+        float2 part = make_float2(0.0f, 0.0f);
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const float2 g = lc_c(nr[k], ni[k]);
+            part.x += g.x - f[k].x;
+            part.y += g.y - f[k].y;
+        }
+        const float2 d = warp_sum_xor2(part);
+        float sn, cs;
+        sincosf(d.y, &sn, &cs);
+        const float mag = expf(d.x);
+        const double xr = static_cast<double>(mag * cs), xi = static_cast<double>(mag * sn);
+        const double e_r = cf.x * xr - cf.y * xi;
+        const double e_i = cf.x * xi + cf.y * xr;
+        er += e_r;
+        ei += e_i;
+        if (GRAD) {
+            const float ex = static_cast<float>(e_r), ey = static_cast<float>(e_i);
+            float2* xrow = X + static_cast<long>(op.offdiag_slot[n]) * P.Mpad + lane;
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                const float2 t2 = tanh_c(nr[k], ni[k]);
+                const float2 v = make_float2(ex * t2.x - ey * t2.y, ex * t2.y + ey * t2.x);
+                U[k].x += v.x;
+                U[k].y += v.y;
+                xrow[32 * k] = v;
+            }
+        }
+    }
+    return make_double2(er, ei);
+}
+
+template <int K>
+__device__ __forceinline__ double2 warp_log_psi(const float2 (&f)[K]) {
+    float2 acc = make_float2(0.0f, 0.0f);
+#pragma unroll
+    for (int k = 0; k < K; k++) { acc.x += f[k].x; acc.y += f[k].y; }
+    acc = warp_sum_xor2(acc);
+    return make_double2(acc.x, acc.y);
+}
+
+// ---------------------------------------------------------------------------
+// Metropolis sampler: one warp per walker for a whole launch
+// (include/spin_ensembles/MonteCarloLoop.hpp:55-138).  The angles are recomputed
+// from the spins at the start of every sweep and before every measurement.
+// ---------------------------------------------------------------------------
+template <int K, int NW>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock) rbm_mc_kernel(RbmDev P, OpDev op, int has_op, McLaunch L) {
+    const int lane = threadIdx.x & 31;
+    const int w = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+    if (w >= L.B) return;
+    WalkerRng rng;
+    rng.init(L.seed, L.walker_base + static_cast<uint32_t>(w), L.rng_index[w]);
+    Spins<NW> s;
+    if (L.init) {
+#pragma unroll
+        for (int k = 0; k < NW; k++) s.w[k] = 0;
+        if (L.total_z) s.w[0] = draw_n_over_k(rng, P.N, static_cast<unsigned>((L.sector + P.N) / 2));
+        else draw_spins(rng, P.N, s);
+    } else {
+#pragma unroll
+        for (int k = 0; k < NW; k++) s.w[k] = L.spins[static_cast<long>(w) * NW + k];
+    }
+    float tr[K], ti[K], re[K];
+    unsigned long long acc = 0, props = 0;
+    const int total_sweeps = L.n_therm + L.n_samples * L.sweeps_per_sample;
+    int sample = 0;
+    for (int sw = 0; sw < total_sweeps; sw++) {
+        rbm_refresh(P, s, tr, ti, lane);
+#pragma unroll
+        for (int k = 0; k < K; k++) re[k] = lc_re(tr[k], ti[k]);
+        for (int p = 0; p < P.N; p++) acc += rbm_mh_step(P, s, tr, ti, re, rng, lane, L.total_z);
+        props += P.N;
+        const int done = sw + 1 - L.n_therm;
+        if (done > 0 && done % L.sweeps_per_sample == 0) {
+            const long row = static_cast<long>(L.sample_base + sample) * L.B + w;
+            if (L.sample_spins && lane == 0) {
+#pragma unroll
+                for (int k = 0; k < NW; k++) L.sample_spins[row * NW + k] = s.w[k];
+            }
+            if (L.eloc || L.logpsi) {
+                rbm_refresh(P, s, tr, ti, lane);
+                float2 f[K];
+#pragma unroll
+                for (int k = 0; k < K; k++) f[k] = lc_c(tr[k], ti[k]);
+                if (L.logpsi) {
+                    const double2 lp = warp_log_psi(f);
+                    if (lane == 0) L.logpsi[row] = lp;
+                }
+                if (L.eloc && has_op) {
+                    float2 T[K], U[K];
+                    const double2 e = rbm_local_energy<false>(P, op, s, tr, ti, f, T, U, nullptr, lane);
+                    if (lane == 0) L.eloc[row] = e;
+                }
+            }
+            sample++;
+        }
+    }
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < NW; k++) L.spins[static_cast<long>(w) * NW + k] = s.w[k];
+        L.rng_index[w] = rng.index;
+        L.accepts[w] += acc;
+        L.proposals[w] += props;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Estimator pass over given configurations (one warp each): local energy, log psi,
+// the O_k vectors T = tanh(theta), the E_k vectors U and X, and psi' quantities for
+// the Hilbert-space distance.
+// ---------------------------------------------------------------------------
+template <int K, int NW>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock) rbm_est_kernel(RbmDev P, OpDev op, int has_op, RbmDev PP,
+                                                                       EstLaunch L) {
+    const int lane = threadIdx.x & 31;
+    const long t = static_cast<long>(blockIdx.x) * kWarpsPerBlock + (threadIdx.x >> 5);
+    if (t >= L.count) return;
+    Spins<NW> s;
+    if (L.flags & EST_ENUMERATE) {
+        const uint64_t idx = L.enum_base + static_cast<uint64_t>(t);
+        s.w[0] = P.N >= 64 ? idx : (idx & ((1ull << P.N) - 1ull));
+#pragma unroll
+        for (int k = 1; k < NW; k++) s.w[k] = 0;
+    } else {
+#pragma unroll
+        for (int k = 0; k < NW; k++) s.w[k] = L.spins[t * NW + k];
+    }
+    if (L.flags & (EST_ELOC | EST_LOGPSI | EST_GRADVEC)) {
+        float tr[K], ti[K];
+        rbm_refresh(P, s, tr, ti, lane);
+        float2 f[K], T[K], U[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) f[k] = lc_c(tr[k], ti[k]);
+        if (L.flags & EST_LOGPSI) {
+            const double2 lp = warp_log_psi(f);
+            if (lane == 0) L.logpsi[t] = lp;
+        }
+        if (L.flags & EST_GRADVEC) {
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                T[k] = tanh_c(tr[k], ti[k]);
+                L.T[t * P.Mpad + lane + 32 * k] = T[k];
+            }
+            const double2 e = rbm_local_energy<true>(P, op, s, tr, ti, f, T, U,
+                                                     L.X + t * op.num_offdiag * P.Mpad, lane);
+            const float shx = static_cast<float>(L.e_shift.x), shy = static_cast<float>(L.e_shift.y);
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                U[k].x -= shx * T[k].x - shy * T[k].y;
+                U[k].y -= shx * T[k].y + shy * T[k].x;
+                L.U[t * P.Mpad + lane + 32 * k] = U[k];
+            }
+            if (lane == 0 && L.eloc) L.eloc[t] = e;
+        } else if ((L.flags & EST_ELOC) && has_op) {
+            const double2 e = rbm_local_energy<false>(P, op, s, tr, ti, f, T, U, nullptr, lane);
+            if (lane == 0) L.eloc[t] = e;
+        }
+    }
+    if (L.flags & EST_PRIME) {
+        float pr[K], pi[K];
+        rbm_refresh(PP, s, pr, pi, lane);
+        float2 fp[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) fp[k] = lc_c(pr[k], pi[k]);
+        const double2 lp = warp_log_psi(fp);
+        if (lane == 0) L.logpsi_prime[t] = lp;
+        if (L.Tp) {
+#pragma unroll
+            for (int k = 0; k < K; k++) L.Tp[t * PP.Mpad + lane + 32 * k] = tanh_c(pr[k], pi[k]);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// launchers for this K (instantiated by rbm_k<K>.cu)
+// ---------------------------------------------------------------------------
+template <int K>
+cudaError_t rbm_mc_launch_k(const RbmDev& P, const OpDev* op, const McLaunch& L, cudaStream_t st) {
+    const int nw = (P.N + 63) / 64;
+    const dim3 grid((L.B + kWarpsPerBlock - 1) / kWarpsPerBlock), block(32 * kWarpsPerBlock);
+    OpDev o = op ? *op : OpDev{};
+    const int has = op != nullptr;
+    switch (nw) {
+        case 1: rbm_mc_kernel<K, 1><<<grid, block, 0, st>>>(P, o, has, L); break;
+        case 2: rbm_mc_kernel<K, 2><<<grid, block, 0, st>>>(P, o, has, L); break;
+        case 3: rbm_mc_kernel<K, 3><<<grid, block, 0, st>>>(P, o, has, L); break;
+        case 4: rbm_mc_kernel<K, 4><<<grid, block, 0, st>>>(P, o, has, L); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+template <int K>
+cudaError_t rbm_est_launch_k(const RbmDev& P, const OpDev* op, const RbmDev* PP, const EstLaunch& L,
+                             cudaStream_t st) {
+    const int nw = (P.N + 63) / 64;
+    const dim3 grid((L.count + kWarpsPerBlock - 1) / kWarpsPerBlock), block(32 * kWarpsPerBlock);
+    OpDev o = op ? *op : OpDev{};
+    const int has = op != nullptr;
+    RbmDev pp = PP ? *PP : P;
+    switch (nw) {
+        case 1: rbm_est_kernel<K, 1><<<grid, block, 0, st>>>(P, o, has, pp, L); break;
+        case 2: rbm_est_kernel<K, 2><<<grid, block, 0, st>>>(P, o, has, pp, L); break;
+        case 3: rbm_est_kernel<K, 3><<<grid, block, 0, st>>>(P, o, has, pp, L); break;
+        case 4: rbm_est_kernel<K, 4><<<grid, block, 0, st>>>(P, o, has, pp, L); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace rbmg

@@ -1,0 +1,7 @@
+// Complex-RBM kernels instantiated for K = 4 hidden units per lane (M <= 128).
+#include "rbm_impl.cuh"
+
+namespace rbmg {
+template cudaError_t rbm_mc_launch_k<4>(const RbmDev&, const OpDev*, const McLaunch&, cudaStream_t);
+template cudaError_t rbm_est_launch_k<4>(const RbmDev&, const OpDev*, const RbmDev*, const EstLaunch&, cudaStream_t);
+}  // namespace rbmg
