@@ -543,6 +543,9 @@ extern "C" int rbmg_ensemble_destroy(rbmg_ensemble* ens) {
 }
 
 // ====================================================================== sample streams
+static int rbm_upload64(const rbmg_psi* p);
+static Rbm64 rbm64(const rbmg_psi* p);
+
 namespace rbmg {
 
 // One chunk of samples: spins on the device (or basis indices when enumerate),
@@ -561,16 +564,25 @@ struct StreamResult {
     double log_norm = 0.0;      // log of sum_s prefactor^2 |psi|^2 (exact)
 };
 
+// FP64 log psi of a batch of configurations (exact-summation weights, psi vector,
+// log_psi queries): the rational activation cancels to ~1e-7 absolute near theta = 0 in
+// FP32, a bias that would shift the normalisation sum by ~1e-6 relative.
 static int psi_log_psi_dev(const rbmg_psi* psi, int count, const uint64_t* d_spins, uint64_t enum_base,
                            int enumerate, double2* d_out) {
     if (psi->kind == 0) {
-        EstLaunch L{};
+        const int r = ::rbm_upload64(psi);
+        if (r != RBMG_OK) return r;
+        Hsd64Launch L{};
         L.count = count;
         L.enum_base = enum_base;
+        L.enumerate = enumerate;
         L.spins = d_spins;
-        L.flags = EST_LOGPSI | (enumerate ? EST_ENUMERATE : 0);
         L.logpsi = d_out;
-        RBMG_CK(launch_rbm_estimate(psi->rbm_dev(), nullptr, nullptr, L, stream()));
+        OpDev none{};
+        Rbm64 nopp{};
+        nopp.N = psi->N;
+        nopp.M = psi->M;
+        RBMG_CK(launch_rbm_hsd64(::rbm64(psi), nopp, none, L, stream()));
         return RBMG_OK;
     }
     return deep_log_psi(psi, count, d_spins, enum_base, enumerate, d_out, stream());
@@ -1142,10 +1154,12 @@ extern "C" int rbmg_hsd_gradient(const rbmg_psi* psi, const rbmg_psi* pp, const 
         if (!want_grad) break;
         // ---- stage 2: sum_s w_s c_s O_k(s) over the kept samples
         const int mode = passes == 1 ? 0 : (pass == 0 ? 1 : 2);
+        const double pf = std::pow(dist, static_cast<double>(nu));
+        const double scale = mode == 0 ? 1.0 / (v * v * pf) : (mode == 1 ? 1.0 / (v * v * dist) : 1.0 / (v * dist));
         RBMG_CK(W.coef1.ensure(sizeof(double2) * count));
         RBMG_CK(launch_hsd_coef(count, weighted ? all_w : nullptr, W.omega.as<double2>(), W.pr.as<double2>(),
-                                make_double2(omega.real(), -omega.imag()), v, u, nn, mode, W.coef1.as<double2>(),
-                                stream()));
+                                make_double2(omega.real(), -omega.imag()), v, u, nn, mode, scale,
+                                W.coef1.as<double2>(), stream()));
         RBMG_CK(W.acc_wO.ensure(sizeof(double2) * ok_len));
         RBMG_CK(cudaMemsetAsync(W.acc_wO.p, 0, sizeof(double2) * ok_len, stream()));
         const uint64_t* sp = enumerated ? (ens->exact_total_z ? ens->d_allowed.as<uint64_t>() : nullptr) : all_spins;
@@ -1178,13 +1192,13 @@ extern "C" int rbmg_hsd_gradient(const rbmg_psi* psi, const rbmg_psi* pp, const 
         std::vector<double2> acc(ok_len);
         RBMG_CK(cudaMemcpyAsync(acc.data(), W.acc_wO.p, sizeof(double2) * ok_len, cudaMemcpyDeviceToHost, stream()));
         RBMG_CK(cudaStreamSynchronize(stream()));
+        // the coefficients already carry 1/v^2/d^nu (mode 0), 1/v^2/d (mode 1), 1/v/d (mode 2)
         if (mode == 0) {          // HilbertSpaceDistance.cu:253-263
-            const double pf = std::pow(dist, static_cast<double>(nu));
-            for (size_t k = 0; k < ok_len; k++) gout[2 * N + k] = -(cplx(acc[k].x, acc[k].y) * f) / (v * v) / pf;
+            for (size_t k = 0; k < ok_len; k++) gout[2 * N + k] = -(cplx(acc[k].x, acc[k].y) * f);
         } else if (mode == 1) {   // HilbertSpaceDistance_PsiPair.cu:121-133
-            for (size_t k = 0; k < ok_len; k++) gout[2 * N + k] = cplx(-(acc[k].x * f) / (v * v) / dist, 0.0);
+            for (size_t k = 0; k < ok_len; k++) gout[2 * N + k] = cplx(-(acc[k].x * f), 0.0);
         } else {                  // HilbertSpaceDistance_PsiPair.cu:153-163
-            for (size_t k = 0; k < ok_len; k++) gout[2 * N + k] += cplx(0.0, -(acc[k].x * f) / v / dist);
+            for (size_t k = 0; k < ok_len; k++) gout[2 * N + k] += cplx(0.0, -(acc[k].x * f));
         }
     }
     *distance = dist;

@@ -1,6 +1,10 @@
 // PsiDeep / PsiPair kernels (include/quantum_state/PsiDeep.hpp:89-293, PsiPair.hpp:36-119).
 //
 // One CTA per configuration: thread j owns unit j of the layer being evaluated;
+// the estimator kernels (local energies, O_k and E_k rows) run in FP64 -- for these
+// nets log psi(s') - log psi(s) is the difference of two full forward passes, so FP32
+// would cost ~1e-7 |log psi| per local-energy term -- while the Metropolis sampler runs
+// in FP32;
 // the layer's inputs, angles and activations live in shared memory; weights are read
 // coalesced over j ([connectivity][size] layout, as the reference stores them).
 // The backward pass gathers over the rhs connection lists compiled on the host in
@@ -65,6 +69,30 @@ template <bool REAL> __device__ __forceinline__ double2 act(double2 a) {
 // derivative: my_tanh for complex nets, 1 for the real nets (psi_functions.hpp:127-136)
 template <bool REAL> __device__ __forceinline__ float2 dact(float2 a) {
     return REAL ? make_float2(1.f, 0.f) : tanh_c(a.x, a.y);
+}
+// my_tanh in FP64 (psi_functions.hpp:97-114)
+__device__ __forceinline__ double2 tanh64(double2 z) {
+    const double s = z.x > 0.0 ? 1.0 : -1.0;
+    const double2 u = make_double2(s * z.x, s * z.y);
+    double2 d = make_double2(u.x + 3.746646023906276, u.y);
+    d = cmul(u, d); d.x += 7.771429504240965;
+    d = cmul(u, d); d.x += 10.218021346543315;
+    d = cmul(u, d); d.x += 9.19376335670885;
+    double2 q = make_double2(6.746450656267947 + 0.9003320053750442 * u.x, 0.9003320053750442 * u.y);
+    q = cmul(u, q); q.x += 26.632014683761202;
+    q = cmul(u, q); q.x += 70.82878897882324;
+    q = cmul(u, q); q.x += 146.36284300074402;
+    q = cmul(u, q); q.x += 199.24474920889975;
+    q = cmul(u, q); q.x += 177.6769746361748;
+    q = cmul(u, q); q.x += 83.68563506532087;
+    q = cmul(u, q);
+    const double2 d2 = cmul(d, d);
+    const double den = d2.x * d2.x + d2.y * d2.y;
+    const double2 h = make_double2((q.x * d2.x + q.y * d2.y) / den, (q.y * d2.x - q.x * d2.y) / den);
+    return make_double2(s * h.x, s * h.y);
+}
+template <bool REAL> __device__ __forceinline__ double2 dact(double2 a) {
+    return REAL ? make_double2(1.0, 0.0) : tanh64(a);
 }
 
 template <typename V> struct W_of;
@@ -181,25 +209,26 @@ __device__ V state_log_psi(const DeepNetDev& n0, const DeepNetDev& n1, int pair,
 
 // reverse pass (PsiDeep.hpp:214-293) after forward_once<STORE>; emit(k, value) with k
 // counted from the first O_k entry (parameter index - 2N)
-template <bool REAL, typename Emit>
-__device__ void backward(const DeepNetDev& net, const uint64_t* s, Work<float2>& w, float2 log_psi, Emit emit) {
+template <typename V, bool REAL, typename Emit>
+__device__ void backward(const DeepNetDev& net, const uint64_t* s, Work<V>& w, V log_psi, Emit emit) {
     const int t = threadIdx.x;
     const int L = net.L;
-    float2* cur = w.in;
-    float2* nxt = w.out;
+    V* cur = w.in;
+    V* nxt = w.out;
     for (int l = L - 1; l >= 0; l--) {
         const int size = net.size[l];
-        float2 d = make_float2(0.f, 0.f);
+        V d = czero<V>();
         if (t < size) {
-            const float2 ang = w.angles[net.begin_angle[l] + t];
+            const V ang = w.angles[net.begin_angle[l] + t];
             if (l == L - 1) {
-                d = cmul(net.fw[t], dact<REAL>(ang));
+                d = cmul(W_of<V>::fw(net)[t], dact<REAL>(ang));
             } else {
                 const int nsize = net.size[l + 1];
-                float2 acc = make_float2(0.f, 0.f);
+                V acc = czero<V>();
+                const V* wn = W_of<V>::w(net, l + 1);
                 for (int e = net.rptr[l][t]; e < net.rptr[l][t + 1]; e++) {
                     const int q = net.rq[l][e];
-                    acc = cadd(acc, cmul(net.w[l + 1][q], nxt[q % nsize]));
+                    acc = cadd(acc, cmul(wn[q], nxt[q % nsize]));
                 }
                 d = cmul(acc, dact<REAL>(ang));
             }
@@ -212,13 +241,12 @@ __device__ void backward(const DeepNetDev& net, const uint64_t* s, Work<float2>&
             const int conn = net.conn[l];
             for (int c = 0; c < conn; c++) {
                 const int src = net.cidx[l][c * size + t];
-                const float2 in = l == 0 ? make_float2(bit_up(s, src) ? 1.f : -1.f, 0.f)
-                                         : w.acts[net.begin_angle[l - 1] + src];
+                const V in = l == 0 ? creal<V>(bit_up(s, src) ? 1.0 : -1.0) : w.acts[net.begin_angle[l - 1] + src];
                 emit(base + size + c * size + t, cmul(d, in));
             }
         }
         __syncthreads();
-        float2* tmp = cur;
+        V* tmp = cur;
         cur = nxt;
         nxt = tmp;
     }
@@ -296,7 +324,7 @@ __global__ void deep_logpsi_kernel(DeepNetDev n0, DeepNetDev n1, int pair, int c
     uint64_t* shifted = w.s + kMaxWords;
     const long t = blockIdx.x;
     if (t >= count) return;
-    load_config(spins, enum_base, enum_base >= 0 && enumerate, t, n0.N, w.s);
+    load_config(spins, enum_base, enumerate, t, n0.N, w.s);
     const V lp = state_log_psi<V>(n0, n1, pair, w.s, w, shifted);
     if (threadIdx.x == 0) out[t] = make_double2(lp.x, lp.y);
 }
@@ -346,34 +374,33 @@ __global__ void deep_eloc_kernel(DeepNetDev n0, DeepNetDev n1, int pair, DeepNet
 // O_k rows [count][P - 2N] of one net (complex, or a real PsiPair net stored as (x, 0))
 template <bool REAL>
 __global__ void deep_ok_kernel(DeepNetDev net, int count, const uint64_t* spins, uint64_t enum_base, int enumerate,
-                               float2* rows, long ld) {
+                               double2* rows, long ld) {
     extern __shared__ __align__(16) unsigned char smem[];
-    Work<float2> w = carve<float2>(smem, net, true);
+    Work<double2> w = carve<double2>(smem, net, true);
     const long t = blockIdx.x;
     if (t >= count) return;
     load_config(spins, enum_base, enumerate, t, net.N, w.s);
-    const float2 lp = forward_once<float2, REAL, true>(net, w.s, w);
-    float2* row = rows + t * ld;
-    backward<REAL>(net, w.s, w, lp, [&](int k, float2 v) { row[k] = v; });
+    const double2 lp = forward_once<double2, REAL, true>(net, w.s, w);
+    double2* row = rows + t * ld;
+    backward<double2, REAL>(net, w.s, w, lp, [&](int k, double2 v) { row[k] = v; });
 }
 
-// per sample: E_loc, O_k(s) row, and the centred E_k row
+// per sample (FP64): E_loc, O_k(s) row, and the centred E_k row
 //   Ek[s] = (E_diag - E0) O(s) + sum_{off-diagonal n} e_n O(s'_n)
 // (Operator.hpp:145-179 with the shift of the gradient estimator)
 __global__ void deep_grad_kernel(DeepNetDev net, OpDev op, int count, const uint64_t* spins, uint64_t enum_base,
-                                 int enumerate, double2 e_shift, double2* eloc, float2* Orows, float2* Ekrows,
+                                 int enumerate, double2 e_shift, double2* eloc, double2* Orows, double2* Ekrows,
                                  long ld) {
     extern __shared__ __align__(16) unsigned char smem[];
-    Work<float2> w = carve<float2>(smem, net, true);
+    Work<double2> w = carve<double2>(smem, net, true);
     uint64_t* sp = w.s + kMaxWords;
     const long t = blockIdx.x;
     if (t >= count) return;
     load_config(spins, enum_base, enumerate, t, net.N, w.s);
-    float2* orow = Orows + t * ld;
-    float2* erow = Ekrows + t * ld;
-    const float2 lp = forward_once<float2, false, true>(net, w.s, w);
-    backward<false>(net, w.s, w, lp, [&](int k, float2 v) { orow[k] = v; });
-    // diagonal part first
+    double2* orow = Orows + t * ld;
+    double2* erow = Ekrows + t * ld;
+    const double2 lp = forward_once<double2, false, true>(net, w.s, w);
+    backward<double2, false>(net, w.s, w, lp, [&](int k, double2 v) { orow[k] = v; });
     double dr_ = 0.0, di_ = 0.0;
     for (int n = 0; n < op.S; n++) {
         if (op.nflip[n] != 0) continue;
@@ -383,7 +410,7 @@ __global__ void deep_grad_kernel(DeepNetDev net, OpDev op, int count, const uint
     }
     double er = dr_, ei = di_;
     {
-        const float2 c = make_float2(static_cast<float>(dr_ - e_shift.x), static_cast<float>(di_ - e_shift.y));
+        const double2 c = make_double2(dr_ - e_shift.x, di_ - e_shift.y);
         const int P = net.P - 2 * net.N;
         for (int k = threadIdx.x; k < P; k += blockDim.x) erow[k] = cmul(c, orow[k]);
     }
@@ -391,46 +418,32 @@ __global__ void deep_grad_kernel(DeepNetDev net, OpDev op, int count, const uint
     for (int n = 0; n < op.S; n++) {
         if (op.nflip[n] == 0) continue;
         const double2 cf = apply_string(op, n, w.s, sp);
-        const float2 lq = forward_once<float2, false, true>(net, sp, w);
-        const double dr = static_cast<double>(lq.x) - lp.x, di = static_cast<double>(lq.y) - lp.y;
+        const double2 lq = forward_once<double2, false, true>(net, sp, w);
+        const double dr = lq.x - lp.x, di = lq.y - lp.y;
         const double m = exp(dr);
         const double xr = m * cos(di), xi = m * sin(di);
-        const double e_r = cf.x * xr - cf.y * xi, e_i = cf.x * xi + cf.y * xr;
-        er += e_r;
-        ei += e_i;
-        const float2 e = make_float2(static_cast<float>(e_r), static_cast<float>(e_i));
-        backward<false>(net, sp, w, lq, [&](int k, float2 v) { erow[k] = cadd(erow[k], cmul(e, v)); });
+        const double2 e = make_double2(cf.x * xr - cf.y * xi, cf.x * xi + cf.y * xr);
+        er += e.x;
+        ei += e.y;
+        backward<double2, false>(net, sp, w, lq, [&](int k, double2 v) { erow[k] = cadd(erow[k], cmul(e, v)); });
     }
     if (threadIdx.x == 0) eloc[t] = make_double2(er, ei);
 }
 
-// out[k] += sum_s c[s] f(A[s][k]) over count samples, f = conj if conj_a
-__global__ void col_reduce_kernel(int count, int P, const double2* __restrict__ c, const float2* __restrict__ A,
+// out[k] += sum_s c[s] f(A[s][k]) over count samples, f = conj if conj_a (FP64)
+__global__ void col_reduce_kernel(int count, int P, const double2* __restrict__ c, const double2* __restrict__ A,
                                   long ld, int conj_a, double2* __restrict__ partial, int per_split) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const long s0 = static_cast<long>(blockIdx.y) * per_split;
     const long s1 = min(static_cast<long>(count), s0 + per_split);
+    if (k >= P) return;
     double2 acc = make_double2(0.0, 0.0);
-    if (k < P) {
-        float2 part = make_float2(0.f, 0.f);
-        int n = 0;
-        for (long s = s0; s < s1; s++) {
-            float2 a = A[s * ld + k];
-            if (conj_a) a.y = -a.y;
-            const double2 cc = c[s];
-            const float2 cf = make_float2(static_cast<float>(cc.x), static_cast<float>(cc.y));
-            part = cadd(part, cmul(cf, a));
-            if (++n == 32) {
-                acc.x += part.x;
-                acc.y += part.y;
-                part = make_float2(0.f, 0.f);
-                n = 0;
-            }
-        }
-        acc.x += part.x;
-        acc.y += part.y;
-        partial[static_cast<long>(blockIdx.y) * P + k] = acc;
+    for (long s = s0; s < s1; s++) {
+        double2 a = A[s * ld + k];
+        if (conj_a) a.y = -a.y;
+        acc = cadd(acc, cmul(c[s], a));
     }
+    partial[static_cast<long>(blockIdx.y) * P + k] = acc;
 }
 
 __global__ void col_finish_kernel(int P, int splits, const double2* __restrict__ partial, double2* out) {
@@ -646,10 +659,11 @@ int deep_log_psi(const rbmg_psi* psi, int count, const uint64_t* d_spins, uint64
                  double2* d_out, cudaStream_t st) {
     if (count <= 0) return RBMG_OK;
     const DeepNetDev n0 = net_of(psi, 0), n1 = net_of(psi, 1);
-    const size_t sm = smem_for(n0, sizeof(float2), false);
-    RBMG_CK(set_smem(deep_logpsi_kernel<float2>, sm));
-    deep_logpsi_kernel<float2><<<count, threads_for(n0), sm, st>>>(n0, n1, psi->kind == 2, count, d_spins, enum_base,
-                                                                   enumerate, d_out);
+    // FP64: exact-summation weights and the psi vector are built from these values
+    const size_t sm = smem_for(n0, sizeof(double2), false) + sizeof(uint64_t) * kMaxWords;
+    RBMG_CK(set_smem(deep_logpsi_kernel<double2>, sm));
+    deep_logpsi_kernel<double2><<<count, threads_for(n0), sm, st>>>(n0, n1, psi->kind == 2, count, d_spins, enum_base,
+                                                                     enumerate, d_out);
     RBMG_CK(cudaGetLastError());
     return RBMG_OK;
 }
@@ -657,11 +671,11 @@ int deep_log_psi(const rbmg_psi* psi, int count, const uint64_t* d_spins, uint64
 int deep_eloc_chunk(const rbmg_psi* psi, const rbmg_operator* op, const Chunk& c, double2* d_eloc, cudaStream_t st) {
     if (c.count <= 0) return RBMG_OK;
     const DeepNetDev n0 = net_of(psi, 0), n1 = net_of(psi, 1);
-    const size_t sm = smem_for(n0, sizeof(float2), false);
-    RBMG_CK(set_smem(deep_eloc_kernel<float2, false>, sm));
-    deep_eloc_kernel<float2, false><<<c.count, threads_for(n0), sm, st>>>(n0, n1, psi->kind == 2, n0, n1, op->dev(),
-                                                                         c.count, c.spins, c.enum_base, c.enumerate,
-                                                                         d_eloc, nullptr);
+    const size_t sm = smem_for(n0, sizeof(double2), false) + 2 * sizeof(uint64_t) * kMaxWords;
+    RBMG_CK(set_smem(deep_eloc_kernel<double2, false>, sm));
+    deep_eloc_kernel<double2, false><<<c.count, threads_for(n0), sm, st>>>(n0, n1, psi->kind == 2, n0, n1, op->dev(),
+                                                                           c.count, c.spins, c.enum_base, c.enumerate,
+                                                                           d_eloc, nullptr);
     RBMG_CK(cudaGetLastError());
     return RBMG_OK;
 }
@@ -686,7 +700,7 @@ static DevBuf& rows_buf(int which) {
     return b[which];
 }
 
-static int col_reduce(int count, int P, const double2* c, const float2* A, long ld, int conj_a, double2* out,
+static int col_reduce(int count, int P, const double2* c, const double2* A, long ld, int conj_a, double2* out,
                       cudaStream_t st) {
     if (count <= 0) return RBMG_OK;
     const int per_split = std::max(64, (count + 63) / 64);
@@ -704,25 +718,25 @@ int deep_hsd_okreduce(const rbmg_psi* pp, int pair_part, int count, const uint64
                       int enumerate, const double2* d_coef, double2* acc, cudaStream_t st) {
     const DeepNetDev net = net_of(pp, pair_part == 1 ? 1 : 0);
     const int P = net.P - 2 * net.N;
-    const int chunk = std::max(1, static_cast<int>((size_t(256) << 20) / (sizeof(float2) * P)));
+    const int chunk = std::max(1, static_cast<int>((size_t(256) << 20) / (sizeof(double2) * P)));
     DevBuf& rows = rows_buf(0);
-    RBMG_CK(rows.ensure(sizeof(float2) * static_cast<size_t>(std::min(chunk, count)) * P));
-    const size_t sm = smem_for(net, sizeof(float2), true);
+    RBMG_CK(rows.ensure(sizeof(double2) * static_cast<size_t>(std::min(chunk, count)) * P));
+    const size_t sm = smem_for(net, sizeof(double2), true);
     for (int base = 0; base < count; base += chunk) {
         const int cnt = std::min(chunk, count - base);
         const uint64_t* sp = d_spins ? d_spins + static_cast<size_t>(base) * ((net.N + 63) / 64) : nullptr;
         if (pp->kind == 2) {
             RBMG_CK(set_smem(deep_ok_kernel<true>, sm));
             deep_ok_kernel<true><<<cnt, threads_for(net), sm, st>>>(net, cnt, sp, enum_base + base, enumerate,
-                                                                    rows.as<float2>(), P);
+                                                                    rows.as<double2>(), P);
         } else {
             RBMG_CK(set_smem(deep_ok_kernel<false>, sm));
             deep_ok_kernel<false><<<cnt, threads_for(net), sm, st>>>(net, cnt, sp, enum_base + base, enumerate,
-                                                                     rows.as<float2>(), P);
+                                                                     rows.as<double2>(), P);
         }
         RBMG_CK(cudaGetLastError());
         // real O_k (PsiPair) multiply the real or complex coefficient; complex O_k enter conjugated
-        const int r = col_reduce(cnt, P, d_coef + base, rows.as<float2>(), P, pp->kind == 2 ? 0 : 1, acc, st);
+        const int r = col_reduce(cnt, P, d_coef + base, rows.as<double2>(), P, pp->kind == 2 ? 0 : 1, acc, st);
         if (r != RBMG_OK) return r;
     }
     return RBMG_OK;
@@ -733,17 +747,17 @@ int deep_ok_vector(const rbmg_psi* psi, const uint64_t* d_spins, double2* d_out,
     const DeepNetDev net = net_of(psi, 0);
     const int P = net.P - 2 * net.N;
     DevBuf& rows = rows_buf(0);
-    RBMG_CK(rows.ensure(sizeof(float2) * P));
-    const size_t sm = smem_for(net, sizeof(float2), true);
+    RBMG_CK(rows.ensure(sizeof(double2) * P));
+    const size_t sm = smem_for(net, sizeof(double2), true);
     RBMG_CK(set_smem(deep_ok_kernel<false>, sm));
-    deep_ok_kernel<false><<<1, threads_for(net), sm, st>>>(net, 1, d_spins, 0, 0, rows.as<float2>(), P);
+    deep_ok_kernel<false><<<1, threads_for(net), sm, st>>>(net, 1, d_spins, 0, 0, rows.as<double2>(), P);
     RBMG_CK(cudaGetLastError());
     RBMG_CK(cudaMemsetAsync(d_out, 0, sizeof(double2) * P, st));
     DevBuf& one = rows_buf(1);
     RBMG_CK(one.ensure(sizeof(double2)));
     const double2 h1 = make_double2(1.0, 0.0);
     RBMG_CK(cudaMemcpyAsync(one.p, &h1, sizeof(double2), cudaMemcpyHostToDevice, st));
-    return col_reduce(1, P, one.as<double2>(), rows.as<float2>(), P, 0, d_out, st);
+    return col_reduce(1, P, one.as<double2>(), rows.as<double2>(), P, 0, d_out, st);
 }
 
 int deep_gradient_chunk(const rbmg_psi* psi, const rbmg_operator* op, const Chunk& c, double2 e_shift,
@@ -752,26 +766,26 @@ int deep_gradient_chunk(const rbmg_psi* psi, const rbmg_operator* op, const Chun
     if (psi->kind == 2) return fail(RBMG_EUNSUPPORTED, "gradient: not instantiated for PsiPair (ExpectationValue.cu:553)");
     const DeepNetDev net = net_of(psi, 0);
     const int P = net.P - 2 * net.N;
-    const int chunk = std::max(1, static_cast<int>((size_t(384) << 20) / (2 * sizeof(float2) * P)));
+    const int chunk = std::max(1, static_cast<int>((size_t(512) << 20) / (2 * sizeof(double2) * P)));
     DevBuf& orows = rows_buf(0);
     DevBuf& erows = rows_buf(1);
-    RBMG_CK(orows.ensure(sizeof(float2) * static_cast<size_t>(std::min(chunk, c.count)) * P));
-    RBMG_CK(erows.ensure(sizeof(float2) * static_cast<size_t>(std::min(chunk, c.count)) * P));
-    const size_t sm = smem_for(net, sizeof(float2), true) + sizeof(uint64_t) * kMaxWords;
+    RBMG_CK(orows.ensure(sizeof(double2) * static_cast<size_t>(std::min(chunk, c.count)) * P));
+    RBMG_CK(erows.ensure(sizeof(double2) * static_cast<size_t>(std::min(chunk, c.count)) * P));
+    const size_t sm = smem_for(net, sizeof(double2), true) + sizeof(uint64_t) * kMaxWords;
     RBMG_CK(set_smem(deep_grad_kernel, sm));
     RBMG_CK(launch_coef(c.count, c.weights, nullptr, 1.0, coef1, st));
     for (int base = 0; base < c.count; base += chunk) {
         const int cnt = std::min(chunk, c.count - base);
         const uint64_t* sp = c.spins ? c.spins + static_cast<size_t>(base) * ((net.N + 63) / 64) : nullptr;
         deep_grad_kernel<<<cnt, threads_for(net), sm, st>>>(net, op->dev(), cnt, sp, c.enum_base + base, c.enumerate,
-                                                            e_shift, d_eloc + base, orows.as<float2>(),
-                                                            erows.as<float2>(), P);
+                                                            e_shift, d_eloc + base, orows.as<double2>(),
+                                                            erows.as<double2>(), P);
         RBMG_CK(cudaGetLastError());
         RBMG_CK(launch_coef(cnt, c.weights ? c.weights + base : nullptr, d_eloc + base, 1.0, coef2 + base, st,
                             e_shift));
-        int r = col_reduce(cnt, P, coef1 + base, orows.as<float2>(), P, 0, acc_O, st);
-        if (r == RBMG_OK) r = col_reduce(cnt, P, coef2 + base, orows.as<float2>(), P, 1, acc_EO, st);
-        if (r == RBMG_OK) r = col_reduce(cnt, P, coef1 + base, erows.as<float2>(), P, 0, acc_Ek, st);
+        int r = col_reduce(cnt, P, coef1 + base, orows.as<double2>(), P, 0, acc_O, st);
+        if (r == RBMG_OK) r = col_reduce(cnt, P, coef2 + base, orows.as<double2>(), P, 1, acc_EO, st);
+        if (r == RBMG_OK) r = col_reduce(cnt, P, coef1 + base, erows.as<double2>(), P, 0, acc_Ek, st);
         if (r != RBMG_OK) return r;
     }
     return RBMG_OK;

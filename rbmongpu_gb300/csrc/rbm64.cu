@@ -46,7 +46,9 @@ __device__ __forceinline__ double2 warp_sum64(double2 v) {
 
 __device__ __forceinline__ bool spin_up(const uint64_t* s, int i) { return (s[i >> 6] >> (i & 63)) & 1ull; }
 
-// shared memory per warp: theta[M], f[M] (double2 each)
+// shared memory per warp: theta[M], f[M] (double2 each).  op.S = 0 skips the local
+// energy and PP.W = null skips log psi'; with both it is the FP64 log psi pass that the
+// exact-summation weights and the psi vector use.
 __global__ void rbm_hsd64_kernel(Rbm64 P, Rbm64 PP, OpDev op, Hsd64Launch L) {
     extern __shared__ double2 smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -119,7 +121,7 @@ __global__ void rbm_hsd64_kernel(Rbm64 P, Rbm64 PP, OpDev op, Hsd64Launch L) {
     }
     // log psi'(s) - log psi(s), angle by angle
     double2 dl = make_double2(0.0, 0.0);
-    for (int j = lane; j < M; j += 32) {
+    for (int j = lane; PP.W && j < M; j += 32) {
         double2 a = PP.b[j];
         for (int i = 0; i < N; i++) {
             const double2 w = PP.W[static_cast<long>(i) * M + j];
@@ -134,7 +136,7 @@ __global__ void rbm_hsd64_kernel(Rbm64 P, Rbm64 PP, OpDev op, Hsd64Launch L) {
     if (lane == 0) {
         if (L.eloc) L.eloc[t] = make_double2(er, ei);
         if (L.logpsi) L.logpsi[t] = lp;
-        L.dlogpsi[t] = dl;
+        if (L.dlogpsi) L.dlogpsi[t] = dl;
     }
 }
 
@@ -164,7 +166,7 @@ __global__ void hsd_terms64_kernel(int count, const double2* __restrict__ eloc, 
 // per-sample gradient coefficients w_s * B_s (see capi.cu, rbmg_hsd_gradient)
 __global__ void hsd_coef_kernel(int count, const double* __restrict__ w, const double2* __restrict__ omega,
                                 const double2* __restrict__ pr, double2 conj_omega_bar, double v, double u,
-                                double nn_bar, int mode, double2* c) {
+                                double nn_bar, int mode, double scale, double2* c) {
     for (long s = blockIdx.x * 256L + threadIdx.x; s < count; s += static_cast<long>(gridDim.x) * 256) {
         const double ws = w ? w[s] : 1.0;
         const double2 om = omega[s];
@@ -176,7 +178,7 @@ __global__ void hsd_coef_kernel(int count, const double* __restrict__ w, const d
             r = make_double2(a.x * v - u * nn_bar * pr[s].x, a.y * v);   // B_s
             if (mode == 1) r.y = 0.0;                                     // Re B_s
         }
-        c[s] = make_double2(ws * r.x, ws * r.y);
+        c[s] = make_double2(scale * ws * r.x, scale * ws * r.y);
     }
 }
 
@@ -204,11 +206,11 @@ cudaError_t launch_hsd_terms64(int count, const double2* eloc, const double2* dl
 }
 
 cudaError_t launch_hsd_coef(int count, const double* w, const double2* omega, const double2* pr,
-                            double2 conj_omega_bar, double v, double u, double nn_bar, int mode, double2* c,
-                            cudaStream_t st) {
+                            double2 conj_omega_bar, double v, double u, double nn_bar, int mode, double scale,
+                            double2* c, cudaStream_t st) {
     if (count <= 0) return cudaSuccess;
     hsd_coef_kernel<<<static_cast<int>(std::min(1024L, (count + 255L) / 256)), 256, 0, st>>>(
-        count, w, omega, pr, conj_omega_bar, v, u, nn_bar, mode, c);
+        count, w, omega, pr, conj_omega_bar, v, u, nn_bar, mode, scale, c);
     return cudaGetLastError();
 }
 

@@ -29,9 +29,10 @@ cudaError_t launch_rbm_hsd64(const Rbm64& P, const Rbm64& PP, const OpDev& op, c
                              cudaStream_t st);
 cudaError_t launch_hsd_terms64(int count, const double2* eloc, const double2* dl, int is_unitary, double2* omega,
                                double2* pr, double2* nn, cudaStream_t st);
-// mode 0: w B_s, mode 1: w Re B_s, mode 2: w Im(conj(<omega>) omega_s)
+// mode 0: w B_s, mode 1: w Re B_s, mode 2: w Im(conj(<omega>) omega_s), each times scale
+// (the host folds the final 1/v^2 / d^nu into scale so the FP32 reduction stays in range)
 cudaError_t launch_hsd_coef(int count, const double* w, const double2* omega, const double2* pr,
-                            double2 conj_omega_bar, double v, double u, double nn_bar, int mode, double2* c,
-                            cudaStream_t st);
+                            double2 conj_omega_bar, double v, double u, double nn_bar, int mode, double scale,
+                            double2* c, cudaStream_t st);
 
 }  // namespace rbmg
