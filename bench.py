@@ -32,7 +32,7 @@ if REPO not in sys.path:
     sys.path.insert(0, REPO)
 
 N_SPINS, M_HIDDEN, SIGMA, PARAM_SEED, FIELD, WALKERS = 100, 400, 0.1, 104, 1.0, 16384
-THERM_SWEEPS = 30
+THERM_SWEEPS = 1000          # several tau_int of the plain chain (~130 sweeps)
 METRIC = "effective samples/s (ESS of E_loc), plain single-flip Metropolis, N=100 RBM"
 UNIT = "samples/s"
 L2_FLUSH_BYTES = 256 << 20
@@ -207,7 +207,7 @@ def run_gpu(args, rank, world, local_rank):
 
     # end to end through the public API with host buffers: per step the parameters go
     # host -> device (psi.params) and the walkers' local energies device -> host
-    e2e_K = max(4, K // 4)
+    e2e_K = max(4, K // 10)
     p_host = psi.params
     host_eloc = np.empty((e2e_K, B), np.complex128)
     pinned = torch.empty((B, 2), dtype=torch.float64, pin_memory=True)
@@ -250,7 +250,7 @@ def run_gpu(args, rank, world, local_rank):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--walkers", type=int, default=WALKERS)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
@@ -323,11 +323,12 @@ def main():
         "mean_energy": r["E_mean"].real,
         "e2e": {"value": r["e2e_ess"] / r["e2e_s"], "unit": UNIT, "h2d_bytes_per_step": int(r["h2d"]),
                 "d2h_bytes_per_step": int(r["d2h"])},
-        "gpu_launches": args.steps,
+        "gpu_launches": 2 * args.steps,     # per step: the sampler and the local-energy pass
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak if peak else None, "traffic": None,
                      "peak_source": "measured in this run by the library's FP32 FMA probe kernel",
-                     "kernel": "rbm_mc_kernel<13,2>", "flops_per_launch": fl},
+                     "kernel": "rbm_mc_kernel<13,2> + rbm_eloc_kernel<13,2> (one step)",
+                     "flops_per_launch": fl},
         "cpu_baseline": cpu,
         "clocks": r["clocks"],
     }

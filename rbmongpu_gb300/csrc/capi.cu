@@ -627,15 +627,22 @@ static int mc_stream(rbmg_ensemble* e, const rbmg_psi* psi, const rbmg_operator*
         L.sweeps_per_sample = static_cast<int>(e->num_sweeps);
         L.sample_base = 0;
         L.sample_spins = W.sample_spins.as<uint64_t>();
-        L.eloc = want_eloc ? W.eloc.as<double2>() : nullptr;
         L.accepts = e->accepts.as<unsigned long long>();
         L.proposals = e->proposals.as<unsigned long long>();
-        RBMG_CK(launch_rbm_mc(psi->rbm_dev(), op ? &od : nullptr, L, stream()));
+        RBMG_CK(launch_rbm_mc(psi->rbm_dev(), nullptr, L, stream()));
         first = false;
         Chunk c;
         c.count = rows * B;
         c.spins = W.sample_spins.as<uint64_t>();
-        c.eloc = want_eloc ? W.eloc.as<double2>() : nullptr;
+        if (want_eloc && op) {
+            EstLaunch E{};
+            E.count = c.count;
+            E.spins = c.spins;
+            E.flags = EST_ELOC;
+            E.eloc = W.eloc.as<double2>();
+            RBMG_CK(launch_rbm_estimate(psi->rbm_dev(), &od, nullptr, E, stream()));
+            c.eloc = W.eloc.as<double2>();
+        }
         const int r = fn(c);
         if (r != RBMG_OK) return r;
     }
@@ -1345,24 +1352,43 @@ extern "C" int rbmg_chain_sweep_async(rbmg_chain* c, const rbmg_psi* psi, const 
     if (d_eloc_out && (!op || measure_every <= 0)) return fail(RBMG_EINVAL, "chain sweep: measurement needs op");
     if (op && op->max_site >= psi->N) return fail(RBMG_EINVAL, "chain sweep: operator acts on a site >= N");
     if (n_sweeps == 0) return RBMG_OK;
-    const int every = d_eloc_out ? measure_every : n_sweeps;
+    cudaStream_t cs = st ? static_cast<cudaStream_t>(st) : stream();
+    const RbmDev P = psi->rbm_dev();
+    OpDev od;
+    if (op) od = op->dev();
     McLaunch L{};
     L.B = static_cast<int>(c->walkers);
     L.walker_base = 0;
     L.seed = c->seed;
     L.spins = c->spins.as<uint64_t>();
     L.rng_index = c->rng_index.as<uint64_t>();
-    L.init = c->initialised ? 0 : 1;
-    L.n_therm = d_eloc_out ? n_sweeps % every : n_sweeps;
-    L.n_samples = d_eloc_out ? n_sweeps / every : 0;
-    L.sweeps_per_sample = every;
-    L.eloc = static_cast<double2*>(d_eloc_out);
+    L.sweeps_per_sample = 1;
     L.accepts = c->accepts.as<unsigned long long>();
     L.proposals = c->proposals.as<unsigned long long>();
-    OpDev od;
-    if (op) od = op->dev();
-    RBMG_CK(launch_rbm_mc(psi->rbm_dev(), op ? &od : nullptr, L, st ? static_cast<cudaStream_t>(st) : stream()));
-    c->initialised = true;
+    auto sweeps = [&](int n) -> int {
+        if (n <= 0) return RBMG_OK;
+        L.init = c->initialised ? 0 : 1;
+        L.n_therm = n;
+        L.n_samples = 0;
+        RBMG_CK(launch_rbm_mc(P, nullptr, L, cs));
+        c->initialised = true;
+        return RBMG_OK;
+    };
+    if (!d_eloc_out) return sweeps(n_sweeps);
+    // n_sweeps % measure_every leading sweeps, then (measure_every sweeps, measurement) rows
+    int r = sweeps(n_sweeps % measure_every);
+    if (r != RBMG_OK) return r;
+    double2* out = static_cast<double2*>(d_eloc_out);
+    for (int row = 0; row < n_sweeps / measure_every; row++) {
+        r = sweeps(measure_every);
+        if (r != RBMG_OK) return r;
+        EstLaunch E{};
+        E.count = static_cast<int>(c->walkers);
+        E.spins = c->spins.as<uint64_t>();
+        E.flags = EST_ELOC;
+        E.eloc = out + static_cast<size_t>(row) * c->walkers;
+        RBMG_CK(launch_rbm_estimate(P, &od, nullptr, E, cs));
+    }
     return RBMG_OK;
 }
 
@@ -1382,3 +1408,4 @@ extern "C" int rbmg_chain_state(const rbmg_chain* c, uint64_t* spins, uint64_t* 
     if (proposals) *proposals = sp;
     return RBMG_OK;
 }
+

@@ -47,8 +47,6 @@ struct McLaunch {
     int sweeps_per_sample;
     int sample_base;            // index of the first recorded sample within the output rows
     uint64_t* sample_spins;     // [rows][B][NW] or null
-    double2* eloc;              // [rows][B] or null (needs op)
-    double2* logpsi;            // [rows][B] or null
     unsigned long long* accepts;   // [B], accumulated
     unsigned long long* proposals; // [B], accumulated
 };

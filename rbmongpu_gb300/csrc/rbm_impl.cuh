@@ -87,29 +87,30 @@ __device__ __forceinline__ bool rbm_mh_step(const RbmDev& P, Spins<NW>& s, float
         sites[1] = sec;
         ns = 2;
     }
-    float nr[K], ni[K], nre[K];
-#pragma unroll
-    for (int k = 0; k < K; k++) { nr[k] = tr[k]; ni[k] = ti[k]; }
+    // The trial angles are not kept: each is formed, evaluated and dropped, and on the
+    // (rare) accept they are formed again -- bit-identical -- to commit.  Only theta and
+    // Re f(theta) stay live, which keeps the register footprint low.
     Spins<NW> s2 = s;
+    float two_s[2];
+    const float2* rows[2];
 #pragma unroll
     for (int q = 0; q < 2; q++) {
         if (q >= ns) break;
         const int site = q == 0 ? sites[0] : sites[1];
         s2.flip(site);
-        const float two_s = s2.up(site) ? 2.0f : -2.0f;
-        const float2* row = P.W + static_cast<long>(site) * P.Mpad + lane;
-#pragma unroll
-        for (int k = 0; k < K; k++) {
-            const float2 w = __ldg(row + 32 * k);
-            nr[k] = __fmaf_rn(two_s, w.x, nr[k]);
-            ni[k] = __fmaf_rn(two_s, w.y, ni[k]);
-        }
+        two_s[q] = s2.up(site) ? 2.0f : -2.0f;
+        rows[q] = P.W + static_cast<long>(site) * P.Mpad + lane;
     }
     float part = 0.0f;
 #pragma unroll
     for (int k = 0; k < K; k++) {
-        nre[k] = lc_re(nr[k], ni[k]);
-        part = __fadd_rn(part, __fsub_rn(nre[k], re[k]));
+        float nr = tr[k], ni = ti[k];
+        for (int q = 0; q < ns; q++) {
+            const float2 w = __ldg(rows[q] + 32 * k);
+            nr = __fmaf_rn(two_s[q], w.x, nr);
+            ni = __fmaf_rn(two_s[q], w.y, ni);
+        }
+        part = __fadd_rn(part, __fsub_rn(lc_re(nr, ni), re[k]));
     }
     const float delta = warp_sum_xor(part);
     bool accept = delta > 0.0f;
@@ -117,7 +118,14 @@ __device__ __forceinline__ bool rbm_mh_step(const RbmDev& P, Spins<NW>& s, float
     if (accept) {
         s = s2;
 #pragma unroll
-        for (int k = 0; k < K; k++) { tr[k] = nr[k]; ti[k] = ni[k]; re[k] = nre[k]; }
+        for (int k = 0; k < K; k++) {
+            for (int q = 0; q < ns; q++) {
+                const float2 w = __ldg(rows[q] + 32 * k);
+                tr[k] = __fmaf_rn(two_s[q], w.x, tr[k]);
+                ti[k] = __fmaf_rn(two_s[q], w.y, ti[k]);
+            }
+            re[k] = lc_re(tr[k], ti[k]);
+        }
     }
     return accept;
 }
@@ -229,10 +237,12 @@ __device__ __forceinline__ double2 warp_log_psi(const float2 (&f)[K]) {
 // ---------------------------------------------------------------------------
 // Metropolis sampler: one warp per walker for a whole launch
 // (include/spin_ensembles/MonteCarloLoop.hpp:55-138).  The angles are recomputed
-// from the spins at the start of every sweep and before every measurement.
+// from the spins at the start of every sweep.  Measurements (local energies, log psi)
+// are a separate pass (rbm_est_kernel) over the recorded configurations, which keeps
+// the sampler's register footprint to the walker state.
 // ---------------------------------------------------------------------------
 template <int K, int NW>
-__global__ void __launch_bounds__(32 * kWarpsPerBlock) rbm_mc_kernel(RbmDev P, OpDev op, int has_op, McLaunch L) {
+__global__ void __launch_bounds__(32 * kWarpsPerBlock) rbm_mc_kernel(RbmDev P, McLaunch L) {
     const int lane = threadIdx.x & 31;
     const int w = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
     if (w >= L.B) return;
@@ -264,21 +274,6 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) rbm_mc_kernel(RbmDev P, O
             if (L.sample_spins && lane == 0) {
 #pragma unroll
                 for (int k = 0; k < NW; k++) L.sample_spins[row * NW + k] = s.w[k];
-            }
-            if (L.eloc || L.logpsi) {
-                rbm_refresh(P, s, tr, ti, lane);
-                float2 f[K];
-#pragma unroll
-                for (int k = 0; k < K; k++) f[k] = lc_c(tr[k], ti[k]);
-                if (L.logpsi) {
-                    const double2 lp = warp_log_psi(f);
-                    if (lane == 0) L.logpsi[row] = lp;
-                }
-                if (L.eloc && has_op) {
-                    float2 T[K], U[K];
-                    const double2 e = rbm_local_energy<false>(P, op, s, tr, ti, f, T, U, nullptr, lane);
-                    if (lane == 0) L.eloc[row] = e;
-                }
             }
             sample++;
         }
@@ -360,19 +355,92 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) rbm_est_kernel(RbmDev P, 
 }
 
 // ---------------------------------------------------------------------------
+// Local energies only (the measurement of a chain step): one warp per configuration,
+// angles and f(theta) in registers, each string's flipped angles formed and dropped
+// angle by angle (Operator.hpp:90-115).
+// ---------------------------------------------------------------------------
+template <int K, int NW>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock) rbm_eloc_kernel(RbmDev P, OpDev op, EstLaunch L) {
+    const int lane = threadIdx.x & 31;
+    const long t = static_cast<long>(blockIdx.x) * kWarpsPerBlock + (threadIdx.x >> 5);
+    if (t >= L.count) return;
+    Spins<NW> s;
+    if (L.flags & EST_ENUMERATE) {
+        const uint64_t idx = L.enum_base + static_cast<uint64_t>(t);
+        s.w[0] = P.N >= 64 ? idx : (idx & ((1ull << P.N) - 1ull));
+#pragma unroll
+        for (int k = 1; k < NW; k++) s.w[k] = 0;
+    } else {
+#pragma unroll
+        for (int k = 0; k < NW; k++) s.w[k] = L.spins[t * NW + k];
+    }
+    float tr[K], ti[K];
+    rbm_refresh(P, s, tr, ti, lane);
+    float2 f[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) f[k] = lc_c(tr[k], ti[k]);
+    double er = 0.0, ei = 0.0;
+    for (int n = 0; n < op.S; n++) {
+        const double2 cf = string_factor(op, n, s);
+        const int nf = op.nflip[n];
+        if (nf == 0) {
+            er += cf.x;
+            ei += cf.y;
+            continue;
+        }
+        const int off = op.flip_off[n];
+        float2 part = make_float2(0.0f, 0.0f);
+        if (nf == 1) {
+            const int site = op.flip_sites[off];
+            const float two_s = s.up(site) ? -2.0f : 2.0f;
+            const float2* row = P.W + static_cast<long>(site) * P.Mpad + lane;
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                const float2 w = __ldg(row + 32 * k);
+                const float2 g = lc_c(fmaf(two_s, w.x, tr[k]), fmaf(two_s, w.y, ti[k]));
+                part.x += g.x - f[k].x;
+                part.y += g.y - f[k].y;
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                float nr = tr[k], ni = ti[k];
+                for (int q = 0; q < nf; q++) {
+                    const int site = op.flip_sites[off + q];
+                    const float two_s = s.up(site) ? -2.0f : 2.0f;
+                    const float2 w = __ldg(P.W + static_cast<long>(site) * P.Mpad + lane + 32 * k);
+                    nr = fmaf(two_s, w.x, nr);
+                    ni = fmaf(two_s, w.y, ni);
+                }
+                const float2 g = lc_c(nr, ni);
+                part.x += g.x - f[k].x;
+                part.y += g.y - f[k].y;
+            }
+        }
+        const float2 d = warp_sum_xor2(part);
+        float sn, cs;
+        sincosf(d.y, &sn, &cs);
+        const float mag = expf(d.x);
+        const double xr = static_cast<double>(mag * cs), xi = static_cast<double>(mag * sn);
+        er += cf.x * xr - cf.y * xi;
+        ei += cf.x * xi + cf.y * xr;
+    }
+    if (lane == 0) L.eloc[t] = make_double2(er, ei);
+}
+
+// ---------------------------------------------------------------------------
 // launchers for this K (instantiated by rbm_k<K>.cu)
 // ---------------------------------------------------------------------------
 template <int K>
 cudaError_t rbm_mc_launch_k(const RbmDev& P, const OpDev* op, const McLaunch& L, cudaStream_t st) {
     const int nw = (P.N + 63) / 64;
     const dim3 grid((L.B + kWarpsPerBlock - 1) / kWarpsPerBlock), block(32 * kWarpsPerBlock);
-    OpDev o = op ? *op : OpDev{};
-    const int has = op != nullptr;
+    (void)op;
     switch (nw) {
-        case 1: rbm_mc_kernel<K, 1><<<grid, block, 0, st>>>(P, o, has, L); break;
-        case 2: rbm_mc_kernel<K, 2><<<grid, block, 0, st>>>(P, o, has, L); break;
-        case 3: rbm_mc_kernel<K, 3><<<grid, block, 0, st>>>(P, o, has, L); break;
-        case 4: rbm_mc_kernel<K, 4><<<grid, block, 0, st>>>(P, o, has, L); break;
+        case 1: rbm_mc_kernel<K, 1><<<grid, block, 0, st>>>(P, L); break;
+        case 2: rbm_mc_kernel<K, 2><<<grid, block, 0, st>>>(P, L); break;
+        case 3: rbm_mc_kernel<K, 3><<<grid, block, 0, st>>>(P, L); break;
+        case 4: rbm_mc_kernel<K, 4><<<grid, block, 0, st>>>(P, L); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
@@ -386,6 +454,16 @@ cudaError_t rbm_est_launch_k(const RbmDev& P, const OpDev* op, const RbmDev* PP,
     OpDev o = op ? *op : OpDev{};
     const int has = op != nullptr;
     RbmDev pp = PP ? *PP : P;
+    if (has && (L.flags & ~(EST_ELOC | EST_ENUMERATE)) == 0) {
+        switch (nw) {
+            case 1: rbm_eloc_kernel<K, 1><<<grid, block, 0, st>>>(P, o, L); break;
+            case 2: rbm_eloc_kernel<K, 2><<<grid, block, 0, st>>>(P, o, L); break;
+            case 3: rbm_eloc_kernel<K, 3><<<grid, block, 0, st>>>(P, o, L); break;
+            case 4: rbm_eloc_kernel<K, 4><<<grid, block, 0, st>>>(P, o, L); break;
+            default: return cudaErrorInvalidValue;
+        }
+        return cudaGetLastError();
+    }
     switch (nw) {
         case 1: rbm_est_kernel<K, 1><<<grid, block, 0, st>>>(P, o, has, pp, L); break;
         case 2: rbm_est_kernel<K, 2><<<grid, block, 0, st>>>(P, o, has, pp, L); break;
