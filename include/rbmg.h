@@ -196,6 +196,20 @@ RBMG_API int rbmg_chain_state(const rbmg_chain* chain, uint64_t* spins, uint64_t
 /* the library's CUDA stream of the calling thread, as a cudaStream_t */
 RBMG_API int rbmg_stream(void** stream);
 
+/* <op> under ExactSummation(num_spins) for a complex RBM -- the value rbmg_ev_value returns
+ * for an ExactSummation ensemble -- computed without allocating any device memory.
+ * No counterpart in the reference: it is for callers that cannot call cudaMalloc, such as a
+ * framework that owns all device memory through its own pool, or a latency-critical loop
+ * that cannot afford the device-wide synchronisation of cudaFree.
+ * The scratch is a fixed 1 MiB array in device global memory, held by every GPU that loads
+ * the library until the process exits; it limits num_spins to 14 (larger sizes return
+ * RBMG_EINVAL).  The first call on a device looks up the array's address with
+ * cudaGetSymbolAddress (set-up done once per device, on the current device), so make that
+ * first call before any stream capture.  Every call uses
+ * the same array: calls that overlap on the GPU (other host threads, other streams) race. */
+RBMG_API int rbmg_ev_value_exact_noalloc(const rbmg_psi* psi, const rbmg_operator* op, int num_spins,
+                                         double* value /* [2] */);
+
 /* FP32 FMA throughput of the current device in TFLOP/s (a probe kernel of `iters`
  * x 128 independent FMAs per thread), the roofline denominator of the sampler. */
 RBMG_API int rbmg_probe_fp32_tflops(int iters, double* tflops);

@@ -76,6 +76,7 @@ SIGNATURES = {
     "rbmg_chain_state": [_vp, _u64p, _u64p, _u64p],
     "rbmg_stream": [_vpp],
     "rbmg_probe_fp32_tflops": [C.c_int, _dp],
+    "rbmg_ev_value_exact_noalloc": [_vp, _vp, C.c_int, _dp],
 }
 _RESTYPE = {"rbmg_last_error": C.c_char_p, "rbmg_version": C.c_char_p}
 
