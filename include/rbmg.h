@@ -210,6 +210,37 @@ RBMG_API int rbmg_stream(void** stream);
 RBMG_API int rbmg_ev_value_exact_noalloc(const rbmg_psi* psi, const rbmg_operator* op, int num_spins,
                                          double* value /* [2] */);
 
+/* ---------------------------------------------------------------- learned proposal
+ * Extension (no reference counterpart): an MLP on the spins (BF16 operands, FP32
+ * accumulation; N -> 256 -> 256 SiLU -> N seed + 8 length logits) proposes flipping the
+ * contiguous cluster {i, ..., i+l-1}; the Metropolis-Hastings ratio includes the forward and
+ * reverse proposal densities, so the chain's stationary law stays |psi|^2 (the step of
+ * include/spin_ensembles/MonteCarloLoop.hpp:153-256 with a different proposal).  The net
+ * is trained online by REINFORCE (reward min(1, a) * l) with Adam. */
+typedef struct rbmg_proposal rbmg_proposal;
+RBMG_API int rbmg_proposal_create(int N, uint64_t seed, float lr, rbmg_proposal** out);
+RBMG_API int rbmg_proposal_destroy(rbmg_proposal* proposal);
+RBMG_API int rbmg_proposal_num_params(const rbmg_proposal* proposal, int64_t* num_params);
+/* parameters, FP32, order W1 [N][256], b1, W2 [256][256], b2, W3 [256][N+8], b3 */
+RBMG_API int rbmg_proposal_get_params(const rbmg_proposal* proposal, float* params);
+RBMG_API int rbmg_proposal_set_params(rbmg_proposal* proposal, const float* params);
+/* forward on `count` configurations -> logits [count][N+8]; with dlogits [count][N+8] also
+ * the backward pass -> grads [num_params] (host buffers; a test hook of the kernels) */
+RBMG_API int rbmg_proposal_eval(rbmg_proposal* proposal, int count, const uint64_t* spins, const float* dlogits,
+                                float* logits, float* grads);
+/* one Adam step (lr of the proposal, beta 0.9 / 0.999, eps 1e-8) with the given gradient */
+RBMG_API int rbmg_proposal_adam(rbmg_proposal* proposal, const float* grads);
+/* n_steps learned Metropolis-Hastings steps of every walker of the chain.  train = 0 keeps
+ * the weights (the chain is then exactly |psi|^2-stationary); train > 0 follows every step
+ * with one REINFORCE + Adam update on the moves of the first `train` walkers (adaptive
+ * chain: use it to train, then measure with train = 0).  Local energies every
+ * measure_every steps into d_eloc_out [n_steps / measure_every][walkers] (device double2),
+ * as in rbmg_chain_sweep_async.  N must exceed 8. */
+RBMG_API int rbmg_chain_learned_async(rbmg_chain* chain, const rbmg_psi* psi, const rbmg_operator* op,
+                                      rbmg_proposal* proposal, int n_steps, int train, int measure_every,
+                                      void* d_eloc_out, void* stream);
+
+
 /* FP32 FMA throughput of the current device in TFLOP/s (a probe kernel of `iters`
  * x 128 independent FMAs per thread), the roofline denominator of the sampler. */
 RBMG_API int rbmg_probe_fp32_tflops(int iters, double* tflops);

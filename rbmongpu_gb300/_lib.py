@@ -77,6 +77,14 @@ SIGNATURES = {
     "rbmg_stream": [_vpp],
     "rbmg_probe_fp32_tflops": [C.c_int, _dp],
     "rbmg_ev_value_exact_noalloc": [_vp, _vp, C.c_int, _dp],
+    "rbmg_proposal_create": [C.c_int, C.c_uint64, C.c_float, _vpp],
+    "rbmg_proposal_destroy": [_vp],
+    "rbmg_proposal_num_params": [_vp, C.POINTER(C.c_int64)],
+    "rbmg_proposal_get_params": [_vp, C.POINTER(C.c_float)],
+    "rbmg_proposal_set_params": [_vp, C.POINTER(C.c_float)],
+    "rbmg_proposal_eval": [_vp, C.c_int, _u64p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float)],
+    "rbmg_proposal_adam": [_vp, C.POINTER(C.c_float)],
+    "rbmg_chain_learned_async": [_vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_int, _vp, _vp],
 }
 _RESTYPE = {"rbmg_last_error": C.c_char_p, "rbmg_version": C.c_char_p}
 

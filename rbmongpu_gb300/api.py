@@ -584,11 +584,80 @@ class Chain:
              int(n_sweeps), int(measure_every), C.c_void_p(d_eloc) if d_eloc else None,
              C.c_void_p(stream) if stream else None)
 
+    def learned_async(self, psi, operator_, proposal, n_steps, train=0, measure_every=1, d_eloc=0, stream=None):
+        """n_steps learned Metropolis-Hastings steps (cluster flips picked by `proposal`).
+        train > 0: one REINFORCE + Adam update per step on the first `train` walkers' moves;
+        train = 0: frozen proposal, exactly |psi|^2-stationary.  d_eloc: device address of
+        double2 [n_steps // measure_every][walkers], or 0."""
+        call("rbmg_chain_learned_async", self._h, psi._h, operator_._h if operator_ is not None else None,
+             proposal._h, int(n_steps), int(train), int(measure_every), C.c_void_p(d_eloc) if d_eloc else None,
+             C.c_void_p(stream) if stream else None)
+
     def state(self):
         sp = np.zeros((self.num_walkers, nwords(self.N)), np.uint64)
         a, p = C.c_uint64(), C.c_uint64()
         call("rbmg_chain_state", self._h, _p(sp, _u64p), C.byref(a), C.byref(p))
         return sp, a.value, p.value
+
+
+class Proposal:
+    """Learned cluster-flip proposal (extension): an MLP N -> 256 -> 256 (SiLU) -> N seed +
+    8 length logits with BF16 operands and FP32 accumulation, trained by the chain
+    (Chain.learned_async).  Parameters are FP32 in the order W1 [N][256], b1, W2 [256][256],
+    b2, W3 [256][N+8], b3."""
+
+    HIDDEN = 256
+    LENGTHS = 8
+
+    def __init__(self, N, seed=0, lr=1e-3):
+        h = _handle()
+        call("rbmg_proposal_create", int(N), int(seed), float(lr), C.byref(h))
+        self._h = h
+        self.N = int(N)
+        n = C.c_int64()
+        call("rbmg_proposal_num_params", h, C.byref(n))
+        self.num_params = n.value
+
+    def __del__(self):
+        h, self._h = getattr(self, "_h", None), None
+        if h is not None:
+            try:
+                lib().rbmg_proposal_destroy(h)
+            except Exception:
+                pass
+
+    @property
+    def params(self):
+        out = np.zeros(self.num_params, np.float32)
+        call("rbmg_proposal_get_params", self._h, _p(out, C.POINTER(C.c_float)))
+        return out
+
+    @params.setter
+    def params(self, v):
+        v = np.ascontiguousarray(v, np.float32)
+        if v.shape != (self.num_params,):
+            raise ValueError(f"expected {self.num_params} parameters")
+        call("rbmg_proposal_set_params", self._h, _p(v, C.POINTER(C.c_float)))
+
+    def eval(self, spins, dlogits=None):
+        """Forward pass on configurations (uint64 words [count][nwords]) -> logits
+        [count][N+8]; with dlogits also the parameter gradient of sum(dlogits * logits)."""
+        sp = np.ascontiguousarray(spins, np.uint64).reshape(-1, nwords(self.N))
+        count = sp.shape[0]
+        logits = np.zeros((count, self.N + self.LENGTHS), np.float32)
+        fp = C.POINTER(C.c_float)
+        if dlogits is None:
+            call("rbmg_proposal_eval", self._h, count, _p(sp, _u64p), None, _p(logits, fp), None)
+            return logits
+        dl = np.ascontiguousarray(dlogits, np.float32).reshape(count, self.N + self.LENGTHS)
+        grads = np.zeros(self.num_params, np.float32)
+        call("rbmg_proposal_eval", self._h, count, _p(sp, _u64p), _p(dl, fp), _p(logits, fp), _p(grads, fp))
+        return logits, grads
+
+    def adam(self, grads):
+        """One Adam step (betas 0.9 / 0.999, eps 1e-8) with the given gradient."""
+        g = np.ascontiguousarray(grads, np.float32)
+        call("rbmg_proposal_adam", self._h, _p(g, C.POINTER(C.c_float)))
 
 
 def library_stream():

@@ -58,7 +58,6 @@ static Workspace& ws() {
     return w;
 }
 
-static int nwords_of(int N) { return (N + 63) / 64; }
 
 }  // namespace rbmg
 
@@ -1307,14 +1306,6 @@ extern "C" int rbmg_psi_O_k_vector(const rbmg_psi* psi, const uint64_t* spins, d
 }
 
 // ====================================================================== persistent chains
-struct rbmg_chain {
-    int N = 0, nw = 0;
-    uint32_t walkers = 0;
-    uint64_t seed = 0;
-    DevBuf spins, rng_index, accepts, proposals;
-    bool initialised = false;
-};
-
 extern "C" int rbmg_stream(void** st) {
     if (!st) return fail(RBMG_EINVAL, "stream: null");
     *st = static_cast<void*>(stream());

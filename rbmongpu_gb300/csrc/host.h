@@ -55,6 +55,8 @@ struct DevBuf {
 
 cudaStream_t stream();
 
+inline int nwords_of(int N) { return (N + 63) / 64; }
+
 struct DeepLayerHost {
     int size = 0, conn = 0;
     std::vector<uint32_t> connections;   // [conn][size]
@@ -135,4 +137,15 @@ struct rbmg_ensemble {
     rbmg::DevBuf d_allowed;
 
     uint64_t num_steps() const;
+};
+
+// walkers that persist on the device between calls (capi.cu); the learned-proposal
+// steps (proposal.cu) keep their angles and logits in `learned`
+struct rbmg_chain {
+    int N = 0, nw = 0;
+    uint32_t walkers = 0;
+    uint64_t seed = 0;
+    rbmg::DevBuf spins, rng_index, accepts, proposals;
+    bool initialised = false;
+    std::shared_ptr<void> learned;
 };

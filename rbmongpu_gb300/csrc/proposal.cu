@@ -1,0 +1,998 @@
+// Learned Metropolis-Hastings proposal for the complex-RBM chain (extension: the
+// reference proposes single spin flips only, include/spin_ensembles/MonteCarloLoop.hpp:153-256).
+//
+// An MLP on the walker's spins, N -> 256 -> 256 (SiLU) -> N + 8 logits, picks a seed site
+// i (softmax over the first N logits) and a cluster length l in 1..8 (softmax over the
+// last 8); the move flips the contiguous periodic cluster {i, ..., i+l-1}.  For l < N the
+// cluster determines (i, l), so q(s'|s) = p_s(i) p_s(l) and the reverse move has
+// q(s|s') = p_s'(i) p_s'(l): the acceptance min(1, |psi(s')/psi(s)|^2 q(s|s')/q(s'|s))
+// keeps |psi|^2 stationary for any network weights.
+//
+// The network runs in BF16 operands with FP32 accumulation on the tensor cores
+// (mma.sync m16n8k16); forward, backward and Adam are kernels of this file.  It is
+// trained online by REINFORCE on the chain's own moves, reward = min(1, a) * l (expected
+// number of spins flipped), with the batch-mean baseline and an entropy bonus.
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include <cuda_bf16.h>
+
+#include "host.h"
+#include "rbm_impl.cuh"
+
+namespace rbmg {
+
+using bf16 = __nv_bfloat16;
+
+constexpr int kHidden = 256;
+constexpr int kLengths = 8;
+constexpr float kEntropyBonus = 0.01f;
+
+inline int pad8(int x) { return (x + 7) & ~7; }
+
+// ============================================================================ GEMM
+// C[M][N] = A[M][K] B[K][N] with BF16 operands and FP32 accumulation.  A is stored
+// [m][k] (A_MK) or [k][m] (A_KM), B is stored [n][k] (B_NK) or [k][n] (B_KN); leading
+// dimensions are multiples of 8 elements and 16-byte aligned.  Columns past K inside a
+// row's leading dimension must hold zeros (they enter the sums); columns past M or N
+// are only read, never stored.
+enum : int { A_MK = 0, A_KM = 1 };
+enum : int { B_NK = 0, B_KN = 1 };
+enum : int {
+    EPI_F32 = 0,     // C32 = acc + bias
+    EPI_SILU = 1,    // C32 = z = acc + bias, C16 = bf16(silu(z))
+    EPI_DSILU = 2,   // C32 = dz = acc * silu'(Z), C16 = bf16(dz)
+    EPI_PARTIAL = 3  // C32[split] = acc (split-K partial sums)
+};
+
+struct GemmArgs {
+    int M, N, K;
+    const bf16* A;
+    int lda;
+    const bf16* B;
+    int ldb;
+    int k_per_split;     // multiple of kBK
+    const float* bias;   // [N] or null
+    float* C32;
+    int ldc;
+    bf16* C16;
+    int ldc16;
+    const float* Z;
+    int ldz;
+    long split_stride;   // elements between the partial sums of consecutive splits
+};
+
+constexpr int kBM = 128, kBN = 64, kBK = 32, kSK = kBK + 8, kGemmThreads = 256;
+
+__device__ __forceinline__ float silu_f(float z) { return z / (1.0f + expf(-z)); }
+__device__ __forceinline__ float dsilu_f(float z) {
+    const float sg = 1.0f / (1.0f + expf(-z));
+    return sg * (1.0f + z * (1.0f - sg));
+}
+
+__device__ __forceinline__ void mma_bf16_16816(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+template <int LA, int LB, int EPI>
+__global__ void __launch_bounds__(kGemmThreads) gemm_bf16_kernel(GemmArgs g) {
+    __shared__ __align__(16) bf16 sA[kBM][kSK];
+    __shared__ __align__(16) bf16 sB[kBN][kSK];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int wm = warp & 3, wn = warp >> 2;       // 4 x 2 warps, 32 x 32 each
+    const int gq = lane >> 2, tq = lane & 3;
+    const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * kBN;
+    const int kbeg = blockIdx.z * g.k_per_split;
+    const int kend = min(g.K, kbeg + g.k_per_split);
+    float acc[2][4][4];
+#pragma unroll
+    for (int i = 0; i < 2; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+#pragma unroll
+            for (int e = 0; e < 4; e++) acc[i][j][e] = 0.0f;
+    const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
+    for (int k0 = kbeg; k0 < kend; k0 += kBK) {
+        // ---- stage A as sA[m][k]
+        if (LA == A_MK) {
+            for (int c = tid; c < kBM * (kBK / 8); c += kGemmThreads) {
+                const int r = c >> 2, kc = (c & 3) * 8;
+                const int m = m0 + r, k = k0 + kc;
+                uint4 v = zero;
+                if (m < g.M && k < kend) v = *reinterpret_cast<const uint4*>(g.A + static_cast<long>(m) * g.lda + k);
+                *reinterpret_cast<uint4*>(&sA[r][kc]) = v;
+            }
+        } else {
+            for (int c = tid; c < kBK * (kBM / 8); c += kGemmThreads) {
+                const int kk = c / (kBM / 8), mc = (c % (kBM / 8)) * 8;
+                const int k = k0 + kk, m = m0 + mc;
+                uint4 v = zero;
+                if (k < kend && m < g.M) v = *reinterpret_cast<const uint4*>(g.A + static_cast<long>(k) * g.lda + m);
+                const bf16* e = reinterpret_cast<const bf16*>(&v);
+#pragma unroll
+                for (int q = 0; q < 8; q++) sA[mc + q][kk] = e[q];
+            }
+        }
+        // ---- stage B as sB[n][k]
+        if (LB == B_NK) {
+            for (int c = tid; c < kBN * (kBK / 8); c += kGemmThreads) {
+                const int r = c >> 2, kc = (c & 3) * 8;
+                const int n = n0 + r, k = k0 + kc;
+                uint4 v = zero;
+                if (n < g.N && k < kend) v = *reinterpret_cast<const uint4*>(g.B + static_cast<long>(n) * g.ldb + k);
+                *reinterpret_cast<uint4*>(&sB[r][kc]) = v;
+            }
+        } else {
+            for (int c = tid; c < kBK * (kBN / 8); c += kGemmThreads) {
+                const int kk = c / (kBN / 8), nc = (c % (kBN / 8)) * 8;
+                const int k = k0 + kk, n = n0 + nc;
+                uint4 v = zero;
+                if (k < kend && n < g.N) v = *reinterpret_cast<const uint4*>(g.B + static_cast<long>(k) * g.ldb + n);
+                const bf16* e = reinterpret_cast<const bf16*>(&v);
+#pragma unroll
+                for (int q = 0; q < 8; q++) sB[nc + q][kk] = e[q];
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int ks = 0; ks < kBK; ks += 16) {
+            uint32_t af[2][4], bfr[4][2];
+#pragma unroll
+            for (int mi = 0; mi < 2; mi++) {
+                const int row = wm * 32 + mi * 16 + gq;
+                af[mi][0] = *reinterpret_cast<const uint32_t*>(&sA[row][ks + 2 * tq]);
+                af[mi][1] = *reinterpret_cast<const uint32_t*>(&sA[row + 8][ks + 2 * tq]);
+                af[mi][2] = *reinterpret_cast<const uint32_t*>(&sA[row][ks + 2 * tq + 8]);
+                af[mi][3] = *reinterpret_cast<const uint32_t*>(&sA[row + 8][ks + 2 * tq + 8]);
+            }
+#pragma unroll
+            for (int ni = 0; ni < 4; ni++) {
+                const int col = wn * 32 + ni * 8 + gq;
+                bfr[ni][0] = *reinterpret_cast<const uint32_t*>(&sB[col][ks + 2 * tq]);
+                bfr[ni][1] = *reinterpret_cast<const uint32_t*>(&sB[col][ks + 2 * tq + 8]);
+            }
+#pragma unroll
+            for (int mi = 0; mi < 2; mi++)
+#pragma unroll
+                for (int ni = 0; ni < 4; ni++) mma_bf16_16816(acc[mi][ni], af[mi], bfr[ni]);
+        }
+        __syncthreads();
+    }
+    // ---- epilogue: acc[mi][ni][h * 2 + e] is C[row g + 8 h][col 2 t + e] of the tile
+#pragma unroll
+    for (int mi = 0; mi < 2; mi++)
+#pragma unroll
+        for (int ni = 0; ni < 4; ni++)
+#pragma unroll
+            for (int h = 0; h < 2; h++)
+#pragma unroll
+                for (int e = 0; e < 2; e++) {
+                    const int m = m0 + wm * 32 + mi * 16 + gq + 8 * h;
+                    const int n = n0 + wn * 32 + ni * 8 + 2 * tq + e;
+                    if (m >= g.M || n >= g.N) continue;
+                    const float a = acc[mi][ni][h * 2 + e];
+                    if (EPI == EPI_F32) {
+                        g.C32[static_cast<long>(m) * g.ldc + n] = a + (g.bias ? g.bias[n] : 0.0f);
+                    } else if (EPI == EPI_SILU) {
+                        const float z = a + g.bias[n];
+                        g.C32[static_cast<long>(m) * g.ldc + n] = z;
+                        g.C16[static_cast<long>(m) * g.ldc16 + n] = __float2bfloat16_rn(silu_f(z));
+                    } else if (EPI == EPI_DSILU) {
+                        const float dz = a * dsilu_f(g.Z[static_cast<long>(m) * g.ldz + n]);
+                        g.C32[static_cast<long>(m) * g.ldc + n] = dz;
+                        g.C16[static_cast<long>(m) * g.ldc16 + n] = __float2bfloat16_rn(dz);
+                    } else {
+                        g.C32[blockIdx.z * g.split_stride + static_cast<long>(m) * g.ldc + n] = a;
+                    }
+                }
+}
+
+template <int LA, int LB, int EPI>
+cudaError_t gemm(const GemmArgs& g, int splits, cudaStream_t st) {
+    if (g.M <= 0 || g.N <= 0) return cudaSuccess;
+    const dim3 grid((g.M + kBM - 1) / kBM, (g.N + kBN - 1) / kBN, splits);
+    gemm_bf16_kernel<LA, LB, EPI><<<grid, kGemmThreads, 0, st>>>(g);
+    return cudaGetLastError();
+}
+
+// out[m * ldo + n] = sum over splits s (in order) of part[s][m * ldp + n]
+__global__ void split_reduce_kernel(const float* part, int splits, long stride, int M, int N, int ldp, float* out,
+                                    int ldo) {
+    const long t = static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= static_cast<long>(M) * N) return;
+    const int m = static_cast<int>(t / N), n = static_cast<int>(t % N);
+    float s = 0.0f;
+    for (int q = 0; q < splits; q++) s += part[q * stride + static_cast<long>(m) * ldp + n];
+    out[static_cast<long>(m) * ldo + n] = s;
+}
+
+// column sums of X[rows][ld] (first `cols` columns), two passes in a fixed order
+constexpr int kColChunks = 64;
+__global__ void colsum_partial_kernel(const float* X, int rows, int cols, int ld, float* part) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= cols) return;
+    const int per = (rows + kColChunks - 1) / kColChunks;
+    const int r0 = blockIdx.y * per, r1 = min(rows, r0 + per);
+    float s = 0.0f;
+    for (int r = r0; r < r1; r++) s += X[static_cast<long>(r) * ld + n];
+    part[blockIdx.y * cols + n] = s;
+}
+
+__global__ void colsum_final_kernel(const float* part, int cols, float* out) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= cols) return;
+    float s = 0.0f;
+    for (int q = 0; q < kColChunks; q++) s += part[q * cols + n];
+    out[n] = s;
+}
+
+// x[b][i] = +-1 (bf16) for i < N, 0 up to the padded width
+template <int NW>
+__global__ void spins_to_x_kernel(const uint64_t* spins, int count, int N, int Np, bf16* x) {
+    const long t = static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= static_cast<long>(count) * Np) return;
+    const long b = t / Np;
+    const int i = static_cast<int>(t % Np);
+    float v = 0.0f;
+    if (i < N) v = ((spins[b * NW + (i >> 6)] >> (i & 63)) & 1ull) ? 1.0f : -1.0f;
+    x[t] = __float2bfloat16_rn(v);
+}
+
+// dl16[b][j] = bf16(dl32[b][j]) for j < O, 0 up to Op
+__global__ void to_bf16_padded_kernel(const float* src, int rows, int cols, int ldd, bf16* dst) {
+    const long t = static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= static_cast<long>(rows) * ldd) return;
+    const long r = t / ldd;
+    const int c = static_cast<int>(t % ldd);
+    dst[t] = __float2bfloat16_rn(c < cols ? src[r * cols + c] : 0.0f);
+}
+
+// Adam (Kingma & Ba 2015) with bias correction bc1 = 1 - beta1^t, bc2 = 1 - beta2^t
+__global__ void adam_kernel(float* p, const float* g, float* m, float* v, long n, float lr, float bc1, float bc2) {
+    const long t = static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const float gt = g[t];
+    const float mt = 0.9f * m[t] + 0.1f * gt;
+    const float vt = 0.999f * v[t] + 0.001f * gt * gt;
+    m[t] = mt;
+    v[t] = vt;
+    p[t] -= lr * (mt / bc1) / (sqrtf(vt / bc2) + 1e-8f);
+}
+
+// bf16 copy of a [rows][cols] FP32 matrix into [rows][ldd] (pad columns zero)
+__global__ void weights_to_bf16_kernel(const float* w, int rows, int cols, int ldd, bf16* out) {
+    const long t = static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= static_cast<long>(rows) * ldd) return;
+    const long r = t / ldd;
+    const int c = static_cast<int>(t % ldd);
+    out[t] = __float2bfloat16_rn(c < cols ? w[r * cols + c] : 0.0f);
+}
+
+inline unsigned blocks_for(long n, int threads = 256) { return static_cast<unsigned>((n + threads - 1) / threads); }
+
+}  // namespace rbmg
+
+// ============================================================================ the network
+struct rbmg_proposal {
+    int N = 0, O = 0, Np = 0, Op = 0;
+    float lr = 1e-3f;
+    long steps = 0;   // Adam steps taken
+    int64_t P = 0;
+    size_t oW1 = 0, ob1 = 0, oW2 = 0, ob2 = 0, oW3 = 0, ob3 = 0;   // offsets in the FP32 parameter vector
+    rbmg::DevBuf master, adam_m, adam_v, grad;
+    rbmg::DevBuf w1, w2, w3;            // bf16 [N][H], [H][H], [H][Op]
+    int cap = 0;                        // activation rows held
+    rbmg::DevBuf x16, z1, h1, z2, h2;   // [cap][Np] bf16, [cap][H] f32 / bf16
+    rbmg::DevBuf logits;                // [cap][O] f32 (training forward)
+    rbmg::DevBuf dl32, dl16, dz2_32, dz2_16, dz1_32, dz1_16;
+    rbmg::DevBuf partial, colpart;
+};
+
+namespace rbmg {
+
+int proposal_reserve(rbmg_proposal* p, int rows) {
+    if (rows <= p->cap) return RBMG_OK;
+    const size_t r = static_cast<size_t>(rows);
+    RBMG_CK(p->x16.ensure(sizeof(bf16) * r * p->Np));
+    RBMG_CK(p->z1.ensure(sizeof(float) * r * kHidden));
+    RBMG_CK(p->h1.ensure(sizeof(bf16) * r * kHidden));
+    RBMG_CK(p->z2.ensure(sizeof(float) * r * kHidden));
+    RBMG_CK(p->h2.ensure(sizeof(bf16) * r * kHidden));
+    RBMG_CK(p->logits.ensure(sizeof(float) * r * p->O));
+    RBMG_CK(p->dl32.ensure(sizeof(float) * r * p->O));
+    RBMG_CK(p->dl16.ensure(sizeof(bf16) * r * p->Op));
+    RBMG_CK(p->dz2_32.ensure(sizeof(float) * r * kHidden));
+    RBMG_CK(p->dz2_16.ensure(sizeof(bf16) * r * kHidden));
+    RBMG_CK(p->dz1_32.ensure(sizeof(float) * r * kHidden));
+    RBMG_CK(p->dz1_16.ensure(sizeof(bf16) * r * kHidden));
+    p->cap = rows;
+    return RBMG_OK;
+}
+
+cudaError_t proposal_refresh_bf16(rbmg_proposal* p, cudaStream_t st) {
+    const float* w = p->master.as<float>();
+    weights_to_bf16_kernel<<<blocks_for(static_cast<long>(p->N) * kHidden), 256, 0, st>>>(w + p->oW1, p->N, kHidden,
+                                                                                          kHidden, p->w1.as<bf16>());
+    weights_to_bf16_kernel<<<blocks_for(static_cast<long>(kHidden) * kHidden), 256, 0, st>>>(
+        w + p->oW2, kHidden, kHidden, kHidden, p->w2.as<bf16>());
+    weights_to_bf16_kernel<<<blocks_for(static_cast<long>(kHidden) * p->Op), 256, 0, st>>>(w + p->oW3, kHidden, p->O,
+                                                                                         p->Op, p->w3.as<bf16>());
+    return cudaGetLastError();
+}
+
+// logits_out [count][O] of the configurations spins [count][nw]; activations kept in
+// the network's buffers for a following backward pass
+int proposal_forward(rbmg_proposal* p, int count, const uint64_t* spins, float* logits_out, cudaStream_t st) {
+    if (count <= 0) return RBMG_OK;
+    int r = proposal_reserve(p, count);
+    if (r != RBMG_OK) return r;
+    const int nw = nwords_of(p->N);
+    const long xs = static_cast<long>(count) * p->Np;
+    switch (nw) {
+        case 1: spins_to_x_kernel<1><<<blocks_for(xs), 256, 0, st>>>(spins, count, p->N, p->Np, p->x16.as<bf16>()); break;
+        case 2: spins_to_x_kernel<2><<<blocks_for(xs), 256, 0, st>>>(spins, count, p->N, p->Np, p->x16.as<bf16>()); break;
+        case 3: spins_to_x_kernel<3><<<blocks_for(xs), 256, 0, st>>>(spins, count, p->N, p->Np, p->x16.as<bf16>()); break;
+        default: spins_to_x_kernel<4><<<blocks_for(xs), 256, 0, st>>>(spins, count, p->N, p->Np, p->x16.as<bf16>()); break;
+    }
+    RBMG_CK(cudaGetLastError());
+    const float* w = p->master.as<float>();
+    GemmArgs g{};
+    g.M = count;
+    g.N = kHidden;
+    g.K = p->N;
+    g.A = p->x16.as<bf16>();
+    g.lda = p->Np;
+    g.B = p->w1.as<bf16>();
+    g.ldb = kHidden;
+    g.k_per_split = (g.K + kBK - 1) / kBK * kBK;
+    g.bias = w + p->ob1;
+    g.C32 = p->z1.as<float>();
+    g.ldc = kHidden;
+    g.C16 = p->h1.as<bf16>();
+    g.ldc16 = kHidden;
+    RBMG_CK((gemm<A_MK, B_KN, EPI_SILU>(g, 1, st)));
+    g.K = kHidden;
+    g.A = p->h1.as<bf16>();
+    g.lda = kHidden;
+    g.B = p->w2.as<bf16>();
+    g.k_per_split = kHidden;
+    g.bias = w + p->ob2;
+    g.C32 = p->z2.as<float>();
+    g.C16 = p->h2.as<bf16>();
+    RBMG_CK((gemm<A_MK, B_KN, EPI_SILU>(g, 1, st)));
+    g.N = p->O;
+    g.A = p->h2.as<bf16>();
+    g.B = p->w3.as<bf16>();
+    g.ldb = p->Op;
+    g.bias = w + p->ob3;
+    g.C32 = logits_out;
+    g.ldc = p->O;
+    g.C16 = nullptr;
+    RBMG_CK((gemm<A_MK, B_KN, EPI_F32>(g, 1, st)));
+    return RBMG_OK;
+}
+
+// dW = A^T dZ over `count` rows (split-K partials, reduced in a fixed order) into grad
+static int weight_grad(rbmg_proposal* p, int count, const bf16* A, int lda, int Mrows, const bf16* dZ, int ldz,
+                       int Ncols, float* out, cudaStream_t st) {
+    const int tiles = ((Mrows + kBM - 1) / kBM) * ((Ncols + kBN - 1) / kBN);
+    const int kchunks = (count + kBK - 1) / kBK;
+    int splits = std::max(1, std::min(kchunks, (2 * 152 + tiles - 1) / tiles));
+    const int per = (kchunks + splits - 1) / splits * kBK;
+    splits = (count + per - 1) / per;
+    const long stride = static_cast<long>(Mrows) * Ncols;
+    RBMG_CK(p->partial.ensure(sizeof(float) * stride * splits));
+    GemmArgs g{};
+    g.M = Mrows;
+    g.N = Ncols;
+    g.K = count;
+    g.A = A;
+    g.lda = lda;
+    g.B = dZ;
+    g.ldb = ldz;
+    g.k_per_split = per;
+    g.C32 = p->partial.as<float>();
+    g.ldc = Ncols;
+    g.split_stride = stride;
+    RBMG_CK((gemm<A_KM, B_KN, EPI_PARTIAL>(g, splits, st)));
+    split_reduce_kernel<<<blocks_for(stride), 256, 0, st>>>(p->partial.as<float>(), splits, stride, Mrows, Ncols, Ncols,
+                                                            out, Ncols);
+    RBMG_CK(cudaGetLastError());
+    return RBMG_OK;
+}
+
+static int bias_grad(rbmg_proposal* p, const float* X, int rows, int cols, float* out, cudaStream_t st) {
+    RBMG_CK(p->colpart.ensure(sizeof(float) * kColChunks * cols));
+    colsum_partial_kernel<<<dim3(blocks_for(cols), kColChunks), 256, 0, st>>>(X, rows, cols, cols,
+                                                                            p->colpart.as<float>());
+    colsum_final_kernel<<<blocks_for(cols), 256, 0, st>>>(p->colpart.as<float>(), cols, out);
+    RBMG_CK(cudaGetLastError());
+    return RBMG_OK;
+}
+
+// gradient of sum_b sum_j dl32[b][j] logits[b][j] with respect to all parameters, for
+// the activations of the last proposal_forward over `count` rows -> p->grad
+int proposal_backward(rbmg_proposal* p, int count, cudaStream_t st) {
+    float* gr = p->grad.as<float>();
+    const long n16 = static_cast<long>(count) * p->Op;
+    to_bf16_padded_kernel<<<blocks_for(n16), 256, 0, st>>>(p->dl32.as<float>(), count, p->O, p->Op,
+                                                           p->dl16.as<bf16>());
+    RBMG_CK(cudaGetLastError());
+    int r = weight_grad(p, count, p->h2.as<bf16>(), kHidden, kHidden, p->dl16.as<bf16>(), p->Op, p->O, gr + p->oW3, st);
+    if (r != RBMG_OK) return r;
+    r = bias_grad(p, p->dl32.as<float>(), count, p->O, gr + p->ob3, st);
+    if (r != RBMG_OK) return r;
+    GemmArgs g{};
+    g.M = count;
+    g.N = kHidden;
+    g.K = p->O;
+    g.A = p->dl16.as<bf16>();
+    g.lda = p->Op;
+    g.B = p->w3.as<bf16>();
+    g.ldb = p->Op;
+    g.k_per_split = (p->O + kBK - 1) / kBK * kBK;
+    g.Z = p->z2.as<float>();
+    g.ldz = kHidden;
+    g.C32 = p->dz2_32.as<float>();
+    g.ldc = kHidden;
+    g.C16 = p->dz2_16.as<bf16>();
+    g.ldc16 = kHidden;
+    RBMG_CK((gemm<A_MK, B_NK, EPI_DSILU>(g, 1, st)));
+    r = weight_grad(p, count, p->h1.as<bf16>(), kHidden, kHidden, p->dz2_16.as<bf16>(), kHidden, kHidden, gr + p->oW2,
+                    st);
+    if (r != RBMG_OK) return r;
+    r = bias_grad(p, p->dz2_32.as<float>(), count, kHidden, gr + p->ob2, st);
+    if (r != RBMG_OK) return r;
+    g.K = kHidden;
+    g.A = p->dz2_16.as<bf16>();
+    g.lda = kHidden;
+    g.B = p->w2.as<bf16>();
+    g.ldb = kHidden;
+    g.k_per_split = kHidden;
+    g.Z = p->z1.as<float>();
+    g.C32 = p->dz1_32.as<float>();
+    g.C16 = p->dz1_16.as<bf16>();
+    RBMG_CK((gemm<A_MK, B_NK, EPI_DSILU>(g, 1, st)));
+    r = weight_grad(p, count, p->x16.as<bf16>(), p->Np, p->N, p->dz1_16.as<bf16>(), kHidden, kHidden, gr + p->oW1, st);
+    if (r != RBMG_OK) return r;
+    return bias_grad(p, p->dz1_32.as<float>(), count, kHidden, gr + p->ob1, st);
+}
+
+int proposal_adam(rbmg_proposal* p, cudaStream_t st) {
+    p->steps++;
+    const double bc1 = 1.0 - std::pow(0.9, static_cast<double>(p->steps));
+    const double bc2 = 1.0 - std::pow(0.999, static_cast<double>(p->steps));
+    adam_kernel<<<blocks_for(p->P), 256, 0, st>>>(p->master.as<float>(), p->grad.as<float>(), p->adam_m.as<float>(),
+                                                  p->adam_v.as<float>(), p->P, p->lr, static_cast<float>(bc1),
+                                                  static_cast<float>(bc2));
+    RBMG_CK(cudaGetLastError());
+    RBMG_CK(proposal_refresh_bf16(p, st));
+    return RBMG_OK;
+}
+
+// ============================================================================ chain kernels
+// log-normalisers of the seed and length softmaxes of one logits row (warp-wide,
+// identical in every lane; the same function serves the forward and the reverse
+// density, so both see bit-identical values for identical logits)
+struct LogNorm {
+    float seed, len;
+};
+
+__device__ __forceinline__ LogNorm log_norms(const float* row, int N, int lane) {
+    float m = -INFINITY;
+    for (int j = lane; j < N; j += 32) m = fmaxf(m, row[j]);
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, off));
+    float s = 0.0f;
+    for (int j = lane; j < N; j += 32) s += expf(row[j] - m);
+    s = warp_sum_xor(s);
+    const float vl = lane < kLengths ? row[N + lane] : -INFINITY;
+    float m2 = vl;
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) m2 = fmaxf(m2, __shfl_xor_sync(0xffffffffu, m2, off));
+    const float s2 = warp_sum_xor(lane < kLengths ? expf(vl - m2) : 0.0f);
+    return LogNorm{m + logf(s), m2 + logf(s2)};
+}
+
+// inverse-CDF draw from softmax(row[0..n)) with u in (0, 1]; entries are visited in
+// index order, 32 at a time
+__device__ __forceinline__ int draw_index(const float* row, int n, float lse, float u, int lane) {
+    const float target = u;
+    float base = 0.0f;
+    int last = 0;
+    for (int c = 0; c < n; c += 32) {
+        const int j = c + lane;
+        const float e = j < n ? expf(row[j] - lse) : 0.0f;
+        float x = e;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const float y = __shfl_up_sync(0xffffffffu, x, off);
+            if (lane >= off) x += y;
+        }
+        const float cum = base + x;
+        const unsigned hit = __ballot_sync(0xffffffffu, e > 0.0f && cum >= target);
+        if (hit) return c + __ffs(hit) - 1;
+        const unsigned pos = __ballot_sync(0xffffffffu, e > 0.0f);
+        if (pos) last = c + 31 - __clz(pos);
+        base += __shfl_sync(0xffffffffu, x, 31);
+    }
+    return last;
+}
+
+struct LearnedLaunch {
+    int B, N, O;
+    uint64_t seed;
+    uint64_t* spins;             // [B][NW] chain state
+    uint64_t* rng_index;         // [B]
+    uint64_t* spins_prop;        // [B][NW]
+    uint64_t* spins_pre;         // [B][NW] or null (training copy of the state the move started from)
+    int* site;                   // [B]
+    int* len;                    // [B]
+    float* logq_fwd;             // [B]
+    float* logits_cur;           // [B][O] logits at the current state
+    const float* logits_prop;    // [B][O] logits at the proposed state
+    float2* theta;               // [B][Mpad]
+    float* re;                   // [B][Mpad] Re f(theta)
+    float* reward;               // [B]
+    unsigned long long* accepts;
+    unsigned long long* proposals;
+};
+
+template <int K, int NW>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock) learned_angles_kernel(RbmDev P, LearnedLaunch L) {
+    const int lane = threadIdx.x & 31;
+    const int w = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+    if (w >= L.B) return;
+    Spins<NW> s;
+#pragma unroll
+    for (int k = 0; k < NW; k++) s.w[k] = L.spins[static_cast<long>(w) * NW + k];
+    float tr[K], ti[K];
+    rbm_refresh(P, s, tr, ti, lane);
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        const long o = static_cast<long>(w) * P.Mpad + lane + 32 * k;
+        L.theta[o] = make_float2(tr[k], ti[k]);
+        L.re[o] = lc_re(tr[k], ti[k]);
+    }
+}
+
+template <int NW>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock) learned_propose_kernel(LearnedLaunch L) {
+    const int lane = threadIdx.x & 31;
+    const int w = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+    if (w >= L.B) return;
+    WalkerRng rng;
+    rng.init(L.seed, static_cast<uint32_t>(w), L.rng_index[w]);
+    const float* row = L.logits_cur + static_cast<long>(w) * L.O;
+    const LogNorm ln = log_norms(row, L.N, lane);
+    const int i = draw_index(row, L.N, ln.seed, rng.uniform(), lane);
+    const int l = 1 + draw_index(row + L.N, kLengths, ln.len, rng.uniform(), lane);
+    if (lane == 0) {
+        Spins<NW> s;
+#pragma unroll
+        for (int k = 0; k < NW; k++) s.w[k] = L.spins[static_cast<long>(w) * NW + k];
+        if (L.spins_pre) {
+#pragma unroll
+            for (int k = 0; k < NW; k++) L.spins_pre[static_cast<long>(w) * NW + k] = s.w[k];
+        }
+        for (int q = 0; q < l; q++) {
+            int c = i + q;
+            if (c >= L.N) c -= L.N;
+            s.flip(c);
+        }
+#pragma unroll
+        for (int k = 0; k < NW; k++) L.spins_prop[static_cast<long>(w) * NW + k] = s.w[k];
+        L.site[w] = i;
+        L.len[w] = l;
+        L.logq_fwd[w] = (row[i] - ln.seed) + (row[L.N + l - 1] - ln.len);
+        L.rng_index[w] = rng.index;
+        L.proposals[w] += 1;
+    }
+}
+
+// Metropolis-Hastings test of the proposed cluster flip:
+// log a = 2 (Re log psi(s') - Re log psi(s)) + log q(s|s') - log q(s'|s)
+template <int K, int NW>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock) learned_accept_kernel(RbmDev P, LearnedLaunch L) {
+    const int lane = threadIdx.x & 31;
+    const int w = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+    if (w >= L.B) return;
+    Spins<NW> s;
+#pragma unroll
+    for (int k = 0; k < NW; k++) s.w[k] = L.spins[static_cast<long>(w) * NW + k];
+    const int i = L.site[w], l = L.len[w];
+    const long base = static_cast<long>(w) * P.Mpad + lane;
+    float tr[K], ti[K], re[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        const float2 t = L.theta[base + 32 * k];
+        tr[k] = t.x;
+        ti[k] = t.y;
+        re[k] = L.re[base + 32 * k];
+    }
+    // two_s = 2 * (new spin) for each cluster site, in cluster order
+    float part = 0.0f;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        float nr = tr[k], ni = ti[k];
+        for (int q = 0; q < l; q++) {
+            int c = i + q;
+            if (c >= P.N) c -= P.N;
+            const float two_s = s.up(c) ? -2.0f : 2.0f;
+            const float2 wv = __ldg(P.W + static_cast<long>(c) * P.Mpad + lane + 32 * k);
+            nr = __fmaf_rn(two_s, wv.x, nr);
+            ni = __fmaf_rn(two_s, wv.y, ni);
+        }
+        part = __fadd_rn(part, __fsub_rn(lc_re(nr, ni), re[k]));
+    }
+    const float delta = warp_sum_xor(part);
+    const float* rowp = L.logits_prop + static_cast<long>(w) * L.O;
+    const LogNorm ln = log_norms(rowp, L.N, lane);
+    const float logq_rev = (rowp[i] - ln.seed) + (rowp[L.N + l - 1] - ln.len);
+    const float log_a = 2.0f * delta + logq_rev - L.logq_fwd[w];
+    WalkerRng rng;
+    rng.init(L.seed, static_cast<uint32_t>(w), L.rng_index[w]);
+    const float a = log_a >= 0.0f ? 1.0f : expf_det(log_a);
+    bool accept = log_a >= 0.0f;
+    if (!accept) accept = rng.uniform() <= a;
+    if (accept) {
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            for (int q = 0; q < l; q++) {
+                int c = i + q;
+                if (c >= P.N) c -= P.N;
+                const float two_s = s.up(c) ? -2.0f : 2.0f;
+                const float2 wv = __ldg(P.W + static_cast<long>(c) * P.Mpad + lane + 32 * k);
+                tr[k] = __fmaf_rn(two_s, wv.x, tr[k]);
+                ti[k] = __fmaf_rn(two_s, wv.y, ti[k]);
+            }
+            L.theta[base + 32 * k] = make_float2(tr[k], ti[k]);
+            L.re[base + 32 * k] = lc_re(tr[k], ti[k]);
+        }
+        float* cur = L.logits_cur + static_cast<long>(w) * L.O;
+        for (int j = lane; j < L.O; j += 32) cur[j] = rowp[j];
+    }
+    if (lane == 0) {
+        if (accept) {
+#pragma unroll
+            for (int k = 0; k < NW; k++) L.spins[static_cast<long>(w) * NW + k] = L.spins_prop[static_cast<long>(w) * NW + k];
+            L.accepts[w] += 1;
+        }
+        L.rng_index[w] = rng.index;
+        L.reward[w] = a * static_cast<float>(l);
+    }
+}
+
+// mean reward of the first n walkers (one block, fixed order)
+__global__ void reward_mean_kernel(const float* r, int n, float* out) {
+    __shared__ float part[256];
+    float s = 0.0f;
+    for (int i = threadIdx.x; i < n; i += 256) s += r[i];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int h = 128; h >= 1; h >>= 1) {
+        if (threadIdx.x < h) part[threadIdx.x] += part[threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[0] = part[0] / static_cast<float>(n);
+}
+
+// REINFORCE gradient of the mean over n walkers of
+//   -(r - rbar) log q(i, l) - beta (H_seed + H_len)
+// with respect to the logits (warp per walker) -> dl [n][O]
+__global__ void __launch_bounds__(32 * kWarpsPerBlock) reinforce_kernel(const float* logits, int n, int N, int O,
+                                                                       const int* site, const int* len,
+                                                                       const float* reward, const float* rbar,
+                                                                       float* dl) {
+    const int lane = threadIdx.x & 31;
+    const int w = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+    if (w >= n) return;
+    const float* row = logits + static_cast<long>(w) * O;
+    const LogNorm ln = log_norms(row, N, lane);
+    const float adv = (reward[w] - rbar[0]) / static_cast<float>(n);
+    const float beta = kEntropyBonus / static_cast<float>(n);
+    // entropies H = -sum p log p
+    float hs = 0.0f;
+    for (int j = lane; j < N; j += 32) {
+        const float lp = row[j] - ln.seed;
+        hs -= expf(lp) * lp;
+    }
+    hs = warp_sum_xor(hs);
+    const float lpl = lane < kLengths ? row[N + lane] - ln.len : 0.0f;
+    const float hl = warp_sum_xor(lane < kLengths ? -expf(lpl) * lpl : 0.0f);
+    const int i = site[w], l = len[w];
+    float* out = dl + static_cast<long>(w) * O;
+    for (int j = lane; j < N; j += 32) {
+        const float lp = row[j] - ln.seed, p = expf(lp);
+        out[j] = adv * (p - (j == i ? 1.0f : 0.0f)) + beta * p * (lp + hs);
+    }
+    if (lane < kLengths) {
+        const float p = expf(lpl);
+        out[N + lane] = adv * (p - (lane == l - 1 ? 1.0f : 0.0f)) + beta * p * (lpl + hl);
+    }
+}
+
+template <int K>
+cudaError_t launch_learned_k(int which, int nw, const RbmDev& P, const LearnedLaunch& L, cudaStream_t st) {
+    const dim3 grid((L.B + kWarpsPerBlock - 1) / kWarpsPerBlock), block(32 * kWarpsPerBlock);
+#define RBMG_LEARNED_CASE(NWV)                                                             \
+    case NWV:                                                                               \
+        if (which == 0) learned_angles_kernel<K, NWV><<<grid, block, 0, st>>>(P, L);        \
+        else learned_accept_kernel<K, NWV><<<grid, block, 0, st>>>(P, L);                    \
+        break;
+    switch (nw) {
+        RBMG_LEARNED_CASE(1)
+        RBMG_LEARNED_CASE(2)
+        RBMG_LEARNED_CASE(3)
+        RBMG_LEARNED_CASE(4)
+        default: return cudaErrorInvalidValue;
+    }
+#undef RBMG_LEARNED_CASE
+    return cudaGetLastError();
+}
+
+// which: 0 angles from the spins, 1 accept / reject
+cudaError_t launch_learned(int which, const RbmDev& P, const LearnedLaunch& L, cudaStream_t st) {
+    const int nw = nwords_of(P.N);
+    switch (P.Mpad / 32) {
+        case 1: return launch_learned_k<1>(which, nw, P, L, st);
+        case 2: return launch_learned_k<2>(which, nw, P, L, st);
+        case 4: return launch_learned_k<4>(which, nw, P, L, st);
+        case 8: return launch_learned_k<8>(which, nw, P, L, st);
+        case 13: return launch_learned_k<13>(which, nw, P, L, st);
+        case 18: return launch_learned_k<18>(which, nw, P, L, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_propose(const LearnedLaunch& L, cudaStream_t st) {
+    const dim3 grid((L.B + kWarpsPerBlock - 1) / kWarpsPerBlock), block(32 * kWarpsPerBlock);
+    switch (nwords_of(L.N)) {
+        case 1: learned_propose_kernel<1><<<grid, block, 0, st>>>(L); break;
+        case 2: learned_propose_kernel<2><<<grid, block, 0, st>>>(L); break;
+        case 3: learned_propose_kernel<3><<<grid, block, 0, st>>>(L); break;
+        case 4: learned_propose_kernel<4><<<grid, block, 0, st>>>(L); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+// per-chain buffers of the learned steps
+struct LearnedState {
+    int B = 0, Mpad = 0, nw = 0, O = 0;
+    DevBuf theta, re, spins_prop, spins_pre, site, len, logq, logits_cur, logits_prop, reward, rbar;
+};
+
+}  // namespace rbmg
+
+using namespace rbmg;
+
+// ============================================================================ C ABI
+extern "C" int rbmg_proposal_create(int N, uint64_t seed, float lr, rbmg_proposal** out) {
+    if (!out) return fail(RBMG_EINVAL, "proposal: null output");
+    if (N <= kLengths || N > 64 * kMaxWords)
+        return fail(RBMG_EINVAL, "proposal: N must be in 9..256 (clusters of up to 8 sites must not wrap onto themselves)");
+    if (!(lr > 0.0f) || !std::isfinite(lr)) return fail(RBMG_EINVAL, "proposal: learning rate must be positive");
+    auto p = std::make_unique<rbmg_proposal>();
+    p->N = N;
+    p->O = N + kLengths;
+    p->Np = pad8(N);
+    p->Op = pad8(p->O);
+    p->lr = lr;
+    const int H = kHidden;
+    p->oW1 = 0;
+    p->ob1 = p->oW1 + static_cast<size_t>(N) * H;
+    p->oW2 = p->ob1 + H;
+    p->ob2 = p->oW2 + static_cast<size_t>(H) * H;
+    p->oW3 = p->ob2 + H;
+    p->ob3 = p->oW3 + static_cast<size_t>(H) * p->O;
+    p->P = static_cast<int64_t>(p->ob3 + p->O);
+    // He-uniform hidden layers (splitmix64 stream of the seed); zero output layer, so
+    // the untrained proposal is uniform over seeds and lengths
+    std::vector<float> h(static_cast<size_t>(p->P), 0.0f);
+    uint64_t z = seed;
+    auto uni = [&z]() {
+        z += 0x9E3779B97F4A7C15ull;
+        uint64_t x = z;
+        x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+        x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+        x ^= x >> 31;
+        return static_cast<double>(x >> 11) * (1.0 / 9007199254740992.0);
+    };
+    const double a1 = std::sqrt(6.0 / N), a2 = std::sqrt(6.0 / H);
+    for (size_t t = 0; t < static_cast<size_t>(N) * H; t++) h[p->oW1 + t] = static_cast<float>(a1 * (2.0 * uni() - 1.0));
+    for (size_t t = 0; t < static_cast<size_t>(H) * H; t++) h[p->oW2 + t] = static_cast<float>(a2 * (2.0 * uni() - 1.0));
+    RBMG_CK(p->master.ensure(sizeof(float) * p->P));
+    RBMG_CK(p->adam_m.ensure(sizeof(float) * p->P));
+    RBMG_CK(p->adam_v.ensure(sizeof(float) * p->P));
+    RBMG_CK(p->grad.ensure(sizeof(float) * p->P));
+    RBMG_CK(p->w1.ensure(sizeof(bf16) * static_cast<size_t>(N) * H));
+    RBMG_CK(p->w2.ensure(sizeof(bf16) * static_cast<size_t>(H) * H));
+    RBMG_CK(p->w3.ensure(sizeof(bf16) * static_cast<size_t>(H) * p->Op));
+    RBMG_CK(cudaMemcpy(p->master.p, h.data(), sizeof(float) * p->P, cudaMemcpyHostToDevice));
+    RBMG_CK(cudaMemset(p->adam_m.p, 0, sizeof(float) * p->P));
+    RBMG_CK(cudaMemset(p->adam_v.p, 0, sizeof(float) * p->P));
+    RBMG_CK(cudaMemset(p->grad.p, 0, sizeof(float) * p->P));
+    RBMG_CK(proposal_refresh_bf16(p.get(), stream()));
+    RBMG_CK(cudaStreamSynchronize(stream()));
+    *out = p.release();
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_proposal_destroy(rbmg_proposal* p) {
+    delete p;
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_proposal_num_params(const rbmg_proposal* p, int64_t* n) {
+    if (!p || !n) return fail(RBMG_EINVAL, "proposal: null argument");
+    *n = p->P;
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_proposal_get_params(const rbmg_proposal* p, float* params) {
+    if (!p || !params) return fail(RBMG_EINVAL, "proposal: null argument");
+    RBMG_CK(cudaStreamSynchronize(stream()));
+    RBMG_CK(cudaMemcpy(params, p->master.p, sizeof(float) * p->P, cudaMemcpyDeviceToHost));
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_proposal_set_params(rbmg_proposal* p, const float* params) {
+    if (!p || !params) return fail(RBMG_EINVAL, "proposal: null argument");
+    for (int64_t t = 0; t < p->P; t++)
+        if (!std::isfinite(params[t])) return fail(RBMG_ENAN, "proposal: non-finite parameter");
+    RBMG_CK(cudaStreamSynchronize(stream()));
+    RBMG_CK(cudaMemcpy(p->master.p, params, sizeof(float) * p->P, cudaMemcpyHostToDevice));
+    RBMG_CK(proposal_refresh_bf16(p, stream()));
+    RBMG_CK(cudaStreamSynchronize(stream()));
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_proposal_eval(rbmg_proposal* p, int count, const uint64_t* spins, const float* dlogits,
+                                  float* logits, float* grads) {
+    if (!p || count <= 0 || !spins || !logits) return fail(RBMG_EINVAL, "proposal eval: bad arguments");
+    if (dlogits && !grads) return fail(RBMG_EINVAL, "proposal eval: dlogits needs a gradient output");
+    const int nw = nwords_of(p->N);
+    cudaStream_t st = stream();
+    DevBuf dsp, dlog;
+    RBMG_CK(dsp.ensure(sizeof(uint64_t) * nw * count));
+    RBMG_CK(dlog.ensure(sizeof(float) * static_cast<size_t>(count) * p->O));
+    RBMG_CK(cudaMemcpyAsync(dsp.p, spins, sizeof(uint64_t) * nw * count, cudaMemcpyHostToDevice, st));
+    int r = proposal_forward(p, count, dsp.as<uint64_t>(), dlog.as<float>(), st);
+    if (r != RBMG_OK) return r;
+    RBMG_CK(cudaMemcpyAsync(logits, dlog.p, sizeof(float) * count * p->O, cudaMemcpyDeviceToHost, st));
+    if (dlogits) {
+        RBMG_CK(cudaMemcpyAsync(p->dl32.p, dlogits, sizeof(float) * count * p->O, cudaMemcpyHostToDevice, st));
+        r = proposal_backward(p, count, st);
+        if (r != RBMG_OK) return r;
+        RBMG_CK(cudaMemcpyAsync(grads, p->grad.p, sizeof(float) * p->P, cudaMemcpyDeviceToHost, st));
+    }
+    RBMG_CK(cudaStreamSynchronize(st));
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_proposal_adam(rbmg_proposal* p, const float* grads) {
+    if (!p || !grads) return fail(RBMG_EINVAL, "proposal adam: null argument");
+    cudaStream_t st = stream();
+    RBMG_CK(cudaMemcpyAsync(p->grad.p, grads, sizeof(float) * p->P, cudaMemcpyHostToDevice, st));
+    const int r = proposal_adam(p, st);
+    if (r != RBMG_OK) return r;
+    RBMG_CK(cudaStreamSynchronize(st));
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_chain_learned_async(rbmg_chain* c, const rbmg_psi* psi, const rbmg_operator* op,
+                                        rbmg_proposal* prop, int n_steps, int train, int measure_every,
+                                        void* d_eloc_out, void* stream_ptr) {
+    if (!c || !psi || !prop || n_steps < 0 || train < 0) return fail(RBMG_EINVAL, "learned steps: bad arguments");
+    if (psi->kind != 0 || psi->N != c->N) return fail(RBMG_EINVAL, "learned steps: psi does not match the chain");
+    if (prop->N != c->N) return fail(RBMG_EINVAL, "learned steps: proposal does not match the chain");
+    if (d_eloc_out && (!op || measure_every <= 0)) return fail(RBMG_EINVAL, "learned steps: measurement needs op");
+    if (op && op->max_site >= psi->N) return fail(RBMG_EINVAL, "learned steps: operator acts on a site >= N");
+    if (n_steps == 0) return RBMG_OK;
+    cudaStream_t st = stream_ptr ? static_cast<cudaStream_t>(stream_ptr) : stream();
+    const RbmDev P = psi->rbm_dev();
+    const int B = static_cast<int>(c->walkers);
+    if (!c->initialised) {
+        // random start spins from the walkers' Philox streams (no sweep)
+        McLaunch M{};
+        M.B = B;
+        M.seed = c->seed;
+        M.spins = c->spins.as<uint64_t>();
+        M.rng_index = c->rng_index.as<uint64_t>();
+        M.init = 1;
+        M.sweeps_per_sample = 1;
+        M.accepts = c->accepts.as<unsigned long long>();
+        M.proposals = c->proposals.as<unsigned long long>();
+        RBMG_CK(launch_rbm_mc(P, nullptr, M, st));
+        c->initialised = true;
+    }
+    auto* S = static_cast<LearnedState*>(c->learned.get());
+    if (!S || S->Mpad != P.Mpad || S->O != prop->O) {
+        c->learned = std::make_shared<LearnedState>();
+        S = static_cast<LearnedState*>(c->learned.get());
+        S->B = B;
+        S->Mpad = P.Mpad;
+        S->nw = c->nw;
+        S->O = prop->O;
+        const size_t b = static_cast<size_t>(B);
+        RBMG_CK(S->theta.ensure(sizeof(float2) * b * P.Mpad));
+        RBMG_CK(S->re.ensure(sizeof(float) * b * P.Mpad));
+        RBMG_CK(S->spins_prop.ensure(sizeof(uint64_t) * b * c->nw));
+        RBMG_CK(S->spins_pre.ensure(sizeof(uint64_t) * b * c->nw));
+        RBMG_CK(S->site.ensure(sizeof(int) * b));
+        RBMG_CK(S->len.ensure(sizeof(int) * b));
+        RBMG_CK(S->logq.ensure(sizeof(float) * b));
+        RBMG_CK(S->logits_cur.ensure(sizeof(float) * b * prop->O));
+        RBMG_CK(S->logits_prop.ensure(sizeof(float) * b * prop->O));
+        RBMG_CK(S->reward.ensure(sizeof(float) * b));
+        RBMG_CK(S->rbar.ensure(sizeof(float)));
+    }
+    LearnedLaunch L{};
+    L.B = B;
+    L.N = c->N;
+    L.O = prop->O;
+    L.seed = c->seed;
+    L.spins = c->spins.as<uint64_t>();
+    L.rng_index = c->rng_index.as<uint64_t>();
+    L.spins_prop = S->spins_prop.as<uint64_t>();
+    L.spins_pre = train > 0 ? S->spins_pre.as<uint64_t>() : nullptr;
+    L.site = S->site.as<int>();
+    L.len = S->len.as<int>();
+    L.logq_fwd = S->logq.as<float>();
+    L.logits_cur = S->logits_cur.as<float>();
+    L.logits_prop = S->logits_prop.as<float>();
+    L.theta = S->theta.as<float2>();
+    L.re = S->re.as<float>();
+    L.reward = S->reward.as<float>();
+    L.accepts = c->accepts.as<unsigned long long>();
+    L.proposals = c->proposals.as<unsigned long long>();
+    // the angles and logits of the current states (plain sweeps or new weights may
+    // have changed them since the last call)
+    RBMG_CK(launch_learned(0, P, L, st));
+    int r = proposal_forward(prop, B, L.spins, L.logits_cur, st);
+    if (r != RBMG_OK) return r;
+    const int nt = std::min(train, B);
+    OpDev od;
+    if (op) od = op->dev();
+    double2* out = static_cast<double2*>(d_eloc_out);
+    const int lead = d_eloc_out ? n_steps % measure_every : n_steps;
+    for (int step = 0; step < n_steps; step++) {
+        RBMG_CK(launch_propose(L, st));
+        r = proposal_forward(prop, B, L.spins_prop, S->logits_prop.as<float>(), st);
+        if (r != RBMG_OK) return r;
+        RBMG_CK(launch_learned(1, P, L, st));
+        if (nt > 0) {
+            // REINFORCE on the moves of the first nt walkers, from the states they started at
+            r = proposal_forward(prop, nt, L.spins_pre, prop->logits.as<float>(), st);
+            if (r != RBMG_OK) return r;
+            reward_mean_kernel<<<1, 256, 0, st>>>(L.reward, nt, S->rbar.as<float>());
+            reinforce_kernel<<<(nt + kWarpsPerBlock - 1) / kWarpsPerBlock, 32 * kWarpsPerBlock, 0, st>>>(
+                prop->logits.as<float>(), nt, c->N, prop->O, L.site, L.len, L.reward, S->rbar.as<float>(),
+                prop->dl32.as<float>());
+            RBMG_CK(cudaGetLastError());
+            r = proposal_backward(prop, nt, st);
+            if (r != RBMG_OK) return r;
+            r = proposal_adam(prop, st);
+            if (r != RBMG_OK) return r;
+            // the walkers' current logits under the new weights
+            r = proposal_forward(prop, B, L.spins, L.logits_cur, st);
+            if (r != RBMG_OK) return r;
+        }
+        if (d_eloc_out && step >= lead && (step - lead + 1) % measure_every == 0) {
+            EstLaunch E{};
+            E.count = B;
+            E.spins = L.spins;
+            E.flags = EST_ELOC;
+            E.eloc = out + static_cast<size_t>((step - lead) / measure_every) * B;
+            RBMG_CK(launch_rbm_estimate(P, &od, nullptr, E, st));
+        }
+    }
+    return RBMG_OK;
+}
