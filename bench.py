@@ -1,18 +1,28 @@
 #!/usr/bin/env python
-"""Benchmark of the plain Metropolis chain of the N=100 complex RBM.
+"""Benchmark: learned-proposal vs plain Metropolis chains of the N=100 complex RBM.
 
 Workload (the configuration the headline metric is quoted on): complex RBM with
 N=100 visible and M=400 hidden units, parameters complex Normal(0, 0.1^2) drawn from
-PCG64(104); periodic 1D transverse-field Ising chain with h=1.0 (200 Pauli
-strings); 16384 walkers.  One step = one sweep (N single-spin Metropolis proposals
-per walker) followed by the local energy of every walker.  The headline metric is
-effective samples per second: walkers x steps / tau_int(E_loc) per second, with
-tau_int from Sokal's automatic windowing (c = 5) of the walkers' E_loc series;
-E_loc/s is reported beside it.
+PCG64(104); periodic 1D transverse-field Ising chain with h=1.0 (200 Pauli strings);
+16384 walkers per GPU.  Two chains run on the same GPU:
+
+* plain: single-spin-flip Metropolis (the reference's method); one step = one row =
+  `--sweeps-per-row` sweeps of N proposals per walker, then the local energy of every
+  walker;
+* learned: after the same thermalisation and `--train-steps` steps of online training
+  (REINFORCE + Adam on the first `--train-walkers` walkers' moves), the frozen proposal
+  network's cluster-flip Metropolis-Hastings steps; one row = `--learned-steps-per-row`
+  steps, then the local energy of every walker.
+
+The headline metric is effective samples per second of the learned chain: walkers x
+rows / tau_int(E_loc) per second of its timed rows, tau_int (in rows) from Sokal's
+automatic windowing (c = 5) of the walkers' E_loc series; the plain chain's figures sit
+beside it ("plain"), with E_loc/s, the energy standard error per spin, and a flag where
+the window did not converge (tau_int is then a lower bound).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
-For N > 1 run under torchrun: every rank samples its own replica of the walker set
+For N > 1 run under torchrun: every rank samples its own replica of the walker sets
 (Philox keys offset by rank), no data-path collective; value = all ranks' effective
 samples / max over ranks of the timed region.
 """
@@ -32,8 +42,8 @@ if REPO not in sys.path:
     sys.path.insert(0, REPO)
 
 N_SPINS, M_HIDDEN, SIGMA, PARAM_SEED, FIELD, WALKERS = 100, 400, 0.1, 104, 1.0, 16384
-THERM_SWEEPS = 1000          # several tau_int of the plain chain (~130 sweeps)
-METRIC = "effective samples/s (ESS of E_loc), plain single-flip Metropolis, N=100 RBM"
+THERM_SWEEPS = 1000
+METRIC = "effective samples/s (ESS of E_loc) at N=100: learned-proposal MCMC (plain single-flip beside)"
 UNIT = "samples/s"
 L2_FLUSH_BYTES = 256 << 20
 
@@ -52,30 +62,49 @@ def workload():
     return b, W
 
 
-def flops_per_walker_step(N=N_SPINS, M=M_HIDDEN, n_offdiag=N_SPINS):
-    sweep = N * M * FLOPS_PROPOSAL_ANGLE + 2 * N * M + FLOPS_LC_RE * M     # proposals + angle refresh
-    measure = 2 * N * M + FLOPS_LC_C * M + n_offdiag * M * FLOPS_ELOC_ANGLE
-    return sweep + measure
+def flops_per_sweep(N=N_SPINS, M=M_HIDDEN):
+    """FP32 flops of one sweep of one walker: N proposals + the angle refresh."""
+    return N * M * FLOPS_PROPOSAL_ANGLE + 2 * N * M + FLOPS_LC_RE * M
+
+
+def flops_per_eloc(N=N_SPINS, M=M_HIDDEN, n_offdiag=N_SPINS):
+    return 2 * N * M + FLOPS_LC_C * M + n_offdiag * M * FLOPS_ELOC_ANGLE
 
 
 def tau_int(series, c=5.0):
-    """Integrated autocorrelation time (in steps) of E_loc, Sokal's automatic windowing:
+    """Integrated autocorrelation time (in rows) of E_loc, Sokal's automatic windowing:
     tau(W) = 1 + 2 sum_{t=1}^{W} rho(t), smallest W with W >= c tau(W); rho averaged over
-    walkers, each series centred on the all-walker mean.  series: [K, walkers]."""
+    walkers, each series centred on the all-walker mean.  series: [K, walkers].
+    Returns (tau, window, converged); not converged means no window W < K satisfied the
+    rule, and tau is then a lower bound."""
     x = np.asarray(series.real, np.float64)
     x = x - x.mean()
     K = x.shape[0]
     f = np.fft.rfft(x, n=2 * K, axis=0)
     ac = np.fft.irfft(f * np.conj(f), n=2 * K, axis=0)[:K].mean(axis=1) / np.arange(K, 0, -1)
     if ac[0] <= 0:
-        return 1.0, 1
+        return 1.0, 1, True
     rho = ac / ac[0]
     tau, window = 1.0, 1
     for window in range(1, K):
         tau = 1.0 + 2.0 * rho[1:window + 1].sum()
         if window >= c * tau:
-            break
-    return max(tau, 1.0), window
+            return max(tau, 1.0), window, True
+    return max(tau, 1.0), window, False
+
+
+def series_stats(series, seconds, N=N_SPINS):
+    """ESS figures of an E_loc series [rows, walkers] measured over `seconds`."""
+    x = np.asarray(series.real, np.float64)
+    rows, B = x.shape
+    tau, window, ok = tau_int(series)
+    se = x.std() * np.sqrt(tau / x.size)
+    wm = x.mean(axis=0)
+    se_walkers = wm.std(ddof=1) / np.sqrt(B)
+    return {"ess": x.size / tau, "ess_per_s": x.size / tau / seconds, "tau_int_rows": tau, "tau_window": window,
+            "tau_converged": ok, "rows": rows, "seconds": seconds, "eloc_per_s": x.size / seconds,
+            "energy_per_spin": x.mean() / N, "se_per_spin": se / N, "se_per_spin_walker_means": se_walkers / N,
+            "ess_walker_means": x.var() / se_walkers ** 2 if se_walkers > 0 else None}
 
 
 # --------------------------------------------------------------------- clocks
@@ -158,7 +187,7 @@ def cpu_chains(steps, seconds_per_step, workers, tmpdir):
     return np.concatenate(series, axis=0), wall, sweeps
 
 
-# --------------------------------------------------------------------- GPU arm
+# --------------------------------------------------------------------- GPU arms
 def run_gpu(args, rank, world, local_rank):
     import torch
     import rbmongpu_gb300 as rg
@@ -167,62 +196,94 @@ def run_gpu(args, rank, world, local_rank):
     rg.setDevice(local_rank)
     b, W = workload()
     psi = rg.Psi(np.zeros(N_SPINS), np.zeros(N_SPINS), b, W, 1.0, False, True)
-    op_t = rg.operators.tfim_chain(N_SPINS, 1.0, FIELD)
-    op = rg.Operator(*op_t)
-    B = args.walkers
-    chain = rg.Chain(psi, B, seed=1000 + rank)
+    op = rg.Operator(*rg.operators.tfim_chain(N_SPINS, 1.0, FIELD))
+    B, K, Wm = args.walkers, args.steps, args.warmup
+    S, L = args.sweeps_per_row, args.learned_steps_per_row
     sp = rg.library_stream()
     stream = torch.cuda.ExternalStream(sp)
-    K, Wm = args.steps, args.warmup
     eloc = torch.empty((K, B, 2), dtype=torch.float64, device="cuda")
-    scratch = torch.empty((max(Wm, 1), B, 2), dtype=torch.float64, device="cuda")
+    scratch = torch.empty((B, 2), dtype=torch.float64, device="cuda")
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
-    with torch.cuda.stream(stream):
-        chain.sweep_async(psi, None, THERM_SWEEPS, 1, 0, sp)
-        for w in range(Wm):
-            chain.sweep_async(psi, op, 1, 1, scratch[w].data_ptr(), sp)
-    torch.cuda.synchronize()
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    clocks = ClockSampler(local_rank)
-    clocks.start()
-    with torch.cuda.stream(stream):
-        for k in range(K):
-            flush.fill_(k & 0xFF)                 # L2 flush between timed steps (not timed)
-            starts[k].record(stream)
-            chain.sweep_async(psi, op, 1, 1, eloc[k].data_ptr(), sp)
-            ends[k].record(stream)
-    torch.cuda.synchronize()
-    clk = clocks.stop()
-    if world > 1:
-        torch.distributed.barrier()
-    step_ms = np.array([s.elapsed_time(e) for s, e in zip(starts, ends)])
-    total_s = float(step_ms.sum()) / 1e3
-    series = eloc.cpu().numpy().view(np.complex128)[..., 0]
-    tau, window = tau_int(series)
-    _, acc, props = chain.state()
 
-    # end to end through the public API with host buffers: per step the parameters go
-    # host -> device (psi.params) and the walkers' local energies device -> host
+    def sync():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    def timed_rows(n, row):
+        """per-row milliseconds (CUDA events on the library stream), L2 flushed between rows"""
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(n)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(n)]
+        with torch.cuda.stream(stream):
+            for k in range(n):
+                flush.fill_(k & 0xFF)
+                starts[k].record(stream)
+                row(k)
+                ends[k].record(stream)
+        torch.cuda.synchronize()
+        return np.array([a.elapsed_time(e) for a, e in zip(starts, ends)])
+
+    def series_of(n):
+        return eloc[:n].cpu().numpy().view(np.complex128)[..., 0]
+
+    clocks = ClockSampler(local_rank)
+    # ---- plain single-flip chain
+    plain = rg.Chain(psi, B, seed=1000 + rank)
+    with torch.cuda.stream(stream):
+        plain.sweep_async(psi, None, THERM_SWEEPS, 1, 0, sp)
+        for _ in range(Wm):
+            plain.sweep_async(psi, op, S, S, scratch.data_ptr(), sp)
+    sync()
+    clocks.start()
+    _, a0, p0 = plain.state()
+    plain_ms = timed_rows(K, lambda k: plain.sweep_async(psi, op, S, S, eloc[k].data_ptr(), sp))
+    _, a1, p1 = plain.state()
+    plain_series = series_of(K)
+    # the sampler kernel alone (one launch of S sweeps), for its roofline
+    kernel_ms = timed_rows(max(3, K // 20), lambda k: plain.sweep_async(psi, None, S, 1, 0, sp))
+    plain_accept = (a1 - a0) / max(p1 - p0, 1)
+
+    # ---- learned-proposal chain
+    prop = rg.Proposal(N_SPINS, seed=2000 + rank, lr=1e-3)
+    lc = rg.Chain(psi, B, seed=3000 + rank)
+    with torch.cuda.stream(stream):
+        lc.sweep_async(psi, None, THERM_SWEEPS, 1, 0, sp)
+    sync()
+    t0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        lc.learned_async(psi, None, prop, args.train_steps, args.train_walkers, 1, 0, sp)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    with torch.cuda.stream(stream):
+        for _ in range(Wm):
+            lc.learned_async(psi, op, prop, L, 0, L, scratch.data_ptr(), sp)
+    sync()
+    _, a0, p0 = lc.state()
+    learned_ms = timed_rows(K, lambda k: lc.learned_async(psi, op, prop, L, 0, L, eloc[k].data_ptr(), sp))
+    _, a1, p1 = lc.state()
+    clk = clocks.stop()
+    learned_series = series_of(K)
+    learned_accept = (a1 - a0) / max(p1 - p0, 1)
+
+    plain_stats = series_stats(plain_series, float(plain_ms.sum()) / 1e3)
+    learned_stats = series_stats(learned_series, float(learned_ms.sum()) / 1e3)
+
+    # end to end through the public API with host buffers: per row the RBM parameters go
+    # host -> device (psi.params) and the row's local energies device -> host (pinned)
     e2e_K = max(4, K // 10)
     p_host = psi.params
-    host_eloc = np.empty((e2e_K, B), np.complex128)
     pinned = torch.empty((B, 2), dtype=torch.float64, pin_memory=True)
-    dbuf = torch.empty((B, 2), dtype=torch.float64, device="cuda")
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for k in range(e2e_K):
         psi.params = p_host
         with torch.cuda.stream(stream):
-            chain.sweep_async(psi, op, 1, 1, dbuf.data_ptr(), sp)
-            pinned.copy_(dbuf, non_blocking=True)
+            lc.learned_async(psi, op, prop, L, 0, L, scratch.data_ptr(), sp)
+            pinned.copy_(scratch, non_blocking=True)
         stream.synchronize()
-        host_eloc[k] = pinned.numpy().view(np.complex128)[:, 0]
+        _ = pinned.numpy().view(np.complex128)[:, 0].mean()
     e2e_s = time.perf_counter() - t0
-    # the short e2e series cannot resolve tau_int; it shares the device-timed chains' tau
     h2d = (N_SPINS + 1) * ((M_HIDDEN + 31) // 32 * 32) * 8     # complex64 W and b, padded rows
     d2h = B * 16
 
@@ -234,25 +295,31 @@ def run_gpu(args, rank, world, local_rank):
         call("rbmg_probe_fp32_tflops", 20000, ctypes.byref(v))
         fp32_peak = v.value
 
-    stats = np.array([total_s, B * K / tau, B * K, e2e_s, B * e2e_K / tau], np.float64)
+    # whole-job sums over ranks (walker sets are independent replicas); times are maxima
+    tot = np.array([learned_stats["ess"], plain_stats["ess"], B * e2e_K / learned_stats["tau_int_rows"],
+                    learned_series.size, plain_series.size], np.float64)
+    tmax = np.array([learned_stats["seconds"], plain_stats["seconds"], e2e_s], np.float64)
     if world > 1:
-        t = torch.tensor(stats, device="cuda")
-        mx = t.clone()
-        torch.distributed.all_reduce(mx, op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)
-        stats = t.cpu().numpy()
-        stats[0], stats[3] = mx[0].item(), mx[3].item()
-    return dict(step_ms=step_ms, total_s=stats[0], ess=stats[1], samples=stats[2], tau=tau, window=window,
-                e2e_s=stats[3], e2e_ess=stats[4], h2d=h2d, d2h=d2h, clocks=clk, accept=acc / max(props, 1),
-                fp32_peak=fp32_peak, E_mean=complex(series.mean()))
+        t1 = torch.tensor(tot, device="cuda")
+        t2 = torch.tensor(tmax, device="cuda")
+        torch.distributed.all_reduce(t1, op=torch.distributed.ReduceOp.SUM)
+        torch.distributed.all_reduce(t2, op=torch.distributed.ReduceOp.MAX)
+        tot, tmax = t1.cpu().numpy(), t2.cpu().numpy()
+    return dict(tot=tot, tmax=tmax, plain=plain_stats, learned=learned_stats, plain_ms=plain_ms,
+                learned_ms=learned_ms, kernel_ms=kernel_ms, plain_accept=plain_accept, learned_accept=learned_accept,
+                train_s=train_s, e2e_K=e2e_K, h2d=h2d, d2h=d2h, clocks=clk, fp32_peak=fp32_peak)
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=2000)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=400, help="timed rows of each chain")
+    ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--walkers", type=int, default=WALKERS)
+    ap.add_argument("--sweeps-per-row", type=int, default=10)
+    ap.add_argument("--learned-steps-per-row", type=int, default=50)
+    ap.add_argument("--train-steps", type=int, default=2000)
+    ap.add_argument("--train-walkers", type=int, default=4096)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=16.0, help="budget of the CPU baseline leg")
     args = ap.parse_args()
@@ -264,13 +331,13 @@ def main():
 
     if args.impl == "reference":
         # the reference cannot run N=100 (MAX_SPINS=64 in its include/types.h); its CPU
-        # algorithm is timed through the FP64 restatement on the host cores
+        # algorithm (single-flip Metropolis in FP64) is timed through the restatement
         if rank != 0:
             return
         with tempfile.TemporaryDirectory() as td:
             series, wall, sweeps = cpu_chains(args.warmup + args.steps, 1.0, workers, td)
         series = series[args.warmup * sweeps:]
-        tau, _ = tau_int(series)
+        tau, _, ok = tau_int(series)
         n = series.size
         timed = wall * args.steps / (args.warmup + args.steps)
         value = n / tau / timed
@@ -278,12 +345,12 @@ def main():
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * timed / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic (seeded PCG64 parameters)",
-                "config": {"workload": "rbm_n100_m400_tfim_chain_plain_metropolis", "walkers": workers,
-                           "sweeps_per_step": sweeps},
+                "config": {"workload": "rbm_n100_m400_tfim_chain", "method": "plain single-flip Metropolis",
+                           "walkers": workers, "sweeps_per_step": sweeps},
                 "cpu_baseline": {"value": value, "unit": UNIT, "cores": workers, "kind": "port",
-                                 "sample": f"{workers} chains x {args.steps * sweeps} sweeps with E_loc each"},
+                                 "sample": f"{workers} FP64 chains x {args.steps * sweeps} sweeps with E_loc each"},
                 "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-                "eloc_per_s": n / timed, "tau_int_sweeps": tau}
+                "eloc_per_s": n / timed, "tau_int_sweeps": tau, "tau_converged": ok}
         print(json.dumps(line))
         return
 
@@ -296,39 +363,54 @@ def main():
             import torch
             torch.distributed.destroy_process_group()
         return
-    fl = flops_per_walker_step() * args.walkers
-    avg_launch = float(np.mean(r["step_ms"])) / 1e3
+    S, L, B = args.sweeps_per_row, args.learned_steps_per_row, args.walkers
+    ess_l, ess_p, ess_e2e, n_l, n_p = r["tot"]
+    sec_l, sec_p, sec_e2e = r["tmax"]
+    fl = flops_per_sweep() * S * B
+    avg_launch = float(np.mean(r["kernel_ms"])) / 1e3
     achieved = fl / avg_launch / 1e12
     peak = r["fp32_peak"]
-    # CPU baseline on the host cores: same chains, FP64 restatement, bounded sample
+    pl, le = r["plain"], r["learned"]
+    # CPU baseline on the host cores: the plain method, FP64 restatement, bounded sample
     cpu = None
     if args.cpu_seconds > 0:
         with tempfile.TemporaryDirectory() as td:
             cs, cwall, csweeps = cpu_chains(max(1, int(args.cpu_seconds)), 1.0, workers, td)
         cpu_eloc_s = cs.size / cwall
-        cpu = {"value": cpu_eloc_s / r["tau"], "unit": UNIT, "cores": workers, "kind": "port",
-               "sample": f"{workers} FP64 restatement chains x {cs.shape[0]} sweeps with E_loc; "
-                         f"ESS/s uses the GPU chains' tau_int", "eloc_per_s": cpu_eloc_s}
+        tau_sweeps = pl["tau_int_rows"] * S
+        cpu = {"value": cpu_eloc_s / tau_sweeps, "unit": UNIT, "cores": workers, "kind": "port",
+               "sample": f"{workers} FP64 restatement chains x {cs.shape[0]} sweeps with E_loc each; ESS/s "
+                         f"divides their E_loc/s by the GPU plain chain's tau_int in sweeps",
+               "eloc_per_s": cpu_eloc_s}
+    gap = (le["energy_per_spin"] - pl["energy_per_spin"]) / np.hypot(le["se_per_spin"], pl["se_per_spin"])
     line = {
-        "metric": METRIC, "value": r["ess"] / r["total_s"], "unit": UNIT, "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * r["total_s"] / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (complex64), FP64 sums",
+        "metric": METRIC, "value": ess_l / sec_l, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(r["learned_ms"])),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (complex64 RBM), bf16 MLP with f32 accumulation",
         "data": "synthetic (seeded PCG64 parameters, random +-1 starts)",
-        "config": {"workload": "rbm_n100_m400_tfim_chain_plain_metropolis", "N": N_SPINS, "M": M_HIDDEN,
-                   "walkers_per_gpu": args.walkers, "sigma": SIGMA, "h": FIELD,
-                   "step": "1 sweep (N proposals) + E_loc per walker", "l2": "flushed between timed steps"},
-        "eloc_per_s": r["samples"] / r["total_s"],
-        "proposals_per_s": r["samples"] * N_SPINS / r["total_s"],
-        "tau_int_sweeps": r["tau"], "tau_window": r["window"], "acceptance": r["accept"],
-        "mean_energy": r["E_mean"].real,
-        "e2e": {"value": r["e2e_ess"] / r["e2e_s"], "unit": UNIT, "h2d_bytes_per_step": int(r["h2d"]),
+        "config": {"workload": "rbm_n100_m400_tfim_chain_learned_vs_plain", "N": N_SPINS, "M": M_HIDDEN,
+                   "walkers_per_gpu": B, "sigma": SIGMA, "h": FIELD, "therm_sweeps": THERM_SWEEPS,
+                   "step": f"learned: {L} frozen MH steps + E_loc; plain: {S} sweeps + E_loc",
+                   "train_steps": args.train_steps, "train_walkers": args.train_walkers,
+                   "l2": "flushed between timed rows"},
+        "learned": dict(le, ess_per_s=ess_l / sec_l, acceptance=r["learned_accept"], train_seconds=r["train_s"],
+                        ms_per_row=float(np.mean(r["learned_ms"]))),
+        "plain": dict(pl, ess_per_s=ess_p / sec_p, acceptance=r["plain_accept"],
+                      ms_per_row=float(np.mean(r["plain_ms"]))),
+        "learned_over_plain_ess_per_s": (ess_l / sec_l) / (ess_p / sec_p),
+        "energy_gap_in_se": gap,
+        "eloc_per_s": n_l / sec_l,
+        "e2e": {"value": ess_e2e / sec_e2e, "unit": UNIT, "h2d_bytes_per_step": int(r["h2d"]),
                 "d2h_bytes_per_step": int(r["d2h"])},
-        "gpu_launches": 2 * args.steps,     # per step: the sampler and the local-energy pass
+        # per learned row: L x (propose, spins_to_x, 3 GEMM layers, accept) + angles, the
+        # current-state forward (spins_to_x + 3 GEMM layers) and the local-energy pass
+        "gpu_launches": args.steps * (6 * L + 6),
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak if peak else None, "traffic": None,
                      "peak_source": "measured in this run by the library's FP32 FMA probe kernel",
-                     "kernel": "rbm_mc_kernel<13,2> + rbm_eloc_kernel<13,2> (one step)",
-                     "flops_per_launch": fl},
+                     "kernel": f"rbm_mc_kernel<13,2> (plain sampler, {S} sweeps per launch)",
+                     "flops_per_launch": fl, "ms_per_launch": avg_launch * 1e3},
         "cpu_baseline": cpu,
         "clocks": r["clocks"],
     }

@@ -230,10 +230,16 @@ RBMG_API int rbmg_proposal_eval(rbmg_proposal* proposal, int count, const uint64
                                 float* logits, float* grads);
 /* one Adam step (lr of the proposal, beta 0.9 / 0.999, eps 1e-8) with the given gradient */
 RBMG_API int rbmg_proposal_adam(rbmg_proposal* proposal, const float* grads);
+/* training objective of rbmg_chain_learned_async: cross-entropy to the locally balanced
+ * proposal p*(i, l) propto |psi(s')/psi(s)| over all N x 8 cluster moves of the training
+ * walkers (default), or REINFORCE on the acceptance, reward min(1, a) * l */
+#define RBMG_PROPOSAL_LOCALLY_BALANCED 0
+#define RBMG_PROPOSAL_REINFORCE 1
+RBMG_API int rbmg_proposal_set_objective(rbmg_proposal* proposal, int objective);
 /* n_steps learned Metropolis-Hastings steps of every walker of the chain.  train = 0 keeps
  * the weights (the chain is then exactly |psi|^2-stationary); train > 0 follows every step
- * with one REINFORCE + Adam update on the moves of the first `train` walkers (adaptive
- * chain: use it to train, then measure with train = 0).  Local energies every
+ * with one update (objective of rbmg_proposal_set_objective) + Adam step on the first
+ * `train` walkers (adaptive chain: use it to train, then measure with train = 0).  Local energies every
  * measure_every steps into d_eloc_out [n_steps / measure_every][walkers] (device double2),
  * as in rbmg_chain_sweep_async.  N must exceed 8. */
 RBMG_API int rbmg_chain_learned_async(rbmg_chain* chain, const rbmg_psi* psi, const rbmg_operator* op,

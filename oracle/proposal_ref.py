@@ -115,3 +115,33 @@ def log_q(logits, N, seed, length):
     ls = logits[:N] - np.logaddexp.reduce(logits[:N])
     ll = logits[N:] - np.logaddexp.reduce(logits[N:])
     return ls[seed] + ll[length - 1]
+
+
+def emulate_chain(log_psi_re, logits_all, N, B, steps, seed, with_reverse=True):
+    """Vectorised emulation of the learned Metropolis-Hastings chain over an enumerated
+    state space (state = spin bit pattern, N <= 20): seed and length drawn by inverse
+    CDF, the contiguous periodic cluster flipped, accepted with
+    min(1, exp(2 dRe log psi) q(s|s') / q(s'|s)).  with_reverse=False drops the density
+    ratio (a deliberately wrong chain, used to show that the tests detect it).
+    Returns the final states of B independent walkers and the acceptance rate."""
+    r = np.random.default_rng(seed)
+    ls = logits_all[:, :N] - np.logaddexp.reduce(logits_all[:, :N], axis=1, keepdims=True)
+    ll = logits_all[:, N:] - np.logaddexp.reduce(logits_all[:, N:], axis=1, keepdims=True)
+    state = r.integers(0, 2 ** N, B)
+    acc = 0
+    for _ in range(steps):
+        cs = np.cumsum(np.exp(ls[state]), axis=1)
+        i = (cs < r.random(B)[:, None] * cs[:, -1:]).sum(axis=1).clip(0, N - 1)
+        cl = np.cumsum(np.exp(ll[state]), axis=1)
+        l = 1 + (cl < r.random(B)[:, None] * cl[:, -1:]).sum(axis=1).clip(0, LENGTHS - 1)
+        mask = np.zeros(B, np.int64)
+        for q in range(LENGTHS):
+            mask |= np.where(q < l, 1 << ((i + q) % N), 0)
+        new = state ^ mask
+        loga = 2 * (log_psi_re[new] - log_psi_re[state])
+        if with_reverse:
+            loga = loga + ls[new, i] + ll[new, l - 1] - ls[state, i] - ll[state, l - 1]
+        a = r.random(B) < np.exp(np.minimum(loga, 0.0))
+        acc += int(a.sum())
+        state = np.where(a, new, state)
+    return state, acc / (B * steps)

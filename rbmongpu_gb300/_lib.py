@@ -84,6 +84,7 @@ SIGNATURES = {
     "rbmg_proposal_set_params": [_vp, C.POINTER(C.c_float)],
     "rbmg_proposal_eval": [_vp, C.c_int, _u64p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float)],
     "rbmg_proposal_adam": [_vp, C.POINTER(C.c_float)],
+    "rbmg_proposal_set_objective": [_vp, C.c_int],
     "rbmg_chain_learned_async": [_vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_int, _vp, _vp],
 }
 _RESTYPE = {"rbmg_last_error": C.c_char_p, "rbmg_version": C.c_char_p}

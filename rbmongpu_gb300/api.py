@@ -608,8 +608,10 @@ class Proposal:
 
     HIDDEN = 256
     LENGTHS = 8
+    LOCALLY_BALANCED = 0
+    REINFORCE = 1
 
-    def __init__(self, N, seed=0, lr=1e-3):
+    def __init__(self, N, seed=0, lr=1e-3, objective=LOCALLY_BALANCED):
         h = _handle()
         call("rbmg_proposal_create", int(N), int(seed), float(lr), C.byref(h))
         self._h = h
@@ -617,6 +619,12 @@ class Proposal:
         n = C.c_int64()
         call("rbmg_proposal_num_params", h, C.byref(n))
         self.num_params = n.value
+        self.set_objective(objective)
+
+    def set_objective(self, objective):
+        """LOCALLY_BALANCED (default): cross-entropy to p*(i, l) propto |psi(s')/psi(s)| over
+        all cluster moves; REINFORCE: policy gradient on the acceptance."""
+        call("rbmg_proposal_set_objective", self._h, int(objective))
 
     def __del__(self):
         h, self._h = getattr(self, "_h", None), None

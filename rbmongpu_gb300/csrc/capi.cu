@@ -365,6 +365,10 @@ static int op_compile(rbmg_operator* op) {
         return cudaMemcpy(d.p, h, bytes, cudaMemcpyHostToDevice);
     };
     RBMG_CK(up(op->d_coef, op->coef.data(), sizeof(cplx) * op->S));
+    std::vector<float2> c32(op->S);
+    for (int n = 0; n < op->S; n++)
+        c32[n] = make_float2(static_cast<float>(op->coef[n].real()), static_cast<float>(op->coef[n].imag()));
+    RBMG_CK(up(op->d_coef32, c32.data(), sizeof(float2) * op->S));
     RBMG_CK(up(op->d_ypow, op->ypow.data(), sizeof(int) * op->S));
     RBMG_CK(up(op->d_zmask, op->zmask.data(), sizeof(uint64_t) * op->zmask.size()));
     RBMG_CK(up(op->d_nflip, op->nflip.data(), sizeof(int) * op->S));

@@ -31,6 +31,7 @@ struct OpDev {
     const int* flip_sites;     // flat
     const int* offdiag_slot;   // [S] index among off-diagonal strings, -1 if diagonal
     int num_offdiag;
+    const float2* coef32;      // [S] coefficients rounded to FP32 (local-energy sums)
 };
 
 // Metropolis launch: one warp per walker (include/spin_ensembles/MonteCarloLoop.hpp:55-256)

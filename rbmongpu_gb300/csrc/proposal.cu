@@ -10,8 +10,14 @@
 //
 // The network runs in BF16 operands with FP32 accumulation on the tensor cores
 // (mma.sync m16n8k16); forward, backward and Adam are kernels of this file.  It is
-// trained online by REINFORCE on the chain's own moves, reward = min(1, a) * l (expected
-// number of spins flipped), with the batch-mean baseline and an entropy bonus.
+// trained online on the chain's own configurations.  The default objective is the
+// cross-entropy to the locally balanced proposal (Zanella 2020), p*(i, l | s) propto
+// sqrt(|psi(s')|^2 / |psi(s)|^2) over all N x 8 cluster moves, computed exactly for the
+// training walkers: it is the proposal whose Metropolis-Hastings acceptance
+// Z(s) / Z(s') tends to 1, and the factorised network is fitted to its seed and length
+// marginals.  The alternative objective, REINFORCE on the acceptance itself (reward
+// min(1, a) * l, batch-mean baseline, entropy bonus), has degenerate optima: a proposal
+// that pairs states (s -> s' -> s ...) is accepted almost always and does not mix.
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -282,6 +288,7 @@ inline unsigned blocks_for(long n, int threads = 256) { return static_cast<unsig
 struct rbmg_proposal {
     int N = 0, O = 0, Np = 0, Op = 0;
     float lr = 1e-3f;
+    int objective = RBMG_PROPOSAL_LOCALLY_BALANCED;
     long steps = 0;   // Adam steps taken
     int64_t P = 0;
     size_t oW1 = 0, ob1 = 0, oW2 = 0, ob2 = 0, oW3 = 0, ob3 = 0;   // offsets in the FP32 parameter vector
@@ -616,20 +623,28 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) learned_accept_kernel(Rbm
         ti[k] = t.y;
         re[k] = L.re[base + 32 * k];
     }
-    // two_s = 2 * (new spin) for each cluster site, in cluster order
+    // trial angles: two_s = 2 * (new spin) for each cluster site, in cluster order; the K
+    // loads of one W row are issued together
+    float nr[K], ni[K], nre[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) { nr[k] = tr[k]; ni[k] = ti[k]; }
+    for (int q = 0; q < l; q++) {
+        int c = i + q;
+        if (c >= P.N) c -= P.N;
+        const float two_s = s.up(c) ? -2.0f : 2.0f;
+        const float2* row = P.W + static_cast<long>(c) * P.Mpad + lane;
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const float2 wv = __ldg(row + 32 * k);
+            nr[k] = __fmaf_rn(two_s, wv.x, nr[k]);
+            ni[k] = __fmaf_rn(two_s, wv.y, ni[k]);
+        }
+    }
     float part = 0.0f;
 #pragma unroll
     for (int k = 0; k < K; k++) {
-        float nr = tr[k], ni = ti[k];
-        for (int q = 0; q < l; q++) {
-            int c = i + q;
-            if (c >= P.N) c -= P.N;
-            const float two_s = s.up(c) ? -2.0f : 2.0f;
-            const float2 wv = __ldg(P.W + static_cast<long>(c) * P.Mpad + lane + 32 * k);
-            nr = __fmaf_rn(two_s, wv.x, nr);
-            ni = __fmaf_rn(two_s, wv.y, ni);
-        }
-        part = __fadd_rn(part, __fsub_rn(lc_re(nr, ni), re[k]));
+        nre[k] = lc_re(nr[k], ni[k]);
+        part = __fadd_rn(part, __fsub_rn(nre[k], re[k]));
     }
     const float delta = warp_sum_xor(part);
     const float* rowp = L.logits_prop + static_cast<long>(w) * L.O;
@@ -644,16 +659,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) learned_accept_kernel(Rbm
     if (accept) {
 #pragma unroll
         for (int k = 0; k < K; k++) {
-            for (int q = 0; q < l; q++) {
-                int c = i + q;
-                if (c >= P.N) c -= P.N;
-                const float two_s = s.up(c) ? -2.0f : 2.0f;
-                const float2 wv = __ldg(P.W + static_cast<long>(c) * P.Mpad + lane + 32 * k);
-                tr[k] = __fmaf_rn(two_s, wv.x, tr[k]);
-                ti[k] = __fmaf_rn(two_s, wv.y, ti[k]);
-            }
-            L.theta[base + 32 * k] = make_float2(tr[k], ti[k]);
-            L.re[base + 32 * k] = lc_re(tr[k], ti[k]);
+            L.theta[base + 32 * k] = make_float2(nr[k], ni[k]);
+            L.re[base + 32 * k] = nre[k];
         }
         float* cur = L.logits_cur + static_cast<long>(w) * L.O;
         for (int j = lane; j < L.O; j += 32) cur[j] = rowp[j];
@@ -667,6 +674,89 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) learned_accept_kernel(Rbm
         L.rng_index[w] = rng.index;
         L.reward[w] = a * static_cast<float>(l);
     }
+}
+
+__device__ __forceinline__ float log_add(float a, float b) {
+    const float m = fmaxf(a, b);
+    if (m == -INFINITY) return m;
+    return m + logf(expf(a - m) + expf(b - m));
+}
+
+// Locally balanced target of the first n walkers (warp per walker): Re Delta(i, l) =
+// Re log psi(s with {i..i+l-1} flipped) - Re log psi(s) for all N seeds and 8 lengths,
+// p*(i, l) propto exp(Re Delta(i, l)); writes dl = (q - p*) / n, the gradient of the mean
+// cross-entropy -sum p* log q with respect to the seed and length logits (q factorises
+// into the seed and length softmaxes, whose optimum is the marginals of p*).
+template <int K, int NW>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock) lb_target_kernel(RbmDev P, int n, const uint64_t* spins,
+                                                                       const float2* theta, const float* re_all,
+                                                                       const float* logits, int O, float* dl) {
+    const int lane = threadIdx.x & 31;
+    const int w = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+    if (w >= n) return;
+    Spins<NW> s;
+#pragma unroll
+    for (int k = 0; k < NW; k++) s.w[k] = spins[static_cast<long>(w) * NW + k];
+    const long base = static_cast<long>(w) * P.Mpad + lane;
+    float tr[K], ti[K], re[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        const float2 t = theta[base + 32 * k];
+        tr[k] = t.x;
+        ti[k] = t.y;
+        re[k] = re_all[base + 32 * k];
+    }
+    constexpr int kSlots = (64 * NW + 31) / 32;   // seeds i = lane + 32 c held by lane
+    float ms[kSlots], ml[kLengths];
+#pragma unroll
+    for (int c = 0; c < kSlots; c++) ms[c] = -INFINITY;
+#pragma unroll
+    for (int q = 0; q < kLengths; q++) ml[q] = -INFINITY;
+    for (int i = 0; i < P.N; i++) {
+        float nr[K], ni[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) { nr[k] = tr[k]; ni[k] = ti[k]; }
+        float seed_acc = -INFINITY;
+#pragma unroll
+        for (int q = 0; q < kLengths; q++) {
+            int c = i + q;
+            if (c >= P.N) c -= P.N;
+            const float two_s = s.up(c) ? -2.0f : 2.0f;
+            const float2* row = P.W + static_cast<long>(c) * P.Mpad + lane;
+            float part = 0.0f;
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                const float2 wv = __ldg(row + 32 * k);
+                nr[k] = __fmaf_rn(two_s, wv.x, nr[k]);
+                ni[k] = __fmaf_rn(two_s, wv.y, ni[k]);
+                part += lc_re(nr[k], ni[k]) - re[k];
+            }
+            const float d = warp_sum_xor(part);
+            seed_acc = log_add(seed_acc, d);
+            ml[q] = log_add(ml[q], d);
+        }
+        const int slot = i >> 5;
+        if (lane == (i & 31)) {
+#pragma unroll
+            for (int c = 0; c < kSlots; c++)
+                if (c == slot) ms[c] = seed_acc;
+        }
+    }
+    float total = -INFINITY;
+#pragma unroll
+    for (int q = 0; q < kLengths; q++) total = log_add(total, ml[q]);
+    const float* row = logits + static_cast<long>(w) * O;
+    const LogNorm ln = log_norms(row, P.N, lane);
+    float* out = dl + static_cast<long>(w) * O;
+    const float inv = 1.0f / static_cast<float>(n);
+#pragma unroll
+    for (int c = 0; c < kSlots; c++) {
+        const int j = lane + 32 * c;
+        if (j < P.N) out[j] = (expf(row[j] - ln.seed) - expf(ms[c] - total)) * inv;
+    }
+#pragma unroll
+    for (int q = 0; q < kLengths; q++)
+        if (lane == q) out[P.N + q] = (expf(row[P.N + q] - ln.len) - expf(ml[q] - total)) * inv;
 }
 
 // mean reward of the first n walkers (one block, fixed order)
@@ -761,6 +851,34 @@ cudaError_t launch_propose(const LearnedLaunch& L, cudaStream_t st) {
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
+}
+
+template <int K>
+cudaError_t launch_lb_k(int nw, const RbmDev& P, int n, const uint64_t* spins, const float2* theta, const float* re,
+                        const float* logits, int O, float* dl, cudaStream_t st) {
+    const dim3 grid((n + kWarpsPerBlock - 1) / kWarpsPerBlock), block(32 * kWarpsPerBlock);
+    switch (nw) {
+        case 1: lb_target_kernel<K, 1><<<grid, block, 0, st>>>(P, n, spins, theta, re, logits, O, dl); break;
+        case 2: lb_target_kernel<K, 2><<<grid, block, 0, st>>>(P, n, spins, theta, re, logits, O, dl); break;
+        case 3: lb_target_kernel<K, 3><<<grid, block, 0, st>>>(P, n, spins, theta, re, logits, O, dl); break;
+        case 4: lb_target_kernel<K, 4><<<grid, block, 0, st>>>(P, n, spins, theta, re, logits, O, dl); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lb_target(const RbmDev& P, int n, const uint64_t* spins, const float2* theta, const float* re,
+                             const float* logits, int O, float* dl, cudaStream_t st) {
+    const int nw = nwords_of(P.N);
+    switch (P.Mpad / 32) {
+        case 1: return launch_lb_k<1>(nw, P, n, spins, theta, re, logits, O, dl, st);
+        case 2: return launch_lb_k<2>(nw, P, n, spins, theta, re, logits, O, dl, st);
+        case 4: return launch_lb_k<4>(nw, P, n, spins, theta, re, logits, O, dl, st);
+        case 8: return launch_lb_k<8>(nw, P, n, spins, theta, re, logits, O, dl, st);
+        case 13: return launch_lb_k<13>(nw, P, n, spins, theta, re, logits, O, dl, st);
+        case 18: return launch_lb_k<18>(nw, P, n, spins, theta, re, logits, O, dl, st);
+        default: return cudaErrorInvalidValue;
+    }
 }
 
 // per-chain buffers of the learned steps
@@ -887,6 +1005,14 @@ extern "C" int rbmg_proposal_adam(rbmg_proposal* p, const float* grads) {
     return RBMG_OK;
 }
 
+extern "C" int rbmg_proposal_set_objective(rbmg_proposal* p, int objective) {
+    if (!p) return fail(RBMG_EINVAL, "proposal: null");
+    if (objective != RBMG_PROPOSAL_LOCALLY_BALANCED && objective != RBMG_PROPOSAL_REINFORCE)
+        return fail(RBMG_EINVAL, "proposal: unknown objective");
+    p->objective = objective;
+    return RBMG_OK;
+}
+
 extern "C" int rbmg_chain_learned_async(rbmg_chain* c, const rbmg_psi* psi, const rbmg_operator* op,
                                         rbmg_proposal* prop, int n_steps, int train, int measure_every,
                                         void* d_eloc_out, void* stream_ptr) {
@@ -942,7 +1068,7 @@ extern "C" int rbmg_chain_learned_async(rbmg_chain* c, const rbmg_psi* psi, cons
     L.spins = c->spins.as<uint64_t>();
     L.rng_index = c->rng_index.as<uint64_t>();
     L.spins_prop = S->spins_prop.as<uint64_t>();
-    L.spins_pre = train > 0 ? S->spins_pre.as<uint64_t>() : nullptr;
+    L.spins_pre = train > 0 && prop->objective == RBMG_PROPOSAL_REINFORCE ? S->spins_pre.as<uint64_t>() : nullptr;
     L.site = S->site.as<int>();
     L.len = S->len.as<int>();
     L.logq_fwd = S->logq.as<float>();
@@ -968,7 +1094,13 @@ extern "C" int rbmg_chain_learned_async(rbmg_chain* c, const rbmg_psi* psi, cons
         r = proposal_forward(prop, B, L.spins_prop, S->logits_prop.as<float>(), st);
         if (r != RBMG_OK) return r;
         RBMG_CK(launch_learned(1, P, L, st));
-        if (nt > 0) {
+        if (nt > 0 && prop->objective == RBMG_PROPOSAL_LOCALLY_BALANCED) {
+            // cross-entropy to the locally balanced proposal at the first nt walkers' states
+            r = proposal_forward(prop, nt, L.spins, prop->logits.as<float>(), st);
+            if (r != RBMG_OK) return r;
+            RBMG_CK(launch_lb_target(P, nt, L.spins, L.theta, L.re, prop->logits.as<float>(), prop->O,
+                                     prop->dl32.as<float>(), st));
+        } else if (nt > 0) {
             // REINFORCE on the moves of the first nt walkers, from the states they started at
             r = proposal_forward(prop, nt, L.spins_pre, prop->logits.as<float>(), st);
             if (r != RBMG_OK) return r;
@@ -977,6 +1109,8 @@ extern "C" int rbmg_chain_learned_async(rbmg_chain* c, const rbmg_psi* psi, cons
                 prop->logits.as<float>(), nt, c->N, prop->O, L.site, L.len, L.reward, S->rbar.as<float>(),
                 prop->dl32.as<float>());
             RBMG_CK(cudaGetLastError());
+        }
+        if (nt > 0) {
             r = proposal_backward(prop, nt, st);
             if (r != RBMG_OK) return r;
             r = proposal_adam(prop, st);

@@ -102,15 +102,28 @@ __device__ __forceinline__ bool rbm_mh_step(const RbmDev& P, Spins<NW>& s, float
         rows[q] = P.W + static_cast<long>(site) * P.Mpad + lane;
     }
     float part = 0.0f;
+    if (ns == 1) {
+        // single flip: the K loads of the W row are issued together
+        float2 w[K];
 #pragma unroll
-    for (int k = 0; k < K; k++) {
-        float nr = tr[k], ni = ti[k];
-        for (int q = 0; q < ns; q++) {
-            const float2 w = __ldg(rows[q] + 32 * k);
-            nr = __fmaf_rn(two_s[q], w.x, nr);
-            ni = __fmaf_rn(two_s[q], w.y, ni);
+        for (int k = 0; k < K; k++) w[k] = __ldg(rows[0] + 32 * k);
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const float nr = __fmaf_rn(two_s[0], w[k].x, tr[k]);
+            const float ni = __fmaf_rn(two_s[0], w[k].y, ti[k]);
+            part = __fadd_rn(part, __fsub_rn(lc_re(nr, ni), re[k]));
         }
-        part = __fadd_rn(part, __fsub_rn(lc_re(nr, ni), re[k]));
+    } else {
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            float nr = tr[k], ni = ti[k];
+            for (int q = 0; q < ns; q++) {
+                const float2 w = __ldg(rows[q] + 32 * k);
+                nr = __fmaf_rn(two_s[q], w.x, nr);
+                ni = __fmaf_rn(two_s[q], w.y, ni);
+            }
+            part = __fadd_rn(part, __fsub_rn(lc_re(nr, ni), re[k]));
+        }
     }
     const float delta = warp_sum_xor(part);
     bool accept = delta > 0.0f;
@@ -130,22 +143,48 @@ __device__ __forceinline__ bool rbm_mh_step(const RbmDev& P, Spins<NW>& s, float
     return accept;
 }
 
-// sign * (-i)^ypow of string n for the current (original) spins
+// sign * (-i)^ypow * coef of string n for the current (original) spins, in FP32: the
+// local-energy sums run in FP32 with compensated (Kahan) accumulation, since GB300's
+// FP64 rate is 1/64 of its FP32 rate and every lane of the warp executes the sum
 template <int NW>
-__device__ __forceinline__ double2 string_factor(const OpDev& op, int n, const Spins<NW>& s) {
+__device__ __forceinline__ float2 string_factor(const OpDev& op, int n, const Spins<NW>& s) {
     int parity = 0;
 #pragma unroll
     for (int k = 0; k < NW; k++) parity += __popcll(op.zmask[n * kMaxWords + k] & ~s.w[k]);
-    const double sg = (parity & 1) ? -1.0 : 1.0;
-    const double2 c = op.coef[n];
+    const float2 c = op.coef32[n];
     const int yp = op.ypow[n] & 3;
-    // c * (-i)^yp * sg
-    double2 r;
-    if (yp == 0) r = make_double2(c.x, c.y);
-    else if (yp == 1) r = make_double2(c.y, -c.x);
-    else if (yp == 2) r = make_double2(-c.x, -c.y);
-    else r = make_double2(-c.y, c.x);
-    return make_double2(sg * r.x, sg * r.y);
+    float2 r;
+    if (yp == 0) r = c;
+    else if (yp == 1) r = make_float2(c.y, -c.x);
+    else if (yp == 2) r = make_float2(-c.x, -c.y);
+    else r = make_float2(-c.y, c.x);
+    return (parity & 1) ? make_float2(-r.x, -r.y) : r;
+}
+
+// compensated FP32 sum (Kahan 1965): the represented value is s - c
+struct KahanC {
+    float sr = 0.0f, si = 0.0f, cr = 0.0f, ci = 0.0f;
+    __device__ __forceinline__ void add(float x, float y) {
+        const float yr = __fsub_rn(x, cr), yi = __fsub_rn(y, ci);
+        const float tr = __fadd_rn(sr, yr), ti = __fadd_rn(si, yi);
+        cr = __fsub_rn(__fsub_rn(tr, sr), yr);
+        ci = __fsub_rn(__fsub_rn(ti, si), yi);
+        sr = tr;
+        si = ti;
+    }
+    __device__ __forceinline__ double2 value() const {
+        return make_double2(static_cast<double>(sr) - static_cast<double>(cr),
+                            static_cast<double>(si) - static_cast<double>(ci));
+    }
+};
+
+// coef * exp(d) for the complex log-ratio d
+__device__ __forceinline__ float2 string_term(float2 cf, float2 d) {
+    float sn, cs;
+    sincosf(d.y, &sn, &cs);
+    const float mag = expf(d.x);
+    const float xr = mag * cs, xi = mag * sn;
+    return make_float2(fmaf(cf.x, xr, -cf.y * xi), fmaf(cf.x, xi, cf.y * xr));
 }
 
 // Local energy E_loc(s) = sum_n coef_n phase_n exp(log psi(s'_n) - log psi(s))
@@ -157,19 +196,18 @@ __device__ __forceinline__ double2 rbm_local_energy(const RbmDev& P, const OpDev
                                                     const float (&tr)[K], const float (&ti)[K],
                                                     const float2 (&f)[K], const float2 (&T)[K], float2 (&U)[K],
                                                     float2* X, int lane) {
-    double er = 0.0, ei = 0.0;
+    KahanC acc;
     if (GRAD) {
 #pragma unroll
         for (int k = 0; k < K; k++) U[k] = make_float2(0.0f, 0.0f);
     }
     for (int n = 0; n < op.S; n++) {
-        const double2 cf = string_factor(op, n, s);
+        const float2 cf = string_factor(op, n, s);
         const int nf = op.nflip[n];
         if (nf == 0) {
-            er += cf.x;
-            ei += cf.y;
+            acc.add(cf.x, cf.y);
             if (GRAD) {
-                const float ex = static_cast<float>(cf.x), ey = static_cast<float>(cf.y);
+                const float ex = cf.x, ey = cf.y;
 #pragma unroll
                 for (int k = 0; k < K; k++) {
                     U[k].x += ex * T[k].x - ey * T[k].y;
@@ -200,17 +238,10 @@ __device__ __forceinline__ double2 rbm_local_energy(const RbmDev& P, const OpDev
             part.x += g.x - f[k].x;
             part.y += g.y - f[k].y;
         }
-        const float2 d = warp_sum_xor2(part);
-        float sn, cs;
-        sincosf(d.y, &sn, &cs);
-        const float mag = expf(d.x);
-        const double xr = static_cast<double>(mag * cs), xi = static_cast<double>(mag * sn);
-        const double e_r = cf.x * xr - cf.y * xi;
-        const double e_i = cf.x * xi + cf.y * xr;
-        er += e_r;
-        ei += e_i;
+        const float2 e = string_term(cf, warp_sum_xor2(part));
+        acc.add(e.x, e.y);
         if (GRAD) {
-            const float ex = static_cast<float>(e_r), ey = static_cast<float>(e_i);
+            const float ex = e.x, ey = e.y;
             float2* xrow = X + static_cast<long>(op.offdiag_slot[n]) * P.Mpad + lane;
 #pragma unroll
             for (int k = 0; k < K; k++) {
@@ -222,7 +253,7 @@ __device__ __forceinline__ double2 rbm_local_energy(const RbmDev& P, const OpDev
             }
         }
     }
-    return make_double2(er, ei);
+    return acc.value();
 }
 
 template <int K>
@@ -379,13 +410,12 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) rbm_eloc_kernel(RbmDev P,
     float2 f[K];
 #pragma unroll
     for (int k = 0; k < K; k++) f[k] = lc_c(tr[k], ti[k]);
-    double er = 0.0, ei = 0.0;
+    KahanC acc;
     for (int n = 0; n < op.S; n++) {
-        const double2 cf = string_factor(op, n, s);
+        const float2 cf = string_factor(op, n, s);
         const int nf = op.nflip[n];
         if (nf == 0) {
-            er += cf.x;
-            ei += cf.y;
+            acc.add(cf.x, cf.y);
             continue;
         }
         const int off = op.flip_off[n];
@@ -417,15 +447,10 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) rbm_eloc_kernel(RbmDev P,
                 part.y += g.y - f[k].y;
             }
         }
-        const float2 d = warp_sum_xor2(part);
-        float sn, cs;
-        sincosf(d.y, &sn, &cs);
-        const float mag = expf(d.x);
-        const double xr = static_cast<double>(mag * cs), xi = static_cast<double>(mag * sn);
-        er += cf.x * xr - cf.y * xi;
-        ei += cf.x * xi + cf.y * xr;
+        const float2 e = string_term(cf, warp_sum_xor2(part));
+        acc.add(e.x, e.y);
     }
-    if (lane == 0) L.eloc[t] = make_double2(er, ei);
+    if (lane == 0) L.eloc[t] = acc.value();
 }
 
 // ---------------------------------------------------------------------------

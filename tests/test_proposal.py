@@ -110,11 +110,51 @@ def small_rbm(N, M, sigma, seed):
     return rg.Psi(np.zeros(N), np.zeros(N), b, W, 1.0, False, True)
 
 
-def exact_probs(psi, N):
-    words = np.arange(2 ** N, dtype=np.uint64)
-    lp = psi.log_psi_batch(words)
-    w = np.exp(2 * (lp.real - lp.real.max()))
-    return w / w.sum()
+def chi_square(p, states, B):
+    """Chi-square of B sampled states against the probabilities p, states grouped (in
+    order of probability) to at least 20 expected counts; returns (chi2, dof)."""
+    counts = np.bincount(np.asarray(states, np.int64), minlength=p.size)
+    chi2, dof, e_acc, c_acc = 0.0, -1, 0.0, 0
+    for s in np.argsort(p):
+        e_acc += p[s] * B
+        c_acc += counts[s]
+        if e_acc >= 20:
+            chi2 += (c_acc - e_acc) ** 2 / e_acc
+            dof += 1
+            e_acc, c_acc = 0.0, 0
+    return chi2, dof
+
+
+def chi_square_ok(chi2, dof):
+    return chi2 < dof + 6 * np.sqrt(2 * dof)
+
+
+EXACT_N, EXACT_M, EXACT_SIGMA, EXACT_STEPS = 10, 20, 0.15, 500
+
+
+def exactness_setup():
+    """N=10 RBM (sigma 0.15) and a random, clearly non-uniform proposal network."""
+    from oracle import pyoracle as po
+    rng = np.random.default_rng(5)
+    b = rng.normal(0, EXACT_SIGMA, EXACT_M) + 1j * rng.normal(0, EXACT_SIGMA, EXACT_M)
+    W = rng.normal(0, EXACT_SIGMA, (EXACT_N, EXACT_M)) + 1j * rng.normal(0, EXACT_SIGMA, (EXACT_N, EXACT_M))
+    words = np.arange(2 ** EXACT_N, dtype=np.uint64)
+    lp = np.array([po.log_psi(po.RBM(b, W, 1.0), int(w)) for w in words]).real
+    p = np.exp(2 * (lp - lp.max()))
+    return b, W, lp, p / p.sum(), random_params(EXACT_N, 8)
+
+
+def test_chi_square_detects_a_chain_without_the_reverse_density():
+    """CPU emulation of the learned chain: the chi-square statistic of the GPU test
+    accepts the exact chain and rejects one that drops q(s|s') / q(s'|s)."""
+    _, _, lp, p, params = exactness_setup()
+    words = np.arange(2 ** EXACT_N, dtype=np.uint64).reshape(-1, 1)
+    logits, _ = pr.forward(params, words, EXACT_N, exact=True)
+    B = 8192
+    good, _ = pr.emulate_chain(lp, logits, EXACT_N, B, EXACT_STEPS, 1)
+    bad, _ = pr.emulate_chain(lp, logits, EXACT_N, B, EXACT_STEPS, 1, with_reverse=False)
+    assert chi_square_ok(*chi_square(p, good, B))
+    assert not chi_square_ok(*chi_square(p, bad, B))
 
 
 @pytest.mark.gpu
@@ -122,41 +162,52 @@ def test_learned_chain_samples_psi_squared():
     """A frozen, non-uniform proposal: the final states of 16384 independent walkers
     follow |psi|^2 (chi-square over states grouped to >= 20 expected counts)."""
     import rbmongpu_gb300 as rg
-    N, B = 10, 16384
-    psi = small_rbm(N, 20, 0.3, 5)
-    prop = rg.Proposal(N, seed=2)
-    pv = random_params(N, 8)
-    d = pr.unpack(pv, N)
-    d["W3"] *= 10.0            # strongly non-uniform seeds and lengths
-    prop.params = pr.pack(d, N)
+    B = 16384
+    b, W, _, p, params = exactness_setup()
+    psi = rg.Psi(np.zeros(EXACT_N), np.zeros(EXACT_N), b, W, 1.0, False, True)
+    prop = rg.Proposal(EXACT_N, seed=2)
+    prop.params = params
     chain = rg.Chain(psi, B, seed=77)
-    chain.learned_async(psi, None, prop, 400, train=0)
+    chain.learned_async(psi, None, prop, EXACT_STEPS, train=0)
     words, acc, props = chain.state()
-    assert props == 400 * B and 0 < acc < props
-    p = exact_probs(psi, N)
-    counts = np.bincount(words[:, 0].astype(np.int64), minlength=2 ** N)
-    order = np.argsort(p)
-    chi2, dof, e_acc, c_acc = 0.0, -1, 0.0, 0
-    for s in order:
-        e_acc += p[s] * B
-        c_acc += counts[s]
-        if e_acc >= 20:
-            chi2 += (c_acc - e_acc) ** 2 / e_acc
-            dof += 1
-            e_acc, c_acc = 0.0, 0
-    assert dof > 20, dof
-    assert chi2 < dof + 6 * np.sqrt(2 * dof), (chi2, dof)
+    assert props == EXACT_STEPS * B and 0.05 < acc / props < 1
+    chi2, dof = chi_square(p, words[:, 0], B)
+    assert dof > 100 and chi_square_ok(chi2, dof), (chi2, dof)
+
+
+def lb_marginals(psi, words, N):
+    """Seed and length marginals of the locally balanced proposal p*(i, l) propto
+    exp(Re log psi(s') - Re log psi(s)) over all N x 8 contiguous cluster flips."""
+    L = pr.LENGTHS
+    masks = np.zeros((N, L), np.uint64)
+    for i in range(N):
+        for l in range(1, L + 1):
+            masks[i, l - 1] = sum(1 << ((i + q) % N) for q in range(l))
+    w = np.asarray(words, np.uint64).reshape(-1)
+    lp0 = psi.log_psi_batch(w).real
+    moved = (w[:, None, None] ^ masks[None]).reshape(-1)
+    lp = psi.log_psi_batch(moved).real.reshape(len(w), N, L) - lp0[:, None, None]
+    p = np.exp(lp - lp.max(axis=(1, 2), keepdims=True))
+    p /= p.sum(axis=(1, 2), keepdims=True)
+    return p.sum(axis=2), p.sum(axis=1)
+
+
+def mean_kl(ps, pl, logits, N):
+    ls = logits[:, :N] - np.logaddexp.reduce(logits[:, :N], axis=1, keepdims=True)
+    ll = logits[:, N:] - np.logaddexp.reduce(logits[:, N:], axis=1, keepdims=True)
+    kl = (ps * (np.log(ps + 1e-300) - ls)).sum(axis=1) + (pl * (np.log(pl + 1e-300) - ll)).sum(axis=1)
+    return float(kl.mean())
 
 
 @pytest.mark.gpu
-def test_training_raises_accepted_moves_and_keeps_the_energy():
-    """N=20 RBM: after online training the frozen proposal accepts at least 1.5x as many
-    moves per step as the untrained (uniform seed and length) one, and the learned
-    chain's mean local energy agrees with exact summation."""
+def test_training_fits_the_locally_balanced_proposal():
+    """N=20 RBM (sigma 0.25): online training brings the proposal's seed and length
+    distributions to the locally balanced marginals (mean KL at the chain's states at
+    most half the untrained one), and the frozen trained proposal accepts at least 1.5x
+    as many moves as the untrained (uniform) one."""
     import rbmongpu_gb300 as rg
     N, B = 20, 4096
     psi = small_rbm(N, 40, 0.25, 6)
-    op = rg.Operator(*rg.operators.tfim_chain(N, 1.0, 1.0))
 
     def rate(chain, prop, steps):
         _, a0, p0 = chain.state()
@@ -168,16 +219,56 @@ def test_training_raises_accepted_moves_and_keeps_the_energy():
     chain = rg.Chain(psi, B, seed=5)
     chain.sweep_async(psi, None, 50)
     untrained = rate(chain, prop, 100)
-    chain.learned_async(psi, None, prop, 400, train=B)
+    words = chain.state()[0][:256]
+    ps, pl = lb_marginals(psi, words, N)
+    kl0 = mean_kl(ps, pl, prop.eval(words), N)
+    chain.learned_async(psi, None, prop, 600, train=1024)
+    words = chain.state()[0][:256]
+    ps, pl = lb_marginals(psi, words, N)
+    kl1 = mean_kl(ps, pl, prop.eval(words), N)
+    assert kl1 < 0.5 * kl0, (kl0, kl1)
     trained = rate(chain, prop, 100)
     assert trained >= 1.5 * untrained, (untrained, trained)
+
+
+@pytest.mark.gpu
+def test_trained_chain_energy_matches_exact_summation():
+    """N=20 RBM with sigma 0.12 (where single-flip chains equilibrate within a few
+    hundred sweeps): the frozen trained proposal's chain reproduces the exact energy
+    within 5 standard errors of its walker means (walkers are independent chains)."""
+    import rbmongpu_gb300 as rg
     import torch
-    rows = 40
+    N, B, rows = 20, 4096, 40
+    psi = small_rbm(N, 40, 0.12, 6)
+    op = rg.Operator(*rg.operators.tfim_chain(N, 1.0, 1.0))
+    prop = rg.Proposal(N, seed=4)
+    chain = rg.Chain(psi, B, seed=9)
+    chain.sweep_async(psi, None, 200)
+    chain.learned_async(psi, None, prop, 300, train=1024)
+    chain.learned_async(psi, None, prop, 500, train=0)
     el = torch.zeros((rows, B, 2), dtype=torch.float64, device="cuda")
     chain.learned_async(psi, op, prop, rows * 10, train=0, measure_every=10, d_eloc=el.data_ptr(),
                         stream=rg.library_stream())
     torch.cuda.synchronize()
     e = el[..., 0].cpu().numpy()
-    E = rg.ExpectationValue()(psi, op, rg.ExactSummation(N)) / psi.norm(rg.ExactSummation(N)) ** 2
-    se = e.mean(axis=1).std() / np.sqrt(rows) + e.std() / np.sqrt(e.size)
-    assert abs(e.mean() - E.real) < 6 * se + 1e-3, (e.mean(), E.real, se)
+    es = rg.ExactSummation(N)
+    E = rg.ExpectationValue()(psi, op, es) / psi.norm(es) ** 2
+    se = e.mean(axis=0).std() / np.sqrt(B)
+    assert abs(e.mean() - E.real) < 5 * se + 1e-3, (e.mean(), E.real, se)
+
+
+@pytest.mark.gpu
+def test_reinforce_objective_raises_the_acceptance():
+    import rbmongpu_gb300 as rg
+    N, B = 20, 4096
+    psi = small_rbm(N, 40, 0.25, 6)
+    prop = rg.Proposal(N, seed=3, objective=rg.Proposal.REINFORCE)
+    chain = rg.Chain(psi, B, seed=5)
+    chain.sweep_async(psi, None, 50)
+    _, a0, p0 = chain.state()
+    chain.learned_async(psi, None, prop, 100, train=0)
+    _, a1, p1 = chain.state()
+    chain.learned_async(psi, None, prop, 300, train=B)
+    chain.learned_async(psi, None, prop, 100, train=0)
+    _, a2, p2 = chain.state()
+    assert (a2 - a1) / (p2 - p1) >= 1.5 * (a1 - a0) / (p1 - p0)
