@@ -280,6 +280,15 @@ __global__ void weights_to_bf16_kernel(const float* w, int rows, int cols, int l
     out[t] = __float2bfloat16_rn(c < cols ? w[r * cols + c] : 0.0f);
 }
 
+// out[n][k] = bf16(w[k][n]) for a [rows][cols] FP32 matrix w, out [out_rows][ldo]; zero
+// outside (k >= rows or n >= cols)
+__global__ void weights_to_bf16_t_kernel(const float* w, int rows, int cols, int out_rows, int ldo, bf16* out) {
+    const long t = static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= static_cast<long>(out_rows) * ldo) return;
+    const int n = static_cast<int>(t / ldo), k = static_cast<int>(t % ldo);
+    out[t] = __float2bfloat16_rn(n < cols && k < rows ? w[static_cast<long>(k) * cols + n] : 0.0f);
+}
+
 inline unsigned blocks_for(long n, int threads = 256) { return static_cast<unsigned>((n + threads - 1) / threads); }
 
 }  // namespace rbmg
@@ -294,6 +303,9 @@ struct rbmg_proposal {
     size_t oW1 = 0, ob1 = 0, oW2 = 0, ob2 = 0, oW3 = 0, ob3 = 0;   // offsets in the FP32 parameter vector
     rbmg::DevBuf master, adam_m, adam_v, grad;
     rbmg::DevBuf w1, w2, w3;            // bf16 [N][H], [H][H], [H][Op]
+    // transposed bf16 copies for the fused inference kernel: [H][ldw1], [H][H], [w3_rows][H]
+    rbmg::DevBuf w1t, w2t, w3t;
+    int ldw1 = 0, w3_rows = 0;
     int cap = 0;                        // activation rows held
     rbmg::DevBuf x16, z1, h1, z2, h2;   // [cap][Np] bf16, [cap][H] f32 / bf16
     rbmg::DevBuf logits;                // [cap][O] f32 (training forward)
@@ -330,15 +342,23 @@ cudaError_t proposal_refresh_bf16(rbmg_proposal* p, cudaStream_t st) {
         w + p->oW2, kHidden, kHidden, kHidden, p->w2.as<bf16>());
     weights_to_bf16_kernel<<<blocks_for(static_cast<long>(kHidden) * p->Op), 256, 0, st>>>(w + p->oW3, kHidden, p->O,
                                                                                          p->Op, p->w3.as<bf16>());
+    weights_to_bf16_t_kernel<<<blocks_for(static_cast<long>(kHidden) * p->ldw1), 256, 0, st>>>(
+        w + p->oW1, p->N, kHidden, kHidden, p->ldw1, p->w1t.as<bf16>());
+    weights_to_bf16_t_kernel<<<blocks_for(static_cast<long>(kHidden) * kHidden), 256, 0, st>>>(
+        w + p->oW2, kHidden, kHidden, kHidden, kHidden, p->w2t.as<bf16>());
+    weights_to_bf16_t_kernel<<<blocks_for(static_cast<long>(p->w3_rows) * kHidden), 256, 0, st>>>(
+        w + p->oW3, kHidden, p->O, p->w3_rows, kHidden, p->w3t.as<bf16>());
     return cudaGetLastError();
 }
 
-// logits_out [count][O] of the configurations spins [count][nw]; activations kept in
+// logits_out [count][O] of the configurations spins [count][nw] (logits_out null: the
+// network's own logits buffer, valid only after the reserve below); activations kept in
 // the network's buffers for a following backward pass
 int proposal_forward(rbmg_proposal* p, int count, const uint64_t* spins, float* logits_out, cudaStream_t st) {
     if (count <= 0) return RBMG_OK;
     int r = proposal_reserve(p, count);
     if (r != RBMG_OK) return r;
+    if (!logits_out) logits_out = p->logits.as<float>();
     const int nw = nwords_of(p->N);
     const long xs = static_cast<long>(count) * p->Np;
     switch (nw) {
@@ -566,40 +586,6 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) learned_angles_kernel(Rbm
         const long o = static_cast<long>(w) * P.Mpad + lane + 32 * k;
         L.theta[o] = make_float2(tr[k], ti[k]);
         L.re[o] = lc_re(tr[k], ti[k]);
-    }
-}
-
-template <int NW>
-__global__ void __launch_bounds__(32 * kWarpsPerBlock) learned_propose_kernel(LearnedLaunch L) {
-    const int lane = threadIdx.x & 31;
-    const int w = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
-    if (w >= L.B) return;
-    WalkerRng rng;
-    rng.init(L.seed, static_cast<uint32_t>(w), L.rng_index[w]);
-    const float* row = L.logits_cur + static_cast<long>(w) * L.O;
-    const LogNorm ln = log_norms(row, L.N, lane);
-    const int i = draw_index(row, L.N, ln.seed, rng.uniform(), lane);
-    const int l = 1 + draw_index(row + L.N, kLengths, ln.len, rng.uniform(), lane);
-    if (lane == 0) {
-        Spins<NW> s;
-#pragma unroll
-        for (int k = 0; k < NW; k++) s.w[k] = L.spins[static_cast<long>(w) * NW + k];
-        if (L.spins_pre) {
-#pragma unroll
-            for (int k = 0; k < NW; k++) L.spins_pre[static_cast<long>(w) * NW + k] = s.w[k];
-        }
-        for (int q = 0; q < l; q++) {
-            int c = i + q;
-            if (c >= L.N) c -= L.N;
-            s.flip(c);
-        }
-#pragma unroll
-        for (int k = 0; k < NW; k++) L.spins_prop[static_cast<long>(w) * NW + k] = s.w[k];
-        L.site[w] = i;
-        L.len[w] = l;
-        L.logq_fwd[w] = (row[i] - ln.seed) + (row[L.N + l - 1] - ln.len);
-        L.rng_index[w] = rng.index;
-        L.proposals[w] += 1;
     }
 }
 
@@ -841,18 +827,6 @@ cudaError_t launch_learned(int which, const RbmDev& P, const LearnedLaunch& L, c
     }
 }
 
-cudaError_t launch_propose(const LearnedLaunch& L, cudaStream_t st) {
-    const dim3 grid((L.B + kWarpsPerBlock - 1) / kWarpsPerBlock), block(32 * kWarpsPerBlock);
-    switch (nwords_of(L.N)) {
-        case 1: learned_propose_kernel<1><<<grid, block, 0, st>>>(L); break;
-        case 2: learned_propose_kernel<2><<<grid, block, 0, st>>>(L); break;
-        case 3: learned_propose_kernel<3><<<grid, block, 0, st>>>(L); break;
-        case 4: learned_propose_kernel<4><<<grid, block, 0, st>>>(L); break;
-        default: return cudaErrorInvalidValue;
-    }
-    return cudaGetLastError();
-}
-
 template <int K>
 cudaError_t launch_lb_k(int nw, const RbmDev& P, int n, const uint64_t* spins, const float2* theta, const float* re,
                         const float* logits, int O, float* dl, cudaStream_t st) {
@@ -877,6 +851,229 @@ cudaError_t launch_lb_target(const RbmDev& P, int n, const uint64_t* spins, cons
         case 8: return launch_lb_k<8>(nw, P, n, spins, theta, re, logits, O, dl, st);
         case 13: return launch_lb_k<13>(nw, P, n, spins, theta, re, logits, O, dl, st);
         case 18: return launch_lb_k<18>(nw, P, n, spins, theta, re, logits, O, dl, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+// ============================================================================ fused inference
+// One CTA runs the whole network for 64 configurations with the activations in shared
+// memory: x [64][<=256] -> h1 -> h2 -> logits, the weights streamed through a
+// double-buffered cp.async pipeline in chunks of 32 input features (the same k order,
+// tile arithmetic and epilogue as the layer-by-layer GEMM path, so the logits agree bit
+// for bit).  With PROPOSE the CTA first draws the walkers' moves from their current
+// logits and evaluates the network on the proposed configurations.
+constexpr int kFRows = 64;                   // configurations per CTA
+constexpr int kFLd = kHidden + 8;            // activation row stride (bf16)
+constexpr int kFWLd = 40;                    // weight-chunk row stride (bf16)
+constexpr size_t kFSmem = 2 * sizeof(bf16) * kFRows * kFLd + 2 * sizeof(bf16) * kHidden * kFWLd;
+
+struct FusedNet {
+    int N, O, ldw1;
+    const bf16* w1t;   // [256][ldw1]
+    const bf16* w2t;   // [256][256]
+    const bf16* w3t;   // [passes * 128][256]
+    const float* b1;
+    const float* b2;
+    const float* b3;
+};
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int NPEND>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(NPEND)); }
+
+// acc = A [64][k] (shared, stride kFLd) x Wt^T, Wt [NT*32][ldw] (global, k contiguous);
+// 8 warps as 2 (rows) x 4 (columns), each 32 rows x NT*8 columns
+template <int NT>
+__device__ __forceinline__ void fused_layer(const bf16* sA, int kchunks, const bf16* Wt, int ldw, bf16* sW,
+                                            float (&acc)[2][NT][4]) {
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int wm = warp & 1, wn = warp >> 1;
+    const int gq = lane >> 2, tq = lane & 3;
+    constexpr int kOut = NT * 32;
+#pragma unroll
+    for (int i = 0; i < 2; i++)
+#pragma unroll
+        for (int j = 0; j < NT; j++)
+#pragma unroll
+            for (int e = 0; e < 4; e++) acc[i][j][e] = 0.0f;
+    auto issue = [&](int kc, int buf) {
+        bf16* dst = sW + buf * (kHidden * kFWLd);
+        for (int c = tid; c < kOut * 4; c += 256) {
+            const int n = c >> 2, q = (c & 3) * 8;
+            cp_async16(dst + n * kFWLd + q, Wt + static_cast<long>(n) * ldw + kc * 32 + q);
+        }
+        cp_async_commit();
+    };
+    issue(0, 0);
+    for (int kc = 0; kc < kchunks; kc++) {
+        if (kc + 1 < kchunks) {
+            issue(kc + 1, (kc + 1) & 1);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncthreads();
+        const bf16* w = sW + (kc & 1) * (kHidden * kFWLd);
+#pragma unroll
+        for (int ks = 0; ks < 32; ks += 16) {
+            uint32_t af[2][4], bfr[NT][2];
+            const int col = kc * 32 + ks + 2 * tq;
+#pragma unroll
+            for (int mi = 0; mi < 2; mi++) {
+                const int row = wm * 32 + mi * 16 + gq;
+                af[mi][0] = *reinterpret_cast<const uint32_t*>(sA + row * kFLd + col);
+                af[mi][1] = *reinterpret_cast<const uint32_t*>(sA + (row + 8) * kFLd + col);
+                af[mi][2] = *reinterpret_cast<const uint32_t*>(sA + row * kFLd + col + 8);
+                af[mi][3] = *reinterpret_cast<const uint32_t*>(sA + (row + 8) * kFLd + col + 8);
+            }
+#pragma unroll
+            for (int ni = 0; ni < NT; ni++) {
+                const int n = wn * NT * 8 + ni * 8 + gq;
+                bfr[ni][0] = *reinterpret_cast<const uint32_t*>(w + n * kFWLd + ks + 2 * tq);
+                bfr[ni][1] = *reinterpret_cast<const uint32_t*>(w + n * kFWLd + ks + 2 * tq + 8);
+            }
+#pragma unroll
+            for (int mi = 0; mi < 2; mi++)
+#pragma unroll
+                for (int ni = 0; ni < NT; ni++) mma_bf16_16816(acc[mi][ni], af[mi], bfr[ni]);
+        }
+        __syncthreads();
+    }
+}
+
+// h = bf16(silu(acc + b)) into dst [64][kFLd]
+__device__ __forceinline__ void fused_silu_store(const float (&acc)[2][8][4], const float* b, bf16* dst) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int wm = warp & 1, wn = warp >> 1, gq = lane >> 2, tq = lane & 3;
+#pragma unroll
+    for (int mi = 0; mi < 2; mi++)
+#pragma unroll
+        for (int ni = 0; ni < 8; ni++)
+#pragma unroll
+            for (int h = 0; h < 2; h++)
+#pragma unroll
+                for (int e = 0; e < 2; e++) {
+                    const int r = wm * 32 + mi * 16 + gq + 8 * h, n = wn * 64 + ni * 8 + 2 * tq + e;
+                    dst[r * kFLd + n] = __float2bfloat16_rn(silu_f(acc[mi][ni][h * 2 + e] + b[n]));
+                }
+}
+
+template <int NW, bool PROPOSE>
+__global__ void __launch_bounds__(256, 2) mlp_fused_kernel(FusedNet net, LearnedLaunch L, const uint64_t* in_spins,
+                                                           int count, float* logits_out) {
+    extern __shared__ __align__(16) unsigned char fsm[];
+    bf16* sX = reinterpret_cast<bf16*>(fsm);
+    bf16* sH = sX + kFRows * kFLd;
+    bf16* sW = sH + kFRows * kFLd;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int row0 = blockIdx.x * kFRows;
+    // ---- the input configurations (proposed moves with PROPOSE), one warp per row
+    for (int r = warp; r < kFRows; r += 8) {
+        const int w = row0 + r;
+        Spins<NW> s;
+#pragma unroll
+        for (int k = 0; k < NW; k++) s.w[k] = 0;
+        if (w < count) {
+            if (PROPOSE) {
+                WalkerRng rng;
+                rng.init(L.seed, static_cast<uint32_t>(w), L.rng_index[w]);
+                const float* row = L.logits_cur + static_cast<long>(w) * L.O;
+                const LogNorm ln = log_norms(row, L.N, lane);
+                const int i = draw_index(row, L.N, ln.seed, rng.uniform(), lane);
+                const int l = 1 + draw_index(row + L.N, kLengths, ln.len, rng.uniform(), lane);
+#pragma unroll
+                for (int k = 0; k < NW; k++) s.w[k] = L.spins[static_cast<long>(w) * NW + k];
+                if (lane == 0 && L.spins_pre) {
+#pragma unroll
+                    for (int k = 0; k < NW; k++) L.spins_pre[static_cast<long>(w) * NW + k] = s.w[k];
+                }
+                for (int q = 0; q < l; q++) {
+                    int c = i + q;
+                    if (c >= L.N) c -= L.N;
+                    s.flip(c);
+                }
+                if (lane == 0) {
+#pragma unroll
+                    for (int k = 0; k < NW; k++) L.spins_prop[static_cast<long>(w) * NW + k] = s.w[k];
+                    L.site[w] = i;
+                    L.len[w] = l;
+                    L.logq_fwd[w] = (row[i] - ln.seed) + (row[L.N + l - 1] - ln.len);
+                    L.rng_index[w] = rng.index;
+                    L.proposals[w] += 1;
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < NW; k++) s.w[k] = in_spins[static_cast<long>(w) * NW + k];
+            }
+        }
+        for (int i = lane; i < net.ldw1; i += 32) {
+            const float v = (w < count && i < net.N) ? (s.up(i) ? 1.0f : -1.0f) : 0.0f;
+            sX[r * kFLd + i] = __float2bfloat16_rn(v);
+        }
+    }
+    __syncthreads();
+    {
+        float acc[2][8][4];
+        fused_layer<8>(sX, net.ldw1 / 32, net.w1t, net.ldw1, sW, acc);
+        fused_silu_store(acc, net.b1, sH);
+        __syncthreads();
+        fused_layer<8>(sH, kHidden / 32, net.w2t, kHidden, sW, acc);
+        fused_silu_store(acc, net.b2, sX);
+        __syncthreads();
+    }
+    const int wm = warp & 1, wn = warp >> 1, gq = lane >> 2, tq = lane & 3;
+    for (int pass = 0; pass * 128 < net.O; pass++) {
+        float acc[2][4][4];
+        fused_layer<4>(sX, kHidden / 32, net.w3t + static_cast<long>(pass) * 128 * kHidden, kHidden, sW, acc);
+#pragma unroll
+        for (int mi = 0; mi < 2; mi++)
+#pragma unroll
+            for (int ni = 0; ni < 4; ni++)
+#pragma unroll
+                for (int h = 0; h < 2; h++)
+#pragma unroll
+                    for (int e = 0; e < 2; e++) {
+                        const int r = wm * 32 + mi * 16 + gq + 8 * h;
+                        const int n = pass * 128 + wn * 32 + ni * 8 + 2 * tq + e;
+                        if (row0 + r < count && n < net.O)
+                            logits_out[static_cast<long>(row0 + r) * net.O + n] = acc[mi][ni][h * 2 + e] + net.b3[n];
+                    }
+    }
+}
+
+FusedNet fused_net(const rbmg_proposal* p) {
+    const float* w = p->master.as<float>();
+    return FusedNet{p->N, p->O, p->ldw1, p->w1t.as<bf16>(), p->w2t.as<bf16>(), p->w3t.as<bf16>(),
+                    w + p->ob1, w + p->ob2, w + p->ob3};
+}
+
+template <int NW, bool PROPOSE>
+cudaError_t launch_fused_nw(const FusedNet& net, const LearnedLaunch& L, const uint64_t* in, int count, float* out,
+                            cudaStream_t st) {
+    // the attribute belongs to the current device's context: set it on every launch
+    const cudaError_t e = cudaFuncSetAttribute(mlp_fused_kernel<NW, PROPOSE>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kFSmem));
+    if (e != cudaSuccess) return e;
+    mlp_fused_kernel<NW, PROPOSE><<<(count + kFRows - 1) / kFRows, 256, kFSmem, st>>>(net, L, in, count, out);
+    return cudaGetLastError();
+}
+
+// logits of `count` configurations (PROPOSE = false: in_spins) or of the walkers' proposed
+// moves (PROPOSE = true: drawn from L.logits_cur, written to L's move buffers)
+template <bool PROPOSE>
+cudaError_t launch_fused(const rbmg_proposal* p, const LearnedLaunch& L, const uint64_t* in, int count, float* out,
+                         cudaStream_t st) {
+    if (count <= 0) return cudaSuccess;
+    const FusedNet net = fused_net(p);
+    switch (nwords_of(p->N)) {
+        case 1: return launch_fused_nw<1, PROPOSE>(net, L, in, count, out, st);
+        case 2: return launch_fused_nw<2, PROPOSE>(net, L, in, count, out, st);
+        case 3: return launch_fused_nw<3, PROPOSE>(net, L, in, count, out, st);
+        case 4: return launch_fused_nw<4, PROPOSE>(net, L, in, count, out, st);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -933,6 +1130,11 @@ extern "C" int rbmg_proposal_create(int N, uint64_t seed, float lr, rbmg_proposa
     RBMG_CK(p->w1.ensure(sizeof(bf16) * static_cast<size_t>(N) * H));
     RBMG_CK(p->w2.ensure(sizeof(bf16) * static_cast<size_t>(H) * H));
     RBMG_CK(p->w3.ensure(sizeof(bf16) * static_cast<size_t>(H) * p->Op));
+    p->ldw1 = (N + 31) / 32 * 32;
+    p->w3_rows = (p->O + 127) / 128 * 128;
+    RBMG_CK(p->w1t.ensure(sizeof(bf16) * static_cast<size_t>(H) * p->ldw1));
+    RBMG_CK(p->w2t.ensure(sizeof(bf16) * static_cast<size_t>(H) * H));
+    RBMG_CK(p->w3t.ensure(sizeof(bf16) * static_cast<size_t>(p->w3_rows) * H));
     RBMG_CK(cudaMemcpy(p->master.p, h.data(), sizeof(float) * p->P, cudaMemcpyHostToDevice));
     RBMG_CK(cudaMemset(p->adam_m.p, 0, sizeof(float) * p->P));
     RBMG_CK(cudaMemset(p->adam_v.p, 0, sizeof(float) * p->P));
@@ -982,8 +1184,13 @@ extern "C" int rbmg_proposal_eval(rbmg_proposal* p, int count, const uint64_t* s
     RBMG_CK(dsp.ensure(sizeof(uint64_t) * nw * count));
     RBMG_CK(dlog.ensure(sizeof(float) * static_cast<size_t>(count) * p->O));
     RBMG_CK(cudaMemcpyAsync(dsp.p, spins, sizeof(uint64_t) * nw * count, cudaMemcpyHostToDevice, st));
-    int r = proposal_forward(p, count, dsp.as<uint64_t>(), dlog.as<float>(), st);
-    if (r != RBMG_OK) return r;
+    int r = RBMG_OK;
+    if (dlogits) {
+        r = proposal_forward(p, count, dsp.as<uint64_t>(), dlog.as<float>(), st);
+        if (r != RBMG_OK) return r;
+    } else {
+        RBMG_CK(launch_fused<false>(p, LearnedLaunch{}, dsp.as<uint64_t>(), count, dlog.as<float>(), st));
+    }
     RBMG_CK(cudaMemcpyAsync(logits, dlog.p, sizeof(float) * count * p->O, cudaMemcpyDeviceToHost, st));
     if (dlogits) {
         RBMG_CK(cudaMemcpyAsync(p->dl32.p, dlogits, sizeof(float) * count * p->O, cudaMemcpyHostToDevice, st));
@@ -1082,27 +1289,25 @@ extern "C" int rbmg_chain_learned_async(rbmg_chain* c, const rbmg_psi* psi, cons
     // the angles and logits of the current states (plain sweeps or new weights may
     // have changed them since the last call)
     RBMG_CK(launch_learned(0, P, L, st));
-    int r = proposal_forward(prop, B, L.spins, L.logits_cur, st);
-    if (r != RBMG_OK) return r;
+    RBMG_CK(launch_fused<false>(prop, L, L.spins, B, L.logits_cur, st));
+    int r = RBMG_OK;
     const int nt = std::min(train, B);
     OpDev od;
     if (op) od = op->dev();
     double2* out = static_cast<double2*>(d_eloc_out);
     const int lead = d_eloc_out ? n_steps % measure_every : n_steps;
     for (int step = 0; step < n_steps; step++) {
-        RBMG_CK(launch_propose(L, st));
-        r = proposal_forward(prop, B, L.spins_prop, S->logits_prop.as<float>(), st);
-        if (r != RBMG_OK) return r;
+        RBMG_CK(launch_fused<true>(prop, L, nullptr, B, S->logits_prop.as<float>(), st));
         RBMG_CK(launch_learned(1, P, L, st));
         if (nt > 0 && prop->objective == RBMG_PROPOSAL_LOCALLY_BALANCED) {
             // cross-entropy to the locally balanced proposal at the first nt walkers' states
-            r = proposal_forward(prop, nt, L.spins, prop->logits.as<float>(), st);
+            r = proposal_forward(prop, nt, L.spins, nullptr, st);
             if (r != RBMG_OK) return r;
             RBMG_CK(launch_lb_target(P, nt, L.spins, L.theta, L.re, prop->logits.as<float>(), prop->O,
                                      prop->dl32.as<float>(), st));
         } else if (nt > 0) {
             // REINFORCE on the moves of the first nt walkers, from the states they started at
-            r = proposal_forward(prop, nt, L.spins_pre, prop->logits.as<float>(), st);
+            r = proposal_forward(prop, nt, L.spins_pre, nullptr, st);
             if (r != RBMG_OK) return r;
             reward_mean_kernel<<<1, 256, 0, st>>>(L.reward, nt, S->rbar.as<float>());
             reinforce_kernel<<<(nt + kWarpsPerBlock - 1) / kWarpsPerBlock, 32 * kWarpsPerBlock, 0, st>>>(
@@ -1116,8 +1321,7 @@ extern "C" int rbmg_chain_learned_async(rbmg_chain* c, const rbmg_psi* psi, cons
             r = proposal_adam(prop, st);
             if (r != RBMG_OK) return r;
             // the walkers' current logits under the new weights
-            r = proposal_forward(prop, B, L.spins, L.logits_cur, st);
-            if (r != RBMG_OK) return r;
+            RBMG_CK(launch_fused<false>(prop, L, L.spins, B, L.logits_cur, st));
         }
         if (d_eloc_out && step >= lead && (step - lead + 1) % measure_every == 0) {
             EstLaunch E{};

@@ -35,8 +35,8 @@ __device__ __forceinline__ void rbm_refresh(const RbmDev& P, const Spins<NW>& s,
     }
 }
 
-template <int NW>
-__device__ __forceinline__ void draw_spins(WalkerRng& rng, int N, Spins<NW>& s) {
+template <int NW, class Rng>
+__device__ __forceinline__ void draw_spins(Rng& rng, int N, Spins<NW>& s) {
 #pragma unroll
     for (int k = 0; k < NW; k++) {
         const uint64_t lo = rng.next();
@@ -47,7 +47,8 @@ __device__ __forceinline__ void draw_spins(WalkerRng& rng, int N, Spins<NW>& s) 
 }
 
 // include/random.h:60-79 with 64-bit masks (single word, N <= 64)
-__device__ __forceinline__ uint64_t draw_n_over_k(WalkerRng& rng, unsigned n, unsigned k) {
+template <class Rng>
+__device__ __forceinline__ uint64_t draw_n_over_k(Rng& rng, unsigned n, unsigned k) {
     const uint64_t mask = n >= 64 ? ~0ull : ((1ull << n) - 1ull);
     uint64_t w = rng.next();
     w |= static_cast<uint64_t>(rng.next()) << 32;
@@ -69,18 +70,18 @@ __device__ __forceinline__ uint64_t draw_n_over_k(WalkerRng& rng, unsigned n, un
 // site `u32 % N` (and a partner with the same new spin under S_z symmetry), update the
 // angles of the trial state, accept if Delta > 0 or u <= exp(2 Delta), u drawn only
 // when Delta <= 0.
-template <int K, int NW>
+template <int K, int NW, class Rng>
 __device__ __forceinline__ bool rbm_mh_step(const RbmDev& P, Spins<NW>& s, float (&tr)[K], float (&ti)[K],
-                                            float (&re)[K], WalkerRng& rng, int lane, int total_z) {
-    const int N = P.N;
+                                            float (&re)[K], Rng& rng, int lane, int total_z, uint64_t nmagic) {
+    const uint32_t N = static_cast<uint32_t>(P.N);
     int sites[2];
     int ns = 1;
-    sites[0] = static_cast<int>(rng.next() % static_cast<uint32_t>(N));
+    sites[0] = static_cast<int>(fastmod(rng.next(), nmagic, N));
     if (total_z) {
         const bool first_new = !s.up(sites[0]);
         int sec = sites[0];
         for (int guard = 0; guard < (1 << 20); guard++) {
-            const int c = static_cast<int>(rng.next() % static_cast<uint32_t>(N));
+            const int c = static_cast<int>(fastmod(rng.next(), nmagic, N));
             const bool v = c == sites[0] ? first_new : s.up(c);
             if (v == first_new) { sec = c; break; }
         }
@@ -273,12 +274,13 @@ __device__ __forceinline__ double2 warp_log_psi(const float2 (&f)[K]) {
 // the sampler's register footprint to the walker state.
 // ---------------------------------------------------------------------------
 template <int K, int NW>
-__global__ void __launch_bounds__(32 * kWarpsPerBlock) rbm_mc_kernel(RbmDev P, McLaunch L) {
+__global__ void __launch_bounds__(32 * kWarpsPerBlock, K > 13 ? 3 : 4) rbm_mc_kernel(RbmDev P, McLaunch L) {
     const int lane = threadIdx.x & 31;
     const int w = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
     if (w >= L.B) return;
-    WalkerRng rng;
-    rng.init(L.seed, L.walker_base + static_cast<uint32_t>(w), L.rng_index[w]);
+    WarpRng rng;
+    rng.init(L.seed, L.walker_base + static_cast<uint32_t>(w), L.rng_index[w], lane);
+    const uint64_t nmagic = fastmod_magic(static_cast<uint32_t>(P.N));
     Spins<NW> s;
     if (L.init) {
 #pragma unroll
@@ -297,7 +299,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) rbm_mc_kernel(RbmDev P, M
         rbm_refresh(P, s, tr, ti, lane);
 #pragma unroll
         for (int k = 0; k < K; k++) re[k] = lc_re(tr[k], ti[k]);
-        for (int p = 0; p < P.N; p++) acc += rbm_mh_step(P, s, tr, ti, re, rng, lane, L.total_z);
+        for (int p = 0; p < P.N; p++) acc += rbm_mh_step(P, s, tr, ti, re, rng, lane, L.total_z, nmagic);
         props += P.N;
         const int done = sw + 1 - L.n_therm;
         if (done > 0 && done % L.sweeps_per_sample == 0) {
