@@ -167,6 +167,20 @@ RBMG_API int rbmg_ev_fluctuation(const rbmg_psi* psi, const rbmg_operator* op, r
 RBMG_API int rbmg_ev_gradient(const rbmg_psi* psi, const rbmg_operator* op, rbmg_ensemble* ens, double* grad /* [2P] */,
                      double* value /* [2] */);
 
+/* Extension (no reference counterpart): local energies of `count` given configurations
+ * (spins [count][ceil(N/64)]) -> out [2 count]; the reference computes them only inside
+ * its ensembles' foreach (include/operator/Operator.hpp:90-115). */
+RBMG_API int rbmg_local_energies(const rbmg_psi* psi, const rbmg_operator* op, int count, const uint64_t* spins,
+                                 double* out);
+/* Extension (PsiDeep): gradient of the local energy by a hand-written adjoint (reverse
+ * mode) kernel that recomputes every forward pass, in PyTorch's convention for a real
+ * loss L: grad_k = dL/dRe(theta_k) + i dL/dIm(theta_k).  score = 0: L = Re <E_loc> over
+ * the ensemble's samples held fixed; score = 1: L = <H>, adding the sampling term, which
+ * equals rbmg_ev_gradient except at the final weights (include/quantum_state/PsiDeep.hpp:285-292
+ * scales their O_k by log psi; here d log psi / d w_final = activation). */
+RBMG_API int rbmg_ev_eloc_gradient(const rbmg_psi* psi, const rbmg_operator* op, rbmg_ensemble* ens, int score,
+                                   double* grad /* [2P] */, double* value /* [2] */);
+
 /* ---------------------------------------------------------------- HilbertSpaceDistance
  * (source/network_functions/HilbertSpaceDistance.cu:14-269, HilbertSpaceDistance_PsiPair.cu:99-169,
  * pyRBMonGPU/main.cpp:342-418).  The ensemble samples psi. */

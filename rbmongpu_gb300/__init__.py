@@ -9,9 +9,9 @@ runs in the CUDA library ``librbmg.so`` (include/rbmg.h) through ctypes.
 from . import operators
 from .api import (Chain, ExactSummation, ExpectationValue, HilbertSpaceDistance, MonteCarloLoop, Operator, Psi, PsiDeep,
                   PsiPair, Proposal, RbmgError, Spins, activation_function, new_deep_neural_network, new_neural_network,
-                  psi_O_k_vector, setDevice, start_profiling, stop_profiling, library_stream)
+                  psi_O_k_vector, local_energies, setDevice, start_profiling, stop_profiling, library_stream)
 
 __all__ = ["Chain", "Proposal", "library_stream", "Psi", "PsiDeep", "PsiPair", "Operator", "Spins", "MonteCarloLoop", "ExactSummation",
-           "ExpectationValue", "HilbertSpaceDistance", "psi_O_k_vector", "activation_function", "setDevice",
+           "ExpectationValue", "HilbertSpaceDistance", "psi_O_k_vector", "local_energies", "activation_function", "setDevice",
            "start_profiling", "stop_profiling", "new_neural_network", "new_deep_neural_network", "RbmgError",
            "operators"]

@@ -68,6 +68,8 @@ SIGNATURES = {
     "rbmg_ev_values": [_vp, _vpp, C.c_int, _vp, _dp],
     "rbmg_ev_fluctuation": [_vp, _vp, _vp, _dp, _dp],
     "rbmg_ev_gradient": [_vp, _vp, _vp, _dp, _dp],
+    "rbmg_local_energies": [_vp, _vp, C.c_int, _u64p, _dp],
+    "rbmg_ev_eloc_gradient": [_vp, _vp, _vp, C.c_int, _dp, _dp],
     "rbmg_hsd_distance": [_vp, _vp, _vp, C.c_int, _vp, _dp],
     "rbmg_hsd_gradient": [_vp, _vp, _vp, C.c_int, _vp, C.c_float, _dp, _dp],
     "rbmg_chain_create": [_vp, C.c_uint32, C.c_uint64, _vpp],

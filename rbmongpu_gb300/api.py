@@ -527,6 +527,24 @@ class ExpectationValue:
         call("rbmg_ev_gradient", psi._h, operator_._h, spin_ensemble._h, _p(g.view(np.float64)), _p(out))
         return g, complex(out[0], out[1])
 
+    def eloc_gradient(self, psi, operator_, spin_ensemble, score=True):
+        """Extension (PsiDeep): the adjoint-kernel gradient, in PyTorch's convention
+        dL/dRe + i dL/dIm.  score=False: L = Re <E_loc> on the ensemble's samples held
+        fixed; score=True: L = <H> (the sampling term included).  -> (grad[P], <E_loc>)"""
+        g = np.zeros(psi.num_params, np.complex128)
+        out = np.zeros(2)
+        call("rbmg_ev_eloc_gradient", psi._h, operator_._h, spin_ensemble._h, int(bool(score)),
+             _p(g.view(np.float64)), _p(out))
+        return g, complex(out[0], out[1])
+
+
+def local_energies(psi, operator_, spins_words):
+    """Extension: E_loc of given configurations (uint64 words [count][nwords])."""
+    w = np.ascontiguousarray(spins_words, np.uint64).reshape(-1, nwords(psi.N))
+    out = np.zeros(2 * len(w))
+    call("rbmg_local_energies", psi._h, operator_._h, len(w), _p(w, _u64p), _p(out))
+    return out.view(np.complex128)
+
 
 class HilbertSpaceDistance:
     """source/network_functions/HilbertSpaceDistance.cu (pyRBMonGPU/main.cpp:342-418)."""

@@ -1055,6 +1055,118 @@ extern "C" int rbmg_ev_gradient(const rbmg_psi* psi, const rbmg_operator* op, rb
     return RBMG_OK;
 }
 
+// local energies of given configurations (extension: the reference evaluates them only
+// inside its ensembles' foreach, Operator.hpp:90-115); FP64 estimator path for PsiDeep
+extern "C" int rbmg_local_energies(const rbmg_psi* psi, const rbmg_operator* op, int count, const uint64_t* spins,
+                                   double* out) {
+    if (!psi || !op || count < 0 || (count > 0 && (!spins || !out))) return fail(RBMG_EINVAL, "local energies: bad arguments");
+    if (op->max_site >= psi->N) return fail(RBMG_EINVAL, "local energies: operator acts on a site >= N");
+    if (count == 0) return RBMG_OK;
+    const int nw = nwords_of(psi->N);
+    Workspace& W = ws();
+    RBMG_CK(W.sample_spins.ensure(sizeof(uint64_t) * nw * count));
+    RBMG_CK(cudaMemcpyAsync(W.sample_spins.p, spins, sizeof(uint64_t) * nw * count, cudaMemcpyHostToDevice, stream()));
+    Chunk c;
+    c.count = count;
+    c.spins = W.sample_spins.as<uint64_t>();
+    const double2* e = nullptr;
+    const int r = chunk_eloc(psi, op, c, &e);
+    if (r != RBMG_OK) return r;
+    RBMG_CK(cudaMemcpyAsync(out, e, sizeof(double2) * count, cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaStreamSynchronize(stream()));
+    return RBMG_OK;
+}
+
+// ====================================================================== adjoint
+namespace rbmg {
+int deep_adjoint_chunk(const rbmg_psi* psi, const rbmg_operator* op, const Chunk& c, int score, double2* d_eloc,
+                       double2* G, double2* GO, const std::vector<size_t>& goff, cudaStream_t st);
+}  // namespace rbmg
+
+// Gradient of the local energy by the adjoint kernel (extension, PsiDeep): in PyTorch's
+// convention for a real loss, grad_k = dL/dRe(theta_k) + i dL/dIm(theta_k), with
+//   score = 0: L = Re <E_loc> over the ensemble's samples held fixed, i.e.
+//              grad = conj(<sum_n e_n O(s'_n) - E_loc O(s)>);
+//   score = 1: L = <H>, adding the sampling term 2 <(Re E_loc - <Re E>) O*>, so that
+//              grad equals the reference's estimator (ExpectationValue.cu:243-253) except
+//              at the final weights, whose derivative is the last layer's activation here
+//              and activation * log psi there (PsiDeep.hpp:285-292).
+extern "C" int rbmg_ev_eloc_gradient(const rbmg_psi* psi, const rbmg_operator* op, rbmg_ensemble* ens, int score,
+                                     double* grad, double* value) {
+    if (!op || !grad || !value) return fail(RBMG_EINVAL, "adjoint: null");
+    int r = check_pair(psi, op, ens);
+    if (r != RBMG_OK) return r;
+    if (psi->kind != 1) return fail(RBMG_EUNSUPPORTED, "adjoint: PsiDeep only");
+    if (psi->translational_invariance) return fail(RBMG_EUNSUPPORTED, "adjoint: translational averaging not provided");
+    const int N = psi->N, P = psi->num_params();
+    const int L = static_cast<int>(psi->layers.size());
+    std::vector<size_t> goff;
+    size_t tot = 0;
+    for (int l = 0; l < L; l++) {
+        const int size = psi->layers[l].size, in = l == 0 ? N : psi->layers[l - 1].size;
+        goff.push_back(tot);
+        tot += static_cast<size_t>(size) * in;
+        goff.push_back(tot);
+        tot += size;
+    }
+    goff.push_back(tot);
+    tot += psi->layers[L - 1].size;
+    Workspace& W = ws();
+    // G: sum over configurations of alpha delta (x) a; GO: sum over samples of w O(s)
+    RBMG_CK(W.acc_O.ensure(sizeof(double2) * tot));
+    RBMG_CK(W.acc_EO.ensure(sizeof(double2) * tot));
+    RBMG_CK(cudaMemsetAsync(W.acc_O.p, 0, sizeof(double2) * tot, stream()));
+    RBMG_CK(cudaMemsetAsync(W.acc_EO.p, 0, sizeof(double2) * tot, stream()));
+    RBMG_CK(W.sums.ensure(sizeof(double2) * kMaxSeries));
+    RBMG_CK(W.block_scratch.ensure(sizeof(double2) * kSumBlocks * kMaxSeries));
+    RBMG_CK(cudaMemsetAsync(W.sums.p, 0, sizeof(double2) * kMaxSeries, stream()));
+    StreamResult res;
+    r = run_stream(ens, psi, op, false, 4096, &res, [&](const Chunk& c) -> int {
+        RBMG_CK(W.eloc.ensure(sizeof(double2) * c.count));
+        const int rr = deep_adjoint_chunk(psi, op, c, score, W.eloc.as<double2>(), W.acc_O.as<double2>(),
+                                          W.acc_EO.as<double2>(), goff, stream());
+        if (rr != RBMG_OK) return rr;
+        SeriesSet set{};
+        set.n = 1;
+        set.v[0] = W.eloc.as<double2>();
+        RBMG_CK(launch_weighted_sums(c.count, c.weights, set, W.block_scratch.as<double2>(), W.sums.as<double2>(),
+                                     stream()));
+        return RBMG_OK;
+    });
+    if (r != RBMG_OK) return r;
+    std::vector<double2> G(tot), GO(tot);
+    double2 Es;
+    RBMG_CK(cudaMemcpyAsync(G.data(), W.acc_O.p, sizeof(double2) * tot, cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaMemcpyAsync(GO.data(), W.acc_EO.p, sizeof(double2) * tot, cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaMemcpyAsync(&Es, W.sums.p, sizeof(double2), cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaStreamSynchronize(stream()));
+    const double f = res.norm_factor;
+    const double e_mean = score ? Es.x * f : 0.0;   // <Re E_loc> of this same pass
+    cplx* g = reinterpret_cast<cplx*>(grad);
+    for (int k = 0; k < P; k++) g[k] = 0.0;
+    auto put = [&](size_t k, size_t q) {
+        const cplx v = cplx(G[q].x, G[q].y) - 2.0 * e_mean * cplx(GO[q].x, GO[q].y);
+        g[k] = std::conj(v * f);
+    };
+    size_t k = 2 * static_cast<size_t>(N);
+    for (int l = 0; l < L; l++) {
+        const DeepLayerHost& ly = psi->layers[l];
+        const int in = l == 0 ? N : psi->layers[l - 1].size;
+        for (int j = 0; j < ly.size; j++) put(k + j, goff[2 * l + 1] + j);
+        k += ly.size;
+        for (int c = 0; c < ly.conn; c++)
+            for (int j = 0; j < ly.size; j++) {
+                const int i = static_cast<int>(ly.connections[static_cast<size_t>(c) * ly.size + j]);
+                put(k + static_cast<size_t>(c) * ly.size + j, goff[2 * l] + static_cast<size_t>(j) * in + i);
+            }
+        k += static_cast<size_t>(ly.conn) * ly.size;
+    }
+    for (int j = 0; j < psi->layers[L - 1].size; j++) put(k + j, goff[2 * L] + j);
+    value[0] = Es.x * f;
+    value[1] = Es.y * f;
+    return RBMG_OK;
+}
+
 // ====================================================================== HSD
 namespace rbmg {
 int deep_hsd64_chunk(const rbmg_psi* psi, const rbmg_psi* pp, const rbmg_operator* op, const Chunk& c,

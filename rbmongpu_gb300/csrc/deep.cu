@@ -527,6 +527,198 @@ __global__ void deep_mc_kernel(DeepNetDev n0, DeepNetDev n1, int pair, McLaunch 
     }
 }
 
+// ---------------------------------------------------------------- adjoint of E_loc
+// Extension (no reference counterpart): reverse-mode derivative of the local energy,
+//   d E_loc(s) / d theta = sum_n e_n O(s'_n) - E_loc(s) O(s),  e_n = c_n psi(s'_n) / psi(s),
+// with O = d log psi / d theta (holomorphic, final weights d log psi / d fw_j = act_j).
+// Per configuration x the reverse pass yields the error vector delta_l(x) = d log psi /
+// d z_l of every layer; the parameter gradient is then the weighted sum over
+// configurations of the outer products delta_l(x) (x) a_{l-1}(x), formed as batched
+// reductions over all configurations of a chunk.  Every forward pass is recomputed
+// from the spins (no angles are kept per walker between calls).
+
+// delta_l for every layer after forward_once<STORE>; emit(layer, unit, delta)
+template <typename V, bool REAL, typename Emit>
+__device__ void backward_deltas(const DeepNetDev& net, Work<V>& w, Emit emit) {
+    const int t = threadIdx.x;
+    const int L = net.L;
+    V* cur = w.in;
+    V* nxt = w.out;
+    for (int l = L - 1; l >= 0; l--) {
+        const int size = net.size[l];
+        V d = czero<V>();
+        if (t < size) {
+            const V ang = w.angles[net.begin_angle[l] + t];
+            if (l == L - 1) {
+                d = cmul(W_of<V>::fw(net)[t], dact<REAL>(ang));
+            } else {
+                const int nsize = net.size[l + 1];
+                V acc = czero<V>();
+                const V* wn = W_of<V>::w(net, l + 1);
+                for (int e = net.rptr[l][t]; e < net.rptr[l][t + 1]; e++) {
+                    const int q = net.rq[l][e];
+                    acc = cadd(acc, cmul(wn[q], nxt[q % nsize]));
+                }
+                d = cmul(acc, dact<REAL>(ang));
+            }
+        }
+        __syncthreads();
+        if (t < size) {
+            cur[t] = d;
+            emit(l, t, d);
+        }
+        __syncthreads();
+        V* tmp = cur;
+        cur = nxt;
+        nxt = tmp;
+    }
+}
+
+// One CTA per sample: E_loc(s) (FP32 passes, FP64 sum), then for every configuration x
+// of the sample (x = s first, then s'_n for the off-diagonal strings in order) its spins,
+// activations and alpha_x * delta_l(x), with alpha_{s'_n} = w_s e_n and
+// alpha_s = w_s (-sum_{off-diagonal n} e_n + score * 2 Re E_loc(s)) (diagonal strings leave
+// the configuration unchanged and drop out of the derivative).  With score, also
+// w_s delta_l(s) and w_s (dltsO, alphaO) for the -2 <Re E> <O*> part of the sampling term.
+__global__ void deep_adjoint_kernel(DeepNetDev net, OpDev op, int count, const uint64_t* spins, uint64_t enum_base,
+                                    int enumerate, const double* weights, int score, double2* eloc, float2* acts,
+                                    float2* dlts, float2* alpha, uint64_t* xspins, int xs, float2* dltsO,
+                                    float2* alphaO) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    Work<float2> w = carve<float2>(smem, net, true);
+    uint64_t* sp = w.s + kMaxWords;
+    double2* ebuf = reinterpret_cast<double2*>(w.s + 4 * kMaxWords);
+    const long t = blockIdx.x;
+    if (t >= count) return;
+    const int nw = (net.N + 63) / 64;
+    load_config(spins, enum_base, enumerate, t, net.N, w.s);
+    const float2 lp = forward_once<float2, false, false>(net, w.s, w);
+    double er = 0.0, ei = 0.0, eor = 0.0, eoi = 0.0;
+    int slot = 0;
+    for (int n = 0; n < op.S; n++) {
+        const double2 cf = apply_string(op, n, w.s, sp);
+        if (op.nflip[n] == 0) {
+            er += cf.x;
+            ei += cf.y;
+            continue;
+        }
+        const float2 lq = forward_once<float2, false, false>(net, sp, w);
+        const double dr = static_cast<double>(lq.x) - lp.x, di = static_cast<double>(lq.y) - lp.y;
+        const double m = exp(dr);
+        const double2 e = make_double2(m * (cf.x * cos(di) - cf.y * sin(di)), m * (cf.x * sin(di) + cf.y * cos(di)));
+        eor += e.x;
+        eoi += e.y;
+        if (threadIdx.x == 0) ebuf[slot] = e;
+        slot++;
+    }
+    er += eor;
+    ei += eoi;
+    __syncthreads();
+    const double ws = weights ? weights[t] : 1.0;
+    for (int q = 0; q < xs; q++) {
+        double2 a;
+        const uint64_t* x = w.s;
+        if (q == 0) {
+            a = make_double2(-eor, -eoi);
+            if (score) a.x += 2.0 * er;
+        } else {
+            int k = 0, n = 0;   // the (q-1)-th off-diagonal string
+            for (; n < op.S; n++)
+                if (op.nflip[n] != 0 && k++ == q - 1) break;
+            apply_string(op, n, w.s, sp);
+            x = sp;
+            a = ebuf[q - 1];
+        }
+        const float2 af = make_float2(static_cast<float>(ws * a.x), static_cast<float>(ws * a.y));
+        const long xi = t * xs + q;
+        forward_once<float2, false, true>(net, x, w);
+        for (int k = threadIdx.x; k < net.units; k += blockDim.x) acts[xi * net.units + k] = w.acts[k];
+        if (threadIdx.x < nw) xspins[xi * nw + threadIdx.x] = x[threadIdx.x];
+        if (threadIdx.x == 0) alpha[xi] = af;
+        const float wsf = static_cast<float>(ws);
+        const bool self = score && q == 0;
+        backward_deltas<float2, false>(net, w, [&](int l, int j, float2 d) {
+            dlts[xi * net.units + net.begin_angle[l] + j] = cmul(af, d);
+            if (self) dltsO[t * net.units + net.begin_angle[l] + j] = make_float2(wsf * d.x, wsf * d.y);
+        });
+        if (self && threadIdx.x == 0) alphaO[t] = make_float2(wsf, 0.f);
+    }
+    if (threadIdx.x == 0) eloc[t] = make_double2(er, ei);
+}
+
+// partial[z][m][n] = sum over the configurations x of split z of D[x][m] * A(x, n), where
+// D[x][m] = D[x * ldd + m] and A(x, n) = A[x * lda + n] (A_ACTS), +-1 for spin n of the
+// spin row xsp + x * xld (A_SPINS) or 1 (A_ONES).  FP32 products and sums within a split,
+// FP64 partials.
+enum : int { A_ACTS = 0, A_SPINS = 1, A_ONES = 2 };
+template <int AMODE>
+__global__ void __launch_bounds__(256) adj_cgemm_kernel(int K, int M, int Nn, const float2* __restrict__ D, int ldd,
+                                                        const float2* __restrict__ A, int lda,
+                                                        const uint64_t* __restrict__ xsp, int xld, int per_split,
+                                                        double2* __restrict__ partial) {
+    __shared__ float2 sD[32][33];
+    __shared__ float2 sA[32][33];
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int m0 = blockIdx.x * 32, n0 = blockIdx.y * 32;
+    const int k0 = blockIdx.z * per_split, k1 = min(K, k0 + per_split);
+    float2 acc[2][2];
+#pragma unroll
+    for (int i = 0; i < 2; i++)
+#pragma unroll
+        for (int j = 0; j < 2; j++) acc[i][j] = make_float2(0.f, 0.f);
+    for (int kb = k0; kb < k1; kb += 32) {
+        for (int e = threadIdx.x; e < 32 * 32; e += 256) {
+            const int kk = e >> 5, c = e & 31;
+            const int x = kb + kk;
+            const bool ok = x < k1;
+            sD[kk][c] = (ok && m0 + c < M) ? D[static_cast<long>(x) * ldd + m0 + c] : make_float2(0.f, 0.f);
+            float2 av = make_float2(0.f, 0.f);
+            if (ok && n0 + c < Nn) {
+                if (AMODE == A_ACTS) av = A[static_cast<long>(x) * lda + n0 + c];
+                else if (AMODE == A_SPINS) {
+                    const int i = n0 + c;
+                    av.x = ((xsp[static_cast<long>(x) * xld + (i >> 6)] >> (i & 63)) & 1ull) ? 1.f : -1.f;
+                } else av.x = 1.f;
+            }
+            sA[kk][c] = av;
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int kk = 0; kk < 32; kk++) {
+            const float2 d0 = sD[kk][ty], d1 = sD[kk][ty + 16];
+            const float2 a0 = sA[kk][tx], a1 = sA[kk][tx + 16];
+            acc[0][0] = cadd(acc[0][0], cmul(d0, a0));
+            acc[0][1] = cadd(acc[0][1], cmul(d0, a1));
+            acc[1][0] = cadd(acc[1][0], cmul(d1, a0));
+            acc[1][1] = cadd(acc[1][1], cmul(d1, a1));
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 2; i++)
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+            const int m = m0 + ty + 16 * i, n = n0 + tx + 16 * j;
+            if (m < M && n < Nn)
+                partial[(static_cast<long>(blockIdx.z) * M + m) * Nn + n] =
+                    make_double2(acc[i][j].x, acc[i][j].y);
+        }
+}
+
+// G[m][n] += sum over splits (in order) of partial[z][m][n]
+__global__ void adj_split_sum_kernel(int M, int Nn, int splits, const double2* __restrict__ partial, double2* G) {
+    const long t = static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= static_cast<long>(M) * Nn) return;
+    double2 a = make_double2(0.0, 0.0);
+    for (int z = 0; z < splits; z++) {
+        const double2 v = partial[static_cast<long>(z) * M * Nn + t];
+        a.x += v.x;
+        a.y += v.y;
+    }
+    G[t].x += a.x;
+    G[t].y += a.y;
+}
+
 int threads_for(const DeepNetDev& n) {
     const int width = std::max(n.width, n.N);
     return std::min(1024, std::max(32, (width + 31) / 32 * 32));
@@ -787,6 +979,86 @@ int deep_gradient_chunk(const rbmg_psi* psi, const rbmg_operator* op, const Chun
         if (r == RBMG_OK) r = col_reduce(cnt, P, coef2 + base, orows.as<double2>(), P, 1, acc_EO, st);
         if (r == RBMG_OK) r = col_reduce(cnt, P, coef1 + base, erows.as<double2>(), P, 0, acc_Ek, st);
         if (r != RBMG_OK) return r;
+    }
+    return RBMG_OK;
+}
+
+// Adjoint of the local energy over one chunk of samples, accumulated into the dense
+// per-layer gradient blocks G (double2): for layer l, G_w[l] [size_l][in_l] (in_0 = N)
+// and G_b[l] [size_l], then G_fw [last]; offsets in `goff`.  d_eloc receives E_loc.
+int deep_adjoint_chunk(const rbmg_psi* psi, const rbmg_operator* op, const Chunk& c, int score, double2* d_eloc,
+                       double2* G, double2* GO, const std::vector<size_t>& goff, cudaStream_t st) {
+    const DeepNetDev net = net_of(psi, 0);
+    const int nw = (net.N + 63) / 64;
+    const int xs = 1 + op->num_offdiag;
+    static thread_local DevBuf acts, dlts, alpha, xsp, dltsO, alphaO, partial;
+    const size_t per_sample = static_cast<size_t>(xs) * (2 * sizeof(float2) * net.units + sizeof(float2) + 8 * nw) +
+                              sizeof(float2) * (net.units + 1);
+    const int chunk = std::max(1, static_cast<int>(std::min<size_t>(c.count, (size_t(768) << 20) / per_sample)));
+    RBMG_CK(acts.ensure(sizeof(float2) * static_cast<size_t>(chunk) * xs * net.units));
+    RBMG_CK(dlts.ensure(sizeof(float2) * static_cast<size_t>(chunk) * xs * net.units));
+    RBMG_CK(alpha.ensure(sizeof(float2) * static_cast<size_t>(chunk) * xs));
+    RBMG_CK(xsp.ensure(sizeof(uint64_t) * static_cast<size_t>(chunk) * xs * nw));
+    RBMG_CK(dltsO.ensure(sizeof(float2) * static_cast<size_t>(chunk) * net.units));
+    RBMG_CK(alphaO.ensure(sizeof(float2) * static_cast<size_t>(chunk)));
+    const size_t sm = smem_for(net, sizeof(float2), true) + sizeof(double2) * std::max(1, op->num_offdiag);
+    RBMG_CK(set_smem(deep_adjoint_kernel, sm));
+    constexpr int kMaxSplits = 64;
+    for (int base = 0; base < c.count; base += chunk) {
+        const int cnt = std::min(chunk, c.count - base);
+        const uint64_t* sp = c.spins ? c.spins + static_cast<size_t>(base) * nw : nullptr;
+        deep_adjoint_kernel<<<cnt, threads_for(net), sm, st>>>(
+            net, op->dev(), cnt, sp, c.enum_base + base, c.enumerate, c.weights ? c.weights + base : nullptr, score,
+            d_eloc + base, acts.as<float2>(), dlts.as<float2>(), alpha.as<float2>(), xsp.as<uint64_t>(), xs,
+            dltsO.as<float2>(), alphaO.as<float2>());
+        RBMG_CK(cudaGetLastError());
+        // reduce over K configurations whose rows are `stride` configurations apart
+        auto reduce = [&](int K, int amode, int M, int Nn, const float2* D, int ldd, const float2* A, int lda, int xld,
+                          double2* out) -> int {
+            const int splits = std::min(kMaxSplits, std::max(1, K / 256));
+            const int per = (K + splits - 1) / splits;
+            RBMG_CK(partial.ensure(sizeof(double2) * static_cast<size_t>(splits) * M * Nn));
+            const dim3 grid((M + 31) / 32, (Nn + 31) / 32, splits);
+            if (amode == A_ACTS)
+                adj_cgemm_kernel<A_ACTS><<<grid, 256, 0, st>>>(K, M, Nn, D, ldd, A, lda, xsp.as<uint64_t>(), xld, per,
+                                                                partial.as<double2>());
+            else if (amode == A_SPINS)
+                adj_cgemm_kernel<A_SPINS><<<grid, 256, 0, st>>>(K, M, Nn, D, ldd, A, lda, xsp.as<uint64_t>(), xld, per,
+                                                                 partial.as<double2>());
+            else
+                adj_cgemm_kernel<A_ONES><<<grid, 256, 0, st>>>(K, M, Nn, D, ldd, A, lda, xsp.as<uint64_t>(), xld, per,
+                                                                partial.as<double2>());
+            RBMG_CK(cudaGetLastError());
+            const long tot = static_cast<long>(M) * Nn;
+            adj_split_sum_kernel<<<static_cast<unsigned>((tot + 255) / 256), 256, 0, st>>>(M, Nn, splits,
+                                                                                         partial.as<double2>(), out);
+            RBMG_CK(cudaGetLastError());
+            return RBMG_OK;
+        };
+        // pass 0: all configurations with alpha-weighted deltas -> G; pass 1 (score): the
+        // samples themselves with weight w_s -> GO
+        for (int pass = 0; pass < (score ? 2 : 1); pass++) {
+            const int K = pass == 0 ? cnt * xs : cnt;
+            const int row = pass == 0 ? net.units : xs * net.units;     // activation row stride
+            const float2* dl = pass == 0 ? dlts.as<float2>() : dltsO.as<float2>();
+            double2* out = pass == 0 ? G : GO;
+            for (int l = 0; l < net.L; l++) {
+                const int size = net.size[l];
+                const int in = l == 0 ? net.N : net.size[l - 1];
+                const float2* D = dl + net.begin_angle[l];
+                int r = l == 0 ? reduce(K, A_SPINS, size, in, D, net.units, nullptr, 0, pass == 0 ? nw : xs * nw,
+                                        out + goff[2 * l])
+                               : reduce(K, A_ACTS, size, in, D, net.units, acts.as<float2>() + net.begin_angle[l - 1],
+                                        row, 0, out + goff[2 * l]);
+                if (r != RBMG_OK) return r;
+                r = reduce(K, A_ONES, size, 1, D, net.units, nullptr, 0, 0, out + goff[2 * l + 1]);
+                if (r != RBMG_OK) return r;
+            }
+            const int last = net.size[net.L - 1];
+            const int r = reduce(K, A_ACTS, 1, last, pass == 0 ? alpha.as<float2>() : alphaO.as<float2>(), 1,
+                                 acts.as<float2>() + net.begin_angle[net.L - 1], row, 0, out + goff[2 * net.L]);
+            if (r != RBMG_OK) return r;
+        }
     }
     return RBMG_OK;
 }
