@@ -261,6 +261,31 @@ RBMG_API int rbmg_chain_learned_async(rbmg_chain* chain, const rbmg_psi* psi, co
                                       void* d_eloc_out, void* stream);
 
 
+/* ---------------------------------------------------------------- batched serving
+ * Extension (no reference counterpart; the reference runs one network per call,
+ * include/spin_ensembles/MonteCarloLoop.hpp:294-339): many complex RBMs of uneven N and M,
+ * each with its own operator, walkers and Philox seed, sampled, given local energies and
+ * the O_k gradient 2 (<E O*> - <E> <O*>) in one persistent launch replayed from a CUDA
+ * graph.  Walker w of instance i draws the Philox stream (seeds[i], w), as a Chain of
+ * that instance would.  The instances' psi and operator handles must outlive the batch. */
+typedef struct rbmg_batch rbmg_batch;
+RBMG_API int rbmg_batch_create(int num_instances, const rbmg_psi* const* psis, const rbmg_operator* const* ops,
+                               const uint32_t* walkers, const uint64_t* seeds, rbmg_batch** out);
+RBMG_API int rbmg_batch_destroy(rbmg_batch* batch);
+/* one replay: the first draws random start spins and runs `therm` + `sweeps` sweeps, later
+ * ones continue the chains for `sweeps` sweeps; then every walker's local energy and the
+ * per-instance O_k sums.  RBMG_ETIMEOUT if a reduction task gave up waiting. */
+RBMG_API int rbmg_batch_run(rbmg_batch* batch, int therm, int sweeps);
+/* launch shape: warps per block in {2, 4, 8}, reduction tile rows in {8, 16} */
+RBMG_API int rbmg_batch_set_shape(rbmg_batch* batch, int warps_per_block, int rows);
+RBMG_API int rbmg_batch_get_shape(const rbmg_batch* batch, int* warps_per_block, int* rows, int* blocks);
+/* times the 6 shapes on `reps` replays of `sweeps` sweeps each and keeps the fastest;
+ * ms [6] (nullable) gets their mean replay times, order (2,8) (2,16) (4,8) (4,16) (8,8) (8,16) */
+RBMG_API int rbmg_batch_autotune(rbmg_batch* batch, int sweeps, int reps, double* ms);
+/* last replay's results of instance i: energy [2], grad [2P] (nullable), eloc [2 walkers] (nullable) */
+RBMG_API int rbmg_batch_result(const rbmg_batch* batch, int instance, double* energy, double* grad, double* eloc);
+RBMG_API int rbmg_batch_info(const rbmg_batch* batch, int* num_instances, uint64_t* accepts, double* tuned_ms);
+
 /* FP32 FMA throughput of the current device in TFLOP/s (a probe kernel of `iters`
  * x 128 independent FMAs per thread), the roofline denominator of the sampler. */
 RBMG_API int rbmg_probe_fp32_tflops(int iters, double* tflops);

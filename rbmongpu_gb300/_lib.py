@@ -87,6 +87,14 @@ SIGNATURES = {
     "rbmg_proposal_eval": [_vp, C.c_int, _u64p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float)],
     "rbmg_proposal_adam": [_vp, C.POINTER(C.c_float)],
     "rbmg_proposal_set_objective": [_vp, C.c_int],
+    "rbmg_batch_create": [C.c_int, _vpp, _vpp, C.POINTER(C.c_uint32), _u64p, _vpp],
+    "rbmg_batch_destroy": [_vp],
+    "rbmg_batch_run": [_vp, C.c_int, C.c_int],
+    "rbmg_batch_set_shape": [_vp, C.c_int, C.c_int],
+    "rbmg_batch_get_shape": [_vp, _ip, _ip, _ip],
+    "rbmg_batch_autotune": [_vp, C.c_int, C.c_int, _dp],
+    "rbmg_batch_result": [_vp, C.c_int, _dp, _dp, _dp],
+    "rbmg_batch_info": [_vp, _ip, _u64p, _dp],
     "rbmg_chain_learned_async": [_vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_int, _vp, _vp],
 }
 _RESTYPE = {"rbmg_last_error": C.c_char_p, "rbmg_version": C.c_char_p}

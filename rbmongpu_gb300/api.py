@@ -686,6 +686,66 @@ class Proposal:
         call("rbmg_proposal_adam", self._h, _p(g, C.POINTER(C.c_float)))
 
 
+class Batch:
+    """Many complex RBMs of uneven N and M served by one persistent launch replayed from a
+    CUDA graph (extension).  instances: list of (psi, operator, walkers, seed)."""
+
+    def __init__(self, instances):
+        self._keep = [(p, o) for p, o, _, _ in instances]
+        n = len(instances)
+        psis = (C.c_void_p * n)(*[p._h.value for p, _, _, _ in instances])
+        ops = (C.c_void_p * n)(*[o._h.value for _, o, _, _ in instances])
+        walkers = (C.c_uint32 * n)(*[int(w) for _, _, w, _ in instances])
+        seeds = (C.c_uint64 * n)(*[int(sd) for _, _, _, sd in instances])
+        h = _handle()
+        call("rbmg_batch_create", n, psis, ops, walkers, seeds, C.byref(h))
+        self._h = h
+        self.instances = [(p.N, p.num_params, int(w)) for p, _, w, _ in instances]
+
+    def __del__(self):
+        h, self._h = getattr(self, "_h", None), None
+        if h is not None:
+            try:
+                lib().rbmg_batch_destroy(h)
+            except Exception:
+                pass
+
+    def run(self, therm=0, sweeps=1):
+        call("rbmg_batch_run", self._h, int(therm), int(sweeps))
+
+    def set_shape(self, warps_per_block, rows):
+        call("rbmg_batch_set_shape", self._h, int(warps_per_block), int(rows))
+
+    @property
+    def shape(self):
+        w, r, b = C.c_int(), C.c_int(), C.c_int()
+        call("rbmg_batch_get_shape", self._h, C.byref(w), C.byref(r), C.byref(b))
+        return w.value, r.value, b.value
+
+    def autotune(self, sweeps=1, reps=3):
+        """Times the launch shapes on the batch itself, keeps the fastest; returns
+        {(warps_per_block, rows): ms per replay}."""
+        ms = np.zeros(6)
+        call("rbmg_batch_autotune", self._h, int(sweeps), int(reps), _p(ms))
+        shapes = [(2, 8), (2, 16), (4, 8), (4, 16), (8, 8), (8, 16)]
+        return dict(zip(shapes, ms.tolist()))
+
+    def result(self, i, want_eloc=False):
+        """(<E_loc>, O_k gradient [P], local energies or None) of instance i, last replay."""
+        N, P, w = self.instances[i]
+        e = np.zeros(2)
+        g = np.zeros(P, np.complex128)
+        el = np.zeros(w, np.complex128) if want_eloc else None
+        call("rbmg_batch_result", self._h, int(i), _p(e), _p(g.view(np.float64)),
+             _p(el.view(np.float64)) if want_eloc else None)
+        return complex(e[0], e[1]), g, el
+
+    def accepts(self):
+        a = C.c_uint64()
+        call("rbmg_batch_info", self._h, None, C.byref(a), None)
+        return a.value
+
+
 def library_stream():
     """The library's CUDA stream of the calling thread (a cudaStream_t as int)."""
     st = C.c_void_p()
@@ -753,6 +813,6 @@ def new_deep_neural_network(N, M, C_, initial_value=(0.01 + 1j * math.pi / 4), a
     return cls(alpha, beta, b, connections, W, final_weights, 1.0, free_quantum_axis, gpu)
 
 
-__all__ = ["Chain", "library_stream", "Psi", "PsiDeep", "PsiPair", "Operator", "Spins", "MonteCarloLoop", "ExactSummation",
+__all__ = ["Batch", "Chain", "library_stream", "Psi", "PsiDeep", "PsiPair", "Operator", "Spins", "MonteCarloLoop", "ExactSummation",
            "ExpectationValue", "HilbertSpaceDistance", "psi_O_k_vector", "activation_function", "setDevice",
            "start_profiling", "stop_profiling", "new_neural_network", "new_deep_neural_network", "RbmgError"]

@@ -1,0 +1,624 @@
+// Batched serving of many independent complex RBMs of uneven N and M (extension: the
+// reference runs one network per call, include/spin_ensembles/MonteCarloLoop.hpp:294-339).
+//
+// One persistent launch serves the whole batch.  Its warps take tasks from a global
+// queue (one atomic counter): first the walker tasks of every instance, longest first
+// (sweeps of single-flip Metropolis, the local energy and tanh(theta) of the final
+// configuration), then the reduction tasks, each a tile of rows of one instance's
+// O_k sums, which start once that instance's walkers are all done (a per-instance
+// counter; the wait is bounded by a wall-clock limit after which the kernel raises an
+// error flag and returns).  Hidden units per lane are a runtime count (up to 18, M <= 576)
+// with register arrays of the maximum size, so one kernel serves every shape.  The
+// launch (counter resets + kernel) is captured once in a CUDA graph and replayed; the
+// warps per block and the reduction tile height come from an autotuner that times the
+// candidates on the batch itself.
+//
+// Per instance and replay the result is <E_loc> over its walkers and the O_k gradient
+// 2 (<E O*> - <E> <O*>), the reference's estimator (ExpectationValue.cu:243-253) with
+// conj<E_k> replaced by <E O*>, its expectation for a hermitian operator.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <memory>
+#include <vector>
+
+#include "host.h"
+#include "rbm_impl.cuh"
+
+namespace rbmg {
+namespace {
+
+constexpr int kSK = 18;   // hidden units per lane at most (Mpad <= 576)
+constexpr int kSW = 3;    // spin words at most (N <= 192)
+
+struct SInst {
+    int N, M, Mpad, K, nw;
+    const float2* W;
+    const float2* b;
+    OpDev op;
+    int walkers;
+    uint64_t seed;
+    double2* eloc;        // [walkers]
+    float2* T;            // [walkers][Mpad]
+    uint64_t* spins;      // [walkers][nw]
+    uint64_t* rng_index;  // [walkers]
+    float2* gO;           // [N + 1][Mpad]  sum_w conj(O)   (row N: the biases)
+    float2* gEO;          // [N + 1][Mpad]  sum_w E conj(O)
+    unsigned int* done;   // walkers finished in this replay
+};
+
+struct STask {
+    int kind;    // 0 walker, 1 reduction tile
+    int inst;
+    int index;   // walker within the instance, or first row of the tile
+};
+
+struct SLaunch {
+    const SInst* inst;
+    const STask* tasks;
+    int ntasks;
+    unsigned int* next;
+    int therm, sweeps;    // sweeps before this replay's measurement: therm (first replay) + sweeps
+    int first;            // 1: draw the walkers' start spins
+    int* error;           // 1: a reduction task gave up waiting
+    unsigned long long* accepts;   // [1]
+};
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+template <int NW>
+__device__ __forceinline__ void s_refresh(const SInst& I, const Spins<NW>& s, float (&tr)[kSK], float (&ti)[kSK],
+                                          int lane) {
+#pragma unroll
+    for (int k = 0; k < kSK; k++)
+        if (k < I.K) {
+            const float2 b = __ldg(I.b + lane + 32 * k);
+            tr[k] = b.x;
+            ti[k] = b.y;
+        }
+    const float2* row = I.W + lane;
+    for (int i = 0; i < I.N; i++, row += I.Mpad) {
+        const float sg = s.up(i) ? 1.0f : -1.0f;
+#pragma unroll
+        for (int k = 0; k < kSK; k++)
+            if (k < I.K) {
+                const float2 w = __ldg(row + 32 * k);
+                tr[k] = __fadd_rn(tr[k], sg * w.x);
+                ti[k] = __fadd_rn(ti[k], sg * w.y);
+            }
+    }
+}
+
+// single-flip Metropolis step: the arithmetic and draw order of rbm_mh_step
+template <int NW>
+__device__ __forceinline__ bool s_mh_step(const SInst& I, Spins<NW>& s, float (&tr)[kSK], float (&ti)[kSK],
+                                          float (&re)[kSK], WarpRng& rng, int lane, uint64_t nmagic) {
+    const int site = static_cast<int>(fastmod(rng.next(), nmagic, static_cast<uint32_t>(I.N)));
+    Spins<NW> s2 = s;
+    s2.flip(site);
+    const float two_s = s2.up(site) ? 2.0f : -2.0f;
+    const float2* row = I.W + static_cast<long>(site) * I.Mpad + lane;
+    float2 w[kSK];
+#pragma unroll
+    for (int k = 0; k < kSK; k++)
+        if (k < I.K) w[k] = __ldg(row + 32 * k);
+    float part = 0.0f;
+#pragma unroll
+    for (int k = 0; k < kSK; k++)
+        if (k < I.K) {
+            const float nr = __fmaf_rn(two_s, w[k].x, tr[k]);
+            const float ni = __fmaf_rn(two_s, w[k].y, ti[k]);
+            part = __fadd_rn(part, __fsub_rn(lc_re(nr, ni), re[k]));
+        }
+    const float delta = warp_sum_xor(part);
+    bool accept = delta > 0.0f;
+    if (!accept) accept = rng.uniform() <= expf_det(__fmul_rn(2.0f, delta));
+    if (accept) {
+        s = s2;
+#pragma unroll
+        for (int k = 0; k < kSK; k++)
+            if (k < I.K) {
+                const float2 ww = __ldg(row + 32 * k);
+                tr[k] = __fmaf_rn(two_s, ww.x, tr[k]);
+                ti[k] = __fmaf_rn(two_s, ww.y, ti[k]);
+                re[k] = lc_re(tr[k], ti[k]);
+            }
+    }
+    return accept;
+}
+
+// each task kind is a separate (not inlined) function, so that the register allocation of
+// one does not constrain the others
+__device__ __noinline__ void walker_task(const SLaunch& L, const SInst& I, int w, int lane) {
+    constexpr int NW = kSW;
+    WarpRng rng;
+    rng.init(I.seed, static_cast<uint32_t>(w), I.rng_index[w], lane);
+    const uint64_t nmagic = fastmod_magic(static_cast<uint32_t>(I.N));
+    Spins<NW> s;
+#pragma unroll
+    for (int k = 0; k < NW; k++) s.w[k] = 0;
+    if (L.first) {
+        // the draws of draw_spins for this instance's word count (low then high half)
+#pragma unroll
+        for (int k = 0; k < NW; k++)
+            if (k < I.nw) {
+                const uint64_t lo = rng.next();
+                const uint64_t hi = rng.next();
+                s.w[k] = lo | (hi << 32);
+            }
+#pragma unroll
+        for (int k = 0; k < NW; k++)
+            if (k == I.N / 64 && k < I.nw) s.w[k] &= (1ull << (I.N % 64)) - 1ull;
+    } else {
+#pragma unroll
+        for (int k = 0; k < NW; k++)
+            if (k < I.nw) s.w[k] = I.spins[static_cast<long>(w) * I.nw + k];
+    }
+    float tr[kSK], ti[kSK], re[kSK];
+    unsigned long long acc = 0;
+    const int total = (L.first ? L.therm : 0) + L.sweeps;
+    for (int sw = 0; sw < total; sw++) {
+        s_refresh(I, s, tr, ti, lane);
+#pragma unroll
+        for (int k = 0; k < kSK; k++)
+            if (k < I.K) re[k] = lc_re(tr[k], ti[k]);
+        for (int p = 0; p < I.N; p++) acc += s_mh_step(I, s, tr, ti, re, rng, lane, nmagic);
+    }
+    // measurement: local energy and tanh(theta) of the final configuration; f(theta) in
+    // this warp's shared-memory slice [kSK][32] keeps the register footprint of the sweeps
+    s_refresh(I, s, tr, ti, lane);
+    extern __shared__ float2 s_f[];
+    float2* myf = s_f + (threadIdx.x >> 5) * kSK * 32 + lane;
+#pragma unroll
+    for (int k = 0; k < kSK; k++)
+        if (k < I.K) {
+            myf[32 * k] = lc_c(tr[k], ti[k]);
+            I.T[static_cast<long>(w) * I.Mpad + lane + 32 * k] = tanh_c(tr[k], ti[k]);
+        }
+    KahanC e;
+    for (int n = 0; n < I.op.S; n++) {
+        const float2 cf = string_factor(I.op, n, s);
+        const int nf = I.op.nflip[n];
+        if (nf == 0) {
+            e.add(cf.x, cf.y);
+            continue;
+        }
+        const int off = I.op.flip_off[n];
+        float2 part = make_float2(0.0f, 0.0f);
+        if (nf == 1) {
+            const int site = I.op.flip_sites[off];
+            const float two_s = s.up(site) ? -2.0f : 2.0f;
+            const float2* row = I.W + static_cast<long>(site) * I.Mpad + lane;
+#pragma unroll
+            for (int k = 0; k < kSK; k++)
+                if (k < I.K) {
+                    const float2 wv = __ldg(row + 32 * k);
+                    const float2 g = lc_c(fmaf(two_s, wv.x, tr[k]), fmaf(two_s, wv.y, ti[k]));
+                    const float2 f0 = myf[32 * k];
+                    part.x += g.x - f0.x;
+                    part.y += g.y - f0.y;
+                }
+        } else {
+#pragma unroll
+            for (int k = 0; k < kSK; k++)
+                if (k < I.K) {
+                    float nr = tr[k], ni = ti[k];
+                    for (int q = 0; q < nf; q++) {
+                        const int site = I.op.flip_sites[off + q];
+                        const float two_s = s.up(site) ? -2.0f : 2.0f;
+                        const float2 wv = __ldg(I.W + static_cast<long>(site) * I.Mpad + lane + 32 * k);
+                        nr = fmaf(two_s, wv.x, nr);
+                        ni = fmaf(two_s, wv.y, ni);
+                    }
+                    const float2 g = lc_c(nr, ni);
+                    const float2 f0 = myf[32 * k];
+                    part.x += g.x - f0.x;
+                    part.y += g.y - f0.y;
+                }
+        }
+        const float2 t = string_term(cf, warp_sum_xor2(part));
+        e.add(t.x, t.y);
+    }
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < NW; k++)
+            if (k < I.nw) I.spins[static_cast<long>(w) * I.nw + k] = s.w[k];
+        I.rng_index[w] = rng.index;
+        I.eloc[w] = e.value();
+        atomicAdd(L.accepts, acc);
+    }
+    __syncwarp();
+    __threadfence();
+    if (lane == 0) atomicAdd(I.done, 1u);
+}
+
+// rows [r0, r0 + R) of the instance's O_k sums (row N: the biases), every column
+template <int R>
+__device__ __noinline__ void reduce_task(const SLaunch& L, const SInst& I, int r0, int lane) {
+    // wait for the instance's walkers (bounded: 20 s of wall clock)
+    if (lane == 0) {
+        const unsigned long long t0 = global_ns();
+        while (atomicAdd(I.done, 0u) < static_cast<unsigned int>(I.walkers)) {
+            if (global_ns() - t0 > 20000000000ull) {
+                atomicExch(L.error, 1);
+                break;
+            }
+            __nanosleep(1000);
+        }
+    }
+    __syncwarp();
+    if (*reinterpret_cast<volatile int*>(L.error)) return;
+    __threadfence();
+    for (int kc = 0; kc < I.K; kc++) {
+        float2 aO[R], aE[R];
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            aO[r] = make_float2(0.0f, 0.0f);
+            aE[r] = make_float2(0.0f, 0.0f);
+        }
+        const int j = lane + 32 * kc;
+        const int wd0 = r0 >> 6, wd1 = min(r0 + R - 1, I.N - 1) >> 6;   // the rows span at most two words
+        for (int w = 0; w < I.walkers; w++) {
+            // L2 loads (__ldcg): the walkers' results were written by other SMs
+            const float2 t = __ldcg(I.T + static_cast<long>(w) * I.Mpad + j);
+            const double2 ed = __ldcg(I.eloc + w);
+            const float ex = static_cast<float>(ed.x), ey = static_cast<float>(ed.y);
+            // conj(t) and E conj(t)
+            const float cx = t.x, cy = -t.y;
+            const float ecx = ex * cx - ey * cy, ecy = ex * cy + ey * cx;
+            const unsigned long long* sw = reinterpret_cast<const unsigned long long*>(I.spins) +
+                                           static_cast<long>(w) * I.nw;
+            const uint64_t word0 = wd0 < I.nw ? __ldcg(sw + wd0) : 0ull;
+            const uint64_t word1 = wd1 < I.nw ? __ldcg(sw + wd1) : 0ull;
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                const int i = r0 + r;
+                float sg = 1.0f;
+                if (i < I.N) {
+                    const uint64_t word = (i >> 6) == wd0 ? word0 : word1;
+                    sg = ((word >> (i & 63)) & 1ull) ? 1.0f : -1.0f;
+                }
+                aO[r].x += sg * cx;
+                aO[r].y += sg * cy;
+                aE[r].x += sg * ecx;
+                aE[r].y += sg * ecy;
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            const int i = r0 + r;
+            if (i <= I.N) {
+                I.gO[static_cast<long>(i) * I.Mpad + j] = aO[r];
+                I.gEO[static_cast<long>(i) * I.Mpad + j] = aE[r];
+            }
+        }
+    }
+}
+
+template <int R>
+__global__ void serve_kernel(SLaunch L) {
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        int t = 0;
+        if (lane == 0) t = static_cast<int>(atomicAdd(L.next, 1u));
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= L.ntasks) return;
+        const STask task = L.tasks[t];
+        const SInst& I = L.inst[task.inst];
+        if (task.kind == 0) {
+            walker_task(L, I, task.index, lane);
+        } else {
+            reduce_task<R>(L, I, task.index, lane);
+        }
+    }
+}
+
+}  // namespace
+}  // namespace rbmg
+
+using namespace rbmg;
+
+struct rbmg_batch {
+    int n = 0;
+    std::vector<const rbmg_psi*> psis;
+    std::vector<const rbmg_operator*> ops;
+    std::vector<SInst> host_inst;
+    std::vector<uint32_t> walkers;
+    DevBuf d_inst, d_tasks, d_next, d_done, d_error, d_accepts;
+    std::vector<std::unique_ptr<DevBuf>> bufs;
+    int ntasks_walk = 0, ntasks = 0;
+    int rows = 16;              // reduction tile height
+    int warps_per_block = 4;
+    int blocks = 0;
+    bool first = true;
+    int therm = 0, sweeps = 1;  // graph parameters
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int graph_rows = 0, graph_wpb = 0, graph_first = -1, graph_therm = -1, graph_sweeps = -1;
+    double tuned_ms = 0.0;
+    ~rbmg_batch() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+    }
+};
+
+namespace {
+
+int batch_tasks(rbmg_batch* b) {
+    // walker tasks, longest first (cost ~ N * Mpad per sweep), then reduction tiles
+    std::vector<int> order(b->n);
+    for (int i = 0; i < b->n; i++) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
+        return static_cast<long>(b->host_inst[a].N) * b->host_inst[a].Mpad >
+               static_cast<long>(b->host_inst[c].N) * b->host_inst[c].Mpad;
+    });
+    std::vector<STask> tasks;
+    for (int i : order)
+        for (int w = 0; w < b->host_inst[i].walkers; w++) tasks.push_back(STask{0, i, w});
+    b->ntasks_walk = static_cast<int>(tasks.size());
+    for (int i : order)
+        for (int r0 = 0; r0 <= b->host_inst[i].N; r0 += b->rows) tasks.push_back(STask{1, i, r0});
+    b->ntasks = static_cast<int>(tasks.size());
+    RBMG_CK(b->d_tasks.ensure(sizeof(STask) * tasks.size()));
+    RBMG_CK(cudaMemcpy(b->d_tasks.p, tasks.data(), sizeof(STask) * tasks.size(), cudaMemcpyHostToDevice));
+    return RBMG_OK;
+}
+
+size_t serve_smem(int warps_per_block) { return sizeof(float2) * kSK * 32 * warps_per_block; }
+
+cudaError_t launch_serve(rbmg_batch* b, cudaStream_t st) {
+    SLaunch L{};
+    L.inst = b->d_inst.as<SInst>();
+    L.tasks = b->d_tasks.as<STask>();
+    L.ntasks = b->ntasks;
+    L.next = b->d_next.as<unsigned int>();
+    L.therm = b->therm;
+    L.sweeps = b->sweeps;
+    L.first = b->first ? 1 : 0;
+    L.error = b->d_error.as<int>();
+    L.accepts = b->d_accepts.as<unsigned long long>();
+    const int threads = 32 * b->warps_per_block;
+    const size_t sm = serve_smem(b->warps_per_block);
+    if (b->rows == 8) serve_kernel<8><<<b->blocks, threads, sm, st>>>(L);
+    else serve_kernel<16><<<b->blocks, threads, sm, st>>>(L);
+    return cudaGetLastError();
+}
+
+// (re)captures the replay: counter resets and the persistent launch
+int batch_capture(rbmg_batch* b) {
+    if (b->exec && b->graph_rows == b->rows && b->graph_wpb == b->warps_per_block &&
+        b->graph_first == static_cast<int>(b->first) && b->graph_therm == b->therm && b->graph_sweeps == b->sweeps)
+        return RBMG_OK;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+    int dev = 0, sms = 0, per_sm = 0;
+    RBMG_CK(cudaGetDevice(&dev));
+    RBMG_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int threads = 32 * b->warps_per_block;
+    const size_t sm = serve_smem(b->warps_per_block);
+    if (b->rows == 8) RBMG_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, serve_kernel<8>, threads, sm));
+    else RBMG_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, serve_kernel<16>, threads, sm));
+    b->blocks = std::max(1, sms * std::max(1, per_sm));
+    cudaStream_t st = stream();
+    RBMG_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    cudaMemsetAsync(b->d_next.p, 0, sizeof(unsigned int), st);
+    cudaMemsetAsync(b->d_done.p, 0, sizeof(unsigned int) * b->n, st);
+    cudaMemsetAsync(b->d_accepts.p, 0, sizeof(unsigned long long), st);
+    const cudaError_t le = launch_serve(b, st);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(st, &g);
+    RBMG_CK(le);
+    RBMG_CK(ce);
+    b->graph = g;
+    RBMG_CK(cudaGraphInstantiate(&b->exec, b->graph, 0));
+    b->graph_rows = b->rows;
+    b->graph_wpb = b->warps_per_block;
+    b->graph_first = static_cast<int>(b->first);
+    b->graph_therm = b->therm;
+    b->graph_sweeps = b->sweeps;
+    return RBMG_OK;
+}
+
+int batch_replay(rbmg_batch* b) {
+    int r = batch_capture(b);
+    if (r != RBMG_OK) return r;
+    RBMG_CK(cudaGraphLaunch(b->exec, stream()));
+    int err = 0;
+    RBMG_CK(cudaMemcpyAsync(&err, b->d_error.p, sizeof(int), cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaStreamSynchronize(stream()));
+    if (err) {
+        RBMG_CK(cudaMemset(b->d_error.p, 0, sizeof(int)));
+        return fail(RBMG_ETIMEOUT, "batch: a reduction task timed out waiting for its walkers");
+    }
+    b->first = false;
+    return RBMG_OK;
+}
+
+}  // namespace
+
+extern "C" int rbmg_batch_create(int n, const rbmg_psi* const* psis, const rbmg_operator* const* ops,
+                                 const uint32_t* walkers, const uint64_t* seeds, rbmg_batch** out) {
+    if (n <= 0 || !psis || !ops || !walkers || !seeds || !out) return fail(RBMG_EINVAL, "batch: bad arguments");
+    auto b = std::make_unique<rbmg_batch>();
+    b->n = n;
+    for (int i = 0; i < n; i++) {
+        const rbmg_psi* p = psis[i];
+        const rbmg_operator* o = ops[i];
+        if (!p || !o || walkers[i] == 0) return fail(RBMG_EINVAL, "batch: null instance or no walkers");
+        if (p->kind != 0) return fail(RBMG_EUNSUPPORTED, "batch: complex RBM (Psi) instances only");
+        if (p->Mpad / 32 > kSK) return fail(RBMG_EUNSUPPORTED, "batch: M <= 576");
+        if (p->N > 64 * kSW) return fail(RBMG_EUNSUPPORTED, "batch: N <= 192");
+        if (o->max_site >= p->N) return fail(RBMG_EINVAL, "batch: operator acts on a site >= N");
+        const int nw = nwords_of(p->N);
+        SInst I{};
+        I.N = p->N;
+        I.M = p->M;
+        I.Mpad = p->Mpad;
+        I.K = p->Mpad / 32;
+        I.nw = nw;
+        const RbmDev d = p->rbm_dev();
+        I.W = d.W;
+        I.b = d.b;
+        I.op = o->dev();
+        I.walkers = static_cast<int>(walkers[i]);
+        I.seed = seeds[i];
+        auto alloc = [&](size_t bytes) -> void* {
+            b->bufs.push_back(std::make_unique<DevBuf>());
+            if (b->bufs.back()->ensure(std::max<size_t>(bytes, 16)) != cudaSuccess) return nullptr;
+            return b->bufs.back()->p;
+        };
+        const size_t B = walkers[i];
+        I.eloc = static_cast<double2*>(alloc(sizeof(double2) * B));
+        I.T = static_cast<float2*>(alloc(sizeof(float2) * B * p->Mpad));
+        I.spins = static_cast<uint64_t*>(alloc(sizeof(uint64_t) * B * nw));
+        I.rng_index = static_cast<uint64_t*>(alloc(sizeof(uint64_t) * B));
+        I.gO = static_cast<float2*>(alloc(sizeof(float2) * (p->N + 1) * p->Mpad));
+        I.gEO = static_cast<float2*>(alloc(sizeof(float2) * (p->N + 1) * p->Mpad));
+        if (!I.eloc || !I.T || !I.spins || !I.rng_index || !I.gO || !I.gEO)
+            return fail(RBMG_ENOMEM, "batch: device allocation failed");
+        RBMG_CK(cudaMemset(I.rng_index, 0, sizeof(uint64_t) * B));
+        b->psis.push_back(p);
+        b->ops.push_back(o);
+        b->walkers.push_back(walkers[i]);
+        b->host_inst.push_back(I);
+    }
+    RBMG_CK(b->d_done.ensure(sizeof(unsigned int) * n));
+    for (int i = 0; i < n; i++) b->host_inst[i].done = b->d_done.as<unsigned int>() + i;
+    RBMG_CK(b->d_inst.ensure(sizeof(SInst) * n));
+    RBMG_CK(cudaMemcpy(b->d_inst.p, b->host_inst.data(), sizeof(SInst) * n, cudaMemcpyHostToDevice));
+    RBMG_CK(b->d_next.ensure(sizeof(unsigned int)));
+    RBMG_CK(b->d_error.ensure(sizeof(int)));
+    RBMG_CK(b->d_accepts.ensure(sizeof(unsigned long long)));
+    RBMG_CK(cudaMemset(b->d_error.p, 0, sizeof(int)));
+    const int r = batch_tasks(b.get());
+    if (r != RBMG_OK) return r;
+    *out = b.release();
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_batch_destroy(rbmg_batch* b) {
+    delete b;
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_batch_set_shape(rbmg_batch* b, int warps_per_block, int rows) {
+    if (!b || (warps_per_block != 2 && warps_per_block != 4 && warps_per_block != 8) || (rows != 8 && rows != 16))
+        return fail(RBMG_EINVAL, "batch: warps per block in {2, 4, 8}, tile rows in {8, 16}");
+    if (rows != b->rows) {
+        b->rows = rows;
+        const int r = batch_tasks(b);
+        if (r != RBMG_OK) return r;
+    }
+    b->warps_per_block = warps_per_block;
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_batch_get_shape(const rbmg_batch* b, int* warps_per_block, int* rows, int* blocks) {
+    if (!b) return fail(RBMG_EINVAL, "batch: null");
+    if (warps_per_block) *warps_per_block = b->warps_per_block;
+    if (rows) *rows = b->rows;
+    if (blocks) *blocks = b->blocks;
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_batch_run(rbmg_batch* b, int therm, int sweeps) {
+    if (!b || therm < 0 || sweeps < 0) return fail(RBMG_EINVAL, "batch run: bad arguments");
+    b->therm = therm;
+    b->sweeps = sweeps;
+    return batch_replay(b);
+}
+
+// Times every candidate shape on `reps` replays of `sweeps` sweeps (the chains advance),
+// keeps the fastest; ms_out [6] receives the candidates' mean milliseconds per replay in
+// the order (2,8) (2,16) (4,8) (4,16) (8,8) (8,16).
+extern "C" int rbmg_batch_autotune(rbmg_batch* b, int sweeps, int reps, double* ms_out) {
+    if (!b || sweeps < 0 || reps <= 0) return fail(RBMG_EINVAL, "batch autotune: bad arguments");
+    if (b->first) {   // start the chains outside the timing
+        const int r = rbmg_batch_run(b, 0, 0);
+        if (r != RBMG_OK) return r;
+    }
+    const int wpbs[3] = {2, 4, 8}, rowss[2] = {8, 16};
+    double best = 1e300;
+    int bw = 4, brows = 16, c = 0;
+    for (int wpb : wpbs)
+        for (int rows : rowss) {
+            int r = rbmg_batch_set_shape(b, wpb, rows);
+            if (r != RBMG_OK) return r;
+            b->therm = 0;
+            b->sweeps = sweeps;
+            r = batch_replay(b);   // capture + warm-up
+            if (r != RBMG_OK) return r;
+            cudaEvent_t e0, e1;
+            RBMG_CK(cudaEventCreate(&e0));
+            RBMG_CK(cudaEventCreate(&e1));
+            RBMG_CK(cudaEventRecord(e0, stream()));
+            for (int k = 0; k < reps; k++) RBMG_CK(cudaGraphLaunch(b->exec, stream()));
+            RBMG_CK(cudaEventRecord(e1, stream()));
+            RBMG_CK(cudaEventSynchronize(e1));
+            float ms = 0.0f;
+            RBMG_CK(cudaEventElapsedTime(&ms, e0, e1));
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            int err = 0;
+            RBMG_CK(cudaMemcpy(&err, b->d_error.p, sizeof(int), cudaMemcpyDeviceToHost));
+            if (err) return fail(RBMG_ETIMEOUT, "batch autotune: a reduction task timed out");
+            const double per = ms / reps;
+            if (ms_out) ms_out[c] = per;
+            c++;
+            if (per < best) {
+                best = per;
+                bw = wpb;
+                brows = rows;
+            }
+        }
+    b->tuned_ms = best;
+    return rbmg_batch_set_shape(b, bw, brows);
+}
+
+// results of the last replay for instance i: <E_loc> over its walkers, the O_k gradient
+// 2 (<E O*> - <E> <O*>) in the reference's parameter layout [2P] (alpha and beta entries 0),
+// optionally the walkers' local energies [2 walkers]
+extern "C" int rbmg_batch_result(const rbmg_batch* b, int i, double* energy, double* grad, double* eloc) {
+    if (!b || i < 0 || i >= b->n || !energy) return fail(RBMG_EINVAL, "batch result: bad arguments");
+    const SInst& I = b->host_inst[i];
+    std::vector<double2> e(I.walkers);
+    RBMG_CK(cudaMemcpy(e.data(), I.eloc, sizeof(double2) * I.walkers, cudaMemcpyDeviceToHost));
+    cplx E(0.0, 0.0);
+    for (const auto& v : e) E += cplx(v.x, v.y);
+    E /= static_cast<double>(I.walkers);
+    energy[0] = E.real();
+    energy[1] = E.imag();
+    if (eloc) std::memcpy(eloc, e.data(), sizeof(double2) * I.walkers);
+    if (grad) {
+        const size_t rows = static_cast<size_t>(I.N + 1) * I.Mpad;
+        std::vector<float2> gO(rows), gEO(rows);
+        RBMG_CK(cudaMemcpy(gO.data(), I.gO, sizeof(float2) * rows, cudaMemcpyDeviceToHost));
+        RBMG_CK(cudaMemcpy(gEO.data(), I.gEO, sizeof(float2) * rows, cudaMemcpyDeviceToHost));
+        cplx* g = reinterpret_cast<cplx*>(grad);
+        const int N = I.N, M = I.M;
+        const double inv = 1.0 / I.walkers;
+        for (int k = 0; k < 2 * N; k++) g[k] = 0.0;
+        auto val = [&](int row, int j) {
+            const float2 o = gO[static_cast<size_t>(row) * I.Mpad + j], eo = gEO[static_cast<size_t>(row) * I.Mpad + j];
+            return 2.0 * (cplx(eo.x, eo.y) * inv - E * cplx(o.x, o.y) * inv);
+        };
+        for (int j = 0; j < M; j++) g[2 * N + j] = val(N, j);
+        for (int r = 0; r < N; r++)
+            for (int j = 0; j < M; j++) g[2 * N + M + static_cast<size_t>(r) * M + j] = val(r, j);
+    }
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_batch_info(const rbmg_batch* b, int* num_instances, uint64_t* accepts, double* tuned_ms) {
+    if (!b) return fail(RBMG_EINVAL, "batch: null");
+    if (num_instances) *num_instances = b->n;
+    if (accepts) RBMG_CK(cudaMemcpy(accepts, b->d_accepts.p, sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    if (tuned_ms) *tuned_ms = b->tuned_ms;
+    return RBMG_OK;
+}
