@@ -310,6 +310,103 @@ def run_gpu(args, rank, world, local_rank):
                 train_s=train_s, e2e_K=e2e_K, h2d=h2d, d2h=d2h, clocks=clk, fp32_peak=fp32_peak)
 
 
+# --------------------------------------------------------------------- serving workload
+def serving_instances(rg):
+    """64 complex RBMs: N uniform in {16, 24, ..., 144}, alpha in {1, 2, 4}, parameters complex
+    Normal(0, 0.05^2) from PCG64(105000 + i), periodic TFIM with h uniform in [0.5, 2],
+    256 N / 16 walkers each (PCG64(105) draws the shapes)."""
+    rng = np.random.Generator(np.random.PCG64(105))
+    inst = []
+    for i in range(64):
+        N = int(rng.choice(np.arange(16, 145, 8)))
+        alpha = int(rng.choice([1, 2, 4]))
+        h = float(rng.uniform(0.5, 2.0))
+        pr = np.random.Generator(np.random.PCG64(105_000 + i))
+        M = alpha * N
+        b = pr.normal(0, 0.05, M) + 1j * pr.normal(0, 0.05, M)
+        W = pr.normal(0, 0.05, (N, M)) + 1j * pr.normal(0, 0.05, (N, M))
+        psi = rg.Psi(np.zeros(N), np.zeros(N), b, W, 1.0, False, True)
+        inst.append((psi, rg.Operator(*rg.operators.tfim_chain(N, 1.0, h)), 256 * N // 16, 5000 + i))
+    return inst
+
+
+def run_serving(args):
+    """One step = one replay of the batch graph: a sweep of every walker of the 64 networks,
+    their local energies and every network's O_k sums."""
+    import torch
+    import rbmongpu_gb300 as rg
+    torch.cuda.set_device(0)
+    inst = serving_instances(rg)
+    batch = rg.Batch(inst)
+    batch.run(100, 1)
+    tune = batch.autotune(sweeps=1, reps=3)
+    sp = rg.library_stream()
+    stream = torch.cuda.ExternalStream(sp)
+    for _ in range(args.warmup):
+        batch.run(0, 1)
+    K = args.steps
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    clocks = ClockSampler(0)
+    clocks.start()
+    for k in range(K):
+        with torch.cuda.stream(stream):
+            flush.fill_(k & 0xFF)
+            starts[k].record(stream)
+        batch.run(0, 1)
+        with torch.cuda.stream(stream):
+            ends[k].record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = np.array([a.elapsed_time(e) for a, e in zip(starts, ends)])
+    walkers = sum(w for _, _, w, _ in inst)
+    # end to end: the replay plus every network's energy and gradient back on the host
+    e2e_K = max(3, K // 5)
+    t0 = time.perf_counter()
+    d2h = 0
+    for _ in range(e2e_K):
+        batch.run(0, 1)
+        for q in range(len(inst)):
+            E, g, _ = batch.result(q)
+            d2h += 16 * inst[q][2] + 2 * 8 * (inst[q][0].N + 1) * ((inst[q][0].M + 31) // 32 * 32)
+    e2e_s = time.perf_counter() - t0
+    flops = 0
+    for psi, _, w, _ in inst:
+        N, M = psi.N, psi.M
+        flops += w * (flops_per_sweep(N, M) + flops_per_eloc(N, M, N) + 8 * (N + 1) * M)
+    peak = None
+    import ctypes
+    from rbmongpu_gb300._lib import call
+    v = ctypes.c_double()
+    call("rbmg_probe_fp32_tflops", 20000, ctypes.byref(v))
+    peak = v.value
+    sec = float(ms.mean()) / 1e3
+    w_shape, rows, blocks = batch.shape
+    line = {
+        "metric": "serving: walker-sweeps/s with E_loc and O_k sums, 64 uneven RBMs in one persistent launch",
+        "value": walkers / sec, "unit": "walker-sweeps/s", "n_gpus": 1, "steps": K, "warmup": args.warmup,
+        "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (complex64)", "data": "synthetic (seeded PCG64 parameters)",
+        "config": {"workload": "serving_64_rbm_n16_144_alpha124_tfim", "instances": len(inst), "walkers": walkers,
+                   "step": "1 sweep + E_loc of every walker + O_k sums (one CUDA-graph replay)",
+                   "shape": {"warps_per_block": w_shape, "tile_rows": rows, "blocks": blocks},
+                   "autotune_ms": {f"{a}x{b}": t for (a, b), t in tune.items()},
+                   "l2": "flushed between timed steps"},
+        "eloc_per_s": walkers / sec,
+        "e2e": {"value": walkers * e2e_K / e2e_s, "unit": "walker-sweeps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": int(d2h / e2e_K)},
+        "gpu_launches": K,
+        "roofline": {"bound": "fp32", "achieved": flops / sec / 1e12, "peak": peak, "unit": "TFLOP/s",
+                     "frac": flops / sec / 1e12 / peak, "traffic": None,
+                     "peak_source": "measured in this run by the library's FP32 FMA probe kernel",
+                     "kernel": "serve_kernel (persistent)", "flops_per_launch": flops},
+        "cpu_baseline": None,
+        "clocks": clk,
+    }
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -317,17 +414,25 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--walkers", type=int, default=WALKERS)
     ap.add_argument("--sweeps-per-row", type=int, default=10)
-    ap.add_argument("--learned-steps-per-row", type=int, default=50)
+    ap.add_argument("--learned-steps-per-row", type=int, default=150,
+                    help="learned steps per row; 150 makes a learned row last about as long as a plain row")
     ap.add_argument("--train-steps", type=int, default=2000)
     ap.add_argument("--train-walkers", type=int, default=4096)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=16.0, help="budget of the CPU baseline leg")
+    ap.add_argument("--workload", default="learned", choices=["learned", "serving"],
+                    help="learned: the N=100 learned-vs-plain chains (headline); serving: 64 uneven RBMs")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     workers = max(1, min(os.cpu_count() or 1, 64))
     import tempfile
+
+    if args.workload == "serving" and args.impl == "ours":
+        if rank == 0:
+            run_serving(args)
+        return
 
     if args.impl == "reference":
         # the reference cannot run N=100 (MAX_SPINS=64 in its include/types.h); its CPU
@@ -399,6 +504,8 @@ def main():
         "plain": dict(pl, ess_per_s=ess_p / sec_p, acceptance=r["plain_accept"],
                       ms_per_row=float(np.mean(r["plain_ms"]))),
         "learned_over_plain_ess_per_s": (ess_l / sec_l) / (ess_p / sec_p),
+        "note": "rows of both chains take about the same time; where tau_converged is false the "
+                "window reached the series length, tau_int is a lower bound and ESS/s an upper bound",
         "energy_gap_in_se": gap,
         "eloc_per_s": n_l / sec_l,
         "e2e": {"value": ess_e2e / sec_e2e, "unit": UNIT, "h2d_bytes_per_step": int(r["h2d"]),

@@ -569,6 +569,7 @@ struct LearnedLaunch {
     float* reward;               // [B]
     unsigned long long* accepts;
     unsigned long long* proposals;
+    int propose_next;            // accept kernel: also draw the next step's move (frozen network)
 };
 
 template <int K, int NW>
@@ -651,15 +652,41 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) learned_accept_kernel(Rbm
         float* cur = L.logits_cur + static_cast<long>(w) * L.O;
         for (int j = lane; j < L.O; j += 32) cur[j] = rowp[j];
     }
+    Spins<NW> cur = s;
+    if (accept) {
+#pragma unroll
+        for (int k = 0; k < NW; k++) cur.w[k] = L.spins_prop[static_cast<long>(w) * NW + k];
+    }
     if (lane == 0) {
         if (accept) {
 #pragma unroll
-            for (int k = 0; k < NW; k++) L.spins[static_cast<long>(w) * NW + k] = L.spins_prop[static_cast<long>(w) * NW + k];
+            for (int k = 0; k < NW; k++) L.spins[static_cast<long>(w) * NW + k] = cur.w[k];
             L.accepts[w] += 1;
         }
-        L.rng_index[w] = rng.index;
         L.reward[w] = a * static_cast<float>(l);
     }
+    if (L.propose_next) {
+        // the next step's move, drawn from the logits of the state the walker is now in
+        // (the draws a separate proposal pass would make, in the same order)
+        const float* row = accept ? rowp : L.logits_cur + static_cast<long>(w) * L.O;
+        const LogNorm lnn = accept ? ln : log_norms(row, L.N, lane);
+        const int i2 = draw_index(row, L.N, lnn.seed, rng.uniform(), lane);
+        const int l2 = 1 + draw_index(row + L.N, kLengths, lnn.len, rng.uniform(), lane);
+        if (lane == 0) {
+            for (int q = 0; q < l2; q++) {
+                int c = i2 + q;
+                if (c >= L.N) c -= L.N;
+                cur.flip(c);
+            }
+#pragma unroll
+            for (int k = 0; k < NW; k++) L.spins_prop[static_cast<long>(w) * NW + k] = cur.w[k];
+            L.site[w] = i2;
+            L.len[w] = l2;
+            L.logq_fwd[w] = (row[i2] - lnn.seed) + (row[L.N + l2 - 1] - lnn.len);
+            L.proposals[w] += 1;
+        }
+    }
+    if (lane == 0) L.rng_index[w] = rng.index;
 }
 
 __device__ __forceinline__ float log_add(float a, float b) {
@@ -856,16 +883,19 @@ cudaError_t launch_lb_target(const RbmDev& P, int n, const uint64_t* spins, cons
 }
 
 // ============================================================================ fused inference
-// One CTA runs the whole network for 64 configurations with the activations in shared
-// memory: x [64][<=256] -> h1 -> h2 -> logits, the weights streamed through a
-// double-buffered cp.async pipeline in chunks of 32 input features (the same k order,
-// tile arithmetic and epilogue as the layer-by-layer GEMM path, so the logits agree bit
-// for bit).  With PROPOSE the CTA first draws the walkers' moves from their current
-// logits and evaluates the network on the proposed configurations.
-constexpr int kFRows = 64;                   // configurations per CTA
-constexpr int kFLd = kHidden + 8;            // activation row stride (bf16)
-constexpr int kFWLd = 40;                    // weight-chunk row stride (bf16)
-constexpr size_t kFSmem = 2 * sizeof(bf16) * kFRows * kFLd + 2 * sizeof(bf16) * kHidden * kFWLd;
+// One CTA runs the whole network for 128 configurations with the activations in shared
+// memory: x [128][<=256] -> h1 -> h2 -> logits.  The weights stream through a 4-stage
+// cp.async pipeline in chunks of 32 input features; the MMA fragments come from shared
+// memory by ldmatrix.  The k order, tile arithmetic and epilogues are those of the
+// layer-by-layer GEMM path, so the logits agree bit for bit.  With PROPOSE the CTA first
+// draws the walkers' moves from their current logits and evaluates the network on the
+// proposed configurations.
+constexpr int kFRows = 128;                  // configurations per CTA
+constexpr int kFThreads = 512;               // 16 warps: 4 (rows) x 4 (columns)
+constexpr int kFStages = 4;
+constexpr int kFLd = kHidden + 8;            // activation row stride (bf16): 528 bytes
+constexpr int kFWLd = 40;                    // weight-chunk row stride (bf16): 80 bytes
+constexpr size_t kFSmem = 2 * sizeof(bf16) * kFRows * kFLd + kFStages * sizeof(bf16) * kHidden * kFWLd;
 
 struct FusedNet {
     int N, O, ldw1;
@@ -885,14 +915,22 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int NPEND>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(NPEND)); }
 
-// acc = A [64][k] (shared, stride kFLd) x Wt^T, Wt [NT*32][ldw] (global, k contiguous);
-// 8 warps as 2 (rows) x 4 (columns), each 32 rows x NT*8 columns
+// four 8x8 b16 matrices; lanes 8q..8q+7 address the rows of matrix q
+__device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const bf16* p) {
+    const unsigned a = static_cast<unsigned>(__cvta_generic_to_shared(p));
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(a));
+}
+
+// acc = A [128][k] (shared, stride kFLd) x Wt^T, Wt [NT*32][ldw] (global, k contiguous);
+// warp (wm, wn) computes rows wm*32 .. +32 and columns wn*NT*8 .. +NT*8
 template <int NT>
 __device__ __forceinline__ void fused_layer(const bf16* sA, int kchunks, const bf16* Wt, int ldw, bf16* sW,
                                             float (&acc)[2][NT][4]) {
+    static_assert(NT % 2 == 0, "B fragments are loaded two n8 tiles at a time");
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int wm = warp & 1, wn = warp >> 1;
-    const int gq = lane >> 2, tq = lane & 3;
+    const int wm = warp & 3, wn = warp >> 2;
     constexpr int kOut = NT * 32;
 #pragma unroll
     for (int i = 0; i < 2; i++)
@@ -900,55 +938,58 @@ __device__ __forceinline__ void fused_layer(const bf16* sA, int kchunks, const b
         for (int j = 0; j < NT; j++)
 #pragma unroll
             for (int e = 0; e < 4; e++) acc[i][j][e] = 0.0f;
-    auto issue = [&](int kc, int buf) {
-        bf16* dst = sW + buf * (kHidden * kFWLd);
-        for (int c = tid; c < kOut * 4; c += 256) {
+    auto issue = [&](int kc, int stage) {
+        bf16* dst = sW + stage * (kHidden * kFWLd);
+        for (int c = tid; c < kOut * 4; c += kFThreads) {
             const int n = c >> 2, q = (c & 3) * 8;
             cp_async16(dst + n * kFWLd + q, Wt + static_cast<long>(n) * ldw + kc * 32 + q);
         }
         cp_async_commit();
     };
-    issue(0, 0);
+#pragma unroll
+    for (int st = 0; st < kFStages - 1; st++) {
+        if (st < kchunks) issue(st, st);
+        else cp_async_commit();
+    }
+    // ldmatrix row addresses of this lane: A rows (lane & 15), column half (lane >> 4);
+    // B rows (lane & 7) + 8 (lane >> 4), column half (lane >> 3) & 1
+    const int a_row = wm * 32 + (lane & 15), a_col = (lane >> 4) * 8;
+    const int b_row = wn * NT * 8 + (lane & 7) + ((lane >> 4) << 3), b_col = ((lane >> 3) & 1) * 8;
     for (int kc = 0; kc < kchunks; kc++) {
-        if (kc + 1 < kchunks) {
-            issue(kc + 1, (kc + 1) & 1);
-            cp_async_wait<1>();
-        } else {
-            cp_async_wait<0>();
-        }
+        cp_async_wait<kFStages - 2>();
         __syncthreads();
-        const bf16* w = sW + (kc & 1) * (kHidden * kFWLd);
+        const int nk = kc + kFStages - 1;
+        if (nk < kchunks) issue(nk, nk % kFStages);
+        else cp_async_commit();
+        const bf16* w = sW + (kc % kFStages) * (kHidden * kFWLd);
 #pragma unroll
         for (int ks = 0; ks < 32; ks += 16) {
             uint32_t af[2][4], bfr[NT][2];
-            const int col = kc * 32 + ks + 2 * tq;
 #pragma unroll
-            for (int mi = 0; mi < 2; mi++) {
-                const int row = wm * 32 + mi * 16 + gq;
-                af[mi][0] = *reinterpret_cast<const uint32_t*>(sA + row * kFLd + col);
-                af[mi][1] = *reinterpret_cast<const uint32_t*>(sA + (row + 8) * kFLd + col);
-                af[mi][2] = *reinterpret_cast<const uint32_t*>(sA + row * kFLd + col + 8);
-                af[mi][3] = *reinterpret_cast<const uint32_t*>(sA + (row + 8) * kFLd + col + 8);
-            }
+            for (int mi = 0; mi < 2; mi++) ldsm_x4(af[mi], sA + (a_row + mi * 16) * kFLd + kc * 32 + ks + a_col);
 #pragma unroll
-            for (int ni = 0; ni < NT; ni++) {
-                const int n = wn * NT * 8 + ni * 8 + gq;
-                bfr[ni][0] = *reinterpret_cast<const uint32_t*>(w + n * kFWLd + ks + 2 * tq);
-                bfr[ni][1] = *reinterpret_cast<const uint32_t*>(w + n * kFWLd + ks + 2 * tq + 8);
+            for (int ni = 0; ni < NT; ni += 2) {
+                uint32_t r[4];
+                ldsm_x4(r, w + (b_row + ni * 8) * kFWLd + ks + b_col);
+                bfr[ni][0] = r[0];
+                bfr[ni][1] = r[1];
+                bfr[ni + 1][0] = r[2];
+                bfr[ni + 1][1] = r[3];
             }
 #pragma unroll
             for (int mi = 0; mi < 2; mi++)
 #pragma unroll
                 for (int ni = 0; ni < NT; ni++) mma_bf16_16816(acc[mi][ni], af[mi], bfr[ni]);
         }
-        __syncthreads();
     }
+    cp_async_wait<0>();
+    __syncthreads();   // every warp is done with the stages before they are refilled
 }
 
-// h = bf16(silu(acc + b)) into dst [64][kFLd]
+// h = bf16(silu(acc + b)) into dst [128][kFLd]
 __device__ __forceinline__ void fused_silu_store(const float (&acc)[2][8][4], const float* b, bf16* dst) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int wm = warp & 1, wn = warp >> 1, gq = lane >> 2, tq = lane & 3;
+    const int wm = warp & 3, wn = warp >> 2, gq = lane >> 2, tq = lane & 3;
 #pragma unroll
     for (int mi = 0; mi < 2; mi++)
 #pragma unroll
@@ -963,8 +1004,9 @@ __device__ __forceinline__ void fused_silu_store(const float (&acc)[2][8][4], co
 }
 
 template <int NW, bool PROPOSE>
-__global__ void __launch_bounds__(256, 2) mlp_fused_kernel(FusedNet net, LearnedLaunch L, const uint64_t* in_spins,
-                                                           int count, float* logits_out) {
+__global__ void __launch_bounds__(kFThreads, 1) mlp_fused_kernel(FusedNet net, LearnedLaunch L,
+                                                                 const uint64_t* in_spins, int count,
+                                                                 float* logits_out) {
     extern __shared__ __align__(16) unsigned char fsm[];
     bf16* sX = reinterpret_cast<bf16*>(fsm);
     bf16* sH = sX + kFRows * kFLd;
@@ -972,7 +1014,7 @@ __global__ void __launch_bounds__(256, 2) mlp_fused_kernel(FusedNet net, Learned
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int row0 = blockIdx.x * kFRows;
     // ---- the input configurations (proposed moves with PROPOSE), one warp per row
-    for (int r = warp; r < kFRows; r += 8) {
+    for (int r = warp; r < kFRows; r += kFThreads / 32) {
         const int w = row0 + r;
         Spins<NW> s;
 #pragma unroll
@@ -1025,7 +1067,7 @@ __global__ void __launch_bounds__(256, 2) mlp_fused_kernel(FusedNet net, Learned
         fused_silu_store(acc, net.b2, sX);
         __syncthreads();
     }
-    const int wm = warp & 1, wn = warp >> 1, gq = lane >> 2, tq = lane & 3;
+    const int wm = warp & 3, wn = warp >> 2, gq = lane >> 2, tq = lane & 3;
     for (int pass = 0; pass * 128 < net.O; pass++) {
         float acc[2][4][4];
         fused_layer<4>(sX, kHidden / 32, net.w3t + static_cast<long>(pass) * 128 * kHidden, kHidden, sW, acc);
@@ -1058,7 +1100,7 @@ cudaError_t launch_fused_nw(const FusedNet& net, const LearnedLaunch& L, const u
     const cudaError_t e = cudaFuncSetAttribute(mlp_fused_kernel<NW, PROPOSE>,
                                                cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kFSmem));
     if (e != cudaSuccess) return e;
-    mlp_fused_kernel<NW, PROPOSE><<<(count + kFRows - 1) / kFRows, 256, kFSmem, st>>>(net, L, in, count, out);
+    mlp_fused_kernel<NW, PROPOSE><<<(count + kFRows - 1) / kFRows, kFThreads, kFSmem, st>>>(net, L, in, count, out);
     return cudaGetLastError();
 }
 
@@ -1297,7 +1339,12 @@ extern "C" int rbmg_chain_learned_async(rbmg_chain* c, const rbmg_psi* psi, cons
     double2* out = static_cast<double2*>(d_eloc_out);
     const int lead = d_eloc_out ? n_steps % measure_every : n_steps;
     for (int step = 0; step < n_steps; step++) {
-        RBMG_CK(launch_fused<true>(prop, L, nullptr, B, S->logits_prop.as<float>(), st));
+        // frozen network: the accept kernel draws the next move, so the later steps only
+        // evaluate the network on the proposed configurations; while training, the weights
+        // change after every step and each step draws its move from the new logits
+        if (nt == 0 && step > 0) RBMG_CK(launch_fused<false>(prop, L, L.spins_prop, B, S->logits_prop.as<float>(), st));
+        else RBMG_CK(launch_fused<true>(prop, L, nullptr, B, S->logits_prop.as<float>(), st));
+        L.propose_next = nt == 0 && step + 1 < n_steps ? 1 : 0;
         RBMG_CK(launch_learned(1, P, L, st));
         if (nt > 0 && prop->objective == RBMG_PROPOSAL_LOCALLY_BALANCED) {
             // cross-entropy to the locally balanced proposal at the first nt walkers' states

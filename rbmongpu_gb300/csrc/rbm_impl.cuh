@@ -29,8 +29,8 @@ __device__ __forceinline__ void rbm_refresh(const RbmDev& P, const Spins<NW>& s,
 #pragma unroll
         for (int k = 0; k < K; k++) {
             const float2 w = __ldg(row + 32 * k);
-            tr[k] = __fadd_rn(tr[k], sg * w.x);
-            ti[k] = __fadd_rn(ti[k], sg * w.y);
+            tr[k] = __fmaf_rn(sg, w.x, tr[k]);   // sg = +-1: the product is exact
+            ti[k] = __fmaf_rn(sg, w.y, ti[k]);
         }
     }
 }

@@ -4,8 +4,9 @@
 // One persistent launch serves the whole batch.  Its warps take tasks from a global
 // queue (one atomic counter): first the walker tasks of every instance, longest first
 // (sweeps of single-flip Metropolis, the local energy and tanh(theta) of the final
-// configuration), then the reduction tasks, each a tile of rows of one instance's
-// O_k sums, which start once that instance's walkers are all done (a per-instance
+// configuration), then the reduction tasks, each a tile of rows by a chunk of walkers
+// of one instance's O_k sums (added with FP32 atomics), which start once that instance's
+// walkers are all done (a per-instance
 // counter; the wait is bounded by a wall-clock limit after which the kernel raises an
 // error flag and returns).  Hidden units per lane are a runtime count (up to 18, M <= 576)
 // with register arrays of the maximum size, so one kernel serves every shape.  The
@@ -51,7 +52,10 @@ struct STask {
     int kind;    // 0 walker, 1 reduction tile
     int inst;
     int index;   // walker within the instance, or first row of the tile
+    int w0;      // reduction tile: first walker of its walker chunk
 };
+
+constexpr int kReduceWalkers = 256;   // walkers per reduction tile
 
 struct SLaunch {
     const SInst* inst;
@@ -87,8 +91,8 @@ __device__ __forceinline__ void s_refresh(const SInst& I, const Spins<NW>& s, fl
         for (int k = 0; k < kSK; k++)
             if (k < I.K) {
                 const float2 w = __ldg(row + 32 * k);
-                tr[k] = __fadd_rn(tr[k], sg * w.x);
-                ti[k] = __fadd_rn(ti[k], sg * w.y);
+                tr[k] = __fmaf_rn(sg, w.x, tr[k]);   // sg = +-1: the product is exact
+                ti[k] = __fmaf_rn(sg, w.y, ti[k]);
             }
     }
 }
@@ -236,9 +240,11 @@ __device__ __noinline__ void walker_task(const SLaunch& L, const SInst& I, int w
     if (lane == 0) atomicAdd(I.done, 1u);
 }
 
-// rows [r0, r0 + R) of the instance's O_k sums (row N: the biases), every column
+// rows [r0, r0 + R) of the instance's O_k sums (row N: the biases), every column, over
+// walkers [w0, w0 + kReduceWalkers): added to the sums with FP32 atomics (the sums are
+// zeroed by the replay; their order of addition is not fixed)
 template <int R>
-__device__ __noinline__ void reduce_task(const SLaunch& L, const SInst& I, int r0, int lane) {
+__device__ __noinline__ void reduce_task(const SLaunch& L, const SInst& I, int r0, int w0, int lane) {
     // wait for the instance's walkers (bounded: 20 s of wall clock)
     if (lane == 0) {
         const unsigned long long t0 = global_ns();
@@ -262,7 +268,8 @@ __device__ __noinline__ void reduce_task(const SLaunch& L, const SInst& I, int r
         }
         const int j = lane + 32 * kc;
         const int wd0 = r0 >> 6, wd1 = min(r0 + R - 1, I.N - 1) >> 6;   // the rows span at most two words
-        for (int w = 0; w < I.walkers; w++) {
+        const int w1 = min(I.walkers, w0 + kReduceWalkers);
+        for (int w = w0; w < w1; w++) {
             // L2 loads (__ldcg): the walkers' results were written by other SMs
             const float2 t = __ldcg(I.T + static_cast<long>(w) * I.Mpad + j);
             const double2 ed = __ldcg(I.eloc + w);
@@ -292,8 +299,12 @@ __device__ __noinline__ void reduce_task(const SLaunch& L, const SInst& I, int r
         for (int r = 0; r < R; r++) {
             const int i = r0 + r;
             if (i <= I.N) {
-                I.gO[static_cast<long>(i) * I.Mpad + j] = aO[r];
-                I.gEO[static_cast<long>(i) * I.Mpad + j] = aE[r];
+                float* o = reinterpret_cast<float*>(I.gO + static_cast<long>(i) * I.Mpad + j);
+                float* eo = reinterpret_cast<float*>(I.gEO + static_cast<long>(i) * I.Mpad + j);
+                atomicAdd(o, aO[r].x);
+                atomicAdd(o + 1, aO[r].y);
+                atomicAdd(eo, aE[r].x);
+                atomicAdd(eo + 1, aE[r].y);
             }
         }
     }
@@ -312,7 +323,7 @@ __global__ void serve_kernel(SLaunch L) {
         if (task.kind == 0) {
             walker_task(L, I, task.index, lane);
         } else {
-            reduce_task<R>(L, I, task.index, lane);
+            reduce_task<R>(L, I, task.index, task.w0, lane);
         }
     }
 }
@@ -328,7 +339,8 @@ struct rbmg_batch {
     std::vector<const rbmg_operator*> ops;
     std::vector<SInst> host_inst;
     std::vector<uint32_t> walkers;
-    DevBuf d_inst, d_tasks, d_next, d_done, d_error, d_accepts;
+    DevBuf d_inst, d_tasks, d_next, d_done, d_error, d_accepts, d_sums;
+    size_t sums_bytes = 0;
     std::vector<std::unique_ptr<DevBuf>> bufs;
     int ntasks_walk = 0, ntasks = 0;
     int rows = 16;              // reduction tile height
@@ -358,10 +370,11 @@ int batch_tasks(rbmg_batch* b) {
     });
     std::vector<STask> tasks;
     for (int i : order)
-        for (int w = 0; w < b->host_inst[i].walkers; w++) tasks.push_back(STask{0, i, w});
+        for (int w = 0; w < b->host_inst[i].walkers; w++) tasks.push_back(STask{0, i, w, 0});
     b->ntasks_walk = static_cast<int>(tasks.size());
     for (int i : order)
-        for (int r0 = 0; r0 <= b->host_inst[i].N; r0 += b->rows) tasks.push_back(STask{1, i, r0});
+        for (int r0 = 0; r0 <= b->host_inst[i].N; r0 += b->rows)
+            for (int w0 = 0; w0 < b->host_inst[i].walkers; w0 += kReduceWalkers) tasks.push_back(STask{1, i, r0, w0});
     b->ntasks = static_cast<int>(tasks.size());
     RBMG_CK(b->d_tasks.ensure(sizeof(STask) * tasks.size()));
     RBMG_CK(cudaMemcpy(b->d_tasks.p, tasks.data(), sizeof(STask) * tasks.size(), cudaMemcpyHostToDevice));
@@ -410,6 +423,7 @@ int batch_capture(rbmg_batch* b) {
     cudaMemsetAsync(b->d_next.p, 0, sizeof(unsigned int), st);
     cudaMemsetAsync(b->d_done.p, 0, sizeof(unsigned int) * b->n, st);
     cudaMemsetAsync(b->d_accepts.p, 0, sizeof(unsigned long long), st);
+    cudaMemsetAsync(b->d_sums.p, 0, b->sums_bytes, st);
     const cudaError_t le = launch_serve(b, st);
     cudaGraph_t g = nullptr;
     const cudaError_t ce = cudaStreamEndCapture(st, &g);
@@ -478,15 +492,27 @@ extern "C" int rbmg_batch_create(int n, const rbmg_psi* const* psis, const rbmg_
         I.T = static_cast<float2*>(alloc(sizeof(float2) * B * p->Mpad));
         I.spins = static_cast<uint64_t*>(alloc(sizeof(uint64_t) * B * nw));
         I.rng_index = static_cast<uint64_t*>(alloc(sizeof(uint64_t) * B));
-        I.gO = static_cast<float2*>(alloc(sizeof(float2) * (p->N + 1) * p->Mpad));
-        I.gEO = static_cast<float2*>(alloc(sizeof(float2) * (p->N + 1) * p->Mpad));
-        if (!I.eloc || !I.T || !I.spins || !I.rng_index || !I.gO || !I.gEO)
+        if (!I.eloc || !I.T || !I.spins || !I.rng_index)
             return fail(RBMG_ENOMEM, "batch: device allocation failed");
         RBMG_CK(cudaMemset(I.rng_index, 0, sizeof(uint64_t) * B));
         b->psis.push_back(p);
         b->ops.push_back(o);
         b->walkers.push_back(walkers[i]);
         b->host_inst.push_back(I);
+    }
+    // the O_k sums of all instances in one buffer, zeroed by every replay
+    size_t tot = 0;
+    for (const auto& I : b->host_inst) tot += 2 * static_cast<size_t>(I.N + 1) * I.Mpad;
+    b->sums_bytes = sizeof(float2) * tot;
+    RBMG_CK(b->d_sums.ensure(b->sums_bytes));
+    {
+        float2* q = b->d_sums.as<float2>();
+        for (auto& I : b->host_inst) {
+            I.gO = q;
+            q += static_cast<size_t>(I.N + 1) * I.Mpad;
+            I.gEO = q;
+            q += static_cast<size_t>(I.N + 1) * I.Mpad;
+        }
     }
     RBMG_CK(b->d_done.ensure(sizeof(unsigned int) * n));
     for (int i = 0; i < n; i++) b->host_inst[i].done = b->d_done.as<unsigned int>() + i;
