@@ -369,6 +369,12 @@ static int op_compile(rbmg_operator* op) {
     for (int n = 0; n < op->S; n++)
         c32[n] = make_float2(static_cast<float>(op->coef[n].real()), static_cast<float>(op->coef[n].imag()));
     RBMG_CK(up(op->d_coef32, c32.data(), sizeof(float2) * op->S));
+    std::vector<int> site1(op->S, -1), next1(op->S + 1, op->S);
+    for (int n = 0; n < op->S; n++)
+        if (op->nflip[n] == 1) site1[n] = op->flip_sites[op->flip_off[n]];
+    for (int n = op->S - 1; n >= 0; n--) next1[n] = site1[n] >= 0 ? n : next1[n + 1];
+    RBMG_CK(up(op->d_site1, site1.data(), sizeof(int) * op->S));
+    RBMG_CK(up(op->d_next1, next1.data(), sizeof(int) * (op->S + 1)));
     RBMG_CK(up(op->d_ypow, op->ypow.data(), sizeof(int) * op->S));
     RBMG_CK(up(op->d_zmask, op->zmask.data(), sizeof(uint64_t) * op->zmask.size()));
     RBMG_CK(up(op->d_nflip, op->nflip.data(), sizeof(int) * op->S));

@@ -102,7 +102,7 @@ struct rbmg_operator {
     std::vector<uint64_t> zmask;
     int num_offdiag = 0;
     int max_site = -1;
-    rbmg::DevBuf d_coef, d_coef32, d_ypow, d_zmask, d_nflip, d_flip_off, d_flip_sites, d_slot;
+    rbmg::DevBuf d_coef, d_coef32, d_site1, d_next1, d_ypow, d_zmask, d_nflip, d_flip_off, d_flip_sites, d_slot;
     // per-site CSR of the off-diagonal slots whose string flips the site (E_k term)
     std::vector<int> site_ptr, site_slots;
     rbmg::DevBuf d_site_ptr, d_site_slots;
@@ -117,7 +117,9 @@ struct rbmg_operator {
                            d_flip_sites.as<int>(),
                            d_slot.as<int>(),
                            num_offdiag,
-                           d_coef32.as<float2>()};
+                           d_coef32.as<float2>(),
+                           d_site1.as<int>(),
+                           d_next1.as<int>()};
     }
 };
 

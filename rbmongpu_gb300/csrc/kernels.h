@@ -32,6 +32,8 @@ struct OpDev {
     const int* offdiag_slot;   // [S] index among off-diagonal strings, -1 if diagonal
     int num_offdiag;
     const float2* coef32;      // [S] coefficients rounded to FP32 (local-energy sums)
+    const int* site1;          // [S] the flipped site of a single-flip string, -1 otherwise
+    const int* next1;          // [S + 1] next1[n]: first single-flip string >= n (S if none)
 };
 
 // Metropolis launch: one warp per walker (include/spin_ensembles/MonteCarloLoop.hpp:55-256)

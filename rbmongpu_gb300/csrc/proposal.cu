@@ -72,9 +72,11 @@ struct GemmArgs {
 
 constexpr int kBM = 128, kBN = 64, kBK = 32, kSK = kBK + 8, kGemmThreads = 256;
 
-__device__ __forceinline__ float silu_f(float z) { return z / (1.0f + expf(-z)); }
+// SiLU and its derivative with the hardware exponential and division: the activations
+// are rounded to BF16 (8 significant bits) right after, far above their ~1e-6 error
+__device__ __forceinline__ float silu_f(float z) { return __fdividef(z, 1.0f + __expf(-z)); }
 __device__ __forceinline__ float dsilu_f(float z) {
-    const float sg = 1.0f / (1.0f + expf(-z));
+    const float sg = __fdividef(1.0f, 1.0f + __expf(-z));
     return sg * (1.0f + z * (1.0f - sg));
 }
 
@@ -986,21 +988,29 @@ __device__ __forceinline__ void fused_layer(const bf16* sA, int kchunks, const b
     __syncthreads();   // every warp is done with the stages before they are refilled
 }
 
-// h = bf16(silu(acc + b)) into dst [128][kFLd]
+// h = bf16(silu(acc + b)) into dst [128][kFLd]; the thread's 16 bias values are loaded once
 __device__ __forceinline__ void fused_silu_store(const float (&acc)[2][8][4], const float* b, bf16* dst) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int wm = warp & 3, wn = warp >> 2, gq = lane >> 2, tq = lane & 3;
+    float bias[8][2];
+#pragma unroll
+    for (int ni = 0; ni < 8; ni++) {
+        const float2 v = *reinterpret_cast<const float2*>(b + wn * 64 + ni * 8 + 2 * tq);
+        bias[ni][0] = v.x;
+        bias[ni][1] = v.y;
+    }
 #pragma unroll
     for (int mi = 0; mi < 2; mi++)
 #pragma unroll
         for (int ni = 0; ni < 8; ni++)
 #pragma unroll
-            for (int h = 0; h < 2; h++)
-#pragma unroll
-                for (int e = 0; e < 2; e++) {
-                    const int r = wm * 32 + mi * 16 + gq + 8 * h, n = wn * 64 + ni * 8 + 2 * tq + e;
-                    dst[r * kFLd + n] = __float2bfloat16_rn(silu_f(acc[mi][ni][h * 2 + e] + b[n]));
-                }
+            for (int h = 0; h < 2; h++) {
+                const int r = wm * 32 + mi * 16 + gq + 8 * h, n = wn * 64 + ni * 8 + 2 * tq;
+                __nv_bfloat162 v;
+                v.x = __float2bfloat16_rn(silu_f(acc[mi][ni][h * 2] + bias[ni][0]));
+                v.y = __float2bfloat16_rn(silu_f(acc[mi][ni][h * 2 + 1] + bias[ni][1]));
+                *reinterpret_cast<__nv_bfloat162*>(dst + r * kFLd + n) = v;
+            }
 }
 
 template <int NW, bool PROPOSE>

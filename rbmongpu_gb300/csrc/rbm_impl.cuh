@@ -393,7 +393,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) rbm_est_kernel(RbmDev P, 
 // angle by angle (Operator.hpp:90-115).
 // ---------------------------------------------------------------------------
 template <int K, int NW>
-__global__ void __launch_bounds__(32 * kWarpsPerBlock) rbm_eloc_kernel(RbmDev P, OpDev op, EstLaunch L) {
+__global__ void __launch_bounds__(32 * kWarpsPerBlock, K > 13 ? 3 : 4) rbm_eloc_kernel(RbmDev P, OpDev op, EstLaunch L) {
     const int lane = threadIdx.x & 31;
     const long t = static_cast<long>(blockIdx.x) * kWarpsPerBlock + (threadIdx.x >> 5);
     if (t >= L.count) return;
@@ -412,7 +412,16 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) rbm_eloc_kernel(RbmDev P,
     float2 f[K];
 #pragma unroll
     for (int k = 0; k < K; k++) f[k] = lc_c(tr[k], ti[k]);
+    // the W row of the next single-flip string is loaded while the current string is
+    // evaluated, so the row's latency is off the per-string critical path
     KahanC acc;
+    float2 wbuf[K];
+    int nxt = op.next1[0];
+    if (nxt < op.S) {
+        const float2* row = P.W + static_cast<long>(op.site1[nxt]) * P.Mpad + lane;
+#pragma unroll
+        for (int k = 0; k < K; k++) wbuf[k] = __ldg(row + 32 * k);
+    }
     for (int n = 0; n < op.S; n++) {
         const float2 cf = string_factor(op, n, s);
         const int nf = op.nflip[n];
@@ -420,20 +429,27 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) rbm_eloc_kernel(RbmDev P,
             acc.add(cf.x, cf.y);
             continue;
         }
-        const int off = op.flip_off[n];
         float2 part = make_float2(0.0f, 0.0f);
-        if (nf == 1) {
-            const int site = op.flip_sites[off];
+        if (nf == 1) {   // n == nxt
+            const int site = op.site1[n];
             const float two_s = s.up(site) ? -2.0f : 2.0f;
-            const float2* row = P.W + static_cast<long>(site) * P.Mpad + lane;
+            float2 w[K];
+#pragma unroll
+            for (int k = 0; k < K; k++) w[k] = wbuf[k];
+            nxt = op.next1[n + 1];
+            if (nxt < op.S) {
+                const float2* row = P.W + static_cast<long>(op.site1[nxt]) * P.Mpad + lane;
+#pragma unroll
+                for (int k = 0; k < K; k++) wbuf[k] = __ldg(row + 32 * k);
+            }
 #pragma unroll
             for (int k = 0; k < K; k++) {
-                const float2 w = __ldg(row + 32 * k);
-                const float2 g = lc_c(fmaf(two_s, w.x, tr[k]), fmaf(two_s, w.y, ti[k]));
+                const float2 g = lc_c(fmaf(two_s, w[k].x, tr[k]), fmaf(two_s, w[k].y, ti[k]));
                 part.x += g.x - f[k].x;
                 part.y += g.y - f[k].y;
             }
         } else {
+            const int off = op.flip_off[n];
 #pragma unroll
             for (int k = 0; k < K; k++) {
                 float nr = tr[k], ni = ti[k];
