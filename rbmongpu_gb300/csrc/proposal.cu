@@ -514,14 +514,21 @@ struct LogNorm {
 };
 
 __device__ __forceinline__ LogNorm log_norms(const float* row, int N, int lane) {
-    float m = -INFINITY;
-    for (int j = lane; j < N; j += 32) m = fmaxf(m, row[j]);
+    // the row's entries j = lane + 32 c (N <= 256) are loaded together first
+    float v[8];
+#pragma unroll
+    for (int c = 0; c < 8; c++) v[c] = lane + 32 * c < N ? row[lane + 32 * c] : -INFINITY;
+    const float vl = lane < kLengths ? row[N + lane] : -INFINITY;
+    float m = v[0];
+#pragma unroll
+    for (int c = 1; c < 8; c++) m = fmaxf(m, v[c]);
 #pragma unroll
     for (int off = 16; off >= 1; off >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, off));
     float s = 0.0f;
-    for (int j = lane; j < N; j += 32) s += expf(row[j] - m);
+#pragma unroll
+    for (int c = 0; c < 8; c++)
+        if (lane + 32 * c < N) s += expf(v[c] - m);
     s = warp_sum_xor(s);
-    const float vl = lane < kLengths ? row[N + lane] : -INFINITY;
     float m2 = vl;
 #pragma unroll
     for (int off = 16; off >= 1; off >>= 1) m2 = fmaxf(m2, __shfl_xor_sync(0xffffffffu, m2, off));

@@ -8,8 +8,8 @@
 // of one instance's O_k sums (added with FP32 atomics), which start once that instance's
 // walkers are all done (a per-instance
 // counter; the wait is bounded by a wall-clock limit after which the kernel raises an
-// error flag and returns).  Hidden units per lane are a runtime count (up to 18, M <= 576)
-// with register arrays of the maximum size, so one kernel serves every shape.  The
+// error flag and returns).  The walker tasks are compiled for each hidden-unit count per
+// lane (1, 2, 4, 8, 13, 18: M <= 576) as separate functions of the one kernel.  The
 // launch (counter resets + kernel) is captured once in a CUDA graph and replayed; the
 // warps per block and the reduction tile height come from an autotuner that times the
 // candidates on the batch itself.
@@ -74,71 +74,68 @@ __device__ __forceinline__ unsigned long long global_ns() {
     return t;
 }
 
-template <int NW>
-__device__ __forceinline__ void s_refresh(const SInst& I, const Spins<NW>& s, float (&tr)[kSK], float (&ti)[kSK],
+template <int K, int NW>
+__device__ __forceinline__ void s_refresh(const SInst& I, const Spins<NW>& s, float (&tr)[K], float (&ti)[K],
                                           int lane) {
 #pragma unroll
-    for (int k = 0; k < kSK; k++)
-        if (k < I.K) {
-            const float2 b = __ldg(I.b + lane + 32 * k);
-            tr[k] = b.x;
-            ti[k] = b.y;
-        }
+    for (int k = 0; k < K; k++) {
+        const float2 b = __ldg(I.b + lane + 32 * k);
+        tr[k] = b.x;
+        ti[k] = b.y;
+    }
     const float2* row = I.W + lane;
     for (int i = 0; i < I.N; i++, row += I.Mpad) {
         const float sg = s.up(i) ? 1.0f : -1.0f;
 #pragma unroll
-        for (int k = 0; k < kSK; k++)
-            if (k < I.K) {
-                const float2 w = __ldg(row + 32 * k);
-                tr[k] = __fmaf_rn(sg, w.x, tr[k]);   // sg = +-1: the product is exact
-                ti[k] = __fmaf_rn(sg, w.y, ti[k]);
-            }
+        for (int k = 0; k < K; k++) {
+            const float2 w = __ldg(row + 32 * k);
+            tr[k] = __fmaf_rn(sg, w.x, tr[k]);   // sg = +-1: the product is exact
+            ti[k] = __fmaf_rn(sg, w.y, ti[k]);
+        }
     }
 }
 
 // single-flip Metropolis step: the arithmetic and draw order of rbm_mh_step
-template <int NW>
-__device__ __forceinline__ bool s_mh_step(const SInst& I, Spins<NW>& s, float (&tr)[kSK], float (&ti)[kSK],
-                                          float (&re)[kSK], WarpRng& rng, int lane, uint64_t nmagic) {
+template <int K, int NW>
+__device__ __forceinline__ bool s_mh_step(const SInst& I, Spins<NW>& s, float (&tr)[K], float (&ti)[K],
+                                          float (&re)[K], WarpRng& rng, int lane, uint64_t nmagic) {
     const int site = static_cast<int>(fastmod(rng.next(), nmagic, static_cast<uint32_t>(I.N)));
     Spins<NW> s2 = s;
     s2.flip(site);
     const float two_s = s2.up(site) ? 2.0f : -2.0f;
     const float2* row = I.W + static_cast<long>(site) * I.Mpad + lane;
-    float2 w[kSK];
+    float2 w[K];
 #pragma unroll
-    for (int k = 0; k < kSK; k++)
-        if (k < I.K) w[k] = __ldg(row + 32 * k);
+    for (int k = 0; k < K; k++) w[k] = __ldg(row + 32 * k);
     float part = 0.0f;
 #pragma unroll
-    for (int k = 0; k < kSK; k++)
-        if (k < I.K) {
-            const float nr = __fmaf_rn(two_s, w[k].x, tr[k]);
-            const float ni = __fmaf_rn(two_s, w[k].y, ti[k]);
-            part = __fadd_rn(part, __fsub_rn(lc_re(nr, ni), re[k]));
-        }
+    for (int k = 0; k < K; k++) {
+        const float nr = __fmaf_rn(two_s, w[k].x, tr[k]);
+        const float ni = __fmaf_rn(two_s, w[k].y, ti[k]);
+        part = __fadd_rn(part, __fsub_rn(lc_re(nr, ni), re[k]));
+    }
     const float delta = warp_sum_xor(part);
     bool accept = delta > 0.0f;
     if (!accept) accept = rng.uniform() <= expf_det(__fmul_rn(2.0f, delta));
     if (accept) {
         s = s2;
 #pragma unroll
-        for (int k = 0; k < kSK; k++)
-            if (k < I.K) {
-                const float2 ww = __ldg(row + 32 * k);
-                tr[k] = __fmaf_rn(two_s, ww.x, tr[k]);
-                ti[k] = __fmaf_rn(two_s, ww.y, ti[k]);
-                re[k] = lc_re(tr[k], ti[k]);
-            }
+        for (int k = 0; k < K; k++) {
+            const float2 ww = __ldg(row + 32 * k);
+            tr[k] = __fmaf_rn(two_s, ww.x, tr[k]);
+            ti[k] = __fmaf_rn(two_s, ww.y, ti[k]);
+            re[k] = lc_re(tr[k], ti[k]);
+        }
     }
     return accept;
 }
 
 // each task kind is a separate (not inlined) function, so that the register allocation of
 // one does not constrain the others
-__device__ __noinline__ void walker_task(const SLaunch& L, const SInst& I, int w, int lane) {
+template <int K>
+__device__ __noinline__ void walker_task(const SLaunch& L, const SInst& Ig, int w, int lane) {
     constexpr int NW = kSW;
+    const SInst I = Ig;   // the descriptor in registers / local memory, not re-read from global
     WarpRng rng;
     rng.init(I.seed, static_cast<uint32_t>(w), I.rng_index[w], lane);
     const uint64_t nmagic = fastmod_magic(static_cast<uint32_t>(I.N));
@@ -162,14 +159,13 @@ __device__ __noinline__ void walker_task(const SLaunch& L, const SInst& I, int w
         for (int k = 0; k < NW; k++)
             if (k < I.nw) s.w[k] = I.spins[static_cast<long>(w) * I.nw + k];
     }
-    float tr[kSK], ti[kSK], re[kSK];
+    float tr[K], ti[K], re[K];
     unsigned long long acc = 0;
     const int total = (L.first ? L.therm : 0) + L.sweeps;
     for (int sw = 0; sw < total; sw++) {
         s_refresh(I, s, tr, ti, lane);
 #pragma unroll
-        for (int k = 0; k < kSK; k++)
-            if (k < I.K) re[k] = lc_re(tr[k], ti[k]);
+        for (int k = 0; k < K; k++) re[k] = lc_re(tr[k], ti[k]);
         for (int p = 0; p < I.N; p++) acc += s_mh_step(I, s, tr, ti, re, rng, lane, nmagic);
     }
     // measurement: local energy and tanh(theta) of the final configuration; f(theta) in
@@ -178,11 +174,10 @@ __device__ __noinline__ void walker_task(const SLaunch& L, const SInst& I, int w
     extern __shared__ float2 s_f[];
     float2* myf = s_f + (threadIdx.x >> 5) * kSK * 32 + lane;
 #pragma unroll
-    for (int k = 0; k < kSK; k++)
-        if (k < I.K) {
-            myf[32 * k] = lc_c(tr[k], ti[k]);
-            I.T[static_cast<long>(w) * I.Mpad + lane + 32 * k] = tanh_c(tr[k], ti[k]);
-        }
+    for (int k = 0; k < K; k++) {
+        myf[32 * k] = lc_c(tr[k], ti[k]);
+        I.T[static_cast<long>(w) * I.Mpad + lane + 32 * k] = tanh_c(tr[k], ti[k]);
+    }
     KahanC e;
     for (int n = 0; n < I.op.S; n++) {
         const float2 cf = string_factor(I.op, n, s);
@@ -197,19 +192,19 @@ __device__ __noinline__ void walker_task(const SLaunch& L, const SInst& I, int w
             const int site = I.op.flip_sites[off];
             const float two_s = s.up(site) ? -2.0f : 2.0f;
             const float2* row = I.W + static_cast<long>(site) * I.Mpad + lane;
+            float2 wv[K];
 #pragma unroll
-            for (int k = 0; k < kSK; k++)
-                if (k < I.K) {
-                    const float2 wv = __ldg(row + 32 * k);
-                    const float2 g = lc_c(fmaf(two_s, wv.x, tr[k]), fmaf(two_s, wv.y, ti[k]));
-                    const float2 f0 = myf[32 * k];
-                    part.x += g.x - f0.x;
-                    part.y += g.y - f0.y;
-                }
+            for (int k = 0; k < K; k++) wv[k] = __ldg(row + 32 * k);
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                const float2 g = lc_c(fmaf(two_s, wv[k].x, tr[k]), fmaf(two_s, wv[k].y, ti[k]));
+                const float2 f0 = myf[32 * k];
+                part.x += g.x - f0.x;
+                part.y += g.y - f0.y;
+            }
         } else {
 #pragma unroll
-            for (int k = 0; k < kSK; k++)
-                if (k < I.K) {
+            for (int k = 0; k < K; k++) {
                     float nr = tr[k], ni = ti[k];
                     for (int q = 0; q < nf; q++) {
                         const int site = I.op.flip_sites[off + q];
@@ -321,7 +316,14 @@ __global__ void serve_kernel(SLaunch L) {
         const STask task = L.tasks[t];
         const SInst& I = L.inst[task.inst];
         if (task.kind == 0) {
-            walker_task(L, I, task.index, lane);
+            switch (I.K) {   // the hidden-unit counts per lane of rbm_lanes_k
+                case 1: walker_task<1>(L, I, task.index, lane); break;
+                case 2: walker_task<2>(L, I, task.index, lane); break;
+                case 4: walker_task<4>(L, I, task.index, lane); break;
+                case 8: walker_task<8>(L, I, task.index, lane); break;
+                case 13: walker_task<13>(L, I, task.index, lane); break;
+                default: walker_task<18>(L, I, task.index, lane); break;
+            }
         } else {
             reduce_task<R>(L, I, task.index, task.w0, lane);
         }
@@ -467,6 +469,11 @@ extern "C" int rbmg_batch_create(int n, const rbmg_psi* const* psis, const rbmg_
         if (!p || !o || walkers[i] == 0) return fail(RBMG_EINVAL, "batch: null instance or no walkers");
         if (p->kind != 0) return fail(RBMG_EUNSUPPORTED, "batch: complex RBM (Psi) instances only");
         if (p->Mpad / 32 > kSK) return fail(RBMG_EUNSUPPORTED, "batch: M <= 576");
+        {
+            const int K = p->Mpad / 32;
+            if (K != 1 && K != 2 && K != 4 && K != 8 && K != 13 && K != 18)
+                return fail(RBMG_EINVAL, "batch: unexpected hidden-unit padding");
+        }
         if (p->N > 64 * kSW) return fail(RBMG_EUNSUPPORTED, "batch: N <= 192");
         if (o->max_site >= p->N) return fail(RBMG_EINVAL, "batch: operator acts on a site >= N");
         const int nw = nwords_of(p->N);
