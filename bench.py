@@ -46,6 +46,9 @@ THERM_SWEEPS = 1000
 METRIC = "effective samples/s (ESS of E_loc) at N=100: learned-proposal MCMC (plain single-flip beside)"
 UNIT = "samples/s"
 L2_FLUSH_BYTES = 256 << 20
+# DRAM bytes of one sampler launch, dram__bytes_read.sum + dram__bytes_write.sum of an ncu
+# capture of rbm_mc_kernel<13,2> with these 16384 walkers (profiles/rbm_mc_kernel_n100_m400_w16384.md)
+SAMPLER_DRAM_BYTES = 1.059e6
 
 # algorithmic FP32 flops of the sampler, from the operation list of
 # rbmongpu_gb300/csrc/device_math.cuh and rbm_impl.cuh (FMA = 2, mul/add/div = 1)
@@ -514,7 +517,9 @@ def main():
         # current-state forward (spins_to_x + 3 GEMM layers) and the local-energy pass
         "gpu_launches": args.steps * (6 * L + 6),
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak if peak else None, "traffic": None,
+                     "frac": achieved / peak if peak else None, "traffic": SAMPLER_DRAM_BYTES,
+                     "traffic_source": "ncu dram__bytes_read + write of one launch (W and walker state are "
+                                       "read once per launch whatever its sweep count)",
                      "peak_source": "measured in this run by the library's FP32 FMA probe kernel",
                      "kernel": f"rbm_mc_kernel<13,2> (plain sampler, {S} sweeps per launch)",
                      "flops_per_launch": fl, "ms_per_launch": avg_launch * 1e3},
