@@ -10,9 +10,10 @@ PCG64(104); periodic 1D transverse-field Ising chain with h=1.0 (200 Pauli strin
   `--sweeps-per-row` sweeps of N proposals per walker, then the local energy of every
   walker;
 * learned: after the same thermalisation and `--train-steps` steps of online training
-  (REINFORCE + Adam on the first `--train-walkers` walkers' moves), the frozen proposal
-  network's cluster-flip Metropolis-Hastings steps; one row = `--learned-steps-per-row`
-  steps, then the local energy of every walker.
+  (cross-entropy to the locally balanced proposal + Adam on the first `--train-walkers`
+  walkers), the frozen proposal network's cluster-flip Metropolis-Hastings steps; one
+  row = `--learned-steps-per-row` steps (a row of about the plain row's duration), then
+  the local energy of every walker.
 
 The headline metric is effective samples per second of the learned chain: walkers x
 rows / tau_int(E_loc) per second of its timed rows, tau_int (in rows) from Sokal's
@@ -20,7 +21,10 @@ automatic windowing (c = 5) of the walkers' E_loc series; the plain chain's figu
 beside it ("plain"), with E_loc/s, the energy standard error per spin, and a flag where
 the window did not converge (tau_int is then a lower bound).
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--workload serving]
+
+`--workload serving` times the batched serving of 64 uneven RBMs instead (one line of
+its own).
 
 For N > 1 run under torchrun: every rank samples its own replica of the walker sets
 (Philox keys offset by rank), no data-path collective; value = all ranks' effective
@@ -46,8 +50,8 @@ THERM_SWEEPS = 1000
 METRIC = "effective samples/s (ESS of E_loc) at N=100: learned-proposal MCMC (plain single-flip beside)"
 UNIT = "samples/s"
 L2_FLUSH_BYTES = 256 << 20
-# DRAM bytes of one sampler launch, dram__bytes_read.sum + dram__bytes_write.sum of an ncu
-# capture of rbm_mc_kernel<13,2> with these 16384 walkers (profiles/rbm_mc_kernel_n100_m400_w16384.md)
+# DRAM bytes of one sampler launch: dram__bytes_read.sum + dram__bytes_write.sum of an ncu
+# capture of rbm_mc_kernel<13,2> on these 16384 walkers
 SAMPLER_DRAM_BYTES = 1.059e6
 
 # algorithmic FP32 flops of the sampler, from the operation list of
@@ -190,6 +194,24 @@ def cpu_chains(steps, seconds_per_step, workers, tmpdir):
     return np.concatenate(series, axis=0), wall, sweeps
 
 
+# --------------------------------------------------------------------- ranks
+def combine_ranks(tot, tmax, device):
+    """Whole-job figures of independent replicas: sums of `tot` (effective samples,
+    samples) and maxima of `tmax` (seconds) over the ranks of the default process group."""
+    import torch
+    t1 = torch.tensor(np.asarray(tot, np.float64), device=device)
+    t2 = torch.tensor(np.asarray(tmax, np.float64), device=device)
+    torch.distributed.all_reduce(t1, op=torch.distributed.ReduceOp.SUM)
+    torch.distributed.all_reduce(t2, op=torch.distributed.ReduceOp.MAX)
+    return t1.cpu().numpy(), t2.cpu().numpy()
+
+
+def replica_seeds(rank):
+    """Philox keys of the rank's plain chain, learned chain and proposal network: every rank
+    samples its own replica of the walker sets."""
+    return 1000 + rank, 3000 + rank, 2000 + rank
+
+
 # --------------------------------------------------------------------- GPU arms
 def run_gpu(args, rank, world, local_rank):
     import torch
@@ -232,7 +254,8 @@ def run_gpu(args, rank, world, local_rank):
 
     clocks = ClockSampler(local_rank)
     # ---- plain single-flip chain
-    plain = rg.Chain(psi, B, seed=1000 + rank)
+    seed_plain, seed_learned, seed_net = replica_seeds(rank)
+    plain = rg.Chain(psi, B, seed=seed_plain)
     with torch.cuda.stream(stream):
         plain.sweep_async(psi, None, THERM_SWEEPS, 1, 0, sp)
         for _ in range(Wm):
@@ -248,8 +271,8 @@ def run_gpu(args, rank, world, local_rank):
     plain_accept = (a1 - a0) / max(p1 - p0, 1)
 
     # ---- learned-proposal chain
-    prop = rg.Proposal(N_SPINS, seed=2000 + rank, lr=1e-3)
-    lc = rg.Chain(psi, B, seed=3000 + rank)
+    prop = rg.Proposal(N_SPINS, seed=seed_net, lr=1e-3)
+    lc = rg.Chain(psi, B, seed=seed_learned)
     with torch.cuda.stream(stream):
         lc.sweep_async(psi, None, THERM_SWEEPS, 1, 0, sp)
     sync()
@@ -303,11 +326,7 @@ def run_gpu(args, rank, world, local_rank):
                     learned_series.size, plain_series.size], np.float64)
     tmax = np.array([learned_stats["seconds"], plain_stats["seconds"], e2e_s], np.float64)
     if world > 1:
-        t1 = torch.tensor(tot, device="cuda")
-        t2 = torch.tensor(tmax, device="cuda")
-        torch.distributed.all_reduce(t1, op=torch.distributed.ReduceOp.SUM)
-        torch.distributed.all_reduce(t2, op=torch.distributed.ReduceOp.MAX)
-        tot, tmax = t1.cpu().numpy(), t2.cpu().numpy()
+        tot, tmax = combine_ranks(tot, tmax, "cuda")
     return dict(tot=tot, tmax=tmax, plain=plain_stats, learned=learned_stats, plain_ms=plain_ms,
                 learned_ms=learned_ms, kernel_ms=kernel_ms, plain_accept=plain_accept, learned_accept=learned_accept,
                 train_s=train_s, e2e_K=e2e_K, h2d=h2d, d2h=d2h, clocks=clk, fp32_peak=fp32_peak)
