@@ -206,6 +206,12 @@ RBMG_API int rbmg_chain_destroy(rbmg_chain* chain);
 RBMG_API int rbmg_chain_sweep_async(rbmg_chain* chain, const rbmg_psi* psi, const rbmg_operator* op, int n_sweeps,
                                     int measure_every, void* d_eloc_out, void* stream);
 /* host copies of the walkers' configurations [num_walkers * nwords] and acceptance counters */
+/* walker checkpoint (the reference checkpoints no chain state): spins [walkers][ceil(N/64)],
+ * next Philox word, accept and proposal counters [walkers]; restoring continues bit for bit */
+RBMG_API int rbmg_chain_get_checkpoint(const rbmg_chain* chain, uint64_t* spins, uint64_t* rng_index,
+                                       uint64_t* accepts, uint64_t* proposals);
+RBMG_API int rbmg_chain_set_checkpoint(rbmg_chain* chain, const uint64_t* spins, const uint64_t* rng_index,
+                                       const uint64_t* accepts, const uint64_t* proposals);
 RBMG_API int rbmg_chain_state(const rbmg_chain* chain, uint64_t* spins, uint64_t* accepts, uint64_t* proposals);
 /* the library's CUDA stream of the calling thread, as a cudaStream_t */
 RBMG_API int rbmg_stream(void** stream);
@@ -250,6 +256,10 @@ RBMG_API int rbmg_proposal_adam(rbmg_proposal* proposal, const float* grads);
 #define RBMG_PROPOSAL_LOCALLY_BALANCED 0
 #define RBMG_PROPOSAL_REINFORCE 1
 RBMG_API int rbmg_proposal_set_objective(rbmg_proposal* proposal, int objective);
+/* training state for checkpoints: FP32 parameters, Adam moments [num_params] each, Adam steps */
+RBMG_API int rbmg_proposal_get_state(const rbmg_proposal* proposal, float* params, float* m, float* v, int64_t* steps);
+RBMG_API int rbmg_proposal_set_state(rbmg_proposal* proposal, const float* params, const float* m, const float* v,
+                                     int64_t steps);
 /* n_steps learned Metropolis-Hastings steps of every walker of the chain.  train = 0 keeps
  * the weights (the chain is then exactly |psi|^2-stationary); train > 0 follows every step
  * with one update (objective of rbmg_proposal_set_objective) + Adam step on the first

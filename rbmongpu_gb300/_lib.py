@@ -87,6 +87,11 @@ SIGNATURES = {
     "rbmg_proposal_eval": [_vp, C.c_int, _u64p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float)],
     "rbmg_proposal_adam": [_vp, C.POINTER(C.c_float)],
     "rbmg_proposal_set_objective": [_vp, C.c_int],
+    "rbmg_proposal_get_state": [_vp, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                C.POINTER(C.c_int64)],
+    "rbmg_proposal_set_state": [_vp, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int64],
+    "rbmg_chain_get_checkpoint": [_vp, _u64p, _u64p, _u64p, _u64p],
+    "rbmg_chain_set_checkpoint": [_vp, _u64p, _u64p, _u64p, _u64p],
     "rbmg_batch_create": [C.c_int, _vpp, _vpp, C.POINTER(C.c_uint32), _u64p, _vpp],
     "rbmg_batch_destroy": [_vp],
     "rbmg_batch_run": [_vp, C.c_int, C.c_int],

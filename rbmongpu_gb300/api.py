@@ -611,6 +611,27 @@ class Chain:
              proposal._h, int(n_steps), int(train), int(measure_every), C.c_void_p(d_eloc) if d_eloc else None,
              C.c_void_p(stream) if stream else None)
 
+    def checkpoint(self):
+        """{spins, rng_index, accepts, proposals}: restoring it continues the chains bit for bit."""
+        B = self.num_walkers
+        d = dict(spins=np.zeros((B, nwords(self.N)), np.uint64), rng_index=np.zeros(B, np.uint64),
+                 accepts=np.zeros(B, np.uint64), proposals=np.zeros(B, np.uint64))
+        call("rbmg_chain_get_checkpoint", self._h, *[_p(d[k], _u64p) for k in ("spins", "rng_index", "accepts",
+                                                                              "proposals")])
+        return d
+
+    def restore(self, ckpt):
+        d = {k: np.ascontiguousarray(ckpt[k], np.uint64) for k in ("spins", "rng_index", "accepts", "proposals")}
+        call("rbmg_chain_set_checkpoint", self._h, *[_p(d[k], _u64p) for k in ("spins", "rng_index", "accepts",
+                                                                              "proposals")])
+
+    def save(self, path):
+        np.savez(path, **self.checkpoint())
+
+    def load(self, path):
+        with np.load(path) as f:
+            self.restore({k: f[k] for k in f.files})
+
     def state(self):
         sp = np.zeros((self.num_walkers, nwords(self.N)), np.uint64)
         a, p = C.c_uint64(), C.c_uint64()
@@ -679,6 +700,23 @@ class Proposal:
         grads = np.zeros(self.num_params, np.float32)
         call("rbmg_proposal_eval", self._h, count, _p(sp, _u64p), _p(dl, fp), _p(logits, fp), _p(grads, fp))
         return logits, grads
+
+    def checkpoint(self):
+        """{params, m, v, steps}: the network and its Adam state."""
+        fp = C.POINTER(C.c_float)
+        d = dict(params=np.zeros(self.num_params, np.float32), m=np.zeros(self.num_params, np.float32),
+                 v=np.zeros(self.num_params, np.float32))
+        steps = C.c_int64()
+        call("rbmg_proposal_get_state", self._h, _p(d["params"], fp), _p(d["m"], fp), _p(d["v"], fp),
+             C.byref(steps))
+        d["steps"] = steps.value
+        return d
+
+    def restore(self, ckpt):
+        fp = C.POINTER(C.c_float)
+        arr = {k: np.ascontiguousarray(ckpt[k], np.float32) for k in ("params", "m", "v")}
+        call("rbmg_proposal_set_state", self._h, _p(arr["params"], fp), _p(arr["m"], fp), _p(arr["v"], fp),
+             int(ckpt["steps"]))
 
     def adam(self, grads):
         """One Adam step (betas 0.9 / 0.999, eps 1e-8) with the given gradient."""

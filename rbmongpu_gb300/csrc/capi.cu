@@ -1505,6 +1505,37 @@ extern "C" int rbmg_chain_sweep_async(rbmg_chain* c, const rbmg_psi* psi, const 
     return RBMG_OK;
 }
 
+// checkpoint of the walkers: spins [walkers][nw], next Philox word [walkers], accept and
+// proposal counters [walkers]; restoring it continues the chains bit for bit
+extern "C" int rbmg_chain_get_checkpoint(const rbmg_chain* c, uint64_t* spins, uint64_t* rng_index, uint64_t* accepts,
+                                         uint64_t* proposals) {
+    if (!c || !spins || !rng_index || !accepts || !proposals) return fail(RBMG_EINVAL, "chain checkpoint: null");
+    if (!c->initialised) return fail(RBMG_EINVAL, "chain checkpoint: the chain has not started");
+    RBMG_CK(cudaDeviceSynchronize());
+    const size_t B = c->walkers;
+    RBMG_CK(cudaMemcpy(spins, c->spins.p, sizeof(uint64_t) * c->nw * B, cudaMemcpyDeviceToHost));
+    RBMG_CK(cudaMemcpy(rng_index, c->rng_index.p, sizeof(uint64_t) * B, cudaMemcpyDeviceToHost));
+    RBMG_CK(cudaMemcpy(accepts, c->accepts.p, sizeof(uint64_t) * B, cudaMemcpyDeviceToHost));
+    RBMG_CK(cudaMemcpy(proposals, c->proposals.p, sizeof(uint64_t) * B, cudaMemcpyDeviceToHost));
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_chain_set_checkpoint(rbmg_chain* c, const uint64_t* spins, const uint64_t* rng_index,
+                                         const uint64_t* accepts, const uint64_t* proposals) {
+    if (!c || !spins || !rng_index || !accepts || !proposals) return fail(RBMG_EINVAL, "chain checkpoint: null");
+    const size_t B = c->walkers;
+    for (size_t w = 0; w < B; w++)
+        if (c->N % 64 && (spins[w * c->nw + c->nw - 1] >> (c->N % 64)))
+            return fail(RBMG_EINVAL, "chain checkpoint: spin bits beyond N");
+    RBMG_CK(cudaDeviceSynchronize());
+    RBMG_CK(cudaMemcpy(c->spins.p, spins, sizeof(uint64_t) * c->nw * B, cudaMemcpyHostToDevice));
+    RBMG_CK(cudaMemcpy(c->rng_index.p, rng_index, sizeof(uint64_t) * B, cudaMemcpyHostToDevice));
+    RBMG_CK(cudaMemcpy(c->accepts.p, accepts, sizeof(uint64_t) * B, cudaMemcpyHostToDevice));
+    RBMG_CK(cudaMemcpy(c->proposals.p, proposals, sizeof(uint64_t) * B, cudaMemcpyHostToDevice));
+    c->initialised = true;
+    return RBMG_OK;
+}
+
 extern "C" int rbmg_chain_state(const rbmg_chain* c, uint64_t* spins, uint64_t* accepts, uint64_t* proposals) {
     if (!c) return fail(RBMG_EINVAL, "chain state: null");
     RBMG_CK(cudaDeviceSynchronize());

@@ -1271,6 +1271,33 @@ extern "C" int rbmg_proposal_adam(rbmg_proposal* p, const float* grads) {
     return RBMG_OK;
 }
 
+// training state: FP32 parameters, Adam moments (each [num_params]) and the Adam step count
+extern "C" int rbmg_proposal_get_state(const rbmg_proposal* p, float* params, float* m, float* v, int64_t* steps) {
+    if (!p || !params || !m || !v || !steps) return fail(RBMG_EINVAL, "proposal state: null");
+    RBMG_CK(cudaDeviceSynchronize());
+    RBMG_CK(cudaMemcpy(params, p->master.p, sizeof(float) * p->P, cudaMemcpyDeviceToHost));
+    RBMG_CK(cudaMemcpy(m, p->adam_m.p, sizeof(float) * p->P, cudaMemcpyDeviceToHost));
+    RBMG_CK(cudaMemcpy(v, p->adam_v.p, sizeof(float) * p->P, cudaMemcpyDeviceToHost));
+    *steps = p->steps;
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_proposal_set_state(rbmg_proposal* p, const float* params, const float* m, const float* v,
+                                       int64_t steps) {
+    if (!p || !params || !m || !v || steps < 0) return fail(RBMG_EINVAL, "proposal state: bad arguments");
+    for (int64_t t = 0; t < p->P; t++)
+        if (!std::isfinite(params[t]) || !std::isfinite(m[t]) || !(v[t] >= 0.0f))
+            return fail(RBMG_ENAN, "proposal state: non-finite entry or negative second moment");
+    RBMG_CK(cudaDeviceSynchronize());
+    RBMG_CK(cudaMemcpy(p->master.p, params, sizeof(float) * p->P, cudaMemcpyHostToDevice));
+    RBMG_CK(cudaMemcpy(p->adam_m.p, m, sizeof(float) * p->P, cudaMemcpyHostToDevice));
+    RBMG_CK(cudaMemcpy(p->adam_v.p, v, sizeof(float) * p->P, cudaMemcpyHostToDevice));
+    p->steps = steps;
+    RBMG_CK(proposal_refresh_bf16(p, stream()));
+    RBMG_CK(cudaStreamSynchronize(stream()));
+    return RBMG_OK;
+}
+
 extern "C" int rbmg_proposal_set_objective(rbmg_proposal* p, int objective) {
     if (!p) return fail(RBMG_EINVAL, "proposal: null");
     if (objective != RBMG_PROPOSAL_LOCALLY_BALANCED && objective != RBMG_PROPOSAL_REINFORCE)
