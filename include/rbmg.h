@@ -248,6 +248,9 @@ RBMG_API int rbmg_proposal_set_params(rbmg_proposal* proposal, const float* para
  * the backward pass -> grads [num_params] (host buffers; a test hook of the kernels) */
 RBMG_API int rbmg_proposal_eval(rbmg_proposal* proposal, int count, const uint64_t* spins, const float* dlogits,
                                 float* logits, float* grads);
+/* waits for the device and reports RBMG_ETIMEOUT (once) if a tensor-core pass of the
+ * network gave up waiting for its MMAs since the last call */
+RBMG_API int rbmg_proposal_status(rbmg_proposal* proposal);
 /* one Adam step (lr of the proposal, beta 0.9 / 0.999, eps 1e-8) with the given gradient */
 RBMG_API int rbmg_proposal_adam(rbmg_proposal* proposal, const float* grads);
 /* training objective of rbmg_chain_learned_async: cross-entropy to the locally balanced

@@ -87,6 +87,7 @@ SIGNATURES = {
     "rbmg_proposal_eval": [_vp, C.c_int, _u64p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float)],
     "rbmg_proposal_adam": [_vp, C.POINTER(C.c_float)],
     "rbmg_proposal_set_objective": [_vp, C.c_int],
+    "rbmg_proposal_status": [_vp],
     "rbmg_proposal_get_state": [_vp, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
                                 C.POINTER(C.c_int64)],
     "rbmg_proposal_set_state": [_vp, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int64],

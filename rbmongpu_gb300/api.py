@@ -718,6 +718,10 @@ class Proposal:
         call("rbmg_proposal_set_state", self._h, _p(arr["params"], fp), _p(arr["m"], fp), _p(arr["v"], fp),
              int(ckpt["steps"]))
 
+    def status(self):
+        """Waits for the device; raises if a tensor-core pass of the network timed out."""
+        call("rbmg_proposal_status", self._h)
+
     def adam(self, grads):
         """One Adam step (betas 0.9 / 0.999, eps 1e-8) with the given gradient."""
         g = np.ascontiguousarray(grads, np.float32)

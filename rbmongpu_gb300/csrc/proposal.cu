@@ -308,6 +308,7 @@ struct rbmg_proposal {
     // transposed bf16 copies for the fused inference kernel: [H][ldw1], [H][H], [w3_rows][H]
     rbmg::DevBuf w1t, w2t, w3t;
     int ldw1 = 0, w3_rows = 0;
+    rbmg::DevBuf tc_error;              // set by the tensor-core kernel when a bounded wait gives up
     int cap = 0;                        // activation rows held
     rbmg::DevBuf x16, z1, h1, z2, h2;   // [cap][Np] bf16, [cap][H] f32 / bf16
     rbmg::DevBuf logits;                // [cap][O] f32 (training forward)
@@ -597,6 +598,53 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) learned_angles_kernel(Rbm
         L.theta[o] = make_float2(tr[k], ti[k]);
         L.re[o] = lc_re(tr[k], ti[k]);
     }
+}
+
+// the move of every walker drawn from the logits of its current state (warp per walker)
+template <int NW>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock) learned_draw_kernel(LearnedLaunch L) {
+    const int lane = threadIdx.x & 31;
+    const int w = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+    if (w >= L.B) return;
+    WalkerRng rng;
+    rng.init(L.seed, static_cast<uint32_t>(w), L.rng_index[w]);
+    const float* row = L.logits_cur + static_cast<long>(w) * L.O;
+    const LogNorm ln = log_norms(row, L.N, lane);
+    const int i = draw_index(row, L.N, ln.seed, rng.uniform(), lane);
+    const int l = 1 + draw_index(row + L.N, kLengths, ln.len, rng.uniform(), lane);
+    if (lane == 0) {
+        Spins<NW> s;
+#pragma unroll
+        for (int k = 0; k < NW; k++) s.w[k] = L.spins[static_cast<long>(w) * NW + k];
+        if (L.spins_pre) {
+#pragma unroll
+            for (int k = 0; k < NW; k++) L.spins_pre[static_cast<long>(w) * NW + k] = s.w[k];
+        }
+        for (int q = 0; q < l; q++) {
+            int c = i + q;
+            if (c >= L.N) c -= L.N;
+            s.flip(c);
+        }
+#pragma unroll
+        for (int k = 0; k < NW; k++) L.spins_prop[static_cast<long>(w) * NW + k] = s.w[k];
+        L.site[w] = i;
+        L.len[w] = l;
+        L.logq_fwd[w] = (row[i] - ln.seed) + (row[L.N + l - 1] - ln.len);
+        L.rng_index[w] = rng.index;
+        L.proposals[w] += 1;
+    }
+}
+
+cudaError_t launch_draw(const LearnedLaunch& L, cudaStream_t st) {
+    const dim3 grid((L.B + kWarpsPerBlock - 1) / kWarpsPerBlock), block(32 * kWarpsPerBlock);
+    switch (nwords_of(L.N)) {
+        case 1: learned_draw_kernel<1><<<grid, block, 0, st>>>(L); break;
+        case 2: learned_draw_kernel<2><<<grid, block, 0, st>>>(L); break;
+        case 3: learned_draw_kernel<3><<<grid, block, 0, st>>>(L); break;
+        case 4: learned_draw_kernel<4><<<grid, block, 0, st>>>(L); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
 }
 
 // Metropolis-Hastings test of the proposed cluster flip:
@@ -891,6 +939,19 @@ cudaError_t launch_lb_target(const RbmDev& P, int n, const uint64_t* spins, cons
     }
 }
 
+// tensor-core (tcgen05) inference, mlp_tc.cu
+struct TcNet {
+    int N, O, ldw1;
+    const bf16* w1t;
+    const bf16* w2t;
+    const bf16* w3t;
+    const float* b1;
+    const float* b2;
+    const float* b3;
+};
+cudaError_t launch_mlp_tc(const TcNet& net, int nw, const uint64_t* spins, int count, float* out, int* error,
+                          cudaStream_t st);
+
 // ============================================================================ fused inference
 // One CTA runs the whole network for 128 configurations with the activations in shared
 // memory: x [128][<=256] -> h1 -> h2 -> logits.  The weights stream through a 4-stage
@@ -1128,6 +1189,11 @@ cudaError_t launch_fused(const rbmg_proposal* p, const LearnedLaunch& L, const u
                          cudaStream_t st) {
     if (count <= 0) return cudaSuccess;
     const FusedNet net = fused_net(p);
+    if (!PROPOSE && p->O <= 128) {
+        // tcgen05 / TMEM path (one output pass of 128): every logits row of the chain comes from it
+        const TcNet tn{net.N, net.O, net.ldw1, net.w1t, net.w2t, net.w3t, net.b1, net.b2, net.b3};
+        return launch_mlp_tc(tn, nwords_of(p->N), in, count, out, p->tc_error.as<int>(), st);
+    }
     switch (nwords_of(p->N)) {
         case 1: return launch_fused_nw<1, PROPOSE>(net, L, in, count, out, st);
         case 2: return launch_fused_nw<2, PROPOSE>(net, L, in, count, out, st);
@@ -1194,6 +1260,8 @@ extern "C" int rbmg_proposal_create(int N, uint64_t seed, float lr, rbmg_proposa
     RBMG_CK(p->w1t.ensure(sizeof(bf16) * static_cast<size_t>(H) * p->ldw1));
     RBMG_CK(p->w2t.ensure(sizeof(bf16) * static_cast<size_t>(H) * H));
     RBMG_CK(p->w3t.ensure(sizeof(bf16) * static_cast<size_t>(p->w3_rows) * H));
+    RBMG_CK(p->tc_error.ensure(sizeof(int)));
+    RBMG_CK(cudaMemset(p->tc_error.p, 0, sizeof(int)));
     RBMG_CK(cudaMemcpy(p->master.p, h.data(), sizeof(float) * p->P, cudaMemcpyHostToDevice));
     RBMG_CK(cudaMemset(p->adam_m.p, 0, sizeof(float) * p->P));
     RBMG_CK(cudaMemset(p->adam_v.p, 0, sizeof(float) * p->P));
@@ -1233,6 +1301,18 @@ extern "C" int rbmg_proposal_set_params(rbmg_proposal* p, const float* params) {
     return RBMG_OK;
 }
 
+extern "C" int rbmg_proposal_status(rbmg_proposal* p) {
+    if (!p) return fail(RBMG_EINVAL, "proposal status: null");
+    int err = 0;
+    RBMG_CK(cudaDeviceSynchronize());
+    RBMG_CK(cudaMemcpy(&err, p->tc_error.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) {
+        RBMG_CK(cudaMemset(p->tc_error.p, 0, sizeof(int)));
+        return fail(RBMG_ETIMEOUT, "proposal: a tensor-core pass gave up waiting for its MMAs");
+    }
+    return RBMG_OK;
+}
+
 extern "C" int rbmg_proposal_eval(rbmg_proposal* p, int count, const uint64_t* spins, const float* dlogits,
                                   float* logits, float* grads) {
     if (!p || count <= 0 || !spins || !logits) return fail(RBMG_EINVAL, "proposal eval: bad arguments");
@@ -1250,6 +1330,8 @@ extern "C" int rbmg_proposal_eval(rbmg_proposal* p, int count, const uint64_t* s
     } else {
         RBMG_CK(launch_fused<false>(p, LearnedLaunch{}, dsp.as<uint64_t>(), count, dlog.as<float>(), st));
     }
+    r = rbmg_proposal_status(p);
+    if (r != RBMG_OK) return r;
     RBMG_CK(cudaMemcpyAsync(logits, dlog.p, sizeof(float) * count * p->O, cudaMemcpyDeviceToHost, st));
     if (dlogits) {
         RBMG_CK(cudaMemcpyAsync(p->dl32.p, dlogits, sizeof(float) * count * p->O, cudaMemcpyHostToDevice, st));
@@ -1386,8 +1468,15 @@ extern "C" int rbmg_chain_learned_async(rbmg_chain* c, const rbmg_psi* psi, cons
         // frozen network: the accept kernel draws the next move, so the later steps only
         // evaluate the network on the proposed configurations; while training, the weights
         // change after every step and each step draws its move from the new logits
-        if (nt == 0 && step > 0) RBMG_CK(launch_fused<false>(prop, L, L.spins_prop, B, S->logits_prop.as<float>(), st));
-        else RBMG_CK(launch_fused<true>(prop, L, nullptr, B, S->logits_prop.as<float>(), st));
+        if (nt == 0 && step > 0) {
+            RBMG_CK(launch_fused<false>(prop, L, L.spins_prop, B, S->logits_prop.as<float>(), st));
+        } else if (prop->O <= 128) {
+            // the tensor-core path evaluates every logits row, so the draw is its own pass
+            RBMG_CK(launch_draw(L, st));
+            RBMG_CK(launch_fused<false>(prop, L, L.spins_prop, B, S->logits_prop.as<float>(), st));
+        } else {
+            RBMG_CK(launch_fused<true>(prop, L, nullptr, B, S->logits_prop.as<float>(), st));
+        }
         L.propose_next = nt == 0 && step + 1 < n_steps ? 1 : 0;
         RBMG_CK(launch_learned(1, P, L, st));
         if (nt > 0 && prop->objective == RBMG_PROPOSAL_LOCALLY_BALANCED) {

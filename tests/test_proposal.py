@@ -63,8 +63,10 @@ def rel_err(a, b):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("N,count", [(20, 333), (100, 1000)])
+@pytest.mark.parametrize("N,count", [(20, 333), (100, 1000), (128, 300)])
 def test_forward_and_backward_match_restatement(N, count):
+    """eval without dlogits runs the inference kernel (tcgen05 for N + 8 <= 128, the fused
+    mma.sync kernel above), with dlogits the layer-by-layer GEMMs and the backward pass."""
     import rbmongpu_gb300 as rg
     prop = rg.Proposal(N, seed=5)
     params = random_params(N, 17 + N)
@@ -80,7 +82,14 @@ def test_forward_and_backward_match_restatement(N, count):
     for name, (o, s) in lay.items():
         n = int(np.prod(s))
         assert rel_err(grads[o:o + n], ref_g[o:o + n]) < 1e-2, name
-    np.testing.assert_array_equal(prop.eval(words), logits)   # forward alone, deterministic
+    inf = prop.eval(words)
+    if N + 8 > 128:
+        np.testing.assert_array_equal(inf, logits)   # same k order and epilogue as the GEMMs
+    else:
+        assert rel_err(inf, ref_logits) < 3e-3       # tensor-core accumulation order differs
+        assert rel_err(inf, logits) < 3e-3
+    np.testing.assert_array_equal(prop.eval(words), inf)   # deterministic
+    prop.status()
 
 
 @pytest.mark.gpu
@@ -170,6 +179,7 @@ def test_learned_chain_samples_psi_squared():
     chain = rg.Chain(psi, B, seed=77)
     chain.learned_async(psi, None, prop, EXACT_STEPS, train=0)
     words, acc, props = chain.state()
+    prop.status()
     assert props == EXACT_STEPS * B and 0.05 < acc / props < 1
     chi2, dof = chi_square(p, words[:, 0], B)
     assert dof > 100 and chi_square_ok(chi2, dof), (chi2, dof)
