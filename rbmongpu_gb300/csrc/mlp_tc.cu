@@ -1,15 +1,17 @@
 // Proposal-network inference on the 5th-generation tensor cores (tcgen05, TMEM).
 //
-// One CTA (4 warps) evaluates the network N -> 256 -> 256 (SiLU) -> N+8 for 128
+// One CTA (16 warps) evaluates the network N -> 256 -> 256 (SiLU) -> N+8 for 128
 // configurations.  Per layer the activations (A, 128 x K) and the layer's transposed
 // weights (B, n x K) sit in shared memory in the canonical K-major layout without swizzle
 // (8-row x 16-byte core matrices, 128 contiguous bytes each); one elected thread issues
 // K/16 tcgen05.mma (kind::f16, BF16 operands, FP32 accumulation, M = 128) into a
 // 256-column TMEM accumulator (of 512 allocated), and tcgen05.commit arrives on an
-// mbarrier when they are done.  Each thread then reads its row of the accumulator with
-// tcgen05.ld, adds the bias, applies SiLU and writes the BF16 result as the next layer's A
-// operand.  The waits on the mbarrier are bounded: on timeout the kernel raises an error
-// flag, waits (bounded) for its MMAs, frees its TMEM and returns.
+// mbarrier when they are done.  The next layer's weights are then copied into B while the
+// epilogue runs: warp w reads TMEM lanes 32 (w % 4) .. +31 (its rows) and a quarter of the
+// columns with tcgen05.ld, adds the bias, applies SiLU and writes the BF16 result as the
+// next layer's A operand.  The logits are staged in shared memory and written out
+// row-contiguous.  The waits on the mbarrier are bounded: on timeout the kernel raises an
+// error flag, waits (bounded) for its MMAs, frees its TMEM and returns.
 #include <cuda_bf16.h>
 
 #include "host.h"
@@ -22,17 +24,20 @@ using bf16 = __nv_bfloat16;
 namespace {
 
 constexpr int kTcRows = 128;               // configurations per CTA (the MMA's M)
-constexpr int kTcThreads = 128;            // one thread per row
+constexpr int kTcThreads = 512;            // 16 warps: 4 TMEM lane quarters x 4 column groups
 constexpr int kTcHidden = 256;
 // TMEM columns allocated: the accumulator uses 256 (FP32, 128 x 256); the whole 512 are
 // held (one CTA per SM by its shared memory) so no MMA shape can reach unallocated columns
 constexpr int kTcCols = 512;
 constexpr uint32_t kTcSpin = 1u << 24;     // mbarrier polls before giving up
 
-// shared memory: A [128 x 256] bf16 = 64 KB, B [256 x 256] bf16 = 128 KB, barrier + slot
+// shared memory: A [128 x 256] bf16 = 64 KB, B [256 x 256] bf16 = 128 KB (after the last
+// MMA it holds the FP32 logits, [128][O + 1]), biases (256 + 256 + 128 floats), barrier + slot
 constexpr size_t kTcA = size_t(kTcRows) * kTcHidden * 2;
 constexpr size_t kTcB = size_t(kTcHidden) * kTcHidden * 2;
-constexpr size_t kTcSmem = kTcA + kTcB + 64;
+constexpr size_t kTcBias = (2 * kTcHidden + kTcRows) * sizeof(float);
+constexpr size_t kTcSmem = kTcA + kTcB + kTcBias + 64;
+static_assert(size_t(kTcRows) * (kTcRows + 1) * sizeof(float) <= kTcB, "logit staging fits in B");
 
 // byte offset of element (row, col) of a K-major operand with `rows` rows in the canonical
 // no-swizzle layout, one block per MMA K step of 16 columns: within the block of step
@@ -114,18 +119,30 @@ __device__ __forceinline__ void cp16(uint32_t saddr, const void* g) {
 
 // B <- rows [0, n) of Wt [n][ldw] (k contiguous), k < K, in the canonical layout with n rows
 __device__ __forceinline__ void load_weights(uint32_t sB, const bf16* Wt, int ldw, int n, int K) {
-    const int chunks = n * (K / 8);
+    const int kc = K / 8, chunks = n * kc;
     for (int c = threadIdx.x; c < chunks; c += kTcThreads) {
-        const int row = c / (K / 8), kb = c % (K / 8);
+        const int row = c / kc, kb = c - row * kc;
         cp16(sB + kmajor_offset(row, kb * 8, n), Wt + static_cast<long>(row) * ldw + kb * 8);
     }
     asm volatile("cp.async.commit_group;\n" ::);
 }
 
-// the SiLU of the layer-by-layer path: hardware exponential and division, then BF16
-__device__ __forceinline__ bf16 tc_silu(float acc, float b) {
-    const float z = acc + b;
-    return __float2bfloat16_rn(__fdividef(z, 1.0f + __expf(-z)));
+__device__ __forceinline__ float tanh_hw(float x) {
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// SiLU(z) = z sigmoid(z) = h + h tanh(h) with h = z / 2: one hardware tanh per element;
+// the result is rounded to BF16, coarser than the tanh's own error
+__device__ __forceinline__ float tc_silu(float z) {
+    const float h = 0.5f * z;
+    return fmaf(h, tanh_hw(h), h);
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t*>(&v);
 }
 
 }  // namespace
@@ -146,11 +163,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) mlp_tc_kernel(TcNet net, const 
     extern __shared__ __align__(1024) unsigned char tsm[];
     unsigned char* sA = tsm;
     unsigned char* sB = tsm + kTcA;
-    uint64_t* mbar = reinterpret_cast<uint64_t*>(tsm + kTcA + kTcB);
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(tsm + kTcA + kTcB + 16);
-    const int tid = threadIdx.x, warp = tid >> 5;
+    float* sBias = reinterpret_cast<float*>(tsm + kTcA + kTcB);   // b1 | b2 | b3
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(tsm + kTcA + kTcB + kTcBias);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(tsm + kTcA + kTcB + kTcBias + 16);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int quarter = warp & 3, cgroup = warp >> 2;
     const int row0 = blockIdx.x * kTcRows;
+    const int rows = min(kTcRows, count - row0);
     const uint32_t aA = saddr_of(sA), aB = saddr_of(sB), aM = saddr_of(mbar);
+    // ---- layer-1 weights start streaming in at once
+    load_weights(aB, net.w1t, net.ldw1, kTcHidden, net.ldw1);
     // ---- TMEM (warp 0) and the mbarrier (thread 0)
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(saddr_of(tslot)),
@@ -161,39 +183,52 @@ __global__ void __launch_bounds__(kTcThreads, 1) mlp_tc_kernel(TcNet net, const 
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(aM));
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
+    for (int j = tid; j < 2 * kTcHidden + kTcRows; j += kTcThreads) {
+        float b = 0.0f;
+        if (j < kTcHidden) b = net.b1[j];
+        else if (j < 2 * kTcHidden) b = net.b2[j - kTcHidden];
+        else if (j - 2 * kTcHidden < net.O) b = net.b3[j - 2 * kTcHidden];
+        sBias[j] = b;
+    }
+    // ---- layer-1 input: row r = configuration row0 + r, +-1 spins, zero beyond N
+    {
+        const int kc = net.ldw1 / 8;
+        for (int c = tid; c < kTcRows * kc; c += kTcThreads) {
+            const int r = c % kTcRows, col = (c / kTcRows) * 8;
+            const bool live = r < rows;
+            uint32_t pk[4];
+#pragma unroll
+            for (int e = 0; e < 8; e += 2) {
+                float x[2];
+#pragma unroll
+                for (int u = 0; u < 2; u++) {
+                    const int i = col + e + u;
+                    x[u] = 0.0f;
+                    if (live && i < net.N) {
+                        const uint64_t word = spins[static_cast<long>(row0 + r) * NW + (i >> 6)];
+                        x[u] = ((word >> (i & 63)) & 1ull) ? 1.0f : -1.0f;
+                    }
+                }
+                pk[e / 2] = pack_bf16(x[0], x[1]);
+            }
+            *reinterpret_cast<uint4*>(sA + kmajor_offset(r, col, kTcRows)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+        }
+    }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
     const uint32_t tmem = *tslot;
-    // ---- layer-1 input: row tid = configuration row0 + tid, +-1 spins, zero beyond N
-    {
-        const int w = row0 + tid;
-        uint64_t s[NW];
-#pragma unroll
-        for (int k = 0; k < NW; k++) s[k] = w < count ? spins[static_cast<long>(w) * NW + k] : 0ull;
-        for (int c = 0; c < net.ldw1; c += 8) {
-            __align__(16) bf16 v[8];
-#pragma unroll
-            for (int e = 0; e < 8; e++) {
-                const int i = c + e;
-                float x = 0.0f;
-                if (w < count && i < net.N) x = ((s[i >> 6] >> (i & 63)) & 1ull) ? 1.0f : -1.0f;
-                v[e] = __float2bfloat16_rn(x);
-            }
-            *reinterpret_cast<uint4*>(sA + kmajor_offset(tid, c, kTcRows)) = *reinterpret_cast<const uint4*>(v);
-        }
-    }
     bool ok = true;
     uint32_t phase = 0;
-    const uint32_t lane_base = static_cast<uint32_t>(warp * 32) << 16;
+    const int r = quarter * 32 + lane;                                  // this thread's row (TMEM lane)
+    const uint32_t lane_base = static_cast<uint32_t>(quarter * 32) << 16;
     for (int layer = 0; layer < 3; layer++) {
         const int K = layer == 0 ? net.ldw1 : kTcHidden;
-        const int n = layer == 2 ? 128 : kTcHidden;
-        const bf16* Wt = layer == 0 ? net.w1t : (layer == 1 ? net.w2t : net.w3t);
-        const int ldw = layer == 0 ? net.ldw1 : kTcHidden;
-        load_weights(aB, Wt, ldw, n, K);
+        const int n = layer == 2 ? kTcRows : kTcHidden;
+        // this layer's weights have landed (each thread its own copies, then the barrier),
+        // the epilogue's generic-proxy writes of A are visible to the tensor cores
         asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");   // generic-proxy writes -> async proxy
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
         __syncthreads();
         if (tid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
@@ -206,42 +241,55 @@ __global__ void __launch_bounds__(kTcThreads, 1) mlp_tc_kernel(TcNet net, const 
             tc_commit(aM);
         }
         __syncwarp();
-        // every thread has seen the MMAs complete (or the block gives up) before A is rewritten
+        // every thread has seen the MMAs complete (or the block gives up) before A or B is rewritten
         ok = __syncthreads_and(mbar_wait(aM, phase)) != 0;
         if (!ok) break;
         phase ^= 1u;
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
-        // ---- epilogue: this thread's row of the accumulator
-        const float* bias = layer == 0 ? net.b1 : (layer == 1 ? net.b2 : net.b3);
-        for (int c = 0; c < n; c += 32) {
-            float v[32];
-            tc_ld32(tmem + lane_base + static_cast<uint32_t>(c), v);
-            if (layer < 2) {
+        // the next layer's weights stream into B during the epilogue
+        if (layer == 0) load_weights(aB, net.w2t, kTcHidden, kTcHidden, kTcHidden);
+        if (layer == 1) load_weights(aB, net.w3t, kTcHidden, kTcRows, kTcHidden);
+        if (layer < 2) {
+            const float* bias = sBias + layer * kTcHidden;
+            for (int c = cgroup * 64; c < cgroup * 64 + 64; c += 32) {
+                float v[32];
+                tc_ld32(tmem + lane_base + static_cast<uint32_t>(c), v);
 #pragma unroll
                 for (int g = 0; g < 32; g += 8) {
-                    __align__(16) bf16 h[8];
+                    uint32_t pk[4];
 #pragma unroll
-                    for (int e = 0; e < 8; e++) h[e] = tc_silu(v[g + e], bias[c + g + e]);
-                    *reinterpret_cast<uint4*>(sA + kmajor_offset(tid, c + g, kTcRows)) =
-                        *reinterpret_cast<const uint4*>(h);
+                    for (int e = 0; e < 8; e += 2)
+                        pk[e / 2] = pack_bf16(tc_silu(v[g + e] + bias[c + g + e]),
+                                              tc_silu(v[g + e + 1] + bias[c + g + e + 1]));
+                    *reinterpret_cast<uint4*>(sA + kmajor_offset(r, c + g, kTcRows)) =
+                        make_uint4(pk[0], pk[1], pk[2], pk[3]);
                 }
-            } else {
-                const int w = row0 + tid;
+            }
+        } else {
+            // logits [128][O + 1] (odd stride: lanes = rows hit distinct banks) over B
+            float* stage = reinterpret_cast<float*>(sB);
+            const int ld = net.O + 1;
+            const int c = cgroup * 32;
+            float v[32];
+            tc_ld32(tmem + lane_base + static_cast<uint32_t>(c), v);
 #pragma unroll
-                for (int e = 0; e < 32; e++) {
-                    const int j = c + e;
-                    if (w < count && j < net.O) logits_out[static_cast<long>(w) * net.O + j] = v[e] + bias[j];
-                }
+            for (int e = 0; e < 32; e++)
+                if (c + e < net.O) stage[r * ld + c + e] = v[e] + sBias[2 * kTcHidden + c + e];
+            __syncthreads();
+            float* out = logits_out + static_cast<long>(row0) * net.O;
+            for (int i = tid; i < rows * net.O; i += kTcThreads) {
+                const int rr = i / net.O, j = i - rr * net.O;
+                out[i] = stage[rr * ld + j];
             }
         }
         asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
-        __syncthreads();
     }
     if (!ok) {
         if (tid == 0) atomicExch(error, 1);
         // the MMAs of the timed-out layer may still run: give them a bounded second wait
         mbar_wait(aM, phase);
     }
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
     __syncthreads();
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTcCols));

@@ -514,12 +514,22 @@ struct LogNorm {
     float seed, len;
 };
 
-__device__ __forceinline__ LogNorm log_norms(const float* row, int N, int lane) {
-    // the row's entries j = lane + 32 c (N <= 256) are loaded together first
-    float v[8];
+// one logits row in registers: seed logits j = lane + 32 c (N <= 256), length logit `lane`
+struct RowRegs {
+    float v[8], vl;
+};
+
+__device__ __forceinline__ RowRegs load_row(const float* row, int N, int lane) {
+    RowRegs r;
 #pragma unroll
-    for (int c = 0; c < 8; c++) v[c] = lane + 32 * c < N ? row[lane + 32 * c] : -INFINITY;
-    const float vl = lane < kLengths ? row[N + lane] : -INFINITY;
+    for (int c = 0; c < 8; c++) r.v[c] = lane + 32 * c < N ? row[lane + 32 * c] : -INFINITY;
+    r.vl = lane < kLengths ? row[N + lane] : -INFINITY;
+    return r;
+}
+
+__device__ __forceinline__ LogNorm log_norms_of(const RowRegs& r, int N, int lane) {
+    const float* v = r.v;
+    const float vl = r.vl;
     float m = v[0];
 #pragma unroll
     for (int c = 1; c < 8; c++) m = fmaxf(m, v[c]);
@@ -535,6 +545,10 @@ __device__ __forceinline__ LogNorm log_norms(const float* row, int N, int lane) 
     for (int off = 16; off >= 1; off >>= 1) m2 = fmaxf(m2, __shfl_xor_sync(0xffffffffu, m2, off));
     const float s2 = warp_sum_xor(lane < kLengths ? expf(vl - m2) : 0.0f);
     return LogNorm{m + logf(s), m2 + logf(s2)};
+}
+
+__device__ __forceinline__ LogNorm log_norms(const float* row, int N, int lane) {
+    return log_norms_of(load_row(row, N, lane), N, lane);
 }
 
 // inverse-CDF draw from softmax(row[0..n)) with u in (0, 1]; entries are visited in
@@ -654,10 +668,14 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) learned_accept_kernel(Rbm
     const int lane = threadIdx.x & 31;
     const int w = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
     if (w >= L.B) return;
+    // every independent load is issued up front: the move, the spins, the proposed
+    // state's logits row, the angles and their Re f
     Spins<NW> s;
 #pragma unroll
     for (int k = 0; k < NW; k++) s.w[k] = L.spins[static_cast<long>(w) * NW + k];
     const int i = L.site[w], l = L.len[w];
+    const float* rowp = L.logits_prop + static_cast<long>(w) * L.O;
+    const RowRegs rr = load_row(rowp, L.N, lane);
     const long base = static_cast<long>(w) * P.Mpad + lane;
     float tr[K], ti[K], re[K];
 #pragma unroll
@@ -667,21 +685,37 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) learned_accept_kernel(Rbm
         ti[k] = t.y;
         re[k] = L.re[base + 32 * k];
     }
-    // trial angles: two_s = 2 * (new spin) for each cluster site, in cluster order; the K
-    // loads of one W row are issued together
+    // trial angles: two_s = 2 * (new spin) for each cluster site, added in cluster order;
+    // the W rows of two sites are loaded together
     float nr[K], ni[K], nre[K];
 #pragma unroll
     for (int k = 0; k < K; k++) { nr[k] = tr[k]; ni[k] = ti[k]; }
-    for (int q = 0; q < l; q++) {
-        int c = i + q;
-        if (c >= P.N) c -= P.N;
-        const float two_s = s.up(c) ? -2.0f : 2.0f;
-        const float2* row = P.W + static_cast<long>(c) * P.Mpad + lane;
+    for (int q = 0; q < l; q += 2) {
+        int c0 = i + q;
+        if (c0 >= P.N) c0 -= P.N;
+        int c1 = c0 + 1;
+        if (c1 >= P.N) c1 -= P.N;
+        const bool two = q + 1 < l;
+        const float s0 = s.up(c0) ? -2.0f : 2.0f, s1 = s.up(c1) ? -2.0f : 2.0f;
+        const float2* row0 = P.W + static_cast<long>(c0) * P.Mpad + lane;
+        const float2* row1 = P.W + static_cast<long>(c1) * P.Mpad + lane;
+        float2 w0[K], w1[K];
 #pragma unroll
         for (int k = 0; k < K; k++) {
-            const float2 wv = __ldg(row + 32 * k);
-            nr[k] = __fmaf_rn(two_s, wv.x, nr[k]);
-            ni[k] = __fmaf_rn(two_s, wv.y, ni[k]);
+            w0[k] = __ldg(row0 + 32 * k);
+            w1[k] = two ? __ldg(row1 + 32 * k) : make_float2(0.0f, 0.0f);
+        }
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            nr[k] = __fmaf_rn(s0, w0[k].x, nr[k]);
+            ni[k] = __fmaf_rn(s0, w0[k].y, ni[k]);
+        }
+        if (two) {
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                nr[k] = __fmaf_rn(s1, w1[k].x, nr[k]);
+                ni[k] = __fmaf_rn(s1, w1[k].y, ni[k]);
+            }
         }
     }
     float part = 0.0f;
@@ -691,8 +725,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) learned_accept_kernel(Rbm
         part = __fadd_rn(part, __fsub_rn(nre[k], re[k]));
     }
     const float delta = warp_sum_xor(part);
-    const float* rowp = L.logits_prop + static_cast<long>(w) * L.O;
-    const LogNorm ln = log_norms(rowp, L.N, lane);
+    const LogNorm ln = log_norms_of(rr, L.N, lane);
     const float logq_rev = (rowp[i] - ln.seed) + (rowp[L.N + l - 1] - ln.len);
     const float log_a = 2.0f * delta + logq_rev - L.logq_fwd[w];
     WalkerRng rng;
