@@ -299,6 +299,48 @@ RBMG_API int rbmg_batch_autotune(rbmg_batch* batch, int sweeps, int reps, double
 RBMG_API int rbmg_batch_result(const rbmg_batch* batch, int instance, double* energy, double* grad, double* eloc);
 RBMG_API int rbmg_batch_info(const rbmg_batch* batch, int* num_instances, uint64_t* accepts, double* tuned_ms);
 
+/* ---------------------------------------------------------------- optimisers
+ * The reference's gradient-descent methods (pyRBMonGPU/gradient_descent.py, Python on the
+ * host) as device kernels with their state on the device.  hyper[5] = {eta, gamma or
+ * beta1, beta2, epsilon, p}; unused entries are ignored:
+ *   VANILLA eta (:14-22)            MOMENTUM eta, gamma (:37-47)     NAG eta, gamma (:51-61)
+ *   ADAGRAD eta, eps (:70-83)       ADADELTA gamma, eps (:86-108)    RMSPROP eta, gamma, eps (:111-126)
+ *   ADAM beta1, beta2, eta, eps (:135-152)   PADAM beta1, beta2, eta, eps, p (:161-181)
+ *   ADAMAX beta1, beta2, eta, eps (:190-214)
+ * Adam divides by 1 - beta (no power of the step count) as the reference does
+ * (:147-148) unless flags has RBMG_OPT_STANDARD_BIAS (Kingma & Ba's 1 - beta^t). */
+#define RBMG_OPT_VANILLA 0
+#define RBMG_OPT_MOMENTUM 1
+#define RBMG_OPT_NAG 2
+#define RBMG_OPT_ADAGRAD 3
+#define RBMG_OPT_ADADELTA 4
+#define RBMG_OPT_RMSPROP 5
+#define RBMG_OPT_ADAM 6
+#define RBMG_OPT_PADAM 7
+#define RBMG_OPT_ADAMAX 8
+#define RBMG_OPT_STANDARD_BIAS 1
+typedef struct rbmg_optimizer rbmg_optimizer;
+RBMG_API int rbmg_optimizer_create(int method, int num_params, const double* hyper, int num_hyper, int flags,
+                                   rbmg_optimizer** out);
+RBMG_API int rbmg_optimizer_destroy(rbmg_optimizer* opt);
+/* zero the state (velocities, moments) and the step count */
+RBMG_API int rbmg_optimizer_reset(rbmg_optimizer* opt);
+RBMG_API int rbmg_optimizer_num_steps(const rbmg_optimizer* opt, uint64_t* steps);
+/* one step of the generators' loop body with a host gradient (the reference's
+ * gradient_function): params [2P] in/out, grad [2P]; eta >= 0 overrides hyper[0] for this
+ * step (the reference's callable eta), eta < 0 keeps it */
+RBMG_API int rbmg_optimizer_update(rbmg_optimizer* opt, double* params, const double* grad, double eta);
+/* NAG's evaluation point params - gamma velocity (:56) -> out [2P] */
+RBMG_API int rbmg_optimizer_lookahead(rbmg_optimizer* opt, const double* params, double* out);
+/* Fused ground-state step (the groundstate branch of set_params_and_return_gradient,
+ * pyRBMonGPU/LearningByGradientDescent.py:128-137, with the optimiser's update): the
+ * energy gradient of rbmg_ev_gradient formed on the device, the update applied to the
+ * device copy of psi's parameters, and psi's device parameters rewritten; only the
+ * energy <H> [2] (at the parameters before the update) comes back.  NAG takes the
+ * gradient at params - gamma velocity.  psi's host parameters follow on the next read. */
+RBMG_API int rbmg_optimizer_step_energy(rbmg_optimizer* opt, rbmg_psi* psi, const rbmg_operator* op,
+                                        rbmg_ensemble* ens, double eta, double* energy /* [2] */);
+
 /* FP32 FMA throughput of the current device in TFLOP/s (a probe kernel of `iters`
  * x 128 independent FMAs per thread), the roofline denominator of the sampler. */
 RBMG_API int rbmg_probe_fp32_tflops(int iters, double* tflops);

@@ -102,6 +102,13 @@ SIGNATURES = {
     "rbmg_batch_result": [_vp, C.c_int, _dp, _dp, _dp],
     "rbmg_batch_info": [_vp, _ip, _u64p, _dp],
     "rbmg_chain_learned_async": [_vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_int, _vp, _vp],
+    "rbmg_optimizer_create": [C.c_int, C.c_int, _dp, C.c_int, C.c_int, _vpp],
+    "rbmg_optimizer_destroy": [_vp],
+    "rbmg_optimizer_reset": [_vp],
+    "rbmg_optimizer_num_steps": [_vp, _u64p],
+    "rbmg_optimizer_update": [_vp, _dp, _dp, C.c_double],
+    "rbmg_optimizer_lookahead": [_vp, _dp, _dp],
+    "rbmg_optimizer_step_energy": [_vp, _vp, _vp, _vp, C.c_double, _dp],
 }
 _RESTYPE = {"rbmg_last_error": C.c_char_p, "rbmg_version": C.c_char_p}
 

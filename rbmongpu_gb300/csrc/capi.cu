@@ -133,6 +133,8 @@ static int rbm_upload(rbmg_psi* p) {
 // FP64 parameter copies for the Hilbert-space distance pass, uploaded on first use
 static int rbm_upload64(const rbmg_psi* p) {
     if (p->f64_valid) return RBMG_OK;
+    const int rs = psi_sync_host(p);
+    if (rs != RBMG_OK) return rs;
     RBMG_CK(p->db64.ensure(sizeof(cplx) * p->M));
     RBMG_CK(p->dW64.ensure(sizeof(cplx) * p->W.size()));
     RBMG_CK(cudaMemcpyAsync(p->db64.p, p->b.data(), sizeof(cplx) * p->M, cudaMemcpyHostToDevice, stream()));
@@ -217,6 +219,8 @@ extern "C" int rbmg_psi_deep_create(int N, int num_layers, const int* sizes, con
 
 extern "C" int rbmg_psi_copy(const rbmg_psi* psi, rbmg_psi** out) {
     if (!psi || !out) return fail(RBMG_EINVAL, "copy: null handle");
+    const int rs = psi_sync_host(psi);
+    if (rs != RBMG_OK) return rs;
     auto p = std::make_unique<rbmg_psi>();
     p->kind = psi->kind;
     p->N = psi->N;
@@ -258,6 +262,8 @@ extern "C" int rbmg_psi_shape(const rbmg_psi* psi, int* N, int* M, int* num_para
 
 extern "C" int rbmg_psi_get_params(const rbmg_psi* psi, double* params) {
     if (!psi || !params) return fail(RBMG_EINVAL, "get_params: null");
+    const int rs = psi_sync_host(psi);
+    if (rs != RBMG_OK) return rs;
     cplx* out = reinterpret_cast<cplx*>(params);
     const int N = psi->N;
     for (int i = 0; i < N; i++) {
@@ -285,6 +291,8 @@ extern "C" int rbmg_psi_set_params(rbmg_psi* psi, const double* params) {
     const int P = psi->num_params();
     for (int k = 0; k < P; k++)
         if (!std::isfinite(in[k].real()) || !std::isfinite(in[k].imag())) return fail(RBMG_ENAN, "set_params: non-finite");
+    psi->host_stale = false;     // the host copy is the truth again; the device master
+    psi->master_valid = false;   // is rebuilt from it by the next device optimiser step
     for (int i = 0; i < N; i++) {
         psi->alpha[i] = in[i].real();
         psi->beta[i] = in[N + i].real();
@@ -935,9 +943,11 @@ extern "C" int rbmg_ev_fluctuation(const rbmg_psi* psi, const rbmg_operator* op,
     return RBMG_OK;
 }
 
-extern "C" int rbmg_ev_gradient(const rbmg_psi* psi, const rbmg_operator* op, rbmg_ensemble* ens, double* grad,
-                                double* value) {
-    if (!op || !grad || !value) return fail(RBMG_EINVAL, "gradient: null");
+// The gradient's sums, left on the device: acc_O = sum w O, acc_EO = sum w (E - E0) O*,
+// acc_Ek = sum w (E_k - E0 O) over the O_k entries k >= 2N, sums[0] = sum w E; E0 (the
+// first chunk's mean local energy) and the ensemble's normalisation factor come back.
+static int ev_gradient_sums(const rbmg_psi* psi, const rbmg_operator* op, rbmg_ensemble* ens, cplx* E0_out,
+                            double* norm_out) {
     int r = check_pair(psi, op, ens);
     if (r != RBMG_OK) return r;
     const int N = psi->N, P = psi->num_params();
@@ -1037,6 +1047,21 @@ extern "C" int rbmg_ev_gradient(const rbmg_psi* psi, const rbmg_operator* op, rb
         return RBMG_OK;
     });
     if (r != RBMG_OK) return r;
+    *E0_out = E0;
+    *norm_out = res.norm_factor;
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_ev_gradient(const rbmg_psi* psi, const rbmg_operator* op, rbmg_ensemble* ens, double* grad,
+                                double* value) {
+    if (!op || !grad || !value) return fail(RBMG_EINVAL, "gradient: null");
+    cplx E0;
+    double f = 0.0;
+    int r = ev_gradient_sums(psi, op, ens, &E0, &f);
+    if (r != RBMG_OK) return r;
+    const int N = psi->N;
+    const size_t ok_len = static_cast<size_t>(psi->num_params() - 2 * N);
+    Workspace& W = ws();
     std::vector<double2> O(ok_len), EO(ok_len), Ek(ok_len);
     double2 Es;
     RBMG_CK(cudaMemcpyAsync(O.data(), W.acc_O.p, sizeof(double2) * ok_len, cudaMemcpyDeviceToHost, stream()));
@@ -1047,7 +1072,6 @@ extern "C" int rbmg_ev_gradient(const rbmg_psi* psi, const rbmg_operator* op, rb
     // ExpectationValue.cu:243-253: grad = <E O*> + conj<E_k> - 2 <E> <O*>.  With the centred
     // sums <E O*> = EO' + E0 conj<O> and <E_k> = Ek' + E0 <O>, so
     // grad = EO' + conj(Ek') + (E0 + conj(E0) - 2 <E>) conj<O>.
-    const double f = res.norm_factor;
     const cplx E = cplx(Es.x, Es.y) * f;
     const cplx shift_sum = E0 + std::conj(E0) - 2.0 * E;
     cplx* g = reinterpret_cast<cplx*>(grad);
@@ -1058,6 +1082,29 @@ extern "C" int rbmg_ev_gradient(const rbmg_psi* psi, const rbmg_operator* op, rb
     }
     value[0] = E.real();
     value[1] = E.imag();
+    return RBMG_OK;
+}
+
+// The same gradient left on the device: d_grad [P] complex128 (entries below 2N zero),
+// formed by launch_grad_final from the sums above; the energy comes back to the host.
+int rbmg::ev_gradient_device(const rbmg_psi* psi, const rbmg_operator* op, rbmg_ensemble* ens, double2* d_grad,
+                       double* value) {
+    if (!op || !d_grad || !value) return fail(RBMG_EINVAL, "gradient: null");
+    cplx E0;
+    double f = 0.0;
+    int r = ev_gradient_sums(psi, op, ens, &E0, &f);
+    if (r != RBMG_OK) return r;
+    Workspace& W = ws();
+    const int N = psi->N;
+    const long ok_len = psi->num_params() - 2 * N;
+    RBMG_CK(launch_grad_final(W.acc_O.as<double2>(), W.acc_EO.as<double2>(), W.acc_Ek.as<double2>(),
+                              W.sums.as<double2>(), f, make_double2(E0.real(), E0.imag()), 2 * N, ok_len, d_grad,
+                              stream()));
+    double2 Es;
+    RBMG_CK(cudaMemcpyAsync(&Es, W.sums.p, sizeof(double2), cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaStreamSynchronize(stream()));
+    value[0] = Es.x * f;
+    value[1] = Es.y * f;
     return RBMG_OK;
 }
 

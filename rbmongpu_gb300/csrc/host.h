@@ -87,11 +87,32 @@ struct rbmg_psi {
     std::shared_ptr<void> deep_host;       // owner of the device buffers behind deep_dev
     int width = 0;
 
+    // device master copy of the packed parameter vector [P] complex128, written by the
+    // device optimiser (optim.cu); while host_stale is set the vectors above are out of
+    // date and psi_sync_host refreshes them before any host read
+    rbmg::DevBuf dmaster;
+    bool master_valid = false;
+    mutable bool host_stale = false;
+
     int num_params() const;
     rbmg::RbmDev rbm_dev() const {
         return rbmg::RbmDev{N, M, Mpad, static_cast<const float2*>(dW.p), static_cast<const float2*>(db.p)};
     }
 };
+
+namespace rbmg {
+// optim.cu: host copy of the parameters from the device master when the optimiser
+// has moved them; packed device master from the host copy; device parameters (the
+// layouts the kernels read) from a packed vector on the device
+int psi_sync_host(const rbmg_psi* psi);
+int psi_master_ensure(rbmg_psi* psi);
+int psi_scatter(rbmg_psi* psi, const double2* packed);
+// capi.cu: the energy gradient formed on the device, d_grad [P]; energy to value[2]
+int ev_gradient_device(const rbmg_psi* psi, const rbmg_operator* op, rbmg_ensemble* ens, double2* d_grad,
+                       double* value);
+cudaError_t launch_grad_final(const double2* O, const double2* EO, const double2* Ek, const double2* sums,
+                              double norm, double2 E0, int first, long count, double2* grad, cudaStream_t st);
+}  // namespace rbmg
 
 struct rbmg_operator {
     int S = 0, L = 0;
