@@ -341,6 +341,19 @@ RBMG_API int rbmg_optimizer_lookahead(rbmg_optimizer* opt, const double* params,
 RBMG_API int rbmg_optimizer_step_energy(rbmg_optimizer* opt, rbmg_psi* psi, const rbmg_operator* op,
                                         rbmg_ensemble* ens, double eta, double* energy /* [2] */);
 
+/* ---------------------------------------------------------------- S matrix
+ * get_S_matrix (source/network_functions/S_matrix.cu:10-53; the reference instantiates it
+ * for Psi with ExactSummation and binds it to no Python name): S [P][P] complex128,
+ * S[k][k'] = sum_s O_k(s) conj(O_k'(s)) / num_steps over every configuration of the
+ * ensemble.  As in the reference the exact-summation weight |psi|^2 is not applied and
+ * entries k < 2N are zero.  flags: RBMG_S_WEIGHTED weights each configuration by its
+ * normalised |psi|^2 (no change for MonteCarloLoop, whose samples carry weight 1);
+ * RBMG_S_CENTERED subtracts <O_k> conj(<O_k'>) (the covariance of stochastic
+ * reconfiguration).  Psi and PsiDeep, both ensembles; PsiPair has no O_k. */
+#define RBMG_S_WEIGHTED 1
+#define RBMG_S_CENTERED 2
+RBMG_API int rbmg_s_matrix(const rbmg_psi* psi, rbmg_ensemble* ens, int flags, double* out /* [2 P P] */);
+
 /* FP32 FMA throughput of the current device in TFLOP/s (a probe kernel of `iters`
  * x 128 independent FMAs per thread), the roofline denominator of the sampler. */
 RBMG_API int rbmg_probe_fp32_tflops(int iters, double* tflops);

@@ -184,6 +184,21 @@ def O_k(psi, spins):
     return out.view(np.complex128)
 
 
+def s_matrix(psi, spins, weights=None, centered=False):
+    """get_S_matrix (source/network_functions/S_matrix.cu:10-53): S[k, k'] = sum_s c_s
+    O_k(s) conj(O_k'(s)) / sum_s c_s over the configurations `spins` [n][nwords], with
+    c_s = 1 as the reference has it (its ExactSummation weight is not applied) or the
+    given weights; centered subtracts <O> <O>^dagger (the covariance of SR)."""
+    O = np.array([O_k(psi, s) for s in np.asarray(spins, np.uint64)])
+    c = np.ones(len(O)) if weights is None else np.asarray(weights, np.float64)
+    c = c / c.sum()
+    S = np.einsum("s,sk,sl->kl", c, O, O.conj())
+    if centered:
+        m = c @ O
+        S = S - np.outer(m, m.conj())
+    return S
+
+
 def local_energy(psi, op, spins, lp=None):
     s = np.ascontiguousarray(spins, np.uint64)
     if lp is None:

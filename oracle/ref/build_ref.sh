@@ -15,7 +15,8 @@ mkdir -p "$OUT/obj"
 UNITS="Array RNGStates quantum_state/Psi quantum_state/PsiDeep quantum_state/PsiPair \
  spin_ensembles/MonteCarloLoop spin_ensembles/ExactSummation operator/Operator \
  network_functions/ExpectationValue network_functions/PsiNorm network_functions/HilbertSpaceDistance \
- network_functions/HilbertSpaceDistance_PsiPair network_functions/PsiVector network_functions/PsiOkVector"
+ network_functions/HilbertSpaceDistance_PsiPair network_functions/PsiVector network_functions/PsiOkVector \
+ network_functions/S_matrix"
 pids=""
 for u in $UNITS; do
   o="$OUT/obj/$(echo "$u" | tr / _).o"

@@ -14,6 +14,7 @@
 #include "network_functions/PsiNorm.hpp"
 #include "network_functions/PsiVector.hpp"
 #include "network_functions/PsiOkVector.hpp"
+#include "network_functions/S_matrix.hpp"
 
 #include <complex>
 #include <cstdio>
@@ -208,6 +209,14 @@ int main(int argc, char** argv) {
         }
         if (meta_i("ok", 0)) ok_vectors(psi, P);
         if (meta_i("mc_samples", 0)) mc_outputs(psi, op, N, P);
+        if (meta_i("smatrix", 0)) {
+            // get_S_matrix (source/network_functions/S_matrix.cu:10-53), ExactSummation
+            ExactSummation es(static_cast<unsigned>(N), false);
+            auto S = get_S_matrix(psi, es);
+            std::vector<cplx> out(static_cast<size_t>(P) * P);
+            for (size_t q = 0; q < out.size(); q++) out[q] = cplx(S[q].real(), S[q].imag());
+            save("smatrix", out.data(), out.size());
+        }
         // activation function samples
         const auto z = load<cplx>("act_in.bin");
         std::vector<cplx> lc(z.size()), th(z.size());

@@ -9,6 +9,7 @@
 #include <cuda_profiler_api.h>
 
 #include "host.h"
+#include "smatrix.h"
 #include "rbm64.h"
 #include "reduce.h"
 
@@ -51,6 +52,7 @@ int deep_log_psi(const rbmg_psi* psi, int count, const uint64_t* d_spins, uint64
 struct Workspace {
     DevBuf sample_spins, eloc, logpsi, logpsi_p, T, U, X, Tp, weights, coef1, coef2, coef3, omega, pr, nn;
     DevBuf partial, block_scratch, sums, acc_O, acc_EO, acc_Ek, acc_wO, acc_pO, block_max, zsum;
+    DevBuf smat, smean, okrows;
 };
 
 static Workspace& ws() {
@@ -1475,6 +1477,97 @@ extern "C" int rbmg_psi_O_k_vector(const rbmg_psi* psi, const uint64_t* spins, d
 }
 
 // ====================================================================== persistent chains
+namespace rbmg {
+int deep_ok_rows(const rbmg_psi* psi, int count, const uint64_t* d_spins, uint64_t enum_base, int enumerate,
+                 double2* rows, long ld, cudaStream_t st);
+}  // namespace rbmg
+
+// get_S_matrix (source/network_functions/S_matrix.cu:10-53, instantiated for Psi with
+// ExactSummation only): S[k][k'] = sum_s O_k(s) conj(O_k'(s)) / num_steps over every
+// configuration of the ensemble, without the ensemble's weight (the reference ignores the
+// weight its foreach passes); flags add the weight and / or centre it (the SR covariance).
+extern "C" int rbmg_s_matrix(const rbmg_psi* psi, rbmg_ensemble* ens, int flags, double* out) {
+    if (!psi || !ens || !out) return fail(RBMG_EINVAL, "S_matrix: null");
+    if (psi->kind == 2) return fail(RBMG_EUNSUPPORTED, "S_matrix: PsiPair has no O_k (PsiPair.hpp:73-76)");
+    if (ens->kind == 1 && static_cast<int>(ens->num_spins) != psi->N)
+        return fail(RBMG_EINVAL, "S_matrix: ExactSummation size differs from psi's N");
+    const int N = psi->N, P = psi->num_params(), L = P - 2 * N, nw = nwords_of(N);
+    const bool weighted = (flags & RBMG_S_WEIGHTED) != 0, centered = (flags & RBMG_S_CENTERED) != 0;
+    Workspace& W = ws();
+    const size_t sbytes = sizeof(double2) * static_cast<size_t>(L) * L;
+    RBMG_CK(W.smat.ensure(sbytes));
+    RBMG_CK(W.smean.ensure(sizeof(double2) * L));
+    RBMG_CK(cudaMemsetAsync(W.smat.p, 0, sbytes, stream()));
+    RBMG_CK(cudaMemsetAsync(W.smean.p, 0, sizeof(double2) * L, stream()));
+    int dev = 0, sms = 0;
+    RBMG_CK(cudaGetDevice(&dev));
+    RBMG_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    uint64_t total = 0;
+    StreamResult res;
+    const int r = run_stream(ens, psi, nullptr, false, 4096, &res, [&](const Chunk& c) -> int {
+        total += static_cast<uint64_t>(c.count);
+        SmSource a{};
+        a.L = L;
+        a.N = N;
+        a.M = psi->M;
+        a.Mpad = psi->Mpad;
+        a.nw = nw;
+        a.weighted = weighted && c.weights;
+        if (psi->kind == 0) {
+            RBMG_CK(W.Tp.ensure(sizeof(float2) * static_cast<size_t>(c.count) * psi->Mpad));
+            RBMG_CK(W.logpsi_p.ensure(sizeof(double2) * c.count));
+            EstLaunch E{};
+            E.count = c.count;
+            E.enum_base = c.enum_base;
+            E.spins = c.spins;
+            E.flags = EST_PRIME | (c.enumerate ? EST_ENUMERATE : 0);
+            E.logpsi_prime = W.logpsi_p.as<double2>();
+            E.Tp = W.Tp.as<float2>();
+            const RbmDev d = psi->rbm_dev();
+            RBMG_CK(launch_rbm_estimate(d, nullptr, &d, E, stream()));
+            a.kind = 0;
+            a.count = c.count;
+            a.enumerate = c.enumerate;
+            a.enum_base = c.enum_base;
+            a.spins = c.spins;
+            a.T = W.Tp.as<float2>();
+            a.w = c.weights;
+            RBMG_CK(launch_sm_accumulate(a, W.smat.as<double2>(), centered ? W.smean.as<double2>() : nullptr, sms,
+                                         stream()));
+            return RBMG_OK;
+        }
+        // PsiDeep: FP64 O_k rows, in pieces of at most 256 MB
+        const int piece = static_cast<int>(std::max<size_t>(1, (size_t(256) << 20) / (sizeof(double2) * L)));
+        RBMG_CK(W.okrows.ensure(sizeof(double2) * static_cast<size_t>(std::min(piece, c.count)) * L));
+        for (int base = 0; base < c.count; base += piece) {
+            const int cnt = std::min(piece, c.count - base);
+            const uint64_t* sp = c.spins ? c.spins + static_cast<size_t>(base) * nw : nullptr;
+            const int rr = deep_ok_rows(psi, cnt, sp, c.enum_base + base, c.enumerate, W.okrows.as<double2>(), L,
+                                        stream());
+            if (rr != RBMG_OK) return rr;
+            a.kind = 1;
+            a.count = cnt;
+            a.rows = W.okrows.as<double2>();
+            a.ld = L;
+            a.w = c.weights ? c.weights + base : nullptr;
+            a.weighted = weighted && a.w;
+            RBMG_CK(launch_sm_accumulate(a, W.smat.as<double2>(), centered ? W.smean.as<double2>() : nullptr, sms,
+                                         stream()));
+        }
+        return RBMG_OK;
+    });
+    if (r != RBMG_OK) return r;
+    if (total == 0) return fail(RBMG_EINVAL, "S_matrix: the ensemble has no samples");
+    // the exact-summation weights are normalised to sum 1; otherwise divide by the count
+    const double z = (weighted && ens->kind == 1) ? 1.0 : static_cast<double>(total);
+    RBMG_CK(launch_sm_finish(L, W.smat.as<double2>(), W.smean.as<double2>(), 1.0 / z, centered ? 1 : 0, stream()));
+    std::memset(out, 0, sizeof(double2) * static_cast<size_t>(P) * P);
+    RBMG_CK(cudaMemcpy2DAsync(out + 2 * (static_cast<size_t>(2 * N) * P + 2 * N), sizeof(double2) * P, W.smat.p,
+                              sizeof(double2) * L, sizeof(double2) * L, L, cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaStreamSynchronize(stream()));
+    return RBMG_OK;
+}
+
 extern "C" int rbmg_stream(void** st) {
     if (!st) return fail(RBMG_EINVAL, "stream: null");
     *st = static_cast<void*>(stream());

@@ -906,6 +906,19 @@ static int col_reduce(int count, int P, const double2* c, const double2* A, long
     return RBMG_OK;
 }
 
+// O_k rows (k >= 2N) of `count` configurations into rows [count][ld] (FP64, PsiDeep)
+int deep_ok_rows(const rbmg_psi* psi, int count, const uint64_t* d_spins, uint64_t enum_base, int enumerate,
+                 double2* rows, long ld, cudaStream_t st) {
+    if (psi->kind != 1) return fail(RBMG_EUNSUPPORTED, "O_k rows: PsiDeep only (PsiPair.hpp:73-76 defines none)");
+    if (count <= 0) return RBMG_OK;
+    const DeepNetDev net = net_of(psi, 0);
+    const size_t sm = smem_for(net, sizeof(double2), true);
+    RBMG_CK(set_smem(deep_ok_kernel<false>, sm));
+    deep_ok_kernel<false><<<count, threads_for(net), sm, st>>>(net, count, d_spins, enum_base, enumerate, rows, ld);
+    RBMG_CK(cudaGetLastError());
+    return RBMG_OK;
+}
+
 int deep_hsd_okreduce(const rbmg_psi* pp, int pair_part, int count, const uint64_t* d_spins, uint64_t enum_base,
                       int enumerate, const double2* d_coef, double2* acc, cudaStream_t st) {
     const DeepNetDev net = net_of(pp, pair_part == 1 ? 1 : 0);

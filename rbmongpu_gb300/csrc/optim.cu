@@ -248,7 +248,16 @@ int psi_scatter(rbmg_psi* psi, const double2* packed) {
         rbm_scatter_kernel<<<blocks_of(total, 256), 256, 0, stream()>>>(packed, psi->N, psi->M, psi->Mpad,
                                                                          psi->db.as<float2>(), psi->dW.as<float2>());
         RBMG_CK(cudaGetLastError());
-        psi->f64_valid = false;
+        // the FP64 copies (exact-summation weights, Hilbert-space distance) in the host
+        // layout b [M], W [N][M] are the packed vector's tail as it stands
+        const size_t M = psi->M, NM = static_cast<size_t>(psi->N) * psi->M;
+        RBMG_CK(psi->db64.ensure(sizeof(cplx) * M));
+        RBMG_CK(psi->dW64.ensure(sizeof(cplx) * NM));
+        RBMG_CK(cudaMemcpyAsync(psi->db64.p, packed + 2 * psi->N, sizeof(cplx) * M, cudaMemcpyDeviceToDevice,
+                                stream()));
+        RBMG_CK(cudaMemcpyAsync(psi->dW64.p, packed + 2 * psi->N + M, sizeof(cplx) * NM, cudaMemcpyDeviceToDevice,
+                                stream()));
+        psi->f64_valid = true;
         return RBMG_OK;
     }
     ScatterTable t{};

@@ -1,0 +1,216 @@
+// The S matrix S[k][k'] = < O_k conj(O_k') > over an ensemble (the reference's
+// get_S_matrix, source/network_functions/S_matrix.cu:10-53, which adds
+// O_k O_k'* for every configuration with a complex global atomic per entry).
+//
+// Here it is a complex Hermitian rank-n update S += F^T conj(F) of the per-sample O_k
+// rows F [n][L] (L = P - 2N), tiled 64 x 64 over the upper triangle of S: each CTA
+// stages 16 samples of its row block and its column block in shared memory, every
+// thread accumulates a 4 x 4 block of complex products in FP32 registers, and every
+// 1024 samples the CTA adds its partial tile into the FP64 matrix in HBM (plain
+// read-modify-write when it owns the tile, FP64 atomics when the samples are split
+// across CTAs).  For the complex RBM the rows are never stored: an element of F is
+// tanh(theta_j) (k < M) or s_i tanh(theta_j) (k = M + i M + j, Psi.hpp:165-178), formed
+// while the tile is loaded from the sample's tanh row and spins.  PsiDeep rows come
+// from the FP64 reverse pass.  The lower triangle is mirrored at the end.
+#include "host.h"
+#include "smatrix.h"
+
+namespace rbmg {
+
+namespace {
+
+constexpr int kT = 64;          // tile edge
+constexpr int kS = 16;          // samples per shared-memory stage
+constexpr int kFlush = 1024;    // samples accumulated in FP32 before the FP64 update
+
+struct Elem {
+    int i, j;   // RBM: spin index (-1: bias block) and hidden unit; rows: column k
+    bool live;
+};
+
+__device__ __forceinline__ Elem elem_of(const SmSource& a, int k) {
+    Elem e{-1, k, k < a.L};
+    if (a.kind == 0 && e.live && k >= a.M) {
+        const int r = k - a.M;
+        e.i = r / a.M;
+        e.j = r - e.i * a.M;
+    }
+    return e;
+}
+
+// sqrt(w_s) F[s][k] (or F[s][k] unweighted), zero outside the matrix
+__device__ __forceinline__ float2 load_f(const SmSource& a, const Elem& e, int s) {
+    if (!e.live || s >= a.count) return make_float2(0.0f, 0.0f);
+    float2 v;
+    if (a.kind == 0) {
+        v = a.T[static_cast<long>(s) * a.Mpad + e.j];
+        if (e.i >= 0) {
+            const uint64_t word = a.enumerate ? ((e.i >> 6) == 0 ? a.enum_base + static_cast<uint64_t>(s) : 0ull)
+                                              : a.spins[static_cast<long>(s) * a.nw + (e.i >> 6)];
+            if (!((word >> (e.i & 63)) & 1ull)) v = make_float2(-v.x, -v.y);
+        }
+    } else {
+        const double2 d = a.rows[static_cast<long>(s) * a.ld + e.j];
+        v = make_float2(static_cast<float>(d.x), static_cast<float>(d.y));
+    }
+    if (a.weighted) {
+        const float c = static_cast<float>(sqrt(a.w[s]));
+        v.x *= c;
+        v.y *= c;
+    }
+    return v;
+}
+
+__global__ void __launch_bounds__(256) sm_herk_kernel(SmSource a, double2* __restrict__ S, int nt, int slice,
+                                                      int atomic) {
+    const int tm = blockIdx.x / nt, tn = blockIdx.x - (blockIdx.x / nt) * nt;
+    if (tm > tn) return;   // lower triangle: mirrored at the end
+    const int s_begin = blockIdx.y * slice;
+    const int s_end = min(a.count, s_begin + slice);
+    if (s_begin >= s_end) return;
+    __shared__ float2 Fa[kS][kT], Fb[kS][kT];
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    const int m0 = tm * kT, n0 = tn * kT;
+    // this thread's four loader columns of each block, sample row ty of the stage
+    Elem ea[4], eb[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        ea[q] = elem_of(a, m0 + tx + 16 * q);
+        eb[q] = elem_of(a, n0 + tx + 16 * q);
+    }
+    for (int f0 = s_begin; f0 < s_end; f0 += kFlush) {
+        const int f1 = min(s_end, f0 + kFlush);
+        float re[4][4], im[4][4];
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) re[i][j] = im[i][j] = 0.0f;
+        float2 pa[4], pb[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            pa[q] = f0 + ty < f1 ? load_f(a, ea[q], f0 + ty) : make_float2(0.0f, 0.0f);
+            pb[q] = f0 + ty < f1 ? load_f(a, eb[q], f0 + ty) : make_float2(0.0f, 0.0f);
+        }
+        for (int s0 = f0; s0 < f1; s0 += kS) {
+            __syncthreads();
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                Fa[ty][tx + 16 * q] = pa[q];
+                Fb[ty][tx + 16 * q] = pb[q];
+            }
+            __syncthreads();
+            const int sn = s0 + kS + ty;   // next stage's sample of this thread, loaded during the products
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                pa[q] = sn < f1 ? load_f(a, ea[q], sn) : make_float2(0.0f, 0.0f);
+                pb[q] = sn < f1 ? load_f(a, eb[q], sn) : make_float2(0.0f, 0.0f);
+            }
+#pragma unroll
+            for (int s = 0; s < kS; s++) {
+                float2 x[4], y[4];
+#pragma unroll
+                for (int i = 0; i < 4; i++) x[i] = Fa[s][ty + 16 * i];
+#pragma unroll
+                for (int j = 0; j < 4; j++) y[j] = Fb[s][tx + 16 * j];
+#pragma unroll
+                for (int i = 0; i < 4; i++)
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        // x conj(y)
+                        re[i][j] = fmaf(x[i].x, y[j].x, fmaf(x[i].y, y[j].y, re[i][j]));
+                        im[i][j] = fmaf(x[i].y, y[j].x, fmaf(-x[i].x, y[j].y, im[i][j]));
+                    }
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int r = m0 + ty + 16 * i;
+            if (r >= a.L) continue;
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int c = n0 + tx + 16 * j;
+                if (c >= a.L) continue;
+                double2* p = S + static_cast<long>(r) * a.L + c;
+                if (atomic) {
+                    atomicAdd(&p->x, static_cast<double>(re[i][j]));
+                    atomicAdd(&p->y, static_cast<double>(im[i][j]));
+                } else {
+                    double2 v = *p;
+                    v.x += static_cast<double>(re[i][j]);
+                    v.y += static_cast<double>(im[i][j]);
+                    *p = v;
+                }
+            }
+        }
+    }
+}
+
+// mean[k] += sum_s w_s F[s][k] (FP64)
+__global__ void sm_mean_kernel(SmSource a, double2* mean) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a.L) return;
+    SmSource u = a;
+    u.weighted = 0;
+    const Elem e = elem_of(u, k);
+    double sr = 0.0, si = 0.0;
+    for (int s = 0; s < a.count; s++) {
+        const float2 v = load_f(u, e, s);
+        const double c = a.weighted ? a.w[s] : 1.0;
+        sr += c * v.x;
+        si += c * v.y;
+    }
+    mean[k].x += sr;
+    mean[k].y += si;
+}
+
+// S <- S / Z with the lower triangle mirrored from the upper and a real diagonal;
+// centred: - m m^dagger with m = mean / Z
+__global__ void sm_finish_kernel(int L, double2* S, const double2* mean, double inv_z, int centered) {
+    const long idx = static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (idx >= static_cast<long>(L) * L) return;
+    const int r = static_cast<int>(idx / L), c = static_cast<int>(idx - static_cast<long>(r) * L);
+    // the upper triangle only (the diagonal tiles' lower halves are rewritten from their
+    // upper halves, so that S is Hermitian to the bit); the mirror images are written below
+    if (r > c) return;
+    double2 v = S[idx];
+    if (r == c) v.y = 0.0;
+    v.x *= inv_z;
+    v.y *= inv_z;
+    if (centered) {
+        const double2 a = mean[r], b = mean[c];
+        const double ar = a.x * inv_z, ai = a.y * inv_z, br = b.x * inv_z, bi = b.y * inv_z;
+        v.x -= ar * br + ai * bi;
+        v.y -= ai * br - ar * bi;
+        if (r == c) v.y = 0.0;
+    }
+    S[idx] = v;
+    if (r < c) S[static_cast<long>(c) * L + r] = make_double2(v.x, -v.y);
+}
+
+}  // namespace
+
+cudaError_t launch_sm_accumulate(const SmSource& a, double2* S, double2* mean, int num_sms, cudaStream_t st) {
+    if (a.count <= 0) return cudaSuccess;
+    const int nt = (a.L + kT - 1) / kT;
+    const int upper = nt * (nt + 1) / 2;
+    // split the samples over CTAs only when the triangle alone cannot fill the GPU
+    int split = 1;
+    const int want = 2 * num_sms;
+    if (upper < want) split = std::min((a.count + kFlush - 1) / kFlush, (want + upper - 1) / upper);
+    split = std::max(split, 1);
+    const int slice = (a.count + split - 1) / split;
+    const dim3 grid(nt * nt, split);
+    sm_herk_kernel<<<grid, 256, 0, st>>>(a, S, nt, slice, split > 1);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || !mean) return e;
+    sm_mean_kernel<<<(a.L + 127) / 128, 128, 0, st>>>(a, mean);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sm_finish(int L, double2* S, const double2* mean, double inv_z, int centered, cudaStream_t st) {
+    const long n = static_cast<long>(L) * L;
+    sm_finish_kernel<<<static_cast<int>((n + 255) / 256), 256, 0, st>>>(L, S, mean, inv_z, centered);
+    return cudaGetLastError();
+}
+
+}  // namespace rbmg

@@ -1,0 +1,31 @@
+// S-matrix kernels (smatrix.cu), driven from capi.cu::rbmg_s_matrix.
+#pragma once
+
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace rbmg {
+
+// one chunk of samples whose O_k rows (k >= 2N, L of them) enter the S matrix
+struct SmSource {
+    int kind;                // 0 complex RBM (rows formed from tanh(theta) and the spins), 1 FP64 rows
+    int count, L;
+    int N, M, Mpad, nw;      // RBM shape
+    int enumerate;           // configurations are enum_base + s (exact summation without a sector)
+    uint64_t enum_base;
+    const uint64_t* spins;   // [count][nw] when not enumerated
+    const float2* T;         // RBM: tanh(theta) [count][Mpad]
+    const double2* rows;     // kind 1: O_k rows [count][ld]
+    long ld;
+    const double* w;         // per-sample weights (exact summation), used when weighted
+    int weighted;
+};
+
+// S [L][L] += sum_s c_s F_s^T conj(F_s) on the upper tiles (c_s = w_s when weighted, else
+// 1); mean [L] += sum_s c_s F_s when mean is not null
+cudaError_t launch_sm_accumulate(const SmSource& src, double2* S, double2* mean, int num_sms, cudaStream_t st);
+// S /= Z, lower triangle mirrored; centred: S -= (mean / Z)(mean / Z)^dagger
+cudaError_t launch_sm_finish(int L, double2* S, const double2* mean, double inv_z, int centered, cudaStream_t st);
+
+}  // namespace rbmg

@@ -4,7 +4,7 @@ Builds seeded inputs with numpy, runs them through ``oracle/_ref/ref_harness`` (
 reference's own host path, compiled from its sources by ``oracle/ref/build_ref.sh``)
 and stores inputs and reference outputs together in ``<case>.npz``.
 
-    sh oracle/ref/build_ref.sh && python tests/golden/make_golden.py
+    sh oracle/ref/build_ref.sh && python tests/golden/make_golden.py [case ...]
 
 Needs the reference sources; the committed .npz files are what the tests read.
 """
@@ -141,7 +141,7 @@ def act_points(rng):
     return np.asarray(z, np.complex128)
 
 
-def rbm_case(name, N, M, sigma, seed, op, hop, unitary, nu, mc=None, normalize=True, ok_count=4):
+def rbm_case(name, N, M, sigma, seed, op, hop, unitary, nu, mc=None, normalize=True, ok_count=4, smatrix=False):
     rng = np.random.Generator(np.random.PCG64(seed))
     b = cnormal(rng, M, sigma)
     W = cnormal(rng, (N, M), sigma)
@@ -149,7 +149,7 @@ def rbm_case(name, N, M, sigma, seed, op, hop, unitary, nu, mc=None, normalize=T
     pW = W + cnormal(rng, (N, M), 1e-3)
     ok_spins = rng.integers(0, 2 ** min(N, 62), ok_count, dtype=np.uint64)
     meta = {"kind": "rbm", "N": N, "M": M, "prefactor": 1.0, "normalize": int(normalize),
-            "exact": int(N <= 16), "ok": 1, "hsd_unitary": int(unitary), "hsd_nu": nu}
+            "exact": int(N <= 16), "ok": 1, "hsd_unitary": int(unitary), "hsd_nu": nu, "smatrix": int(smatrix)}
     if mc:
         meta.update(mc)
     arrays = {"b.bin": b, "W.bin": W, "pp_b.bin": pb, "pp_W.bin": pW, "ok_spins.bin": ok_spins,
@@ -191,8 +191,15 @@ def deep_case(name, kind, N, sizes, conns, sigma, seed, op, hop, unitary, nu, mc
 
 
 def main():
+    """Writes every case, or only the cases named on the command line."""
     if not os.path.exists(HARNESS):
         sys.exit("build the reference harness first: sh oracle/ref/build_ref.sh")
+    only = set(sys.argv[1:])
+    global rbm_case, deep_case
+    if only:
+        def pick(fn):
+            return lambda name, *a, **k: fn(name, *a, **k) if name in only else None
+        rbm_case, deep_case = pick(rbm_case), pick(deep_case)
     # N=12, M=24 complex RBM, sigma 0.01, periodic TFIM h=1: exact <H>, gradient, HSD to a
     # copy perturbed by complex N(0, 1e-3^2) under the identity operator (unitary).
     rbm_case("c1_rbm_exact", 12, 24, 0.01, 101, tfim_chain(12, 1.0, 1.0), identity_op(), True, 1.0,
@@ -215,6 +222,8 @@ def main():
     # dense 10 -> 20 -> 10 -> 5 (the layer pattern of the 100->200->100->50 net, scaled down)
     deep_case("deep10_dense", "deep", 10, [20, 10, 5], [10, 20, 10], 0.1, 104, tfim_chain(10), identity_op(),
               True, 1.0)
+    # get_S_matrix of a small RBM over ExactSummation (the reference's only instantiation)
+    rbm_case("rbm6_smatrix", 6, 12, 0.3, 13, tfim_chain(6, 1.0, 1.0), identity_op(), True, 1.0, smatrix=True)
     # PsiPair 3 -> [9, 6] connectivity [1, 3] (the reference's test fixture)
     deep_case("pair3", "pair", 3, [9, 6], [1, 3], 0.3, 105, tfim_chain(3), identity_op(), True, 1.0)
 

@@ -130,7 +130,7 @@ FUSED = [("c1_rbm_exact", "adam", dict(beta1=0.9, beta2=0.999, eta=4e-3, epsilon
          ("c1_rbm_exact", "nag", dict(eta=0.05, gamma=0.9)),
          ("c1_rbm_exact", "rmsprop", dict(eta=1e-3, gamma=0.9, epsilon=1e-3)),
          ("deep8_sparse", "padam", dict(beta1=0.9, beta2=0.999, eta=1e-2, epsilon=1e-4, p=0.25)),
-         ("pair3", "momentum", dict(eta=0.02, gamma=0.9))]
+         ("deep10_dense", "momentum", dict(eta=0.02, gamma=0.9))]
 
 
 @gpu

@@ -1,0 +1,118 @@
+"""S matrix: the CPU restatement (oracle/pyoracle.py::s_matrix) against the reference's own
+get_S_matrix (tests/golden/rbm6_smatrix.npz, from its host build), and the CUDA kernels
+(rbmg_s_matrix) against both.
+
+Tolerance: 1e-5 of the largest entry (complex64 tanh rows, FP32 products accumulated
+over at most 1024 samples before the FP64 sum; the RBM path's tolerance elsewhere).
+"""
+import numpy as np
+import pytest
+
+from golden_cases import Case
+from oracle import pyoracle as po
+
+RTOL = 1e-5
+
+
+def rel(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def all_states(N):
+    return np.arange(2 ** N, dtype=np.uint64)[:, None]
+
+
+def exact_weights(opsi, N):
+    v = po.psi_vector(opsi)
+    w = np.abs(v) ** 2
+    return w / w.sum()
+
+
+# ----------------------------------------------------------------------------- CPU
+def test_restatement_matches_reference():
+    c = Case("rbm6_smatrix")
+    b, W = c.rbm()
+    S = po.s_matrix(po.RBM(b, W, c.prefactor), all_states(c.N))
+    ref = c.o("smatrix").reshape(S.shape)
+    assert rel(S, ref) < 1e-13
+    assert np.abs(ref[: 2 * c.N]).max() == 0.0
+
+
+def test_restatement_centered_is_psd_and_hermitian():
+    c = Case("rbm6_smatrix")
+    b, W = c.rbm()
+    opsi = po.RBM(b, W, c.prefactor)
+    S = po.s_matrix(opsi, all_states(c.N), exact_weights(opsi, c.N), centered=True)
+    assert np.abs(S - S.conj().T).max() < 1e-14
+    assert np.linalg.eigvalsh(S).min() > -1e-12
+
+
+# ----------------------------------------------------------------------------- GPU
+gpu = pytest.mark.gpu
+
+
+@gpu
+def test_reference_golden():
+    import rbmongpu_gb300 as rg
+    c = Case("rbm6_smatrix")
+    b, W = c.rbm()
+    psi = rg.Psi(np.zeros(c.N), np.zeros(c.N), b, W, c.prefactor, False, True)
+    S = rg.get_S_matrix(psi, rg.ExactSummation(c.N))
+    assert rel(S, c.o("smatrix").reshape(S.shape)) < RTOL
+
+
+@gpu
+@pytest.mark.parametrize("weighted,centered", [(False, False), (True, False), (True, True), (False, True)])
+def test_exact_rbm_vs_restatement(weighted, centered):
+    import rbmongpu_gb300 as rg
+    c = Case("c1_rbm_exact")
+    b, W = c.rbm()
+    psi = rg.Psi(np.zeros(c.N), np.zeros(c.N), b, W, c.prefactor, False, True)
+    opsi = po.RBM(b, W, c.prefactor)
+    S = rg.get_S_matrix(psi, rg.ExactSummation(c.N), weighted=weighted, centered=centered)
+    ref = po.s_matrix(opsi, all_states(c.N), exact_weights(opsi, c.N) if weighted else None, centered)
+    assert rel(S, ref) < RTOL
+
+
+@gpu
+@pytest.mark.parametrize("weighted", [False, True])
+def test_exact_deep_vs_restatement(weighted):
+    import rbmongpu_gb300 as rg
+    c = Case("deep8_sparse")
+    b, cn, w, fw = c.deep()
+    psi = rg.PsiDeep(np.zeros(c.N), np.zeros(c.N), b, cn, w, fw, c.prefactor, False, True)
+    opsi = po.Deep(c.N, b, cn, w, fw, c.prefactor)
+    S = rg.get_S_matrix(psi, rg.ExactSummation(c.N), weighted=weighted, centered=weighted)
+    ref = po.s_matrix(opsi, all_states(c.N), exact_weights(opsi, c.N) if weighted else None, weighted)
+    assert rel(S, ref) < 1e-9     # FP64 rows, FP32 products
+
+
+@gpu
+def test_monte_carlo_ragged_size_vs_restatement():
+    """N = 32, M = 60: L = 1980 is no multiple of the 64-wide tiles; 2048 MC samples on the
+    same Philox streams as a restatement over the sampled configurations."""
+    import rbmongpu_gb300 as rg
+    rng = np.random.default_rng(31)
+    N, M = 32, 60
+    b = 0.05 * (rng.normal(size=M) + 1j * rng.normal(size=M))
+    W = 0.05 * (rng.normal(size=(N, M)) + 1j * rng.normal(size=(N, M)))
+    psi = rg.Psi(np.zeros(N), np.zeros(N), b, W, 1.0, False, True)
+    mk = lambda: rg.MonteCarloLoop(2048, 1, 10, 512, True, seed=3)   # noqa: E731
+    sp, _, _ = mk().samples(psi)
+    S = rg.get_S_matrix(psi, mk(), centered=True)
+    O = np.array([po.O_k(po.RBM(b, W, 1.0), s) for s in sp])
+    m = O.mean(axis=0)
+    ref = O.T @ O.conj() / len(O) - np.outer(m, m.conj())
+    assert rel(S, ref) < RTOL
+    assert np.abs(S - S.conj().T).max() == 0.0
+
+
+@gpu
+def test_pair_is_rejected():
+    import rbmongpu_gb300 as rg
+    c = Case("pair3")
+    b, cn, w, fw = c.deep()
+    psi = rg.PsiPair(np.zeros(c.N), np.zeros(c.N), b, cn, w, fw, c.prefactor, False, True)
+    with pytest.raises(rg.RbmgError):
+        rg.get_S_matrix(psi, rg.ExactSummation(c.N))
