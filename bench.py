@@ -21,10 +21,11 @@ automatic windowing (c = 5) of the walkers' E_loc series; the plain chain's figu
 beside it ("plain"), with E_loc/s, the energy standard error per spin, and a flag where
 the window did not converge (tau_int is then a lower bound).
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--workload serving]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--workload serving|s_matrix]
 
 `--workload serving` times the batched serving of 64 uneven RBMs instead (one line of
-its own).
+its own); `--workload s_matrix` times get_S_matrix of the N=64, M=128 RBM over 16384
+Monte Carlo samples (P = 8448).
 
 For N > 1 run under torchrun: every rank samples its own replica of the walker sets
 (Philox keys offset by rank), no data-path collective; value = all ranks' effective
@@ -429,6 +430,100 @@ def run_serving(args):
     print(json.dumps(line))
 
 
+# --------------------------------------------------------------------- S-matrix workload
+SM_N, SM_M, SM_CHAINS, SM_PER_CHAIN = 64, 128, 4096, 4
+
+
+def sm_workload(N=SM_N, M=SM_M):
+    """The N=64, M=128 complex RBM (sigma 0.05, PCG64(102)) sampled by 4096 chains."""
+    rng = np.random.Generator(np.random.PCG64(102))
+    b = rng.normal(0, 0.05, M) + 1j * rng.normal(0, 0.05, M)
+    W = rng.normal(0, 0.05, (N, M)) + 1j * rng.normal(0, 0.05, (N, M))
+    return b, W
+
+
+def sm_cpu_baseline(b, W, samples, workers):
+    """The oracle's FP64 O_k rows of `samples` configurations and the rank-n update with
+    numpy's BLAS on the host cores -> samples/s."""
+    from oracle import pyoracle as po
+    opsi = po.RBM(b, W, 1.0)
+    rng = np.random.default_rng(5)
+    sp = rng.integers(0, 2 ** 63, (samples, 1), dtype=np.uint64)
+    t0 = time.perf_counter()
+    O = np.array([po.O_k(opsi, s) for s in sp])
+    S = O.T @ O.conj() / samples
+    dt = time.perf_counter() - t0
+    assert S.shape[0] == O.shape[1]
+    return samples / dt
+
+
+def run_smatrix(args):
+    """One step = one get_S_matrix call (the reference's get_S_matrix,
+    source/network_functions/S_matrix.cu) over a MonteCarloLoop pass of 16384 samples:
+    sampling, tanh rows, the Hermitian rank-16384 update of the 8320 x 8320 block and the
+    P x P result copied to the host."""
+    import torch
+    import ctypes
+    import rbmongpu_gb300 as rg
+    from rbmongpu_gb300._lib import call
+    torch.cuda.set_device(0)
+    Ns, Ms = args.sm_n, args.sm_m
+    b, W = sm_workload(Ns, Ms)
+    psi = rg.Psi(np.zeros(Ns), np.zeros(Ns), b, W, 1.0, False, True)
+    n = SM_CHAINS * SM_PER_CHAIN
+    mc = rg.MonteCarloLoop(n, 1, 20, SM_CHAINS, True, seed=11)
+    L = Ms + Ns * Ms
+    for _ in range(args.warmup):
+        rg.get_S_matrix(psi, mc)
+    ms_acc, walls = [], []
+    ms = ctypes.c_double()
+    launches = ctypes.c_int()
+    clocks = ClockSampler(0)
+    clocks.start()
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        S = rg.get_S_matrix(psi, mc)
+        walls.append(time.perf_counter() - t0)
+        call("rbmg_s_matrix_timing", ctypes.byref(ms), ctypes.byref(launches))
+        ms_acc.append(ms.value)
+    clk = clocks.stop()
+    assert np.isfinite(S[2 * Ns:, 2 * Ns:]).all()
+    wall = float(np.mean(walls))
+    acc_s = float(np.mean(ms_acc)) / 1e3
+    flops = 8.0 * L * (L + 1) / 2 * n          # 4 FMA per upper-triangle entry and sample
+    v = ctypes.c_double()
+    call("rbmg_probe_fp32_tflops", 20000, ctypes.byref(v))
+    peak = v.value
+    P = 2 * Ns + L
+    cpu = None
+    if args.cpu_seconds > 0:
+        cs = 512
+        cpu = {"value": sm_cpu_baseline(b, W, cs, os.cpu_count() or 1), "unit": "samples/s",
+               "cores": os.cpu_count() or 1, "kind": "port",
+               "sample": f"{cs} random configurations: oracle FP64 O_k rows + numpy BLAS rank-{cs} update"}
+    line = {
+        "metric": "S matrix (get_S_matrix): MC samples folded into the P x P O_k covariance per second",
+        "value": n / acc_s, "unit": "samples/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": acc_s * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 products (complex64 rows), f64 accumulation", "data": "synthetic (seeded PCG64 parameters)",
+        "config": {"workload": f"s_matrix_rbm_n{Ns}_m{Ms}_mc{n}", "N": Ns, "M": Ms, "P": P,
+                   "samples": n, "chains": SM_CHAINS,
+                   "l2": f"the {16 * L * L / 1e9:.2f} GB FP64 matrix, read and written every 1024 samples, "
+                         "exceeds L2 at N=64"},
+        "e2e": {"value": n / wall, "unit": "samples/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 16 * P * P},
+        "gpu_launches": int(launches.value) * args.steps,
+        "roofline": {"bound": "fp32", "achieved": flops / acc_s / 1e12, "peak": peak, "unit": "TFLOP/s",
+                     "frac": flops / acc_s / 1e12 / peak, "traffic": None,
+                     "peak_source": "measured in this run by the library's FP32 FMA probe kernel",
+                     "kernel": "sm_herk_kernel", "flops_per_launch": flops / max(1, launches.value)},
+        "cpu_baseline": cpu,
+        "clocks": clk,
+    }
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -442,8 +537,11 @@ def main():
     ap.add_argument("--train-walkers", type=int, default=4096)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=16.0, help="budget of the CPU baseline leg")
-    ap.add_argument("--workload", default="learned", choices=["learned", "serving"],
-                    help="learned: the N=100 learned-vs-plain chains (headline); serving: 64 uneven RBMs")
+    ap.add_argument("--sm-n", type=int, default=SM_N, help="s_matrix workload: visible units")
+    ap.add_argument("--sm-m", type=int, default=SM_M, help="s_matrix workload: hidden units")
+    ap.add_argument("--workload", default="learned", choices=["learned", "serving", "s_matrix"],
+                    help="learned: the N=100 learned-vs-plain chains (headline); serving: 64 uneven RBMs; "
+                         "s_matrix: get_S_matrix of the N=64, M=128 RBM over 16384 MC samples")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -454,6 +552,10 @@ def main():
     if args.workload == "serving" and args.impl == "ours":
         if rank == 0:
             run_serving(args)
+        return
+    if args.workload == "s_matrix" and args.impl == "ours":
+        if rank == 0:
+            run_smatrix(args)
         return
 
     if args.impl == "reference":

@@ -353,6 +353,9 @@ RBMG_API int rbmg_optimizer_step_energy(rbmg_optimizer* opt, rbmg_psi* psi, cons
 #define RBMG_S_WEIGHTED 1
 #define RBMG_S_CENTERED 2
 RBMG_API int rbmg_s_matrix(const rbmg_psi* psi, rbmg_ensemble* ens, int flags, double* out /* [2 P P] */);
+/* Extension: device time (CUDA events) of the last rbmg_s_matrix call's accumulation
+ * launches on this thread, and their number (the measurement hook of the benchmark). */
+RBMG_API int rbmg_s_matrix_timing(double* ms, int* launches);
 
 /* FP32 FMA throughput of the current device in TFLOP/s (a probe kernel of `iters`
  * x 128 independent FMAs per thread), the roofline denominator of the sampler. */

@@ -110,6 +110,7 @@ SIGNATURES = {
     "rbmg_optimizer_lookahead": [_vp, _dp, _dp],
     "rbmg_optimizer_step_energy": [_vp, _vp, _vp, _vp, C.c_double, _dp],
     "rbmg_s_matrix": [_vp, _vp, C.c_int, _dp],
+    "rbmg_s_matrix_timing": [_dp, _ip],
 }
 _RESTYPE = {"rbmg_last_error": C.c_char_p, "rbmg_version": C.c_char_p}
 

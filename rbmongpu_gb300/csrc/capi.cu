@@ -1477,6 +1477,9 @@ extern "C" int rbmg_psi_O_k_vector(const rbmg_psi* psi, const uint64_t* spins, d
 }
 
 // ====================================================================== persistent chains
+static thread_local double g_sm_timing_ms = 0.0;
+static thread_local int g_sm_timing_launches = 0;
+
 namespace rbmg {
 int deep_ok_rows(const rbmg_psi* psi, int count, const uint64_t* d_spins, uint64_t enum_base, int enumerate,
                  double2* rows, long ld, cudaStream_t st);
@@ -1504,6 +1507,21 @@ extern "C" int rbmg_s_matrix(const rbmg_psi* psi, rbmg_ensemble* ens, int flags,
     RBMG_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     uint64_t total = 0;
     StreamResult res;
+    // CUDA events around every accumulation launch (rbmg_s_matrix_timing)
+    std::vector<cudaEvent_t> ev;
+    auto mark = [&]() -> cudaError_t {
+        cudaEvent_t e;
+        cudaError_t err = cudaEventCreate(&e);
+        if (err != cudaSuccess) return err;
+        ev.push_back(e);
+        return cudaEventRecord(e, stream());
+    };
+    struct EvFree {
+        std::vector<cudaEvent_t>& v;
+        ~EvFree() {
+            for (auto e : v) cudaEventDestroy(e);
+        }
+    } ev_free{ev};
     const int r = run_stream(ens, psi, nullptr, false, 4096, &res, [&](const Chunk& c) -> int {
         total += static_cast<uint64_t>(c.count);
         SmSource a{};
@@ -1532,8 +1550,10 @@ extern "C" int rbmg_s_matrix(const rbmg_psi* psi, rbmg_ensemble* ens, int flags,
             a.spins = c.spins;
             a.T = W.Tp.as<float2>();
             a.w = c.weights;
+            RBMG_CK(mark());
             RBMG_CK(launch_sm_accumulate(a, W.smat.as<double2>(), centered ? W.smean.as<double2>() : nullptr, sms,
                                          stream()));
+            RBMG_CK(mark());
             return RBMG_OK;
         }
         // PsiDeep: FP64 O_k rows, in pieces of at most 256 MB
@@ -1551,8 +1571,10 @@ extern "C" int rbmg_s_matrix(const rbmg_psi* psi, rbmg_ensemble* ens, int flags,
             a.ld = L;
             a.w = c.weights ? c.weights + base : nullptr;
             a.weighted = weighted && a.w;
+            RBMG_CK(mark());
             RBMG_CK(launch_sm_accumulate(a, W.smat.as<double2>(), centered ? W.smean.as<double2>() : nullptr, sms,
                                          stream()));
+            RBMG_CK(mark());
         }
         return RBMG_OK;
     });
@@ -1565,6 +1587,21 @@ extern "C" int rbmg_s_matrix(const rbmg_psi* psi, rbmg_ensemble* ens, int flags,
     RBMG_CK(cudaMemcpy2DAsync(out + 2 * (static_cast<size_t>(2 * N) * P + 2 * N), sizeof(double2) * P, W.smat.p,
                               sizeof(double2) * L, sizeof(double2) * L, L, cudaMemcpyDeviceToHost, stream()));
     RBMG_CK(cudaStreamSynchronize(stream()));
+    double ms = 0.0;
+    for (size_t q = 0; q + 1 < ev.size(); q += 2) {
+        float t = 0.0f;
+        RBMG_CK(cudaEventElapsedTime(&t, ev[q], ev[q + 1]));
+        ms += t;
+    }
+    g_sm_timing_ms = ms;
+    g_sm_timing_launches = static_cast<int>(ev.size() / 2);
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_s_matrix_timing(double* ms, int* launches) {
+    if (!ms || !launches) return fail(RBMG_EINVAL, "S_matrix timing: null");
+    *ms = g_sm_timing_ms;
+    *launches = g_sm_timing_launches;
     return RBMG_OK;
 }
 
