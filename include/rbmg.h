@@ -186,6 +186,19 @@ RBMG_API int rbmg_ev_eloc_gradient(const rbmg_psi* psi, const rbmg_operator* op,
  * pyRBMonGPU/main.cpp:342-418).  The ensemble samples psi. */
 RBMG_API int rbmg_hsd_distance(const rbmg_psi* psi, const rbmg_psi* psi_prime, const rbmg_operator* op, int is_unitary,
                       rbmg_ensemble* ens, double* distance);
+/* distance_2nd_order (source/network_functions/HilbertSpaceDistance_2nd_order.cu:69-95,
+ * pyRBMonGPU/main.cpp:352-363 builds op = Operator(expr) and op2 = Operator(expr * expr)):
+ * the distance between exp(A) psi, expanded to second order, and psi_prime, with
+ * omega_s = exp(E_A + (E_A2 - E_A^2) / 2 + conj(log psi' - log psi)). */
+RBMG_API int rbmg_hsd_distance_2nd_order(const rbmg_psi* psi, const rbmg_psi* psi_prime, const rbmg_operator* op,
+                                         const rbmg_operator* op2, rbmg_ensemble* ens, double* distance);
+/* DiagDensityOp(sub_system_size, gpu)(psi, op, spin_ensemble) (pyRBMonGPU/main.cpp:497-533,
+ * source/network_functions/DiagDensityOp.cu:12-50): out [2^sub_system_size] =
+ * <|E_loc|^2 binned by the configuration of the first sub_system_size spins>, each bin's
+ * weighted sum over num_steps.  Psi, PsiDeep and PsiPair, both ensembles (the reference
+ * instantiates PsiDeep and PsiExact); sub_system_size <= min(N, 30). */
+RBMG_API int rbmg_diag_density(const rbmg_psi* psi, const rbmg_operator* op, rbmg_ensemble* ens,
+                               int sub_system_size, double* out);
 RBMG_API int rbmg_hsd_gradient(const rbmg_psi* psi, const rbmg_psi* psi_prime, const rbmg_operator* op, int is_unitary,
                       rbmg_ensemble* ens, float nu, double* grad /* [2 P'] */, double* distance);
 

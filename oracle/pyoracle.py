@@ -192,11 +192,42 @@ def s_matrix(psi, spins, weights=None, centered=False):
     O = np.array([O_k(psi, s) for s in np.asarray(spins, np.uint64)])
     c = np.ones(len(O)) if weights is None else np.asarray(weights, np.float64)
     c = c / c.sum()
-    S = np.einsum("s,sk,sl->kl", c, O, O.conj())
-    if centered:
-        m = c @ O
-        S = S - np.outer(m, m.conj())
-    return S
+    if centered:   # rows centred first: the covariance is not the difference of two large sums
+        O = O - c @ O
+    return np.einsum("s,sk,sl->kl", c, O, O.conj())
+
+
+def hsd_2nd_order(psi, psi_prime, op, op2, spins, weights=None):
+    """distance_2nd_order (source/network_functions/HilbertSpaceDistance_2nd_order.cu:14-95)
+    over the configurations `spins` with weights (exact summation: prefactor^2 |psi|^2;
+    None: 1 per sample, Monte Carlo)."""
+    om = np.zeros(len(spins), complex)
+    nn = np.zeros(len(spins))
+    pr = np.zeros(len(spins))
+    for n, s in enumerate(np.asarray(spins, np.uint64)):
+        lp, lpp = log_psi(psi, s), log_psi(psi_prime, s)
+        e1, e2 = local_energy(psi, op, s, lp), local_energy(psi, op2, s, lp)
+        x = e1 + 0.5 * (e2 - e1 * e1)
+        om[n] = np.exp(x + np.conj(lpp - lp))
+        nn[n] = np.exp(2.0 * x.real)
+        pr[n] = np.exp(2.0 * (lpp - lp).real)
+    w = np.ones(len(spins)) if weights is None else np.asarray(weights, np.float64)
+    o, a, b = (w * om).sum(), (w * nn).sum(), (w * pr).sum()
+    return np.sqrt(1.0 - abs(o) ** 2 / (a * b))
+
+
+def diag_density(psi, op, spins, na, weights=None):
+    """DiagDensityOp (source/network_functions/DiagDensityOp.cu:12-50): sum of
+    weight |E_loc|^2 per configuration of the first na spins; weights None: 1 per sample
+    and the sums divided by the sample count (Monte Carlo), else the exact-summation
+    weights prefactor^2 |psi|^2."""
+    out = np.zeros(1 << na)
+    sp = np.asarray(spins, np.uint64)
+    for n, s in enumerate(sp):
+        e = local_energy(psi, op, s)
+        w = 1.0 if weights is None else weights[n]
+        out[int(s[0]) & ((1 << na) - 1)] += w * abs(e) ** 2
+    return out / len(sp) if weights is None else out
 
 
 def local_energy(psi, op, spins, lp=None):

@@ -16,7 +16,7 @@ UNITS="Array RNGStates quantum_state/Psi quantum_state/PsiDeep quantum_state/Psi
  spin_ensembles/MonteCarloLoop spin_ensembles/ExactSummation operator/Operator \
  network_functions/ExpectationValue network_functions/PsiNorm network_functions/HilbertSpaceDistance \
  network_functions/HilbertSpaceDistance_PsiPair network_functions/PsiVector network_functions/PsiOkVector \
- network_functions/S_matrix"
+ network_functions/S_matrix network_functions/HilbertSpaceDistance_2nd_order network_functions/DiagDensityOp"
 pids=""
 for u in $UNITS; do
   o="$OUT/obj/$(echo "$u" | tr / _).o"

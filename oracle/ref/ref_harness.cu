@@ -15,6 +15,7 @@
 #include "network_functions/PsiVector.hpp"
 #include "network_functions/PsiOkVector.hpp"
 #include "network_functions/S_matrix.hpp"
+#include "network_functions/DiagDensityOp.hpp"
 
 #include <complex>
 #include <cstdio>
@@ -239,6 +240,24 @@ int main(int argc, char** argv) {
         if (meta_i("exact", 0)) exact_outputs(psi, psi_prime, op, N, P);
         if (meta_i("ok", 0)) ok_vectors(psi, P);
         if (meta_i("mc_samples", 0)) mc_outputs(psi, op, N, P);
+        if (meta_i("hsd2", 0)) {
+            // HilbertSpaceDistance::distance_2nd_order (HilbertSpaceDistance_2nd_order.cu:69-95)
+            const auto op_a = load_operator("h2a_");
+            const auto op_b = load_operator("h2b_");
+            ExactSummation es(static_cast<unsigned>(N), false);
+            HilbertSpaceDistance hsd(static_cast<unsigned>(N), static_cast<unsigned>(P), false);
+            scalar("hsd2_distance", hsd.distance_2nd_order(psi, psi_prime, op_a, op_b, es));
+        }
+        if (meta_i("diag_density", 0)) {
+            // DiagDensityOp::operator() (source/network_functions/DiagDensityOp.cu:12-50)
+            const unsigned na = static_cast<unsigned>(meta_i("diag_density"));
+            ExactSummation es(static_cast<unsigned>(N), false);
+            DiagDensityOp dd(na, false);
+            dd(psi, op, es);
+            std::vector<double> v(1u << na);
+            for (size_t q = 0; q < v.size(); q++) v[q] = dd.diag_densities_ar[q];
+            save("diag_density", v.data(), v.size());
+        }
     } else if (kind == "pair") {
         PsiPair psi = load_deep<PsiPair>("", N);
         PsiPair psi_prime = load_deep<PsiPair>("pp_", N);

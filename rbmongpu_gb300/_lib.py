@@ -111,6 +111,8 @@ SIGNATURES = {
     "rbmg_optimizer_step_energy": [_vp, _vp, _vp, _vp, C.c_double, _dp],
     "rbmg_s_matrix": [_vp, _vp, C.c_int, _dp],
     "rbmg_s_matrix_timing": [_dp, _ip],
+    "rbmg_hsd_distance_2nd_order": [_vp, _vp, _vp, _vp, _vp, _dp],
+    "rbmg_diag_density": [_vp, _vp, _vp, C.c_int, _dp],
 }
 _RESTYPE = {"rbmg_last_error": C.c_char_p, "rbmg_version": C.c_char_p}
 

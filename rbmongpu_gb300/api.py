@@ -559,12 +559,46 @@ class HilbertSpaceDistance:
              C.byref(d))
         return d.value
 
+    def distance_2nd_order(self, psi, psi_prime, expr, spin_ensemble, expr_squared=None):
+        """distance_2nd_order (pyRBMonGPU/main.cpp:352-363): the reference builds
+        Operator(expr) and Operator(expr * expr) from a PauliExpression; here ``expr`` is an
+        Operator (or anything Operator accepts) and its square is formed from its Pauli
+        tables (``operators.product``) unless given."""
+        from . import operators
+
+        def as_op(x):
+            if isinstance(x, Operator):
+                return x
+            return Operator(*x) if isinstance(x, (tuple, list)) else Operator(x)
+        op = as_op(expr)
+        if expr_squared is None:
+            t = (op.coefficients, op.pauli_types, op.pauli_indices)
+            expr_squared = Operator(*operators.product(t, t))
+        op2 = as_op(expr_squared)
+        d = C.c_double()
+        call("rbmg_hsd_distance_2nd_order", psi._h, psi_prime._h, op._h, op2._h, spin_ensemble._h, C.byref(d))
+        return d.value
+
     def gradient(self, psi, psi_prime, operator_, is_unitary, spin_ensemble, nu=1.0):
         g = np.zeros(psi_prime.num_params, np.complex128)
         d = C.c_double()
         call("rbmg_hsd_gradient", psi._h, psi_prime._h, operator_._h, int(bool(is_unitary)), spin_ensemble._h,
              C.c_float(nu), _p(g.view(np.float64)), C.byref(d))
         return g, d.value
+
+
+class DiagDensityOp:
+    """DiagDensityOp(sub_system_size, gpu) (pyRBMonGPU/main.cpp:497-533): called with
+    (psi, operator_, spin_ensemble) it returns the 2^sub_system_size densities
+    <|E_loc|^2> binned by the configuration of the first sub_system_size spins."""
+
+    def __init__(self, sub_system_size, gpu=True):
+        self.sub_system_size = int(sub_system_size)
+
+    def __call__(self, psi, operator_, spin_ensemble):
+        out = np.zeros(1 << self.sub_system_size)
+        call("rbmg_diag_density", psi._h, operator_._h, spin_ensemble._h, self.sub_system_size, _p(out))
+        return out
 
 
 def psi_O_k_vector(psi, spins):

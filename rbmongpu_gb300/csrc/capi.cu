@@ -52,7 +52,7 @@ int deep_log_psi(const rbmg_psi* psi, int count, const uint64_t* d_spins, uint64
 struct Workspace {
     DevBuf sample_spins, eloc, logpsi, logpsi_p, T, U, X, Tp, weights, coef1, coef2, coef3, omega, pr, nn;
     DevBuf partial, block_scratch, sums, acc_O, acc_EO, acc_Ek, acc_wO, acc_pO, block_max, zsum;
-    DevBuf smat, smean, okrows;
+    DevBuf smat, smean, okrows, sshift;
 };
 
 static Workspace& ws() {
@@ -1383,6 +1383,105 @@ extern "C" int rbmg_hsd_gradient(const rbmg_psi* psi, const rbmg_psi* pp, const 
     return RBMG_OK;
 }
 
+// DiagDensityOp(sub_system_size)(psi, op, ensemble) (source/network_functions/DiagDensityOp.cu:
+// 12-50): densities [2^N_A] = sum_s weight |E_loc(s)|^2 binned by the first N_A spins, over
+// num_steps (the reference's local_energy1 * conj(local_energy2) of one operator)
+extern "C" int rbmg_diag_density(const rbmg_psi* psi, const rbmg_operator* op, rbmg_ensemble* ens,
+                                 int sub_system_size, double* out) {
+    if (!out) return fail(RBMG_EINVAL, "DiagDensityOp: null");
+    int r = check_pair(psi, op, ens);
+    if (r != RBMG_OK) return r;
+    if (sub_system_size < 0 || sub_system_size > std::min(psi->N, 30))
+        return fail(RBMG_EINVAL, "DiagDensityOp: sub_system_size must lie in [0, min(N, 30)]");
+    const int na = sub_system_size, bins = 1 << na, nw = nwords_of(psi->N);
+    Workspace& W = ws();
+    RBMG_CK(W.coef3.ensure(sizeof(double) * bins));
+    RBMG_CK(cudaMemsetAsync(W.coef3.p, 0, sizeof(double) * bins, stream()));
+    StreamResult res;
+    r = run_stream(ens, psi, op, true, size_t(1) << 20, &res, [&](const Chunk& c) -> int {
+        const double2* e = nullptr;
+        const int rr = chunk_eloc(psi, op, c, &e);
+        if (rr != RBMG_OK) return rr;
+        RBMG_CK(launch_diag_density(c.count, c.enumerate, c.enum_base, c.spins, nw, c.weights, e, na,
+                                    W.coef3.as<double>(), stream()));
+        return RBMG_OK;
+    });
+    if (r != RBMG_OK) return r;
+    RBMG_CK(cudaMemcpyAsync(out, W.coef3.p, sizeof(double) * bins, cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaStreamSynchronize(stream()));
+    for (int i = 0; i < bins; i++) out[i] *= res.norm_factor;
+    return RBMG_OK;
+}
+
+// HilbertSpaceDistance::distance_2nd_order (source/network_functions/HilbertSpaceDistance_2nd_order.cu:
+// 14-95): the distance to psi' of the state exp(A) psi expanded to second order, with the
+// local energies of A (op) and of A^2 (op2) in FP64
+extern "C" int rbmg_hsd_distance_2nd_order(const rbmg_psi* psi, const rbmg_psi* pp, const rbmg_operator* op,
+                                           const rbmg_operator* op2, rbmg_ensemble* ens, double* distance) {
+    if (!pp || !op || !op2 || !distance) return fail(RBMG_EINVAL, "hsd 2nd order: null");
+    int r = check_pair(psi, op, ens);
+    if (r == RBMG_OK) r = check_pair(psi, op2, ens);
+    if (r != RBMG_OK) return r;
+    if (pp->N != psi->N) return fail(RBMG_EINVAL, "hsd 2nd order: psi and psi_prime differ in N");
+    if (psi->kind != pp->kind) return fail(RBMG_EUNSUPPORTED, "hsd 2nd order: psi and psi_prime must be of the same kind");
+    if (psi->kind == 2) return fail(RBMG_EUNSUPPORTED, "hsd 2nd order: not instantiated for PsiPair");
+    if (psi->kind == 0) {
+        r = rbm_upload64(psi);
+        if (r == RBMG_OK) r = rbm_upload64(pp);
+        if (r != RBMG_OK) return r;
+    }
+    Workspace& W = ws();
+    RBMG_CK(W.sums.ensure(sizeof(double2) * kMaxSeries));
+    RBMG_CK(W.block_scratch.ensure(sizeof(double2) * kSumBlocks * kMaxSeries));
+    RBMG_CK(cudaMemsetAsync(W.sums.p, 0, sizeof(double2) * kMaxSeries, stream()));
+    const OpDev od = op->dev(), od2 = op2->dev();
+    StreamResult res;
+    r = run_stream(ens, psi, op, false, size_t(1) << 20, &res, [&](const Chunk& c) -> int {
+        RBMG_CK(W.eloc.ensure(sizeof(double2) * c.count));
+        RBMG_CK(W.coef2.ensure(sizeof(double2) * c.count));
+        RBMG_CK(W.logpsi_p.ensure(sizeof(double2) * c.count));
+        RBMG_CK(W.omega.ensure(sizeof(double2) * c.count));
+        RBMG_CK(W.pr.ensure(sizeof(double2) * c.count));
+        RBMG_CK(W.nn.ensure(sizeof(double2) * c.count));
+        for (int which = 0; which < 2; which++) {
+            double2* e = which == 0 ? W.eloc.as<double2>() : W.coef2.as<double2>();
+            if (psi->kind == 0) {
+                Hsd64Launch L{};
+                L.count = c.count;
+                L.enum_base = c.enum_base;
+                L.enumerate = c.enumerate;
+                L.spins = c.spins;
+                L.eloc = e;
+                L.dlogpsi = W.logpsi_p.as<double2>();
+                RBMG_CK(launch_rbm_hsd64(rbm64(psi), rbm64(pp), which == 0 ? od : od2, L, stream()));
+            } else {
+                const int rr = deep_hsd64_chunk(psi, pp, which == 0 ? op : op2, c, e, W.logpsi_p.as<double2>(),
+                                                stream());
+                if (rr != RBMG_OK) return rr;
+            }
+        }
+        RBMG_CK(launch_hsd2_terms64(c.count, W.eloc.as<double2>(), W.coef2.as<double2>(), W.logpsi_p.as<double2>(),
+                                    W.omega.as<double2>(), W.pr.as<double2>(), W.nn.as<double2>(), stream()));
+        SeriesSet set{};
+        set.n = 3;
+        set.v[0] = W.omega.as<double2>();
+        set.v[1] = W.pr.as<double2>();
+        set.v[2] = W.nn.as<double2>();
+        RBMG_CK(launch_weighted_sums(c.count, c.weights, set, W.block_scratch.as<double2>(), W.sums.as<double2>(),
+                                     stream()));
+        return RBMG_OK;
+    });
+    if (r != RBMG_OK) return r;
+    double2 s3[3];
+    RBMG_CK(cudaMemcpyAsync(s3, W.sums.p, sizeof(s3), cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaStreamSynchronize(stream()));
+    const double f = res.norm_factor;   // HilbertSpaceDistance_2nd_order.cu:83-94
+    const cplx omega = cplx(s3[0].x, s3[0].y) * f;
+    const double pr = s3[1].x * f, nn = s3[2].x * f;
+    *distance = std::sqrt(1.0 - std::norm(omega) / (nn * pr));
+    return RBMG_OK;
+}
+
 extern "C" int rbmg_hsd_distance(const rbmg_psi* psi, const rbmg_psi* pp, const rbmg_operator* op, int is_unitary,
                                  rbmg_ensemble* ens, double* distance) {
     return rbmg_hsd_gradient(psi, pp, op, is_unitary, ens, 1.0f, nullptr, distance);
@@ -1507,6 +1606,20 @@ extern "C" int rbmg_s_matrix(const rbmg_psi* psi, rbmg_ensemble* ens, int flags,
     RBMG_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     uint64_t total = 0;
     StreamResult res;
+    // centred: every row is shifted by the first chunk's mean row (in FP64) before the FP32
+    // products, so that the covariance is not the small difference of two large sums
+    RBMG_CK(W.sshift.ensure(sizeof(double2) * L));
+    bool have_shift = false;
+    auto with_shift = [&](SmSource& a) -> cudaError_t {
+        if (!centered) return cudaSuccess;
+        if (!have_shift) {
+            const cudaError_t e = launch_sm_row_mean(a, W.sshift.as<double2>(), stream());
+            if (e != cudaSuccess) return e;
+            have_shift = true;
+        }
+        a.shift = W.sshift.as<double2>();
+        return cudaSuccess;
+    };
     // CUDA events around every accumulation launch (rbmg_s_matrix_timing)
     std::vector<cudaEvent_t> ev;
     auto mark = [&]() -> cudaError_t {
@@ -1550,6 +1663,7 @@ extern "C" int rbmg_s_matrix(const rbmg_psi* psi, rbmg_ensemble* ens, int flags,
             a.spins = c.spins;
             a.T = W.Tp.as<float2>();
             a.w = c.weights;
+            RBMG_CK(with_shift(a));
             RBMG_CK(mark());
             RBMG_CK(launch_sm_accumulate(a, W.smat.as<double2>(), centered ? W.smean.as<double2>() : nullptr, sms,
                                          stream()));
@@ -1571,6 +1685,7 @@ extern "C" int rbmg_s_matrix(const rbmg_psi* psi, rbmg_ensemble* ens, int flags,
             a.ld = L;
             a.w = c.weights ? c.weights + base : nullptr;
             a.weighted = weighted && a.w;
+            RBMG_CK(with_shift(a));
             RBMG_CK(mark());
             RBMG_CK(launch_sm_accumulate(a, W.smat.as<double2>(), centered ? W.smean.as<double2>() : nullptr, sms,
                                          stream()));

@@ -110,6 +110,9 @@ int psi_scatter(rbmg_psi* psi, const double2* packed);
 // capi.cu: the energy gradient formed on the device, d_grad [P]; energy to value[2]
 int ev_gradient_device(const rbmg_psi* psi, const rbmg_operator* op, rbmg_ensemble* ens, double2* d_grad,
                        double* value);
+// density.cu: out [2^na] += w_s |eloc_s|^2 at the bin of the first na spins
+cudaError_t launch_diag_density(int count, int enumerate, uint64_t enum_base, const uint64_t* spins, int nw,
+                                const double* w, const double2* eloc, int na, double* out, cudaStream_t st);
 cudaError_t launch_grad_final(const double2* O, const double2* EO, const double2* Ek, const double2* sums,
                               double norm, double2 E0, int first, long count, double2* grad, cudaStream_t st);
 }  // namespace rbmg

@@ -197,6 +197,30 @@ cudaError_t launch_rbm_hsd64(const Rbm64& P, const Rbm64& PP, const OpDev& op, c
     return cudaGetLastError();
 }
 
+// second order (HilbertSpaceDistance_2nd_order.cu:44-60): x = E1 + (E2 - E1^2) / 2,
+// omega = exp(x + conj(log psi' - log psi)), norm = exp(2 Re x), ratio = exp(2 Re(log psi' - log psi))
+__global__ void hsd2_terms64_kernel(int count, const double2* __restrict__ e1, const double2* __restrict__ e2,
+                                    const double2* __restrict__ dl, double2* omega, double2* pr, double2* nn) {
+    for (long s = blockIdx.x * 256L + threadIdx.x; s < count; s += static_cast<long>(gridDim.x) * 256) {
+        const double2 a = e1[s], b = e2[s];
+        const double xr = a.x + 0.5 * (b.x - (a.x * a.x - a.y * a.y));
+        const double xi = a.y + 0.5 * (b.y - 2.0 * a.x * a.y);
+        const double m = exp(xr + dl[s].x);
+        const double ph = xi - dl[s].y;
+        omega[s] = make_double2(m * cos(ph), m * sin(ph));
+        nn[s] = make_double2(exp(2.0 * xr), 0.0);
+        pr[s] = make_double2(exp(2.0 * dl[s].x), 0.0);
+    }
+}
+
+cudaError_t launch_hsd2_terms64(int count, const double2* e1, const double2* e2, const double2* dl, double2* omega,
+                                double2* pr, double2* nn, cudaStream_t st) {
+    if (count <= 0) return cudaSuccess;
+    const int blocks = std::min((count + 255) / 256, 4096);
+    hsd2_terms64_kernel<<<blocks, 256, 0, st>>>(count, e1, e2, dl, omega, pr, nn);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_hsd_terms64(int count, const double2* eloc, const double2* dl, int is_unitary, double2* omega,
                                double2* pr, double2* nn, cudaStream_t st) {
     if (count <= 0) return cudaSuccess;

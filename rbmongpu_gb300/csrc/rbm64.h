@@ -29,6 +29,8 @@ cudaError_t launch_rbm_hsd64(const Rbm64& P, const Rbm64& PP, const OpDev& op, c
                              cudaStream_t st);
 cudaError_t launch_hsd_terms64(int count, const double2* eloc, const double2* dl, int is_unitary, double2* omega,
                                double2* pr, double2* nn, cudaStream_t st);
+cudaError_t launch_hsd2_terms64(int count, const double2* e1, const double2* e2, const double2* dl, double2* omega,
+                                double2* pr, double2* nn, cudaStream_t st);
 // mode 0: w B_s, mode 1: w Re B_s, mode 2: w Im(conj(<omega>) omega_s), each times scale
 // (the host folds the final 1/v^2 / d^nu into scale so the FP32 reduction stays in range)
 cudaError_t launch_hsd_coef(int count, const double* w, const double2* omega, const double2* pr,

@@ -38,21 +38,27 @@ __device__ __forceinline__ Elem elem_of(const SmSource& a, int k) {
     return e;
 }
 
-// sqrt(w_s) F[s][k] (or F[s][k] unweighted), zero outside the matrix
-__device__ __forceinline__ float2 load_f(const SmSource& a, const Elem& e, int s) {
+// sqrt(w_s) (F[s][k] - shift[k]) (weight 1 unweighted), zero outside the matrix; the
+// shift is subtracted in FP64 so that a centred matrix keeps the rows' small spread
+__device__ __forceinline__ float2 load_f(const SmSource& a, const Elem& e, int s, int k) {
     if (!e.live || s >= a.count) return make_float2(0.0f, 0.0f);
-    float2 v;
+    double2 d;
     if (a.kind == 0) {
-        v = a.T[static_cast<long>(s) * a.Mpad + e.j];
+        const float2 t = a.T[static_cast<long>(s) * a.Mpad + e.j];
+        d = make_double2(t.x, t.y);
         if (e.i >= 0) {
             const uint64_t word = a.enumerate ? ((e.i >> 6) == 0 ? a.enum_base + static_cast<uint64_t>(s) : 0ull)
                                               : a.spins[static_cast<long>(s) * a.nw + (e.i >> 6)];
-            if (!((word >> (e.i & 63)) & 1ull)) v = make_float2(-v.x, -v.y);
+            if (!((word >> (e.i & 63)) & 1ull)) d = make_double2(-d.x, -d.y);
         }
     } else {
-        const double2 d = a.rows[static_cast<long>(s) * a.ld + e.j];
-        v = make_float2(static_cast<float>(d.x), static_cast<float>(d.y));
+        d = a.rows[static_cast<long>(s) * a.ld + e.j];
     }
+    if (a.shift) {
+        d.x -= a.shift[k].x;
+        d.y -= a.shift[k].y;
+    }
+    float2 v = make_float2(static_cast<float>(d.x), static_cast<float>(d.y));
     if (a.weighted) {
         const float c = static_cast<float>(sqrt(a.w[s]));
         v.x *= c;
@@ -88,8 +94,8 @@ __global__ void __launch_bounds__(256) sm_herk_kernel(SmSource a, double2* __res
         float2 pa[4], pb[4];
 #pragma unroll
         for (int q = 0; q < 4; q++) {
-            pa[q] = f0 + ty < f1 ? load_f(a, ea[q], f0 + ty) : make_float2(0.0f, 0.0f);
-            pb[q] = f0 + ty < f1 ? load_f(a, eb[q], f0 + ty) : make_float2(0.0f, 0.0f);
+            pa[q] = f0 + ty < f1 ? load_f(a, ea[q], f0 + ty, m0 + tx + 16 * q) : make_float2(0.0f, 0.0f);
+            pb[q] = f0 + ty < f1 ? load_f(a, eb[q], f0 + ty, n0 + tx + 16 * q) : make_float2(0.0f, 0.0f);
         }
         for (int s0 = f0; s0 < f1; s0 += kS) {
             __syncthreads();
@@ -102,8 +108,8 @@ __global__ void __launch_bounds__(256) sm_herk_kernel(SmSource a, double2* __res
             const int sn = s0 + kS + ty;   // next stage's sample of this thread, loaded during the products
 #pragma unroll
             for (int q = 0; q < 4; q++) {
-                pa[q] = sn < f1 ? load_f(a, ea[q], sn) : make_float2(0.0f, 0.0f);
-                pb[q] = sn < f1 ? load_f(a, eb[q], sn) : make_float2(0.0f, 0.0f);
+                pa[q] = sn < f1 ? load_f(a, ea[q], sn, m0 + tx + 16 * q) : make_float2(0.0f, 0.0f);
+                pb[q] = sn < f1 ? load_f(a, eb[q], sn, n0 + tx + 16 * q) : make_float2(0.0f, 0.0f);
             }
 #pragma unroll
             for (int s = 0; s < kS; s++) {
@@ -145,8 +151,8 @@ __global__ void __launch_bounds__(256) sm_herk_kernel(SmSource a, double2* __res
     }
 }
 
-// mean[k] += sum_s w_s F[s][k] (FP64)
-__global__ void sm_mean_kernel(SmSource a, double2* mean) {
+// mean[k] += sum_s w_s (F[s][k] - shift[k]) (FP64); assign: mean[k] = the sum * scale
+__global__ void sm_mean_kernel(SmSource a, double2* mean, int assign, double scale) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= a.L) return;
     SmSource u = a;
@@ -154,17 +160,22 @@ __global__ void sm_mean_kernel(SmSource a, double2* mean) {
     const Elem e = elem_of(u, k);
     double sr = 0.0, si = 0.0;
     for (int s = 0; s < a.count; s++) {
-        const float2 v = load_f(u, e, s);
+        const float2 v = load_f(u, e, s, k);
         const double c = a.weighted ? a.w[s] : 1.0;
         sr += c * v.x;
         si += c * v.y;
     }
-    mean[k].x += sr;
-    mean[k].y += si;
+    if (assign) {
+        mean[k] = make_double2(sr * scale, si * scale);
+    } else {
+        mean[k].x += sr;
+        mean[k].y += si;
+    }
 }
 
 // S <- S / Z with the lower triangle mirrored from the upper and a real diagonal;
-// centred: - m m^dagger with m = mean / Z
+// centred: - m m^dagger with m = mean / Z (mean of the shifted rows: the covariance does
+// not depend on the shift)
 __global__ void sm_finish_kernel(int L, double2* S, const double2* mean, double inv_z, int centered) {
     const long idx = static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (idx >= static_cast<long>(L) * L) return;
@@ -203,7 +214,15 @@ cudaError_t launch_sm_accumulate(const SmSource& a, double2* S, double2* mean, i
     sm_herk_kernel<<<grid, 256, 0, st>>>(a, S, nt, slice, split > 1);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || !mean) return e;
-    sm_mean_kernel<<<(a.L + 127) / 128, 128, 0, st>>>(a, mean);
+    sm_mean_kernel<<<(a.L + 127) / 128, 128, 0, st>>>(a, mean, 0, 1.0);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sm_row_mean(const SmSource& a, double2* out, cudaStream_t st) {
+    SmSource u = a;
+    u.weighted = 0;
+    u.shift = nullptr;
+    sm_mean_kernel<<<(a.L + 127) / 128, 128, 0, st>>>(u, out, 1, 1.0 / static_cast<double>(a.count));
     return cudaGetLastError();
 }
 

@@ -20,11 +20,14 @@ struct SmSource {
     long ld;
     const double* w;         // per-sample weights (exact summation), used when weighted
     int weighted;
+    const double2* shift;    // [L] subtracted from every row before the products, or null
 };
 
-// S [L][L] += sum_s c_s F_s^T conj(F_s) on the upper tiles (c_s = w_s when weighted, else
-// 1); mean [L] += sum_s c_s F_s when mean is not null
+// S [L][L] += sum_s c_s G_s^T conj(G_s) on the upper tiles, G_s = F_s - shift (c_s = w_s
+// when weighted, else 1); mean [L] += sum_s c_s G_s when mean is not null
 cudaError_t launch_sm_accumulate(const SmSource& src, double2* S, double2* mean, int num_sms, cudaStream_t st);
+// out [L] = sum_s F_s / count (unweighted, unshifted): the shift of a centred S matrix
+cudaError_t launch_sm_row_mean(const SmSource& src, double2* out, cudaStream_t st);
 // S /= Z, lower triangle mirrored; centred: S -= (mean / Z)(mean / Z)^dagger
 cudaError_t launch_sm_finish(int L, double2* S, const double2* mean, double inv_z, int centered, cudaStream_t st);
 

@@ -62,3 +62,61 @@ def identity():
 def scaled(op, factor):
     coef, types, idx = op
     return np.asarray(coef) * factor, types, idx
+
+
+# single-site Pauli products: _MUL[a][b] = (phase, c) with sigma_a sigma_b = phase sigma_c
+_MUL = [[(1, I), (1, X), (1, Y), (1, Z)],
+        [(1, X), (1, I), (1j, Z), (-1j, Y)],
+        [(1, Y), (-1j, Z), (1, I), (1j, X)],
+        [(1, Z), (1j, Y), (-1j, X), (1, I)]]
+
+
+def _strings(op):
+    """(coefficient, {site: pauli}) per row, repeated sites multiplied in row order."""
+    coef, types, idx = op
+    out = []
+    for n in range(len(coef)):
+        c, sites = complex(coef[n]), {}
+        for t, i in zip(types[n], idx[n]):
+            if i < 0:
+                break
+            if t == I:
+                continue
+            ph, r = _MUL[sites.get(int(i), I)][int(t)]
+            c *= ph
+            if r == I:
+                sites.pop(int(i), None)
+            else:
+                sites[int(i)] = r
+        out.append((c, sites))
+    return out
+
+
+def _merge(terms):
+    acc = {}
+    for c, sites in terms:
+        key = tuple(sorted(sites.items()))
+        acc[key] = acc.get(key, 0) + c
+    keys = [k for k, v in acc.items() if v != 0]
+    if not keys:
+        return identity()[0] * 0, identity()[1], identity()[2]
+    return table([[(t, i) for i, t in k] for k in keys], [acc[k] for k in keys])
+
+
+def product(op_a, op_b):
+    """The operator product A B of two operator tables (the reference multiplies
+    QuantumExpression objects, e.g. expr * expr for the second-order distance), equal
+    strings merged, sites in ascending order."""
+    terms = []
+    for ca, sa in _strings(op_a):
+        for cb, sb in _strings(op_b):
+            c, sites = ca * cb, dict(sa)
+            for i, t in sb.items():
+                ph, r = _MUL[sites.get(i, I)][t]
+                c *= ph
+                if r == I:
+                    sites.pop(i, None)
+                else:
+                    sites[i] = r
+            terms.append((c, sites))
+    return _merge(terms)

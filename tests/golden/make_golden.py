@@ -159,7 +159,8 @@ def rbm_case(name, N, M, sigma, seed, op, hop, unitary, nu, mc=None, normalize=T
     run_case(name, meta, arrays, keep={k.replace(".bin", "") for k in arrays})
 
 
-def deep_case(name, kind, N, sizes, conns, sigma, seed, op, hop, unitary, nu, mc=None, dense=False):
+def deep_case(name, kind, N, sizes, conns, sigma, seed, op, hop, unitary, nu, mc=None, dense=False, hsd2=None,
+              diag_density=0):
     rng = np.random.Generator(np.random.PCG64(seed))
     if dense:
         conn = [np.tile(np.arange(c, dtype=np.uint32)[:, None], (1, m)) for c, m in zip(conns, sizes)]
@@ -187,6 +188,17 @@ def deep_case(name, kind, N, sizes, conns, sigma, seed, op, hop, unitary, nu, mc
         meta.update(mc)
     arrays.update(op_arrays("op_", op))
     arrays.update(op_arrays("hop_", hop))
+    if diag_density:
+        meta["diag_density"] = diag_density    # DiagDensityOp(sub_system_size) with op_
+    if hsd2 is not None:
+        # the second-order distance's operator and its square (the reference's expr and
+        # expr * expr), the square formed by rbmongpu_gb300.operators.product
+        if REPO not in sys.path:
+            sys.path.insert(0, REPO)
+        from rbmongpu_gb300.operators import product
+        meta["hsd2"] = 1
+        arrays.update(op_arrays("h2a_", hsd2))
+        arrays.update(op_arrays("h2b_", product(hsd2, hsd2)))
     run_case(name, meta, arrays, keep={k.replace(".bin", "") for k in arrays})
 
 
@@ -224,6 +236,12 @@ def main():
               True, 1.0)
     # get_S_matrix of a small RBM over ExactSummation (the reference's only instantiation)
     rbm_case("rbm6_smatrix", 6, 12, 0.3, 13, tfim_chain(6, 1.0, 1.0), identity_op(), True, 1.0, smatrix=True)
+    # second-order distance (PsiDeep with ExactSummation, its only instantiation) for the
+    # step generator -i t H, t = 0.02, of the periodic TFIM chain; DiagDensityOp of the
+    # first 3 spins with the chain Hamiltonian
+    cf, ty, ix = tfim_chain(6, 1.0, 1.0)
+    deep_case("deep6_hsd2", "deep", 6, [12, 6], [3, 4], 0.2, 106, tfim_chain(6), identity_op(), True, 1.0,
+              hsd2=(-0.02j * cf, ty, ix), diag_density=3)
     # PsiPair 3 -> [9, 6] connectivity [1, 3] (the reference's test fixture)
     deep_case("pair3", "pair", 3, [9, 6], [1, 3], 0.3, 105, tfim_chain(3), identity_op(), True, 1.0)
 

@@ -85,7 +85,7 @@ def test_exact_deep_vs_restatement(weighted):
     opsi = po.Deep(c.N, b, cn, w, fw, c.prefactor)
     S = rg.get_S_matrix(psi, rg.ExactSummation(c.N), weighted=weighted, centered=weighted)
     ref = po.s_matrix(opsi, all_states(c.N), exact_weights(opsi, c.N) if weighted else None, weighted)
-    assert rel(S, ref) < 1e-9     # FP64 rows, FP32 products
+    assert rel(S, ref) < RTOL     # FP64 rows (centred in FP64), FP32 products
 
 
 @gpu
@@ -102,8 +102,8 @@ def test_monte_carlo_ragged_size_vs_restatement():
     sp, _, _ = mk().samples(psi)
     S = rg.get_S_matrix(psi, mk(), centered=True)
     O = np.array([po.O_k(po.RBM(b, W, 1.0), s) for s in sp])
-    m = O.mean(axis=0)
-    ref = O.T @ O.conj() / len(O) - np.outer(m, m.conj())
+    O = O - O.mean(axis=0)
+    ref = O.T @ O.conj() / len(O)
     assert rel(S, ref) < RTOL
     assert np.abs(S - S.conj().T).max() == 0.0
 
