@@ -199,6 +199,14 @@ RBMG_API int rbmg_hsd_distance_2nd_order(const rbmg_psi* psi, const rbmg_psi* ps
  * instantiates PsiDeep and PsiExact); sub_system_size <= min(N, 30). */
 RBMG_API int rbmg_diag_density(const rbmg_psi* psi, const rbmg_operator* op, rbmg_ensemble* ens,
                                int sub_system_size, double* out);
+/* KullbackLeibler(num_params, gpu) value / gradient (source/network_functions/
+ * KullbackLeibler.cu:14-137, pyRBMonGPU/main.cpp:421-470) with D = log psi' - log psi:
+ * value = sqrt(<|D|^2> - |<D>|^2), grad_k = (<D O_k*> - <D><O_k*>) / max(value, 1e-6)^nu
+ * over psi's ensemble (O_k of psi_prime).  The reference instantiates it with PsiClassical
+ * or PsiExact as psi, types outside this library; here psi and psi_prime are any of
+ * Psi / PsiDeep / PsiPair (PsiPair psi_prime: value only).  grad [2P] nullable. */
+RBMG_API int rbmg_kl_gradient(const rbmg_psi* psi, const rbmg_psi* psi_prime, rbmg_ensemble* ens, double nu,
+                              double* grad, double* value);
 RBMG_API int rbmg_hsd_gradient(const rbmg_psi* psi, const rbmg_psi* psi_prime, const rbmg_operator* op, int is_unitary,
                       rbmg_ensemble* ens, float nu, double* grad /* [2 P'] */, double* distance);
 

@@ -216,6 +216,23 @@ def hsd_2nd_order(psi, psi_prime, op, op2, spins, weights=None):
     return np.sqrt(1.0 - abs(o) ** 2 / (a * b))
 
 
+def kl(psi, psi_prime, spins, weights=None, nu=1.0, gradient=True):
+    """KullbackLeibler value / gradient (source/network_functions/KullbackLeibler.cu:14-137):
+    D = log psi' - log psi, value = sqrt(<|D|^2> - |<D>|^2), grad_k = (<D O_k'*> -
+    <D><O_k'*>) / max(value, 1e-6)^nu; weights None: 1 per sample (Monte Carlo), else the
+    exact-summation weights prefactor^2 |psi|^2."""
+    sp = np.asarray(spins, np.uint64)
+    D = np.array([log_psi(psi_prime, s) - log_psi(psi, s) for s in sp])
+    w = np.ones(len(sp)) / len(sp) if weights is None else np.asarray(weights, np.float64)
+    m = (w * D).sum()
+    value = np.sqrt((w * np.abs(D) ** 2).sum() - abs(m) ** 2)
+    if not gradient:
+        return None, value
+    O = np.array([O_k(psi_prime, s) for s in sp])
+    g = ((w * D) @ O.conj() - m * (w @ O.conj())) / max(value, 1e-6) ** nu
+    return g, value
+
+
 def diag_density(psi, op, spins, na, weights=None):
     """DiagDensityOp (source/network_functions/DiagDensityOp.cu:12-50): sum of
     weight |E_loc|^2 per configuration of the first na spins; weights None: 1 per sample

@@ -16,6 +16,11 @@
 #include "network_functions/PsiOkVector.hpp"
 #include "network_functions/S_matrix.hpp"
 #include "network_functions/DiagDensityOp.hpp"
+#include "network_functions/KullbackLeibler.hpp"
+// The reference's KullbackLeibler source, compiled in place in this unit: it instantiates
+// the templates only for PsiClassical / PsiExact as psi (types this harness does not
+// build), so the complex-RBM pair is instantiated below, for the golden vectors only.
+#include "../source/network_functions/KullbackLeibler.cu"
 
 #include <complex>
 #include <cstdio>
@@ -27,6 +32,12 @@
 
 using namespace rbm_on_gpu;
 using cplx = std::complex<double>;
+
+namespace rbm_on_gpu {
+template double KullbackLeibler::value(const Psi& psi, const Psi& psi_prime, ExactSummation& spin_ensemble);
+template double KullbackLeibler::gradient(std::complex<double>* result, const Psi& psi, const Psi& psi_prime,
+                                          ExactSummation& spin_ensemble, const double nu);
+}  // namespace rbm_on_gpu
 
 static std::string g_dir;
 static std::map<std::string, std::string> g_meta;
@@ -210,6 +221,16 @@ int main(int argc, char** argv) {
         }
         if (meta_i("ok", 0)) ok_vectors(psi, P);
         if (meta_i("mc_samples", 0)) mc_outputs(psi, op, N, P);
+        if (meta_i("kl", 0)) {
+            // KullbackLeibler value / gradient (source/network_functions/KullbackLeibler.cu:91-137)
+            Psi psi_prime = load_rbm("pp_", N, M);
+            ExactSummation es(static_cast<unsigned>(N), false);
+            KullbackLeibler kl(static_cast<unsigned>(P), false);
+            scalar("kl_value", kl.value(psi, psi_prime, es));
+            std::vector<cplx> g(P);
+            scalar("kl_grad_value", kl.gradient(g.data(), psi, psi_prime, es, meta_d("hsd_nu", 1.0)));
+            save("kl_gradient", g.data(), g.size());
+        }
         if (meta_i("smatrix", 0)) {
             // get_S_matrix (source/network_functions/S_matrix.cu:10-53), ExactSummation
             ExactSummation es(static_cast<unsigned>(N), false);

@@ -113,6 +113,7 @@ SIGNATURES = {
     "rbmg_s_matrix_timing": [_dp, _ip],
     "rbmg_hsd_distance_2nd_order": [_vp, _vp, _vp, _vp, _vp, _dp],
     "rbmg_diag_density": [_vp, _vp, _vp, C.c_int, _dp],
+    "rbmg_kl_gradient": [_vp, _vp, _vp, C.c_double, _dp, _dp],
 }
 _RESTYPE = {"rbmg_last_error": C.c_char_p, "rbmg_version": C.c_char_p}
 

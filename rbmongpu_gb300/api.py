@@ -587,6 +587,27 @@ class HilbertSpaceDistance:
         return g, d.value
 
 
+class KullbackLeibler:
+    """KullbackLeibler(num_params, gpu) (pyRBMonGPU/main.cpp:421-470): ``__call__(psi,
+    psi_prime, spin_ensemble)`` -> value, ``gradient(psi, psi_prime, spin_ensemble, nu)``
+    -> (grad[P], value), with D = log psi' - log psi, value = sqrt(<|D|^2> - |<D>|^2)."""
+
+    def __init__(self, num_params, gpu=True):
+        self.num_params = num_params
+
+    def __call__(self, psi, psi_prime, spin_ensemble):
+        v = C.c_double()
+        call("rbmg_kl_gradient", psi._h, psi_prime._h, spin_ensemble._h, 1.0, None, C.byref(v))
+        return v.value
+
+    def gradient(self, psi, psi_prime, spin_ensemble, nu=1.0):
+        g = np.zeros(psi_prime.num_params, np.complex128)
+        v = C.c_double()
+        call("rbmg_kl_gradient", psi._h, psi_prime._h, spin_ensemble._h, float(nu), _p(g.view(np.float64)),
+             C.byref(v))
+        return g, v.value
+
+
 class DiagDensityOp:
     """DiagDensityOp(sub_system_size, gpu) (pyRBMonGPU/main.cpp:497-533): called with
     (psi, operator_, spin_ensemble) it returns the 2^sub_system_size densities

@@ -1383,6 +1383,122 @@ extern "C" int rbmg_hsd_gradient(const rbmg_psi* psi, const rbmg_psi* pp, const 
     return RBMG_OK;
 }
 
+// KullbackLeibler::value / gradient (source/network_functions/KullbackLeibler.cu:14-137)
+// with D = log psi' - log psi per configuration (FP64):
+//   value = sqrt(<|D|^2> - |<D>|^2),  grad_k = (<D O_k*> - <D><O_k*>) / max(value, 1e-6)^nu
+// (O_k of psi').  The reference instantiates it with PsiClassical / PsiExact as psi; the
+// formula holds for any pair of states, here every pair of this library's kinds with the
+// same N (PsiPair psi' for the value only).  The gradient sums w (D - <D>) O_k*, the same
+// quantity with the mean taken out first.
+extern "C" int rbmg_kl_gradient(const rbmg_psi* psi, const rbmg_psi* pp, rbmg_ensemble* ens, double nu,
+                                double* grad, double* value) {
+    if (!psi || !pp || !ens || !value) return fail(RBMG_EINVAL, "KullbackLeibler: null");
+    if (pp->N != psi->N) return fail(RBMG_EINVAL, "KullbackLeibler: psi and psi_prime differ in N");
+    if (ens->kind == 1 && static_cast<int>(ens->num_spins) != psi->N)
+        return fail(RBMG_EINVAL, "KullbackLeibler: ExactSummation size differs from psi's N");
+    if (grad && pp->kind == 2) return fail(RBMG_EUNSUPPORTED, "KullbackLeibler: gradient for a PsiPair psi_prime");
+    int r = RBMG_OK;
+    if (psi->kind == 0) r = rbm_upload64(psi);
+    if (r == RBMG_OK && pp->kind == 0) r = rbm_upload64(pp);
+    if (r != RBMG_OK) return r;
+    const int N = pp->N, P = pp->num_params(), nw = nwords_of(N);
+    const size_t ok_len = static_cast<size_t>(P - 2 * N);
+    const uint64_t total = ens->num_steps();
+    Workspace& W = ws();
+    RBMG_CK(W.omega.ensure(sizeof(double2) * total));      // D of every sample
+    RBMG_CK(W.coef3.ensure(sizeof(double) * total));       // weights of every sample
+    RBMG_CK(W.Tp.ensure(sizeof(uint64_t) * nw * total));  // spins of every sample
+    RBMG_CK(W.sums.ensure(sizeof(double2) * kMaxSeries));
+    RBMG_CK(W.block_scratch.ensure(sizeof(double2) * kSumBlocks * kMaxSeries));
+    RBMG_CK(cudaMemsetAsync(W.sums.p, 0, sizeof(double2) * kMaxSeries, stream()));
+    double2* D = W.omega.as<double2>();
+    uint64_t* all_spins = W.Tp.as<uint64_t>();
+    double* all_w = W.coef3.as<double>();
+    bool weighted = false, enumerated = false;
+    uint64_t offset = 0;
+    StreamResult res;
+    r = run_stream(ens, psi, nullptr, false, size_t(1) << 20, &res, [&](const Chunk& c) -> int {
+        RBMG_CK(W.pr.ensure(sizeof(double2) * c.count));
+        RBMG_CK(W.nn.ensure(sizeof(double2) * c.count));
+        RBMG_CK(W.coef2.ensure(sizeof(double2) * c.count));
+        int rr = psi_log_psi_dev(psi, c.count, c.spins, c.enum_base, c.enumerate, W.pr.as<double2>());
+        if (rr == RBMG_OK) rr = psi_log_psi_dev(pp, c.count, c.spins, c.enum_base, c.enumerate, W.nn.as<double2>());
+        if (rr != RBMG_OK) return rr;
+        RBMG_CK(launch_sub(c.count, W.nn.as<double2>(), W.pr.as<double2>(), D + offset, stream()));
+        RBMG_CK(launch_abs2(c.count, D + offset, W.coef2.as<double2>(), stream()));
+        SeriesSet set{};
+        set.n = 2;
+        set.v[0] = D + offset;
+        set.v[1] = W.coef2.as<double2>();
+        RBMG_CK(launch_weighted_sums(c.count, c.weights, set, W.block_scratch.as<double2>(), W.sums.as<double2>(),
+                                     stream()));
+        if (c.spins) {
+            RBMG_CK(cudaMemcpyAsync(all_spins + offset * nw, c.spins, sizeof(uint64_t) * nw * c.count,
+                                    cudaMemcpyDeviceToDevice, stream()));
+        } else {
+            enumerated = true;
+        }
+        if (c.weights) {
+            weighted = true;
+            RBMG_CK(cudaMemcpyAsync(all_w + offset, c.weights, sizeof(double) * c.count, cudaMemcpyDeviceToDevice,
+                                    stream()));
+        }
+        offset += c.count;
+        return RBMG_OK;
+    });
+    if (r != RBMG_OK) return r;
+    double2 s2[2];
+    RBMG_CK(cudaMemcpyAsync(s2, W.sums.p, sizeof(s2), cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaStreamSynchronize(stream()));
+    const double f = res.norm_factor;
+    const cplx mean = cplx(s2[0].x, s2[0].y) * f;
+    const double v = std::sqrt(s2[1].x * f - std::norm(mean));   // KullbackLeibler.cu:100-104
+    *value = v;
+    if (!grad) return RBMG_OK;
+    const int count = static_cast<int>(offset);
+    const double factor = std::pow(std::max(v, 1e-6), nu);        // :119-121
+    RBMG_CK(W.coef1.ensure(sizeof(double2) * count));
+    RBMG_CK(launch_coef(count, weighted ? all_w : nullptr, D, f / factor, W.coef1.as<double2>(), stream(),
+                        make_double2(mean.real(), mean.imag())));
+    RBMG_CK(W.acc_wO.ensure(sizeof(double2) * ok_len));
+    RBMG_CK(cudaMemsetAsync(W.acc_wO.p, 0, sizeof(double2) * ok_len, stream()));
+    const uint64_t* sp = enumerated ? (ens->exact_total_z ? ens->d_allowed.as<uint64_t>() : nullptr) : all_spins;
+    const int enumerate = (enumerated && !ens->exact_total_z) ? 1 : 0;
+    if (pp->kind == 0) {
+        constexpr int kSplits = 64;
+        RBMG_CK(W.partial.ensure(sizeof(double2) * kSplits * (1 + N) * pp->M));
+        const int chunk = std::max(1024, static_cast<int>((size_t(256) << 20) / (sizeof(float2) * pp->Mpad)));
+        RBMG_CK(W.T.ensure(sizeof(float2) * std::min(chunk, count) * pp->Mpad));
+        RBMG_CK(W.logpsi_p.ensure(sizeof(double2) * std::min(chunk, count)));
+        const RbmDev pd = pp->rbm_dev();
+        for (int base = 0; base < count; base += chunk) {
+            const int cnt = std::min(chunk, count - base);
+            EstLaunch L{};
+            L.count = cnt;
+            L.enum_base = static_cast<uint64_t>(base);
+            L.spins = sp ? sp + static_cast<size_t>(base) * nw : nullptr;
+            L.flags = EST_PRIME | (enumerate ? EST_ENUMERATE : 0);
+            L.logpsi_prime = W.logpsi_p.as<double2>();
+            L.Tp = W.T.as<float2>();
+            RBMG_CK(launch_rbm_estimate(pd, nullptr, &pd, L, stream()));
+            RBMG_CK(launch_outer_reduce(cnt, N, nw, pp->M, L.spins, L.enum_base, enumerate,
+                                        W.coef1.as<double2>() + base, W.T.as<float2>(), pp->Mpad, 1,
+                                        W.acc_wO.as<double2>(), W.partial.as<double2>(), kSplits, stream()));
+        }
+    } else {
+        const int rr = deep_hsd_okreduce(pp, -1, count, sp, 0, enumerate, W.coef1.as<double2>(),
+                                         W.acc_wO.as<double2>(), stream());
+        if (rr != RBMG_OK) return rr;
+    }
+    std::vector<double2> acc(ok_len);
+    RBMG_CK(cudaMemcpyAsync(acc.data(), W.acc_wO.p, sizeof(double2) * ok_len, cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaStreamSynchronize(stream()));
+    cplx* g = reinterpret_cast<cplx*>(grad);
+    for (int k = 0; k < 2 * N; k++) g[k] = 0.0;
+    for (size_t k = 0; k < ok_len; k++) g[2 * N + k] = cplx(acc[k].x, acc[k].y);
+    return RBMG_OK;
+}
+
 // DiagDensityOp(sub_system_size)(psi, op, ensemble) (source/network_functions/DiagDensityOp.cu:
 // 12-50): densities [2^N_A] = sum_s weight |E_loc(s)|^2 binned by the first N_A spins, over
 // num_steps (the reference's local_energy1 * conj(local_energy2) of one operator)

@@ -35,7 +35,19 @@ __global__ void diag_density_kernel(int count, int enumerate, uint64_t enum_base
         if (hist[i] != 0.0) atomicAdd(&out[i], hist[i]);
 }
 
+__global__ void sub_kernel(int count, const double2* a, const double2* b, double2* out) {
+    for (long s = static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x; s < count;
+         s += static_cast<long>(gridDim.x) * blockDim.x)
+        out[s] = make_double2(a[s].x - b[s].x, a[s].y - b[s].y);
+}
+
 }  // namespace
+
+cudaError_t launch_sub(int count, const double2* a, const double2* b, double2* out, cudaStream_t st) {
+    if (count <= 0) return cudaSuccess;
+    sub_kernel<<<std::min((count + 255) / 256, 4096), 256, 0, st>>>(count, a, b, out);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_diag_density(int count, int enumerate, uint64_t enum_base, const uint64_t* spins, int nw,
                                 const double* w, const double2* eloc, int na, double* out, cudaStream_t st) {

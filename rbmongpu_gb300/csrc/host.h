@@ -110,6 +110,8 @@ int psi_scatter(rbmg_psi* psi, const double2* packed);
 // capi.cu: the energy gradient formed on the device, d_grad [P]; energy to value[2]
 int ev_gradient_device(const rbmg_psi* psi, const rbmg_operator* op, rbmg_ensemble* ens, double2* d_grad,
                        double* value);
+// density.cu: out = a - b elementwise
+cudaError_t launch_sub(int count, const double2* a, const double2* b, double2* out, cudaStream_t st);
 // density.cu: out [2^na] += w_s |eloc_s|^2 at the bin of the first na spins
 cudaError_t launch_diag_density(int count, int enumerate, uint64_t enum_base, const uint64_t* spins, int nw,
                                 const double* w, const double2* eloc, int na, double* out, cudaStream_t st);

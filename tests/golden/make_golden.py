@@ -141,7 +141,8 @@ def act_points(rng):
     return np.asarray(z, np.complex128)
 
 
-def rbm_case(name, N, M, sigma, seed, op, hop, unitary, nu, mc=None, normalize=True, ok_count=4, smatrix=False):
+def rbm_case(name, N, M, sigma, seed, op, hop, unitary, nu, mc=None, normalize=True, ok_count=4, smatrix=False,
+             kl=False):
     rng = np.random.Generator(np.random.PCG64(seed))
     b = cnormal(rng, M, sigma)
     W = cnormal(rng, (N, M), sigma)
@@ -149,7 +150,8 @@ def rbm_case(name, N, M, sigma, seed, op, hop, unitary, nu, mc=None, normalize=T
     pW = W + cnormal(rng, (N, M), 1e-3)
     ok_spins = rng.integers(0, 2 ** min(N, 62), ok_count, dtype=np.uint64)
     meta = {"kind": "rbm", "N": N, "M": M, "prefactor": 1.0, "normalize": int(normalize),
-            "exact": int(N <= 16), "ok": 1, "hsd_unitary": int(unitary), "hsd_nu": nu, "smatrix": int(smatrix)}
+            "exact": int(N <= 16), "ok": 1, "hsd_unitary": int(unitary), "hsd_nu": nu, "smatrix": int(smatrix),
+            "kl": int(kl)}
     if mc:
         meta.update(mc)
     arrays = {"b.bin": b, "W.bin": W, "pp_b.bin": pb, "pp_W.bin": pW, "ok_spins.bin": ok_spins,
@@ -235,7 +237,9 @@ def main():
     deep_case("deep10_dense", "deep", 10, [20, 10, 5], [10, 20, 10], 0.1, 104, tfim_chain(10), identity_op(),
               True, 1.0)
     # get_S_matrix of a small RBM over ExactSummation (the reference's only instantiation)
-    rbm_case("rbm6_smatrix", 6, 12, 0.3, 13, tfim_chain(6, 1.0, 1.0), identity_op(), True, 1.0, smatrix=True)
+    # and the KullbackLeibler value and gradient to the perturbed copy (nu = 0.5)
+    rbm_case("rbm6_smatrix", 6, 12, 0.3, 13, tfim_chain(6, 1.0, 1.0), identity_op(), True, 0.5, smatrix=True,
+             kl=True)
     # second-order distance (PsiDeep with ExactSummation, its only instantiation) for the
     # step generator -i t H, t = 0.02, of the periodic TFIM chain; DiagDensityOp of the
     # first 3 spins with the chain Hamiltonian
