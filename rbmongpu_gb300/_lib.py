@@ -102,6 +102,7 @@ SIGNATURES = {
     "rbmg_batch_result": [_vp, C.c_int, _dp, _dp, _dp],
     "rbmg_batch_info": [_vp, _ip, _u64p, _dp],
     "rbmg_chain_learned_async": [_vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_int, _vp, _vp],
+    "rbmg_chain_set_learned_streams": [_vp, C.c_int],
     "rbmg_optimizer_create": [C.c_int, C.c_int, _dp, C.c_int, C.c_int, _vpp],
     "rbmg_optimizer_destroy": [_vp],
     "rbmg_optimizer_reset": [_vp],

@@ -670,6 +670,10 @@ class Chain:
              int(n_sweeps), int(measure_every), C.c_void_p(d_eloc) if d_eloc else None,
              C.c_void_p(stream) if stream else None)
 
+    def set_learned_streams(self, streams):
+        """Frozen learned steps on 1 or 2 streams (0: automatic, 2 from 8192 walkers on)."""
+        call("rbmg_chain_set_learned_streams", self._h, int(streams))
+
     def learned_async(self, psi, operator_, proposal, n_steps, train=0, measure_every=1, d_eloc=0, stream=None):
         """n_steps learned Metropolis-Hastings steps (cluster flips picked by `proposal`).
         train > 0: one REINFORCE + Adam update per step on the first `train` walkers' moves;

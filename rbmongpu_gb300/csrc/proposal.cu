@@ -594,6 +594,7 @@ struct LearnedLaunch {
     unsigned long long* accepts;
     unsigned long long* proposals;
     int propose_next;            // accept kernel: also draw the next step's move (frozen network)
+    int walker_base;             // walker index of entry 0 (a slice of the chain): keys its Philox streams
 };
 
 template <int K, int NW>
@@ -621,7 +622,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) learned_draw_kernel(Learn
     const int w = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
     if (w >= L.B) return;
     WalkerRng rng;
-    rng.init(L.seed, static_cast<uint32_t>(w), L.rng_index[w]);
+    rng.init(L.seed, static_cast<uint32_t>(L.walker_base + w), L.rng_index[w]);
     const float* row = L.logits_cur + static_cast<long>(w) * L.O;
     const LogNorm ln = log_norms(row, L.N, lane);
     const int i = draw_index(row, L.N, ln.seed, rng.uniform(), lane);
@@ -729,7 +730,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) learned_accept_kernel(Rbm
     const float logq_rev = (rowp[i] - ln.seed) + (rowp[L.N + l - 1] - ln.len);
     const float log_a = 2.0f * delta + logq_rev - L.logq_fwd[w];
     WalkerRng rng;
-    rng.init(L.seed, static_cast<uint32_t>(w), L.rng_index[w]);
+    rng.init(L.seed, static_cast<uint32_t>(L.walker_base + w), L.rng_index[w]);
     const float a = log_a >= 0.0f ? 1.0f : expf_det(log_a);
     bool accept = log_a >= 0.0f;
     if (!accept) accept = rng.uniform() <= a;
@@ -1133,7 +1134,7 @@ __global__ void __launch_bounds__(kFThreads, 1) mlp_fused_kernel(FusedNet net, L
         if (w < count) {
             if (PROPOSE) {
                 WalkerRng rng;
-                rng.init(L.seed, static_cast<uint32_t>(w), L.rng_index[w]);
+                rng.init(L.seed, static_cast<uint32_t>(L.walker_base + w), L.rng_index[w]);
                 const float* row = L.logits_cur + static_cast<long>(w) * L.O;
                 const LogNorm ln = log_norms(row, L.N, lane);
                 const int i = draw_index(row, L.N, ln.seed, rng.uniform(), lane);
@@ -1237,10 +1238,48 @@ cudaError_t launch_fused(const rbmg_proposal* p, const LearnedLaunch& L, const u
 }
 
 // per-chain buffers of the learned steps
+// chains of at least this many walkers run their frozen steps as two halves on two streams
+constexpr int kSplitWalkers = 8192;
+
 struct LearnedState {
     int B = 0, Mpad = 0, nw = 0, O = 0;
     DevBuf theta, re, spins_prop, spins_pre, site, len, logq, logits_cur, logits_prop, reward, rbar;
+    // second stream of the frozen steps: the two halves of the walkers run as independent
+    // chains, so that one half's network pass overlaps the other half's accept pass
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+    LearnedState() = default;
+    LearnedState(const LearnedState&) = delete;
+    LearnedState& operator=(const LearnedState&) = delete;
+    ~LearnedState() {
+        if (fork) cudaEventDestroy(fork);
+        if (join) cudaEventDestroy(join);
+        if (side) cudaStreamDestroy(side);
+    }
 };
+
+// walkers [base, base + count) of a chain as a chain of their own (same Philox streams)
+LearnedLaunch learned_slice(const LearnedLaunch& L, int base, int count, int nw, int Mpad) {
+    LearnedLaunch h = L;
+    const size_t b = static_cast<size_t>(base);
+    h.B = count;
+    h.walker_base = L.walker_base + base;
+    h.spins = L.spins + b * nw;
+    h.rng_index = L.rng_index + b;
+    h.spins_prop = L.spins_prop + b * nw;
+    h.spins_pre = L.spins_pre ? L.spins_pre + b * nw : nullptr;
+    h.site = L.site + b;
+    h.len = L.len + b;
+    h.logq_fwd = L.logq_fwd + b;
+    h.logits_cur = L.logits_cur + b * L.O;
+    h.logits_prop = L.logits_prop + b * L.O;
+    h.theta = L.theta + b * Mpad;
+    h.re = L.re + b * Mpad;
+    h.reward = L.reward + b;
+    h.accepts = L.accepts + b;
+    h.proposals = L.proposals + b;
+    return h;
+}
 
 }  // namespace rbmg
 
@@ -1421,6 +1460,12 @@ extern "C" int rbmg_proposal_set_objective(rbmg_proposal* p, int objective) {
     return RBMG_OK;
 }
 
+extern "C" int rbmg_chain_set_learned_streams(rbmg_chain* c, int streams) {
+    if (!c || streams < 0 || streams > 2) return fail(RBMG_EINVAL, "learned streams: 0 (automatic), 1 or 2");
+    c->learned_streams = streams;
+    return RBMG_OK;
+}
+
 extern "C" int rbmg_chain_learned_async(rbmg_chain* c, const rbmg_psi* psi, const rbmg_operator* op,
                                         rbmg_proposal* prop, int n_steps, int train, int measure_every,
                                         void* d_eloc_out, void* stream_ptr) {
@@ -1497,6 +1542,56 @@ extern "C" int rbmg_chain_learned_async(rbmg_chain* c, const rbmg_psi* psi, cons
     if (op) od = op->dev();
     double2* out = static_cast<double2*>(d_eloc_out);
     const int lead = d_eloc_out ? n_steps % measure_every : n_steps;
+    auto measure = [&](int step, cudaStream_t s) -> cudaError_t {
+        EstLaunch E{};
+        E.count = B;
+        E.spins = L.spins;
+        E.flags = EST_ELOC;
+        E.eloc = out + static_cast<size_t>((step - lead) / measure_every) * B;
+        return launch_rbm_estimate(P, &od, nullptr, E, s);
+    };
+    auto measured = [&](int step) { return d_eloc_out && step >= lead && (step - lead + 1) % measure_every == 0; };
+    const bool split = c->learned_streams == 2 || (c->learned_streams == 0 && B >= kSplitWalkers);
+    if (nt == 0 && split && B >= 256) {
+        // frozen network, many walkers: two halves as independent chains on two streams
+        // (every walker keeps its own Philox stream and arithmetic, so the chains are the
+        // ones a single pass would produce)
+        if (!S->side) {
+            RBMG_CK(cudaStreamCreateWithFlags(&S->side, cudaStreamNonBlocking));
+            RBMG_CK(cudaEventCreateWithFlags(&S->fork, cudaEventDisableTiming));
+            RBMG_CK(cudaEventCreateWithFlags(&S->join, cudaEventDisableTiming));
+        }
+        const int h0 = (B / 2) / 128 * 128;
+        LearnedLaunch Lh[2] = {learned_slice(L, 0, h0, c->nw, P.Mpad), learned_slice(L, h0, B - h0, c->nw, P.Mpad)};
+        const cudaStream_t sh[2] = {st, S->side};
+        RBMG_CK(cudaEventRecord(S->fork, st));
+        RBMG_CK(cudaStreamWaitEvent(S->side, S->fork, 0));
+        for (int step = 0; step < n_steps; step++) {
+            for (int h = 0; h < 2; h++) {
+                LearnedLaunch& Q = Lh[h];
+                if (step > 0) {
+                    RBMG_CK(launch_fused<false>(prop, Q, Q.spins_prop, Q.B, const_cast<float*>(Q.logits_prop), sh[h]));
+                } else if (prop->O <= 128) {
+                    RBMG_CK(launch_draw(Q, sh[h]));
+                    RBMG_CK(launch_fused<false>(prop, Q, Q.spins_prop, Q.B, const_cast<float*>(Q.logits_prop), sh[h]));
+                } else {
+                    RBMG_CK(launch_fused<true>(prop, Q, nullptr, Q.B, const_cast<float*>(Q.logits_prop), sh[h]));
+                }
+                Q.propose_next = step + 1 < n_steps ? 1 : 0;
+                RBMG_CK(launch_learned(1, P, Q, sh[h]));
+            }
+            if (measured(step)) {
+                RBMG_CK(cudaEventRecord(S->join, S->side));
+                RBMG_CK(cudaStreamWaitEvent(st, S->join, 0));
+                RBMG_CK(measure(step, st));
+                RBMG_CK(cudaEventRecord(S->fork, st));
+                RBMG_CK(cudaStreamWaitEvent(S->side, S->fork, 0));
+            }
+        }
+        RBMG_CK(cudaEventRecord(S->join, S->side));
+        RBMG_CK(cudaStreamWaitEvent(st, S->join, 0));
+        return RBMG_OK;
+    }
     for (int step = 0; step < n_steps; step++) {
         // frozen network: the accept kernel draws the next move, so the later steps only
         // evaluate the network on the proposed configurations; while training, the weights
@@ -1536,14 +1631,7 @@ extern "C" int rbmg_chain_learned_async(rbmg_chain* c, const rbmg_psi* psi, cons
             // the walkers' current logits under the new weights
             RBMG_CK(launch_fused<false>(prop, L, L.spins, B, L.logits_cur, st));
         }
-        if (d_eloc_out && step >= lead && (step - lead + 1) % measure_every == 0) {
-            EstLaunch E{};
-            E.count = B;
-            E.spins = L.spins;
-            E.flags = EST_ELOC;
-            E.eloc = out + static_cast<size_t>((step - lead) / measure_every) * B;
-            RBMG_CK(launch_rbm_estimate(P, &od, nullptr, E, st));
-        }
+        if (measured(step)) RBMG_CK(measure(step, st));
     }
     return RBMG_OK;
 }

@@ -61,3 +61,31 @@ def test_checkpoint_rejects_spins_beyond_n():
     ck["spins"][0, 0] |= np.uint64(1 << 12)
     with pytest.raises(rg.RbmgError):
         c.restore(ck)
+
+
+def test_two_stream_frozen_steps_equal_one_stream():
+    """The frozen learned steps of 8320 walkers as two half-chains on two streams (4096 +
+    4224 walkers) give the chains, counters and measured local energies of one stream."""
+    import torch
+    import rbmongpu_gb300 as rg
+    N, B, rows = 40, 8320, 3
+    psi = rbm(N, 80, 7, sigma=0.15)
+    op = rg.Operator(*rg.operators.tfim_chain(N, 1.0, 1.0))
+    prop = rg.Proposal(N, seed=8)
+    warm = rg.Chain(psi, 1024, seed=1)
+    warm.learned_async(psi, None, prop, 30, train=512)
+    runs = []
+    for streams in (1, 2):
+        c = rg.Chain(psi, B, seed=12)
+        c.set_learned_streams(streams)
+        c.sweep_async(psi, None, 2)
+        el = torch.zeros((rows, B, 2), dtype=torch.float64, device="cuda")
+        c.learned_async(psi, op, prop, rows * 4 + 1, train=0, measure_every=4, d_eloc=el.data_ptr(),
+                        stream=rg.library_stream())
+        torch.cuda.synchronize()
+        runs.append((c.checkpoint(), el.cpu().numpy()))
+    (ca, ea), (cb, eb) = runs
+    for k in ca:
+        np.testing.assert_array_equal(ca[k], cb[k])
+    np.testing.assert_array_equal(ea, eb)
+    assert int(ca["accepts"].sum()) > 0
