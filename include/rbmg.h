@@ -293,10 +293,10 @@ RBMG_API int rbmg_proposal_set_state(rbmg_proposal* proposal, const float* param
 RBMG_API int rbmg_chain_learned_async(rbmg_chain* chain, const rbmg_psi* psi, const rbmg_operator* op,
                                       rbmg_proposal* proposal, int n_steps, int train, int measure_every,
                                       void* d_eloc_out, void* stream);
-/* Extension: the frozen learned steps of a chain run its walkers as two independent halves
- * on two streams (one half's network pass overlapping the other's accept pass) when
- * streams = 2, on one stream when 1; 0 (default) picks 2 from 8192 walkers on.  Every
- * walker keeps its Philox stream, so the chains do not depend on the choice. */
+/* Extension: the frozen learned steps of a chain run its walkers as `streams` (1 to 4)
+ * independent slices on as many streams (one slice's network pass overlapping another's
+ * accept pass); 0 (default) picks 2 from 8192 walkers on and 4 from 16384.  Every walker
+ * keeps its Philox stream, so the chains do not depend on the choice. */
 RBMG_API int rbmg_chain_set_learned_streams(rbmg_chain* chain, int streams);
 
 

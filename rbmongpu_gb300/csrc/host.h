@@ -176,6 +176,6 @@ struct rbmg_chain {
     uint64_t seed = 0;
     rbmg::DevBuf spins, rng_index, accepts, proposals;
     bool initialised = false;
-    int learned_streams = 0;   // frozen learned steps on 1 or 2 streams; 0: 2 from 8192 walkers on
+    int learned_streams = 0;   // frozen learned steps on 1 to 4 streams; 0: automatic
     std::shared_ptr<void> learned;
 };

@@ -1238,23 +1238,27 @@ cudaError_t launch_fused(const rbmg_proposal* p, const LearnedLaunch& L, const u
 }
 
 // per-chain buffers of the learned steps
-// chains of at least this many walkers run their frozen steps as two halves on two streams
+// chains of at least 8192 walkers run their frozen steps as 2 slices on 2 streams, from
+// 16384 walkers on as 4 slices on 4 streams
 constexpr int kSplitWalkers = 8192;
+constexpr int kMaxSlices = 4;
 
 struct LearnedState {
     int B = 0, Mpad = 0, nw = 0, O = 0;
     DevBuf theta, re, spins_prop, spins_pre, site, len, logq, logits_cur, logits_prop, reward, rbar;
-    // second stream of the frozen steps: the two halves of the walkers run as independent
-    // chains, so that one half's network pass overlaps the other half's accept pass
-    cudaStream_t side = nullptr;
-    cudaEvent_t fork = nullptr, join = nullptr;
+    // extra streams of the frozen steps: slices of the walkers run as independent chains,
+    // so that one slice's network pass overlaps another slice's accept pass
+    cudaStream_t side[kMaxSlices - 1] = {};
+    cudaEvent_t fork = nullptr, join[kMaxSlices - 1] = {};
     LearnedState() = default;
     LearnedState(const LearnedState&) = delete;
     LearnedState& operator=(const LearnedState&) = delete;
     ~LearnedState() {
         if (fork) cudaEventDestroy(fork);
-        if (join) cudaEventDestroy(join);
-        if (side) cudaStreamDestroy(side);
+        for (int i = 0; i < kMaxSlices - 1; i++) {
+            if (join[i]) cudaEventDestroy(join[i]);
+            if (side[i]) cudaStreamDestroy(side[i]);
+        }
     }
 };
 
@@ -1461,7 +1465,8 @@ extern "C" int rbmg_proposal_set_objective(rbmg_proposal* p, int objective) {
 }
 
 extern "C" int rbmg_chain_set_learned_streams(rbmg_chain* c, int streams) {
-    if (!c || streams < 0 || streams > 2) return fail(RBMG_EINVAL, "learned streams: 0 (automatic), 1 or 2");
+    if (!c || streams < 0 || streams > kMaxSlices)
+        return fail(RBMG_EINVAL, "learned streams: 0 (automatic) or 1 to 4");
     c->learned_streams = streams;
     return RBMG_OK;
 }
@@ -1551,23 +1556,45 @@ extern "C" int rbmg_chain_learned_async(rbmg_chain* c, const rbmg_psi* psi, cons
         return launch_rbm_estimate(P, &od, nullptr, E, s);
     };
     auto measured = [&](int step) { return d_eloc_out && step >= lead && (step - lead + 1) % measure_every == 0; };
-    const bool split = c->learned_streams == 2 || (c->learned_streams == 0 && B >= kSplitWalkers);
-    if (nt == 0 && split && B >= 256) {
-        // frozen network, many walkers: two halves as independent chains on two streams
+    int slices = c->learned_streams;
+    if (slices == 0) slices = B >= 2 * kSplitWalkers ? 4 : (B >= kSplitWalkers ? 2 : 1);
+    if (nt == 0 && slices > 1 && B >= 128 * slices) {
+        // frozen network, many walkers: slices as independent chains on their own streams
         // (every walker keeps its own Philox stream and arithmetic, so the chains are the
         // ones a single pass would produce)
-        if (!S->side) {
-            RBMG_CK(cudaStreamCreateWithFlags(&S->side, cudaStreamNonBlocking));
-            RBMG_CK(cudaEventCreateWithFlags(&S->fork, cudaEventDisableTiming));
-            RBMG_CK(cudaEventCreateWithFlags(&S->join, cudaEventDisableTiming));
+        if (!S->fork) RBMG_CK(cudaEventCreateWithFlags(&S->fork, cudaEventDisableTiming));
+        for (int q = 0; q < slices - 1; q++) {
+            if (!S->side[q]) {
+                RBMG_CK(cudaStreamCreateWithFlags(&S->side[q], cudaStreamNonBlocking));
+                RBMG_CK(cudaEventCreateWithFlags(&S->join[q], cudaEventDisableTiming));
+            }
         }
-        const int h0 = (B / 2) / 128 * 128;
-        LearnedLaunch Lh[2] = {learned_slice(L, 0, h0, c->nw, P.Mpad), learned_slice(L, h0, B - h0, c->nw, P.Mpad)};
-        const cudaStream_t sh[2] = {st, S->side};
-        RBMG_CK(cudaEventRecord(S->fork, st));
-        RBMG_CK(cudaStreamWaitEvent(S->side, S->fork, 0));
+        // slice boundaries at multiples of 128 walkers (whole tensor-core tiles)
+        LearnedLaunch Lh[kMaxSlices];
+        cudaStream_t sh[kMaxSlices];
+        int base = 0;
+        for (int q = 0; q < slices; q++) {
+            const int end = q + 1 == slices ? B : (B * (q + 1) / slices) / 128 * 128;
+            Lh[q] = learned_slice(L, base, end - base, c->nw, P.Mpad);
+            sh[q] = q == 0 ? st : S->side[q - 1];
+            base = end;
+        }
+        auto fork_all = [&]() -> cudaError_t {
+            cudaError_t e = cudaEventRecord(S->fork, st);
+            for (int q = 1; q < slices && e == cudaSuccess; q++) e = cudaStreamWaitEvent(sh[q], S->fork, 0);
+            return e;
+        };
+        auto join_all = [&]() -> cudaError_t {
+            cudaError_t e = cudaSuccess;
+            for (int q = 1; q < slices && e == cudaSuccess; q++) {
+                e = cudaEventRecord(S->join[q - 1], sh[q]);
+                if (e == cudaSuccess) e = cudaStreamWaitEvent(st, S->join[q - 1], 0);
+            }
+            return e;
+        };
+        RBMG_CK(fork_all());
         for (int step = 0; step < n_steps; step++) {
-            for (int h = 0; h < 2; h++) {
+            for (int h = 0; h < slices; h++) {
                 LearnedLaunch& Q = Lh[h];
                 if (step > 0) {
                     RBMG_CK(launch_fused<false>(prop, Q, Q.spins_prop, Q.B, const_cast<float*>(Q.logits_prop), sh[h]));
@@ -1581,15 +1608,12 @@ extern "C" int rbmg_chain_learned_async(rbmg_chain* c, const rbmg_psi* psi, cons
                 RBMG_CK(launch_learned(1, P, Q, sh[h]));
             }
             if (measured(step)) {
-                RBMG_CK(cudaEventRecord(S->join, S->side));
-                RBMG_CK(cudaStreamWaitEvent(st, S->join, 0));
+                RBMG_CK(join_all());
                 RBMG_CK(measure(step, st));
-                RBMG_CK(cudaEventRecord(S->fork, st));
-                RBMG_CK(cudaStreamWaitEvent(S->side, S->fork, 0));
+                RBMG_CK(fork_all());
             }
         }
-        RBMG_CK(cudaEventRecord(S->join, S->side));
-        RBMG_CK(cudaStreamWaitEvent(st, S->join, 0));
+        RBMG_CK(join_all());
         return RBMG_OK;
     }
     for (int step = 0; step < n_steps; step++) {

@@ -5,7 +5,8 @@
 // Here it is a complex Hermitian rank-n update S += F^T conj(F) of the per-sample O_k
 // rows F [n][L] (L = P - 2N), tiled 64 x 64 over the upper triangle of S: each CTA
 // stages 16 samples of its row block and its column block in shared memory, every
-// thread accumulates a 4 x 4 block of complex products in FP32 registers, and every
+// thread accumulates a 4 x 4 block of complex products in FP32 registers (its rows and
+// columns read with 128-bit shared loads, 64 FFMA per 4 loads), and every
 // 1024 samples the CTA adds its partial tile into the FP64 matrix in HBM (plain
 // read-modify-write when it owns the tile, FP64 atomics when the samples are split
 // across CTAs).  For the complex RBM the rows are never stored: an element of F is
@@ -74,7 +75,8 @@ __global__ void __launch_bounds__(256) sm_herk_kernel(SmSource a, double2* __res
     const int s_begin = blockIdx.y * slice;
     const int s_end = min(a.count, s_begin + slice);
     if (s_begin >= s_end) return;
-    __shared__ float2 Fa[kS][kT], Fb[kS][kT];
+    __shared__ __align__(16) float2 Fa[kS][kT];
+    __shared__ __align__(16) float2 Fb[kS][kT];
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
     const int m0 = tm * kT, n0 = tn * kT;
     // this thread's four loader columns of each block, sample row ty of the stage
@@ -113,11 +115,16 @@ __global__ void __launch_bounds__(256) sm_herk_kernel(SmSource a, double2* __res
             }
 #pragma unroll
             for (int s = 0; s < kS; s++) {
-                float2 x[4], y[4];
-#pragma unroll
-                for (int i = 0; i < 4; i++) x[i] = Fa[s][ty + 16 * i];
-#pragma unroll
-                for (int j = 0; j < 4; j++) y[j] = Fb[s][tx + 16 * j];
+                // rows 2 ty, 2 ty + 1, 32 + 2 ty, 33 + 2 ty of the tile (columns alike with tx):
+                // two 128-bit loads per block, consecutive threads on consecutive 16 bytes
+                const float4 a0 = *reinterpret_cast<const float4*>(&Fa[s][2 * ty]);
+                const float4 a1 = *reinterpret_cast<const float4*>(&Fa[s][32 + 2 * ty]);
+                const float4 b0 = *reinterpret_cast<const float4*>(&Fb[s][2 * tx]);
+                const float4 b1 = *reinterpret_cast<const float4*>(&Fb[s][32 + 2 * tx]);
+                const float2 x[4] = {make_float2(a0.x, a0.y), make_float2(a0.z, a0.w), make_float2(a1.x, a1.y),
+                                     make_float2(a1.z, a1.w)};
+                const float2 y[4] = {make_float2(b0.x, b0.y), make_float2(b0.z, b0.w), make_float2(b1.x, b1.y),
+                                     make_float2(b1.z, b1.w)};
 #pragma unroll
                 for (int i = 0; i < 4; i++)
 #pragma unroll
@@ -130,11 +137,11 @@ __global__ void __launch_bounds__(256) sm_herk_kernel(SmSource a, double2* __res
         }
 #pragma unroll
         for (int i = 0; i < 4; i++) {
-            const int r = m0 + ty + 16 * i;
+            const int r = m0 + (i >> 1) * 32 + 2 * ty + (i & 1);
             if (r >= a.L) continue;
 #pragma unroll
             for (int j = 0; j < 4; j++) {
-                const int c = n0 + tx + 16 * j;
+                const int c = n0 + (j >> 1) * 32 + 2 * tx + (j & 1);
                 if (c >= a.L) continue;
                 double2* p = S + static_cast<long>(r) * a.L + c;
                 if (atomic) {

@@ -63,9 +63,10 @@ def test_checkpoint_rejects_spins_beyond_n():
         c.restore(ck)
 
 
-def test_two_stream_frozen_steps_equal_one_stream():
-    """The frozen learned steps of 8320 walkers as two half-chains on two streams (4096 +
-    4224 walkers) give the chains, counters and measured local energies of one stream."""
+def test_sliced_frozen_steps_equal_one_stream():
+    """The frozen learned steps of 8320 walkers as 2 or 4 slices on as many streams (4096 +
+    4224; 2048 + 2048 + 2176 + 2048 walkers) give the chains, counters and measured local
+    energies of one stream."""
     import torch
     import rbmongpu_gb300 as rg
     N, B, rows = 40, 8320, 3
@@ -75,7 +76,7 @@ def test_two_stream_frozen_steps_equal_one_stream():
     warm = rg.Chain(psi, 1024, seed=1)
     warm.learned_async(psi, None, prop, 30, train=512)
     runs = []
-    for streams in (1, 2):
+    for streams in (1, 2, 4):
         c = rg.Chain(psi, B, seed=12)
         c.set_learned_streams(streams)
         c.sweep_async(psi, None, 2)
@@ -84,8 +85,9 @@ def test_two_stream_frozen_steps_equal_one_stream():
                         stream=rg.library_stream())
         torch.cuda.synchronize()
         runs.append((c.checkpoint(), el.cpu().numpy()))
-    (ca, ea), (cb, eb) = runs
-    for k in ca:
-        np.testing.assert_array_equal(ca[k], cb[k])
-    np.testing.assert_array_equal(ea, eb)
+    ca, ea = runs[0]
+    for cb, eb in runs[1:]:
+        for k in ca:
+            np.testing.assert_array_equal(ca[k], cb[k])
+        np.testing.assert_array_equal(ea, eb)
     assert int(ca["accepts"].sum()) > 0
