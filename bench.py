@@ -535,7 +535,7 @@ def main():
     ap.add_argument("--learned-steps-per-row", type=int, default=150,
                     help="learned steps per row; 150 makes a learned row last about as long as a plain row")
     ap.add_argument("--learned-streams", type=int, default=0,
-                    help="streams of the frozen learned steps (0: automatic, 4 slices at 16384 walkers)")
+                    help="streams of the frozen learned steps (0: automatic, 2 slices from 8192 walkers)")
     ap.add_argument("--train-steps", type=int, default=2000)
     ap.add_argument("--train-walkers", type=int, default=4096)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
@@ -625,7 +625,7 @@ def main():
                    "walkers_per_gpu": B, "sigma": SIGMA, "h": FIELD, "therm_sweeps": THERM_SWEEPS,
                    "step": f"learned: {L} frozen MH steps + E_loc; plain: {S} sweeps + E_loc",
                    "train_steps": args.train_steps, "train_walkers": args.train_walkers,
-                   "learned_streams": args.learned_streams or (4 if B >= 16384 else (2 if B >= 8192 else 1)),
+                   "learned_streams": args.learned_streams or (2 if B >= 8192 else 1),
                    "l2": "flushed between timed rows"},
         "learned": dict(le, ess_per_s=ess_l / sec_l, acceptance=r["learned_accept"], train_seconds=r["train_s"],
                         ms_per_row=float(np.mean(r["learned_ms"]))),

@@ -295,7 +295,7 @@ RBMG_API int rbmg_chain_learned_async(rbmg_chain* chain, const rbmg_psi* psi, co
                                       void* d_eloc_out, void* stream);
 /* Extension: the frozen learned steps of a chain run its walkers as `streams` (1 to 4)
  * independent slices on as many streams (one slice's network pass overlapping another's
- * accept pass); 0 (default) picks 2 from 8192 walkers on and 4 from 16384.  Every walker
+ * accept pass); 0 (default) picks 2 from 8192 walkers on.  Every walker
  * keeps its Philox stream, so the chains do not depend on the choice. */
 RBMG_API int rbmg_chain_set_learned_streams(rbmg_chain* chain, int streams);
 

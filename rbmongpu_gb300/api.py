@@ -671,8 +671,7 @@ class Chain:
              C.c_void_p(stream) if stream else None)
 
     def set_learned_streams(self, streams):
-        """Frozen learned steps on 1 to 4 streams (0: automatic, 2 from 8192 walkers on, 4
-        from 16384)."""
+        """Frozen learned steps on 1 to 4 streams (0: automatic, 2 from 8192 walkers on)."""
         call("rbmg_chain_set_learned_streams", self._h, int(streams))
 
     def learned_async(self, psi, operator_, proposal, n_steps, train=0, measure_every=1, d_eloc=0, stream=None):

@@ -1238,8 +1238,8 @@ cudaError_t launch_fused(const rbmg_proposal* p, const LearnedLaunch& L, const u
 }
 
 // per-chain buffers of the learned steps
-// chains of at least 8192 walkers run their frozen steps as 2 slices on 2 streams, from
-// 16384 walkers on as 4 slices on 4 streams
+// chains of at least 8192 walkers run their frozen steps as 2 slices on 2 streams (4 slices
+// measured no faster at 16384 walkers: the network pass is latency-bound inside a CTA)
 constexpr int kSplitWalkers = 8192;
 constexpr int kMaxSlices = 4;
 
@@ -1557,7 +1557,7 @@ extern "C" int rbmg_chain_learned_async(rbmg_chain* c, const rbmg_psi* psi, cons
     };
     auto measured = [&](int step) { return d_eloc_out && step >= lead && (step - lead + 1) % measure_every == 0; };
     int slices = c->learned_streams;
-    if (slices == 0) slices = B >= 2 * kSplitWalkers ? 4 : (B >= kSplitWalkers ? 2 : 1);
+    if (slices == 0) slices = B >= kSplitWalkers ? 2 : 1;
     if (nt == 0 && slices > 1 && B >= 128 * slices) {
         // frozen network, many walkers: slices as independent chains on their own streams
         // (every walker keeps its own Philox stream and arithmetic, so the chains are the
