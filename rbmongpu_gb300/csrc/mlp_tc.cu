@@ -3,15 +3,18 @@
 // One CTA (16 warps) evaluates the network N -> 256 -> 256 (SiLU) -> N+8 for 128
 // configurations.  Per layer the activations (A, 128 x K) and the layer's transposed
 // weights (B, n x K) sit in shared memory in the canonical K-major layout without swizzle
-// (8-row x 16-byte core matrices, 128 contiguous bytes each); one elected thread issues
-// K/16 tcgen05.mma (kind::f16, BF16 operands, FP32 accumulation, M = 128) into a
-// 256-column TMEM accumulator (of 512 allocated), and tcgen05.commit arrives on an
-// mbarrier when they are done.  The next layer's weights are then copied into B while the
-// epilogue runs: warp w reads TMEM lanes 32 (w % 4) .. +31 (its rows) and a quarter of the
-// columns with tcgen05.ld, adds the bias, applies SiLU and writes the BF16 result as the
-// next layer's A operand.  The logits are staged in shared memory and written out
-// row-contiguous.  The waits on the mbarrier are bounded: on timeout the kernel raises an
-// error flag, waits (bounded) for its MMAs, frees its TMEM and returns.
+// (8-row x 16-byte core matrices, 128 contiguous bytes each).  The weights are kept in
+// global memory already in that layout (tc_pack_kernel, run when the weights change), so
+// one thread moves a whole layer with a single bulk copy (cp.async.bulk) that completes
+// on an mbarrier.  One elected thread issues K/16 tcgen05.mma (kind::f16, BF16 operands,
+// FP32 accumulation, M = 128) into a 256-column TMEM accumulator (of 512 allocated), and
+// tcgen05.commit arrives on a second mbarrier when they are done; the next layer's
+// weights are then copied into B while the epilogue runs: warp w reads TMEM lanes
+// 32 (w % 4) .. +31 (its rows) and a quarter of the columns with tcgen05.ld, adds the
+// bias, applies SiLU and writes the BF16 result as the next layer's A operand.  The logits
+// are staged in shared memory and written out row-contiguous.  Every wait on an mbarrier is
+// bounded: on timeout the kernel raises an error flag, waits (bounded) for its copies and
+// MMAs in flight, frees its TMEM and returns.
 #include <cuda_bf16.h>
 
 #include "host.h"
@@ -113,18 +116,14 @@ __device__ __forceinline__ void tc_ld32(uint32_t taddr, float (&v)[32]) {
     for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
 
-__device__ __forceinline__ void cp16(uint32_t saddr, const void* g) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(saddr), "l"(g));
-}
-
-// B <- rows [0, n) of Wt [n][ldw] (k contiguous), k < K, in the canonical layout with n rows
-__device__ __forceinline__ void load_weights(uint32_t sB, const bf16* Wt, int ldw, int n, int K) {
-    const int kc = K / 8, chunks = n * kc;
-    for (int c = threadIdx.x; c < chunks; c += kTcThreads) {
-        const int row = c / kc, kb = c - row * kc;
-        cp16(sB + kmajor_offset(row, kb * 8, n), Wt + static_cast<long>(row) * ldw + kb * 8);
-    }
-    asm volatile("cp.async.commit_group;\n" ::);
+// bulk copy of `bytes` (a multiple of 16) from global memory into shared memory,
+// completing on the mbarrier (which expects the bytes first)
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(mbar), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                     dst),
+                 "l"(src), "r"(bytes), "r"(mbar)
+                 : "memory");
 }
 
 __device__ __forceinline__ float tanh_hw(float x) {
@@ -155,7 +154,37 @@ struct TcNet {
     const float* b1;
     const float* b2;
     const float* b3;
+    const bf16* pack;  // the three layers' B operands in the shared-memory layout (tc_pack_size)
 };
+
+// elements of the packed operands: W1 [256 x ldw1], W2 [256 x 256], W3 [128 x 256]
+size_t tc_pack_size(int ldw1) {
+    return static_cast<size_t>(kTcHidden) * ldw1 + static_cast<size_t>(kTcHidden) * kTcHidden +
+           static_cast<size_t>(kTcRows) * kTcHidden;
+}
+
+namespace {
+
+// out (image of a B operand with n rows and K columns) <- Wt [n][ldw]
+__global__ void tc_pack_kernel(const bf16* Wt, int ldw, int n, int K, bf16* out) {
+    const long idx = static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (idx >= static_cast<long>(n) * K) return;
+    const int row = static_cast<int>(idx / K), col = static_cast<int>(idx - static_cast<long>(row) * K);
+    out[kmajor_offset(row, col, n) / 2] = Wt[static_cast<long>(row) * ldw + col];
+}
+
+}  // namespace
+
+cudaError_t launch_tc_pack(const TcNet& net, bf16* pack, cudaStream_t st) {
+    const long n1 = static_cast<long>(kTcHidden) * net.ldw1, n2 = static_cast<long>(kTcHidden) * kTcHidden,
+               n3 = static_cast<long>(kTcRows) * kTcHidden;
+    tc_pack_kernel<<<static_cast<int>((n1 + 255) / 256), 256, 0, st>>>(net.w1t, net.ldw1, kTcHidden, net.ldw1, pack);
+    tc_pack_kernel<<<static_cast<int>((n2 + 255) / 256), 256, 0, st>>>(net.w2t, kTcHidden, kTcHidden, kTcHidden,
+                                                                         pack + n1);
+    tc_pack_kernel<<<static_cast<int>((n3 + 255) / 256), 256, 0, st>>>(net.w3t, kTcHidden, kTcRows, kTcHidden,
+                                                                         pack + n1 + n2);
+    return cudaGetLastError();
+}
 
 template <int NW>
 __global__ void __launch_bounds__(kTcThreads, 1) mlp_tc_kernel(TcNet net, const uint64_t* spins, int count,
@@ -164,24 +193,36 @@ __global__ void __launch_bounds__(kTcThreads, 1) mlp_tc_kernel(TcNet net, const 
     unsigned char* sA = tsm;
     unsigned char* sB = tsm + kTcA;
     float* sBias = reinterpret_cast<float*>(tsm + kTcA + kTcB);   // b1 | b2 | b3
-    uint64_t* mbar = reinterpret_cast<uint64_t*>(tsm + kTcA + kTcB + kTcBias);
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(tsm + kTcA + kTcB + kTcBias);        // MMAs done
     uint32_t* tslot = reinterpret_cast<uint32_t*>(tsm + kTcA + kTcB + kTcBias + 16);
+    uint64_t* wbar = reinterpret_cast<uint64_t*>(tsm + kTcA + kTcB + kTcBias + 32);   // weights landed
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int quarter = warp & 3, cgroup = warp >> 2;
     const int row0 = blockIdx.x * kTcRows;
     const int rows = min(kTcRows, count - row0);
-    const uint32_t aA = saddr_of(sA), aB = saddr_of(sB), aM = saddr_of(mbar);
-    // ---- layer-1 weights start streaming in at once
-    load_weights(aB, net.w1t, net.ldw1, kTcHidden, net.ldw1);
-    // ---- TMEM (warp 0) and the mbarrier (thread 0)
+    const uint32_t aA = saddr_of(sA), aB = saddr_of(sB), aM = saddr_of(mbar), aW = saddr_of(wbar);
+    // layer l's packed B operand and its size
+    auto w_src = [&](int l) {
+        const size_t o1 = static_cast<size_t>(kTcHidden) * net.ldw1;
+        return l == 0 ? net.pack : (l == 1 ? net.pack + o1 : net.pack + o1 + static_cast<size_t>(kTcHidden) * kTcHidden);
+    };
+    auto w_bytes = [&](int l) {
+        return static_cast<uint32_t>(l == 0 ? kTcHidden * net.ldw1 * 2 : (l == 1 ? kTcHidden * kTcHidden * 2
+                                                                                  : kTcRows * kTcHidden * 2));
+    };
+    // ---- the mbarriers, and the layer-1 weights streaming in at once (thread 0)
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(aM));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(aW));
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        bulk_g2s(aB, w_src(0), w_bytes(0), aW);
+    }
+    bool w_pending = true;   // a weight copy is in flight (known to every thread)
+    // ---- TMEM (warp 0)
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(saddr_of(tslot)),
                      "r"(kTcCols));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
-    }
-    if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(aM));
-        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
     for (int j = tid; j < 2 * kTcHidden + kTcRows; j += kTcThreads) {
         float b = 0.0f;
@@ -190,12 +231,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) mlp_tc_kernel(TcNet net, const 
         else if (j - 2 * kTcHidden < net.O) b = net.b3[j - 2 * kTcHidden];
         sBias[j] = b;
     }
-    // ---- layer-1 input: row r = configuration row0 + r, +-1 spins, zero beyond N
+    // ---- layer-1 input: row r = configuration row0 + r, +-1 spins, zero beyond N; the
+    // 8 columns of a chunk lie in one spin word, loaded once
     {
         const int kc = net.ldw1 / 8;
         for (int c = tid; c < kTcRows * kc; c += kTcThreads) {
             const int r = c % kTcRows, col = (c / kTcRows) * 8;
             const bool live = r < rows;
+            const uint64_t word = live ? spins[static_cast<long>(row0 + r) * NW + (col >> 6)] : 0ull;
             uint32_t pk[4];
 #pragma unroll
             for (int e = 0; e < 8; e += 2) {
@@ -203,11 +246,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) mlp_tc_kernel(TcNet net, const 
 #pragma unroll
                 for (int u = 0; u < 2; u++) {
                     const int i = col + e + u;
-                    x[u] = 0.0f;
-                    if (live && i < net.N) {
-                        const uint64_t word = spins[static_cast<long>(row0 + r) * NW + (i >> 6)];
-                        x[u] = ((word >> (i & 63)) & 1ull) ? 1.0f : -1.0f;
-                    }
+                    x[u] = (live && i < net.N) ? (((word >> (i & 63)) & 1ull) ? 1.0f : -1.0f) : 0.0f;
                 }
                 pk[e / 2] = pack_bf16(x[0], x[1]);
             }
@@ -219,17 +258,20 @@ __global__ void __launch_bounds__(kTcThreads, 1) mlp_tc_kernel(TcNet net, const 
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
     const uint32_t tmem = *tslot;
     bool ok = true;
-    uint32_t phase = 0;
+    uint32_t phase = 0, wphase = 0;
+    bool mma_pending = false;
     const int r = quarter * 32 + lane;                                  // this thread's row (TMEM lane)
     const uint32_t lane_base = static_cast<uint32_t>(quarter * 32) << 16;
     for (int layer = 0; layer < 3; layer++) {
         const int K = layer == 0 ? net.ldw1 : kTcHidden;
         const int n = layer == 2 ? kTcRows : kTcHidden;
-        // this layer's weights have landed (each thread its own copies, then the barrier),
-        // the epilogue's generic-proxy writes of A are visible to the tensor cores
-        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        // the epilogue's generic-proxy writes of A are visible to the tensor cores, and this
+        // layer's weights have landed
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-        __syncthreads();
+        ok = __syncthreads_and(mbar_wait(aW, wphase)) != 0;
+        if (!ok) break;
+        w_pending = false;
+        wphase ^= 1u;
         if (tid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
             const uint32_t idesc = instr_desc(n);
@@ -240,16 +282,18 @@ __global__ void __launch_bounds__(kTcThreads, 1) mlp_tc_kernel(TcNet net, const 
             }
             tc_commit(aM);
         }
+        mma_pending = true;
         __syncwarp();
         // every thread has seen the MMAs complete (or the block gives up) before A or B is rewritten
         ok = __syncthreads_and(mbar_wait(aM, phase)) != 0;
         if (!ok) break;
+        mma_pending = false;
         phase ^= 1u;
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
         // the next layer's weights stream into B during the epilogue
-        if (layer == 0) load_weights(aB, net.w2t, kTcHidden, kTcHidden, kTcHidden);
-        if (layer == 1) load_weights(aB, net.w3t, kTcHidden, kTcRows, kTcHidden);
         if (layer < 2) {
+            if (tid == 0) bulk_g2s(aB, w_src(layer + 1), w_bytes(layer + 1), aW);
+            w_pending = true;
             const float* bias = sBias + layer * kTcHidden;
             for (int c = cgroup * 64; c < cgroup * 64 + 64; c += 32) {
                 float v[32];
@@ -286,10 +330,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) mlp_tc_kernel(TcNet net, const 
     }
     if (!ok) {
         if (tid == 0) atomicExch(error, 1);
-        // the MMAs of the timed-out layer may still run: give them a bounded second wait
-        mbar_wait(aM, phase);
+        // copies and MMAs still in flight: a bounded second wait before the block leaves
+        if (w_pending) mbar_wait(aW, wphase);
+        if (mma_pending) mbar_wait(aM, phase);
     }
-    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
     __syncthreads();
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTcCols));

@@ -307,6 +307,7 @@ struct rbmg_proposal {
     rbmg::DevBuf w1, w2, w3;            // bf16 [N][H], [H][H], [H][Op]
     // transposed bf16 copies for the fused inference kernel: [H][ldw1], [H][H], [w3_rows][H]
     rbmg::DevBuf w1t, w2t, w3t;
+    rbmg::DevBuf tcpack;                // the tensor-core kernel's B operands in its shared-memory layout (O <= 128)
     int ldw1 = 0, w3_rows = 0;
     rbmg::DevBuf tc_error;              // set by the tensor-core kernel when a bounded wait gives up
     int cap = 0;                        // activation rows held
@@ -337,6 +338,8 @@ int proposal_reserve(rbmg_proposal* p, int rows) {
     return RBMG_OK;
 }
 
+cudaError_t proposal_refresh_tc(rbmg_proposal* p, cudaStream_t st);
+
 cudaError_t proposal_refresh_bf16(rbmg_proposal* p, cudaStream_t st) {
     const float* w = p->master.as<float>();
     weights_to_bf16_kernel<<<blocks_for(static_cast<long>(p->N) * kHidden), 256, 0, st>>>(w + p->oW1, p->N, kHidden,
@@ -351,7 +354,8 @@ cudaError_t proposal_refresh_bf16(rbmg_proposal* p, cudaStream_t st) {
         w + p->oW2, kHidden, kHidden, kHidden, kHidden, p->w2t.as<bf16>());
     weights_to_bf16_t_kernel<<<blocks_for(static_cast<long>(p->w3_rows) * kHidden), 256, 0, st>>>(
         w + p->oW3, kHidden, p->O, p->w3_rows, kHidden, p->w3t.as<bf16>());
-    return cudaGetLastError();
+    const cudaError_t e = cudaGetLastError();
+    return e != cudaSuccess ? e : proposal_refresh_tc(p, st);
 }
 
 // logits_out [count][O] of the configurations spins [count][nw] (logits_out null: the
@@ -982,7 +986,18 @@ struct TcNet {
     const float* b1;
     const float* b2;
     const float* b3;
+    const bf16* pack;
 };
+size_t tc_pack_size(int ldw1);
+cudaError_t launch_tc_pack(const TcNet& net, bf16* pack, cudaStream_t st);
+// the tensor-core kernel's packed B operands from the transposed BF16 copies
+cudaError_t proposal_refresh_tc(rbmg_proposal* p, cudaStream_t st) {
+    if (p->O > 128) return cudaSuccess;
+    const TcNet tn{p->N, p->O, p->ldw1, p->w1t.as<bf16>(), p->w2t.as<bf16>(), p->w3t.as<bf16>(), nullptr, nullptr,
+                   nullptr, nullptr};
+    return launch_tc_pack(tn, p->tcpack.as<bf16>(), st);
+}
+
 cudaError_t launch_mlp_tc(const TcNet& net, int nw, const uint64_t* spins, int count, float* out, int* error,
                           cudaStream_t st);
 
@@ -1225,7 +1240,7 @@ cudaError_t launch_fused(const rbmg_proposal* p, const LearnedLaunch& L, const u
     const FusedNet net = fused_net(p);
     if (!PROPOSE && p->O <= 128) {
         // tcgen05 / TMEM path (one output pass of 128): every logits row of the chain comes from it
-        const TcNet tn{net.N, net.O, net.ldw1, net.w1t, net.w2t, net.w3t, net.b1, net.b2, net.b3};
+        const TcNet tn{net.N, net.O, net.ldw1, net.w1t, net.w2t, net.w3t, net.b1, net.b2, net.b3, p->tcpack.as<bf16>()};
         return launch_mlp_tc(tn, nwords_of(p->N), in, count, out, p->tc_error.as<int>(), st);
     }
     switch (nwords_of(p->N)) {
@@ -1336,6 +1351,7 @@ extern "C" int rbmg_proposal_create(int N, uint64_t seed, float lr, rbmg_proposa
     RBMG_CK(p->w1t.ensure(sizeof(bf16) * static_cast<size_t>(H) * p->ldw1));
     RBMG_CK(p->w2t.ensure(sizeof(bf16) * static_cast<size_t>(H) * H));
     RBMG_CK(p->w3t.ensure(sizeof(bf16) * static_cast<size_t>(p->w3_rows) * H));
+    if (p->O <= 128) RBMG_CK(p->tcpack.ensure(sizeof(bf16) * tc_pack_size(p->ldw1)));
     RBMG_CK(p->tc_error.ensure(sizeof(int)));
     RBMG_CK(cudaMemset(p->tc_error.p, 0, sizeof(int)));
     RBMG_CK(cudaMemcpy(p->master.p, h.data(), sizeof(float) * p->P, cudaMemcpyHostToDevice));
