@@ -599,15 +599,7 @@ struct LearnedLaunch {
     unsigned long long* proposals;
     int propose_next;            // accept kernel: also draw the next step's move (frozen network)
     int walker_base;             // walker index of entry 0 (a slice of the chain): keys its Philox streams
-    double* lpsi;                // [B] Re log psi of the current state: sum_j Re f(theta_j), FP64
-    int keep_re;                 // accept kernel: keep `re` current (the training target reads it)
 };
-
-__device__ __forceinline__ double warp_sum_xor_d(double v) {
-#pragma unroll
-    for (int off = 16; off >= 1; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-    return v;
-}
 
 template <int K, int NW>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock) learned_angles_kernel(RbmDev P, LearnedLaunch L) {
@@ -619,17 +611,12 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) learned_angles_kernel(Rbm
     for (int k = 0; k < NW; k++) s.w[k] = L.spins[static_cast<long>(w) * NW + k];
     float tr[K], ti[K];
     rbm_refresh(P, s, tr, ti, lane);
-    double sum = 0.0;
 #pragma unroll
     for (int k = 0; k < K; k++) {
         const long o = static_cast<long>(w) * P.Mpad + lane + 32 * k;
         L.theta[o] = make_float2(tr[k], ti[k]);
-        const float f = lc_re(tr[k], ti[k]);
-        L.re[o] = f;
-        sum += static_cast<double>(f);
+        L.re[o] = lc_re(tr[k], ti[k]);
     }
-    sum = warp_sum_xor_d(sum);
-    if (lane == 0) L.lpsi[w] = sum;
 }
 
 // the move of every walker drawn from the logits of its current state (warp per walker)
@@ -687,21 +674,21 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) learned_accept_kernel(Rbm
     const int w = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
     if (w >= L.B) return;
     // every independent load is issued up front: the move, the spins, the proposed
-    // state's logits row, Re log psi and the angles
+    // state's logits row, the angles and their Re f
     Spins<NW> s;
 #pragma unroll
     for (int k = 0; k < NW; k++) s.w[k] = L.spins[static_cast<long>(w) * NW + k];
     const int i = L.site[w], l = L.len[w];
     const float* rowp = L.logits_prop + static_cast<long>(w) * L.O;
     const RowRegs rr = load_row(rowp, L.N, lane);
-    const double lpsi = L.lpsi[w];
     const long base = static_cast<long>(w) * P.Mpad + lane;
-    float tr[K], ti[K];
+    float tr[K], ti[K], re[K];
 #pragma unroll
     for (int k = 0; k < K; k++) {
         const float2 t = L.theta[base + 32 * k];
         tr[k] = t.x;
         ti[k] = t.y;
+        re[k] = L.re[base + 32 * k];
     }
     // trial angles: two_s = 2 * (new spin) for each cluster site, added in cluster order;
     // the W rows of two sites are loaded together
@@ -736,16 +723,13 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) learned_accept_kernel(Rbm
             }
         }
     }
-    // Re log psi of the proposed state, summed in FP64; the difference to the stored value
-    // is the move's change of Re log psi (the state's own sum, so no drift accumulates)
-    double part = 0.0;
+    float part = 0.0f;
 #pragma unroll
     for (int k = 0; k < K; k++) {
         nre[k] = lc_re(nr[k], ni[k]);
-        part += static_cast<double>(nre[k]);
+        part = __fadd_rn(part, __fsub_rn(nre[k], re[k]));
     }
-    const double lpsi_new = warp_sum_xor_d(part);
-    const float delta = static_cast<float>(lpsi_new - lpsi);
+    const float delta = warp_sum_xor(part);
     const LogNorm ln = log_norms_of(rr, L.N, lane);
     const float logq_rev = (rowp[i] - ln.seed) + (rowp[L.N + l - 1] - ln.len);
     const float log_a = 2.0f * delta + logq_rev - L.logq_fwd[w];
@@ -756,12 +740,10 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) learned_accept_kernel(Rbm
     if (!accept) accept = rng.uniform() <= a;
     if (accept) {
 #pragma unroll
-        for (int k = 0; k < K; k++) L.theta[base + 32 * k] = make_float2(nr[k], ni[k]);
-        if (L.keep_re) {
-#pragma unroll
-            for (int k = 0; k < K; k++) L.re[base + 32 * k] = nre[k];
+        for (int k = 0; k < K; k++) {
+            L.theta[base + 32 * k] = make_float2(nr[k], ni[k]);
+            L.re[base + 32 * k] = nre[k];
         }
-        if (lane == 0) L.lpsi[w] = lpsi_new;
         float* cur = L.logits_cur + static_cast<long>(w) * L.O;
         for (int j = lane; j < L.O; j += 32) cur[j] = rowp[j];
     }
@@ -1278,7 +1260,7 @@ constexpr int kMaxSlices = 4;
 
 struct LearnedState {
     int B = 0, Mpad = 0, nw = 0, O = 0;
-    DevBuf theta, re, lpsi, spins_prop, spins_pre, site, len, logq, logits_cur, logits_prop, reward, rbar;
+    DevBuf theta, re, spins_prop, spins_pre, site, len, logq, logits_cur, logits_prop, reward, rbar;
     // extra streams of the frozen steps: slices of the walkers run as independent chains,
     // so that one slice's network pass overlaps another slice's accept pass
     cudaStream_t side[kMaxSlices - 1] = {};
@@ -1312,7 +1294,6 @@ LearnedLaunch learned_slice(const LearnedLaunch& L, int base, int count, int nw,
     h.logits_prop = L.logits_prop + b * L.O;
     h.theta = L.theta + b * Mpad;
     h.re = L.re + b * Mpad;
-    h.lpsi = L.lpsi + b;
     h.reward = L.reward + b;
     h.accepts = L.accepts + b;
     h.proposals = L.proposals + b;
@@ -1543,7 +1524,6 @@ extern "C" int rbmg_chain_learned_async(rbmg_chain* c, const rbmg_psi* psi, cons
         const size_t b = static_cast<size_t>(B);
         RBMG_CK(S->theta.ensure(sizeof(float2) * b * P.Mpad));
         RBMG_CK(S->re.ensure(sizeof(float) * b * P.Mpad));
-        RBMG_CK(S->lpsi.ensure(sizeof(double) * b));
         RBMG_CK(S->spins_prop.ensure(sizeof(uint64_t) * b * c->nw));
         RBMG_CK(S->spins_pre.ensure(sizeof(uint64_t) * b * c->nw));
         RBMG_CK(S->site.ensure(sizeof(int) * b));
@@ -1570,8 +1550,6 @@ extern "C" int rbmg_chain_learned_async(rbmg_chain* c, const rbmg_psi* psi, cons
     L.logits_prop = S->logits_prop.as<float>();
     L.theta = S->theta.as<float2>();
     L.re = S->re.as<float>();
-    L.lpsi = S->lpsi.as<double>();
-    L.keep_re = train > 0 ? 1 : 0;
     L.reward = S->reward.as<float>();
     L.accepts = c->accepts.as<unsigned long long>();
     L.proposals = c->proposals.as<unsigned long long>();
