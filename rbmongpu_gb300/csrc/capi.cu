@@ -127,6 +127,11 @@ static int rbm_upload(rbmg_psi* p) {
     RBMG_CK(p->dW.ensure(hW.size() * sizeof(float2)));
     RBMG_CK(cudaMemcpyAsync(p->db.p, hb.data(), hb.size() * sizeof(float2), cudaMemcpyHostToDevice, stream()));
     RBMG_CK(cudaMemcpyAsync(p->dW.p, hW.data(), hW.size() * sizeof(float2), cudaMemcpyHostToDevice, stream()));
+    const size_t kp = static_cast<size_t>((p->Mpad / 32 + 1) / 2) * 32;
+    RBMG_CK(p->dWq.ensure(sizeof(float4) * kp * p->N));
+    RBMG_CK(p->dbq.ensure(sizeof(float4) * kp));
+    RBMG_CK(launch_rbm_pairs(p->N, p->Mpad, p->dW.as<float2>(), p->db.as<float2>(), p->dWq.as<float4>(),
+                             p->dbq.as<float4>(), stream()));
     RBMG_CK(cudaStreamSynchronize(stream()));
     p->f64_valid = false;
     return RBMG_OK;

@@ -76,7 +76,7 @@ struct rbmg_psi {
     // RBM
     int M = 0, Mpad = 0;
     std::vector<rbmg::cplx> b, W;
-    rbmg::DevBuf dW, db;
+    rbmg::DevBuf dW, db, dWq, dbq;     // complex64 rows, and the sampler's paired copies (kernels.h)
     mutable rbmg::DevBuf dW64, db64;   // FP64 copies for the Hilbert-space distance pass, uploaded on use
     mutable bool f64_valid = false;
     // deep / pair
@@ -96,7 +96,8 @@ struct rbmg_psi {
 
     int num_params() const;
     rbmg::RbmDev rbm_dev() const {
-        return rbmg::RbmDev{N, M, Mpad, static_cast<const float2*>(dW.p), static_cast<const float2*>(db.p)};
+        return rbmg::RbmDev{N, M, Mpad, static_cast<const float2*>(dW.p), static_cast<const float2*>(db.p),
+                            static_cast<const float4*>(dWq.p), static_cast<const float4*>(dbq.p)};
     }
 };
 

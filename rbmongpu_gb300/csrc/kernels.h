@@ -17,7 +17,16 @@ struct RbmDev {
     int N, M, Mpad;
     const float2* W;
     const float2* b;
+    // the same parameters with hidden units k and k + 1 of a lane side by side (lane l,
+    // pair kk: units j = l + 32 (2 kk) and l + 32 (2 kk + 1)), as (x_j0, x_j1, y_j0, y_j1):
+    // Wq [N][ceil(K / 2)][32], bq [ceil(K / 2)][32]; the unit beyond an odd K is zero
+    const float4* Wq;
+    const float4* bq;
 };
+
+// build Wq, bq from W [N][Mpad], b [Mpad] (K = Mpad / 32 hidden units per lane)
+cudaError_t launch_rbm_pairs(int N, int Mpad, const float2* W, const float2* b, float4* Wq, float4* bq,
+                             cudaStream_t st);
 
 // Pauli-string operator in compact form (built from the reference's padded
 // table, include/operator/Operator.hpp:30-88).

@@ -248,6 +248,8 @@ int psi_scatter(rbmg_psi* psi, const double2* packed) {
         rbm_scatter_kernel<<<blocks_of(total, 256), 256, 0, stream()>>>(packed, psi->N, psi->M, psi->Mpad,
                                                                          psi->db.as<float2>(), psi->dW.as<float2>());
         RBMG_CK(cudaGetLastError());
+        RBMG_CK(launch_rbm_pairs(psi->N, psi->Mpad, psi->dW.as<float2>(), psi->db.as<float2>(), psi->dWq.as<float4>(),
+                                 psi->dbq.as<float4>(), stream()));
         // the FP64 copies (exact-summation weights, Hilbert-space distance) in the host
         // layout b [M], W [N][M] are the packed vector's tail as it stands
         const size_t M = psi->M, NM = static_cast<size_t>(psi->N) * psi->M;

@@ -29,6 +29,30 @@ cudaError_t launch_rbm_mc(const RbmDev& P, const OpDev* op, const McLaunch& L, c
     }
 }
 
+// Wq [N][KP][32], bq [KP][32] (KP = ceil(K / 2)): entry (row, kk, lane) holds units
+// j0 = lane + 32 (2 kk) and j1 = j0 + 32; row N is the bias
+__global__ void rbm_pairs_kernel(int N, int Mpad, int KP, const float2* W, const float2* b, float4* Wq, float4* bq) {
+    const long idx = static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const long per_row = static_cast<long>(KP) * 32;
+    if (idx >= (N + 1) * per_row) return;
+    const int row = static_cast<int>(idx / per_row);
+    const int rem = static_cast<int>(idx - row * per_row);
+    const int kk = rem / 32, lane = rem % 32;
+    const int j0 = lane + 32 * (2 * kk), j1 = j0 + 32;
+    const float2* src = row < N ? W + static_cast<long>(row) * Mpad : b;
+    const float2 a = j0 < Mpad ? src[j0] : make_float2(0.0f, 0.0f);
+    const float2 c = j1 < Mpad ? src[j1] : make_float2(0.0f, 0.0f);
+    (row < N ? Wq[idx] : bq[rem]) = make_float4(a.x, c.x, a.y, c.y);
+}
+
+cudaError_t launch_rbm_pairs(int N, int Mpad, const float2* W, const float2* b, float4* Wq, float4* bq,
+                             cudaStream_t st) {
+    const int KP = (Mpad / 32 + 1) / 2;
+    const long n = static_cast<long>(N + 1) * KP * 32;
+    rbm_pairs_kernel<<<static_cast<int>((n + 255) / 256), 256, 0, st>>>(N, Mpad, KP, W, b, Wq, bq);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_rbm_estimate(const RbmDev& P, const OpDev* op, const RbmDev* PP, const EstLaunch& L,
                                 cudaStream_t st) {
     if (PP && PP->Mpad != P.Mpad) return cudaErrorInvalidValue;

@@ -144,6 +144,111 @@ __device__ __forceinline__ bool rbm_mh_step(const RbmDev& P, Spins<NW>& s, float
     return accept;
 }
 
+// ---------------------------------------------------------------------------
+// The sampler's form of the above on packed pairs (device_math.cuh: pair_t, FP32x2):
+// pair kk of a lane holds hidden units k = 2 kk and 2 kk + 1; every half is computed with
+// the scalar form's operations in its order, so angles, Re f and the decision are the
+// scalar ones bit for bit.  KP = ceil(K / 2); for odd K the last pair's second unit is a
+// zero row (W and b padded) that enters no sum.
+// ---------------------------------------------------------------------------
+template <int KP, int NW>
+__device__ __forceinline__ void rbm_refresh2(const RbmDev& P, const Spins<NW>& s, pair_t (&tr)[KP],
+                                             pair_t (&ti)[KP], int lane) {
+#pragma unroll
+    for (int kk = 0; kk < KP; kk++) {
+        const float4 b = __ldg(P.bq + kk * 32 + lane);
+        tr[kk] = pk2(b.x, b.y);
+        ti[kk] = pk2(b.z, b.w);
+    }
+    const float4* row = P.Wq + lane;
+    for (int i = 0; i < P.N; i++, row += KP * 32) {
+        const pair_t sg = splat2(s.up(i) ? 1.0f : -1.0f);
+#pragma unroll
+        for (int kk = 0; kk < KP; kk++) {
+            const float4 w = __ldg(row + 32 * kk);
+            tr[kk] = fma2(sg, pk2(w.x, w.y), tr[kk]);   // sg = +-1: the products are exact
+            ti[kk] = fma2(sg, pk2(w.z, w.w), ti[kk]);
+        }
+    }
+}
+
+template <int K, int KP, int NW, class Rng>
+__device__ __forceinline__ bool rbm_mh_step2(const RbmDev& P, Spins<NW>& s, pair_t (&tr)[KP], pair_t (&ti)[KP],
+                                             pair_t (&re)[KP], Rng& rng, int lane, int total_z, uint64_t nmagic) {
+    const uint32_t N = static_cast<uint32_t>(P.N);
+    int sites[2];
+    int ns = 1;
+    sites[0] = static_cast<int>(fastmod(rng.next(), nmagic, N));
+    if (total_z) {
+        const bool first_new = !s.up(sites[0]);
+        int sec = sites[0];
+        for (int guard = 0; guard < (1 << 20); guard++) {
+            const int c = static_cast<int>(fastmod(rng.next(), nmagic, N));
+            const bool v = c == sites[0] ? first_new : s.up(c);
+            if (v == first_new) { sec = c; break; }
+        }
+        sites[1] = sec;
+        ns = 2;
+    }
+    Spins<NW> s2 = s;
+    pair_t two_s[2];
+    const float4* rows[2];
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+        if (q >= ns) break;
+        const int site = q == 0 ? sites[0] : sites[1];
+        s2.flip(site);
+        two_s[q] = splat2(s2.up(site) ? 2.0f : -2.0f);
+        rows[q] = P.Wq + static_cast<long>(site) * KP * 32 + lane;
+    }
+    float part = 0.0f;
+    if (ns == 1) {
+        // single flip: the KP loads of the paired W row are issued together
+        float4 w[KP];
+#pragma unroll
+        for (int kk = 0; kk < KP; kk++) w[kk] = __ldg(rows[0] + 32 * kk);
+#pragma unroll
+        for (int kk = 0; kk < KP; kk++) {
+            const pair_t nr = fma2(two_s[0], pk2(w[kk].x, w[kk].y), tr[kk]);
+            const pair_t ni = fma2(two_s[0], pk2(w[kk].z, w[kk].w), ti[kk]);
+            float d0, d1;
+            up2(sub2(lc_re2(nr, ni), re[kk]), d0, d1);
+            part = __fadd_rn(part, d0);
+            if (2 * kk + 1 < K) part = __fadd_rn(part, d1);
+        }
+    } else {
+#pragma unroll
+        for (int kk = 0; kk < KP; kk++) {
+            pair_t nr = tr[kk], ni = ti[kk];
+            for (int q = 0; q < ns; q++) {
+                const float4 w = __ldg(rows[q] + 32 * kk);
+                nr = fma2(two_s[q], pk2(w.x, w.y), nr);
+                ni = fma2(two_s[q], pk2(w.z, w.w), ni);
+            }
+            float d0, d1;
+            up2(sub2(lc_re2(nr, ni), re[kk]), d0, d1);
+            part = __fadd_rn(part, d0);
+            if (2 * kk + 1 < K) part = __fadd_rn(part, d1);
+        }
+    }
+    const float delta = warp_sum_xor(part);
+    bool accept = delta > 0.0f;
+    if (!accept) accept = rng.uniform() <= expf_det(__fmul_rn(2.0f, delta));
+    if (accept) {
+        s = s2;
+#pragma unroll
+        for (int kk = 0; kk < KP; kk++) {
+            for (int q = 0; q < ns; q++) {
+                const float4 w = __ldg(rows[q] + 32 * kk);
+                tr[kk] = fma2(two_s[q], pk2(w.x, w.y), tr[kk]);
+                ti[kk] = fma2(two_s[q], pk2(w.z, w.w), ti[kk]);
+            }
+            re[kk] = lc_re2(tr[kk], ti[kk]);
+        }
+    }
+    return accept;
+}
+
 // sign * (-i)^ypow * coef of string n for the current (original) spins, in FP32: the
 // local-energy sums run in FP32 with compensated (Kahan) accumulation, since GB300's
 // FP64 rate is 1/64 of its FP32 rate and every lane of the warp executes the sum
@@ -291,15 +396,17 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, K > 13 ? 3 : 4) rbm_mc_ke
 #pragma unroll
         for (int k = 0; k < NW; k++) s.w[k] = L.spins[static_cast<long>(w) * NW + k];
     }
-    float tr[K], ti[K], re[K];
+    constexpr int KP = (K + 1) / 2;
+    pair_t tr[KP], ti[KP], re[KP];
     unsigned long long acc = 0, props = 0;
     const int total_sweeps = L.n_therm + L.n_samples * L.sweeps_per_sample;
     int sample = 0;
     for (int sw = 0; sw < total_sweeps; sw++) {
-        rbm_refresh(P, s, tr, ti, lane);
+        rbm_refresh2(P, s, tr, ti, lane);
 #pragma unroll
-        for (int k = 0; k < K; k++) re[k] = lc_re(tr[k], ti[k]);
-        for (int p = 0; p < P.N; p++) acc += rbm_mh_step(P, s, tr, ti, re, rng, lane, L.total_z, nmagic);
+        for (int kk = 0; kk < KP; kk++) re[kk] = lc_re2(tr[kk], ti[kk]);
+        for (int p = 0; p < P.N; p++)
+            acc += rbm_mh_step2<K>(P, s, tr, ti, re, rng, lane, L.total_z, nmagic);
         props += P.N;
         const int done = sw + 1 - L.n_therm;
         if (done > 0 && done % L.sweeps_per_sample == 0) {
