@@ -259,21 +259,18 @@ class Psi(_PsiBase):
         self.params = p
 
     def to_json(self):
-        """pyRBMonGPU/Psi.py:8-22"""
-        def cplx(a):
-            a = np.asarray(a)
-            return {"real": a.real.tolist(), "imag": a.imag.tolist()}
-        return {"type": "Psi", "alpha": self.alpha.tolist(), "beta": self.beta.tolist(), "b": cplx(self.b),
-                "W": cplx(self.W), "prefactor": self.prefactor}
+        """pyRBMonGPU/Psi.py:8-22: the parameters in the reference's JSON form."""
+        from .json_numpy import encode
+        return encode(dict(type="Psi", alpha=self.alpha, beta=self.beta, b=self.b, W=self.W,
+                           prefactor=self.prefactor))
 
     @staticmethod
     def from_json(obj, gpu=True):
-        def arr(v):
-            if isinstance(v, dict):
-                return np.asarray(v["real"]) + 1j * np.asarray(v["imag"])
-            return np.asarray(v)
-        return Psi(arr(obj["alpha"]).real, arr(obj["beta"]).real, arr(obj["b"]), arr(obj["W"]), obj["prefactor"],
-                   False, gpu)
+        """pyRBMonGPU/Psi.py:38-47 (arrays in the reference's JSON form or as numpy arrays)."""
+        from .json_numpy import decode
+        o = decode(obj)
+        return Psi(np.asarray(o["alpha"]).real, np.asarray(o["beta"]).real, o["b"], o["W"], o["prefactor"], False,
+                   gpu)
 
 
 class PsiDeep(_PsiBase):
@@ -351,10 +348,35 @@ class PsiDeep(_PsiBase):
         return slice(2 * self.N, 2 * self.N + conn * size + size)
 
 
+def _deep_to_json(self, kind):
+    """pyRBMonGPU/PsiDeep.py:8-24 (PsiPair.py alike)."""
+    from .json_numpy import encode
+    return encode(dict(type=kind, alpha=self.alpha, beta=self.beta, b=list(self.b), connections=list(self.connections),
+                       W=list(self.W), final_weights=self.final_weights, prefactor=self.prefactor,
+                       free_quantum_axis=self.free_quantum_axis))
+
+
+def _deep_from_json(cls, obj, gpu):
+    """pyRBMonGPU/PsiDeep.py:27-46: final_weights default to ones of the last layer's size."""
+    from .json_numpy import decode
+    o = decode(obj)
+    fw = o["final_weights"] if "final_weights" in o else np.ones(np.asarray(o["W"][-1]).shape[-1])
+    return cls(np.asarray(o["alpha"]).real, np.asarray(o["beta"]).real, o["b"], o["connections"], o["W"], fw,
+               o["prefactor"], bool(o.get("free_quantum_axis", False)), gpu)
+
+
+PsiDeep.to_json = lambda self: _deep_to_json(self, "PsiDeep")
+PsiDeep.from_json = staticmethod(lambda obj, gpu=True: _deep_from_json(PsiDeep, obj, gpu))
+
+
 class PsiPair(PsiDeep):
     """Two real PsiDeep nets for Re / Im log psi (include/quantum_state/PsiPair.hpp:166-205)."""
 
     _pair = 1
+
+
+PsiPair.to_json = lambda self: _deep_to_json(self, "PsiPair")
+PsiPair.from_json = staticmethod(lambda obj, gpu=True: _deep_from_json(PsiPair, obj, gpu))
 
 
 # --------------------------------------------------------------------- operator
