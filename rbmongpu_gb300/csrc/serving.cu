@@ -36,6 +36,8 @@ struct SInst {
     int N, M, Mpad, K, nw;
     const float2* W;
     const float2* b;
+    const float4* Wq;     // W and b with a lane's hidden units k and k + 1 side by side (kernels.h)
+    const float4* bq;
     OpDev op;
     int walkers;
     uint64_t seed;
@@ -95,24 +97,49 @@ __device__ __forceinline__ void s_refresh(const SInst& I, const Spins<NW>& s, fl
     }
 }
 
-// single-flip Metropolis step: the arithmetic and draw order of rbm_mh_step
-template <int K, int NW>
-__device__ __forceinline__ bool s_mh_step(const SInst& I, Spins<NW>& s, float (&tr)[K], float (&ti)[K],
-                                          float (&re)[K], WarpRng& rng, int lane, uint64_t nmagic) {
+// the sweeps on packed pairs (rbm_refresh2 / rbm_mh_step2 of the single-network sampler,
+// same arithmetic and draw order)
+template <int KP, int NW>
+__device__ __forceinline__ void s_refresh2(const SInst& I, const Spins<NW>& s, pair_t (&tr)[KP], pair_t (&ti)[KP],
+                                           int lane) {
+#pragma unroll
+    for (int kk = 0; kk < KP; kk++) {
+        const float4 b = __ldg(I.bq + kk * 32 + lane);
+        tr[kk] = pk2(b.x, b.y);
+        ti[kk] = pk2(b.z, b.w);
+    }
+    const float4* row = I.Wq + lane;
+    for (int i = 0; i < I.N; i++, row += KP * 32) {
+        const pair_t sg = splat2(s.up(i) ? 1.0f : -1.0f);
+#pragma unroll
+        for (int kk = 0; kk < KP; kk++) {
+            const float4 w = __ldg(row + 32 * kk);
+            tr[kk] = fma2(sg, pk2(w.x, w.y), tr[kk]);
+            ti[kk] = fma2(sg, pk2(w.z, w.w), ti[kk]);
+        }
+    }
+}
+
+template <int K, int KP, int NW>
+__device__ __forceinline__ bool s_mh_step2(const SInst& I, Spins<NW>& s, pair_t (&tr)[KP], pair_t (&ti)[KP],
+                                           pair_t (&re)[KP], WarpRng& rng, int lane, uint64_t nmagic) {
     const int site = static_cast<int>(fastmod(rng.next(), nmagic, static_cast<uint32_t>(I.N)));
     Spins<NW> s2 = s;
     s2.flip(site);
-    const float two_s = s2.up(site) ? 2.0f : -2.0f;
-    const float2* row = I.W + static_cast<long>(site) * I.Mpad + lane;
-    float2 w[K];
+    const pair_t two_s = splat2(s2.up(site) ? 2.0f : -2.0f);
+    const float4* row = I.Wq + static_cast<long>(site) * KP * 32 + lane;
+    float4 w[KP];
 #pragma unroll
-    for (int k = 0; k < K; k++) w[k] = __ldg(row + 32 * k);
+    for (int kk = 0; kk < KP; kk++) w[kk] = __ldg(row + 32 * kk);
     float part = 0.0f;
 #pragma unroll
-    for (int k = 0; k < K; k++) {
-        const float nr = __fmaf_rn(two_s, w[k].x, tr[k]);
-        const float ni = __fmaf_rn(two_s, w[k].y, ti[k]);
-        part = __fadd_rn(part, __fsub_rn(lc_re(nr, ni), re[k]));
+    for (int kk = 0; kk < KP; kk++) {
+        const pair_t nr = fma2(two_s, pk2(w[kk].x, w[kk].y), tr[kk]);
+        const pair_t ni = fma2(two_s, pk2(w[kk].z, w[kk].w), ti[kk]);
+        float d0, d1;
+        up2(sub2(lc_re2(nr, ni), re[kk]), d0, d1);
+        part = __fadd_rn(part, d0);
+        if (2 * kk + 1 < K) part = __fadd_rn(part, d1);
     }
     const float delta = warp_sum_xor(part);
     bool accept = delta > 0.0f;
@@ -120,11 +147,11 @@ __device__ __forceinline__ bool s_mh_step(const SInst& I, Spins<NW>& s, float (&
     if (accept) {
         s = s2;
 #pragma unroll
-        for (int k = 0; k < K; k++) {
-            const float2 ww = __ldg(row + 32 * k);
-            tr[k] = __fmaf_rn(two_s, ww.x, tr[k]);
-            ti[k] = __fmaf_rn(two_s, ww.y, ti[k]);
-            re[k] = lc_re(tr[k], ti[k]);
+        for (int kk = 0; kk < KP; kk++) {
+            const float4 ww = __ldg(row + 32 * kk);
+            tr[kk] = fma2(two_s, pk2(ww.x, ww.y), tr[kk]);
+            ti[kk] = fma2(two_s, pk2(ww.z, ww.w), ti[kk]);
+            re[kk] = lc_re2(tr[kk], ti[kk]);
         }
     }
     return accept;
@@ -159,17 +186,21 @@ __device__ __noinline__ void walker_task(const SLaunch& L, const SInst& Ig, int 
         for (int k = 0; k < NW; k++)
             if (k < I.nw) s.w[k] = I.spins[static_cast<long>(w) * I.nw + k];
     }
-    float tr[K], ti[K], re[K];
     unsigned long long acc = 0;
-    const int total = (L.first ? L.therm : 0) + L.sweeps;
-    for (int sw = 0; sw < total; sw++) {
-        s_refresh(I, s, tr, ti, lane);
+    {
+        constexpr int KP = (K + 1) / 2;
+        pair_t tp[KP], tq[KP], rp[KP];
+        const int total = (L.first ? L.therm : 0) + L.sweeps;
+        for (int sw = 0; sw < total; sw++) {
+            s_refresh2(I, s, tp, tq, lane);
 #pragma unroll
-        for (int k = 0; k < K; k++) re[k] = lc_re(tr[k], ti[k]);
-        for (int p = 0; p < I.N; p++) acc += s_mh_step(I, s, tr, ti, re, rng, lane, nmagic);
+            for (int kk = 0; kk < KP; kk++) rp[kk] = lc_re2(tp[kk], tq[kk]);
+            for (int p = 0; p < I.N; p++) acc += s_mh_step2<K>(I, s, tp, tq, rp, rng, lane, nmagic);
+        }
     }
     // measurement: local energy and tanh(theta) of the final configuration; f(theta) in
     // this warp's shared-memory slice [kSK][32] keeps the register footprint of the sweeps
+    float tr[K], ti[K];
     s_refresh(I, s, tr, ti, lane);
     extern __shared__ float2 s_f[];
     float2* myf = s_f + (threadIdx.x >> 5) * kSK * 32 + lane;
@@ -486,6 +517,8 @@ extern "C" int rbmg_batch_create(int n, const rbmg_psi* const* psis, const rbmg_
         const RbmDev d = p->rbm_dev();
         I.W = d.W;
         I.b = d.b;
+        I.Wq = d.Wq;
+        I.bq = d.bq;
         I.op = o->dev();
         I.walkers = static_cast<int>(walkers[i]);
         I.seed = seeds[i];

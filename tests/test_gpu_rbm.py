@@ -201,3 +201,31 @@ def test_params_roundtrip_and_errors():
         rg.MonteCarloLoop(10, 1, 0, 3)   # samples not a multiple of chains
     with pytest.raises(rg.RbmgError):
         rg.ExpectationValue()(psi, rg.Operator(*rg.operators.tfim_chain(20)), rg.ExactSummation(12))
+
+
+@pytest.mark.parametrize("N,M,chains", [(10, 20, 7), (40, 60, 16), (150, 100, 5), (70, 250, 16), (100, 400, 9),
+                                        (200, 576, 6)])
+def test_mc_chains_bit_exact_every_instantiation(N, M, chains):
+    """Every hidden-units-per-lane count (K = 1, 2, 4, 8, 13, 18: odd ones with the paired
+    form's zero unit), one to four spin words (N up to 200), walker counts that do not fill
+    a block: spins and accept counts equal the restatement's bit for bit."""
+    rng = np.random.default_rng(N * 1000 + M)
+    b = 0.1 * (rng.normal(size=M) + 1j * rng.normal(size=M))
+    W = 0.1 * (rng.normal(size=(N, M)) + 1j * rng.normal(size=(N, M)))
+    psi = rg.Psi(np.zeros(N), np.zeros(N), b, W, 1.0, False, True)
+    samples, therm, seed = 2, 1, 31
+    mc = rg.MonteCarloLoop(chains * samples, 1, therm, chains, seed=seed)
+    sp, _, _ = mc.samples(psi)
+    acc_gpu, props = mc.acceptance()
+    ospins, _, _, oacc, orej = po.mc_run(po.RBM(b, W, 1.0), None, chains, samples, 1, therm, seed=seed,
+                                         want_eloc=False)
+    assert np.array_equal(sp.reshape(samples, chains, -1), ospins)
+    assert int(acc_gpu) == int(oacc.sum()) > 0
+    assert int(props) == int((oacc + orej).sum())
+
+
+def test_local_energies_of_no_configurations():
+    c = Case("c1_rbm_exact")
+    psi = rbm_gpu(c)
+    out = rg.local_energies(psi, rg.Operator(*c.op()), np.zeros((0, 1), np.uint64))
+    assert out.shape == (0,)
