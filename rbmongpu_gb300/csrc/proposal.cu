@@ -592,8 +592,8 @@ struct LearnedLaunch {
     float* logq_fwd;             // [B]
     float* logits_cur;           // [B][O] logits at the current state
     const float* logits_prop;    // [B][O] logits at the proposed state
-    float2* theta;               // [B][Mpad]
-    float* re;                   // [B][Mpad] Re f(theta)
+    float4* theta;               // [B][KP][32] angles of a lane's units 2 kk, 2 kk + 1: (re, re, im, im)
+    float2* re;                  // [B][KP][32] their Re f(theta)   (KP = ceil(K / 2), kernels.h pairing)
     float* reward;               // [B]
     unsigned long long* accepts;
     unsigned long long* proposals;
@@ -609,13 +609,18 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) learned_angles_kernel(Rbm
     Spins<NW> s;
 #pragma unroll
     for (int k = 0; k < NW; k++) s.w[k] = L.spins[static_cast<long>(w) * NW + k];
-    float tr[K], ti[K];
-    rbm_refresh(P, s, tr, ti, lane);
+    constexpr int KP = (K + 1) / 2;
+    pair_t tr[KP], ti[KP];
+    rbm_refresh2(P, s, tr, ti, lane);
 #pragma unroll
-    for (int k = 0; k < K; k++) {
-        const long o = static_cast<long>(w) * P.Mpad + lane + 32 * k;
-        L.theta[o] = make_float2(tr[k], ti[k]);
-        L.re[o] = lc_re(tr[k], ti[k]);
+    for (int kk = 0; kk < KP; kk++) {
+        const long o = (static_cast<long>(w) * KP + kk) * 32 + lane;
+        float a0, a1, b0, b1, r0, r1;
+        up2(tr[kk], a0, a1);
+        up2(ti[kk], b0, b1);
+        up2(lc_re2(tr[kk], ti[kk]), r0, r1);
+        L.theta[o] = make_float4(a0, a1, b0, b1);
+        L.re[o] = make_float2(r0, r1);
     }
 }
 
@@ -681,53 +686,44 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) learned_accept_kernel(Rbm
     const int i = L.site[w], l = L.len[w];
     const float* rowp = L.logits_prop + static_cast<long>(w) * L.O;
     const RowRegs rr = load_row(rowp, L.N, lane);
-    const long base = static_cast<long>(w) * P.Mpad + lane;
-    float tr[K], ti[K], re[K];
+    constexpr int KP = (K + 1) / 2;
+    const long base = static_cast<long>(w) * KP * 32 + lane;
+    pair_t tr[KP], ti[KP], re[KP];
 #pragma unroll
-    for (int k = 0; k < K; k++) {
-        const float2 t = L.theta[base + 32 * k];
-        tr[k] = t.x;
-        ti[k] = t.y;
-        re[k] = L.re[base + 32 * k];
+    for (int kk = 0; kk < KP; kk++) {
+        const float4 t = L.theta[base + 32 * kk];
+        const float2 f = L.re[base + 32 * kk];
+        tr[kk] = pk2(t.x, t.y);
+        ti[kk] = pk2(t.z, t.w);
+        re[kk] = pk2(f.x, f.y);
     }
-    // trial angles: two_s = 2 * (new spin) for each cluster site, added in cluster order;
-    // the W rows of two sites are loaded together
-    float nr[K], ni[K], nre[K];
+    // trial angles: two_s = 2 * (new spin) for each cluster site, added in cluster order
+    // (per unit the scalar sequence), from the paired W rows
+    pair_t nr[KP], ni[KP], nre[KP];
 #pragma unroll
-    for (int k = 0; k < K; k++) { nr[k] = tr[k]; ni[k] = ti[k]; }
-    for (int q = 0; q < l; q += 2) {
-        int c0 = i + q;
-        if (c0 >= P.N) c0 -= P.N;
-        int c1 = c0 + 1;
-        if (c1 >= P.N) c1 -= P.N;
-        const bool two = q + 1 < l;
-        const float s0 = s.up(c0) ? -2.0f : 2.0f, s1 = s.up(c1) ? -2.0f : 2.0f;
-        const float2* row0 = P.W + static_cast<long>(c0) * P.Mpad + lane;
-        const float2* row1 = P.W + static_cast<long>(c1) * P.Mpad + lane;
-        float2 w0[K], w1[K];
+    for (int kk = 0; kk < KP; kk++) { nr[kk] = tr[kk]; ni[kk] = ti[kk]; }
+    for (int q = 0; q < l; q++) {
+        int c = i + q;
+        if (c >= P.N) c -= P.N;
+        const pair_t ts = splat2(s.up(c) ? -2.0f : 2.0f);
+        const float4* row = P.Wq + static_cast<long>(c) * KP * 32 + lane;
+        float4 wv[KP];
 #pragma unroll
-        for (int k = 0; k < K; k++) {
-            w0[k] = __ldg(row0 + 32 * k);
-            w1[k] = two ? __ldg(row1 + 32 * k) : make_float2(0.0f, 0.0f);
-        }
+        for (int kk = 0; kk < KP; kk++) wv[kk] = __ldg(row + 32 * kk);
 #pragma unroll
-        for (int k = 0; k < K; k++) {
-            nr[k] = __fmaf_rn(s0, w0[k].x, nr[k]);
-            ni[k] = __fmaf_rn(s0, w0[k].y, ni[k]);
-        }
-        if (two) {
-#pragma unroll
-            for (int k = 0; k < K; k++) {
-                nr[k] = __fmaf_rn(s1, w1[k].x, nr[k]);
-                ni[k] = __fmaf_rn(s1, w1[k].y, ni[k]);
-            }
+        for (int kk = 0; kk < KP; kk++) {
+            nr[kk] = fma2(ts, pk2(wv[kk].x, wv[kk].y), nr[kk]);
+            ni[kk] = fma2(ts, pk2(wv[kk].z, wv[kk].w), ni[kk]);
         }
     }
     float part = 0.0f;
 #pragma unroll
-    for (int k = 0; k < K; k++) {
-        nre[k] = lc_re(nr[k], ni[k]);
-        part = __fadd_rn(part, __fsub_rn(nre[k], re[k]));
+    for (int kk = 0; kk < KP; kk++) {
+        nre[kk] = lc_re2(nr[kk], ni[kk]);
+        float d0, d1;
+        up2(sub2(nre[kk], re[kk]), d0, d1);
+        part = __fadd_rn(part, d0);
+        if (2 * kk + 1 < K) part = __fadd_rn(part, d1);
     }
     const float delta = warp_sum_xor(part);
     const LogNorm ln = log_norms_of(rr, L.N, lane);
@@ -740,9 +736,13 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) learned_accept_kernel(Rbm
     if (!accept) accept = rng.uniform() <= a;
     if (accept) {
 #pragma unroll
-        for (int k = 0; k < K; k++) {
-            L.theta[base + 32 * k] = make_float2(nr[k], ni[k]);
-            L.re[base + 32 * k] = nre[k];
+        for (int kk = 0; kk < KP; kk++) {
+            float a0, a1, b0, b1, r0, r1;
+            up2(nr[kk], a0, a1);
+            up2(ni[kk], b0, b1);
+            up2(nre[kk], r0, r1);
+            L.theta[base + 32 * kk] = make_float4(a0, a1, b0, b1);
+            L.re[base + 32 * kk] = make_float2(r0, r1);
         }
         float* cur = L.logits_cur + static_cast<long>(w) * L.O;
         for (int j = lane; j < L.O; j += 32) cur[j] = rowp[j];
@@ -797,7 +797,7 @@ __device__ __forceinline__ float log_add(float a, float b) {
 // into the seed and length softmaxes, whose optimum is the marginals of p*).
 template <int K, int NW>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock) lb_target_kernel(RbmDev P, int n, const uint64_t* spins,
-                                                                       const float2* theta, const float* re_all,
+                                                                       const float4* theta, const float2* re_all,
                                                                        const float* logits, int O, float* dl) {
     const int lane = threadIdx.x & 31;
     const int w = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
@@ -805,14 +805,21 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) lb_target_kernel(RbmDev P
     Spins<NW> s;
 #pragma unroll
     for (int k = 0; k < NW; k++) s.w[k] = spins[static_cast<long>(w) * NW + k];
-    const long base = static_cast<long>(w) * P.Mpad + lane;
+    constexpr int KP = (K + 1) / 2;
+    const long base = static_cast<long>(w) * KP * 32 + lane;
     float tr[K], ti[K], re[K];
 #pragma unroll
-    for (int k = 0; k < K; k++) {
-        const float2 t = theta[base + 32 * k];
-        tr[k] = t.x;
-        ti[k] = t.y;
-        re[k] = re_all[base + 32 * k];
+    for (int kk = 0; kk < KP; kk++) {
+        const float4 t = theta[base + 32 * kk];
+        const float2 f = re_all[base + 32 * kk];
+        tr[2 * kk] = t.x;
+        ti[2 * kk] = t.z;
+        re[2 * kk] = f.x;
+        if (2 * kk + 1 < K) {
+            tr[2 * kk + 1] = t.y;
+            ti[2 * kk + 1] = t.w;
+            re[2 * kk + 1] = f.y;
+        }
     }
     constexpr int kSlots = (64 * NW + 31) / 32;   // seeds i = lane + 32 c held by lane
     float ms[kSlots], ml[kLengths];
@@ -950,7 +957,7 @@ cudaError_t launch_learned(int which, const RbmDev& P, const LearnedLaunch& L, c
 }
 
 template <int K>
-cudaError_t launch_lb_k(int nw, const RbmDev& P, int n, const uint64_t* spins, const float2* theta, const float* re,
+cudaError_t launch_lb_k(int nw, const RbmDev& P, int n, const uint64_t* spins, const float4* theta, const float2* re,
                         const float* logits, int O, float* dl, cudaStream_t st) {
     const dim3 grid((n + kWarpsPerBlock - 1) / kWarpsPerBlock), block(32 * kWarpsPerBlock);
     switch (nw) {
@@ -963,7 +970,7 @@ cudaError_t launch_lb_k(int nw, const RbmDev& P, int n, const uint64_t* spins, c
     return cudaGetLastError();
 }
 
-cudaError_t launch_lb_target(const RbmDev& P, int n, const uint64_t* spins, const float2* theta, const float* re,
+cudaError_t launch_lb_target(const RbmDev& P, int n, const uint64_t* spins, const float4* theta, const float2* re,
                              const float* logits, int O, float* dl, cudaStream_t st) {
     const int nw = nwords_of(P.N);
     switch (P.Mpad / 32) {
@@ -1292,8 +1299,9 @@ LearnedLaunch learned_slice(const LearnedLaunch& L, int base, int count, int nw,
     h.logq_fwd = L.logq_fwd + b;
     h.logits_cur = L.logits_cur + b * L.O;
     h.logits_prop = L.logits_prop + b * L.O;
-    h.theta = L.theta + b * Mpad;
-    h.re = L.re + b * Mpad;
+    const size_t per = static_cast<size_t>((Mpad / 32 + 1) / 2) * 32;   // KP * 32 entries per walker
+    h.theta = L.theta + b * per;
+    h.re = L.re + b * per;
     h.reward = L.reward + b;
     h.accepts = L.accepts + b;
     h.proposals = L.proposals + b;
@@ -1522,8 +1530,9 @@ extern "C" int rbmg_chain_learned_async(rbmg_chain* c, const rbmg_psi* psi, cons
         S->nw = c->nw;
         S->O = prop->O;
         const size_t b = static_cast<size_t>(B);
-        RBMG_CK(S->theta.ensure(sizeof(float2) * b * P.Mpad));
-        RBMG_CK(S->re.ensure(sizeof(float) * b * P.Mpad));
+        const size_t per = static_cast<size_t>((P.Mpad / 32 + 1) / 2) * 32;
+        RBMG_CK(S->theta.ensure(sizeof(float4) * b * per));
+        RBMG_CK(S->re.ensure(sizeof(float2) * b * per));
         RBMG_CK(S->spins_prop.ensure(sizeof(uint64_t) * b * c->nw));
         RBMG_CK(S->spins_pre.ensure(sizeof(uint64_t) * b * c->nw));
         RBMG_CK(S->site.ensure(sizeof(int) * b));
@@ -1548,8 +1557,8 @@ extern "C" int rbmg_chain_learned_async(rbmg_chain* c, const rbmg_psi* psi, cons
     L.logq_fwd = S->logq.as<float>();
     L.logits_cur = S->logits_cur.as<float>();
     L.logits_prop = S->logits_prop.as<float>();
-    L.theta = S->theta.as<float2>();
-    L.re = S->re.as<float>();
+    L.theta = S->theta.as<float4>();
+    L.re = S->re.as<float2>();
     L.reward = S->reward.as<float>();
     L.accepts = c->accepts.as<unsigned long long>();
     L.proposals = c->proposals.as<unsigned long long>();
