@@ -514,20 +514,32 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, K > 13 ? 3 : 4) rbm_eloc_
 #pragma unroll
         for (int k = 0; k < NW; k++) s.w[k] = L.spins[t * NW + k];
     }
-    float tr[K], ti[K];
-    rbm_refresh(P, s, tr, ti, lane);
-    float2 f[K];
+    // angles and f(theta) on packed pairs (units 2 kk, 2 kk + 1 of the lane): every half
+    // is the scalar arithmetic, the sums below run over the units in their scalar order
+    constexpr int KP = (K + 1) / 2;
+    pair_t tr[KP], ti[KP];
+    rbm_refresh2(P, s, tr, ti, lane);
+    // f(theta) of the configuration in this warp's shared-memory slice (re pair, im pair),
+    // read once per string: registers stay for the angles and the prefetched W rows
+    __shared__ float4 f_sm[kWarpsPerBlock][KP][32];
+    float4 (&f)[KP][32] = f_sm[threadIdx.x >> 5];
 #pragma unroll
-    for (int k = 0; k < K; k++) f[k] = lc_c(tr[k], ti[k]);
-    // the W row of the next single-flip string is loaded while the current string is
-    // evaluated, so the row's latency is off the per-string critical path
+    for (int kk = 0; kk < KP; kk++) {
+        const Pair2 v = lc_c2(tr[kk], ti[kk]);
+        float a0, a1, b0, b1;
+        up2(v.re, a0, a1);
+        up2(v.im, b0, b1);
+        f[kk][lane] = make_float4(a0, a1, b0, b1);
+    }
+    // the paired W row of the next single-flip string is loaded while the current string
+    // is evaluated, so the row's latency is off the per-string critical path
     KahanC acc;
-    float2 wbuf[K];
+    float4 wbuf[KP];
     int nxt = op.next1[0];
     if (nxt < op.S) {
-        const float2* row = P.W + static_cast<long>(op.site1[nxt]) * P.Mpad + lane;
+        const float4* row = P.Wq + static_cast<long>(op.site1[nxt]) * KP * 32 + lane;
 #pragma unroll
-        for (int k = 0; k < K; k++) wbuf[k] = __ldg(row + 32 * k);
+        for (int kk = 0; kk < KP; kk++) wbuf[kk] = __ldg(row + 32 * kk);
     }
     for (int n = 0; n < op.S; n++) {
         const float2 cf = string_factor(op, n, s);
@@ -537,39 +549,49 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, K > 13 ? 3 : 4) rbm_eloc_
             continue;
         }
         float2 part = make_float2(0.0f, 0.0f);
+        auto add_unit_pair = [&](const Pair2& g, int kk) {
+            const float4 f0 = f[kk][lane];
+            float a0, a1, b0, b1;
+            up2(sub2(g.re, pk2(f0.x, f0.y)), a0, a1);
+            up2(sub2(g.im, pk2(f0.z, f0.w)), b0, b1);
+            part.x += a0;
+            part.y += b0;
+            if (2 * kk + 1 < K) {
+                part.x += a1;
+                part.y += b1;
+            }
+        };
         if (nf == 1) {   // n == nxt
             const int site = op.site1[n];
-            const float two_s = s.up(site) ? -2.0f : 2.0f;
-            float2 w[K];
+            const pair_t two_s = splat2(s.up(site) ? -2.0f : 2.0f);
+            float4 w[KP];
 #pragma unroll
-            for (int k = 0; k < K; k++) w[k] = wbuf[k];
+            for (int kk = 0; kk < KP; kk++) w[kk] = wbuf[kk];
             nxt = op.next1[n + 1];
             if (nxt < op.S) {
-                const float2* row = P.W + static_cast<long>(op.site1[nxt]) * P.Mpad + lane;
+                const float4* row = P.Wq + static_cast<long>(op.site1[nxt]) * KP * 32 + lane;
 #pragma unroll
-                for (int k = 0; k < K; k++) wbuf[k] = __ldg(row + 32 * k);
+                for (int kk = 0; kk < KP; kk++) wbuf[kk] = __ldg(row + 32 * kk);
             }
 #pragma unroll
-            for (int k = 0; k < K; k++) {
-                const float2 g = lc_c(fmaf(two_s, w[k].x, tr[k]), fmaf(two_s, w[k].y, ti[k]));
-                part.x += g.x - f[k].x;
-                part.y += g.y - f[k].y;
+            for (int kk = 0; kk < KP; kk++) {
+                const Pair2 g = lc_c2(fma2(two_s, pk2(w[kk].x, w[kk].y), tr[kk]),
+                                      fma2(two_s, pk2(w[kk].z, w[kk].w), ti[kk]));
+                add_unit_pair(g, kk);
             }
         } else {
             const int off = op.flip_off[n];
 #pragma unroll
-            for (int k = 0; k < K; k++) {
-                float nr = tr[k], ni = ti[k];
+            for (int kk = 0; kk < KP; kk++) {
+                pair_t nr = tr[kk], ni = ti[kk];
                 for (int q = 0; q < nf; q++) {
                     const int site = op.flip_sites[off + q];
-                    const float two_s = s.up(site) ? -2.0f : 2.0f;
-                    const float2 w = __ldg(P.W + static_cast<long>(site) * P.Mpad + lane + 32 * k);
-                    nr = fmaf(two_s, w.x, nr);
-                    ni = fmaf(two_s, w.y, ni);
+                    const pair_t two_s = splat2(s.up(site) ? -2.0f : 2.0f);
+                    const float4 w = __ldg(P.Wq + static_cast<long>(site) * KP * 32 + lane + 32 * kk);
+                    nr = fma2(two_s, pk2(w.x, w.y), nr);
+                    ni = fma2(two_s, pk2(w.z, w.w), ni);
                 }
-                const float2 g = lc_c(nr, ni);
-                part.x += g.x - f[k].x;
-                part.y += g.y - f[k].y;
+                add_unit_pair(lc_c2(nr, ni), kk);
             }
         }
         const float2 e = string_term(cf, warp_sum_xor2(part));
