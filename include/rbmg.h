@@ -172,6 +172,11 @@ RBMG_API int rbmg_ev_gradient(const rbmg_psi* psi, const rbmg_operator* op, rbmg
  * its ensembles' foreach (include/operator/Operator.hpp:90-115). */
 RBMG_API int rbmg_local_energies(const rbmg_psi* psi, const rbmg_operator* op, int count, const uint64_t* spins,
                                  double* out);
+/* Extension: hidden angles theta = b + s W of `count` given configurations -> out
+ * [2 count M] (complex), built on the tensor cores (spins exact in BF16, W as three BF16
+ * parts, FP32 accumulation); the reference evaluates them one at a time
+ * (kernel::Psi::angle, include/quantum_state/Psi.hpp:43-53).  Complex RBM. */
+RBMG_API int rbmg_psi_angles(const rbmg_psi* psi, int count, const uint64_t* spins, double* out);
 /* Extension (PsiDeep): gradient of the local energy by a hand-written adjoint (reverse
  * mode) kernel that recomputes every forward pass, in PyTorch's convention for a real
  * loss L: grad_k = dL/dRe(theta_k) + i dL/dIm(theta_k).  score = 0: L = Re <E_loc> over

@@ -115,6 +115,7 @@ SIGNATURES = {
     "rbmg_hsd_distance_2nd_order": [_vp, _vp, _vp, _vp, _vp, _dp],
     "rbmg_diag_density": [_vp, _vp, _vp, C.c_int, _dp],
     "rbmg_kl_gradient": [_vp, _vp, _vp, C.c_double, _dp, _dp],
+    "rbmg_psi_angles": [_vp, C.c_int, _u64p, _dp],
 }
 _RESTYPE = {"rbmg_last_error": C.c_char_p, "rbmg_version": C.c_char_p}
 

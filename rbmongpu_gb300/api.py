@@ -200,6 +200,14 @@ class _PsiBase:
         call("rbmg_psi_log_psi", self._h, 1, _p(w, _u64p), _p(out))
         return complex(out[0], out[1])
 
+    def angles(self, spins_words):
+        """Extension (complex RBM): hidden angles theta = b + s W of configurations (uint64
+        words [count][nwords]) -> complex [count][M], built on the tensor cores."""
+        w = np.ascontiguousarray(spins_words, np.uint64).reshape(-1, nwords(self.N))
+        out = np.zeros(2 * len(w) * self.M)
+        call("rbmg_psi_angles", self._h, len(w), _p(w, _u64p), _p(out))
+        return out.view(np.complex128).reshape(len(w), self.M)
+
     def log_psi_batch(self, spins_words):
         w = np.ascontiguousarray(spins_words, np.uint64).reshape(-1, nwords(self.N))
         out = np.zeros(2 * len(w))

@@ -132,6 +132,12 @@ static int rbm_upload(rbmg_psi* p) {
     RBMG_CK(p->dbq.ensure(sizeof(float4) * kp));
     RBMG_CK(launch_rbm_pairs(p->N, p->Mpad, p->dW.as<float2>(), p->db.as<float2>(), p->dWq.as<float4>(),
                              p->dbq.as<float4>(), stream()));
+    if (rbm_tc_supported(p->N, p->Mpad)) {
+        RBMG_CK(p->dWtc.ensure(sizeof(__nv_bfloat16) * rbm_tc_pack_elems(p->Mpad, rbm_tc_kp(p->N))));
+        RBMG_CK(launch_rbm_tc_pack(p->N, p->M, p->Mpad, p->dW.as<float2>(), p->dWtc.as<__nv_bfloat16>(), stream()));
+    }
+    RBMG_CK(p->tc_error.ensure(sizeof(int)));
+    RBMG_CK(cudaMemsetAsync(p->tc_error.p, 0, sizeof(int), stream()));
     RBMG_CK(cudaStreamSynchronize(stream()));
     p->f64_valid = false;
     return RBMG_OK;
@@ -1112,6 +1118,40 @@ int rbmg::ev_gradient_device(const rbmg_psi* psi, const rbmg_operator* op, rbmg_
     RBMG_CK(cudaStreamSynchronize(stream()));
     value[0] = Es.x * f;
     value[1] = Es.y * f;
+    return RBMG_OK;
+}
+
+// Extension: the hidden angles theta = b + s W of given configurations (spins
+// [count][ceil(N/64)]) -> out [2 count M] (complex), from the tensor-core kernel
+// (reference: kernel::Psi::angle, include/quantum_state/Psi.hpp:43-53, one angle at a time)
+extern "C" int rbmg_psi_angles(const rbmg_psi* psi, int count, const uint64_t* spins, double* out) {
+    if (!psi || count < 0 || (count > 0 && (!spins || !out))) return fail(RBMG_EINVAL, "angles: bad arguments");
+    if (psi->kind != 0) return fail(RBMG_EUNSUPPORTED, "angles: complex RBM (Psi) only");
+    if (!psi->dWtc.p) return fail(RBMG_EUNSUPPORTED, "angles: no tensor-core operands for this psi");
+    if (count == 0) return RBMG_OK;
+    const int nw = nwords_of(psi->N);
+    Workspace& W = ws();
+    RBMG_CK(W.sample_spins.ensure(sizeof(uint64_t) * nw * count));
+    RBMG_CK(W.Tp.ensure(sizeof(float2) * static_cast<size_t>(count) * psi->Mpad));
+    RBMG_CK(cudaMemcpyAsync(W.sample_spins.p, spins, sizeof(uint64_t) * nw * count, cudaMemcpyHostToDevice, stream()));
+    RBMG_CK(launch_angles_tc(count, psi->N, psi->Mpad, W.sample_spins.as<uint64_t>(), psi->db.as<float2>(),
+                             psi->dWtc.as<__nv_bfloat16>(), nullptr, nullptr, W.Tp.as<float2>(),
+                             psi->tc_error.as<int>(), stream()));
+    std::vector<float2> h(static_cast<size_t>(count) * psi->Mpad);
+    int err = 0;
+    RBMG_CK(cudaMemcpyAsync(h.data(), W.Tp.p, sizeof(float2) * h.size(), cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaMemcpyAsync(&err, psi->tc_error.p, sizeof(int), cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaStreamSynchronize(stream()));
+    if (err) {
+        RBMG_CK(cudaMemset(psi->tc_error.p, 0, sizeof(int)));
+        return fail(RBMG_ETIMEOUT, "angles: a tensor-core wait gave up");
+    }
+    for (int t = 0; t < count; t++)
+        for (int j = 0; j < psi->M; j++) {
+            const float2 v = h[static_cast<size_t>(t) * psi->Mpad + j];
+            out[2 * (static_cast<size_t>(t) * psi->M + j)] = v.x;
+            out[2 * (static_cast<size_t>(t) * psi->M + j) + 1] = v.y;
+        }
     return RBMG_OK;
 }
 

@@ -9,6 +9,7 @@
 #include <string>
 #include <vector>
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include "../../include/rbmg.h"
@@ -77,6 +78,8 @@ struct rbmg_psi {
     int M = 0, Mpad = 0;
     std::vector<rbmg::cplx> b, W;
     rbmg::DevBuf dW, db, dWq, dbq;     // complex64 rows, and the sampler's paired copies (kernels.h)
+    rbmg::DevBuf dWtc;                 // W as BF16 hi / mid / lo tensor-core operands (angles_tc.cu), if supported
+    rbmg::DevBuf tc_error;             // set when a tensor-core pass of this psi gave up waiting
     mutable rbmg::DevBuf dW64, db64;   // FP64 copies for the Hilbert-space distance pass, uploaded on use
     mutable bool f64_valid = false;
     // deep / pair
@@ -111,6 +114,14 @@ int psi_scatter(rbmg_psi* psi, const double2* packed);
 // capi.cu: the energy gradient formed on the device, d_grad [P]; energy to value[2]
 int ev_gradient_device(const rbmg_psi* psi, const rbmg_operator* op, rbmg_ensemble* ens, double2* d_grad,
                        double* value);
+// angles_tc.cu: hidden angles from scratch on the tensor cores
+bool rbm_tc_supported(int N, int Mpad);
+size_t rbm_tc_pack_elems(int Mpad, int Kp);
+int rbm_tc_kp(int N);
+cudaError_t launch_rbm_tc_pack(int N, int M, int Mpad, const float2* W, __nv_bfloat16* out, cudaStream_t st);
+cudaError_t launch_angles_tc(int count, int N, int Mpad, const uint64_t* spins, const float2* b,
+                             const __nv_bfloat16* images, float4* theta, float2* re, float2* plain, int* error,
+                             cudaStream_t st);
 // density.cu: out = a - b elementwise
 cudaError_t launch_sub(int count, const double2* a, const double2* b, double2* out, cudaStream_t st);
 // density.cu: out [2^na] += w_s |eloc_s|^2 at the bin of the first na spins

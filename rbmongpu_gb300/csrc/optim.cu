@@ -250,6 +250,9 @@ int psi_scatter(rbmg_psi* psi, const double2* packed) {
         RBMG_CK(cudaGetLastError());
         RBMG_CK(launch_rbm_pairs(psi->N, psi->Mpad, psi->dW.as<float2>(), psi->db.as<float2>(), psi->dWq.as<float4>(),
                                  psi->dbq.as<float4>(), stream()));
+        if (psi->dWtc.p)
+            RBMG_CK(launch_rbm_tc_pack(psi->N, psi->M, psi->Mpad, psi->dW.as<float2>(),
+                                       psi->dWtc.as<__nv_bfloat16>(), stream()));
         // the FP64 copies (exact-summation weights, Hilbert-space distance) in the host
         // layout b [M], W [N][M] are the packed vector's tail as it stands
         const size_t M = psi->M, NM = static_cast<size_t>(psi->N) * psi->M;

@@ -1563,8 +1563,14 @@ extern "C" int rbmg_chain_learned_async(rbmg_chain* c, const rbmg_psi* psi, cons
     L.accepts = c->accepts.as<unsigned long long>();
     L.proposals = c->proposals.as<unsigned long long>();
     // the angles and logits of the current states (plain sweeps or new weights may
-    // have changed them since the last call)
-    RBMG_CK(launch_learned(0, P, L, st));
+    // have changed them since the last call); the angles from scratch on the tensor cores
+    // where the psi carries their operands (its waits report through the proposal's flag)
+    if (psi->dWtc.p) {
+        RBMG_CK(launch_angles_tc(B, psi->N, psi->Mpad, L.spins, psi->db.as<float2>(), psi->dWtc.as<__nv_bfloat16>(),
+                                 L.theta, L.re, nullptr, prop->tc_error.as<int>(), st));
+    } else {
+        RBMG_CK(launch_learned(0, P, L, st));
+    }
     RBMG_CK(launch_fused<false>(prop, L, L.spins, B, L.logits_cur, st));
     int r = RBMG_OK;
     const int nt = std::min(train, B);
