@@ -432,6 +432,16 @@ def run_serving(args):
 
 
 # --------------------------------------------------------------------- S-matrix workload
+def measured_peak(key):
+    """A roofline denominator from MEASURED_PEAKS.json beside this file (None if absent)."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)[key])
+    except (OSError, KeyError, ValueError):
+        return None
+
+
 SM_N, SM_M, SM_CHAINS, SM_PER_CHAIN = 64, 128, 4096, 4
 
 
@@ -474,8 +484,9 @@ def run_smatrix(args):
     n = SM_CHAINS * SM_PER_CHAIN
     mc = rg.MonteCarloLoop(n, 1, 20, SM_CHAINS, True, seed=11)
     L = Ms + Ns * Ms
+    simt = bool(args.sm_simt)
     for _ in range(args.warmup):
-        rg.get_S_matrix(psi, mc)
+        rg.get_S_matrix(psi, mc, simt=simt)
     ms_acc, walls = [], []
     ms = ctypes.c_double()
     launches = ctypes.c_int()
@@ -484,7 +495,7 @@ def run_smatrix(args):
     for _ in range(args.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        S = rg.get_S_matrix(psi, mc)
+        S = rg.get_S_matrix(psi, mc, simt=simt)
         walls.append(time.perf_counter() - t0)
         call("rbmg_s_matrix_timing", ctypes.byref(ms), ctypes.byref(launches))
         ms_acc.append(ms.value)
@@ -493,9 +504,25 @@ def run_smatrix(args):
     wall = float(np.mean(walls))
     acc_s = float(np.mean(ms_acc)) / 1e3
     flops = 8.0 * L * (L + 1) / 2 * n          # 4 FMA per upper-triangle entry and sample
-    v = ctypes.c_double()
-    call("rbmg_probe_fp32_tflops", 20000, ctypes.byref(v))
-    peak = v.value
+    if simt:
+        v = ctypes.c_double()
+        call("rbmg_probe_fp32_tflops", 20000, ctypes.byref(v))
+        roof = {"bound": "fp32", "achieved": flops / acc_s / 1e12, "peak": v.value, "unit": "TFLOP/s",
+                "frac": flops / acc_s / 1e12 / v.value, "traffic": None,
+                "peak_source": "measured in this run by the library's FP32 FMA probe kernel",
+                "kernel": "sm_herk_kernel"}
+    else:
+        # six BF16 part products for each of the four real products of a complex one
+        tflops = 6.0 * flops / acc_s / 1e12
+        peak = measured_peak("bf16_tflops")
+        roof = {"bound": "tensor", "achieved": tflops, "peak": peak, "unit": "TFLOP/s",
+                "frac": tflops / peak if peak else None, "traffic": None,
+                "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst), of measured",
+                "kernel": "sm_tc_kernel (+ sm_tc_prep_kernel, in the timed launches)",
+                "fp32_equivalent_tflops": flops / acc_s / 1e12,
+                "algorithmic": "48 BF16 flops per upper-triangle entry and sample (6 part pairs x 4 real "
+                               "products x 2)"}
+    roof["flops_per_launch"] = flops / max(1, launches.value)
     P = 2 * Ns + L
     cpu = None
     if args.cpu_seconds > 0:
@@ -507,18 +534,17 @@ def run_smatrix(args):
         "metric": "S matrix (get_S_matrix): MC samples folded into the P x P O_k covariance per second",
         "value": n / acc_s, "unit": "samples/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": acc_s * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 products (complex64 rows), f64 accumulation", "data": "synthetic (seeded PCG64 parameters)",
+        "dtype": ("f32 products (complex64 rows), f64 accumulation" if simt else
+                  "bf16 x3 split products of complex64 rows, f32 sums of <= 1024 samples, f64 accumulation"),
+        "data": "synthetic (seeded PCG64 parameters)",
         "config": {"workload": f"s_matrix_rbm_n{Ns}_m{Ms}_mc{n}", "N": Ns, "M": Ms, "P": P,
-                   "samples": n, "chains": SM_CHAINS,
+                   "samples": n, "chains": SM_CHAINS, "products": "fp32 cuda cores" if simt else "tensor cores",
                    "l2": f"the {16 * L * L / 1e9:.2f} GB FP64 matrix, read and written every 1024 samples, "
                          "exceeds L2 at N=64"},
         "e2e": {"value": n / wall, "unit": "samples/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 16 * P * P},
         "gpu_launches": int(launches.value) * args.steps,
-        "roofline": {"bound": "fp32", "achieved": flops / acc_s / 1e12, "peak": peak, "unit": "TFLOP/s",
-                     "frac": flops / acc_s / 1e12 / peak, "traffic": None,
-                     "peak_source": "measured in this run by the library's FP32 FMA probe kernel",
-                     "kernel": "sm_herk_kernel", "flops_per_launch": flops / max(1, launches.value)},
+        "roofline": roof,
         "cpu_baseline": cpu,
         "clocks": clk,
     }
@@ -542,6 +568,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=16.0, help="budget of the CPU baseline leg")
     ap.add_argument("--sm-n", type=int, default=SM_N, help="s_matrix workload: visible units")
     ap.add_argument("--sm-m", type=int, default=SM_M, help="s_matrix workload: hidden units")
+    ap.add_argument("--sm-simt", type=int, default=0, help="s_matrix workload: 1 = FP32 CUDA-core products")
     ap.add_argument("--workload", default="learned", choices=["learned", "serving", "s_matrix"],
                     help="learned: the N=100 learned-vs-plain chains (headline); serving: 64 uneven RBMs; "
                          "s_matrix: get_S_matrix of the N=64, M=128 RBM over 16384 MC samples")

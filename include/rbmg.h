@@ -380,12 +380,17 @@ RBMG_API int rbmg_optimizer_step_energy(rbmg_optimizer* opt, rbmg_psi* psi, cons
  * entries k < 2N are zero.  flags: RBMG_S_WEIGHTED weights each configuration by its
  * normalised |psi|^2 (no change for MonteCarloLoop, whose samples carry weight 1);
  * RBMG_S_CENTERED subtracts <O_k> conj(<O_k'>) (the covariance of stochastic
- * reconfiguration).  Psi and PsiDeep, both ensembles; PsiPair has no O_k. */
+ * reconfiguration).  Psi and PsiDeep, both ensembles; PsiPair has no O_k.  The products
+ * run on the tensor cores (BF16 hi / mid / lo parts of the complex64 rows, FP32 sums of at
+ * most 1024 samples, FP64 matrix); RBMG_S_SIMT (extension) takes the FP32 CUDA-core tile
+ * kernel instead.  A tensor-core wait that gives up returns RBMG_ETIMEOUT. */
 #define RBMG_S_WEIGHTED 1
 #define RBMG_S_CENTERED 2
+#define RBMG_S_SIMT 4
 RBMG_API int rbmg_s_matrix(const rbmg_psi* psi, rbmg_ensemble* ens, int flags, double* out /* [2 P P] */);
 /* Extension: device time (CUDA events) of the last rbmg_s_matrix call's accumulation
- * launches on this thread, and their number (the measurement hook of the benchmark). */
+ * launches on this thread, and the number of kernels they launched (the measurement hook
+ * of the benchmark). */
 RBMG_API int rbmg_s_matrix_timing(double* ms, int* launches);
 
 /* FP32 FMA throughput of the current device in TFLOP/s (a probe kernel of `iters`

@@ -660,15 +660,16 @@ def psi_O_k_vector(psi, spins):
     return out
 
 
-def get_S_matrix(psi, spin_ensemble, weighted=False, centered=False):
+def get_S_matrix(psi, spin_ensemble, weighted=False, centered=False, simt=False):
     """get_S_matrix (source/network_functions/S_matrix.cu:10-53; C++ only in the
     reference): S[k, k'] = sum_s O_k(s) conj(O_k'(s)) / num_steps over the ensemble's
     configurations, P x P complex128 with zero rows and columns below 2N.  As in the
     reference the exact-summation weight is not applied; ``weighted=True`` applies the
-    normalised |psi|^2, ``centered=True`` subtracts <O_k> conj(<O_k'>)."""
+    normalised |psi|^2, ``centered=True`` subtracts <O_k> conj(<O_k'>).  The products run
+    on the tensor cores; ``simt=True`` takes the FP32 CUDA-core kernel instead."""
     P = psi.num_params
     out = np.zeros((P, P), np.complex128)
-    flags = (1 if weighted else 0) | (2 if centered else 0)
+    flags = (1 if weighted else 0) | (2 if centered else 0) | (4 if simt else 0)
     call("rbmg_s_matrix", psi._h, spin_ensemble._h, flags, _p(out.view(np.float64)))
     return out
 

@@ -52,7 +52,7 @@ int deep_log_psi(const rbmg_psi* psi, int count, const uint64_t* d_spins, uint64
 struct Workspace {
     DevBuf sample_spins, eloc, logpsi, logpsi_p, T, U, X, Tp, weights, coef1, coef2, coef3, omega, pr, nn;
     DevBuf partial, block_scratch, sums, acc_O, acc_EO, acc_Ek, acc_wO, acc_pO, block_max, zsum;
-    DevBuf smat, smean, okrows, sshift;
+    DevBuf smat, smean, okrows, sshift, splanes, serror;
 };
 
 static Workspace& ws() {
@@ -1756,6 +1756,7 @@ extern "C" int rbmg_s_matrix(const rbmg_psi* psi, rbmg_ensemble* ens, int flags,
         return fail(RBMG_EINVAL, "S_matrix: ExactSummation size differs from psi's N");
     const int N = psi->N, P = psi->num_params(), L = P - 2 * N, nw = nwords_of(N);
     const bool weighted = (flags & RBMG_S_WEIGHTED) != 0, centered = (flags & RBMG_S_CENTERED) != 0;
+    const bool use_tc = (flags & RBMG_S_SIMT) == 0;
     Workspace& W = ws();
     const size_t sbytes = sizeof(double2) * static_cast<size_t>(L) * L;
     RBMG_CK(W.smat.ensure(sbytes));
@@ -1780,6 +1781,26 @@ extern "C" int rbmg_s_matrix(const rbmg_psi* psi, rbmg_ensemble* ens, int flags,
         }
         a.shift = W.sshift.as<double2>();
         return cudaSuccess;
+    };
+    if (use_tc) {
+        RBMG_CK(W.splanes.ensure(sm_tc_planes_bytes(L)));
+        RBMG_CK(W.serror.ensure(sizeof(int)));
+        RBMG_CK(cudaMemsetAsync(W.serror.p, 0, sizeof(int), stream()));
+    }
+    int nlaunch = 0;
+    // the products of one chunk (tensor cores, or the FP32 tile kernel) and its mean row
+    auto accumulate = [&](const SmSource& a) -> cudaError_t {
+        cudaError_t e;
+        if (use_tc) {
+            e = launch_sm_tc_accumulate(a, W.smat.as<double2>(), W.splanes.p, W.serror.as<int>(), &nlaunch,
+                                        stream());
+        } else {
+            e = launch_sm_accumulate(a, W.smat.as<double2>(), nullptr, sms, stream());
+            nlaunch++;
+        }
+        if (e != cudaSuccess || !centered) return e;
+        nlaunch++;
+        return launch_sm_mean(a, W.smean.as<double2>(), stream());
     };
     // CUDA events around every accumulation launch (rbmg_s_matrix_timing)
     std::vector<cudaEvent_t> ev;
@@ -1826,8 +1847,7 @@ extern "C" int rbmg_s_matrix(const rbmg_psi* psi, rbmg_ensemble* ens, int flags,
             a.w = c.weights;
             RBMG_CK(with_shift(a));
             RBMG_CK(mark());
-            RBMG_CK(launch_sm_accumulate(a, W.smat.as<double2>(), centered ? W.smean.as<double2>() : nullptr, sms,
-                                         stream()));
+            RBMG_CK(accumulate(a));
             RBMG_CK(mark());
             return RBMG_OK;
         }
@@ -1848,8 +1868,7 @@ extern "C" int rbmg_s_matrix(const rbmg_psi* psi, rbmg_ensemble* ens, int flags,
             a.weighted = weighted && a.w;
             RBMG_CK(with_shift(a));
             RBMG_CK(mark());
-            RBMG_CK(launch_sm_accumulate(a, W.smat.as<double2>(), centered ? W.smean.as<double2>() : nullptr, sms,
-                                         stream()));
+            RBMG_CK(accumulate(a));
             RBMG_CK(mark());
         }
         return RBMG_OK;
@@ -1862,7 +1881,10 @@ extern "C" int rbmg_s_matrix(const rbmg_psi* psi, rbmg_ensemble* ens, int flags,
     std::memset(out, 0, sizeof(double2) * static_cast<size_t>(P) * P);
     RBMG_CK(cudaMemcpy2DAsync(out + 2 * (static_cast<size_t>(2 * N) * P + 2 * N), sizeof(double2) * P, W.smat.p,
                               sizeof(double2) * L, sizeof(double2) * L, L, cudaMemcpyDeviceToHost, stream()));
+    int tc_err = 0;
+    if (use_tc) RBMG_CK(cudaMemcpyAsync(&tc_err, W.serror.p, sizeof(int), cudaMemcpyDeviceToHost, stream()));
     RBMG_CK(cudaStreamSynchronize(stream()));
+    if (tc_err) return fail(RBMG_ETIMEOUT, "S_matrix: a tensor-core wait gave up");
     double ms = 0.0;
     for (size_t q = 0; q + 1 < ev.size(); q += 2) {
         float t = 0.0f;
@@ -1870,7 +1892,7 @@ extern "C" int rbmg_s_matrix(const rbmg_psi* psi, rbmg_ensemble* ens, int flags,
         ms += t;
     }
     g_sm_timing_ms = ms;
-    g_sm_timing_launches = static_cast<int>(ev.size() / 2);
+    g_sm_timing_launches = nlaunch;
     return RBMG_OK;
 }
 

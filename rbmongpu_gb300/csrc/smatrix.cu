@@ -15,6 +15,7 @@
 // from the FP64 reverse pass.  The lower triangle is mirrored at the end.
 #include "host.h"
 #include "smatrix.h"
+#include "smatrix_rows.cuh"
 
 namespace rbmg {
 
@@ -23,50 +24,6 @@ namespace {
 constexpr int kT = 64;          // tile edge
 constexpr int kS = 16;          // samples per shared-memory stage
 constexpr int kFlush = 1024;    // samples accumulated in FP32 before the FP64 update
-
-struct Elem {
-    int i, j;   // RBM: spin index (-1: bias block) and hidden unit; rows: column k
-    bool live;
-};
-
-__device__ __forceinline__ Elem elem_of(const SmSource& a, int k) {
-    Elem e{-1, k, k < a.L};
-    if (a.kind == 0 && e.live && k >= a.M) {
-        const int r = k - a.M;
-        e.i = r / a.M;
-        e.j = r - e.i * a.M;
-    }
-    return e;
-}
-
-// sqrt(w_s) (F[s][k] - shift[k]) (weight 1 unweighted), zero outside the matrix; the
-// shift is subtracted in FP64 so that a centred matrix keeps the rows' small spread
-__device__ __forceinline__ float2 load_f(const SmSource& a, const Elem& e, int s, int k) {
-    if (!e.live || s >= a.count) return make_float2(0.0f, 0.0f);
-    double2 d;
-    if (a.kind == 0) {
-        const float2 t = a.T[static_cast<long>(s) * a.Mpad + e.j];
-        d = make_double2(t.x, t.y);
-        if (e.i >= 0) {
-            const uint64_t word = a.enumerate ? ((e.i >> 6) == 0 ? a.enum_base + static_cast<uint64_t>(s) : 0ull)
-                                              : a.spins[static_cast<long>(s) * a.nw + (e.i >> 6)];
-            if (!((word >> (e.i & 63)) & 1ull)) d = make_double2(-d.x, -d.y);
-        }
-    } else {
-        d = a.rows[static_cast<long>(s) * a.ld + e.j];
-    }
-    if (a.shift) {
-        d.x -= a.shift[k].x;
-        d.y -= a.shift[k].y;
-    }
-    float2 v = make_float2(static_cast<float>(d.x), static_cast<float>(d.y));
-    if (a.weighted) {
-        const float c = static_cast<float>(sqrt(a.w[s]));
-        v.x *= c;
-        v.y *= c;
-    }
-    return v;
-}
 
 __global__ void __launch_bounds__(256) sm_herk_kernel(SmSource a, double2* __restrict__ S, int nt, int slice,
                                                       int atomic) {
@@ -80,11 +37,11 @@ __global__ void __launch_bounds__(256) sm_herk_kernel(SmSource a, double2* __res
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
     const int m0 = tm * kT, n0 = tn * kT;
     // this thread's four loader columns of each block, sample row ty of the stage
-    Elem ea[4], eb[4];
+    SmElem ea[4], eb[4];
 #pragma unroll
     for (int q = 0; q < 4; q++) {
-        ea[q] = elem_of(a, m0 + tx + 16 * q);
-        eb[q] = elem_of(a, n0 + tx + 16 * q);
+        ea[q] = sm_elem_of(a, m0 + tx + 16 * q);
+        eb[q] = sm_elem_of(a, n0 + tx + 16 * q);
     }
     for (int f0 = s_begin; f0 < s_end; f0 += kFlush) {
         const int f1 = min(s_end, f0 + kFlush);
@@ -96,8 +53,8 @@ __global__ void __launch_bounds__(256) sm_herk_kernel(SmSource a, double2* __res
         float2 pa[4], pb[4];
 #pragma unroll
         for (int q = 0; q < 4; q++) {
-            pa[q] = f0 + ty < f1 ? load_f(a, ea[q], f0 + ty, m0 + tx + 16 * q) : make_float2(0.0f, 0.0f);
-            pb[q] = f0 + ty < f1 ? load_f(a, eb[q], f0 + ty, n0 + tx + 16 * q) : make_float2(0.0f, 0.0f);
+            pa[q] = f0 + ty < f1 ? sm_load_f(a, ea[q], f0 + ty, m0 + tx + 16 * q) : make_float2(0.0f, 0.0f);
+            pb[q] = f0 + ty < f1 ? sm_load_f(a, eb[q], f0 + ty, n0 + tx + 16 * q) : make_float2(0.0f, 0.0f);
         }
         for (int s0 = f0; s0 < f1; s0 += kS) {
             __syncthreads();
@@ -110,8 +67,8 @@ __global__ void __launch_bounds__(256) sm_herk_kernel(SmSource a, double2* __res
             const int sn = s0 + kS + ty;   // next stage's sample of this thread, loaded during the products
 #pragma unroll
             for (int q = 0; q < 4; q++) {
-                pa[q] = sn < f1 ? load_f(a, ea[q], sn, m0 + tx + 16 * q) : make_float2(0.0f, 0.0f);
-                pb[q] = sn < f1 ? load_f(a, eb[q], sn, n0 + tx + 16 * q) : make_float2(0.0f, 0.0f);
+                pa[q] = sn < f1 ? sm_load_f(a, ea[q], sn, m0 + tx + 16 * q) : make_float2(0.0f, 0.0f);
+                pb[q] = sn < f1 ? sm_load_f(a, eb[q], sn, n0 + tx + 16 * q) : make_float2(0.0f, 0.0f);
             }
 #pragma unroll
             for (int s = 0; s < kS; s++) {
@@ -164,10 +121,10 @@ __global__ void sm_mean_kernel(SmSource a, double2* mean, int assign, double sca
     if (k >= a.L) return;
     SmSource u = a;
     u.weighted = 0;
-    const Elem e = elem_of(u, k);
+    const SmElem e = sm_elem_of(u, k);
     double sr = 0.0, si = 0.0;
     for (int s = 0; s < a.count; s++) {
-        const float2 v = load_f(u, e, s, k);
+        const float2 v = sm_load_f(u, e, s, k);
         const double c = a.weighted ? a.w[s] : 1.0;
         sr += c * v.x;
         si += c * v.y;
@@ -221,6 +178,11 @@ cudaError_t launch_sm_accumulate(const SmSource& a, double2* S, double2* mean, i
     sm_herk_kernel<<<grid, 256, 0, st>>>(a, S, nt, slice, split > 1);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || !mean) return e;
+    return launch_sm_mean(a, mean, st);
+}
+
+cudaError_t launch_sm_mean(const SmSource& a, double2* mean, cudaStream_t st) {
+    if (a.count <= 0) return cudaSuccess;
     sm_mean_kernel<<<(a.L + 127) / 128, 128, 0, st>>>(a, mean, 0, 1.0);
     return cudaGetLastError();
 }

@@ -1,6 +1,7 @@
 // S-matrix kernels (smatrix.cu), driven from capi.cu::rbmg_s_matrix.
 #pragma once
 
+#include <cstddef>
 #include <cstdint>
 
 #include <cuda_runtime.h>
@@ -26,8 +27,17 @@ struct SmSource {
 // S [L][L] += sum_s c_s G_s^T conj(G_s) on the upper tiles, G_s = F_s - shift (c_s = w_s
 // when weighted, else 1); mean [L] += sum_s c_s G_s when mean is not null
 cudaError_t launch_sm_accumulate(const SmSource& src, double2* S, double2* mean, int num_sms, cudaStream_t st);
+// mean [L] += sum_s c_s G_s alone
+cudaError_t launch_sm_mean(const SmSource& src, double2* mean, cudaStream_t st);
 // out [L] = sum_s F_s / count (unweighted, unshifted): the shift of a centred S matrix
 cudaError_t launch_sm_row_mean(const SmSource& src, double2* out, cudaStream_t st);
+// the same products on the tensor cores (smatrix_tc.cu): BF16 hi / mid / lo operand planes
+// of one window of 1024 samples in `planes` (sm_tc_planes_bytes(L) bytes), one operand pass
+// and one MMA launch per window (counted into *launches); a tensor-core wait that gives up
+// sets *error
+size_t sm_tc_planes_bytes(int L);
+cudaError_t launch_sm_tc_accumulate(const SmSource& src, double2* S, void* planes, int* error, int* launches,
+                                    cudaStream_t st);
 // S /= Z, lower triangle mirrored; centred: S -= (mean / Z)(mean / Z)^dagger
 cudaError_t launch_sm_finish(int L, double2* S, const double2* mean, double inv_z, int centered, cudaStream_t st);
 
