@@ -5,6 +5,9 @@
 #include <cmath>
 #include <functional>
 #include <memory>
+#include <thread>
+#include <vector>
+#include <unistd.h>
 
 #include <cuda_profiler_api.h>
 
@@ -52,7 +55,7 @@ int deep_log_psi(const rbmg_psi* psi, int count, const uint64_t* d_spins, uint64
 struct Workspace {
     DevBuf sample_spins, eloc, logpsi, logpsi_p, T, U, X, Tp, weights, coef1, coef2, coef3, omega, pr, nn;
     DevBuf partial, block_scratch, sums, acc_O, acc_EO, acc_Ek, acc_wO, acc_pO, block_max, zsum;
-    DevBuf smat, smean, okrows, sshift, splanes, serror;
+    DevBuf smat, smean, okrows, sshift, splanes, serror, sout;
 };
 
 static Workspace& ws() {
@@ -1745,6 +1748,35 @@ int deep_ok_rows(const rbmg_psi* psi, int count, const uint64_t* d_spins, uint64
                  double2* rows, long ld, cudaStream_t st);
 }  // namespace rbmg
 
+// Writes one word of every page of a large host output from several threads while the GPU
+// works, so that the device-to-host copy of the result does not take the first-touch page
+// faults of a freshly allocated array one by one (joined before the copy).
+class Prefault {
+  public:
+    Prefault(void* p, size_t bytes) {
+        const size_t page = static_cast<size_t>(std::max(4096L, sysconf(_SC_PAGESIZE)));
+        if (bytes < (size_t(64) << 20)) return;
+        const int n = static_cast<int>(std::min(16u, std::max(1u, std::thread::hardware_concurrency())));
+        const size_t pages = (bytes + page - 1) / page, per = (pages + n - 1) / n;
+        char* base = static_cast<char*>(p);
+        for (int t = 0; t < n; t++) {
+            const size_t p0 = t * per, p1 = std::min(pages, p0 + per);
+            if (p0 >= p1) break;
+            threads_.emplace_back([=]() {
+                for (size_t q = p0; q < p1; q++) *reinterpret_cast<volatile char*>(base + q * page) = 0;
+            });
+        }
+    }
+    void join() {
+        for (auto& t : threads_) t.join();
+        threads_.clear();
+    }
+    ~Prefault() { join(); }
+
+  private:
+    std::vector<std::thread> threads_;
+};
+
 // get_S_matrix (source/network_functions/S_matrix.cu:10-53, instantiated for Psi with
 // ExactSummation only): S[k][k'] = sum_s O_k(s) conj(O_k'(s)) / num_steps over every
 // configuration of the ensemble, without the ensemble's weight (the reference ignores the
@@ -1759,6 +1791,7 @@ extern "C" int rbmg_s_matrix(const rbmg_psi* psi, rbmg_ensemble* ens, int flags,
     const bool use_tc = (flags & RBMG_S_SIMT) == 0;
     Workspace& W = ws();
     const size_t sbytes = sizeof(double2) * static_cast<size_t>(L) * L;
+    Prefault prefault(out, sizeof(double2) * static_cast<size_t>(P) * P);
     RBMG_CK(W.smat.ensure(sbytes));
     RBMG_CK(W.smean.ensure(sizeof(double2) * L));
     RBMG_CK(cudaMemsetAsync(W.smat.p, 0, sbytes, stream()));
@@ -1783,7 +1816,6 @@ extern "C" int rbmg_s_matrix(const rbmg_psi* psi, rbmg_ensemble* ens, int flags,
         return cudaSuccess;
     };
     if (use_tc) {
-        RBMG_CK(W.splanes.ensure(sm_tc_planes_bytes(L)));
         RBMG_CK(W.serror.ensure(sizeof(int)));
         RBMG_CK(cudaMemsetAsync(W.serror.p, 0, sizeof(int), stream()));
     }
@@ -1792,7 +1824,9 @@ extern "C" int rbmg_s_matrix(const rbmg_psi* psi, rbmg_ensemble* ens, int flags,
     auto accumulate = [&](const SmSource& a) -> cudaError_t {
         cudaError_t e;
         if (use_tc) {
-            e = launch_sm_tc_accumulate(a, W.smat.as<double2>(), W.splanes.p, W.serror.as<int>(), &nlaunch,
+            e = W.splanes.ensure(sm_tc_planes_bytes(L, a.count));
+            if (e != cudaSuccess) return e;
+            e = launch_sm_tc_accumulate(a, W.smat.as<double2>(), W.splanes.p, W.serror.as<int>(), &nlaunch, sms,
                                         stream());
         } else {
             e = launch_sm_accumulate(a, W.smat.as<double2>(), nullptr, sms, stream());
@@ -1877,10 +1911,17 @@ extern "C" int rbmg_s_matrix(const rbmg_psi* psi, rbmg_ensemble* ens, int flags,
     if (total == 0) return fail(RBMG_EINVAL, "S_matrix: the ensemble has no samples");
     // the exact-summation weights are normalised to sum 1; otherwise divide by the count
     const double z = (weighted && ens->kind == 1) ? 1.0 : static_cast<double>(total);
-    RBMG_CK(launch_sm_finish(L, W.smat.as<double2>(), W.smean.as<double2>(), 1.0 / z, centered ? 1 : 0, stream()));
-    std::memset(out, 0, sizeof(double2) * static_cast<size_t>(P) * P);
-    RBMG_CK(cudaMemcpy2DAsync(out + 2 * (static_cast<size_t>(2 * N) * P + 2 * N), sizeof(double2) * P, W.smat.p,
-                              sizeof(double2) * L, sizeof(double2) * L, L, cudaMemcpyDeviceToHost, stream()));
+    // the P x P result on the device (zero rows and columns below 2N), then one contiguous copy
+    const size_t obytes = sizeof(double2) * static_cast<size_t>(P) * P;
+    RBMG_CK(W.sout.ensure(obytes));
+    RBMG_CK(cudaMemsetAsync(W.sout.p, 0, sizeof(double2) * static_cast<size_t>(2 * N) * P, stream()));
+    if (N > 0)
+        RBMG_CK(cudaMemset2DAsync(W.sout.as<double2>() + static_cast<size_t>(2 * N) * P, sizeof(double2) * P, 0,
+                                  sizeof(double2) * 2 * N, L, stream()));
+    RBMG_CK(launch_sm_finish(L, W.smat.as<double2>(), W.smean.as<double2>(), 1.0 / z, centered ? 1 : 0,
+                             W.sout.as<double2>(), P, 2 * N, stream()));
+    prefault.join();
+    RBMG_CK(cudaMemcpyAsync(out, W.sout.p, obytes, cudaMemcpyDeviceToHost, stream()));
     int tc_err = 0;
     if (use_tc) RBMG_CK(cudaMemcpyAsync(&tc_err, W.serror.p, sizeof(int), cudaMemcpyDeviceToHost, stream()));
     RBMG_CK(cudaStreamSynchronize(stream()));

@@ -137,10 +137,12 @@ __global__ void sm_mean_kernel(SmSource a, double2* mean, int assign, double sca
     }
 }
 
-// S <- S / Z with the lower triangle mirrored from the upper and a real diagonal;
+// out[off + r][off + c] = S[r][c] / Z with the lower triangle mirrored from the upper and
+// a real diagonal (out: ldo columns; rows and columns below off are left to the caller);
 // centred: - m m^dagger with m = mean / Z (mean of the shifted rows: the covariance does
 // not depend on the shift)
-__global__ void sm_finish_kernel(int L, double2* S, const double2* mean, double inv_z, int centered) {
+__global__ void sm_finish_kernel(int L, const double2* __restrict__ S, const double2* mean, double inv_z,
+                                 int centered, double2* __restrict__ out, long ldo, int off) {
     const long idx = static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (idx >= static_cast<long>(L) * L) return;
     const int r = static_cast<int>(idx / L), c = static_cast<int>(idx - static_cast<long>(r) * L);
@@ -158,8 +160,8 @@ __global__ void sm_finish_kernel(int L, double2* S, const double2* mean, double 
         v.y -= ai * br - ar * bi;
         if (r == c) v.y = 0.0;
     }
-    S[idx] = v;
-    if (r < c) S[static_cast<long>(c) * L + r] = make_double2(v.x, -v.y);
+    out[(off + r) * ldo + off + c] = v;
+    if (r < c) out[(off + c) * ldo + off + r] = make_double2(v.x, -v.y);
 }
 
 }  // namespace
@@ -195,9 +197,10 @@ cudaError_t launch_sm_row_mean(const SmSource& a, double2* out, cudaStream_t st)
     return cudaGetLastError();
 }
 
-cudaError_t launch_sm_finish(int L, double2* S, const double2* mean, double inv_z, int centered, cudaStream_t st) {
+cudaError_t launch_sm_finish(int L, const double2* S, const double2* mean, double inv_z, int centered,
+                             double2* out, long ldo, int off, cudaStream_t st) {
     const long n = static_cast<long>(L) * L;
-    sm_finish_kernel<<<static_cast<int>((n + 255) / 256), 256, 0, st>>>(L, S, mean, inv_z, centered);
+    sm_finish_kernel<<<static_cast<int>((n + 255) / 256), 256, 0, st>>>(L, S, mean, inv_z, centered, out, ldo, off);
     return cudaGetLastError();
 }
 

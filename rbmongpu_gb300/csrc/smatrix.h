@@ -32,13 +32,15 @@ cudaError_t launch_sm_mean(const SmSource& src, double2* mean, cudaStream_t st);
 // out [L] = sum_s F_s / count (unweighted, unshifted): the shift of a centred S matrix
 cudaError_t launch_sm_row_mean(const SmSource& src, double2* out, cudaStream_t st);
 // the same products on the tensor cores (smatrix_tc.cu): BF16 hi / mid / lo operand planes
-// of one window of 1024 samples in `planes` (sm_tc_planes_bytes(L) bytes), one operand pass
-// and one MMA launch per window (counted into *launches); a tensor-core wait that gives up
-// sets *error
-size_t sm_tc_planes_bytes(int L);
+// of the chunk in `planes` (sm_tc_planes_bytes(L, count) bytes), one operand pass and one
+// persistent MMA launch on num_sms CTAs (counted into *launches); a tensor-core wait that
+// gives up sets *error
+size_t sm_tc_planes_bytes(int L, int count);
 cudaError_t launch_sm_tc_accumulate(const SmSource& src, double2* S, void* planes, int* error, int* launches,
-                                    cudaStream_t st);
-// S /= Z, lower triangle mirrored; centred: S -= (mean / Z)(mean / Z)^dagger
-cudaError_t launch_sm_finish(int L, double2* S, const double2* mean, double inv_z, int centered, cudaStream_t st);
+                                    int num_sms, cudaStream_t st);
+// out [off + r][off + c] (ldo columns) = S / Z with the lower triangle mirrored; centred:
+// minus (mean / Z)(mean / Z)^dagger
+cudaError_t launch_sm_finish(int L, const double2* S, const double2* mean, double inv_z, int centered,
+                             double2* out, long ldo, int off, cudaStream_t st);
 
 }  // namespace rbmg
