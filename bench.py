@@ -443,6 +443,7 @@ def measured_peak(key):
 
 
 SM_N, SM_M, SM_CHAINS, SM_PER_CHAIN = 64, 128, 4096, 4
+SM_TC_DRAM_BYTES = 6.279e9 + 2.571e9   # ncu, one sm_tc_kernel launch of this workload
 
 
 def sm_workload(N=SM_N, M=SM_M):
@@ -522,7 +523,17 @@ def run_smatrix(args):
                 "fp32_equivalent_tflops": flops / acc_s / 1e12,
                 "algorithmic": "48 BF16 flops per upper-triangle entry and sample (6 part pairs x 4 real "
                                "products x 2)"}
-    roof["flops_per_launch"] = flops / max(1, launches.value)
+    if simt:
+        roof["flops_per_launch"] = flops / max(1, launches.value)
+    else:
+        # per launch of sm_tc_kernel (one per 4096-sample chunk; a prep launch precedes each)
+        chunks = max(1, launches.value // 2)
+        roof["flops_per_launch"] = 6.0 * flops / chunks
+        if (Ns, Ms) == (SM_N, SM_M):
+            roof["traffic"] = SM_TC_DRAM_BYTES
+            roof["traffic_source"] = ("dram__bytes_read.sum + dram__bytes_write.sum of one sm_tc_kernel launch "
+                                      "(4096 samples, this workload) from ncu; algorithmic: the FP64 tile "
+                                      "read and written once per 1024-sample window (4.5 GB) + the planes")
     P = 2 * Ns + L
     cpu = None
     if args.cpu_seconds > 0:
