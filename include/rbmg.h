@@ -130,7 +130,13 @@ RBMG_API int rbmg_mc_create(uint32_t num_samples, uint32_t num_sweeps, uint32_t 
                    uint32_t num_markov_chains, uint64_t seed, rbmg_ensemble** out);
 /* MonteCarloLoop(MonteCarloLoop&) (MonteCarloLoop.cu:44-66): same settings, fresh streams */
 RBMG_API int rbmg_mc_copy(const rbmg_ensemble* other, rbmg_ensemble** out);
-/* set_total_z_symmetry / set_fast_sweep (include/spin_ensembles/MonteCarloLoop.hpp:283-291) */
+/* set_total_z_symmetry / set_fast_sweep (include/spin_ensembles/MonteCarloLoop.hpp:283-291).
+ * Fast sweep: each update flips the AND of num_tries random configurations (num_tries 0
+ * draws one, like the reference's loop; above 64 is RBMG_EINVAL); a thermalisation sweep is
+ * N updates, a sampling sweep one (MonteCarloLoop.hpp:108-113, 139-151, 162-171).  Both
+ * networks accept on the change of Re log psi with the flipped sites' angles (the
+ * reference's Psi keeps its angles for these moves and accepts every one); with
+ * total_z symmetry a sampling call returns RBMG_EUNSUPPORTED. */
 RBMG_API int rbmg_mc_set_total_z_symmetry(rbmg_ensemble* mc, int sector);
 RBMG_API int rbmg_mc_set_fast_sweep(rbmg_ensemble* mc, uint32_t num_tries);
 /* acceptance counters of the last sampling call (MonteCarloLoop.hpp:215-219), summed

@@ -997,6 +997,24 @@ static void g32_mc_update(chain_t* c) {
     g32_try(c, sites, ns);
 }
 
+/* fast sweep of the GPU spec (rbm_impl.cuh::rbm_fast_step2): the mask is the AND of
+ * fast_sweep_tries random configurations; its sites in increasing order form one proposal */
+static void g32_fast_update(chain_t* c) {
+    const int N = c->psi->N;
+    uint64_t mask[OR_MAX_WORDS] = {0}, m2[OR_MAX_WORDS] = {0};
+    int sites[OR_MAX_WORDS * 64];
+    int ns = 0;
+    rng_spins(&c->rng, N, mask);
+    for (int t = 1; t < c->cfg->fast_sweep_tries; t++) {
+        rng_spins(&c->rng, N, m2);
+        for (int k = 0; k < c->nw; k++) mask[k] &= m2[k];
+    }
+    for (int k = 0; k < c->nw; k++)
+        for (int b = 0; b < 64; b++)
+            if ((mask[k] >> b) & 1u) sites[ns++] = 64 * k + b;
+    g32_try(c, sites, ns);
+}
+
 static void chain_init_spins(chain_t* c) {
     const or_psi* psi = c->psi;
     memset(c->s, 0, sizeof(c->s));
@@ -1012,7 +1030,7 @@ int or_mc_run(const or_psi* psi, const or_op* op, const or_mc_cfg* cfg,
               uint64_t* spins_out, double* log_psi_out, double* eloc_out,
               uint64_t* accepts, uint64_t* rejects) {
     if (cfg->prec == OR_PREC_GPU32 && psi->kind != OR_PSI_RBM) return -1;
-    if (cfg->prec == OR_PREC_GPU32 && cfg->fast_sweep_tries > 0) return -1;
+    if (cfg->prec == OR_PREC_GPU32 && cfg->fast_sweep_tries > 0 && cfg->total_z) return -1;
     const int N = psi->N;
     const int nw = nwords_of(N);
     const int M = psi->kind == OR_PSI_RBM ? psi->M : 0;
@@ -1051,13 +1069,22 @@ int or_mc_run(const or_psi* psi, const or_op* op, const or_mc_cfg* cfg,
         } else {
             for (int t = 0; t < cfg->num_therm; t++) {
                 g32_refresh(&c);
-                for (int p = 0; p < N; p++) g32_mc_update(&c);
+                for (int p = 0; p < N; p++) {
+                    if (fast) g32_fast_update(&c);
+                    else g32_mc_update(&c);
+                }
             }
         }
         for (int step = 0; step < cfg->samples_per_chain; step++) {
             if (cfg->prec == OR_PREC_REF64) {
                 const long nupd = (long)cfg->num_sweeps * (fast ? 1 : N);
                 for (long t = 0; t < nupd; t++) ref_mc_update(&c);
+            } else if (fast) {
+                /* one update per sweep; angles from scratch at the sample's start and every N updates */
+                for (int t = 0; t < cfg->num_sweeps; t++) {
+                    if (t % N == 0) g32_refresh(&c);
+                    g32_fast_update(&c);
+                }
             } else {
                 for (int t = 0; t < cfg->num_sweeps; t++) {
                     g32_refresh(&c);

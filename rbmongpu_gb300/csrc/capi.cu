@@ -518,10 +518,14 @@ extern "C" int rbmg_mc_set_total_z_symmetry(rbmg_ensemble* mc, int sector) {
     return RBMG_OK;
 }
 
+// set_fast_sweep (MonteCarloLoop.hpp:288-291): multi-spin masks, the AND of num_tries random
+// configurations (0 draws one, as the reference's loop does); a sampling sweep is then one
+// update instead of N
 extern "C" int rbmg_mc_set_fast_sweep(rbmg_ensemble* mc, uint32_t num_tries) {
     if (!mc || mc->kind != 0) return fail(RBMG_EINVAL, "set_fast_sweep: not a MonteCarloLoop");
-    mc->fast_sweep_tries = num_tries;
-    return fail(RBMG_EUNSUPPORTED, "set_fast_sweep: multi-spin masks are not provided by this build");
+    if (num_tries > 64) return fail(RBMG_EINVAL, "set_fast_sweep: num_tries above 64 flips no spin");
+    mc->fast_sweep_tries = std::max(1u, num_tries);
+    return RBMG_OK;
 }
 
 extern "C" int rbmg_mc_acceptance(const rbmg_ensemble* mc, uint64_t* accepts, uint64_t* proposals,
@@ -628,7 +632,8 @@ constexpr int kExactChunk = 1 << 16;
 static int mc_stream(rbmg_ensemble* e, const rbmg_psi* psi, const rbmg_operator* op, bool want_eloc,
                      size_t max_chunk_samples, const std::function<int(const Chunk&)>& fn) {
     if (psi->kind != 0) return fail(RBMG_EUNSUPPORTED, "MonteCarloLoop: PsiDeep / PsiPair chains are sampled by deep.cu");
-    if (e->fast_sweep_tries) return fail(RBMG_EUNSUPPORTED, "fast sweep is not provided");
+    if (e->fast_sweep_tries && e->total_z)
+        return fail(RBMG_EUNSUPPORTED, "fast sweep with total_z symmetry (the reference pairs a mask with an unset site)");
     if (e->total_z && psi->N > 64) return fail(RBMG_EUNSUPPORTED, "total_z symmetry needs N <= 64");
     const int nw = nwords_of(psi->N);
     const int B = static_cast<int>(e->num_chains);
@@ -655,6 +660,7 @@ static int mc_stream(rbmg_ensemble* e, const rbmg_psi* psi, const rbmg_operator*
         L.init = first ? 1 : 0;
         L.total_z = e->total_z;
         L.sector = e->sector;
+        L.fast_tries = static_cast<int>(e->fast_sweep_tries);
         L.n_therm = first ? static_cast<int>(e->num_therm) : 0;
         L.n_samples = rows;
         L.sweeps_per_sample = static_cast<int>(e->num_sweeps);

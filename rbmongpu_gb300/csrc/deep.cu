@@ -459,7 +459,9 @@ __global__ void col_finish_kernel(int P, int splits, const double2* __restrict__
 }
 
 // Metropolis for PsiDeep / PsiPair: one CTA per walker, full forward pass per proposal
-// (PsiDeep.hpp:191-194: angles are not updated incrementally).
+// (PsiDeep.hpp:191-194: angles are not updated incrementally).  Fast sweep
+// (MonteCarloLoop.hpp:162-171): the proposal flips the AND of fast_tries random
+// configurations, N such updates per thermalisation sweep and one per sampling sweep.
 __global__ void deep_mc_kernel(DeepNetDev n0, DeepNetDev n1, int pair, McLaunch L) {
     extern __shared__ __align__(16) unsigned char smem[];
     Work<float2> w = carve<float2>(smem, n0, false);
@@ -489,13 +491,35 @@ __global__ void deep_mc_kernel(DeepNetDev n0, DeepNetDev n1, int pair, McLaunch 
     const int total = L.n_therm + L.n_samples * L.sweeps_per_sample;
     int sample = 0;
     for (int sw = 0; sw < total; sw++) {
-        for (int p = 0; p < N; p++) {
-            const int site = static_cast<int>(rng.next() % static_cast<uint32_t>(N));
-            __syncthreads();
-            if (threadIdx.x < kMaxWords) {
-                uint64_t v = w.s[threadIdx.x];
-                if ((site >> 6) == static_cast<int>(threadIdx.x)) v ^= 1ull << (site & 63);
-                sp[threadIdx.x] = v;
+        const int updates = (L.fast_tries > 0 && sw >= L.n_therm) ? 1 : N;
+        for (int p = 0; p < updates; p++) {
+            if (L.fast_tries > 0) {
+                // every thread draws the same mask words
+                uint64_t m[kMaxWords] = {0, 0, 0, 0};
+                for (int t = 0; t < L.fast_tries; t++) {
+                    for (int k = 0; k < nw; k++) {
+                        const uint64_t lo = rng.next();
+                        const uint64_t hi = rng.next();
+                        const uint64_t v = lo | (hi << 32);
+                        m[k] = t == 0 ? v : (m[k] & v);
+                    }
+                }
+                if (N / 64 < nw) m[N / 64] &= (1ull << (N % 64)) - 1ull;
+                __syncthreads();
+                if (threadIdx.x < kMaxWords) {
+                    uint64_t v = w.s[threadIdx.x];
+                    for (int k = 0; k < kMaxWords; k++)
+                        if (k == static_cast<int>(threadIdx.x)) v ^= m[k];
+                    sp[threadIdx.x] = v;
+                }
+            } else {
+                const int site = static_cast<int>(rng.next() % static_cast<uint32_t>(N));
+                __syncthreads();
+                if (threadIdx.x < kMaxWords) {
+                    uint64_t v = w.s[threadIdx.x];
+                    if ((site >> 6) == static_cast<int>(threadIdx.x)) v ^= 1ull << (site & 63);
+                    sp[threadIdx.x] = v;
+                }
             }
             __syncthreads();
             const float nl = state_log_psi<float2>(n0, n1, pair, sp, w, shifted).x;
@@ -1081,8 +1105,7 @@ int deep_stream(rbmg_ensemble* e, const rbmg_psi* psi, const rbmg_operator* op, 
                 size_t max_chunk_samples, const std::function<int(const Chunk&)>& fn) {
     (void)op;
     (void)want_eloc;
-    if (e->fast_sweep_tries || e->total_z)
-        return fail(RBMG_EUNSUPPORTED, "PsiDeep chains: fast sweep / S_z symmetry are not provided");
+    if (e->total_z) return fail(RBMG_EUNSUPPORTED, "PsiDeep chains: S_z symmetry is not provided");
     const int nw = (psi->N + 63) / 64;
     const int B = static_cast<int>(e->num_chains);
     const int steps = static_cast<int>(e->num_samples / e->num_chains);
@@ -1104,6 +1127,7 @@ int deep_stream(rbmg_ensemble* e, const rbmg_psi* psi, const rbmg_operator* op, 
         L.spins = e->spins.as<uint64_t>();
         L.rng_index = e->rng_index.as<uint64_t>();
         L.init = first ? 1 : 0;
+        L.fast_tries = static_cast<int>(e->fast_sweep_tries);
         L.n_therm = first ? static_cast<int>(e->num_therm) : 0;
         L.n_samples = rows;
         L.sweeps_per_sample = static_cast<int>(e->num_sweeps);

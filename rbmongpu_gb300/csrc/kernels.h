@@ -54,6 +54,7 @@ struct McLaunch {
     uint64_t* rng_index;        // [B] next Philox word, in/out
     int init;                   // 1: draw fresh random start spins
     int total_z, sector;        // S_z-conserving pair updates
+    int fast_tries;             // > 0: fast sweep, multi-spin masks (the AND of fast_tries random words)
     int n_therm;                // sweeps before the first sample
     int n_samples;              // samples recorded by this launch
     int sweeps_per_sample;

@@ -249,6 +249,72 @@ __device__ __forceinline__ bool rbm_mh_step2(const RbmDev& P, Spins<NW>& s, pair
     return accept;
 }
 
+// One update of the fast sweep (MonteCarloLoop.hpp:162-171): the proposal flips the spins
+// of a mask that is the AND of `tries` random configurations (each spin flips with
+// probability 2^-tries; the mask is warp-uniform).  Unlike the reference, whose Psi keeps
+// its angles unchanged for these moves, the proposal's angles follow every flipped site in
+// increasing order (theta += 2 s'_i W_i), and the move is accepted on the change of
+// Re log psi like a single flip.
+template <int K, int KP, int NW, class Rng>
+__device__ __forceinline__ bool rbm_fast_step2(const RbmDev& P, Spins<NW>& s, pair_t (&tr)[KP], pair_t (&ti)[KP],
+                                               pair_t (&re)[KP], Rng& rng, int lane, int tries) {
+    Spins<NW> mask;
+    draw_spins(rng, P.N, mask);
+    for (int t = 1; t < tries; t++) {
+        Spins<NW> m2;
+        draw_spins(rng, P.N, m2);
+#pragma unroll
+        for (int k = 0; k < NW; k++) mask.w[k] &= m2.w[k];
+    }
+    Spins<NW> s2 = s;
+    pair_t nr[KP], ni[KP];
+#pragma unroll
+    for (int kk = 0; kk < KP; kk++) {
+        nr[kk] = tr[kk];
+        ni[kk] = ti[kk];
+    }
+#pragma unroll
+    for (int k = 0; k < NW; k++) {
+        uint64_t m = mask.w[k];
+        while (m) {
+            const int site = 64 * k + (__ffsll(static_cast<long long>(m)) - 1);
+            m &= m - 1;
+            s2.flip(site);
+            const pair_t two_s = splat2(s2.up(site) ? 2.0f : -2.0f);
+            const float4* row = P.Wq + static_cast<long>(site) * KP * 32 + lane;
+#pragma unroll
+            for (int kk = 0; kk < KP; kk++) {
+                const float4 w = __ldg(row + 32 * kk);
+                nr[kk] = fma2(two_s, pk2(w.x, w.y), nr[kk]);
+                ni[kk] = fma2(two_s, pk2(w.z, w.w), ni[kk]);
+            }
+        }
+    }
+    pair_t nre[KP];
+    float part = 0.0f;
+#pragma unroll
+    for (int kk = 0; kk < KP; kk++) {
+        nre[kk] = lc_re2(nr[kk], ni[kk]);
+        float d0, d1;
+        up2(sub2(nre[kk], re[kk]), d0, d1);
+        part = __fadd_rn(part, d0);
+        if (2 * kk + 1 < K) part = __fadd_rn(part, d1);
+    }
+    const float delta = warp_sum_xor(part);
+    bool accept = delta > 0.0f;
+    if (!accept) accept = rng.uniform() <= expf_det(__fmul_rn(2.0f, delta));
+    if (accept) {
+        s = s2;
+#pragma unroll
+        for (int kk = 0; kk < KP; kk++) {
+            tr[kk] = nr[kk];
+            ti[kk] = ni[kk];
+            re[kk] = nre[kk];
+        }
+    }
+    return accept;
+}
+
 // sign * (-i)^ypow * coef of string n for the current (original) spins, in FP32: the
 // local-energy sums run in FP32 with compensated (Kahan) accumulation, since GB300's
 // FP64 rate is 1/64 of its FP32 rate and every lane of the warp executes the sum
@@ -416,6 +482,60 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, K > 13 ? 3 : 4) rbm_mc_ke
                 for (int k = 0; k < NW; k++) L.sample_spins[row * NW + k] = s.w[k];
             }
             sample++;
+        }
+    }
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < NW; k++) L.spins[static_cast<long>(w) * NW + k] = s.w[k];
+        L.rng_index[w] = rng.index;
+        L.accepts[w] += acc;
+        L.proposals[w] += props;
+    }
+}
+
+// Fast-sweep sampler (MonteCarloLoop::set_fast_sweep, MonteCarloLoop.hpp:108-113, 139-151,
+// 162-171): a thermalisation sweep is N mask updates, a sampling sweep one.  The angles are
+// recomputed from the spins every N updates of the thermalisation and at the start of every
+// sample's updates (and every N updates within them).
+template <int K, int NW>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock, K > 13 ? 3 : 4) rbm_mc_fast_kernel(RbmDev P, McLaunch L) {
+    const int lane = threadIdx.x & 31;
+    const int w = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+    if (w >= L.B) return;
+    WarpRng rng;
+    rng.init(L.seed, L.walker_base + static_cast<uint32_t>(w), L.rng_index[w], lane);
+    Spins<NW> s;
+    if (L.init) {
+#pragma unroll
+        for (int k = 0; k < NW; k++) s.w[k] = 0;
+        draw_spins(rng, P.N, s);
+    } else {
+#pragma unroll
+        for (int k = 0; k < NW; k++) s.w[k] = L.spins[static_cast<long>(w) * NW + k];
+    }
+    constexpr int KP = (K + 1) / 2;
+    pair_t tr[KP], ti[KP], re[KP];
+    unsigned long long acc = 0, props = 0;
+    auto refresh = [&]() {
+        rbm_refresh2(P, s, tr, ti, lane);
+#pragma unroll
+        for (int kk = 0; kk < KP; kk++) re[kk] = lc_re2(tr[kk], ti[kk]);
+    };
+    for (int sw = 0; sw < L.n_therm; sw++) {
+        refresh();
+        for (int p = 0; p < P.N; p++) acc += rbm_fast_step2<K>(P, s, tr, ti, re, rng, lane, L.fast_tries);
+        props += P.N;
+    }
+    for (int sample = 0; sample < L.n_samples; sample++) {
+        for (int u = 0; u < L.sweeps_per_sample; u++) {
+            if (u % P.N == 0) refresh();
+            acc += rbm_fast_step2<K>(P, s, tr, ti, re, rng, lane, L.fast_tries);
+        }
+        props += L.sweeps_per_sample;
+        const long row = static_cast<long>(L.sample_base + sample) * L.B + w;
+        if (L.sample_spins && lane == 0) {
+#pragma unroll
+            for (int k = 0; k < NW; k++) L.sample_spins[row * NW + k] = s.w[k];
         }
     }
     if (lane == 0) {
@@ -608,6 +728,17 @@ cudaError_t rbm_mc_launch_k(const RbmDev& P, const OpDev* op, const McLaunch& L,
     const int nw = (P.N + 63) / 64;
     const dim3 grid((L.B + kWarpsPerBlock - 1) / kWarpsPerBlock), block(32 * kWarpsPerBlock);
     (void)op;
+    if (L.fast_tries > 0) {
+        if (L.total_z) return cudaErrorInvalidValue;
+        switch (nw) {
+            case 1: rbm_mc_fast_kernel<K, 1><<<grid, block, 0, st>>>(P, L); break;
+            case 2: rbm_mc_fast_kernel<K, 2><<<grid, block, 0, st>>>(P, L); break;
+            case 3: rbm_mc_fast_kernel<K, 3><<<grid, block, 0, st>>>(P, L); break;
+            case 4: rbm_mc_fast_kernel<K, 4><<<grid, block, 0, st>>>(P, L); break;
+            default: return cudaErrorInvalidValue;
+        }
+        return cudaGetLastError();
+    }
     switch (nw) {
         case 1: rbm_mc_kernel<K, 1><<<grid, block, 0, st>>>(P, L); break;
         case 2: rbm_mc_kernel<K, 2><<<grid, block, 0, st>>>(P, L); break;
