@@ -163,9 +163,25 @@ RBMG_API int rbmg_ensemble_samples(rbmg_ensemble* ens, const rbmg_psi* psi, cons
  * (source/network_functions/ExpectationValue.cu, pyRBMonGPU/main.cpp:295-339) */
 /* __call__(psi, operator, ensemble) -> <O>                        (:17-73)  */
 RBMG_API int rbmg_ev_value(const rbmg_psi* psi, const rbmg_operator* op, rbmg_ensemble* ens, double* value /* [2] */);
-/* __call__(psi, [operators], ensemble) -> [<O_i>]                 (:448-518) */
+/* __call__(psi, [operators], ensemble) -> [<O_i>]                 (:448-518)
+ * one pass over the ensemble: every operator on the same configurations */
 RBMG_API int rbmg_ev_values(const rbmg_psi* psi, const rbmg_operator* const* ops, int num_ops, rbmg_ensemble* ens,
                    double* values /* [2 num_ops] */);
+/* fluctuation_gradient -> grad[P], the gradient of sigma = sqrt(<|E|^2> - |<E>|^2)   (:258-348)
+ * grad_k = (2 conj(<E* E_k> - <E>* <E_k>) - 2 <E>* <E O_k*> + 2 <O_k>* (2|<E>|^2 - <|E|^2>)) / (2 sigma);
+ * entries k < 2N are zero; sigma (may be NULL) receives sigma.  Psi and PsiDeep. */
+RBMG_API int rbmg_ev_fluctuation_gradient(const rbmg_psi* psi, const rbmg_operator* op, rbmg_ensemble* ens,
+                                          double* grad /* [2P] */, double* sigma);
+/* difference(psi, psi_prime, [operators], ensemble) -> [<E'_i> - <r E_i> / <r>]   (:350-446)
+ * over psi's ensemble, E' the local energy under psi_prime, r = |psi / psi_prime|^2; Psi only
+ * (its instantiations), psi_prime with psi's N and padded M. */
+RBMG_API int rbmg_ev_difference(const rbmg_psi* psi, const rbmg_psi* psi_prime, const rbmg_operator* const* ops,
+                                int num_ops, rbmg_ensemble* ens, double* values /* [2 num_ops] */);
+/* corrected(psi, operator, operator2, ensemble) -> (<E> / <a>, <a>), a = exp(2 Im E + Re(E E - E))
+ * (:76-127); as in the reference the local energy is taken with the first operator twice and
+ * operator2 is not used.  The reference binds it for PsiDeep; every network is accepted. */
+RBMG_API int rbmg_ev_corrected(const rbmg_psi* psi, const rbmg_operator* op, const rbmg_operator* op2,
+                               rbmg_ensemble* ens, double* value /* [2] */, double* abs2);
 /* fluctuation -> (sigma, <O>)                                     (:130-175) */
 RBMG_API int rbmg_ev_fluctuation(const rbmg_psi* psi, const rbmg_operator* op, rbmg_ensemble* ens, double* sigma,
                         double* value /* [2] */);

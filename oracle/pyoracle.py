@@ -257,6 +257,89 @@ def local_energy(psi, op, spins, lp=None):
     return complex(out[0], out[1])
 
 
+def E_k(psi, op, spins, lp=None):
+    """E_k(s) = sum_n e_n(s) O_k(s'_n), the local energy's parameter vector
+    (Operator.hpp:145-179 foreach_E_k_s_prime) of one configuration."""
+    s = np.ascontiguousarray(spins, np.uint64)
+    if lp is None:
+        lp = log_psi(psi, s)
+    lpa = np.array([lp.real, lp.imag])
+    acc = np.zeros(2 * psi.num_params)
+    lib().or_E_k_accumulate(C.byref(psi.c), C.byref(op.c), _ptr(s, _u64p), _ptr(lpa), C.c_double(1.0), _ptr(acc))
+    return acc.view(np.complex128)
+
+
+def exact_configs(psi):
+    """Every configuration of N <= 16 spins with the reference's ExactSummation weight
+    prefactor^2 |psi(s)|^2 (Psi.hpp:272-275); averages are sums of weight x value (its
+    get_num_steps is 1)."""
+    s = np.arange(2 ** psi.N, dtype=np.uint64)[:, None]
+    lp = np.array([log_psi(psi, x) for x in s])
+    return s, np.exp(2.0 * (np.log(psi.c.prefactor) + lp.real))
+
+
+def _avg_weights(n, weights):
+    """per-sample factors of the averages: weight / num_steps (MonteCarloLoop: 1 / n)"""
+    return np.full(n, 1.0 / n) if weights is None else np.asarray(weights, np.float64)
+
+
+def fluctuation_gradient(psi, op, spins, weights=None):
+    """ExpectationValue::fluctuation_gradient (ExpectationValue.cu:258-348): the gradient of
+    sigma = sqrt(<|E|^2> - |<E>|^2),
+      1 / (2 sigma) (2 conj(<E* E_k> - <E>* <E_k>) - 2 <E>* <E O_k*> + 2 <O_k>* (2 |<E>|^2 - <|E|^2>))."""
+    sp = np.asarray(spins, np.uint64)
+    c = _avg_weights(len(sp), weights)
+    lp = [log_psi(psi, x) for x in sp]
+    E = np.array([local_energy(psi, op, x, l) for x, l in zip(sp, lp)])
+    O = np.array([O_k(psi, x) for x in sp])
+    Ek = np.array([E_k(psi, op, x, l) for x, l in zip(sp, lp)])
+    Ea = c @ E
+    E2 = c @ np.abs(E) ** 2
+    sigma = np.sqrt(E2 - abs(Ea) ** 2)
+    EEk = c @ (np.conj(E)[:, None] * Ek)
+    Oa = c @ O
+    EO = c @ (E[:, None] * np.conj(O))
+    Eka = c @ Ek
+    return (2 * np.conj(EEk - np.conj(Ea) * Eka) - 2 * np.conj(Ea) * EO
+            + 2 * np.conj(Oa) * (2 * abs(Ea) ** 2 - E2)) / (2 * sigma)
+
+
+def ev_list(psi, ops, spins, weights=None):
+    """ExpectationValue::operator() of an operator list (ExpectationValue.cu:448-518): every
+    operator's <E_loc> over the same configurations."""
+    sp = np.asarray(spins, np.uint64)
+    c = _avg_weights(len(sp), weights)
+    lp = [log_psi(psi, x) for x in sp]
+    return np.array([c @ np.array([local_energy(psi, o, x, l) for x, l in zip(sp, lp)]) for o in ops])
+
+
+def ev_difference(psi, psi_prime, ops, spins, weights=None):
+    """ExpectationValue::difference (ExpectationValue.cu:350-446): for each operator
+    <E'> - <r E> / <r>, E' the local energy under psi_prime, r = |psi / psi_prime|^2."""
+    sp = np.asarray(spins, np.uint64)
+    c = _avg_weights(len(sp), weights)
+    lp = [log_psi(psi, x) for x in sp]
+    lpp = [log_psi(psi_prime, x) for x in sp]
+    r = np.exp(2.0 * (np.real(lp) - np.real(lpp)))
+    out = []
+    for o in ops:
+        a = c @ np.array([local_energy(psi_prime, o, x, l) for x, l in zip(sp, lpp)])
+        b = c @ (r * np.array([local_energy(psi, o, x, l) for x, l in zip(sp, lp)]))
+        out.append(a - b / (c @ r))
+    return np.array(out)
+
+
+def ev_corrected(psi, op, spins, weights=None):
+    """ExpectationValue::corrected (ExpectationValue.cu:76-127).  The reference evaluates its
+    first operator twice (operator2 is not used): with E the local energy, it returns
+    (<E> / <a>, <a>), a = exp(2 Im E + Re(E E - E))."""
+    sp = np.asarray(spins, np.uint64)
+    c = _avg_weights(len(sp), weights)
+    E = np.array([local_energy(psi, op, x) for x in sp])
+    a = np.exp(2.0 * E.imag + (E * E - E).real)
+    return (c @ E) / (c @ a), c @ a
+
+
 def exact_norm(psi):
     return lib().or_exact_norm(C.byref(psi.c))
 

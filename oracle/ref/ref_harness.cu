@@ -221,6 +221,21 @@ int main(int argc, char** argv) {
         }
         if (meta_i("ok", 0)) ok_vectors(psi, P);
         if (meta_i("mc_samples", 0)) mc_outputs(psi, op, N, P);
+        if (meta_i("ev_extra", 0)) {
+            // ExpectationValue::fluctuation_gradient, the operator-list call and difference
+            // (source/network_functions/ExpectationValue.cu:258-348, 350-446, 448-518)
+            Psi psi_prime = load_rbm("pp_", N, M);
+            const auto hop = load_operator("hop_");
+            ExactSummation es(static_cast<unsigned>(N), false);
+            ExpectationValue ev(false);
+            std::vector<cplx> fg(P);
+            ev.fluctuation_gradient(fg.data(), psi, op, es);
+            save("fluct_gradient", fg.data(), fg.size());
+            const auto vals = ev(psi, std::vector<Operator>{op, hop}, es);
+            save("ev_list", vals.data(), vals.size());
+            const auto diff = ev.difference(psi, psi_prime, std::vector<Operator>{op, hop}, es);
+            save("ev_difference", diff.data(), diff.size());
+        }
         if (meta_i("kl", 0)) {
             // KullbackLeibler value / gradient (source/network_functions/KullbackLeibler.cu:91-137)
             Psi psi_prime = load_rbm("pp_", N, M);
@@ -261,6 +276,22 @@ int main(int argc, char** argv) {
         if (meta_i("exact", 0)) exact_outputs(psi, psi_prime, op, N, P);
         if (meta_i("ok", 0)) ok_vectors(psi, P);
         if (meta_i("mc_samples", 0)) mc_outputs(psi, op, N, P);
+        if (meta_i("ev_extra", 0)) {
+            // ExpectationValue::fluctuation_gradient, the operator-list call and corrected
+            // (source/network_functions/ExpectationValue.cu:258-348, 448-518, 76-127)
+            const auto hop = load_operator("hop_");
+            ExactSummation es(static_cast<unsigned>(N), false);
+            ExpectationValue ev(false);
+            std::vector<cplx> fg(P);
+            ev.fluctuation_gradient(fg.data(), psi, op, es);
+            save("fluct_gradient", fg.data(), fg.size());
+            const auto vals = ev(psi, std::vector<Operator>{op, hop}, es);
+            save("ev_list", vals.data(), vals.size());
+            const auto cr = ev.corrected(psi, op, hop, es);
+            scalar("corrected_re", cr.first.real());
+            scalar("corrected_im", cr.first.imag());
+            scalar("corrected_abs2", cr.second);
+        }
         if (meta_i("hsd2", 0)) {
             // HilbertSpaceDistance::distance_2nd_order (HilbertSpaceDistance_2nd_order.cu:69-95)
             const auto op_a = load_operator("h2a_");

@@ -66,6 +66,9 @@ SIGNATURES = {
     "rbmg_ensemble_samples": [_vp, _vp, _vp, _u64p, _dp, _dp],
     "rbmg_ev_value": [_vp, _vp, _vp, _dp],
     "rbmg_ev_values": [_vp, _vpp, C.c_int, _vp, _dp],
+    "rbmg_ev_fluctuation_gradient": [_vp, _vp, _vp, _dp, _dp],
+    "rbmg_ev_difference": [_vp, _vp, _vpp, C.c_int, _vp, _dp],
+    "rbmg_ev_corrected": [_vp, _vp, _vp, _vp, _dp, _dp],
     "rbmg_ev_fluctuation": [_vp, _vp, _vp, _dp, _dp],
     "rbmg_ev_gradient": [_vp, _vp, _vp, _dp, _dp],
     "rbmg_local_energies": [_vp, _vp, C.c_int, _u64p, _dp],

@@ -557,6 +557,30 @@ class ExpectationValue:
         call("rbmg_ev_gradient", psi._h, operator_._h, spin_ensemble._h, _p(g.view(np.float64)), _p(out))
         return g, complex(out[0], out[1])
 
+    def fluctuation_gradient(self, psi, operator_, spin_ensemble):
+        """ExpectationValue.cu:258-348 (main.cpp:301, 310): the gradient [P] of the energy
+        fluctuation sigma = sqrt(<|E_loc|^2> - |<E_loc>|^2)."""
+        g = np.zeros(psi.num_params, np.complex128)
+        call("rbmg_ev_fluctuation_gradient", psi._h, operator_._h, spin_ensemble._h, _p(g.view(np.float64)), None)
+        return g
+
+    def difference(self, psi, psi_prime, operator_list, spin_ensemble):
+        """ExpectationValue.cu:350-446 (main.cpp:304, 323): per operator
+        <E'_loc> - <r E_loc> / <r> over psi's ensemble, r = |psi / psi_prime|^2 (Psi only)."""
+        ops = (C.c_void_p * len(operator_list))(*[o._h for o in operator_list])
+        out = np.zeros(2 * len(operator_list))
+        call("rbmg_ev_difference", psi._h, psi_prime._h, ops, len(operator_list), spin_ensemble._h, _p(out))
+        return list(out.view(np.complex128))
+
+    def corrected(self, psi, operator_, operator2, spin_ensemble):
+        """ExpectationValue.cu:76-127 (main.cpp:309, 328) -> (<E> / <a>, <a>) with
+        a = exp(2 Im E + Re(E E - E)); like the reference it evaluates operator_ twice and
+        does not use operator2."""
+        out = np.zeros(2)
+        a = C.c_double()
+        call("rbmg_ev_corrected", psi._h, operator_._h, operator2._h, spin_ensemble._h, _p(out), C.byref(a))
+        return complex(out[0], out[1]), a.value
+
     def eloc_gradient(self, psi, operator_, spin_ensemble, score=True):
         """Extension (PsiDeep): the adjoint-kernel gradient, in PyTorch's convention
         dL/dRe + i dL/dIm.  score=False: L = Re <E_loc> on the ensemble's samples held

@@ -56,6 +56,7 @@ struct Workspace {
     DevBuf sample_spins, eloc, logpsi, logpsi_p, T, U, X, Tp, weights, coef1, coef2, coef3, omega, pr, nn;
     DevBuf partial, block_scratch, sums, acc_O, acc_EO, acc_Ek, acc_wO, acc_pO, block_max, zsum;
     DevBuf smat, smean, okrows, sshift, splanes, serror, sout;
+    DevBuf acc_B, eabs2, lsums, rw, rwc;
 };
 
 static Workspace& ws() {
@@ -812,7 +813,8 @@ struct Sums {
 
 int deep_gradient_chunk(const rbmg_psi* psi, const rbmg_operator* op, const Chunk& c, double2 e_shift,
                         double2* d_eloc, double2* acc_O, double2* acc_EO, double2* acc_Ek, double2* coef1,
-                        double2* coef2, cudaStream_t st);
+                        double2* coef2, cudaStream_t st,
+                        double2* acc_B = nullptr, double2* coef3 = nullptr);
 int deep_eloc_chunk(const rbmg_psi* psi, const rbmg_operator* op, const Chunk& c, double2* d_eloc, cudaStream_t st);
 int deep_stream(rbmg_ensemble* e, const rbmg_psi* psi, const rbmg_operator* op, bool want_eloc,
                 size_t max_chunk_samples, const std::function<int(const Chunk&)>& fn);
@@ -939,15 +941,156 @@ extern "C" int rbmg_ev_value(const rbmg_psi* psi, const rbmg_operator* op, rbmg_
     return RBMG_OK;
 }
 
+namespace rbmg {
+// device accumulators of `n` complex sums, zeroed
+static int zero_sums(DevBuf& b, int n) {
+    RBMG_CK(b.ensure(sizeof(double2) * std::max(1, n)));
+    RBMG_CK(cudaMemsetAsync(b.p, 0, sizeof(double2) * std::max(1, n), stream()));
+    return RBMG_OK;
+}
+
+// sums[0] += sum_s w[s] v[s]
+static int add_sum(const Chunk& c, const double* w, const double2* v, double2* sum) {
+    Workspace& W = ws();
+    RBMG_CK(W.block_scratch.ensure(sizeof(double2) * kSumBlocks * kMaxSeries));
+    SeriesSet set{};
+    set.n = 1;
+    set.v[0] = v;
+    RBMG_CK(launch_weighted_sums(c.count, w, set, W.block_scratch.as<double2>(), sum, stream()));
+    return RBMG_OK;
+}
+}  // namespace rbmg
+
+// ExpectationValue::operator() of an operator list (ExpectationValue.cu:448-518): one pass
+// over the ensemble, every operator's local energy on the same configurations.
 extern "C" int rbmg_ev_values(const rbmg_psi* psi, const rbmg_operator* const* ops, int num_ops, rbmg_ensemble* ens,
                               double* values) {
     if (!ops || num_ops < 0 || (num_ops > 0 && !values)) return fail(RBMG_EINVAL, "ev list: bad arguments");
-    // one ensemble pass per operator: MC draws continue their streams as the
-    // reference's single pass would not; for ExactSummation the result is identical.
+    if (num_ops == 0) return RBMG_OK;
     for (int q = 0; q < num_ops; q++) {
-        const int r = rbmg_ev_value(psi, ops[q], ens, values + 2 * q);
+        if (!ops[q]) return fail(RBMG_EINVAL, "ev list: null operator");
+        const int r = check_pair(psi, ops[q], ens);
         if (r != RBMG_OK) return r;
     }
+    Workspace& W = ws();
+    int r = zero_sums(W.lsums, num_ops);
+    if (r != RBMG_OK) return r;
+    StreamResult res;
+    r = run_stream(ens, psi, nullptr, false, size_t(1) << 22, &res, [&](const Chunk& c) -> int {
+        for (int q = 0; q < num_ops; q++) {
+            const double2* e = nullptr;
+            int rr = chunk_eloc(psi, ops[q], c, &e);
+            if (rr == RBMG_OK) rr = add_sum(c, c.weights, e, W.lsums.as<double2>() + q);
+            if (rr != RBMG_OK) return rr;
+        }
+        return RBMG_OK;
+    });
+    if (r != RBMG_OK) return r;
+    std::vector<double2> h(num_ops);
+    RBMG_CK(cudaMemcpyAsync(h.data(), W.lsums.p, sizeof(double2) * num_ops, cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaStreamSynchronize(stream()));
+    for (int q = 0; q < num_ops; q++) {
+        values[2 * q] = h[q].x * res.norm_factor;
+        values[2 * q + 1] = h[q].y * res.norm_factor;
+    }
+    return RBMG_OK;
+}
+
+// ExpectationValue::difference (ExpectationValue.cu:350-446), Psi only (its instantiations):
+// per operator <E'> - <r E> / <r> over psi's ensemble, E' the local energy under psi_prime,
+// r = |psi / psi_prime|^2.
+extern "C" int rbmg_ev_difference(const rbmg_psi* psi, const rbmg_psi* psi_prime, const rbmg_operator* const* ops,
+                                  int num_ops, rbmg_ensemble* ens, double* values) {
+    if (!psi || !psi_prime || !ops || num_ops < 0 || (num_ops > 0 && !values))
+        return fail(RBMG_EINVAL, "difference: bad arguments");
+    if (psi->kind != 0 || psi_prime->kind != 0)
+        return fail(RBMG_EUNSUPPORTED, "difference: instantiated for Psi only (ExpectationValue.cu:529, 575)");
+    if (psi_prime->N != psi->N || psi_prime->Mpad != psi->Mpad)
+        return fail(RBMG_EUNSUPPORTED, "difference: psi_prime must have psi's N and padded M");
+    if (num_ops == 0) return RBMG_OK;
+    for (int q = 0; q < num_ops; q++) {
+        if (!ops[q]) return fail(RBMG_EINVAL, "difference: null operator");
+        const int r = check_pair(psi, ops[q], ens);
+        if (r != RBMG_OK) return r;
+    }
+    Workspace& W = ws();
+    int r = zero_sums(W.lsums, 2 * num_ops + 1);
+    if (r != RBMG_OK) return r;
+    double2* sums = W.lsums.as<double2>();
+    StreamResult res;
+    r = run_stream(ens, psi, nullptr, false, size_t(1) << 22, &res, [&](const Chunk& c) -> int {
+        RBMG_CK(W.logpsi.ensure(sizeof(double2) * c.count));
+        RBMG_CK(W.logpsi_p.ensure(sizeof(double2) * c.count));
+        RBMG_CK(W.rw.ensure(sizeof(double) * c.count));
+        RBMG_CK(W.rwc.ensure(sizeof(double2) * c.count));
+        EstLaunch L{};
+        L.count = c.count;
+        L.enum_base = c.enum_base;
+        L.spins = c.spins;
+        L.flags = EST_LOGPSI | EST_PRIME | (c.enumerate ? EST_ENUMERATE : 0);
+        L.logpsi = W.logpsi.as<double2>();
+        L.logpsi_prime = W.logpsi_p.as<double2>();
+        const RbmDev d = psi->rbm_dev(), dp = psi_prime->rbm_dev();
+        RBMG_CK(launch_rbm_estimate(d, nullptr, &dp, L, stream()));
+        RBMG_CK(launch_ratio_weights(c.count, c.weights, W.logpsi.as<double2>(), W.logpsi_p.as<double2>(),
+                                     W.rw.as<double>(), W.rwc.as<double2>(), stream()));
+        int rr = add_sum(c, nullptr, W.rwc.as<double2>(), sums + 2 * num_ops);
+        for (int q = 0; q < num_ops && rr == RBMG_OK; q++) {
+            const double2* e = nullptr;
+            rr = chunk_eloc(psi, ops[q], c, &e);
+            if (rr == RBMG_OK) rr = add_sum(c, W.rw.as<double>(), e, sums + num_ops + q);
+            if (rr == RBMG_OK) rr = chunk_eloc(psi_prime, ops[q], c, &e);
+            if (rr == RBMG_OK) rr = add_sum(c, c.weights, e, sums + q);
+        }
+        return rr;
+    });
+    if (r != RBMG_OK) return r;
+    std::vector<double2> h(2 * num_ops + 1);
+    RBMG_CK(cudaMemcpyAsync(h.data(), sums, sizeof(double2) * h.size(), cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaStreamSynchronize(stream()));
+    const double f = res.norm_factor;
+    const double p = h[2 * num_ops].x * f;
+    for (int q = 0; q < num_ops; q++) {
+        const cplx a = cplx(h[q].x, h[q].y) * f, b = cplx(h[num_ops + q].x, h[num_ops + q].y) * f;
+        const cplx v = a - b / p;
+        values[2 * q] = v.real();
+        values[2 * q + 1] = v.imag();
+    }
+    return RBMG_OK;
+}
+
+// ExpectationValue::corrected (ExpectationValue.cu:76-127).  As in the reference the local
+// energy is evaluated with the first operator twice (operator2 is accepted and not used):
+// value = <E> / <a>, abs2 = <a>, a = exp(2 Im E + Re(E E - E)).
+extern "C" int rbmg_ev_corrected(const rbmg_psi* psi, const rbmg_operator* op, const rbmg_operator* op2,
+                                 rbmg_ensemble* ens, double* value, double* abs2) {
+    if (!op || !op2 || !value || !abs2) return fail(RBMG_EINVAL, "corrected: null");
+    int r = check_pair(psi, op, ens);
+    if (r != RBMG_OK) return r;
+    Workspace& W = ws();
+    r = zero_sums(W.lsums, 2);
+    if (r != RBMG_OK) return r;
+    double2* sums = W.lsums.as<double2>();
+    StreamResult res;
+    r = run_stream(ens, psi, op, true, size_t(1) << 22, &res, [&](const Chunk& c) -> int {
+        const double2* e = nullptr;
+        int rr = chunk_eloc(psi, op, c, &e);
+        if (rr != RBMG_OK) return rr;
+        RBMG_CK(W.eabs2.ensure(sizeof(double2) * c.count));
+        RBMG_CK(launch_corrected_terms(c.count, e, W.eabs2.as<double2>(), stream()));
+        rr = add_sum(c, c.weights, e, sums);
+        if (rr == RBMG_OK) rr = add_sum(c, c.weights, W.eabs2.as<double2>(), sums + 1);
+        return rr;
+    });
+    if (r != RBMG_OK) return r;
+    double2 h[2];
+    RBMG_CK(cudaMemcpyAsync(h, sums, sizeof(h), cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaStreamSynchronize(stream()));
+    const cplx A = cplx(h[0].x, h[0].y) * res.norm_factor;
+    const double a = h[1].x * res.norm_factor;
+    value[0] = (A / a).real();
+    value[1] = (A / a).imag();
+    *abs2 = a;
     return RBMG_OK;
 }
 
@@ -968,8 +1111,10 @@ extern "C" int rbmg_ev_fluctuation(const rbmg_psi* psi, const rbmg_operator* op,
 // The gradient's sums, left on the device: acc_O = sum w O, acc_EO = sum w (E - E0) O*,
 // acc_Ek = sum w (E_k - E0 O) over the O_k entries k >= 2N, sums[0] = sum w E; E0 (the
 // first chunk's mean local energy) and the ensemble's normalisation factor come back.
+// fluct: also B = sum w conj(E - E0) (E_k - E0 O_k) into acc_B and sum w |E|^2 into sums[1]
+// (the further sums of ExpectationValue::fluctuation_gradient)
 static int ev_gradient_sums(const rbmg_psi* psi, const rbmg_operator* op, rbmg_ensemble* ens, cplx* E0_out,
-                            double* norm_out) {
+                            double* norm_out, bool fluct = false) {
     int r = check_pair(psi, op, ens);
     if (r != RBMG_OK) return r;
     const int N = psi->N, P = psi->num_params();
@@ -982,6 +1127,10 @@ static int ev_gradient_sums(const rbmg_psi* psi, const rbmg_operator* op, rbmg_e
     RBMG_CK(cudaMemsetAsync(W.acc_O.p, 0, sizeof(double2) * ok_len, stream()));
     RBMG_CK(cudaMemsetAsync(W.acc_EO.p, 0, sizeof(double2) * ok_len, stream()));
     RBMG_CK(cudaMemsetAsync(W.acc_Ek.p, 0, sizeof(double2) * ok_len, stream()));
+    if (fluct) {
+        RBMG_CK(W.acc_B.ensure(sizeof(double2) * ok_len));
+        RBMG_CK(cudaMemsetAsync(W.acc_B.p, 0, sizeof(double2) * ok_len, stream()));
+    }
     RBMG_CK(W.sums.ensure(sizeof(double2) * kMaxSeries));
     RBMG_CK(W.block_scratch.ensure(sizeof(double2) * kSumBlocks * kMaxSeries));
     RBMG_CK(cudaMemsetAsync(W.sums.p, 0, sizeof(double2) * kMaxSeries, stream()));
@@ -1013,9 +1162,12 @@ static int ev_gradient_sums(const rbmg_psi* psi, const rbmg_operator* op, rbmg_e
             }
             RBMG_CK(W.coef1.ensure(sizeof(double2) * c.count));
             RBMG_CK(W.coef2.ensure(sizeof(double2) * c.count));
+            if (fluct) RBMG_CK(W.coef3.ensure(sizeof(double2) * c.count));
             const int rr = deep_gradient_chunk(psi, op, c, make_double2(E0.real(), E0.imag()), W.eloc.as<double2>(),
                                                W.acc_O.as<double2>(), W.acc_EO.as<double2>(), W.acc_Ek.as<double2>(),
-                                               W.coef1.as<double2>(), W.coef2.as<double2>(), stream());
+                                               W.coef1.as<double2>(), W.coef2.as<double2>(), stream(),
+                                               fluct ? W.acc_B.as<double2>() : nullptr,
+                                               fluct ? W.coef3.as<double2>() : nullptr);
             if (rr != RBMG_OK) return rr;
         } else {
             const OpDev od = op->dev();
@@ -1060,10 +1212,28 @@ static int ev_gradient_sums(const rbmg_psi* psi, const rbmg_operator* op, rbmg_e
                                         c.weights, W.X.as<float2>(), op->num_offdiag, op->d_site_ptr.as<int>(),
                                         op->d_site_slots.as<int>(), W.acc_Ek.as<double2>(), part, kSplits,
                                         stream()));
+            if (fluct) {
+                RBMG_CK(W.coef3.ensure(sizeof(double2) * c.count));
+                RBMG_CK(launch_coef_conj(c.count, c.weights, W.eloc.as<double2>(), make_double2(E0.real(), E0.imag()),
+                                         W.coef3.as<double2>(), stream()));
+                RBMG_CK(launch_outer_reduce(c.count, N, nw, psi->M, c.spins, c.enum_base, c.enumerate,
+                                            W.coef3.as<double2>(), W.U.as<float2>(), psi->Mpad, 0,
+                                            W.acc_B.as<double2>(), part, kSplits, stream()));
+                RBMG_CK(launch_vterm_reduce(c.count, N, nw, psi->M, psi->Mpad, c.spins, c.enum_base, c.enumerate,
+                                            nullptr, W.X.as<float2>(), op->num_offdiag, op->d_site_ptr.as<int>(),
+                                            op->d_site_slots.as<int>(), W.acc_B.as<double2>(), part, kSplits,
+                                            stream(), W.coef3.as<double2>()));
+            }
         }
         SeriesSet set{};
         set.n = 1;
         set.v[0] = W.eloc.as<double2>();
+        if (fluct) {
+            RBMG_CK(W.eabs2.ensure(sizeof(double2) * c.count));
+            RBMG_CK(launch_abs2(c.count, W.eloc.as<double2>(), W.eabs2.as<double2>(), stream()));
+            set.n = 2;
+            set.v[1] = W.eabs2.as<double2>();
+        }
         RBMG_CK(launch_weighted_sums(c.count, c.weights, set, W.block_scratch.as<double2>(), W.sums.as<double2>(),
                                      stream()));
         return RBMG_OK;
@@ -1104,6 +1274,50 @@ extern "C" int rbmg_ev_gradient(const rbmg_psi* psi, const rbmg_operator* op, rb
     }
     value[0] = E.real();
     value[1] = E.imag();
+    return RBMG_OK;
+}
+
+// ExpectationValue::fluctuation_gradient (ExpectationValue.cu:258-348): the gradient of
+// sigma = sqrt(<|E|^2> - |<E>|^2),
+//   1 / (2 sigma) (2 conj(<E* E_k> - <E>* <E_k>) - 2 <E>* <E O_k*> + 2 <O_k>* (2 |<E>|^2 - <|E|^2>)),
+// formed from sums centred on E0 (the first chunk's mean local energy):
+//   <E* E_k> - <E>* <E_k> = B + E0 conj(EO') - conj(<E> - E0) <E_k>,  <E_k> = Ek' + E0 <O>,
+//   -2 <E>* <E O*> + 2 <O>* (2 |<E>|^2 - <|E|^2>) = -2 <E>* EO' + 2 <O>* (<E>* (<E> - E0) - sigma^2),
+// with EO' = <(E - E0) O*>, Ek' = <E_k - E0 O>, B = <(E - E0)* (E_k - E0 O)>.
+extern "C" int rbmg_ev_fluctuation_gradient(const rbmg_psi* psi, const rbmg_operator* op, rbmg_ensemble* ens,
+                                            double* grad, double* sigma) {
+    if (!op || !grad) return fail(RBMG_EINVAL, "fluctuation_gradient: null");
+    cplx E0;
+    double f = 0.0;
+    int r = ev_gradient_sums(psi, op, ens, &E0, &f, true);
+    if (r != RBMG_OK) return r;
+    const int N = psi->N;
+    const size_t ok_len = static_cast<size_t>(psi->num_params() - 2 * N);
+    Workspace& W = ws();
+    std::vector<double2> O(ok_len), EO(ok_len), Ek(ok_len), B(ok_len);
+    double2 Es[2];
+    RBMG_CK(cudaMemcpyAsync(O.data(), W.acc_O.p, sizeof(double2) * ok_len, cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaMemcpyAsync(EO.data(), W.acc_EO.p, sizeof(double2) * ok_len, cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaMemcpyAsync(Ek.data(), W.acc_Ek.p, sizeof(double2) * ok_len, cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaMemcpyAsync(B.data(), W.acc_B.p, sizeof(double2) * ok_len, cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaMemcpyAsync(Es, W.sums.p, sizeof(Es), cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaStreamSynchronize(stream()));
+    const cplx E = cplx(Es[0].x, Es[0].y) * f;
+    const double E2 = Es[1].x * f;
+    const double var = std::max(0.0, E2 - std::norm(E));
+    const double sig = std::sqrt(var);
+    cplx* g = reinterpret_cast<cplx*>(grad);
+    for (int k = 0; k < 2 * N; k++) g[k] = 0.0;
+    const cplx de = E - E0;
+    for (size_t k = 0; k < ok_len; k++) {
+        const cplx o = cplx(O[k].x, O[k].y) * f, eo = cplx(EO[k].x, EO[k].y) * f;
+        const cplx ek = cplx(Ek[k].x, Ek[k].y) * f, b = cplx(B[k].x, B[k].y) * f;
+        const cplx eka = ek + E0 * o;
+        const cplx t1 = 2.0 * std::conj(b + E0 * std::conj(eo) - std::conj(de) * eka);
+        const cplx t23 = -2.0 * std::conj(E) * eo + 2.0 * std::conj(o) * (std::conj(E) * de - var);
+        g[2 * N + k] = (t1 + t23) / (2.0 * sig);
+    }
+    if (sigma) *sigma = sig;
     return RBMG_OK;
 }
 

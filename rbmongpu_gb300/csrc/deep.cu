@@ -991,7 +991,7 @@ int deep_ok_vector(const rbmg_psi* psi, const uint64_t* d_spins, double2* d_out,
 
 int deep_gradient_chunk(const rbmg_psi* psi, const rbmg_operator* op, const Chunk& c, double2 e_shift,
                         double2* d_eloc, double2* acc_O, double2* acc_EO, double2* acc_Ek, double2* coef1,
-                        double2* coef2, cudaStream_t st) {
+                        double2* coef2, cudaStream_t st, double2* acc_B, double2* coef3) {
     if (psi->kind == 2) return fail(RBMG_EUNSUPPORTED, "gradient: not instantiated for PsiPair (ExpectationValue.cu:553)");
     const DeepNetDev net = net_of(psi, 0);
     const int P = net.P - 2 * net.N;
@@ -1015,6 +1015,12 @@ int deep_gradient_chunk(const rbmg_psi* psi, const rbmg_operator* op, const Chun
         int r = col_reduce(cnt, P, coef1 + base, orows.as<double2>(), P, 0, acc_O, st);
         if (r == RBMG_OK) r = col_reduce(cnt, P, coef2 + base, orows.as<double2>(), P, 1, acc_EO, st);
         if (r == RBMG_OK) r = col_reduce(cnt, P, coef1 + base, erows.as<double2>(), P, 0, acc_Ek, st);
+        if (r == RBMG_OK && acc_B) {
+            // sum w conj(E - E0) (E_k - E0 O_k): the fluctuation gradient's covariance term
+            RBMG_CK(launch_coef_conj(cnt, c.weights ? c.weights + base : nullptr, d_eloc + base, e_shift, coef3 + base,
+                                     st));
+            r = col_reduce(cnt, P, coef3 + base, erows.as<double2>(), P, 0, acc_B, st);
+        }
         if (r != RBMG_OK) return r;
     }
     return RBMG_OK;

@@ -105,8 +105,9 @@ __global__ void finish_splits_kernel(long elems, int splits, const double2* __re
 // grid (ceil(M/32), N, splits), block 256 = 8 warps; warp w takes samples w, w+8, ...
 __global__ void vterm_kernel(int count, int N, int nw, int M, int Mpad, const uint64_t* __restrict__ spins,
                              uint64_t enum_base, int enumerate, const double* __restrict__ w,
-                             const float2* __restrict__ X, int num_offdiag, const int* __restrict__ site_ptr,
-                             const int* __restrict__ site_slots, double2* __restrict__ partial, int per_split) {
+                             const double2* __restrict__ cw, const float2* __restrict__ X, int num_offdiag,
+                             const int* __restrict__ site_ptr, const int* __restrict__ site_slots,
+                             double2* __restrict__ partial, int per_split) {
     __shared__ double2 red[8][32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int j = blockIdx.x * 32 + lane;
@@ -125,6 +126,10 @@ __global__ void vterm_kernel(int count, int N, int nw, int M, int Mpad, const ui
                 const float2 v = X[(s * num_offdiag + site_slots[q]) * Mpad + j];
                 x.x += v.x;
                 x.y += v.y;
+            }
+            if (cw) {   // complex per-sample coefficient
+                const float cr = static_cast<float>(cw[s].x), ci = static_cast<float>(cw[s].y);
+                x = make_float2(cr * x.x - ci * x.y, cr * x.y + ci * x.x);
             }
             part.x = fmaf(g, x.x, part.x);
             part.y = fmaf(g, x.y, part.y);
@@ -219,6 +224,33 @@ __global__ void coef_kernel(int count, const double* __restrict__ w, const doubl
     }
 }
 
+// c[s] = w[s] conj(v[s] - shift)
+__global__ void coef_conj_kernel(int count, const double* __restrict__ w, const double2* __restrict__ v,
+                                 double2 shift, double2* c) {
+    for (long s = blockIdx.x * 256L + threadIdx.x; s < count; s += static_cast<long>(gridDim.x) * 256) {
+        const double ws = w ? w[s] : 1.0;
+        c[s] = make_double2(ws * (v[s].x - shift.x), -ws * (v[s].y - shift.y));
+    }
+}
+
+// rw[s] = w[s] exp(2 (Re lp[s] - Re lpp[s])) (ExpectationValue.cu:391-395), rwc[s] = (rw[s], 0)
+__global__ void ratio_weight_kernel(int count, const double* __restrict__ w, const double2* __restrict__ lp,
+                                    const double2* __restrict__ lpp, double* rw, double2* rwc) {
+    for (long s = blockIdx.x * 256L + threadIdx.x; s < count; s += static_cast<long>(gridDim.x) * 256) {
+        const double r = (w ? w[s] : 1.0) * exp(2.0 * (lp[s].x - lpp[s].x));
+        rw[s] = r;
+        rwc[s] = make_double2(r, 0.0);
+    }
+}
+
+// a[s] = exp(2 Im E + Re(E E - E)) (ExpectationValue.cu:106-109)
+__global__ void corrected_kernel(int count, const double2* __restrict__ e, double2* a) {
+    for (long s = blockIdx.x * 256L + threadIdx.x; s < count; s += static_cast<long>(gridDim.x) * 256) {
+        const double2 v = e[s];
+        a[s] = make_double2(exp(2.0 * v.y + (v.x * v.x - v.y * v.y - v.x)), 0.0);
+    }
+}
+
 __global__ void abs2_kernel(int count, const double2* __restrict__ v, double2* out) {
     for (long s = blockIdx.x * 256L + threadIdx.x; s < count; s += static_cast<long>(gridDim.x) * 256)
         out[s] = make_double2(v[s].x * v[s].x + v[s].y * v[s].y, 0.0);
@@ -270,12 +302,12 @@ cudaError_t launch_outer_reduce(int count, int N, int nw, int M, const uint64_t*
 cudaError_t launch_vterm_reduce(int count, int N, int nw, int M, int Mpad, const uint64_t* spins, uint64_t enum_base,
                                 int enumerate, const double* w, const float2* X, int num_offdiag,
                                 const int* site_ptr, const int* site_slots, double2* out, double2* partial,
-                                int max_splits, cudaStream_t st) {
+                                int max_splits, cudaStream_t st, const double2* cw) {
     if (count <= 0 || num_offdiag == 0) return cudaSuccess;
     const int per_split = max(64, (count + max_splits - 1) / max_splits);
     const int splits = (count + per_split - 1) / per_split;
     const dim3 grid((M + 31) / 32, N, splits);
-    vterm_kernel<<<grid, 256, 0, st>>>(count, N, nw, M, Mpad, spins, enum_base, enumerate, w, X, num_offdiag,
+    vterm_kernel<<<grid, 256, 0, st>>>(count, N, nw, M, Mpad, spins, enum_base, enumerate, w, cw, X, num_offdiag,
                                        site_ptr, site_slots, partial, per_split);
     const long elems = static_cast<long>(1 + N) * M;
     finish_splits_kernel<<<grid_for(elems), 256, 0, st>>>(elems, splits, partial, out, -2.0);
@@ -306,6 +338,23 @@ cudaError_t launch_exp_weights(int count, const double2* lp, double shift, doubl
 cudaError_t launch_coef(int count, const double* w, const double2* v, double scale, double2* c, cudaStream_t st,
                         double2 shift) {
     coef_kernel<<<grid_for(count), 256, 0, st>>>(count, w, v, scale, shift, c);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_coef_conj(int count, const double* w, const double2* v, double2 shift, double2* c,
+                             cudaStream_t st) {
+    coef_conj_kernel<<<grid_for(count), 256, 0, st>>>(count, w, v, shift, c);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ratio_weights(int count, const double* w, const double2* lp, const double2* lpp, double* rw,
+                                 double2* rwc, cudaStream_t st) {
+    ratio_weight_kernel<<<grid_for(count), 256, 0, st>>>(count, w, lp, lpp, rw, rwc);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_corrected_terms(int count, const double2* e, double2* a, cudaStream_t st) {
+    corrected_kernel<<<grid_for(count), 256, 0, st>>>(count, e, a);
     return cudaGetLastError();
 }
 

@@ -142,7 +142,7 @@ def act_points(rng):
 
 
 def rbm_case(name, N, M, sigma, seed, op, hop, unitary, nu, mc=None, normalize=True, ok_count=4, smatrix=False,
-             kl=False):
+             kl=False, ev_extra=False):
     rng = np.random.Generator(np.random.PCG64(seed))
     b = cnormal(rng, M, sigma)
     W = cnormal(rng, (N, M), sigma)
@@ -154,6 +154,8 @@ def rbm_case(name, N, M, sigma, seed, op, hop, unitary, nu, mc=None, normalize=T
             "kl": int(kl)}
     if mc:
         meta.update(mc)
+    if ev_extra:   # fluctuation_gradient, the operator list [op, hop] and difference
+        meta["ev_extra"] = 1
     arrays = {"b.bin": b, "W.bin": W, "pp_b.bin": pb, "pp_W.bin": pW, "ok_spins.bin": ok_spins,
               "act_in.bin": act_points(rng)}
     arrays.update(op_arrays("op_", op))
@@ -162,7 +164,7 @@ def rbm_case(name, N, M, sigma, seed, op, hop, unitary, nu, mc=None, normalize=T
 
 
 def deep_case(name, kind, N, sizes, conns, sigma, seed, op, hop, unitary, nu, mc=None, dense=False, hsd2=None,
-              diag_density=0):
+              diag_density=0, ev_extra=False):
     rng = np.random.Generator(np.random.PCG64(seed))
     if dense:
         conn = [np.tile(np.arange(c, dtype=np.uint32)[:, None], (1, m)) for c, m in zip(conns, sizes)]
@@ -188,6 +190,8 @@ def deep_case(name, kind, N, sizes, conns, sigma, seed, op, hop, unitary, nu, mc
     arrays["ok_spins.bin"] = rng.integers(0, 2 ** N, 4, dtype=np.uint64)
     if mc:
         meta.update(mc)
+    if ev_extra:   # fluctuation_gradient, the operator list [op, hop] and corrected(op, hop)
+        meta["ev_extra"] = 1
     arrays.update(op_arrays("op_", op))
     arrays.update(op_arrays("hop_", hop))
     if diag_density:
@@ -217,7 +221,7 @@ def main():
     # N=12, M=24 complex RBM, sigma 0.01, periodic TFIM h=1: exact <H>, gradient, HSD to a
     # copy perturbed by complex N(0, 1e-3^2) under the identity operator (unitary).
     rbm_case("c1_rbm_exact", 12, 24, 0.01, 101, tfim_chain(12, 1.0, 1.0), identity_op(), True, 1.0,
-             mc={"mc_samples": 200, "mc_sweeps": 1, "mc_therm": 10, "mc_gradient": 1})
+             mc={"mc_samples": 200, "mc_sweeps": 1, "mc_therm": 10, "mc_gradient": 1}, ev_extra=True)
     # small RBM, non-unitary HSD with op = 1j * t * H (the reference's test_distance1 form)
     cf, ty, ix = tfim_chain(6, 1.0, 0.7)
     rbm_case("rbm6_hsd_nonunitary", 6, 12, 0.1, 7, tfim_chain(6, 1.0, 0.7), (1j * 1e-3 * cf, ty, ix), False, 2.0)
@@ -225,17 +229,17 @@ def main():
     rng = np.random.Generator(np.random.PCG64(11))
     mixed = mixed_operator(8, rng)
     rbm_case("rbm8_mixed_operator", 8, 16, 0.2, 12, mixed, mixed, False, 1.0,
-             mc={"mc_samples": 100, "mc_sweeps": 2, "mc_therm": 4, "mc_gradient": 1})
+             mc={"mc_samples": 100, "mc_sweeps": 2, "mc_therm": 4, "mc_gradient": 1}, ev_extra=True)
     # N=64, M=128 RBM, sigma 0.05, 8x8 periodic TFIM h=3: one reference chain (host path,
     # mt19937(0)) with spins, log psi, accept counts and the MC gradient with the E_k term.
     rbm_case("c2_rbm_mc", 64, 128, 0.05, 102, tfim_square(8, 1.0, 3.0), identity_op(), True, 1.0,
              mc={"mc_samples": 40, "mc_sweeps": 1, "mc_therm": 5, "mc_gradient": 1}, normalize=False)
     # PsiDeep 8 -> [16, 8, 4] with connectivity [4, 2, 4] (the reference's own test net shape)
     deep_case("deep8_sparse", "deep", 8, [16, 8, 4], [4, 2, 4], 0.1, 103, tfim_chain(8), identity_op(), True, 1.0,
-              mc={"mc_samples": 60, "mc_sweeps": 1, "mc_therm": 3, "mc_gradient": 1})
+              mc={"mc_samples": 60, "mc_sweeps": 1, "mc_therm": 3, "mc_gradient": 1}, ev_extra=True)
     # dense 10 -> 20 -> 10 -> 5 (the layer pattern of the 100->200->100->50 net, scaled down)
     deep_case("deep10_dense", "deep", 10, [20, 10, 5], [10, 20, 10], 0.1, 104, tfim_chain(10), identity_op(),
-              True, 1.0)
+              True, 1.0, ev_extra=True)
     # get_S_matrix of a small RBM over ExactSummation (the reference's only instantiation)
     # and the KullbackLeibler value and gradient to the perturbed copy (nu = 0.5)
     rbm_case("rbm6_smatrix", 6, 12, 0.3, 13, tfim_chain(6, 1.0, 1.0), identity_op(), True, 0.5, smatrix=True,
