@@ -94,6 +94,32 @@ class Spins:
     def hamming_distance(self, other):
         return bin(self.configuration ^ other.configuration).count("1")
 
+    # lattice shifts of an nrows x ncols configuration, row-major (include/Spins.h:287-332).
+    # The reference forms its column masks in 32-bit arithmetic, which is exact up to 32
+    # spins; here the masks are exact for every size.
+    def shift_vertical(self, shift, nrows, ncols):
+        c, n = self.configuration, nrows * ncols
+        return Spins((c << (shift * ncols)) | (c >> ((nrows - shift) * ncols)), n)
+
+    def _columns(self, first, count, nrows, ncols):
+        row = ((1 << count) - 1) << first
+        mask = 0
+        for i in range(nrows):
+            mask |= row << (i * ncols)
+        return Spins(self.configuration & mask, nrows * ncols)
+
+    def shift_horizontal(self, shift, nrows, ncols):
+        # select_left_columns(nrows - shift) | select_right_columns(shift) moved up a row
+        # (Spins.h:314-325; the reference counts the left columns with nrows)
+        tmp = self.rotate_left(shift, nrows * ncols)
+        left = tmp._columns(ncols - (nrows - shift), nrows - shift, nrows, ncols)
+        right = tmp._columns(0, shift, nrows, ncols).shift_vertical(nrows - 1, nrows, ncols)
+        return Spins(left.configuration | right.configuration, nrows * ncols)
+
+    def shift_2d(self, shift_i, shift_j, nrows, ncols):
+        """Spins.h:327-332: the configuration moved by shift_i rows and shift_j columns."""
+        return self.shift_vertical(shift_i, nrows, ncols).shift_horizontal(shift_j, nrows, ncols)
+
     def words(self):
         return spins_to_words(self.configuration, self.N)
 
@@ -287,6 +313,11 @@ class PsiDeep(_PsiBase):
     free_quantum_axis, gpu).  PsiPair subclasses it with two real nets."""
 
     _pair = 0
+    # lattice extents for a translation-invariant net (PsiDeep.hpp:80-81, main.cpp:112-113);
+    # the reference stores them and its only use of them is commented out, so they are kept
+    # here as plain attributes
+    N_i = 0
+    N_j = 0
 
     def __init__(self, alpha, beta, b, connections, W, final_weights, prefactor=1.0, free_quantum_axis=False,
                  gpu=True):

@@ -56,3 +56,22 @@ def test_operator_tables():
     assert np.allclose(coef[:5], -1.0) and np.allclose(coef[5:], -0.5)
     c2, t2, i2 = operators.tfim_square(4)
     assert len(c2) == 3 * 16
+
+
+def test_spins_lattice_shifts():
+    """Spins.shift_2d (include/Spins.h:287-332) on an L x L row-major lattice is the cyclic
+    roll by (shift_i, shift_j); shift_vertical alone rolls whole rows."""
+    from rbmongpu_gb300 import Spins
+    rng = np.random.default_rng(2)
+    for L in (3, 4, 5, 8):
+        N = L * L
+        for _ in range(30):
+            c = int(rng.integers(0, 2 ** min(N, 62)))
+            si, sj = int(rng.integers(0, L)), int(rng.integers(0, L))
+            bits = np.array([(c >> i) & 1 for i in range(N)]).reshape(L, L)
+
+            def word(a):
+                return sum(int(b) << i for i, b in enumerate(a.reshape(-1)))
+
+            assert Spins(c, N).shift_2d(si, sj, L, L).configuration == word(np.roll(bits, (si, sj), axis=(0, 1)))
+            assert Spins(c, N).shift_vertical(si, L, L).configuration == word(np.roll(bits, si, axis=0))
