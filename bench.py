@@ -425,8 +425,9 @@ def run_serving(args):
         "dtype": "f32 (complex64)", "data": "synthetic (seeded PCG64 parameters)",
         "config": {"workload": "serving_64_rbm_n16_144_alpha124_tfim", "instances": len(inst), "walkers": walkers,
                    "step": "1 sweep + E_loc of every walker + O_k sums (one CUDA-graph replay)",
-                   "shape": {"warps_per_block": w_shape, "tile_rows": rows, "blocks": blocks},
-                   "autotune_ms": {f"{a}x{b}": t for (a, b), t in tune.items()},
+                   "shape": {"warps_per_block": w_shape, "tile_rows": rows, "blocks": blocks,
+                             "register_cap": batch.register_cap},
+                   "autotune_ms": {f"r{c}_{a}x{b}": t for (c, a, b), t in tune.items()},
                    "l2": "flushed between timed steps"},
         "eloc_per_s": walkers / sec,
         "e2e": {"value": walkers * e2e_K / e2e_s, "unit": "walker-sweeps/s", "h2d_bytes_per_step": 0,

@@ -345,8 +345,13 @@ RBMG_API int rbmg_batch_run(rbmg_batch* batch, int therm, int sweeps);
 /* launch shape: warps per block in {2, 4, 8}, reduction tile rows in {8, 16} */
 RBMG_API int rbmg_batch_set_shape(rbmg_batch* batch, int warps_per_block, int rows);
 RBMG_API int rbmg_batch_get_shape(const rbmg_batch* batch, int* warps_per_block, int* rows, int* blocks);
-/* times the 6 shapes on `reps` replays of `sweeps` sweeps each and keeps the fastest;
- * ms [6] (nullable) gets their mean replay times, order (2,8) (2,16) (4,8) (4,16) (8,8) (8,16) */
+/* register cap per thread of the persistent kernel: 255 (none), 128 or 96 (the largest
+ * walker task sets the kernel's register count; a cap trades spills for resident warps) */
+RBMG_API int rbmg_batch_set_register_cap(rbmg_batch* batch, int regs);
+RBMG_API int rbmg_batch_get_register_cap(const rbmg_batch* batch, int* regs);
+/* times the 18 shapes (register cap x warps per block x tile rows) on `reps` replays of
+ * `sweeps` sweeps each and keeps the fastest; ms [18] (nullable) gets their mean replay
+ * times, caps 255, 128, 96 in turn, each in the order (2,8) (2,16) (4,8) (4,16) (8,8) (8,16) */
 RBMG_API int rbmg_batch_autotune(rbmg_batch* batch, int sweeps, int reps, double* ms);
 /* last replay's results of instance i: energy [2], grad [2P] (nullable), eloc [2 walkers] (nullable) */
 RBMG_API int rbmg_batch_result(const rbmg_batch* batch, int instance, double* energy, double* grad, double* eloc);

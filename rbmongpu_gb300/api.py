@@ -922,12 +922,22 @@ class Batch:
         call("rbmg_batch_get_shape", self._h, C.byref(w), C.byref(r), C.byref(b))
         return w.value, r.value, b.value
 
+    @property
+    def register_cap(self):
+        r = C.c_int()
+        call("rbmg_batch_get_register_cap", self._h, C.byref(r))
+        return r.value
+
+    @register_cap.setter
+    def register_cap(self, regs):
+        call("rbmg_batch_set_register_cap", self._h, int(regs))
+
     def autotune(self, sweeps=1, reps=3):
         """Times the launch shapes on the batch itself, keeps the fastest; returns
-        {(warps_per_block, rows): ms per replay}."""
-        ms = np.zeros(6)
+        {(register_cap, warps_per_block, rows): ms per replay}."""
+        ms = np.zeros(18)
         call("rbmg_batch_autotune", self._h, int(sweeps), int(reps), _p(ms))
-        shapes = [(2, 8), (2, 16), (4, 8), (4, 16), (8, 8), (8, 16)]
+        shapes = [(c, w, r) for c in (255, 128, 96) for w in (2, 4, 8) for r in (8, 16)]
         return dict(zip(shapes, ms.tolist()))
 
     def result(self, i, want_eloc=False):

@@ -336,8 +336,10 @@ __device__ __noinline__ void reduce_task(const SLaunch& L, const SInst& I, int r
     }
 }
 
-template <int R>
-__global__ void serve_kernel(SLaunch L) {
+// REGS caps the registers per thread (the largest walker task sets the kernel's count, so
+// a cap trades its spills against more resident warps for every task); the autotuner picks
+template <int R, int REGS>
+__global__ void __maxnreg__(REGS) serve_kernel(SLaunch L) {
     const int lane = threadIdx.x & 31;
     for (;;) {
         int t = 0;
@@ -378,12 +380,13 @@ struct rbmg_batch {
     int ntasks_walk = 0, ntasks = 0;
     int rows = 16;              // reduction tile height
     int warps_per_block = 4;
+    int regs = 255;             // register cap per thread: 255, 128 or 96
     int blocks = 0;
     bool first = true;
     int therm = 0, sweeps = 1;  // graph parameters
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    int graph_rows = 0, graph_wpb = 0, graph_first = -1, graph_therm = -1, graph_sweeps = -1;
+    int graph_rows = 0, graph_wpb = 0, graph_regs = 0, graph_first = -1, graph_therm = -1, graph_sweeps = -1;
     double tuned_ms = 0.0;
     ~rbmg_batch() {
         if (exec) cudaGraphExecDestroy(exec);
@@ -416,6 +419,20 @@ int batch_tasks(rbmg_batch* b) {
 
 size_t serve_smem(int warps_per_block) { return sizeof(float2) * kSK * 32 * warps_per_block; }
 
+// calls f with the kernel instantiation of (reduction rows, register cap)
+template <class F>
+void with_serve_kernel(int rows, int regs, F f) {
+    if (rows == 8) {
+        if (regs == 128) f(serve_kernel<8, 128>);
+        else if (regs == 96) f(serve_kernel<8, 96>);
+        else f(serve_kernel<8, 255>);
+    } else {
+        if (regs == 128) f(serve_kernel<16, 128>);
+        else if (regs == 96) f(serve_kernel<16, 96>);
+        else f(serve_kernel<16, 255>);
+    }
+}
+
 cudaError_t launch_serve(rbmg_batch* b, cudaStream_t st) {
     SLaunch L{};
     L.inst = b->d_inst.as<SInst>();
@@ -429,14 +446,13 @@ cudaError_t launch_serve(rbmg_batch* b, cudaStream_t st) {
     L.accepts = b->d_accepts.as<unsigned long long>();
     const int threads = 32 * b->warps_per_block;
     const size_t sm = serve_smem(b->warps_per_block);
-    if (b->rows == 8) serve_kernel<8><<<b->blocks, threads, sm, st>>>(L);
-    else serve_kernel<16><<<b->blocks, threads, sm, st>>>(L);
+    with_serve_kernel(b->rows, b->regs, [&](auto kern) { kern<<<b->blocks, threads, sm, st>>>(L); });
     return cudaGetLastError();
 }
 
 // (re)captures the replay: counter resets and the persistent launch
 int batch_capture(rbmg_batch* b) {
-    if (b->exec && b->graph_rows == b->rows && b->graph_wpb == b->warps_per_block &&
+    if (b->exec && b->graph_rows == b->rows && b->graph_wpb == b->warps_per_block && b->graph_regs == b->regs &&
         b->graph_first == static_cast<int>(b->first) && b->graph_therm == b->therm && b->graph_sweeps == b->sweeps)
         return RBMG_OK;
     if (b->exec) cudaGraphExecDestroy(b->exec);
@@ -448,8 +464,10 @@ int batch_capture(rbmg_batch* b) {
     RBMG_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const int threads = 32 * b->warps_per_block;
     const size_t sm = serve_smem(b->warps_per_block);
-    if (b->rows == 8) RBMG_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, serve_kernel<8>, threads, sm));
-    else RBMG_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, serve_kernel<16>, threads, sm));
+    cudaError_t oe = cudaSuccess;
+    with_serve_kernel(b->rows, b->regs,
+                      [&](auto kern) { oe = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, sm); });
+    RBMG_CK(oe);
     b->blocks = std::max(1, sms * std::max(1, per_sm));
     cudaStream_t st = stream();
     RBMG_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
@@ -466,6 +484,7 @@ int batch_capture(rbmg_batch* b) {
     RBMG_CK(cudaGraphInstantiate(&b->exec, b->graph, 0));
     b->graph_rows = b->rows;
     b->graph_wpb = b->warps_per_block;
+    b->graph_regs = b->regs;
     b->graph_first = static_cast<int>(b->first);
     b->graph_therm = b->therm;
     b->graph_sweeps = b->sweeps;
@@ -585,6 +604,19 @@ extern "C" int rbmg_batch_set_shape(rbmg_batch* b, int warps_per_block, int rows
     return RBMG_OK;
 }
 
+extern "C" int rbmg_batch_set_register_cap(rbmg_batch* b, int regs) {
+    if (!b || (regs != 255 && regs != 128 && regs != 96))
+        return fail(RBMG_EINVAL, "batch: register cap in {255, 128, 96}");
+    b->regs = regs;
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_batch_get_register_cap(const rbmg_batch* b, int* regs) {
+    if (!b || !regs) return fail(RBMG_EINVAL, "batch: null");
+    *regs = b->regs;
+    return RBMG_OK;
+}
+
 extern "C" int rbmg_batch_get_shape(const rbmg_batch* b, int* warps_per_block, int* rows, int* blocks) {
     if (!b) return fail(RBMG_EINVAL, "batch: null");
     if (warps_per_block) *warps_per_block = b->warps_per_block;
@@ -601,20 +633,22 @@ extern "C" int rbmg_batch_run(rbmg_batch* b, int therm, int sweeps) {
 }
 
 // Times every candidate shape on `reps` replays of `sweeps` sweeps (the chains advance),
-// keeps the fastest; ms_out [6] receives the candidates' mean milliseconds per replay in
-// the order (2,8) (2,16) (4,8) (4,16) (8,8) (8,16).
+// keeps the fastest; ms_out [18] receives the candidates' mean milliseconds per replay,
+// register caps 255, 128, 96 in turn, each in the order (2,8) (2,16) (4,8) (4,16) (8,8) (8,16).
 extern "C" int rbmg_batch_autotune(rbmg_batch* b, int sweeps, int reps, double* ms_out) {
     if (!b || sweeps < 0 || reps <= 0) return fail(RBMG_EINVAL, "batch autotune: bad arguments");
     if (b->first) {   // start the chains outside the timing
         const int r = rbmg_batch_run(b, 0, 0);
         if (r != RBMG_OK) return r;
     }
-    const int wpbs[3] = {2, 4, 8}, rowss[2] = {8, 16};
+    const int wpbs[3] = {2, 4, 8}, rowss[2] = {8, 16}, capss[3] = {255, 128, 96};
     double best = 1e300;
-    int bw = 4, brows = 16, c = 0;
+    int bw = 4, brows = 16, bregs = 255, c = 0;
+    for (int regs : capss)
     for (int wpb : wpbs)
         for (int rows : rowss) {
             int r = rbmg_batch_set_shape(b, wpb, rows);
+            if (r == RBMG_OK) r = rbmg_batch_set_register_cap(b, regs);
             if (r != RBMG_OK) return r;
             b->therm = 0;
             b->sweeps = sweeps;
@@ -641,10 +675,12 @@ extern "C" int rbmg_batch_autotune(rbmg_batch* b, int sweeps, int reps, double* 
                 best = per;
                 bw = wpb;
                 brows = rows;
+                bregs = regs;
             }
         }
     b->tuned_ms = best;
-    return rbmg_batch_set_shape(b, bw, brows);
+    const int r = rbmg_batch_set_shape(b, bw, brows);
+    return r != RBMG_OK ? r : rbmg_batch_set_register_cap(b, bregs);
 }
 
 // results of the last replay for instance i: <E_loc> over its walkers, the O_k gradient

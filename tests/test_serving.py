@@ -22,7 +22,10 @@ def rbm(N, alpha, seed, sigma=0.05):
     return rg.Psi(np.zeros(N), np.zeros(N), b, W, 1.0, False, True)
 
 
-def test_batch_chains_match_single_network_chains():
+@pytest.mark.parametrize("regs", [255, 128, 96])
+def test_batch_chains_match_single_network_chains(regs):
+    """Under every register cap of the persistent kernel the chains equal single-network
+    chains (energies and accept counts)."""
     import torch
     import rbmongpu_gb300 as rg
     specs = [(16, 1, 0.7, 64), (24, 2, 1.3, 96), (40, 4, 1.9, 128), (72, 2, 1.0, 32), (136, 1, 0.5, 48)]
@@ -33,6 +36,7 @@ def test_batch_chains_match_single_network_chains():
         nets.append((psi, op, B, 900 + q))
         inst.append((psi, op, B, 900 + q))
     batch = rg.Batch(inst)
+    batch.register_cap = regs
     therm, sweeps = 7, 3
     batch.run(therm, sweeps)
     total_acc = 0
@@ -88,9 +92,9 @@ def test_autotune_keeps_the_fastest_shape():
         inst.append((rbm(N, a, 105_000 + q), op, 256 * N // 16 // 4, q))
     batch = rg.Batch(inst)
     times = batch.autotune(sweeps=1, reps=2)
-    assert len(times) == 6 and all(t > 0 for t in times.values())
+    assert len(times) == 18 and all(t > 0 for t in times.values())
     w, r, blocks = batch.shape
-    assert times[(w, r)] == min(times.values()) and blocks > 0
+    assert times[(batch.register_cap, w, r)] == min(times.values()) and blocks > 0
     batch.run(0, 1)
     E, g, _ = batch.result(0)
     assert np.isfinite(E) and np.all(np.isfinite(g))
