@@ -199,12 +199,13 @@ RBMG_API int rbmg_local_energies(const rbmg_psi* psi, const rbmg_operator* op, i
  * parts, FP32 accumulation); the reference evaluates them one at a time
  * (kernel::Psi::angle, include/quantum_state/Psi.hpp:43-53).  Complex RBM. */
 RBMG_API int rbmg_psi_angles(const rbmg_psi* psi, int count, const uint64_t* spins, double* out);
-/* Extension (PsiDeep): gradient of the local energy by a hand-written adjoint (reverse
- * mode) kernel that recomputes every forward pass, in PyTorch's convention for a real
- * loss L: grad_k = dL/dRe(theta_k) + i dL/dIm(theta_k).  score = 0: L = Re <E_loc> over
- * the ensemble's samples held fixed; score = 1: L = <H>, adding the sampling term, which
+/* Extension: gradient of the local energy in PyTorch's convention for a real loss L:
+ * grad_k = dL/dRe(theta_k) + i dL/dIm(theta_k).  score = 0: L = Re <E_loc> over the
+ * ensemble's samples held fixed; score = 1: L = <H>, adding the sampling term.  PsiDeep: a
+ * hand-written adjoint (reverse mode) kernel that recomputes every forward pass; score = 1
  * equals rbmg_ev_gradient except at the final weights (include/quantum_state/PsiDeep.hpp:285-292
- * scales their O_k by log psi; here d log psi / d w_final = activation). */
+ * scales their O_k by log psi; here d log psi / d w_final = activation).  Psi: formed from
+ * the estimator sums, conj<E_k - E O_k> (+ 2 <(Re E - <Re E>) O_k*> for score = 1). */
 RBMG_API int rbmg_ev_eloc_gradient(const rbmg_psi* psi, const rbmg_operator* op, rbmg_ensemble* ens, int score,
                                    double* grad /* [2P] */, double* value /* [2] */);
 

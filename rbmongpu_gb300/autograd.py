@@ -1,4 +1,5 @@
-"""PyTorch autograd wrapper of the adjoint local-energy gradient (PsiDeep).
+"""PyTorch autograd wrapper of the local-energy gradient (PsiDeep: the adjoint kernels;
+Psi: the derivative formed from the estimator sums).
 
 ``energy(params, psi, operator_, ensemble)`` returns the real scalar <E_loc> of the
 network whose parameters are the complex tensor ``params`` (the reference's layout,

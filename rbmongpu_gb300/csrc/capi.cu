@@ -56,7 +56,7 @@ struct Workspace {
     DevBuf sample_spins, eloc, logpsi, logpsi_p, T, U, X, Tp, weights, coef1, coef2, coef3, omega, pr, nn;
     DevBuf partial, block_scratch, sums, acc_O, acc_EO, acc_Ek, acc_wO, acc_pO, block_max, zsum;
     DevBuf smat, smean, okrows, sshift, splanes, serror, sout;
-    DevBuf acc_B, eabs2, lsums, rw, rwc;
+    DevBuf acc_B, eabs2, lsums, rw, rwc, acc_C2, acc_C3;
 };
 
 static Workspace& ws() {
@@ -1112,9 +1112,11 @@ extern "C" int rbmg_ev_fluctuation(const rbmg_psi* psi, const rbmg_operator* op,
 // acc_Ek = sum w (E_k - E0 O) over the O_k entries k >= 2N, sums[0] = sum w E; E0 (the
 // first chunk's mean local energy) and the ensemble's normalisation factor come back.
 // fluct: also B = sum w conj(E - E0) (E_k - E0 O_k) into acc_B and sum w |E|^2 into sums[1]
-// (the further sums of ExpectationValue::fluctuation_gradient)
+// (the further sums of ExpectationValue::fluctuation_gradient).  adjoint (complex RBM): also
+// C2 = sum w (E - E0) O_k into acc_C2 and C3 = sum w (Re E - Re E0) conj(O_k) into acc_C3
+// (the derivative of <E_loc>, rbmg_ev_eloc_gradient).
 static int ev_gradient_sums(const rbmg_psi* psi, const rbmg_operator* op, rbmg_ensemble* ens, cplx* E0_out,
-                            double* norm_out, bool fluct = false) {
+                            double* norm_out, bool fluct = false, bool adjoint = false) {
     int r = check_pair(psi, op, ens);
     if (r != RBMG_OK) return r;
     const int N = psi->N, P = psi->num_params();
@@ -1130,6 +1132,13 @@ static int ev_gradient_sums(const rbmg_psi* psi, const rbmg_operator* op, rbmg_e
     if (fluct) {
         RBMG_CK(W.acc_B.ensure(sizeof(double2) * ok_len));
         RBMG_CK(cudaMemsetAsync(W.acc_B.p, 0, sizeof(double2) * ok_len, stream()));
+    }
+    if (adjoint) {
+        if (psi->kind != 0) return fail(RBMG_EUNSUPPORTED, "adjoint sums: complex RBM only");
+        RBMG_CK(W.acc_C2.ensure(sizeof(double2) * ok_len));
+        RBMG_CK(W.acc_C3.ensure(sizeof(double2) * ok_len));
+        RBMG_CK(cudaMemsetAsync(W.acc_C2.p, 0, sizeof(double2) * ok_len, stream()));
+        RBMG_CK(cudaMemsetAsync(W.acc_C3.p, 0, sizeof(double2) * ok_len, stream()));
     }
     RBMG_CK(W.sums.ensure(sizeof(double2) * kMaxSeries));
     RBMG_CK(W.block_scratch.ensure(sizeof(double2) * kSumBlocks * kMaxSeries));
@@ -1212,6 +1221,17 @@ static int ev_gradient_sums(const rbmg_psi* psi, const rbmg_operator* op, rbmg_e
                                         c.weights, W.X.as<float2>(), op->num_offdiag, op->d_site_ptr.as<int>(),
                                         op->d_site_slots.as<int>(), W.acc_Ek.as<double2>(), part, kSplits,
                                         stream()));
+            if (adjoint) {
+                RBMG_CK(launch_outer_reduce(c.count, N, nw, psi->M, c.spins, c.enum_base, c.enumerate,
+                                            W.coef2.as<double2>(), W.T.as<float2>(), psi->Mpad, 0,
+                                            W.acc_C2.as<double2>(), part, kSplits, stream()));
+                RBMG_CK(W.coef3.ensure(sizeof(double2) * c.count));
+                RBMG_CK(launch_coef_real(c.count, c.weights, W.eloc.as<double2>(), E0.real(), W.coef3.as<double2>(),
+                                         stream()));
+                RBMG_CK(launch_outer_reduce(c.count, N, nw, psi->M, c.spins, c.enum_base, c.enumerate,
+                                            W.coef3.as<double2>(), W.T.as<float2>(), psi->Mpad, 1,
+                                            W.acc_C3.as<double2>(), part, kSplits, stream()));
+            }
             if (fluct) {
                 RBMG_CK(W.coef3.ensure(sizeof(double2) * c.count));
                 RBMG_CK(launch_coef_conj(c.count, c.weights, W.eloc.as<double2>(), make_double2(E0.real(), E0.imag()),
@@ -1414,12 +1434,54 @@ int deep_adjoint_chunk(const rbmg_psi* psi, const rbmg_operator* op, const Chunk
 //              grad equals the reference's estimator (ExpectationValue.cu:243-253) except
 //              at the final weights, whose derivative is the last layer's activation here
 //              and activation * log psi there (PsiDeep.hpp:285-292).
+// The complex RBM's derivative of <E_loc> in PyTorch's convention (dL/dRe + i dL/dIm of
+// L = Re <E_loc>).  E_loc(s) is holomorphic in the parameters with
+// dE_loc(s)/dtheta_k = E_k(s) - E_loc(s) O_k(s) (E_k the estimator vector of
+// Operator.hpp:145-179), so the fixed-sample part is conj(<E_k - E O_k>) = conj(C1 - C2)
+// (C1 = <E_k - E0 O_k>, C2 = <(E - E0) O_k>); the sampling term (score) adds
+// 2 <(Re E - <Re E>) O_k*> = 2 (C3 - (<Re E> - Re E0) <O_k>*).
+static int rbm_eloc_gradient(const rbmg_psi* psi, const rbmg_operator* op, rbmg_ensemble* ens, int score,
+                             double* grad, double* value) {
+    cplx E0;
+    double f = 0.0;
+    int r = ev_gradient_sums(psi, op, ens, &E0, &f, false, true);
+    if (r != RBMG_OK) return r;
+    const int N = psi->N;
+    const size_t ok_len = static_cast<size_t>(psi->num_params() - 2 * N);
+    Workspace& W = ws();
+    std::vector<double2> O(ok_len), C1(ok_len), C2(ok_len), C3(ok_len);
+    double2 Es;
+    RBMG_CK(cudaMemcpyAsync(O.data(), W.acc_O.p, sizeof(double2) * ok_len, cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaMemcpyAsync(C1.data(), W.acc_Ek.p, sizeof(double2) * ok_len, cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaMemcpyAsync(C2.data(), W.acc_C2.p, sizeof(double2) * ok_len, cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaMemcpyAsync(C3.data(), W.acc_C3.p, sizeof(double2) * ok_len, cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaMemcpyAsync(&Es, W.sums.p, sizeof(double2), cudaMemcpyDeviceToHost, stream()));
+    RBMG_CK(cudaStreamSynchronize(stream()));
+    const cplx E = cplx(Es.x, Es.y) * f;
+    const double dre = E.real() - E0.real();
+    cplx* g = reinterpret_cast<cplx*>(grad);
+    for (int k = 0; k < 2 * N; k++) g[k] = 0.0;
+    for (size_t k = 0; k < ok_len; k++) {
+        const cplx c1 = cplx(C1[k].x, C1[k].y) * f, c2 = cplx(C2[k].x, C2[k].y) * f;
+        cplx v = std::conj(c1 - c2);
+        if (score) {
+            const cplx o = cplx(O[k].x, O[k].y) * f, c3 = cplx(C3[k].x, C3[k].y) * f;
+            v += 2.0 * (c3 - dre * std::conj(o));
+        }
+        g[2 * N + k] = v;
+    }
+    value[0] = E.real();
+    value[1] = E.imag();
+    return RBMG_OK;
+}
+
 extern "C" int rbmg_ev_eloc_gradient(const rbmg_psi* psi, const rbmg_operator* op, rbmg_ensemble* ens, int score,
                                      double* grad, double* value) {
     if (!op || !grad || !value) return fail(RBMG_EINVAL, "adjoint: null");
     int r = check_pair(psi, op, ens);
     if (r != RBMG_OK) return r;
-    if (psi->kind != 1) return fail(RBMG_EUNSUPPORTED, "adjoint: PsiDeep only");
+    if (psi->kind == 0) return rbm_eloc_gradient(psi, op, ens, score, grad, value);
+    if (psi->kind != 1) return fail(RBMG_EUNSUPPORTED, "adjoint: PsiDeep and Psi only");
     if (psi->translational_invariance) return fail(RBMG_EUNSUPPORTED, "adjoint: translational averaging not provided");
     const int N = psi->N, P = psi->num_params();
     const int L = static_cast<int>(psi->layers.size());

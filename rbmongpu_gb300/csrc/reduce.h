@@ -37,6 +37,9 @@ cudaError_t launch_abs2(int count, const double2* v, double2* out, cudaStream_t 
 // c[s] = w[s] conj(v[s] - shift)
 cudaError_t launch_coef_conj(int count, const double* w, const double2* v, double2 shift, double2* c,
                              cudaStream_t st);
+// c[s] = (w[s] (Re v[s] - shift), 0)
+cudaError_t launch_coef_real(int count, const double* w, const double2* v, double shift, double2* c,
+                             cudaStream_t st);
 // rw[s] = w[s] |psi(s) / psi'(s)|^2 from log psi and log psi', rwc[s] = (rw[s], 0)
 cudaError_t launch_ratio_weights(int count, const double* w, const double2* lp, const double2* lpp, double* rw,
                                  double2* rwc, cudaStream_t st);

@@ -233,6 +233,13 @@ __global__ void coef_conj_kernel(int count, const double* __restrict__ w, const 
     }
 }
 
+// c[s] = (w[s] (Re v[s] - shift), 0)
+__global__ void coef_real_kernel(int count, const double* __restrict__ w, const double2* __restrict__ v, double shift,
+                                 double2* c) {
+    for (long s = blockIdx.x * 256L + threadIdx.x; s < count; s += static_cast<long>(gridDim.x) * 256)
+        c[s] = make_double2((w ? w[s] : 1.0) * (v[s].x - shift), 0.0);
+}
+
 // rw[s] = w[s] exp(2 (Re lp[s] - Re lpp[s])) (ExpectationValue.cu:391-395), rwc[s] = (rw[s], 0)
 __global__ void ratio_weight_kernel(int count, const double* __restrict__ w, const double2* __restrict__ lp,
                                     const double2* __restrict__ lpp, double* rw, double2* rwc) {
@@ -344,6 +351,12 @@ cudaError_t launch_coef(int count, const double* w, const double2* v, double sca
 cudaError_t launch_coef_conj(int count, const double* w, const double2* v, double2 shift, double2* c,
                              cudaStream_t st) {
     coef_conj_kernel<<<grid_for(count), 256, 0, st>>>(count, w, v, shift, c);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_coef_real(int count, const double* w, const double2* v, double shift, double2* c,
+                             cudaStream_t st) {
+    coef_real_kernel<<<grid_for(count), 256, 0, st>>>(count, w, v, shift, c);
     return cudaGetLastError();
 }
 

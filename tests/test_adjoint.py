@@ -1,7 +1,7 @@
-"""Adjoint (reverse-mode) gradient of the local energy for PsiDeep behind a
-torch.autograd.Function: against FP64 central finite differences (step 1e-3) on 32
-seeded parameters, against the reference's O_k estimator (rbmg_ev_gradient) on the same
-samples, and through torch's backward.
+"""Adjoint (reverse-mode) gradient of the local energy for PsiDeep, and the complex RBM's
+derivative of <E_loc> from its estimator sums, behind a torch.autograd.Function: against
+FP64 central finite differences on 32 seeded parameters, against the reference's O_k
+estimator (rbmg_ev_gradient), and through torch's backward.
 
 Tolerances: the adjoint runs its forward and reverse passes in FP32 (complex64) with FP64
 sums; gradients agree with the FP64 references within 1e-4 of the gradient's largest
@@ -174,3 +174,112 @@ def test_autograd_function_follows_torchs_complex_convention():
     w = torch.tensor([1 + 2j, 0.5 - 1j], dtype=torch.complex128, requires_grad=True)
     (w * w).real.sum().backward()
     assert torch.equal(z.grad, w.grad)
+
+
+# ----------------------------------------------------------------------------- complex RBM
+# The RBM path computes local energies in FP32, whose round-off over a step of 1e-5 would
+# swamp a finite difference; its derivative is checked against FP64 central differences
+# of the CPU restatement (oracle/pyoracle.py) at the same parameters and samples.
+def rbm_net(N, M, seed, sigma):
+    import rbmongpu_gb300 as rg
+    rng = np.random.Generator(np.random.PCG64(seed))
+    b = sigma * (rng.normal(size=M) + 1j * rng.normal(size=M))
+    W = sigma * (rng.normal(size=(N, M)) + 1j * rng.normal(size=(N, M)))
+    return rg.Psi(np.zeros(N), np.zeros(N), b, W, 1.0, False, True), b, W
+
+
+def oracle_rbm(p, N, M):
+    from oracle import pyoracle as po
+    return po.RBM(p[2 * N:2 * N + M], p[2 * N + M:].reshape(N, M), 1.0)
+
+
+def fd_oracle(loss, p0, grad, idx, h=1e-5, rtol=RTOL):
+    """fd_check on a loss of the parameter vector (FP64, no device)."""
+    vals = {}
+    for k in idx:
+        d = []
+        for hh in (h, 2 * h):
+            v = []
+            for step in (hh, 1j * hh):
+                p = p0.copy()
+                p[k] += step
+                lp = loss(p)
+                p[k] -= 2 * step
+                v.append((lp - loss(p)) / (2 * hh))
+            d.append(v[0] + 1j * v[1])
+        vals[k] = d
+    scale = np.abs(grad).max()
+    good = [k for k in idx if abs(vals[k][0] - vals[k][1]) <= 0.5 * rtol * scale]
+    return np.array(good), np.array([vals[k][0] for k in good])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("N,M", [(12, 24), (40, 80)])
+def test_rbm_fixed_sample_derivative_matches_fp64_finite_differences(N, M):
+    """Psi: score=False is the derivative of Re <E_loc> over the samples held fixed."""
+    import rbmongpu_gb300 as rg
+    from oracle import pyoracle as po
+    psi, b, W = rbm_net(N, M, 41, 0.2)
+    H_t = rg.operators.tfim_chain(N, 1.0, 1.0)
+    H = rg.Operator(*H_t)
+    mk = lambda: rg.MonteCarloLoop(64, 1, 5, 32, seed=13)   # noqa: E731
+    sp, _, _ = mk().samples(psi)
+    g, E = rg.ExpectationValue().eloc_gradient(psi, H, mk(), score=False)
+    el = rg.local_energies(psi, H, sp)
+    assert abs(E - el.mean()) <= 1e-5 * np.abs(el).mean()
+    op = po.Op(*H_t)
+    words = [np.asarray([s], np.uint64) for s in sp]
+
+    def loss(p):
+        o = oracle_rbm(p, N, M)
+        return np.mean([po.local_energy(o, op, s).real for s in words])
+
+    good, fd = fd_oracle(loss, psi.params, g, param_indices(psi, 32, 7))
+    assert len(good) >= 24, len(good)
+    assert rel_err(g[good], fd) < RTOL, (g[good][:4], fd[:4])
+    assert np.all(g[:2 * N] == 0)
+
+
+@pytest.mark.gpu
+def test_rbm_exact_summation_gradient_matches_finite_differences_and_the_reference_estimator():
+    """Psi, normalised, ExactSummation: score=True is the gradient of <H> and equals the
+    reference's O_k estimator (ExpectationValue.cu:243-253) for the hermitian TFIM."""
+    import rbmongpu_gb300 as rg
+    from oracle import pyoracle as po
+    N, M = 8, 16
+    psi, b, W = rbm_net(N, M, 43, 0.3)
+    H_t = rg.operators.tfim_chain(N, 1.0, 1.0)
+    H = rg.Operator(*H_t)
+    es = rg.ExactSummation(N)
+    op = po.Op(*H_t)
+
+    def energy(p):
+        o = oracle_rbm(p, N, M)
+        sig, E = po.exact_fluctuation(o, op)
+        return E.real / po.exact_norm(o) ** 2
+
+    p0 = psi.params
+    psi.prefactor = 1.0 / psi.norm(es)
+    g, E = rg.ExpectationValue().eloc_gradient(psi, H, es, score=True)
+    assert abs(E.real - energy(p0)) <= 1e-5 * abs(E)
+    gr, _ = rg.ExpectationValue().gradient(psi, H, es)
+    assert rel_err(g, gr) < RTOL
+    good, fd = fd_oracle(energy, p0, g, param_indices(psi, 32, 9))
+    assert len(good) >= 24, len(good)
+    assert rel_err(g[good], fd) < RTOL
+
+
+@pytest.mark.gpu
+def test_rbm_torch_backward():
+    import torch
+    import rbmongpu_gb300 as rg
+    from rbmongpu_gb300.autograd import energy
+    N, M = 16, 32
+    psi, _, _ = rbm_net(N, M, 47, 0.1)
+    H = rg.Operator(*rg.operators.tfim_chain(N, 1.0, 1.0))
+    params = torch.tensor(psi.params, requires_grad=True)
+    E = energy(params, psi, H, rg.MonteCarloLoop(256, 1, 5, 128, seed=8))
+    E.backward()
+    g, E2 = rg.ExpectationValue().eloc_gradient(psi, H, rg.MonteCarloLoop(256, 1, 5, 128, seed=8), score=True)
+    assert E.item() == E2.real
+    np.testing.assert_array_equal(params.grad.numpy(), g)
