@@ -346,6 +346,11 @@ RBMG_API int rbmg_batch_run(rbmg_batch* batch, int therm, int sweeps);
 /* launch shape: warps per block in {2, 4, 8}, reduction tile rows in {8, 16} */
 RBMG_API int rbmg_batch_set_shape(rbmg_batch* batch, int warps_per_block, int rows);
 RBMG_API int rbmg_batch_get_shape(const rbmg_batch* batch, int* warps_per_block, int* rows, int* blocks);
+/* wall-clock limit of a reduction task's wait for its instance's walkers (default 20 s),
+ * and walkers to wait for beyond each instance's (default 0): with extra_walkers > 0 the
+ * wait runs out and the next replay returns RBMG_ETIMEOUT, leaving the device usable (the
+ * test of the bounded wait). */
+RBMG_API int rbmg_batch_set_wait(rbmg_batch* batch, double seconds, uint32_t extra_walkers);
 /* register cap per thread of the persistent kernel: 255 (none), 128 or 96 (the largest
  * walker task sets the kernel's register count; a cap trades spills for resident warps) */
 RBMG_API int rbmg_batch_set_register_cap(rbmg_batch* batch, int regs);

@@ -103,6 +103,7 @@ SIGNATURES = {
     "rbmg_batch_get_shape": [_vp, _ip, _ip, _ip],
     "rbmg_batch_autotune": [_vp, C.c_int, C.c_int, _dp],
     "rbmg_batch_set_register_cap": [_vp, C.c_int],
+    "rbmg_batch_set_wait": [_vp, C.c_double, C.c_uint32],
     "rbmg_batch_get_register_cap": [_vp, _ip],
     "rbmg_batch_result": [_vp, C.c_int, _dp, _dp, _dp],
     "rbmg_batch_info": [_vp, _ip, _u64p, _dp],

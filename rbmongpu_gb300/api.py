@@ -922,6 +922,11 @@ class Batch:
         call("rbmg_batch_get_shape", self._h, C.byref(w), C.byref(r), C.byref(b))
         return w.value, r.value, b.value
 
+    def set_wait(self, seconds=20.0, extra_walkers=0):
+        """Wall-clock limit of a reduction task's wait for its instance's walkers; with
+        extra_walkers > 0 the wait cannot end and runs out (the bounded-wait test)."""
+        call("rbmg_batch_set_wait", self._h, float(seconds), int(extra_walkers))
+
     @property
     def register_cap(self):
         r = C.c_int()

@@ -68,6 +68,9 @@ struct SLaunch {
     int first;            // 1: draw the walkers' start spins
     int* error;           // 1: a reduction task gave up waiting
     unsigned long long* accepts;   // [1]
+    unsigned long long wait_ns;    // wall-clock limit of a reduction task's wait
+    unsigned int wait_extra;       // walkers a reduction task waits for beyond the instance's
+                                   // (0; a test sets it so that the wait runs out)
 };
 
 __device__ __forceinline__ unsigned long long global_ns() {
@@ -271,11 +274,14 @@ __device__ __noinline__ void walker_task(const SLaunch& L, const SInst& Ig, int 
 // zeroed by the replay; their order of addition is not fixed)
 template <int R>
 __device__ __noinline__ void reduce_task(const SLaunch& L, const SInst& I, int r0, int w0, int lane) {
-    // wait for the instance's walkers (bounded: 20 s of wall clock)
+    // wait for the instance's walkers (bounded by L.wait_ns of wall clock; a wait that gives
+    // up raises the error flag, and every other waiter leaves as soon as it sees the flag)
     if (lane == 0) {
         const unsigned long long t0 = global_ns();
-        while (atomicAdd(I.done, 0u) < static_cast<unsigned int>(I.walkers)) {
-            if (global_ns() - t0 > 20000000000ull) {
+        const unsigned int need = static_cast<unsigned int>(I.walkers) + L.wait_extra;
+        while (atomicAdd(I.done, 0u) < need) {
+            if (*reinterpret_cast<volatile int*>(L.error)) break;
+            if (global_ns() - t0 > L.wait_ns) {
                 atomicExch(L.error, 1);
                 break;
             }
@@ -384,9 +390,13 @@ struct rbmg_batch {
     int blocks = 0;
     bool first = true;
     int therm = 0, sweeps = 1;  // graph parameters
+    unsigned long long wait_ns = 20000000000ull;
+    unsigned int wait_extra = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int graph_rows = 0, graph_wpb = 0, graph_regs = 0, graph_first = -1, graph_therm = -1, graph_sweeps = -1;
+    unsigned long long graph_wait_ns = 0;
+    unsigned int graph_wait_extra = 0;
     double tuned_ms = 0.0;
     ~rbmg_batch() {
         if (exec) cudaGraphExecDestroy(exec);
@@ -444,6 +454,8 @@ cudaError_t launch_serve(rbmg_batch* b, cudaStream_t st) {
     L.first = b->first ? 1 : 0;
     L.error = b->d_error.as<int>();
     L.accepts = b->d_accepts.as<unsigned long long>();
+    L.wait_ns = b->wait_ns;
+    L.wait_extra = b->wait_extra;
     const int threads = 32 * b->warps_per_block;
     const size_t sm = serve_smem(b->warps_per_block);
     with_serve_kernel(b->rows, b->regs, [&](auto kern) { kern<<<b->blocks, threads, sm, st>>>(L); });
@@ -453,7 +465,8 @@ cudaError_t launch_serve(rbmg_batch* b, cudaStream_t st) {
 // (re)captures the replay: counter resets and the persistent launch
 int batch_capture(rbmg_batch* b) {
     if (b->exec && b->graph_rows == b->rows && b->graph_wpb == b->warps_per_block && b->graph_regs == b->regs &&
-        b->graph_first == static_cast<int>(b->first) && b->graph_therm == b->therm && b->graph_sweeps == b->sweeps)
+        b->graph_first == static_cast<int>(b->first) && b->graph_therm == b->therm && b->graph_sweeps == b->sweeps &&
+        b->graph_wait_ns == b->wait_ns && b->graph_wait_extra == b->wait_extra)
         return RBMG_OK;
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
@@ -488,6 +501,8 @@ int batch_capture(rbmg_batch* b) {
     b->graph_first = static_cast<int>(b->first);
     b->graph_therm = b->therm;
     b->graph_sweeps = b->sweeps;
+    b->graph_wait_ns = b->wait_ns;
+    b->graph_wait_extra = b->wait_extra;
     return RBMG_OK;
 }
 
@@ -601,6 +616,13 @@ extern "C" int rbmg_batch_set_shape(rbmg_batch* b, int warps_per_block, int rows
         if (r != RBMG_OK) return r;
     }
     b->warps_per_block = warps_per_block;
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_batch_set_wait(rbmg_batch* b, double seconds, uint32_t extra_walkers) {
+    if (!b || !(seconds > 0.0) || seconds > 60.0) return fail(RBMG_EINVAL, "batch: wait limit in (0, 60] s");
+    b->wait_ns = static_cast<unsigned long long>(seconds * 1e9);
+    b->wait_extra = extra_walkers;
     return RBMG_OK;
 }
 

@@ -98,3 +98,21 @@ def test_autotune_keeps_the_fastest_shape():
     batch.run(0, 1)
     E, g, _ = batch.result(0)
     assert np.isfinite(E) and np.all(np.isfinite(g))
+
+
+def test_a_wait_that_runs_out_is_reported_and_the_device_stays_usable():
+    """Failure detection without a GPU fault: the reduction tasks wait for one walker more
+    than each instance has, so the bounded wait (0.2 s) runs out; the replay reports
+    RBMG_ETIMEOUT, and the next replay with the ordinary wait succeeds."""
+    import rbmongpu_gb300 as rg
+    inst = [(rbm(16, 1, 106_000 + q), rg.Operator(*rg.operators.tfim_chain(16, 1.0, 1.0)), 64, q) for q in range(3)]
+    batch = rg.Batch(inst)
+    batch.set_wait(0.2, extra_walkers=1)
+    with pytest.raises(rg.RbmgError) as err:
+        batch.run(0, 1)
+    assert err.value.code == 4   # RBMG_ETIMEOUT
+    batch.set_wait(20.0, extra_walkers=0)
+    batch.run(0, 2)
+    for q in range(3):
+        E, g, _ = batch.result(q)
+        assert np.isfinite(E) and np.all(np.isfinite(g))
