@@ -215,6 +215,12 @@ def combine_ranks(tot, tmax, device):
     return t1.cpu().numpy(), t2.cpu().numpy()
 
 
+def learned_slices(args, walkers):
+    """walker slices of a frozen learned row (Chain.set_learned_streams; 0 = automatic:
+    two from 8192 walkers)"""
+    return args.learned_streams or (2 if walkers >= 8192 else 1)
+
+
 def replica_seeds(rank):
     """Philox keys of the rank's plain chain, learned chain and proposal network: every rank
     samples its own replica of the walker sets."""
@@ -676,7 +682,7 @@ def main():
                    "walkers_per_gpu": B, "sigma": SIGMA, "h": FIELD, "therm_sweeps": THERM_SWEEPS,
                    "step": f"learned: {L} frozen MH steps + E_loc; plain: {S} sweeps + E_loc",
                    "train_steps": args.train_steps, "train_walkers": args.train_walkers,
-                   "learned_streams": args.learned_streams or (2 if B >= 8192 else 1),
+                   "learned_streams": learned_slices(args, B),
                    "l2": "flushed between timed rows"},
         "learned": dict(le, ess_per_s=ess_l / sec_l, acceptance=r["learned_accept"], train_seconds=r["train_s"],
                         ms_per_row=float(np.mean(r["learned_ms"]))),
@@ -690,9 +696,10 @@ def main():
         "eloc_per_s": n_l / sec_l,
         "e2e": {"value": ess_e2e / sec_e2e, "unit": UNIT, "h2d_bytes_per_step": int(r["h2d"]),
                 "d2h_bytes_per_step": int(r["d2h"])},
-        # per learned row: L x (propose, spins_to_x, 3 GEMM layers, accept) + angles, the
-        # current-state forward (spins_to_x + 3 GEMM layers) and the local-energy pass
-        "gpu_launches": args.steps * (6 * L + 6),
+        # per learned row and walker slice: the first step's draw, then L x (tensor-core
+        # network on the proposed states, accept + next draw); per row: the angles from
+        # scratch, the current states' network pass and the local-energy pass
+        "gpu_launches": args.steps * (learned_slices(args, B) * (2 * L + 1) + 3),
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak if peak else None, "traffic": SAMPLER_DRAM_BYTES,
                      "traffic_source": "ncu dram__bytes_read + write of one launch (W and walker state are "
