@@ -134,8 +134,9 @@ static int rbm_upload(rbmg_psi* p) {
     const size_t kp = static_cast<size_t>((p->Mpad / 32 + 1) / 2) * 32;
     RBMG_CK(p->dWq.ensure(sizeof(float4) * kp * p->N));
     RBMG_CK(p->dbq.ensure(sizeof(float4) * kp));
+    RBMG_CK(p->dWt.ensure(sizeof(float2) * static_cast<size_t>(p->Mpad) * p->N));
     RBMG_CK(launch_rbm_pairs(p->N, p->Mpad, p->dW.as<float2>(), p->db.as<float2>(), p->dWq.as<float4>(),
-                             p->dbq.as<float4>(), stream()));
+                             p->dbq.as<float4>(), p->dWt.as<float2>(), stream()));
     if (rbm_tc_supported(p->N, p->Mpad)) {
         RBMG_CK(p->dWtc.ensure(sizeof(__nv_bfloat16) * rbm_tc_pack_elems(p->Mpad, rbm_tc_kp(p->N))));
         RBMG_CK(launch_rbm_tc_pack(p->N, p->M, p->Mpad, p->dW.as<float2>(), p->dWtc.as<__nv_bfloat16>(), stream()));
@@ -406,6 +407,11 @@ static int op_compile(rbmg_operator* op) {
     RBMG_CK(up(op->d_flip_off, op->flip_off.data(), sizeof(int) * op->S));
     RBMG_CK(up(op->d_flip_sites, op->flip_sites.data(), sizeof(int) * op->flip_sites.size()));
     RBMG_CK(up(op->d_slot, op->offdiag_slot.data(), sizeof(int) * op->S));
+    std::vector<int> offdiag;
+    for (int n = 0; n < op->S; n++)
+        if (op->offdiag_slot[n] >= 0) offdiag.push_back(n);
+    if (offdiag.empty()) offdiag.push_back(0);
+    RBMG_CK(up(op->d_offdiag, offdiag.data(), sizeof(int) * offdiag.size()));
     return RBMG_OK;
 }
 

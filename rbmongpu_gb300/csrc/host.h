@@ -78,6 +78,7 @@ struct rbmg_psi {
     int M = 0, Mpad = 0;
     std::vector<rbmg::cplx> b, W;
     rbmg::DevBuf dW, db, dWq, dbq;     // complex64 rows, and the sampler's paired copies (kernels.h)
+    rbmg::DevBuf dWt;                  // W transposed [Mpad][N] (the local-energy kernel)
     rbmg::DevBuf dWtc;                 // W as BF16 hi / mid / lo tensor-core operands (angles_tc.cu), if supported
     rbmg::DevBuf tc_error;             // set when a tensor-core pass of this psi gave up waiting
     mutable rbmg::DevBuf dW64, db64;   // FP64 copies for the Hilbert-space distance pass, uploaded on use
@@ -100,7 +101,8 @@ struct rbmg_psi {
     int num_params() const;
     rbmg::RbmDev rbm_dev() const {
         return rbmg::RbmDev{N, M, Mpad, static_cast<const float2*>(dW.p), static_cast<const float2*>(db.p),
-                            static_cast<const float4*>(dWq.p), static_cast<const float4*>(dbq.p)};
+                            static_cast<const float4*>(dWq.p), static_cast<const float4*>(dbq.p),
+                            static_cast<const float2*>(dWt.p)};
     }
 };
 
@@ -141,6 +143,7 @@ struct rbmg_operator {
     int num_offdiag = 0;
     int max_site = -1;
     rbmg::DevBuf d_coef, d_coef32, d_site1, d_next1, d_ypow, d_zmask, d_nflip, d_flip_off, d_flip_sites, d_slot;
+    rbmg::DevBuf d_offdiag;
     // per-site CSR of the off-diagonal slots whose string flips the site (E_k term)
     std::vector<int> site_ptr, site_slots;
     rbmg::DevBuf d_site_ptr, d_site_slots;
@@ -157,7 +160,8 @@ struct rbmg_operator {
                            num_offdiag,
                            d_coef32.as<float2>(),
                            d_site1.as<int>(),
-                           d_next1.as<int>()};
+                           d_next1.as<int>(),
+                           d_offdiag.as<int>()};
     }
 };
 

@@ -22,11 +22,13 @@ struct RbmDev {
     // Wq [N][ceil(K / 2)][32], bq [ceil(K / 2)][32]; the unit beyond an odd K is zero
     const float4* Wq;
     const float4* bq;
+    const float2* Wt;    // W transposed, [Mpad][N] (rows of unit j across the spins)
 };
 
-// build Wq, bq from W [N][Mpad], b [Mpad] (K = Mpad / 32 hidden units per lane)
+// build Wq, bq from W [N][Mpad], b [Mpad] (K = Mpad / 32 hidden units per lane), and
+// Wt [Mpad][N] = W transposed
 cudaError_t launch_rbm_pairs(int N, int Mpad, const float2* W, const float2* b, float4* Wq, float4* bq,
-                             cudaStream_t st);
+                             float2* Wt, cudaStream_t st);
 
 // Pauli-string operator in compact form (built from the reference's padded
 // table, include/operator/Operator.hpp:30-88).
@@ -43,6 +45,7 @@ struct OpDev {
     const float2* coef32;      // [S] coefficients rounded to FP32 (local-energy sums)
     const int* site1;          // [S] the flipped site of a single-flip string, -1 otherwise
     const int* next1;          // [S + 1] next1[n]: first single-flip string >= n (S if none)
+    const int* offdiag;        // [num_offdiag] the off-diagonal strings in order
 };
 
 // Metropolis launch: one warp per walker (include/spin_ensembles/MonteCarloLoop.hpp:55-256)

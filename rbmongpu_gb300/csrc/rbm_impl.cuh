@@ -615,14 +615,23 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) rbm_est_kernel(RbmDev P, 
 }
 
 // ---------------------------------------------------------------------------
-// Local energies only (the measurement of a chain step): one warp per configuration,
-// angles and f(theta) in registers, each string's flipped angles formed and dropped
-// angle by angle (Operator.hpp:90-115).
+// Local energies only (the measurement of a chain step, Operator.hpp:90-115), the lanes
+// over the strings: one warp per configuration; its angles
+// and f(theta) sit in the warp's shared-memory slice, and every lane evaluates the whole
+// log-ratio of its own (off-diagonal string, quarter of the hidden units) item: units
+// j = q, q + 4, ... two at a time on FP32x2 pairs (j and j + 4), the flipped angles from the
+// transposed W (the lanes of a round read neighbouring spins of the same unit rows), the
+// differences f(theta'') - f(theta) summed in pairs (104 units a lane at M = 400; the
+// reciprocal of the activation's denominator is the hardware's approximation, within an
+// ulp).  Two shuffles join a
+// string's quarters; one warp reduction per configuration joins the strings.  No
+// per-string reduction sits on the critical path, and each lane's loop over units is
+// independent work.
 // ---------------------------------------------------------------------------
 template <int K, int NW>
-__global__ void __launch_bounds__(32 * kWarpsPerBlock, K > 13 ? 3 : 4) rbm_eloc_kernel(RbmDev P, OpDev op, EstLaunch L) {
-    const int lane = threadIdx.x & 31;
-    const long t = static_cast<long>(blockIdx.x) * kWarpsPerBlock + (threadIdx.x >> 5);
+__global__ void __launch_bounds__(32 * kWarpsPerBlock) rbm_eloc_t_kernel(RbmDev P, OpDev op, EstLaunch L) {
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const long t = static_cast<long>(blockIdx.x) * kWarpsPerBlock + wib;
     if (t >= L.count) return;
     Spins<NW> s;
     if (L.flags & EST_ENUMERATE) {
@@ -634,90 +643,102 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, K > 13 ? 3 : 4) rbm_eloc_
 #pragma unroll
         for (int k = 0; k < NW; k++) s.w[k] = L.spins[t * NW + k];
     }
-    // angles and f(theta) on packed pairs (units 2 kk, 2 kk + 1 of the lane): every half
-    // is the scalar arithmetic, the sums below run over the units in their scalar order
     constexpr int KP = (K + 1) / 2;
-    pair_t tr[KP], ti[KP];
-    rbm_refresh2(P, s, tr, ti, lane);
-    // f(theta) of the configuration in this warp's shared-memory slice (re pair, im pair),
-    // read once per string: registers stay for the angles and the prefetched W rows
-    __shared__ float4 f_sm[kWarpsPerBlock][KP][32];
-    float4 (&f)[KP][32] = f_sm[threadIdx.x >> 5];
+    constexpr int MP = 32 * K;
+    // (theta.re, theta.im, f.re, f.im) of every unit, in the warp's slice
+    __shared__ float4 tf_sm[kWarpsPerBlock][MP];
+    float4* tf = tf_sm[wib];
+    {
+        // a lane's pair kk holds units lane + 64 kk and lane + 64 kk + 32
+        pair_t tr[KP], ti[KP];
+        rbm_refresh2(P, s, tr, ti, lane);
 #pragma unroll
-    for (int kk = 0; kk < KP; kk++) {
-        const Pair2 v = lc_c2(tr[kk], ti[kk]);
-        float a0, a1, b0, b1;
-        up2(v.re, a0, a1);
-        up2(v.im, b0, b1);
-        f[kk][lane] = make_float4(a0, a1, b0, b1);
+        for (int kk = 0; kk < KP; kk++) {
+            const Pair2 v = lc_c2(tr[kk], ti[kk]);
+            float a0, a1, b0, b1, r0, r1, i0, i1;
+            up2(tr[kk], a0, a1);
+            up2(ti[kk], b0, b1);
+            up2(v.re, r0, r1);
+            up2(v.im, i0, i1);
+            const int j0 = lane + 64 * kk;
+            tf[j0] = make_float4(a0, b0, r0, i0);
+            if (2 * kk + 1 < K) tf[j0 + 32] = make_float4(a1, b1, r1, i1);
+        }
     }
-    // the paired W row of the next single-flip string is loaded while the current string
-    // is evaluated, so the row's latency is off the per-string critical path
+    __syncwarp();
     KahanC acc;
-    float4 wbuf[KP];
-    int nxt = op.next1[0];
-    if (nxt < op.S) {
-        const float4* row = P.Wq + static_cast<long>(op.site1[nxt]) * KP * 32 + lane;
-#pragma unroll
-        for (int kk = 0; kk < KP; kk++) wbuf[kk] = __ldg(row + 32 * kk);
-    }
-    for (int n = 0; n < op.S; n++) {
-        const float2 cf = string_factor(op, n, s);
-        const int nf = op.nflip[n];
-        if (nf == 0) {
+    // diagonal strings: the lanes over the strings
+    for (int n = lane; n < op.S; n += 32) {
+        if (op.nflip[n] == 0) {
+            const float2 cf = string_factor(op, n, s);
             acc.add(cf.x, cf.y);
-            continue;
         }
-        float2 part = make_float2(0.0f, 0.0f);
-        auto add_unit_pair = [&](const Pair2& g, int kk) {
-            const float4 f0 = f[kk][lane];
-            float a0, a1, b0, b1;
-            up2(sub2(g.re, pk2(f0.x, f0.y)), a0, a1);
-            up2(sub2(g.im, pk2(f0.z, f0.w)), b0, b1);
-            part.x += a0;
-            part.y += b0;
-            if (2 * kk + 1 < K) {
-                part.x += a1;
-                part.y += b1;
-            }
-        };
-        if (nf == 1) {   // n == nxt
-            const int site = op.site1[n];
-            const pair_t two_s = splat2(s.up(site) ? -2.0f : 2.0f);
-            float4 w[KP];
-#pragma unroll
-            for (int kk = 0; kk < KP; kk++) w[kk] = wbuf[kk];
-            nxt = op.next1[n + 1];
-            if (nxt < op.S) {
-                const float4* row = P.Wq + static_cast<long>(op.site1[nxt]) * KP * 32 + lane;
-#pragma unroll
-                for (int kk = 0; kk < KP; kk++) wbuf[kk] = __ldg(row + 32 * kk);
-            }
-#pragma unroll
-            for (int kk = 0; kk < KP; kk++) {
-                const Pair2 g = lc_c2(fma2(two_s, pk2(w[kk].x, w[kk].y), tr[kk]),
-                                      fma2(two_s, pk2(w[kk].z, w[kk].w), ti[kk]));
-                add_unit_pair(g, kk);
-            }
-        } else {
-            const int off = op.flip_off[n];
-#pragma unroll
-            for (int kk = 0; kk < KP; kk++) {
-                pair_t nr = tr[kk], ni = ti[kk];
-                for (int q = 0; q < nf; q++) {
-                    const int site = op.flip_sites[off + q];
-                    const pair_t two_s = splat2(s.up(site) ? -2.0f : 2.0f);
-                    const float4 w = __ldg(P.Wq + static_cast<long>(site) * KP * 32 + lane + 32 * kk);
-                    nr = fma2(two_s, pk2(w.x, w.y), nr);
-                    ni = fma2(two_s, pk2(w.z, w.w), ni);
-                }
-                add_unit_pair(lc_c2(nr, ni), kk);
-            }
-        }
-        const float2 e = string_term(cf, warp_sum_xor2(part));
-        acc.add(e.x, e.y);
     }
-    if (lane == 0) L.eloc[t] = acc.value();
+    const int items = 4 * op.num_offdiag;
+    const int N = P.N;
+    for (int it0 = 0; it0 < items; it0 += 32) {
+        const int it = it0 + lane;
+        const bool live = it < items;
+        const int n = live ? op.offdiag[it >> 2] : 0;
+        const int q = it & 3;
+        // sums of the real and imaginary differences on pairs (units j, j + 4)
+        pair_t sr = splat2(0.0f), si = sr;
+        if (live) {
+            const int nf = op.nflip[n];
+            const int off = op.flip_off[n];
+            if (nf == 1) {
+                const int site = op.flip_sites[off];
+                const pair_t two_s = splat2(s.up(site) ? -2.0f : 2.0f);
+                const float2* wcol = P.Wt + site;
+#pragma unroll 2
+                for (int j = q; j < MP; j += 8) {
+                    const float2 w0 = __ldg(wcol + static_cast<long>(j) * N);
+                    const float2 w1 = __ldg(wcol + static_cast<long>(j + 4) * N);
+                    const float4 a0 = tf[j], a1 = tf[j + 4];
+                    const Pair2 g = lc_c2_approx(fma2(two_s, pk2(w0.x, w1.x), pk2(a0.x, a1.x)),
+                                                 fma2(two_s, pk2(w0.y, w1.y), pk2(a0.y, a1.y)));
+                    sr = add2(sr, sub2(g.re, pk2(a0.z, a1.z)));
+                    si = add2(si, sub2(g.im, pk2(a0.w, a1.w)));
+                }
+            } else {
+                for (int j = q; j < MP; j += 8) {
+                    const float4 a0 = tf[j], a1 = tf[j + 4];
+                    pair_t xr = pk2(a0.x, a1.x), xi = pk2(a0.y, a1.y);
+                    for (int u = 0; u < nf; u++) {
+                        const int site = op.flip_sites[off + u];
+                        const pair_t two_s = splat2(s.up(site) ? -2.0f : 2.0f);
+                        const float2 w0 = __ldg(P.Wt + static_cast<long>(j) * N + site);
+                        const float2 w1 = __ldg(P.Wt + static_cast<long>(j + 4) * N + site);
+                        xr = fma2(two_s, pk2(w0.x, w1.x), xr);
+                        xi = fma2(two_s, pk2(w0.y, w1.y), xi);
+                    }
+                    const Pair2 g = lc_c2_approx(xr, xi);
+                    sr = add2(sr, sub2(g.re, pk2(a0.z, a1.z)));
+                    si = add2(si, sub2(g.im, pk2(a0.w, a1.w)));
+                }
+            }
+        }
+        float r0, r1, i0, i1;
+        up2(sr, r0, r1);
+        up2(si, i0, i1);
+        float dx = r0 + r1, dy = i0 + i1;
+        // the four quarters of a string are lanes 4m .. 4m + 3
+        dx += __shfl_xor_sync(0xffffffffu, dx, 1);
+        dy += __shfl_xor_sync(0xffffffffu, dy, 1);
+        dx += __shfl_xor_sync(0xffffffffu, dx, 2);
+        dy += __shfl_xor_sync(0xffffffffu, dy, 2);
+        if (live && q == 0) {
+            const float2 e = string_term(string_factor(op, n, s), make_float2(dx, dy));
+            acc.add(e.x, e.y);
+        }
+    }
+    double2 v = acc.value();
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+    }
+    if (lane == 0) L.eloc[t] = v;
 }
 
 // ---------------------------------------------------------------------------
@@ -759,10 +780,10 @@ cudaError_t rbm_est_launch_k(const RbmDev& P, const OpDev* op, const RbmDev* PP,
     RbmDev pp = PP ? *PP : P;
     if (has && (L.flags & ~(EST_ELOC | EST_ENUMERATE)) == 0) {
         switch (nw) {
-            case 1: rbm_eloc_kernel<K, 1><<<grid, block, 0, st>>>(P, o, L); break;
-            case 2: rbm_eloc_kernel<K, 2><<<grid, block, 0, st>>>(P, o, L); break;
-            case 3: rbm_eloc_kernel<K, 3><<<grid, block, 0, st>>>(P, o, L); break;
-            case 4: rbm_eloc_kernel<K, 4><<<grid, block, 0, st>>>(P, o, L); break;
+            case 1: rbm_eloc_t_kernel<K, 1><<<grid, block, 0, st>>>(P, o, L); break;
+            case 2: rbm_eloc_t_kernel<K, 2><<<grid, block, 0, st>>>(P, o, L); break;
+            case 3: rbm_eloc_t_kernel<K, 3><<<grid, block, 0, st>>>(P, o, L); break;
+            case 4: rbm_eloc_t_kernel<K, 4><<<grid, block, 0, st>>>(P, o, L); break;
             default: return cudaErrorInvalidValue;
         }
         return cudaGetLastError();
