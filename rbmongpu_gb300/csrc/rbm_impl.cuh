@@ -654,7 +654,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) rbm_eloc_t_kernel(RbmDev 
         rbm_refresh2(P, s, tr, ti, lane);
 #pragma unroll
         for (int kk = 0; kk < KP; kk++) {
-            const Pair2 v = lc_c2(tr[kk], ti[kk]);
+            // f(theta) with the same approximate reciprocal as f(theta'') below
+            const Pair2 v = lc_c2_approx(tr[kk], ti[kk]);
             float a0, a1, b0, b1, r0, r1, i0, i1;
             up2(tr[kk], a0, a1);
             up2(ti[kk], b0, b1);

@@ -202,14 +202,16 @@ __device__ __noinline__ void walker_task(const SLaunch& L, const SInst& Ig, int 
         }
     }
     // measurement: local energy and tanh(theta) of the final configuration; f(theta) in
-    // this warp's shared-memory slice [kSK][32] keeps the register footprint of the sweeps
+    // this warp's shared-memory slice [kSK][32] keeps the register footprint of the sweeps;
+    // f(theta) and f(theta'') both with the approximate reciprocal (the local-energy
+    // differences, as rbm_eloc_t_kernel takes them)
     float tr[K], ti[K];
     s_refresh(I, s, tr, ti, lane);
     extern __shared__ float2 s_f[];
     float2* myf = s_f + (threadIdx.x >> 5) * kSK * 32 + lane;
 #pragma unroll
     for (int k = 0; k < K; k++) {
-        myf[32 * k] = lc_c(tr[k], ti[k]);
+        myf[32 * k] = lc_c_approx(tr[k], ti[k]);
         I.T[static_cast<long>(w) * I.Mpad + lane + 32 * k] = tanh_c(tr[k], ti[k]);
     }
     KahanC e;
@@ -231,7 +233,7 @@ __device__ __noinline__ void walker_task(const SLaunch& L, const SInst& Ig, int 
             for (int k = 0; k < K; k++) wv[k] = __ldg(row + 32 * k);
 #pragma unroll
             for (int k = 0; k < K; k++) {
-                const float2 g = lc_c(fmaf(two_s, wv[k].x, tr[k]), fmaf(two_s, wv[k].y, ti[k]));
+                const float2 g = lc_c_approx(fmaf(two_s, wv[k].x, tr[k]), fmaf(two_s, wv[k].y, ti[k]));
                 const float2 f0 = myf[32 * k];
                 part.x += g.x - f0.x;
                 part.y += g.y - f0.y;
@@ -247,7 +249,7 @@ __device__ __noinline__ void walker_task(const SLaunch& L, const SInst& Ig, int 
                         nr = fmaf(two_s, wv.x, nr);
                         ni = fmaf(two_s, wv.y, ni);
                     }
-                    const float2 g = lc_c(nr, ni);
+                    const float2 g = lc_c_approx(nr, ni);
                     const float2 f0 = myf[32 * k];
                     part.x += g.x - f0.x;
                     part.y += g.y - f0.y;
