@@ -1,5 +1,6 @@
 // FP32 FMA throughput probe: the denominator of the sampler's roofline (the sampler
-// is bound by the FP32 pipe, whose peak the driver's measured-peaks file does not list).
+// is bound by the FP32 pipe; the measured peaks at hand cover HBM copy bandwidth and BF16
+// tensor throughput only).
 #include <cuda_runtime.h>
 
 #include "host.h"
