@@ -580,6 +580,128 @@ def run_smatrix(args):
     print(json.dumps(line))
 
 
+# --------------------------------------------------------------------- deep-net adjoint workload
+DEEP_N, DEEP_SIZES, DEEP_WALKERS, DEEP_SEED = 100, (200, 100, 50), 8192, 107
+
+
+def deep_workload():
+    """Dense complex PsiDeep N=100 -> 200 -> 100 -> 50: weights and biases complex
+    Normal(0, 0.1 / fan_in) (variance, split over the real and imaginary parts), final
+    weights 1, PCG64(107)."""
+    rng = np.random.Generator(np.random.PCG64(DEEP_SEED))
+    b, conn, W = [], [], []
+    fan = DEEP_N
+    for m in DEEP_SIZES:
+        sd = np.sqrt(0.1 / fan / 2)
+        b.append(rng.normal(0, sd, m) + 1j * rng.normal(0, sd, m))
+        conn.append(np.array([[c] * m for c in range(fan)]))
+        W.append(rng.normal(0, sd, (fan, m)) + 1j * rng.normal(0, sd, (fan, m)))
+        fan = m
+    return b, conn, W, np.ones(DEEP_SIZES[-1])
+
+
+def deep_flops():
+    """FP32 flops per configuration of one forward pass (a complex MAC = 8 flops per
+    connection, the activation ~50 per unit), and of the adjoint per sample: its N
+    flipped neighbours and itself, each a forward and a reverse pass (2 x the MACs) and
+    the outer products of the parameter gradient (1 x)."""
+    macs = DEEP_N * DEEP_SIZES[0] + DEEP_SIZES[0] * DEEP_SIZES[1] + DEEP_SIZES[1] * DEEP_SIZES[2]
+    fwd = 8 * macs + 50 * sum(DEEP_SIZES)
+    adj = (DEEP_N + 1) * (fwd + 3 * 8 * macs)
+    return fwd, adj
+
+
+def run_deep(args):
+    """One step = the gradient of <H> of the deep net through the adjoint kernels
+    (ExpectationValue.eloc_gradient, score=True; the autograd Function's backward) over a
+    MonteCarloLoop pass of 8192 walkers (3 thermalisation sweeps, then one sample each)."""
+    import torch
+    import rbmongpu_gb300 as rg
+    from rbmongpu_gb300.autograd import energy
+    torch.cuda.set_device(0)
+    b, conn, W, fw = deep_workload()
+    N = DEEP_N
+    psi = rg.PsiDeep(np.zeros(N), np.zeros(N), b, conn, W, fw, 1.0, False, True)
+    H = rg.Operator(*rg.operators.tfim_chain(N, 1.0, 1.0))
+    therm = 3
+    mk = lambda: rg.MonteCarloLoop(DEEP_WALKERS, 1, therm, DEEP_WALKERS, True, seed=21)   # noqa: E731
+    ev = rg.ExpectationValue()
+    for _ in range(args.warmup):
+        ev.eloc_gradient(psi, H, mk(), score=True)
+    sp = rg.library_stream()
+    stream = torch.cuda.ExternalStream(sp)
+    K = args.steps
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    clocks = ClockSampler(0)
+    clocks.start()
+    for k in range(K):
+        torch.cuda.synchronize()
+        starts[k].record(stream)
+        g, E = ev.eloc_gradient(psi, H, mk(), score=True)
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = np.array([a.elapsed_time(e) for a, e in zip(starts, ends)])
+    assert np.isfinite(E) and np.all(np.isfinite(g))
+    sec = float(ms.mean()) / 1e3
+    # end to end through the autograd Function: parameters from a host tensor, the
+    # gradient back in it
+    params = torch.tensor(psi.params, requires_grad=True)
+    t0 = time.perf_counter()
+    for _ in range(K):
+        params.grad = None
+        loss = energy(params, psi, H, mk())
+        loss.backward()
+    e2e_s = (time.perf_counter() - t0) / K
+    fwd, adj = deep_flops()
+    flops = DEEP_WALKERS * ((therm + 1) * N * fwd + adj)
+    v = ctypes_probe_fp32()
+    cpu = None
+    if args.cpu_seconds > 0:
+        from oracle import pyoracle as po
+        opsi = po.Deep(N, b, conn, W, fw, 1.0)
+        rng = np.random.default_rng(5)
+        spins = rng.integers(0, 2 ** 63, (4, 2), dtype=np.uint64)
+        spins[:, 1] &= (1 << (N - 64)) - 1
+        t0 = time.perf_counter()
+        po.samples_gradient(opsi, po.Op(*rg.operators.tfim_chain(N, 1.0, 1.0)), spins)
+        dt = time.perf_counter() - t0
+        cpu = {"value": len(spins) / dt, "unit": "samples/s", "cores": 1, "kind": "port",
+               "sample": "4 configurations: the reference's O_k gradient estimator (E_k term included) in FP64 "
+                         "by the CPU restatement, one core"}
+    P = psi.num_params
+    line = {
+        "metric": "deep-net gradient of <H> (adjoint kernels): MC samples per second",
+        "value": DEEP_WALKERS / sec, "unit": "samples/s", "n_gpus": 1, "steps": K, "warmup": args.warmup,
+        "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (complex64 net), f64 gradient sums", "data": "synthetic (seeded PCG64 parameters)",
+        "config": {"workload": "psideep_100_200_100_50_tfim_adjoint", "N": N, "layers": list(DEEP_SIZES),
+                   "walkers": DEEP_WALKERS, "therm_sweeps": therm,
+                   "step": "MonteCarloLoop pass (3 thermalisation sweeps, 1 sample per walker) + adjoint gradient"},
+        "eloc_per_s": DEEP_WALKERS / sec,
+        "e2e": {"value": DEEP_WALKERS / e2e_s, "unit": "samples/s", "h2d_bytes_per_step": 16 * P,
+                "d2h_bytes_per_step": 16 * P},
+        "gpu_launches": None,
+        "roofline": {"bound": "fp32", "achieved": flops / sec / 1e12, "peak": v, "unit": "TFLOP/s",
+                     "frac": flops / sec / 1e12 / v if v else None, "traffic": None,
+                     "peak_source": "measured in this run by the library's FP32 FMA probe kernel",
+                     "kernel": "deep_mc_kernel + deep_adjoint_kernel + adj_cgemm_kernel (the whole step)",
+                     "flops_per_step": flops},
+        "cpu_baseline": cpu,
+        "clocks": clk,
+    }
+    print(json.dumps(line))
+
+
+def ctypes_probe_fp32():
+    import ctypes
+    from rbmongpu_gb300._lib import call
+    v = ctypes.c_double()
+    call("rbmg_probe_fp32_tflops", 20000, ctypes.byref(v))
+    return v.value
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -598,9 +720,10 @@ def main():
     ap.add_argument("--sm-n", type=int, default=SM_N, help="s_matrix workload: visible units")
     ap.add_argument("--sm-m", type=int, default=SM_M, help="s_matrix workload: hidden units")
     ap.add_argument("--sm-simt", type=int, default=0, help="s_matrix workload: 1 = FP32 CUDA-core products")
-    ap.add_argument("--workload", default="learned", choices=["learned", "serving", "s_matrix"],
+    ap.add_argument("--workload", default="learned", choices=["learned", "serving", "s_matrix", "deep"],
                     help="learned: the N=100 learned-vs-plain chains (headline); serving: 64 uneven RBMs; "
-                         "s_matrix: get_S_matrix of the N=64, M=128 RBM over 16384 MC samples")
+                         "s_matrix: get_S_matrix of the N=64, M=128 RBM over 16384 MC samples; "
+                         "deep: the PsiDeep 100-200-100-50 gradient through the adjoint kernels")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -615,6 +738,10 @@ def main():
     if args.workload == "s_matrix" and args.impl == "ours":
         if rank == 0:
             run_smatrix(args)
+        return
+    if args.workload == "deep" and args.impl == "ours":
+        if rank == 0:
+            run_deep(args)
         return
 
     if args.impl == "reference":
