@@ -601,14 +601,17 @@ def deep_workload():
 
 
 def deep_flops():
-    """FP32 flops per configuration of one forward pass (a complex MAC = 8 flops per
-    connection, the activation ~50 per unit), and of the adjoint per sample: its N
-    flipped neighbours and itself, each a forward and a reverse pass (2 x the MACs) and
-    the outer products of the parameter gradient (1 x)."""
-    macs = DEEP_N * DEEP_SIZES[0] + DEEP_SIZES[0] * DEEP_SIZES[1] + DEEP_SIZES[1] * DEEP_SIZES[2]
+    """FP32 flops (a complex MAC = 8, the activation ~50 per unit) of: one full forward pass;
+    one single-flip proposal of the sampler (layer 0's pre-activations moved by the flipped
+    spin's row, the activations and the later layers evaluated); and the adjoint per
+    sample: its N flipped neighbours and itself, each a forward and a reverse pass
+    (2 x the MACs) and the outer products of the parameter gradient (1 x)."""
+    s0, s1, s2 = DEEP_SIZES
+    macs = DEEP_N * s0 + s0 * s1 + s1 * s2
     fwd = 8 * macs + 50 * sum(DEEP_SIZES)
+    proposal = 8 * s0 + 8 * (s0 * s1 + s1 * s2) + 50 * sum(DEEP_SIZES)
     adj = (DEEP_N + 1) * (fwd + 3 * 8 * macs)
-    return fwd, adj
+    return fwd, proposal, adj
 
 
 def run_deep(args):
@@ -654,8 +657,9 @@ def run_deep(args):
         loss = energy(params, psi, H, mk())
         loss.backward()
     e2e_s = (time.perf_counter() - t0) / K
-    fwd, adj = deep_flops()
-    flops = DEEP_WALKERS * ((therm + 1) * N * fwd + adj)
+    fwd, proposal, adj = deep_flops()
+    # per sweep: layer 0 and log psi from the spins (one full pass), then N proposals
+    flops = DEEP_WALKERS * ((therm + 1) * (fwd + N * proposal) + adj)
     v = ctypes_probe_fp32()
     cpu = None
     if args.cpu_seconds > 0:

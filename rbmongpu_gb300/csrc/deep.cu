@@ -172,6 +172,48 @@ __device__ V forward_once(const DeepNetDev& net, const uint64_t* s, Work<V>& w) 
     return block_sum(term, w.red);
 }
 
+// layer 0's pre-activations of the spins s (the order of forward_once's layer 0)
+__device__ void layer0_pre(const DeepNetDev& net, const uint64_t* s, float2* z0) {
+    const int size = net.size[0], conn = net.conn[0];
+    for (int u = threadIdx.x; u < size; u += blockDim.x) {
+        const float2* wl = net.w[0];
+        const int* ci = net.cidx[0];
+        float2 a = czero<float2>();
+        for (int c = 0; c < conn; c++)
+            a = cadd(a, cmul(wl[c * size + u], creal<float2>(bit_up(s, ci[c * size + u]) ? 1.0 : -1.0)));
+        z0[u] = cadd(a, net.b[0][u]);
+    }
+}
+
+// forward pass of a complex net from its layer-0 pre-activations z0 (the rest as
+// forward_once)
+__device__ float2 forward_from_z0(const DeepNetDev& net, const float2* z0, Work<float2>& w) {
+    const int t = threadIdx.x;
+    const int size0 = net.size[0];
+    for (int u = t; u < size0; u += blockDim.x) w.in[u] = act<false>(z0[u]);
+    __syncthreads();
+    float2* in = w.in;
+    float2* out = w.out;
+    for (int l = 1; l < net.L; l++) {
+        const int size = net.size[l], conn = net.conn[l];
+        if (t < size) {
+            const float2* wl = net.w[l];
+            const int* ci = net.cidx[l];
+            float2 a = czero<float2>();
+            for (int c = 0; c < conn; c++) a = cadd(a, cmul(wl[c * size + t], in[ci[c * size + t]]));
+            out[t] = act<false>(cadd(a, net.b[l][t]));
+        }
+        __syncthreads();
+        float2* tmp = in;
+        in = out;
+        out = tmp;
+    }
+    const int last = net.size[net.L - 1];
+    float2 term = czero<float2>();
+    if (t < last) term = cmul(in[t], net.fw[t]);
+    return block_sum(term, w.red);
+}
+
 // log psi of one net with optional translational averaging (PsiDeep.hpp:135-169)
 template <typename V, bool REAL>
 __device__ V net_log_psi(const DeepNetDev& net, const uint64_t* s, Work<V>& w, uint64_t* shifted) {
@@ -487,12 +529,25 @@ __global__ void deep_mc_kernel(DeepNetDev n0, DeepNetDev n1, int pair, McLaunch 
     if (threadIdx.x < kMaxWords) w.s[threadIdx.x] = s[threadIdx.x];
     __syncthreads();
     float lpr = state_log_psi<float2>(n0, n1, pair, w.s, w, shifted).x;
+    // single-flip proposals of a complex net move layer 0's pre-activations by the flipped
+    // spin's connections (z0' = z0 - 2 s_i W0[i, :]) and evaluate the later layers only;
+    // z0 and log psi are recomputed from the spins at the start of every sweep
+    const bool incr = L.fast_tries == 0 && !pair && !n0.ti;
+    float2* z0 = reinterpret_cast<float2*>(shifted + kMaxWords);   // [size[0]] the state's
+    float2* z0p = z0 + n0.size[0];                                   // [size[0]] a proposal's
     unsigned long long acc = 0, props = 0;
     const int total = L.n_therm + L.n_samples * L.sweeps_per_sample;
     int sample = 0;
     for (int sw = 0; sw < total; sw++) {
         const int updates = (L.fast_tries > 0 && sw >= L.n_therm) ? 1 : N;
+        if (incr) {
+            __syncthreads();
+            layer0_pre(n0, w.s, z0);
+            __syncthreads();
+            lpr = forward_from_z0(n0, z0, w).x;
+        }
         for (int p = 0; p < updates; p++) {
+            int site = -1;
             if (L.fast_tries > 0) {
                 // every thread draws the same mask words
                 uint64_t m[kMaxWords] = {0, 0, 0, 0};
@@ -513,16 +568,33 @@ __global__ void deep_mc_kernel(DeepNetDev n0, DeepNetDev n1, int pair, McLaunch 
                     sp[threadIdx.x] = v;
                 }
             } else {
-                const int site = static_cast<int>(rng.next() % static_cast<uint32_t>(N));
+                site = static_cast<int>(rng.next() % static_cast<uint32_t>(N));
                 __syncthreads();
                 if (threadIdx.x < kMaxWords) {
                     uint64_t v = w.s[threadIdx.x];
                     if ((site >> 6) == static_cast<int>(threadIdx.x)) v ^= 1ull << (site & 63);
                     sp[threadIdx.x] = v;
                 }
+                if (incr)
+                    for (int u = threadIdx.x; u < n0.size[0]; u += blockDim.x) z0p[u] = z0[u];
             }
             __syncthreads();
-            const float nl = state_log_psi<float2>(n0, n1, pair, sp, w, shifted).x;
+            float nl;
+            if (incr && site >= 0) {
+                const float two_s = bit_up(w.s, site) ? -2.0f : 2.0f;
+                const int size0 = n0.size[0];
+                for (int q = n0.sptr[site] + threadIdx.x; q < n0.sptr[site + 1]; q += blockDim.x) {
+                    const int e = n0.sq[q];
+                    const float2 wv = n0.w[0][e];
+                    float2* z = z0p + e % size0;
+                    atomicAdd(&z->x, two_s * wv.x);
+                    atomicAdd(&z->y, two_s * wv.y);
+                }
+                __syncthreads();
+                nl = forward_from_z0(n0, z0p, w).x;
+            } else {
+                nl = state_log_psi<float2>(n0, n1, pair, sp, w, shifted).x;
+            }
             const float delta = nl - lpr;
             bool accept = delta > 0.0f;
             if (!accept) accept = rng.uniform() <= expf_det(2.0f * delta);
@@ -531,6 +603,11 @@ __global__ void deep_mc_kernel(DeepNetDev n0, DeepNetDev n1, int pair, McLaunch 
                 if (threadIdx.x < kMaxWords) w.s[threadIdx.x] = sp[threadIdx.x];
                 lpr = nl;
                 acc++;
+                if (incr && site >= 0) {
+                    float2* tz = z0;
+                    z0 = z0p;
+                    z0p = tz;
+                }
             }
             props++;
             __syncthreads();
@@ -846,6 +923,24 @@ int deep_upload(rbmg_psi* psi) {
             RBMG_CK(upload(h.get(), ptr, &d.rptr[l]));
             RBMG_CK(upload(h.get(), q, &d.rq[l]));
         }
+        {
+            const auto& L0 = psi->layers[0];
+            std::vector<std::vector<int>> lists(psi->N);
+            for (int c = 0; c < L0.conn; c++)
+                for (int j = 0; j < L0.size; j++) {
+                    const int i = static_cast<int>(L0.connections[static_cast<size_t>(c) * L0.size + j]);
+                    if (i < psi->N) lists[i].push_back(c * L0.size + j);
+                }
+            std::vector<int> ptr(psi->N + 1, 0), q;
+            for (int i = 0; i < psi->N; i++) {
+                ptr[i] = static_cast<int>(q.size());
+                q.insert(q.end(), lists[i].begin(), lists[i].end());
+            }
+            ptr[psi->N] = static_cast<int>(q.size());
+            if (q.empty()) q.push_back(0);
+            RBMG_CK(upload(h.get(), ptr, &d.sptr));
+            RBMG_CK(upload(h.get(), q, &d.sq));
+        }
         std::vector<float2> f32(psi->final_weights.size());
         std::vector<double2> f64(psi->final_weights.size());
         for (size_t q = 0; q < f32.size(); q++) {
@@ -1122,7 +1217,8 @@ int deep_stream(rbmg_ensemble* e, const rbmg_psi* psi, const rbmg_operator* op, 
     const int rows_per_chunk = static_cast<int>(std::max<size_t>(1, std::min<size_t>(steps, max_chunk_samples / B)));
     RBMG_CK(samples.ensure(sizeof(uint64_t) * nw * B * rows_per_chunk));
     const DeepNetDev n0 = net_of(psi, 0), n1 = net_of(psi, 1);
-    const size_t sm = smem_for(n0, sizeof(float2), false);
+    // + layer 0's pre-activations of the state and of a proposal
+    const size_t sm = smem_for(n0, sizeof(float2), false) + 2 * sizeof(float2) * n0.size[0];
     RBMG_CK(set_smem(deep_mc_kernel, sm));
     bool first = true;
     for (int row0 = 0; row0 < steps; row0 += rows_per_chunk) {

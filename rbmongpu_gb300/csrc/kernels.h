@@ -106,6 +106,10 @@ struct DeepNetDev {
     const int* rq[3];
     const float2* fw;
     const double2* fw64;
+    // layer 0's connections grouped by input spin: entries c * size[0] + unit of spin i in
+    // sq[sptr[i] .. sptr[i + 1]) (the single-flip update of its pre-activations)
+    const int* sptr;
+    const int* sq;
 };
 
 // ---- launchers (return cudaError_t) ----

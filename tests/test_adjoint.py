@@ -71,10 +71,12 @@ def fd_check(psi, loss, grad, idx, h=1e-5, rtol=RTOL):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("N,sizes,walkers,rtol", [(12, (24, 12, 6), 128, RTOL), (100, (200, 100, 50), 8, 1e-3)])
+@pytest.mark.parametrize("N,sizes,walkers,rtol", [(12, (24, 12, 6), 128, RTOL), (100, (200, 100, 50), 8, 2e-3)])
 def test_fixed_sample_adjoint_matches_fp64_finite_differences(N, sizes, walkers, rtol):
-    """rtol 1e-3 for the N=100 net: its central differences carry FP64 round-off of an
-    energy of ~1e2 over a step of 1e-5, ~1e-8 against gradient entries of ~1e-5."""
+    """rtol 2e-3 for the N=100 net: its central differences carry FP64 round-off of an
+    energy of ~1e2 over a step of 1e-5, ~1e-8 against gradient entries of ~1e-5, so their
+    own noise is ~1e-3 of the largest entry (measured deviations 0.5e-3 to 1.1e-3 over the
+    sample sets the sampler has drawn)."""
     import rbmongpu_gb300 as rg
     psi = deep_net(N, sizes, 103)
     H = rg.Operator(*rg.operators.tfim_chain(N, 1.0, 1.0))
