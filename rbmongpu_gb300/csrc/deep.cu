@@ -688,61 +688,55 @@ __global__ void deep_adjoint_kernel(DeepNetDev net, OpDev op, int count, const u
     extern __shared__ __align__(16) unsigned char smem[];
     Work<float2> w = carve<float2>(smem, net, true);
     uint64_t* sp = w.s + kMaxWords;
-    double2* ebuf = reinterpret_cast<double2*>(w.s + 4 * kMaxWords);
     const long t = blockIdx.x;
     if (t >= count) return;
     const int nw = (net.N + 63) / 64;
     load_config(spins, enum_base, enumerate, t, net.N, w.s);
     const float2 lp = forward_once<float2, false, false>(net, w.s, w);
     double er = 0.0, ei = 0.0, eor = 0.0, eoi = 0.0;
-    int slot = 0;
     for (int n = 0; n < op.S; n++) {
+        if (op.nflip[n] != 0) continue;
         const double2 cf = apply_string(op, n, w.s, sp);
-        if (op.nflip[n] == 0) {
-            er += cf.x;
-            ei += cf.y;
-            continue;
-        }
-        const float2 lq = forward_once<float2, false, false>(net, sp, w);
+        er += cf.x;
+        ei += cf.y;
+    }
+    const double ws = weights ? weights[t] : 1.0;
+    const float wsf = static_cast<float>(ws);
+    // the stored forward pass and the reverse pass of configuration xi with coefficient af
+    auto pass = [&](const uint64_t* x, long xi, float2 af, bool self) {
+        for (int k = threadIdx.x; k < net.units; k += blockDim.x) acts[xi * net.units + k] = w.acts[k];
+        if (threadIdx.x < nw) xspins[xi * nw + threadIdx.x] = x[threadIdx.x];
+        if (threadIdx.x == 0) alpha[xi] = af;
+        backward_deltas<float2, false>(net, w, [&](int l, int j, float2 d) {
+            dlts[xi * net.units + net.begin_angle[l] + j] = cmul(af, d);
+            if (self) dltsO[t * net.units + net.begin_angle[l] + j] = make_float2(wsf * d.x, wsf * d.y);
+        });
+    };
+    // each off-diagonal string's neighbour: one stored forward pass gives its term of the
+    // local energy and feeds its reverse pass (coefficient w_s e_n)
+    int q = 0;
+    for (int n = 0; n < op.S; n++) {
+        if (op.nflip[n] == 0) continue;
+        q++;
+        const double2 cf = apply_string(op, n, w.s, sp);
+        const float2 lq = forward_once<float2, false, true>(net, sp, w);
         const double dr = static_cast<double>(lq.x) - lp.x, di = static_cast<double>(lq.y) - lp.y;
         const double m = exp(dr);
         const double2 e = make_double2(m * (cf.x * cos(di) - cf.y * sin(di)), m * (cf.x * sin(di) + cf.y * cos(di)));
         eor += e.x;
         eoi += e.y;
-        if (threadIdx.x == 0) ebuf[slot] = e;
-        slot++;
+        pass(sp, t * xs + q, make_float2(static_cast<float>(ws * e.x), static_cast<float>(ws * e.y)), false);
     }
     er += eor;
     ei += eoi;
-    __syncthreads();
-    const double ws = weights ? weights[t] : 1.0;
-    for (int q = 0; q < xs; q++) {
-        double2 a;
-        const uint64_t* x = w.s;
-        if (q == 0) {
-            a = make_double2(-eor, -eoi);
-            if (score) a.x += 2.0 * er;
-        } else {
-            int k = 0, n = 0;   // the (q-1)-th off-diagonal string
-            for (; n < op.S; n++)
-                if (op.nflip[n] != 0 && k++ == q - 1) break;
-            apply_string(op, n, w.s, sp);
-            x = sp;
-            a = ebuf[q - 1];
-        }
-        const float2 af = make_float2(static_cast<float>(ws * a.x), static_cast<float>(ws * a.y));
-        const long xi = t * xs + q;
-        forward_once<float2, false, true>(net, x, w);
-        for (int k = threadIdx.x; k < net.units; k += blockDim.x) acts[xi * net.units + k] = w.acts[k];
-        if (threadIdx.x < nw) xspins[xi * nw + threadIdx.x] = x[threadIdx.x];
-        if (threadIdx.x == 0) alpha[xi] = af;
-        const float wsf = static_cast<float>(ws);
-        const bool self = score && q == 0;
-        backward_deltas<float2, false>(net, w, [&](int l, int j, float2 d) {
-            dlts[xi * net.units + net.begin_angle[l] + j] = cmul(af, d);
-            if (self) dltsO[t * net.units + net.begin_angle[l] + j] = make_float2(wsf * d.x, wsf * d.y);
-        });
-        if (self && threadIdx.x == 0) alphaO[t] = make_float2(wsf, 0.f);
+    // the configuration itself last: its coefficient -sum_n e_n (+ 2 E_loc with the
+    // sampling term) needs every neighbour's term
+    {
+        double2 a = make_double2(-eor, -eoi);
+        if (score) a.x += 2.0 * er;
+        forward_once<float2, false, true>(net, w.s, w);
+        pass(w.s, t * xs, make_float2(static_cast<float>(ws * a.x), static_cast<float>(ws * a.y)), score != 0);
+        if (score && threadIdx.x == 0) alphaO[t] = make_float2(wsf, 0.f);
     }
     if (threadIdx.x == 0) eloc[t] = make_double2(er, ei);
 }
