@@ -604,13 +604,15 @@ def deep_flops():
     """FP32 flops (a complex MAC = 8, the activation ~50 per unit) of: one full forward pass;
     one single-flip proposal of the sampler (layer 0's pre-activations moved by the flipped
     spin's row, the activations and the later layers evaluated); and the adjoint per
-    sample: its N flipped neighbours and itself, each a forward and a reverse pass
-    (2 x the MACs) and the outer products of the parameter gradient (1 x)."""
+    sample: one full forward pass of the sample, then for its N flipped neighbours
+    (layer 0 moved like a proposal's) and itself (layer 0 kept) a stored forward pass,
+    a reverse pass (2 x the MACs) and the outer products of the parameter gradient
+    (1 x)."""
     s0, s1, s2 = DEEP_SIZES
     macs = DEEP_N * s0 + s0 * s1 + s1 * s2
     fwd = 8 * macs + 50 * sum(DEEP_SIZES)
     proposal = 8 * s0 + 8 * (s0 * s1 + s1 * s2) + 50 * sum(DEEP_SIZES)
-    adj = (DEEP_N + 1) * (fwd + 3 * 8 * macs)
+    adj = fwd + DEEP_N * proposal + (proposal - 8 * s0) + (DEEP_N + 1) * 3 * 8 * macs
     return fwd, proposal, adj
 
 

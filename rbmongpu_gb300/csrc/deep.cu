@@ -186,11 +186,19 @@ __device__ void layer0_pre(const DeepNetDev& net, const uint64_t* s, float2* z0)
 }
 
 // forward pass of a complex net from its layer-0 pre-activations z0 (the rest as
-// forward_once)
+// forward_once; with STORE keeps every angle and activation)
+template <bool STORE = false>
 __device__ float2 forward_from_z0(const DeepNetDev& net, const float2* z0, Work<float2>& w) {
     const int t = threadIdx.x;
     const int size0 = net.size[0];
-    for (int u = t; u < size0; u += blockDim.x) w.in[u] = act<false>(z0[u]);
+    for (int u = t; u < size0; u += blockDim.x) {
+        const float2 y = act<false>(z0[u]);
+        if (STORE) {
+            w.angles[net.begin_angle[0] + u] = z0[u];
+            w.acts[net.begin_angle[0] + u] = y;
+        }
+        w.in[u] = y;
+    }
     __syncthreads();
     float2* in = w.in;
     float2* out = w.out;
@@ -201,7 +209,13 @@ __device__ float2 forward_from_z0(const DeepNetDev& net, const float2* z0, Work<
             const int* ci = net.cidx[l];
             float2 a = czero<float2>();
             for (int c = 0; c < conn; c++) a = cadd(a, cmul(wl[c * size + t], in[ci[c * size + t]]));
-            out[t] = act<false>(cadd(a, net.b[l][t]));
+            a = cadd(a, net.b[l][t]);
+            const float2 y = act<false>(a);
+            if (STORE) {
+                w.angles[net.begin_angle[l] + t] = a;
+                w.acts[net.begin_angle[l] + t] = y;
+            }
+            out[t] = y;
         }
         __syncthreads();
         float2* tmp = in;
@@ -688,11 +702,18 @@ __global__ void deep_adjoint_kernel(DeepNetDev net, OpDev op, int count, const u
     extern __shared__ __align__(16) unsigned char smem[];
     Work<float2> w = carve<float2>(smem, net, true);
     uint64_t* sp = w.s + kMaxWords;
+    // layer 0's pre-activations of the sample and of a neighbour
+    float2* z0s = reinterpret_cast<float2*>(w.s + 4 * kMaxWords);
+    float2* z0n = z0s + net.size[0];
     const long t = blockIdx.x;
     if (t >= count) return;
     const int nw = (net.N + 63) / 64;
+    const int size0 = net.size[0];
     load_config(spins, enum_base, enumerate, t, net.N, w.s);
-    const float2 lp = forward_once<float2, false, false>(net, w.s, w);
+    __syncthreads();
+    layer0_pre(net, w.s, z0s);
+    __syncthreads();
+    const float2 lp = forward_from_z0(net, z0s, w);
     double er = 0.0, ei = 0.0, eor = 0.0, eoi = 0.0;
     for (int n = 0; n < op.S; n++) {
         if (op.nflip[n] != 0) continue;
@@ -719,7 +740,24 @@ __global__ void deep_adjoint_kernel(DeepNetDev net, OpDev op, int count, const u
         if (op.nflip[n] == 0) continue;
         q++;
         const double2 cf = apply_string(op, n, w.s, sp);
-        const float2 lq = forward_once<float2, false, true>(net, sp, w);
+        // the neighbour's layer 0: the sample's moved by the flipped spins' connections
+        for (int u = threadIdx.x; u < size0; u += blockDim.x) z0n[u] = z0s[u];
+        __syncthreads();
+        for (int f = 0; f < op.nflip[n]; f++) {
+            const int site = op.flip_sites[op.flip_off[n] + f];
+            const float two_s = bit_up(w.s, site) ? -2.0f : 2.0f;
+            for (int k = net.sptr[site] + threadIdx.x; k < net.sptr[site + 1]; k += blockDim.x) {
+                const int e = net.sq[k];
+                const float2 wv = net.w[0][e];
+                float2* z = z0n + e % size0;
+                atomicAdd(&z->x, two_s * wv.x);
+                atomicAdd(&z->y, two_s * wv.y);
+            }
+            // one site at a time: each unit meets a site once, so the sums do not
+            // depend on the order of the atomic additions
+            __syncthreads();
+        }
+        const float2 lq = forward_from_z0<true>(net, z0n, w);
         const double dr = static_cast<double>(lq.x) - lp.x, di = static_cast<double>(lq.y) - lp.y;
         const double m = exp(dr);
         const double2 e = make_double2(m * (cf.x * cos(di) - cf.y * sin(di)), m * (cf.x * sin(di) + cf.y * cos(di)));
@@ -734,7 +772,7 @@ __global__ void deep_adjoint_kernel(DeepNetDev net, OpDev op, int count, const u
     {
         double2 a = make_double2(-eor, -eoi);
         if (score) a.x += 2.0 * er;
-        forward_once<float2, false, true>(net, w.s, w);
+        forward_from_z0<true>(net, z0s, w);
         pass(w.s, t * xs, make_float2(static_cast<float>(ws * a.x), static_cast<float>(ws * a.y)), score != 0);
         if (score && threadIdx.x == 0) alphaO[t] = make_float2(wsf, 0.f);
     }
@@ -1133,7 +1171,7 @@ int deep_adjoint_chunk(const rbmg_psi* psi, const rbmg_operator* op, const Chunk
     RBMG_CK(xsp.ensure(sizeof(uint64_t) * static_cast<size_t>(chunk) * xs * nw));
     RBMG_CK(dltsO.ensure(sizeof(float2) * static_cast<size_t>(chunk) * net.units));
     RBMG_CK(alphaO.ensure(sizeof(float2) * static_cast<size_t>(chunk)));
-    const size_t sm = smem_for(net, sizeof(float2), true) + sizeof(double2) * std::max(1, op->num_offdiag);
+    const size_t sm = smem_for(net, sizeof(float2), true) + 2 * sizeof(float2) * net.size[0];
     RBMG_CK(set_smem(deep_adjoint_kernel, sm));
     constexpr int kMaxSplits = 64;
     for (int base = 0; base < c.count; base += chunk) {
