@@ -9,6 +9,7 @@
 // coalesced over j ([connectivity][size] layout, as the reference stores them).
 // The backward pass gathers over the rhs connection lists compiled on the host in
 // the reference's order (source/quantum_state/PsiDeep.cu:85-117).
+#include <cstdlib>
 #include <algorithm>
 #include <functional>
 #include <memory>
@@ -515,7 +516,9 @@ __global__ void col_finish_kernel(int P, int splits, const double2* __restrict__
 }
 
 // Metropolis for PsiDeep / PsiPair: one CTA per walker, full forward pass per proposal
-// (PsiDeep.hpp:191-194: angles are not updated incrementally).  Fast sweep
+// (PsiDeep.hpp:191-194: angles are not updated incrementally; single flips of a complex
+// net move layer 0 incrementally here, and run several walkers per CTA in
+// deep_mc_multi_kernel).  Fast sweep
 // (MonteCarloLoop.hpp:162-171): the proposal flips the AND of fast_tries random
 // configurations, N such updates per thermalisation sweep and one per sampling sweep.
 __global__ void deep_mc_kernel(DeepNetDev n0, DeepNetDev n1, int pair, McLaunch L) {
@@ -639,6 +642,208 @@ __global__ void deep_mc_kernel(DeepNetDev n0, DeepNetDev n1, int pair, McLaunch 
         L.rng_index[walker] = rng.index;
         L.accepts[walker] += acc;
         L.proposals[walker] += props;
+    }
+}
+
+// The same chains as deep_mc_kernel's incremental path (a complex net, single-flip
+// proposals, no pair or translation sums), WPC walkers per CTA: one thread per unit
+// evaluates that unit for all WPC walkers, so each weight and connection index read from
+// L1 serves WPC independent multiply-add chains.  Walker k's Philox stream is drawn by
+// thread k alone (site, uniform, start spins) and published through shared memory; every
+// walker's arithmetic is deep_mc_kernel's, in the same order, so spins, accept counts and
+// stream positions are identical.
+// forward_from_z0 for WPC walkers at once: walker k's layer-0 pre-activations are
+// z[(2 k + half_k) * size[0] ...] with half_k = bit k of halves
+template <int WPC>
+__device__ __forceinline__ void forward_multi(const DeepNetDev& net, const float2* z, int halves, float2* in,
+                                              float2* out, float2* red, float lp[WPC]) {
+    const int t = threadIdx.x;
+    const int width = net.width, size0 = net.size[0];
+#pragma unroll
+    for (int k = 0; k < WPC; k++) {
+        const float2* zk = z + (2 * k + ((halves >> k) & 1)) * size0;
+        for (int u = t; u < size0; u += blockDim.x) in[k * width + u] = act<false>(zk[u]);
+    }
+    __syncthreads();
+    for (int l = 1; l < net.L; l++) {
+        const int size = net.size[l], conn = net.conn[l];
+        if (t < size) {
+            const float2* wl = net.w[l];
+            const int* ci = net.cidx[l];
+            float2 a[WPC];
+#pragma unroll
+            for (int k = 0; k < WPC; k++) a[k] = czero<float2>();
+            for (int c = 0; c < conn; c++) {
+                const float2 wv = wl[c * size + t];
+                const int i = ci[c * size + t];
+#pragma unroll
+                for (int k = 0; k < WPC; k++) a[k] = cadd(a[k], cmul(wv, in[k * width + i]));
+            }
+            const float2 bv = net.b[l][t];
+#pragma unroll
+            for (int k = 0; k < WPC; k++) out[k * width + t] = act<false>(cadd(a[k], bv));
+        }
+        __syncthreads();
+        float2* tmp = in;
+        in = out;
+        out = tmp;
+    }
+    // each walker's block_sum of its terms, in block_sum's order
+    const int last = net.size[net.L - 1];
+    const int lane = t & 31, warp = t >> 5, nwarps = (blockDim.x + 31) >> 5;
+    float2 v[WPC];
+#pragma unroll
+    for (int k = 0; k < WPC; k++) {
+        v[k] = t < last ? cmul(in[k * width + t], net.fw[t]) : czero<float2>();
+#pragma unroll
+        for (int off = 16; off >= 1; off >>= 1) {
+            v[k].x += __shfl_xor_sync(0xffffffffu, v[k].x, off);
+            v[k].y += __shfl_xor_sync(0xffffffffu, v[k].y, off);
+        }
+    }
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < WPC; k++) red[k * 32 + warp] = v[k];
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < WPC; k++) {
+        float2 r = czero<float2>();
+        for (int q = 0; q < nwarps; q++) r = cadd(r, red[k * 32 + q]);
+        lp[k] = r.x;
+    }
+}
+
+size_t deep_mc_multi_smem(const DeepNetDev& n, int wpc) {
+    return wpc * (sizeof(float2) * (32 + 2 * n.width + 2 * n.size[0]) + sizeof(uint64_t) * kMaxWords +
+                  2 * sizeof(int));
+}
+
+template <int WPC>
+__global__ void deep_mc_multi_kernel(DeepNetDev n0, McLaunch L) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int width = n0.width, size0 = n0.size[0];
+    float2* red = reinterpret_cast<float2*>(smem);                     // [WPC][32]
+    float2* in = red + WPC * 32;                                       // [WPC][width]
+    float2* out = in + WPC * width;                                    // [WPC][width]
+    float2* zb = out + WPC * width;                                    // [WPC][2][size0]
+    uint64_t* s = reinterpret_cast<uint64_t*>(zb + 2 * WPC * size0);   // [WPC][kMaxWords]
+    int* site_sh = reinterpret_cast<int*>(s + WPC * kMaxWords);        // [WPC]
+    int* flag_sh = site_sh + WPC;                                      // [WPC]
+    const int N = n0.N, nw = (N + 63) / 64;
+    const int first = blockIdx.x * WPC;
+    const int t = threadIdx.x;
+    // thread k < WPC owns walker first + k: its stream, spins updates and counters
+    const int mine = first + t;
+    const bool owner = t < WPC && mine < L.B;
+    WalkerRng rng;
+    unsigned long long acc = 0, props = 0;
+    if (t < WPC) {
+        rng.init(L.seed, L.walker_base + static_cast<uint32_t>(mine), owner ? L.rng_index[mine] : 0);
+        uint64_t* sk = s + t * kMaxWords;
+        for (int k = 0; k < kMaxWords; k++) sk[k] = 0;
+        if (owner) {
+            if (L.init) {
+                for (int k = 0; k < nw; k++) {
+                    const uint64_t lo = rng.next();
+                    const uint64_t hi = rng.next();
+                    sk[k] = lo | (hi << 32);
+                }
+                if (N / 64 < nw) sk[N / 64] &= (1ull << (N % 64)) - 1ull;
+            } else {
+                for (int k = 0; k < nw; k++) sk[k] = L.spins[static_cast<long>(mine) * nw + k];
+            }
+        }
+    }
+    constexpr int kAll = (1 << WPC) - 1;
+    float lpr[WPC], nl[WPC];
+    int cur = 0;   // bit k: the half of walker k's layer-0 pair that holds its state
+    const int total = L.n_therm + L.n_samples * L.sweeps_per_sample;
+    int sample = 0;
+    for (int sw = 0; sw < total; sw++) {
+        // layer 0 and log psi of every state from its spins
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < WPC; k++) layer0_pre(n0, s + k * kMaxWords, zb + (2 * k + ((cur >> k) & 1)) * size0);
+        __syncthreads();
+        forward_multi<WPC>(n0, zb, cur, in, out, red, lpr);
+        for (int p = 0; p < N; p++) {
+            if (owner) site_sh[t] = static_cast<int>(rng.next() % static_cast<uint32_t>(N));
+            // a proposal's layer 0: its state's moved by the flipped spin's connections
+#pragma unroll
+            for (int k = 0; k < WPC; k++) {
+                const int h = (cur >> k) & 1;
+                const float2* src = zb + (2 * k + h) * size0;
+                float2* dst = zb + (2 * k + 1 - h) * size0;
+                for (int u = t; u < size0; u += blockDim.x) dst[u] = src[u];
+            }
+            __syncthreads();
+#pragma unroll
+            for (int k = 0; k < WPC; k++) {
+                if (first + k >= L.B) continue;
+                const int site = site_sh[k];
+                const float two_s = bit_up(s + k * kMaxWords, site) ? -2.0f : 2.0f;
+                float2* dst = zb + (2 * k + 1 - ((cur >> k) & 1)) * size0;
+                for (int q = n0.sptr[site] + t; q < n0.sptr[site + 1]; q += blockDim.x) {
+                    const int e = n0.sq[q];
+                    const float2 wv = n0.w[0][e];
+                    float2* zz = dst + e % size0;
+                    atomicAdd(&zz->x, two_s * wv.x);
+                    atomicAdd(&zz->y, two_s * wv.y);
+                }
+            }
+            __syncthreads();
+            forward_multi<WPC>(n0, zb, cur ^ kAll, in, out, red, nl);
+            if (t < WPC) {
+                float mnl = nl[0], mlp = lpr[0];
+#pragma unroll
+                for (int k = 1; k < WPC; k++)
+                    if (k == t) {
+                        mnl = nl[k];
+                        mlp = lpr[k];
+                    }
+                bool accept = false;
+                if (owner) {
+                    const float delta = mnl - mlp;
+                    accept = delta > 0.0f;
+                    if (!accept) accept = rng.uniform() <= expf_det(2.0f * delta);
+                    if (accept) {
+                        const int site = site_sh[t];
+                        s[t * kMaxWords + (site >> 6)] ^= 1ull << (site & 63);
+                        acc++;
+                    }
+                    props++;
+                }
+                flag_sh[t] = accept ? 1 : 0;
+            }
+            __syncthreads();
+#pragma unroll
+            for (int k = 0; k < WPC; k++)
+                if (flag_sh[k]) {
+                    lpr[k] = nl[k];
+                    cur ^= 1 << k;
+                }
+        }
+        const int done = sw + 1 - L.n_therm;
+        if (done > 0 && done % L.sweeps_per_sample == 0) {
+            const long row0 = static_cast<long>(L.sample_base + sample) * L.B;
+            if (L.sample_spins)
+                for (int i = t; i < WPC * nw; i += blockDim.x) {
+                    const int k = i / nw, word = i % nw;
+                    if (first + k < L.B) L.sample_spins[(row0 + first + k) * nw + word] = s[k * kMaxWords + word];
+                }
+            sample++;
+        }
+    }
+    __syncthreads();
+    for (int i = t; i < WPC * nw; i += blockDim.x) {
+        const int k = i / nw, word = i % nw;
+        if (first + k < L.B) L.spins[static_cast<long>(first + k) * nw + word] = s[k * kMaxWords + word];
+    }
+    if (owner) {
+        L.rng_index[mine] = rng.index;
+        L.accepts[mine] += acc;
+        L.proposals[mine] += props;
     }
 }
 
@@ -1252,6 +1457,17 @@ int deep_stream(rbmg_ensemble* e, const rbmg_psi* psi, const rbmg_operator* op, 
     // + layer 0's pre-activations of the state and of a proposal
     const size_t sm = smem_for(n0, sizeof(float2), false) + 2 * sizeof(float2) * n0.size[0];
     RBMG_CK(set_smem(deep_mc_kernel, sm));
+    // single-flip chains of a complex net: several walkers per CTA (RBMG_DEEP_WALKERS_PER_BLOCK
+    // = 1, 2, 4 or 8; default 8, the fastest on the 100-200-100-50 net), the same chains
+    int wpc = 8;
+    if (const char* v = std::getenv("RBMG_DEEP_WALKERS_PER_BLOCK")) wpc = std::atoi(v);
+    if (wpc != 1 && wpc != 2 && wpc != 4 && wpc != 8) return fail(RBMG_EINVAL, "RBMG_DEEP_WALKERS_PER_BLOCK: 1, 2, 4 or 8");
+    if (e->fast_sweep_tries != 0 || psi->kind == 2 || n0.ti) wpc = 1;
+    const size_t smm = deep_mc_multi_smem(n0, wpc);
+    if (wpc == 2) RBMG_CK(set_smem(deep_mc_multi_kernel<2>, smm));
+    if (wpc == 4) RBMG_CK(set_smem(deep_mc_multi_kernel<4>, smm));
+    if (wpc == 8) RBMG_CK(set_smem(deep_mc_multi_kernel<8>, smm));
+    const int blocks = (B + wpc - 1) / wpc;
     bool first = true;
     for (int row0 = 0; row0 < steps; row0 += rows_per_chunk) {
         const int rows = std::min(rows_per_chunk, steps - row0);
@@ -1268,7 +1484,14 @@ int deep_stream(rbmg_ensemble* e, const rbmg_psi* psi, const rbmg_operator* op, 
         L.sample_spins = samples.as<uint64_t>();
         L.accepts = e->accepts.as<unsigned long long>();
         L.proposals = e->proposals.as<unsigned long long>();
-        deep_mc_kernel<<<B, threads_for(n0), sm, stream()>>>(n0, n1, psi->kind == 2, L);
+        if (wpc == 2)
+            deep_mc_multi_kernel<2><<<blocks, threads_for(n0), smm, stream()>>>(n0, L);
+        else if (wpc == 4)
+            deep_mc_multi_kernel<4><<<blocks, threads_for(n0), smm, stream()>>>(n0, L);
+        else if (wpc == 8)
+            deep_mc_multi_kernel<8><<<blocks, threads_for(n0), smm, stream()>>>(n0, L);
+        else
+            deep_mc_kernel<<<B, threads_for(n0), sm, stream()>>>(n0, n1, psi->kind == 2, L);
         RBMG_CK(cudaGetLastError());
         first = false;
         Chunk c;
