@@ -652,17 +652,25 @@ __global__ void deep_mc_kernel(DeepNetDev n0, DeepNetDev n1, int pair, McLaunch 
 // thread k alone (site, uniform, start spins) and published through shared memory; every
 // walker's arithmetic is deep_mc_kernel's, in the same order, so spins, accept counts and
 // stream positions are identical.
-// forward_from_z0 for WPC walkers at once: walker k's layer-0 pre-activations are
-// z[(2 k + half_k) * size[0] ...] with half_k = bit k of halves
-template <int WPC>
-__device__ __forceinline__ void forward_multi(const DeepNetDev& net, const float2* z, int halves, float2* in,
-                                              float2* out, float2* red, float lp[WPC]) {
+// forward_from_z0 for WPC configurations at once: configuration k's layer-0
+// pre-activations are zof(k)[0 .. size[0]); with STORE its angles and activations go to
+// angles / acts + k * units
+template <int WPC, bool STORE, typename ZOf>
+__device__ __forceinline__ void forward_multi(const DeepNetDev& net, ZOf zof, float2* in, float2* out,
+                                              float2* angles, float2* acts, float2* red, float2 lp[WPC]) {
     const int t = threadIdx.x;
-    const int width = net.width, size0 = net.size[0];
+    const int width = net.width, size0 = net.size[0], units = net.units;
 #pragma unroll
     for (int k = 0; k < WPC; k++) {
-        const float2* zk = z + (2 * k + ((halves >> k) & 1)) * size0;
-        for (int u = t; u < size0; u += blockDim.x) in[k * width + u] = act<false>(zk[u]);
+        const float2* zk = zof(k);
+        for (int u = t; u < size0; u += blockDim.x) {
+            const float2 y = act<false>(zk[u]);
+            if (STORE) {
+                angles[k * units + net.begin_angle[0] + u] = zk[u];
+                acts[k * units + net.begin_angle[0] + u] = y;
+            }
+            in[k * width + u] = y;
+        }
     }
     __syncthreads();
     for (int l = 1; l < net.L; l++) {
@@ -681,14 +689,22 @@ __device__ __forceinline__ void forward_multi(const DeepNetDev& net, const float
             }
             const float2 bv = net.b[l][t];
 #pragma unroll
-            for (int k = 0; k < WPC; k++) out[k * width + t] = act<false>(cadd(a[k], bv));
+            for (int k = 0; k < WPC; k++) {
+                const float2 z = cadd(a[k], bv);
+                const float2 y = act<false>(z);
+                if (STORE) {
+                    angles[k * units + net.begin_angle[l] + t] = z;
+                    acts[k * units + net.begin_angle[l] + t] = y;
+                }
+                out[k * width + t] = y;
+            }
         }
         __syncthreads();
         float2* tmp = in;
         in = out;
         out = tmp;
     }
-    // each walker's block_sum of its terms, in block_sum's order
+    // each configuration's block_sum of its terms, in block_sum's order
     const int last = net.size[net.L - 1];
     const int lane = t & 31, warp = t >> 5, nwarps = (blockDim.x + 31) >> 5;
     float2 v[WPC];
@@ -710,7 +726,7 @@ __device__ __forceinline__ void forward_multi(const DeepNetDev& net, const float
     for (int k = 0; k < WPC; k++) {
         float2 r = czero<float2>();
         for (int q = 0; q < nwarps; q++) r = cadd(r, red[k * 32 + q]);
-        lp[k] = r.x;
+        lp[k] = r;
     }
 }
 
@@ -755,8 +771,8 @@ __global__ void deep_mc_multi_kernel(DeepNetDev n0, McLaunch L) {
             }
         }
     }
-    constexpr int kAll = (1 << WPC) - 1;
-    float lpr[WPC], nl[WPC];
+    float lpr[WPC];
+    float2 nl[WPC], lp0[WPC];
     int cur = 0;   // bit k: the half of walker k's layer-0 pair that holds its state
     const int total = L.n_therm + L.n_samples * L.sweeps_per_sample;
     int sample = 0;
@@ -766,7 +782,10 @@ __global__ void deep_mc_multi_kernel(DeepNetDev n0, McLaunch L) {
 #pragma unroll
         for (int k = 0; k < WPC; k++) layer0_pre(n0, s + k * kMaxWords, zb + (2 * k + ((cur >> k) & 1)) * size0);
         __syncthreads();
-        forward_multi<WPC>(n0, zb, cur, in, out, red, lpr);
+        forward_multi<WPC, false>(n0, [&](int k) { return zb + (2 * k + ((cur >> k) & 1)) * size0; }, in, out,
+                                  nullptr, nullptr, red, lp0);
+#pragma unroll
+        for (int k = 0; k < WPC; k++) lpr[k] = lp0[k].x;
         for (int p = 0; p < N; p++) {
             if (owner) site_sh[t] = static_cast<int>(rng.next() % static_cast<uint32_t>(N));
             // a proposal's layer 0: its state's moved by the flipped spin's connections
@@ -793,13 +812,14 @@ __global__ void deep_mc_multi_kernel(DeepNetDev n0, McLaunch L) {
                 }
             }
             __syncthreads();
-            forward_multi<WPC>(n0, zb, cur ^ kAll, in, out, red, nl);
+            forward_multi<WPC, false>(n0, [&](int k) { return zb + (2 * k + 1 - ((cur >> k) & 1)) * size0; }, in,
+                                      out, nullptr, nullptr, red, nl);
             if (t < WPC) {
-                float mnl = nl[0], mlp = lpr[0];
+                float mnl = nl[0].x, mlp = lpr[0];
 #pragma unroll
                 for (int k = 1; k < WPC; k++)
                     if (k == t) {
-                        mnl = nl[k];
+                        mnl = nl[k].x;
                         mlp = lpr[k];
                     }
                 bool accept = false;
@@ -820,7 +840,7 @@ __global__ void deep_mc_multi_kernel(DeepNetDev n0, McLaunch L) {
 #pragma unroll
             for (int k = 0; k < WPC; k++)
                 if (flag_sh[k]) {
-                    lpr[k] = nl[k];
+                    lpr[k] = nl[k].x;
                     cur ^= 1 << k;
                 }
         }
@@ -981,6 +1001,195 @@ __global__ void deep_adjoint_kernel(DeepNetDev net, OpDev op, int count, const u
         pass(w.s, t * xs, make_float2(static_cast<float>(ws * a.x), static_cast<float>(ws * a.y)), score != 0);
         if (score && threadIdx.x == 0) alphaO[t] = make_float2(wsf, 0.f);
     }
+    if (threadIdx.x == 0) eloc[t] = make_double2(er, ei);
+}
+
+// backward_deltas for NB configurations at once (configuration k's angles at angles +
+// k * units, its error buffers at cur / nxt + k * width); emit(k, layer, unit, delta) for
+// k < nb
+template <int NB, typename Emit>
+__device__ void backward_multi(const DeepNetDev& net, const float2* angles, float2* cur, float2* nxt, int nb,
+                               Emit emit) {
+    const int t = threadIdx.x;
+    const int L = net.L, width = net.width, units = net.units;
+    for (int l = L - 1; l >= 0; l--) {
+        const int size = net.size[l];
+        float2 d[NB];
+#pragma unroll
+        for (int k = 0; k < NB; k++) d[k] = czero<float2>();
+        if (t < size) {
+            const int at = net.begin_angle[l] + t;
+            if (l == L - 1) {
+                const float2 f = net.fw[t];
+#pragma unroll
+                for (int k = 0; k < NB; k++) d[k] = cmul(f, dact<false>(angles[k * units + at]));
+            } else {
+                const int nsize = net.size[l + 1];
+                float2 acc[NB];
+#pragma unroll
+                for (int k = 0; k < NB; k++) acc[k] = czero<float2>();
+                const float2* wn = net.w[l + 1];
+                for (int e = net.rptr[l][t]; e < net.rptr[l][t + 1]; e++) {
+                    const int q = net.rq[l][e];
+                    const float2 wv = wn[q];
+                    const int j = q % nsize;
+#pragma unroll
+                    for (int k = 0; k < NB; k++) acc[k] = cadd(acc[k], cmul(wv, nxt[k * width + j]));
+                }
+#pragma unroll
+                for (int k = 0; k < NB; k++) d[k] = cmul(acc[k], dact<false>(angles[k * units + at]));
+            }
+        }
+        __syncthreads();
+        if (t < size)
+#pragma unroll
+            for (int k = 0; k < NB; k++) {
+                cur[k * width + t] = d[k];
+                if (k < nb) emit(k, l, t, d[k]);
+            }
+        __syncthreads();
+        float2* tmp = cur;
+        cur = nxt;
+        nxt = tmp;
+    }
+}
+
+size_t deep_adjoint_multi_smem(const DeepNetDev& n, int nb) {
+    return sizeof(float2) * (nb * (32 + 2 * n.width + 2 * n.units + n.size[0]) + n.size[0]) +
+           sizeof(uint64_t) * (1 + nb) * kMaxWords;
+}
+
+// deep_adjoint_kernel with the off-diagonal neighbours of a sample taken NB at a time: the
+// thread of a unit evaluates it (forward and reverse) for all NB neighbours, so each weight
+// read serves NB chains.  Every configuration's arithmetic and the local energy's order of
+// summation are deep_adjoint_kernel's: the outputs are identical.
+template <int NB>
+__global__ void deep_adjoint_multi_kernel(DeepNetDev net, OpDev op, int count, const uint64_t* spins,
+                                          uint64_t enum_base, int enumerate, const double* weights, int score,
+                                          double2* eloc, float2* acts, float2* dlts, float2* alpha, uint64_t* xspins,
+                                          int xs, float2* dltsO, float2* alphaO) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int width = net.width, size0 = net.size[0], units = net.units;
+    float2* red = reinterpret_cast<float2*>(smem);                   // [NB][32]
+    float2* in = red + NB * 32;                                      // [NB][width]
+    float2* out = in + NB * width;                                   // [NB][width]
+    float2* angles = out + NB * width;                               // [NB][units]
+    float2* actsb = angles + NB * units;                             // [NB][units]
+    float2* z0s = actsb + NB * units;                                // [size0] the sample's layer 0
+    float2* z0n = z0s + size0;                                       // [NB][size0] the neighbours'
+    uint64_t* s = reinterpret_cast<uint64_t*>(z0n + NB * size0);     // [kMaxWords] the sample
+    uint64_t* sp = s + kMaxWords;                                    // [NB][kMaxWords] the neighbours
+    const long t = blockIdx.x;
+    if (t >= count) return;
+    const int nw = (net.N + 63) / 64;
+    load_config(spins, enum_base, enumerate, t, net.N, s);
+    __syncthreads();
+    layer0_pre(net, s, z0s);
+    __syncthreads();
+    auto self_z = [&](int) { return static_cast<const float2*>(z0s); };
+    float2 lp1[1];
+    forward_multi<1, false>(net, self_z, in, out, nullptr, nullptr, red, lp1);
+    const float2 lp = lp1[0];
+    double er = 0.0, ei = 0.0, eor = 0.0, eoi = 0.0;
+    for (int n = 0; n < op.S; n++) {
+        if (op.nflip[n] != 0) continue;
+        const double2 cf = apply_string(op, n, s, sp);
+        er += cf.x;
+        ei += cf.y;
+    }
+    const double ws = weights ? weights[t] : 1.0;
+    const float wsf = static_cast<float>(ws);
+    int q = 0;   // neighbours done
+    int n = 0;   // next string to scan
+    for (;;) {
+        // the next (up to) NB off-diagonal strings, their neighbours' spins and coefficients
+        double2 cf[NB];
+        int ns[NB];
+        int nb = 0;
+#pragma unroll
+        for (int k = 0; k < NB; k++) {
+            while (n < op.S && op.nflip[n] == 0) n++;
+            ns[k] = -1;
+            cf[k] = make_double2(0.0, 0.0);
+            if (n < op.S) {
+                cf[k] = apply_string(op, n, s, sp + k * kMaxWords);
+                ns[k] = n;
+                nb = k + 1;
+                n++;
+            }
+        }
+        if (nb == 0) break;
+        // each neighbour's layer 0: the sample's moved by the flipped spins' connections
+        for (int i = threadIdx.x; i < NB * size0; i += blockDim.x) z0n[i] = z0s[i % size0];
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < NB; k++) {
+            if (k >= nb) break;
+            const int m = ns[k];
+            for (int f = 0; f < op.nflip[m]; f++) {
+                const int site = op.flip_sites[op.flip_off[m] + f];
+                const float two_s = bit_up(s, site) ? -2.0f : 2.0f;
+                for (int e = net.sptr[site] + threadIdx.x; e < net.sptr[site + 1]; e += blockDim.x) {
+                    const int c = net.sq[e];
+                    const float2 wv = net.w[0][c];
+                    float2* z = z0n + k * size0 + c % size0;
+                    atomicAdd(&z->x, two_s * wv.x);
+                    atomicAdd(&z->y, two_s * wv.y);
+                }
+                // one site at a time: each unit meets a site once, so the sums do not
+                // depend on the order of the atomic additions
+                __syncthreads();
+            }
+        }
+        float2 lq[NB];
+        forward_multi<NB, true>(net, [&](int k) { return static_cast<const float2*>(z0n + k * size0); }, in, out,
+                                angles, actsb, red, lq);
+        float2 af[NB];
+#pragma unroll
+        for (int k = 0; k < NB; k++) {
+            af[k] = make_float2(0.f, 0.f);
+            if (k < nb) {
+                const double dr = static_cast<double>(lq[k].x) - lp.x, di = static_cast<double>(lq[k].y) - lp.y;
+                const double mg = exp(dr);
+                const double2 e = make_double2(mg * (cf[k].x * cos(di) - cf[k].y * sin(di)),
+                                               mg * (cf[k].x * sin(di) + cf[k].y * cos(di)));
+                eor += e.x;
+                eoi += e.y;
+                af[k] = make_float2(static_cast<float>(ws * e.x), static_cast<float>(ws * e.y));
+            }
+        }
+        // stored activations, spins and weights of the neighbours, then their reverse passes
+        const long x0 = t * xs + q + 1;
+        for (int i = threadIdx.x; i < nb * units; i += blockDim.x)
+            acts[(x0 + i / units) * units + i % units] = actsb[i];
+        for (int i = threadIdx.x; i < nb * nw; i += blockDim.x)
+            xspins[(x0 + i / nw) * nw + i % nw] = sp[(i / nw) * kMaxWords + i % nw];
+        if (threadIdx.x < nb)
+#pragma unroll
+            for (int k = 0; k < NB; k++)
+                if (k == static_cast<int>(threadIdx.x)) alpha[x0 + k] = af[k];
+        backward_multi<NB>(net, angles, in, out, nb, [&](int k, int l, int j, float2 d) {
+            dlts[(x0 + k) * units + net.begin_angle[l] + j] = cmul(af[k], d);
+        });
+        q += nb;
+    }
+    er += eor;
+    ei += eoi;
+    // the configuration itself last: its coefficient -sum_n e_n (+ 2 E_loc with the
+    // sampling term) needs every neighbour's term
+    double2 a = make_double2(-eor, -eoi);
+    if (score) a.x += 2.0 * er;
+    const float2 afs = make_float2(static_cast<float>(ws * a.x), static_cast<float>(ws * a.y));
+    forward_multi<1, true>(net, self_z, in, out, angles, actsb, red, lp1);
+    const long xi = t * xs;
+    for (int i = threadIdx.x; i < units; i += blockDim.x) acts[xi * units + i] = actsb[i];
+    if (threadIdx.x < nw) xspins[xi * nw + threadIdx.x] = s[threadIdx.x];
+    if (threadIdx.x == 0) alpha[xi] = afs;
+    backward_multi<1>(net, angles, in, out, 1, [&](int, int l, int j, float2 d) {
+        dlts[xi * units + net.begin_angle[l] + j] = cmul(afs, d);
+        if (score) dltsO[t * units + net.begin_angle[l] + j] = make_float2(wsf * d.x, wsf * d.y);
+    });
+    if (score && threadIdx.x == 0) alphaO[t] = make_float2(wsf, 0.f);
     if (threadIdx.x == 0) eloc[t] = make_double2(er, ei);
 }
 
@@ -1378,14 +1587,34 @@ int deep_adjoint_chunk(const rbmg_psi* psi, const rbmg_operator* op, const Chunk
     RBMG_CK(alphaO.ensure(sizeof(float2) * static_cast<size_t>(chunk)));
     const size_t sm = smem_for(net, sizeof(float2), true) + 2 * sizeof(float2) * net.size[0];
     RBMG_CK(set_smem(deep_adjoint_kernel, sm));
+    // neighbours per pass of the reverse kernel (RBMG_DEEP_ADJOINT_BATCH = 1, 2 or 4;
+    // default 4), the same outputs
+    int nbatch = 4;
+    if (const char* v = std::getenv("RBMG_DEEP_ADJOINT_BATCH")) nbatch = std::atoi(v);
+    if (nbatch != 1 && nbatch != 2 && nbatch != 4) return fail(RBMG_EINVAL, "RBMG_DEEP_ADJOINT_BATCH: 1, 2 or 4");
+    const size_t smb = deep_adjoint_multi_smem(net, nbatch);
+    if (nbatch == 2) RBMG_CK(set_smem(deep_adjoint_multi_kernel<2>, smb));
+    if (nbatch == 4) RBMG_CK(set_smem(deep_adjoint_multi_kernel<4>, smb));
     constexpr int kMaxSplits = 64;
     for (int base = 0; base < c.count; base += chunk) {
         const int cnt = std::min(chunk, c.count - base);
         const uint64_t* sp = c.spins ? c.spins + static_cast<size_t>(base) * nw : nullptr;
-        deep_adjoint_kernel<<<cnt, threads_for(net), sm, st>>>(
-            net, op->dev(), cnt, sp, c.enum_base + base, c.enumerate, c.weights ? c.weights + base : nullptr, score,
-            d_eloc + base, acts.as<float2>(), dlts.as<float2>(), alpha.as<float2>(), xsp.as<uint64_t>(), xs,
-            dltsO.as<float2>(), alphaO.as<float2>());
+        const double* wb = c.weights ? c.weights + base : nullptr;
+        if (nbatch == 4)
+            deep_adjoint_multi_kernel<4><<<cnt, threads_for(net), smb, st>>>(
+                net, op->dev(), cnt, sp, c.enum_base + base, c.enumerate, wb, score, d_eloc + base,
+                acts.as<float2>(), dlts.as<float2>(), alpha.as<float2>(), xsp.as<uint64_t>(), xs, dltsO.as<float2>(),
+                alphaO.as<float2>());
+        else if (nbatch == 2)
+            deep_adjoint_multi_kernel<2><<<cnt, threads_for(net), smb, st>>>(
+                net, op->dev(), cnt, sp, c.enum_base + base, c.enumerate, wb, score, d_eloc + base,
+                acts.as<float2>(), dlts.as<float2>(), alpha.as<float2>(), xsp.as<uint64_t>(), xs, dltsO.as<float2>(),
+                alphaO.as<float2>());
+        else
+            deep_adjoint_kernel<<<cnt, threads_for(net), sm, st>>>(
+                net, op->dev(), cnt, sp, c.enum_base + base, c.enumerate, wb, score, d_eloc + base,
+                acts.as<float2>(), dlts.as<float2>(), alpha.as<float2>(), xsp.as<uint64_t>(), xs, dltsO.as<float2>(),
+                alphaO.as<float2>());
         RBMG_CK(cudaGetLastError());
         // reduce over K configurations whose rows are `stride` configurations apart
         auto reduce = [&](int K, int amode, int M, int Nn, const float2* D, int ldd, const float2* A, int lda, int xld,
