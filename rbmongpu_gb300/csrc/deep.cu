@@ -1587,20 +1587,27 @@ int deep_adjoint_chunk(const rbmg_psi* psi, const rbmg_operator* op, const Chunk
     RBMG_CK(alphaO.ensure(sizeof(float2) * static_cast<size_t>(chunk)));
     const size_t sm = smem_for(net, sizeof(float2), true) + 2 * sizeof(float2) * net.size[0];
     RBMG_CK(set_smem(deep_adjoint_kernel, sm));
-    // neighbours per pass of the reverse kernel (RBMG_DEEP_ADJOINT_BATCH = 1, 2 or 4;
+    // neighbours per pass of the reverse kernel (RBMG_DEEP_ADJOINT_BATCH = 1, 2, 4 or 8;
     // default 4), the same outputs
     int nbatch = 4;
     if (const char* v = std::getenv("RBMG_DEEP_ADJOINT_BATCH")) nbatch = std::atoi(v);
-    if (nbatch != 1 && nbatch != 2 && nbatch != 4) return fail(RBMG_EINVAL, "RBMG_DEEP_ADJOINT_BATCH: 1, 2 or 4");
+    if (nbatch != 1 && nbatch != 2 && nbatch != 4 && nbatch != 8)
+        return fail(RBMG_EINVAL, "RBMG_DEEP_ADJOINT_BATCH: 1, 2, 4 or 8");
     const size_t smb = deep_adjoint_multi_smem(net, nbatch);
     if (nbatch == 2) RBMG_CK(set_smem(deep_adjoint_multi_kernel<2>, smb));
     if (nbatch == 4) RBMG_CK(set_smem(deep_adjoint_multi_kernel<4>, smb));
+    if (nbatch == 8) RBMG_CK(set_smem(deep_adjoint_multi_kernel<8>, smb));
     constexpr int kMaxSplits = 64;
     for (int base = 0; base < c.count; base += chunk) {
         const int cnt = std::min(chunk, c.count - base);
         const uint64_t* sp = c.spins ? c.spins + static_cast<size_t>(base) * nw : nullptr;
         const double* wb = c.weights ? c.weights + base : nullptr;
-        if (nbatch == 4)
+        if (nbatch == 8)
+            deep_adjoint_multi_kernel<8><<<cnt, threads_for(net), smb, st>>>(
+                net, op->dev(), cnt, sp, c.enum_base + base, c.enumerate, wb, score, d_eloc + base,
+                acts.as<float2>(), dlts.as<float2>(), alpha.as<float2>(), xsp.as<uint64_t>(), xs, dltsO.as<float2>(),
+                alphaO.as<float2>());
+        else if (nbatch == 4)
             deep_adjoint_multi_kernel<4><<<cnt, threads_for(net), smb, st>>>(
                 net, op->dev(), cnt, sp, c.enum_base + base, c.enumerate, wb, score, d_eloc + base,
                 acts.as<float2>(), dlts.as<float2>(), alpha.as<float2>(), xsp.as<uint64_t>(), xs, dltsO.as<float2>(),

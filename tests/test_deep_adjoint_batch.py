@@ -1,4 +1,4 @@
-"""The PsiDeep adjoint kernel taking a sample's neighbours two or four at a time against
+"""The PsiDeep adjoint kernel taking a sample's neighbours two, four or eight at a time against
 the kernel taking them one at a time: every configuration's arithmetic and the local
 energy's order of summation are the same, so the gradient and <E_loc> are identical, with
 and without the sampling term, on Monte Carlo samples and on exact summation, for
@@ -40,7 +40,7 @@ def gradient(psi, op, ens, score, batch):
 
 
 @pytest.mark.parametrize("score", [False, True])
-@pytest.mark.parametrize("batch", [2, 4])
+@pytest.mark.parametrize("batch", [2, 4, 8])
 def test_tfim_n70_monte_carlo(batch, score):
     psi = dense_net(70, (90, 40, 20), 41)
     op = rg.Operator(*rg.operators.tfim_chain(70, 1.0, 0.8))
@@ -50,7 +50,7 @@ def test_tfim_n70_monte_carlo(batch, score):
     assert np.array_equal(g1, gb) and E1 == Eb
 
 
-@pytest.mark.parametrize("batch", [2, 4])
+@pytest.mark.parametrize("batch", [2, 4, 8])
 def test_sparse_net_exact_summation_heisenberg(batch):
     c = Case("deep8_sparse")
     b, cn, w, fw = c.deep("")
