@@ -688,11 +688,13 @@ def run_deep(args):
         "eloc_per_s": DEEP_WALKERS / sec,
         "e2e": {"value": DEEP_WALKERS / e2e_s, "unit": "samples/s", "h2d_bytes_per_step": 16 * P,
                 "d2h_bytes_per_step": 16 * P},
-        "gpu_launches": None,
+        # per gradient call of this workload (its launch list): the sampler, 6 adjoint chunks,
+        # 84 outer-product reductions, 84 split sums and the 2 weighted-mean launches
+        "gpu_launches": 177 * K,
         "roofline": {"bound": "fp32", "achieved": flops / sec / 1e12, "peak": v, "unit": "TFLOP/s",
                      "frac": flops / sec / 1e12 / v if v else None, "traffic": None,
                      "peak_source": "measured in this run by the library's FP32 FMA probe kernel",
-                     "kernel": "deep_mc_kernel + deep_adjoint_kernel + adj_cgemm_kernel (the whole step)",
+                     "kernel": "deep_mc_multi_kernel + deep_adjoint_multi_kernel + adj_cgemm_kernel (the whole step)",
                      "flops_per_step": flops},
         "cpu_baseline": cpu,
         "clocks": clk,
