@@ -58,9 +58,9 @@ RBMG_API int rbmg_activation(double re, double im, double* out /* [2] */);
 
 /* ---------------------------------------------------------------- Psi (RBM)
  * Psi(alpha, beta, b, W, prefactor, free_quantum_axis, gpu)
- * (include/quantum_state/Psi.hpp:361-378, pyRBMonGPU/main.cpp:50-59).
+ * (include/quantum_state/Psi.hpp:220-238, pyRBMonGPU/main.cpp:50-59).
  * alpha, beta: [N] real; b: [M] complex; W: [N, M] complex row-major.
- * Like the reference (include/quantum_state/PsiBase.hpp:239-249) beta is
+ * Like the reference (include/quantum_state/PsiBase.hpp:168-178, 183-192) beta is
  * initialised from alpha.  free_quantum_axis != 0 returns RBMG_EUNSUPPORTED. */
 RBMG_API int rbmg_psi_create(int N, int M, const double* alpha, const double* beta, const double* b, const double* W,
                     double prefactor, int free_quantum_axis, rbmg_psi** out);
@@ -84,7 +84,7 @@ RBMG_API int rbmg_psi_destroy(rbmg_psi* psi);
 
 /* psi kind: 0 Psi, 1 PsiDeep, 2 PsiPair */
 RBMG_API int rbmg_psi_kind(const rbmg_psi* psi, int* kind);
-/* N, M (RBM) or width (deep), num_params (Psi.hpp:372, PsiDeep.cu:34-66) */
+/* N, M (RBM) or width (deep), num_params (include/quantum_state/Psi.hpp:233, PsiDeep.cu:34-66) */
 RBMG_API int rbmg_psi_shape(const rbmg_psi* psi, int* N, int* M, int* num_params);
 /* params getter / setter, layout [alpha(N), beta(N), ...] (Psi.cu:71-92, PsiDeep.cu:120-177,
  * PsiPair.cu:34-76); values cross as complex128, the device holds complex64. */
@@ -112,7 +112,7 @@ RBMG_API int rbmg_psi_O_k_vector(const rbmg_psi* psi, const uint64_t* spins, dou
 
 /* ---------------------------------------------------------------- Operator
  * Operator(coefficients[S], pauli_types[S, L], pauli_indices[S, L], gpu)
- * (include/operator/Operator.hpp:394-409, pyRBMonGPU/main.cpp:240-245): types
+ * (include/operator/Operator.hpp:212-227, pyRBMonGPU/main.cpp:240-245): types
  * 0 = I, 1 = X, 2 = Y, 3 = Z; an index of -1 ends a string. */
 RBMG_API int rbmg_operator_create(int num_strings, int max_string_length, const double* coefficients, const int* pauli_types,
                          const int* pauli_indices, rbmg_operator** out);
@@ -151,6 +151,11 @@ RBMG_API int rbmg_exact_set_total_z_symmetry(rbmg_ensemble* exact, int sector);
 /* num_steps (main.cpp:281, 291) */
 RBMG_API int rbmg_ensemble_num_steps(const rbmg_ensemble* ens, uint64_t* num_steps);
 RBMG_API int rbmg_ensemble_destroy(rbmg_ensemble* ens);
+/* Extension (no reference counterpart; the reference's ensembles always sample or enumerate):
+ * a fixed set of `count` configurations, spins [count][ceil(N/64)], each with weight 1 / count,
+ * as a MonteCarloLoop pass that produced them (rbmg_ensemble_samples).  Every estimator
+ * accepts it, e.g. the gradient of an energy estimated earlier, on the same samples. */
+RBMG_API int rbmg_samples_create(uint32_t num_spins, uint32_t count, const uint64_t* spins, rbmg_ensemble** out);
 
 /* Runs the ensemble's foreach (MonteCarloLoop.hpp:294-339) and records, per sample
  * index (step * chains + chain), the configuration, log psi and local energy.
@@ -265,8 +270,10 @@ RBMG_API int rbmg_chain_state(const rbmg_chain* chain, uint64_t* spins, uint64_t
 /* the library's CUDA stream of the calling thread, as a cudaStream_t */
 RBMG_API int rbmg_stream(void** stream);
 
-/* <op> under ExactSummation(num_spins) for a complex RBM -- the value rbmg_ev_value returns
- * for an ExactSummation ensemble -- computed without allocating any device memory.
+/* <op> under ExactSummation(num_spins) for a complex RBM, computed without allocating any
+ * device memory.  It agrees with rbmg_ev_value on an ExactSummation ensemble to within
+ * 1e-5 relative, not bit for bit: log psi is evaluated in FP64 from the device's FP32
+ * (complex64) parameters, while rbmg_ev_value's exact path uses the FP64 parameters.
  * No counterpart in the reference: it is for callers that cannot call cudaMalloc, such as a
  * framework that owns all device memory through its own pool, or a latency-critical loop
  * that cannot afford the device-wide synchronisation of cudaFree.
@@ -274,8 +281,10 @@ RBMG_API int rbmg_stream(void** stream);
  * the library until the process exits; it limits num_spins to 14 (larger sizes return
  * RBMG_EINVAL).  The first call on a device looks up the array's address with
  * cudaGetSymbolAddress (set-up done once per device, on the current device), so make that
- * first call before any stream capture.  Every call uses
- * the same array: calls that overlap on the GPU (other host threads, other streams) race. */
+ * first call before any stream capture.  Each call returns once the result is on the host.
+ * Every call uses the same array and clears the sums it accumulates; calls that overlap on
+ * the GPU (other host threads, other streams) race.  After a cudaDeviceReset the cached
+ * address is stale: do not call it on a device that was reset. */
 RBMG_API int rbmg_ev_value_exact_noalloc(const rbmg_psi* psi, const rbmg_operator* op, int num_spins,
                                          double* value /* [2] */);
 
@@ -285,7 +294,8 @@ RBMG_API int rbmg_ev_value_exact_noalloc(const rbmg_psi* psi, const rbmg_operato
  * contiguous cluster {i, ..., i+l-1}; the Metropolis-Hastings ratio includes the forward and
  * reverse proposal densities, so the chain's stationary law stays |psi|^2 (the step of
  * include/spin_ensembles/MonteCarloLoop.hpp:153-256 with a different proposal).  The net
- * is trained online by REINFORCE (reward min(1, a) * l) with Adam. */
+ * is trained online with Adam, by default on the cross-entropy to the locally balanced
+ * proposal over all cluster moves (rbmg_proposal_set_objective selects the objective). */
 typedef struct rbmg_proposal rbmg_proposal;
 RBMG_API int rbmg_proposal_create(int N, uint64_t seed, float lr, rbmg_proposal** out);
 RBMG_API int rbmg_proposal_destroy(rbmg_proposal* proposal);

@@ -91,7 +91,7 @@ uint32_t or_philox_word(uint64_t seed, uint32_t walker, uint64_t index) {
 }
 
 /* MT19937, Matsumoto & Nishimura (1998): the engine the reference's host path uses
- * (std::mt19937(i), source/spin_ensembles/MonteCarloLoop.cu:437-440). */
+ * (std::mt19937(i), source/spin_ensembles/MonteCarloLoop.cu:89-92). */
 typedef struct { uint32_t mt[624]; int idx; } mt19937;
 
 static void mt_seed(mt19937* g, uint32_t seed) {
@@ -568,7 +568,7 @@ static inline void index_spins(uint64_t idx, int N, uint64_t* s) {   /* Spins_t<
     s[0] = N >= 64 ? idx : (idx & (((uint64_t)1 << N) - 1u));
 }
 
-static inline double ref_weight(const or_psi* psi, cd lp) {          /* probability_s, Psi.hpp:272-275 */
+static inline double ref_weight(const or_psi* psi, cd lp) {          /* probability_s, include/quantum_state/Psi.hpp:134-137 */
     return exp(2.0 * (log(psi->prefactor) + lp.re));
 }
 

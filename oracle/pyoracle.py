@@ -271,7 +271,7 @@ def E_k(psi, op, spins, lp=None):
 
 def exact_configs(psi):
     """Every configuration of N <= 16 spins with the reference's ExactSummation weight
-    prefactor^2 |psi(s)|^2 (Psi.hpp:272-275); averages are sums of weight x value (its
+    prefactor^2 |psi(s)|^2 (include/quantum_state/Psi.hpp:134-137); averages are sums of weight x value (its
     get_num_steps is 1)."""
     s = np.arange(2 ** psi.N, dtype=np.uint64)[:, None]
     lp = np.array([log_psi(psi, x) for x in s])

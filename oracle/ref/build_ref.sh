@@ -5,7 +5,12 @@
 # the reference's translation units contain it.  Outputs go to oracle/_ref only.
 set -e
 HERE=$(cd "$(dirname "$0")/.." && pwd)
-REF=${REF_SRC:-/root/reference}
+# the RBMonGPU checkout: first argument, else $RBMONGPU_REF; nothing to do without one
+REF=${1:-$RBMONGPU_REF}
+if [ -z "$REF" ] || [ ! -d "$REF/source" ]; then
+  echo "build_ref.sh: no RBMonGPU sources given (argument or RBMONGPU_REF); reference harness not built"
+  exit 0
+fi
 OUT="$HERE/_ref"
 NVCC=${NVCC:-nvcc}
 FLAGS="-std=c++14 -O2 --expt-extended-lambda -gencode arch=compute_100,code=sm_100 \

@@ -60,6 +60,7 @@ SIGNATURES = {
     "rbmg_mc_set_fast_sweep": [_vp, C.c_uint32],
     "rbmg_mc_acceptance": [_vp, _u64p, _u64p, _u64p],
     "rbmg_exact_create": [C.c_uint32, _vpp],
+    "rbmg_samples_create": [C.c_uint32, C.c_uint32, _u64p, _vpp],
     "rbmg_exact_set_total_z_symmetry": [_vp, C.c_int],
     "rbmg_ensemble_num_steps": [_vp, _u64p],
     "rbmg_ensemble_destroy": [_vp],

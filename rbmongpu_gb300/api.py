@@ -194,7 +194,7 @@ class _PsiBase:
 
     @property
     def vector(self):
-        # alpha / beta rotations of pyRBMonGPU/Psi.py:88-100 need QuantumExpression; with the
+        # alpha / beta rotations of pyRBMonGPU/Psi.py:62-74 need QuantumExpression; with the
         # free quantum axis unsupported they are zero and the vector is the plain amplitude list
         return self._vector()
 
@@ -243,7 +243,7 @@ class _PsiBase:
 
 class Psi(_PsiBase):
     """Complex RBM: Psi(alpha, beta, b, W, prefactor, free_quantum_axis, gpu)
-    (include/quantum_state/Psi.hpp:361-378)."""
+    (include/quantum_state/Psi.hpp:220-238)."""
 
     def __init__(self, alpha, beta, b, W, prefactor=1.0, free_quantum_axis=False, gpu=True):
         b = _c128(b)
@@ -420,7 +420,7 @@ PsiPair.from_json = staticmethod(lambda obj, gpu=True: _deep_from_json(PsiPair, 
 
 # --------------------------------------------------------------------- operator
 class Operator:
-    """Pauli-string sum as the reference's padded table (include/operator/Operator.hpp:394-409).
+    """Pauli-string sum as the reference's padded table (include/operator/Operator.hpp:212-227).
 
     Operator(coefficients[S], pauli_types[S, L], pauli_indices[S, L], gpu); types 0=I 1=X 2=Y 3=Z,
     index -1 ends a string.  An object with a ``to_table()`` method returning the same three
@@ -504,16 +504,18 @@ class _Ensemble:
         call("rbmg_ensemble_num_steps", self._h, C.byref(n))
         return n.value
 
-    def samples(self, psi, operator=None):
-        """(spins words [num_steps, nwords], log psi [num_steps], E_loc or None) of one foreach pass."""
+    def samples(self, psi, operator=None, log_psi=True):
+        """(spins words [num_steps, nwords], log psi [num_steps] or None, E_loc or None) of one
+        foreach pass."""
         n = self.num_steps
         nw = nwords(psi.N)
         sp = np.zeros((n, nw), np.uint64)
-        lp = np.zeros(2 * n)
+        lp = np.zeros(2 * n) if log_psi else None
         el = np.zeros(2 * n) if operator is not None else None
         call("rbmg_ensemble_samples", self._h, psi._h, operator._h if operator is not None else None,
-             _p(sp, _u64p), _p(lp), _p(el) if el is not None else None)
-        return sp, lp.view(np.complex128), (el.view(np.complex128) if el is not None else None)
+             _p(sp, _u64p), _p(lp) if lp is not None else None, _p(el) if el is not None else None)
+        return (sp, lp.view(np.complex128) if lp is not None else None,
+                el.view(np.complex128) if el is not None else None)
 
 
 class MonteCarloLoop(_Ensemble):
@@ -557,6 +559,18 @@ class ExactSummation(_Ensemble):
 
     def set_total_z_symmetry(self, sector):
         call("rbmg_exact_set_total_z_symmetry", self._h, int(sector))
+
+
+class FixedSamples(_Ensemble):
+    """Extension: a fixed set of configurations (spins words [count, nwords]), each with
+    weight 1 / count, e.g. the samples of an earlier MonteCarloLoop pass
+    (`ensemble.samples(psi)`); every estimator accepts it."""
+
+    def __init__(self, num_spins, spins_words):
+        w = np.ascontiguousarray(spins_words, np.uint64).reshape(-1, nwords(num_spins))
+        h = _handle()
+        call("rbmg_samples_create", int(num_spins), len(w), _p(w, _u64p), C.byref(h))
+        self._h = h
 
 
 # --------------------------------------------------------------------- reductions

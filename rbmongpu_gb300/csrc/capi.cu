@@ -78,6 +78,7 @@ int rbmg_psi::num_params() const {
 
 uint64_t rbmg_ensemble::num_steps() const {
     if (kind == 0) return num_samples;
+    if (kind == 2) return fixed_count;
     if (exact_total_z) return allowed.size();
     return 1ull << num_spins;
 }
@@ -180,7 +181,7 @@ extern "C" int rbmg_psi_create(int N, int M, const double* alpha, const double* 
     p->prefactor = prefactor;
     p->alpha.assign(N, 0.0);
     if (alpha) p->alpha.assign(alpha, alpha + N);
-    p->beta = p->alpha;   // include/quantum_state/PsiBase.hpp:246: beta_array(alpha)
+    p->beta = p->alpha;   // include/quantum_state/PsiBase.hpp:176, 190: beta_array(alpha)
     p->b.resize(M);
     p->W.resize(static_cast<size_t>(N) * M);
     std::memcpy(p->b.data(), b, sizeof(cplx) * M);
@@ -575,6 +576,29 @@ extern "C" int rbmg_exact_set_total_z_symmetry(rbmg_ensemble* ex, int sector) {
     return RBMG_OK;
 }
 
+// A fixed set of configurations visited with equal weights 1 / count: the samples of an
+// earlier MonteCarloLoop pass (rbmg_ensemble_samples) evaluated again, e.g. the gradient
+// of the energy an earlier call estimated, on the same configurations.
+extern "C" int rbmg_samples_create(uint32_t num_spins, uint32_t count, const uint64_t* spins, rbmg_ensemble** out) {
+    if (!out || !spins || count == 0 || num_spins == 0 || num_spins > 256)
+        return fail(RBMG_EINVAL, "fixed samples: need 1 <= N <= 256 and at least one configuration");
+    const int nw = nwords_of(static_cast<int>(num_spins));
+    const size_t n = static_cast<size_t>(count) * nw;
+    if (num_spins % 64)
+        for (uint32_t t = 0; t < count; t++)
+            if (spins[static_cast<size_t>(t) * nw + nw - 1] >> (num_spins % 64))
+                return fail(RBMG_EINVAL, "fixed samples: a configuration sets a bit at or beyond N");
+    auto e = std::make_unique<rbmg_ensemble>();
+    e->kind = 2;
+    e->num_spins = num_spins;
+    e->spins_words = nw;
+    e->fixed_count = count;
+    RBMG_CK(e->d_allowed.ensure(sizeof(uint64_t) * n));
+    RBMG_CK(cudaMemcpy(e->d_allowed.p, spins, sizeof(uint64_t) * n, cudaMemcpyHostToDevice));
+    *out = e.release();
+    return RBMG_OK;
+}
+
 extern "C" int rbmg_ensemble_num_steps(const rbmg_ensemble* ens, uint64_t* n) {
     if (!ens || !n) return fail(RBMG_EINVAL, "num_steps: null");
     *n = ens->num_steps();
@@ -886,9 +910,27 @@ static int chunk_mean(const Chunk& c, const double2* v, cplx* out) {
     return RBMG_OK;
 }
 
+// the configurations of a fixed sample set, equal weights
+static int fixed_stream(rbmg_ensemble* e, const rbmg_psi* psi, size_t max_chunk, StreamResult* res,
+                        const std::function<int(const Chunk&)>& fn) {
+    if (static_cast<int>(e->num_spins) != psi->N) return fail(RBMG_EINVAL, "fixed samples: N does not match psi");
+    const uint64_t total = e->num_steps();
+    res->norm_factor = 1.0 / static_cast<double>(total);
+    const uint64_t per = std::max<uint64_t>(1, max_chunk);
+    for (uint64_t base = 0; base < total; base += per) {
+        Chunk c;
+        c.count = static_cast<int>(std::min<uint64_t>(per, total - base));
+        c.spins = e->d_allowed.as<uint64_t>() + base * e->spins_words;
+        const int r = fn(c);
+        if (r != RBMG_OK) return r;
+    }
+    return RBMG_OK;
+}
+
 static int run_stream(rbmg_ensemble* ens, const rbmg_psi* psi, const rbmg_operator* op, bool sampler_eloc,
                       size_t max_chunk, StreamResult* res, const std::function<int(const Chunk&)>& fn) {
     if (ens->kind == 1) return exact_stream(ens, psi, res, fn);
+    if (ens->kind == 2) return fixed_stream(ens, psi, max_chunk, res, fn);
     res->norm_factor = 1.0 / static_cast<double>(ens->num_samples);
     if (psi->kind != 0) return deep_stream(ens, psi, op, sampler_eloc, max_chunk, fn);
     return mc_stream(ens, psi, op, sampler_eloc, max_chunk, fn);
@@ -930,6 +972,8 @@ static int check_pair(const rbmg_psi* psi, const rbmg_operator* op, const rbmg_e
     if (op && op->max_site >= psi->N) return fail(RBMG_EINVAL, "operator acts on a site >= N");
     if (ens->kind == 1 && static_cast<int>(ens->num_spins) != psi->N)
         return fail(RBMG_EINVAL, "ExactSummation size does not match psi");
+    if (ens->kind == 2 && static_cast<int>(ens->num_spins) != psi->N)
+        return fail(RBMG_EINVAL, "fixed sample set: N does not match psi");
     return RBMG_OK;
 }
 

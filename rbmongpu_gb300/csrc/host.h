@@ -166,7 +166,7 @@ struct rbmg_operator {
 };
 
 struct rbmg_ensemble {
-    int kind = 0;   // 0 MonteCarloLoop, 1 ExactSummation
+    int kind = 0;   // 0 MonteCarloLoop, 1 ExactSummation, 2 fixed sample set
     // MonteCarloLoop
     uint32_t num_samples = 0, num_sweeps = 1, num_therm = 0, num_chains = 1;
     uint64_t seed = 0;
@@ -179,7 +179,8 @@ struct rbmg_ensemble {
     uint32_t num_spins = 0;
     int exact_total_z = 0;
     std::vector<uint64_t> allowed;          // sector configurations
-    rbmg::DevBuf d_allowed;
+    rbmg::DevBuf d_allowed;                 // sector configurations; fixed sample set (kind 2)
+    uint64_t fixed_count = 0;               // fixed sample set: number of configurations
 
     uint64_t num_steps() const;
 };

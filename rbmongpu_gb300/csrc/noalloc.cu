@@ -8,6 +8,7 @@
 // workspace on demand; this entry point instead works in one fixed array in device
 // global memory, reserved when the library is loaded and held by every GPU that
 // loads it until the process exits.
+#include <atomic>
 #include <cmath>
 
 #include <cuda_runtime.h>
@@ -70,18 +71,24 @@ __global__ void logpsi64_from32_kernel(RbmDev P, int count, double2* out) {
     if (lane == 0) out[t] = make_double2(lr, li);
 }
 
-// device address of the scratch on the current device, looked up once per device
+// device address of the scratch on the current device, looked up once per device.  Host
+// threads may race on the first lookup; they all store the same address, and the atomic
+// entries make that well defined.  A cudaDeviceReset reloads the module, after which the
+// cached address is stale: a process that resets a device must not call the entry point
+// on that device again.
 int noalloc_scratch(unsigned char** out) {
-    static unsigned char* addr[64] = {};
+    static std::atomic<unsigned char*> addr[64];
     int dev = 0;
     RBMG_CK(cudaGetDevice(&dev));
     if (dev < 0 || dev >= 64) return fail(RBMG_EINVAL, "no-alloc: device index out of range");
-    if (!addr[dev]) {
+    unsigned char* a = addr[dev].load(std::memory_order_acquire);
+    if (!a) {
         void* p = nullptr;
         RBMG_CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-        addr[dev] = static_cast<unsigned char*>(p);
+        a = static_cast<unsigned char*>(p);
+        addr[dev].store(a, std::memory_order_release);
     }
-    *out = addr[dev];
+    *out = a;
     return RBMG_OK;
 }
 

@@ -211,7 +211,7 @@ def deep_case(name, kind, N, sizes, conns, sigma, seed, op, hop, unitary, nu, mc
 def main():
     """Writes every case, or only the cases named on the command line."""
     if not os.path.exists(HARNESS):
-        sys.exit("build the reference harness first: sh oracle/ref/build_ref.sh")
+        sys.exit("build the reference harness first: sh oracle/ref/build_ref.sh <RBMonGPU checkout>")
     only = set(sys.argv[1:])
     global rbm_case, deep_case
     if only:

@@ -25,7 +25,9 @@ def load(root):
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("RBMONGPU_REF")
+    if not root:
+        sys.exit("usage: %s <RBMonGPU checkout>  (or set RBMONGPU_REF)" % sys.argv[0])
     jn = load(root)
     rng = np.random.default_rng(77)
     cn = lambda *s: rng.normal(size=s) + 1j * rng.normal(size=s)   # noqa: E731

@@ -58,7 +58,9 @@ LISTS = {
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("RBMONGPU_REF")
+    if not root:
+        sys.exit("usage: %s <RBMonGPU checkout>  (or set RBMONGPU_REF)" % sys.argv[0])
     gd = load(root)
     p0, target, scale = problem()
     g = gradient(target, scale)

@@ -38,6 +38,10 @@ def test_argument_validation_fails_loudly_without_touching_the_device():
     assert lib.rbmg_mc_create(10, 1, 0, 3, 0, C.byref(h)) == _lib.RBMG_EINVAL
     assert b"multiple" in lib.rbmg_last_error()
     assert lib.rbmg_exact_create(0, C.byref(h)) == _lib.RBMG_EINVAL
+    # a fixed sample set whose configuration sets a bit at or beyond N
+    bad = (C.c_uint64 * 2)(1, 1 << 10)
+    assert lib.rbmg_samples_create(10, 2, bad, C.byref(h)) == _lib.RBMG_EINVAL
+    assert b"beyond N" in lib.rbmg_last_error()
     out = (C.c_double * 2)()
     assert lib.rbmg_activation(0.3, -0.2, out) == _lib.RBMG_OK
 

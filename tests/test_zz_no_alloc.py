@@ -38,6 +38,32 @@ def test_noalloc_energy_matches_allocating_entry_point_twice():
     assert abs(got - complex(c.s("E_re"), c.s("E_im"))) <= RTOL * abs(ref)
 
 
+def test_noalloc_energy_with_order_one_weights():
+    """Weights of order one, where the FP32 rounding of the device parameters (this entry
+    point's log psi comes from them) matters most; still within the 1e-5 tolerance of the
+    allocating entry point and of the FP64 restatement."""
+    from oracle import pyoracle as po
+    rng = np.random.Generator(np.random.PCG64(17))
+    N, M = 10, 20
+    b = rng.normal(0, 1.0, M) + 1j * rng.normal(0, 1.0, M)
+    W = rng.normal(0, 1.0, (N, M)) + 1j * rng.normal(0, 1.0, (N, M))
+    psi = rg.Psi(np.zeros(N), np.zeros(N), b, W, 1.0, False, True)
+    es = rg.ExactSummation(N)
+    psi.normalize(es)
+    table = rg.operators.tfim_chain(N, 1.0, 1.0)
+    op = rg.Operator(*table)
+    ref = rg.ExpectationValue()(psi, op, es)
+    _, exact = po.exact_gradient(po.RBM(b, W, psi.prefactor), po.Op(*table))
+    lib = _lib.lib()
+    for _ in range(2):
+        out = (C.c_double * 2)()
+        rc = lib.rbmg_ev_value_exact_noalloc(psi._h, op._h, N, out)
+        assert rc == _lib.RBMG_OK, lib.rbmg_last_error().decode()
+        got = complex(out[0], out[1])
+        assert abs(got - ref) <= RTOL * abs(ref), (got, ref)
+        assert abs(got - exact) <= RTOL * abs(exact), (got, exact)
+
+
 def test_noalloc_energy_rejects_sizes_beyond_its_scratch():
     rng = np.random.Generator(np.random.PCG64(3))
     N, M = 15, 16
