@@ -331,6 +331,24 @@ RBMG_API int rbmg_proposal_set_state(rbmg_proposal* proposal, const float* param
 RBMG_API int rbmg_chain_learned_async(rbmg_chain* chain, const rbmg_psi* psi, const rbmg_operator* op,
                                       rbmg_proposal* proposal, int n_steps, int train, int measure_every,
                                       void* d_eloc_out, void* stream);
+/* Test hook (no reference counterpart): the locally balanced training target of `count`
+ * configurations spins [count][nw] with the given logits [count][N+8]:
+ * dl [count][N+8] = (q - p*) / count, p*(i, l) propto |psi(s')/psi(s)| over all N x 8 moves
+ * (seed and length marginals), the gradient of the mean cross-entropy. */
+RBMG_API int rbmg_proposal_lb_target(rbmg_proposal* proposal, const rbmg_psi* psi, int count, const uint64_t* spins,
+                                     const float* logits, float* dl);
+/* Test hook (no reference counterpart): n_steps frozen learned steps with the state copied
+ * out around every launch, for a CPU replay of the draws and Metropolis-Hastings decisions.
+ * Before the first step: spins0 [B][nw], rng0 [B] (next Philox word), the angles theta0
+ * [B][Mpad][2] (re, im; Mpad = M rounded up to 32), their Re f re0 [B][Mpad] and the
+ * current states' logits logits0 [B][N+8].  Per step t: the proposed states' logits
+ * logits_prop [t][B][N+8], the move (site, len, logq = log q(s'|s)) [t][B], and after the
+ * accept pass spins [t][B][nw] and the accept counters [t][B]; rng_end [B] at the end.
+ * Networks with N + 8 <= 128. */
+RBMG_API int rbmg_chain_learned_trace(rbmg_chain* chain, const rbmg_psi* psi, rbmg_proposal* proposal, int n_steps,
+                                      uint64_t* spins0, uint64_t* rng0, float* theta0, float* re0, float* logits0,
+                                      float* logits_prop, int* site, int* len, float* logq, uint64_t* spins,
+                                      uint64_t* accepts, uint64_t* rng_end);
 /* Extension: the frozen learned steps of a chain run its walkers as `streams` (1 to 4)
  * independent slices on as many streams (one slice's network pass overlapping another's
  * accept pass); 0 (default) picks 2 from 8192 walkers on.  Every walker
@@ -439,6 +457,8 @@ RBMG_API int rbmg_s_matrix_timing(double* ms, int* launches);
 /* FP32 FMA throughput of the current device in TFLOP/s (a probe kernel of `iters`
  * x 128 independent FMAs per thread), the roofline denominator of the sampler. */
 RBMG_API int rbmg_probe_fp32_tflops(int iters, double* tflops);
+/* the same probe on packed pairs (fma.rn.f32x2, two FMAs per instruction) */
+RBMG_API int rbmg_probe_fp32x2_tflops(int iters, double* tflops);
 
 #ifdef __cplusplus
 }

@@ -307,6 +307,31 @@ float or_expf_det(float x) {
     return (p * s1.f) * s2.f;
 }
 
+/* Deterministic log of a positive normal float, the operation order of
+ * rbmongpu_gb300/csrc/device_math.cuh::logf_det: x = 2^e m, m in [sqrt(1/2), sqrt(2)),
+ * log m = 2 atanh(t), t = (m - 1)/(m + 1), by the odd series to t^13 (Horner in t^2),
+ * plus e ln2 in Cody & Waite's two constants. */
+float or_logf_det(float x) {
+    union { uint32_t u; float f; } b;
+    b.f = x;
+    int e = (int)((b.u >> 23) & 0xffu) - 127;
+    b.u = (b.u & 0x007fffffu) | 0x3f800000u;
+    float m = b.f;
+    if (m > 1.41421356f) { m = m * 0.5f; e += 1; }
+    const float t = (m + -1.0f) / (m + 1.0f);
+    const float t2 = t * t;
+    float p = 7.69230769e-02f;
+    p = fmaf(p, t2, 9.09090909e-02f);
+    p = fmaf(p, t2, 1.11111111e-01f);
+    p = fmaf(p, t2, 1.42857143e-01f);
+    p = fmaf(p, t2, 2.00000000e-01f);
+    p = fmaf(p, t2, 3.33333333e-01f);
+    p = fmaf(p, t2, 1.0f);
+    const float lm = (2.0f * t) * p;
+    const float ef = (float)e;
+    return ef * 0.693145752f + fmaf(ef, 1.42860677e-06f, lm);
+}
+
 /* ------------------------------------------------------------------------- */
 /* RBM (include/quantum_state/Psi.hpp:43-202)                                */
 /* ------------------------------------------------------------------------- */
@@ -1115,5 +1140,159 @@ int or_mc_run(const or_psi* psi, const or_op* op, const or_mc_cfg* cfg,
         free(c.theta);
         free(c.th_r);
     }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Learned-proposal chain, FP32 replay of rbmongpu_gb300/csrc/proposal.cu    */
+/* (learned_draw_kernel, learned_accept_kernel): the step of                 */
+/* include/spin_ensembles/MonteCarloLoop.hpp:206-222 with a cluster proposal */
+/* and the Metropolis-Hastings density ratio.  The proposal has no reference */
+/* counterpart; this replays the device's operation order so that a test    */
+/* fed the device's logits checks every draw and decision bit for bit.       */
+/* ------------------------------------------------------------------------- */
+#define LR_LENGTHS 8
+
+/* the xor butterfly 16, 8, 4, 2, 1 of device_math.cuh::warp_sum_xor */
+static float butterfly32(float* part) {
+    for (int off = 16; off >= 1; off >>= 1) {
+        float nx[32];
+        for (int l = 0; l < 32; l++) nx[l] = part[l] + part[l ^ off];
+        memcpy(part, nx, sizeof(nx));
+    }
+    return part[0];
+}
+
+typedef struct { float seed, len; } lr_norm;
+
+/* proposal.cu::log_norms_of: lane l sums the seed terms j = l + 32 c in c order */
+static lr_norm lr_log_norms(const float* row, int N) {
+    float m = -INFINITY, m2 = -INFINITY;
+    for (int j = 0; j < N; j++) m = fmaxf(m, row[j]);
+    for (int q = 0; q < LR_LENGTHS; q++) m2 = fmaxf(m2, row[N + q]);
+    float part[32], part2[32];
+    for (int l = 0; l < 32; l++) {
+        float a = 0.0f;
+        for (int c = 0; c < 8; c++)
+            if (l + 32 * c < N) a = a + or_expf_det(row[l + 32 * c] - m);
+        part[l] = a;
+        part2[l] = l < LR_LENGTHS ? or_expf_det(row[N + l] - m2) : 0.0f;
+    }
+    lr_norm r;
+    r.seed = m + or_logf_det(butterfly32(part));
+    r.len = m2 + or_logf_det(butterfly32(part2));
+    return r;
+}
+
+/* proposal.cu::draw_index: inverse CDF in chunks of 32, Hillis-Steele inclusive scan */
+static int lr_draw(const float* row, int n, float lse, float u) {
+    float base = 0.0f;
+    int last = 0;
+    for (int c = 0; c < n; c += 32) {
+        float e[32], x[32], y[32];
+        for (int l = 0; l < 32; l++) {
+            e[l] = c + l < n ? or_expf_det(row[c + l] - lse) : 0.0f;
+            x[l] = e[l];
+        }
+        for (int off = 1; off < 32; off <<= 1) {
+            memcpy(y, x, sizeof(y));
+            for (int l = off; l < 32; l++) x[l] = x[l] + y[l - off];
+        }
+        for (int l = 0; l < 32; l++)
+            if (e[l] > 0.0f && base + x[l] >= u) return c + l;
+        for (int l = 31; l >= 0; l--)
+            if (e[l] > 0.0f) { last = c + l; break; }
+        base = base + x[31];
+    }
+    return last;
+}
+
+static inline float lr_log_q(const float* row, int N, int i, int l, lr_norm ln) {
+    return (row[i] - ln.seed) + (row[N + l - 1] - ln.len);
+}
+
+static inline float lr_uniform(rng_t* r) { return (float)rng_real(r); }
+
+int or_learned_replay(int N, int M, int Mpad, const float* Wr, const float* Wi, int B, int steps, uint64_t seed,
+                      uint32_t walker_base, const uint64_t* spins0, const uint64_t* rng0, const float* theta0,
+                      const float* re0, const float* logits0, const float* logits_prop, int* site, int* len,
+                      float* logq, uint64_t* spins_out, uint8_t* accepted, uint64_t* rng_end) {
+    const int nw = nwords_of(N), O = N + LR_LENGTHS, K = Mpad / 32;
+    if (N <= LR_LENGTHS || nw > OR_MAX_WORDS || Mpad % 32 || M > Mpad) return -1;
+    float* tr = (float*)malloc(sizeof(float) * 6 * Mpad);
+    float* cur = (float*)malloc(sizeof(float) * O);
+    if (!tr || !cur) { free(tr); free(cur); return -2; }
+    float *ti = tr + Mpad, *re = tr + 2 * Mpad, *nr = tr + 3 * Mpad, *ni = tr + 4 * Mpad, *nre = tr + 5 * Mpad;
+    for (int w = 0; w < B; w++) {
+        uint64_t s[OR_MAX_WORDS] = {0};
+        memcpy(s, spins0 + (size_t)w * nw, sizeof(uint64_t) * nw);
+        rng_t rng;
+        memset(&rng, 0, sizeof(rng));
+        rng.kind = OR_RNG_PHILOX;
+        rng.seed = seed;
+        rng.walker = walker_base + (uint32_t)w;
+        rng.index = rng0[w];
+        for (int j = 0; j < Mpad; j++) {
+            tr[j] = theta0[((size_t)w * Mpad + j) * 2];
+            ti[j] = theta0[((size_t)w * Mpad + j) * 2 + 1];
+            re[j] = re0[(size_t)w * Mpad + j];
+        }
+        memcpy(cur, logits0 + (size_t)w * O, sizeof(float) * O);
+        /* the first move, drawn from the current state's logits */
+        lr_norm ln = lr_log_norms(cur, N);
+        int i = lr_draw(cur, N, ln.seed, lr_uniform(&rng));
+        int l = 1 + lr_draw(cur + N, LR_LENGTHS, ln.len, lr_uniform(&rng));
+        float lq = lr_log_q(cur, N, i, l, ln);
+        for (int t = 0; t < steps; t++) {
+            const size_t o = (size_t)t * B + w;
+            site[o] = i;
+            len[o] = l;
+            logq[o] = lq;
+            const float* prop = logits_prop + o * O;
+            /* trial angles: 2 s'_c W_c added in cluster order (s' = the flipped spin) */
+            for (int j = 0; j < Mpad; j++) { nr[j] = tr[j]; ni[j] = ti[j]; }
+            for (int q = 0; q < l; q++) {
+                const int c = (i + q) % N;
+                const float ts = spin_at(s, c) > 0 ? -2.0f : 2.0f;
+                for (int j = 0; j < Mpad; j++) {       /* rows zero-padded to Mpad, as on the device */
+                    nr[j] = fmaf(ts, j < M ? Wr[(size_t)c * M + j] : 0.0f, nr[j]);
+                    ni[j] = fmaf(ts, j < M ? Wi[(size_t)c * M + j] : 0.0f, ni[j]);
+                }
+            }
+            float part[32];
+            for (int ln_ = 0; ln_ < 32; ln_++) {
+                float a = 0.0f;
+                for (int k = 0; k < K; k++) {
+                    const int j = ln_ + 32 * k;
+                    nre[j] = or_lc_re_f32(nr[j], ni[j]);
+                    a = a + (nre[j] - re[j]);
+                }
+                part[ln_] = a;
+            }
+            const float delta = butterfly32(part);
+            const lr_norm lp = lr_log_norms(prop, N);
+            const float lq_rev = lr_log_q(prop, N, i, l, lp);
+            const float log_a = fmaf(2.0f, delta, lq_rev) - lq;
+            const float a = log_a >= 0.0f ? 1.0f : or_expf_det(log_a);
+            int acc = log_a >= 0.0f;
+            if (!acc) acc = lr_uniform(&rng) <= a;
+            if (acc) {
+                for (int j = 0; j < Mpad; j++) { tr[j] = nr[j]; ti[j] = ni[j]; re[j] = nre[j]; }
+                memcpy(cur, prop, sizeof(float) * O);
+                for (int q = 0; q < l; q++) spin_flip(s, (i + q) % N);
+            }
+            accepted[o] = (uint8_t)acc;
+            memcpy(spins_out + o * nw, s, sizeof(uint64_t) * nw);
+            if (t + 1 < steps) {
+                ln = acc ? lp : lr_log_norms(cur, N);
+                i = lr_draw(cur, N, ln.seed, lr_uniform(&rng));
+                l = 1 + lr_draw(cur + N, LR_LENGTHS, ln.len, lr_uniform(&rng));
+                lq = lr_log_q(cur, N, i, l, ln);
+            }
+        }
+        rng_end[w] = rng.index;
+    }
+    free(tr);
+    free(cur);
     return 0;
 }

@@ -75,6 +75,7 @@ float or_lc_re_f32(float x, float y);
 void or_lc_f32(float x, float y, float* out);
 void or_tanh_f32(float x, float y, float* out);
 float or_expf_det(float x);
+float or_logf_det(float x);
 
 /* ---- wave functions ---- */
 int or_num_params(const or_psi* psi);
@@ -141,4 +142,11 @@ double or_samples_hsd(const or_psi* psi, const or_psi* psi_prime, const or_op* o
 #ifdef __cplusplus
 }
 #endif
+/* learned-proposal chain: FP32 replay of the frozen Metropolis-Hastings steps of
+ * rbmongpu_gb300/csrc/proposal.cu fed the device's logits (see oracle.c) */
+int or_learned_replay(int N, int M, int Mpad, const float* Wr, const float* Wi, int B, int steps, uint64_t seed,
+                      uint32_t walker_base, const uint64_t* spins0, const uint64_t* rng0, const float* theta0,
+                      const float* re0, const float* logits0, const float* logits_prop, int* site, int* len,
+                      float* logq, uint64_t* spins_out, uint8_t* accepted, uint64_t* rng_end);
+
 #endif

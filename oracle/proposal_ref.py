@@ -145,3 +145,42 @@ def emulate_chain(log_psi_re, logits_all, N, B, steps, seed, with_reverse=True):
         acc += int(a.sum())
         state = np.where(a, new, state)
     return state, acc / (B * steps)
+
+
+def logcosh_ref(z):
+    """The reference's rational activation in FP64, vectorised
+    (include/quantum_state/psi_functions.hpp:49-57)."""
+    z = np.asarray(z, np.complex128)
+    sg = np.where(z.real > 0.0, 1.0, -1.0)
+    t = z * (sg * 3.746646023906276 + z) + 7.771429504240965
+    t = z * t + sg * 10.2180213465
+    t = z * t + 9.19376335670885
+    num = (5.49914721954 - sg * 2.16564366435 * z.real) - 1j * sg * 2.16564366435 * z.imag
+    return sg * 0.9003320053750442 * z + num / t - 0.598139
+
+
+def lb_target(W, b, words, logits, N):
+    """The locally balanced training target of proposal.cu::lb_target_kernel in FP64:
+    for every seed i and length l the cluster move's Re Delta = Re log psi(s') - Re log psi(s)
+    (Zanella 2020: p*(i, l) propto exp(Re Delta) = |psi(s')/psi(s)|), the seed and length
+    marginals of p*, and dl = (softmax(logits) - marginal) / count.
+    W [N][M] and b [M] are the RBM's complex parameters as the device holds them."""
+    x = spins_to_x(words, N)                              # [B][N] +-1
+    count = len(x)
+    theta = x @ W + b                                     # [B][M]
+    base = logcosh_ref(theta).real.sum(axis=1)            # [B]
+    delta = np.zeros((count, N, LENGTHS))
+    for i in range(N):
+        th = theta.copy()
+        for q in range(LENGTHS):
+            c = (i + q) % N
+            th = th - 2.0 * x[:, c:c + 1] * W[c][None, :]
+            delta[:, i, q] = logcosh_ref(th).real.sum(axis=1) - base
+    m = delta.reshape(count, -1).max(axis=1)[:, None, None]
+    p = np.exp(delta - m)
+    p /= p.sum(axis=(1, 2), keepdims=True)
+    lg = np.asarray(logits, np.float64)
+    qs = np.exp(lg[:, :N] - np.logaddexp.reduce(lg[:, :N], axis=1, keepdims=True))
+    ql = np.exp(lg[:, N:] - np.logaddexp.reduce(lg[:, N:], axis=1, keepdims=True))
+    dl = np.concatenate([qs - p.sum(axis=2), ql - p.sum(axis=1)], axis=1) / count
+    return dl

@@ -67,6 +67,8 @@ def lib():
         L.or_lc_re_f32.argtypes = [C.c_float, C.c_float]
         L.or_expf_det.restype = C.c_float
         L.or_expf_det.argtypes = [C.c_float]
+        L.or_logf_det.restype = C.c_float
+        L.or_logf_det.argtypes = [C.c_float]
         L.or_exact_norm.restype = C.c_double
         L.or_exact_hsd.restype = C.c_double
         L.or_samples_hsd.restype = C.c_double
@@ -446,3 +448,39 @@ def expf_det(x):
 
 def lc_re_f32(x, y):
     return lib().or_lc_re_f32(C.c_float(x), C.c_float(y))
+
+
+def logf_det(x):
+    """The deterministic FP32 log of the proposal's softmax (device_math.cuh::logf_det)."""
+    return lib().or_logf_det(C.c_float(x))
+
+
+def learned_replay(W, trace, seed, walker_base=0):
+    """FP32 replay of the frozen learned Metropolis-Hastings steps recorded by
+    Chain.learned_trace (rbmongpu_gb300/csrc/proposal.cu learned_draw_kernel and
+    learned_accept_kernel), fed the device's initial angles and its logits: returns the
+    replay's moves (site, len, logq), acceptances, spins after every step and the final
+    Philox positions."""
+    W = np.asarray(W, np.complex128)
+    N, M = W.shape
+    Wr = np.ascontiguousarray(W.real.astype(np.float32))
+    Wi = np.ascontiguousarray(W.imag.astype(np.float32))
+    steps, B = trace["site"].shape
+    Mpad = trace["re0"].shape[1]
+    nw = nwords(N)
+    out = dict(site=np.zeros((steps, B), np.int32), len=np.zeros((steps, B), np.int32),
+               logq=np.zeros((steps, B), np.float32), spins=np.zeros((steps, B, nw), np.uint64),
+               accepted=np.zeros((steps, B), np.uint8), rng_end=np.zeros(B, np.uint64))
+    fp = C.POINTER(C.c_float)
+    ip = C.POINTER(C.c_int)
+    arr = lambda a, t: np.ascontiguousarray(a).ctypes.data_as(t)   # noqa: E731
+    keep = {k: np.ascontiguousarray(trace[k]) for k in ("spins0", "rng0", "theta0", "re0", "logits0", "logits_prop")}
+    r = lib().or_learned_replay(
+        N, M, Mpad, arr(Wr, fp), arr(Wi, fp), B, steps, C.c_uint64(seed), C.c_uint32(walker_base),
+        arr(keep["spins0"], _u64p), arr(keep["rng0"], _u64p), arr(keep["theta0"], fp), arr(keep["re0"], fp),
+        arr(keep["logits0"], fp), arr(keep["logits_prop"], fp), arr(out["site"], ip), arr(out["len"], ip),
+        arr(out["logq"], fp), arr(out["spins"], _u64p), out["accepted"].ctypes.data_as(C.POINTER(C.c_uint8)),
+        arr(out["rng_end"], _u64p))
+    if r != 0:
+        raise ValueError(f"or_learned_replay failed ({r})")
+    return out

@@ -25,6 +25,7 @@ _ip = C.POINTER(C.c_int)
 _u64p = C.POINTER(C.c_uint64)
 _vp = C.c_void_p
 _vpp = C.POINTER(C.c_void_p)
+_fp = C.POINTER(C.c_float)
 
 # name -> argtypes (all return int status unless listed in _RESTYPE)
 SIGNATURES = {
@@ -82,6 +83,7 @@ SIGNATURES = {
     "rbmg_chain_state": [_vp, _u64p, _u64p, _u64p],
     "rbmg_stream": [_vpp],
     "rbmg_probe_fp32_tflops": [C.c_int, _dp],
+    "rbmg_probe_fp32x2_tflops": [C.c_int, _dp],
     "rbmg_ev_value_exact_noalloc": [_vp, _vp, C.c_int, _dp],
     "rbmg_proposal_create": [C.c_int, C.c_uint64, C.c_float, _vpp],
     "rbmg_proposal_destroy": [_vp],
@@ -109,6 +111,9 @@ SIGNATURES = {
     "rbmg_batch_result": [_vp, C.c_int, _dp, _dp, _dp],
     "rbmg_batch_info": [_vp, _ip, _u64p, _dp],
     "rbmg_chain_learned_async": [_vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_int, _vp, _vp],
+    "rbmg_proposal_lb_target": [_vp, _vp, C.c_int, _u64p, _fp, _fp],
+    "rbmg_chain_learned_trace": [_vp, _vp, _vp, C.c_int, _u64p, _u64p, _fp, _fp, _fp, _fp, _ip, _ip, _fp, _u64p,
+                                 _u64p, _u64p],
     "rbmg_chain_set_learned_streams": [_vp, C.c_int],
     "rbmg_optimizer_create": [C.c_int, C.c_int, _dp, C.c_int, C.c_int, _vpp],
     "rbmg_optimizer_destroy": [_vp],

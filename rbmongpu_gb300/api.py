@@ -783,6 +783,26 @@ class Chain:
              proposal._h, int(n_steps), int(train), int(measure_every), C.c_void_p(d_eloc) if d_eloc else None,
              C.c_void_p(stream) if stream else None)
 
+    def learned_trace(self, psi, proposal, n_steps):
+        """Test hook: n_steps frozen learned steps with the state recorded around every
+        launch (rbmg_chain_learned_trace); returns a dict of host arrays."""
+        B, N, nw = self.num_walkers, self.N, nwords(self.N)
+        Mpad = (psi.M + 31) // 32 * 32
+        O = N + Proposal.LENGTHS
+        f32 = lambda *sh: np.zeros(sh, np.float32)   # noqa: E731
+        d = dict(spins0=np.zeros((B, nw), np.uint64), rng0=np.zeros(B, np.uint64), theta0=f32(B, Mpad, 2),
+                 re0=f32(B, Mpad), logits0=f32(B, O), logits_prop=f32(n_steps, B, O),
+                 site=np.zeros((n_steps, B), np.int32), len=np.zeros((n_steps, B), np.int32),
+                 logq=f32(n_steps, B), spins=np.zeros((n_steps, B, nw), np.uint64),
+                 accepts=np.zeros((n_steps, B), np.uint64), rng_end=np.zeros(B, np.uint64))
+        fp = C.POINTER(C.c_float)
+        ip = C.POINTER(C.c_int)
+        call("rbmg_chain_learned_trace", self._h, psi._h, proposal._h, int(n_steps), _p(d["spins0"], _u64p),
+             _p(d["rng0"], _u64p), _p(d["theta0"], fp), _p(d["re0"], fp), _p(d["logits0"], fp),
+             _p(d["logits_prop"], fp), _p(d["site"], ip), _p(d["len"], ip), _p(d["logq"], fp),
+             _p(d["spins"], _u64p), _p(d["accepts"], _u64p), _p(d["rng_end"], _u64p))
+        return d
+
     def checkpoint(self):
         """{spins, rng_index, accepts, proposals}: restoring it continues the chains bit for bit."""
         B = self.num_walkers
@@ -872,6 +892,16 @@ class Proposal:
         grads = np.zeros(self.num_params, np.float32)
         call("rbmg_proposal_eval", self._h, count, _p(sp, _u64p), _p(dl, fp), _p(logits, fp), _p(grads, fp))
         return logits, grads
+
+    def lb_target(self, psi, spins, logits):
+        """Test hook: the locally balanced training target (q - p*) / count of the
+        configurations `spins` (uint64 words [count][nwords]) under `logits` [count][N+8]."""
+        sp = np.ascontiguousarray(spins, np.uint64).reshape(-1, nwords(self.N))
+        lg = np.ascontiguousarray(logits, np.float32).reshape(len(sp), self.N + self.LENGTHS)
+        dl = np.zeros_like(lg)
+        fp = C.POINTER(C.c_float)
+        call("rbmg_proposal_lb_target", self._h, psi._h, len(sp), _p(sp, _u64p), _p(lg, fp), _p(dl, fp))
+        return dl
 
     def checkpoint(self):
         """{params, m, v, steps}: the network and its Adam state."""

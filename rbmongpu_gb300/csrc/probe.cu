@@ -1,8 +1,10 @@
-// FP32 FMA throughput probe: the denominator of the sampler's roofline (the sampler
-// is bound by the FP32 pipe; the measured peaks at hand cover HBM copy bandwidth and BF16
-// tensor throughput only).
+// FP32 FMA throughput probes, scalar fma.rn.f32 and packed fma.rn.f32x2: the denominator
+// of the sampler's roofline is the larger of the two (the sampler is bound by the FP32
+// pipe; the measured peaks at hand cover HBM copy bandwidth and BF16 tensor throughput
+// only).
 #include <cuda_runtime.h>
 
+#include "device_math.cuh"
 #include "host.h"
 
 namespace rbmg {
@@ -22,12 +24,32 @@ __global__ void fma_probe_kernel(float* out, int iters, float a, float b) {
     if (s == 123.456f) out[threadIdx.x] = s;   // keeps the chains alive, never true in practice
 }
 
-}  // namespace
-}  // namespace rbmg
+// the same chains on packed pairs: fma.rn.f32x2, two FMAs per instruction
+__global__ void fma2_probe_kernel(float* out, int iters, float a, float b) {
+    const float x0 = threadIdx.x * 1e-7f;
+    pair_t x[8];
+#pragma unroll
+    for (int c = 0; c < 8; c++) x[c] = pk2(x0 + c, x0 + c + 0.5f);
+    const pair_t aa = splat2(a), bb = splat2(b);
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int u = 0; u < 16; u++) {
+#pragma unroll
+            for (int c = 0; c < 8; c++) x[c] = fma2(x[c], aa, bb);
+        }
+    }
+    float s = 0.0f;
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+        float lo, hi;
+        up2(x[c], lo, hi);
+        s += lo + hi;
+    }
+    if (s == 123.456f) out[threadIdx.x] = s;
+}
 
-using namespace rbmg;
-
-extern "C" int rbmg_probe_fp32_tflops(int iters, double* tflops) {
+template <bool PAIRS>
+int probe(int iters, double* tflops) {
     if (!tflops || iters <= 0) return fail(RBMG_EINVAL, "probe: bad arguments");
     int dev = 0, sms = 0;
     RBMG_CK(cudaGetDevice(&dev));
@@ -38,9 +60,13 @@ extern "C" int rbmg_probe_fp32_tflops(int iters, double* tflops) {
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     const int blocks = sms * 8, threads = 256;
-    fma_probe_kernel<<<blocks, threads, 0, stream()>>>(out, iters / 4, 0.9999f, 1e-4f);   // warm-up
+    auto run = [&](int n) {
+        if (PAIRS) fma2_probe_kernel<<<blocks, threads, 0, stream()>>>(out, n, 0.9999f, 1e-4f);
+        else fma_probe_kernel<<<blocks, threads, 0, stream()>>>(out, n, 0.9999f, 1e-4f);
+    };
+    run(iters / 4);   // warm-up
     cudaEventRecord(e0, stream());
-    fma_probe_kernel<<<blocks, threads, 0, stream()>>>(out, iters, 0.9999f, 1e-4f);
+    run(iters);
     cudaEventRecord(e1, stream());
     cudaError_t err = cudaEventSynchronize(e1);
     float ms = 0.f;
@@ -49,7 +75,16 @@ extern "C" int rbmg_probe_fp32_tflops(int iters, double* tflops) {
     cudaEventDestroy(e1);
     cudaFree(out);
     if (err != cudaSuccess) return cuda_fail(err, "probe");
-    const double flops = 2.0 * 8 * 16 * static_cast<double>(iters) * blocks * threads;
+    const double flops = (PAIRS ? 4.0 : 2.0) * 8 * 16 * static_cast<double>(iters) * blocks * threads;
     *tflops = flops / (ms * 1e-3) / 1e12;
     return RBMG_OK;
 }
+
+}  // namespace
+}  // namespace rbmg
+
+using namespace rbmg;
+
+extern "C" int rbmg_probe_fp32_tflops(int iters, double* tflops) { return probe<false>(iters, tflops); }
+
+extern "C" int rbmg_probe_fp32x2_tflops(int iters, double* tflops) { return probe<true>(iters, tflops); }

@@ -513,7 +513,9 @@ int proposal_adam(rbmg_proposal* p, cudaStream_t st) {
 // ============================================================================ chain kernels
 // log-normalisers of the seed and length softmaxes of one logits row (warp-wide,
 // identical in every lane; the same function serves the forward and the reverse
-// density, so both see bit-identical values for identical logits)
+// density, so both see bit-identical values for identical logits).  The softmax
+// arithmetic (expf_det, logf_det, explicitly rounded sums in a fixed order) is replayed
+// bit for bit by the CPU restatement, so the chain's draws can be checked exactly.
 struct LogNorm {
     float seed, len;
 };
@@ -542,13 +544,13 @@ __device__ __forceinline__ LogNorm log_norms_of(const RowRegs& r, int N, int lan
     float s = 0.0f;
 #pragma unroll
     for (int c = 0; c < 8; c++)
-        if (lane + 32 * c < N) s += expf(v[c] - m);
+        if (lane + 32 * c < N) s = __fadd_rn(s, expf_det(__fsub_rn(v[c], m)));
     s = warp_sum_xor(s);
     float m2 = vl;
 #pragma unroll
     for (int off = 16; off >= 1; off >>= 1) m2 = fmaxf(m2, __shfl_xor_sync(0xffffffffu, m2, off));
-    const float s2 = warp_sum_xor(lane < kLengths ? expf(vl - m2) : 0.0f);
-    return LogNorm{m + logf(s), m2 + logf(s2)};
+    const float s2 = warp_sum_xor(lane < kLengths ? expf_det(__fsub_rn(vl, m2)) : 0.0f);
+    return LogNorm{__fadd_rn(m, logf_det(s)), __fadd_rn(m2, logf_det(s2))};
 }
 
 __device__ __forceinline__ LogNorm log_norms(const float* row, int N, int lane) {
@@ -563,21 +565,26 @@ __device__ __forceinline__ int draw_index(const float* row, int n, float lse, fl
     int last = 0;
     for (int c = 0; c < n; c += 32) {
         const int j = c + lane;
-        const float e = j < n ? expf(row[j] - lse) : 0.0f;
+        const float e = j < n ? expf_det(__fsub_rn(row[j], lse)) : 0.0f;
         float x = e;
 #pragma unroll
         for (int off = 1; off < 32; off <<= 1) {
             const float y = __shfl_up_sync(0xffffffffu, x, off);
-            if (lane >= off) x += y;
+            if (lane >= off) x = __fadd_rn(x, y);
         }
-        const float cum = base + x;
+        const float cum = __fadd_rn(base, x);
         const unsigned hit = __ballot_sync(0xffffffffu, e > 0.0f && cum >= target);
         if (hit) return c + __ffs(hit) - 1;
         const unsigned pos = __ballot_sync(0xffffffffu, e > 0.0f);
         if (pos) last = c + 31 - __clz(pos);
-        base += __shfl_sync(0xffffffffu, x, 31);
+        base = __fadd_rn(base, __shfl_sync(0xffffffffu, x, 31));
     }
     return last;
+}
+
+// log q(i, l) = log softmax_seed(i) + log softmax_len(l) of one logits row
+__device__ __forceinline__ float log_q_of(const float* row, int N, int i, int l, const LogNorm& ln) {
+    return __fadd_rn(__fsub_rn(row[i], ln.seed), __fsub_rn(row[N + l - 1], ln.len));
 }
 
 struct LearnedLaunch {
@@ -653,7 +660,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) learned_draw_kernel(Learn
         for (int k = 0; k < NW; k++) L.spins_prop[static_cast<long>(w) * NW + k] = s.w[k];
         L.site[w] = i;
         L.len[w] = l;
-        L.logq_fwd[w] = (row[i] - ln.seed) + (row[L.N + l - 1] - ln.len);
+        L.logq_fwd[w] = log_q_of(row, L.N, i, l, ln);
         L.rng_index[w] = rng.index;
         L.proposals[w] += 1;
     }
@@ -727,8 +734,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) learned_accept_kernel(Rbm
     }
     const float delta = warp_sum_xor(part);
     const LogNorm ln = log_norms_of(rr, L.N, lane);
-    const float logq_rev = (rowp[i] - ln.seed) + (rowp[L.N + l - 1] - ln.len);
-    const float log_a = 2.0f * delta + logq_rev - L.logq_fwd[w];
+    const float logq_rev = log_q_of(rowp, L.N, i, l, ln);
+    const float log_a = __fsub_rn(__fmaf_rn(2.0f, delta, logq_rev), L.logq_fwd[w]);
     WalkerRng rng;
     rng.init(L.seed, static_cast<uint32_t>(L.walker_base + w), L.rng_index[w]);
     const float a = log_a >= 0.0f ? 1.0f : expf_det(log_a);
@@ -777,7 +784,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) learned_accept_kernel(Rbm
             for (int k = 0; k < NW; k++) L.spins_prop[static_cast<long>(w) * NW + k] = cur.w[k];
             L.site[w] = i2;
             L.len[w] = l2;
-            L.logq_fwd[w] = (row[i2] - lnn.seed) + (row[L.N + l2 - 1] - lnn.len);
+            L.logq_fwd[w] = log_q_of(row, L.N, i2, l2, lnn);
             L.proposals[w] += 1;
         }
     }
@@ -1177,7 +1184,7 @@ __global__ void __launch_bounds__(kFThreads, 1) mlp_fused_kernel(FusedNet net, L
                     for (int k = 0; k < NW; k++) L.spins_prop[static_cast<long>(w) * NW + k] = s.w[k];
                     L.site[w] = i;
                     L.len[w] = l;
-                    L.logq_fwd[w] = (row[i] - ln.seed) + (row[L.N + l - 1] - ln.len);
+                    L.logq_fwd[w] = log_q_of(row, L.N, i, l, ln);
                     L.rng_index[w] = rng.index;
                     L.proposals[w] += 1;
                 }
@@ -1495,16 +1502,11 @@ extern "C" int rbmg_chain_set_learned_streams(rbmg_chain* c, int streams) {
     return RBMG_OK;
 }
 
-extern "C" int rbmg_chain_learned_async(rbmg_chain* c, const rbmg_psi* psi, const rbmg_operator* op,
-                                        rbmg_proposal* prop, int n_steps, int train, int measure_every,
-                                        void* d_eloc_out, void* stream_ptr) {
-    if (!c || !psi || !prop || n_steps < 0 || train < 0) return fail(RBMG_EINVAL, "learned steps: bad arguments");
-    if (psi->kind != 0 || psi->N != c->N) return fail(RBMG_EINVAL, "learned steps: psi does not match the chain");
-    if (prop->N != c->N) return fail(RBMG_EINVAL, "learned steps: proposal does not match the chain");
-    if (d_eloc_out && (!op || measure_every <= 0)) return fail(RBMG_EINVAL, "learned steps: measurement needs op");
-    if (op && op->max_site >= psi->N) return fail(RBMG_EINVAL, "learned steps: operator acts on a site >= N");
-    if (n_steps == 0) return RBMG_OK;
-    cudaStream_t st = stream_ptr ? static_cast<cudaStream_t>(stream_ptr) : stream();
+// The chain's learned-step buffers (allocated on first use or when the shapes change), the
+// launch record of its walkers, and the angles and logits of the current states: plain
+// sweeps or new weights may have changed them since the last call.
+static int learned_prepare(rbmg_chain* c, const rbmg_psi* psi, rbmg_proposal* prop, int train, cudaStream_t st,
+                           LearnedState** state, LearnedLaunch& L) {
     const RbmDev P = psi->rbm_dev();
     const int B = static_cast<int>(c->walkers);
     if (!c->initialised) {
@@ -1543,7 +1545,6 @@ extern "C" int rbmg_chain_learned_async(rbmg_chain* c, const rbmg_psi* psi, cons
         RBMG_CK(S->reward.ensure(sizeof(float) * b));
         RBMG_CK(S->rbar.ensure(sizeof(float)));
     }
-    LearnedLaunch L{};
     L.B = B;
     L.N = c->N;
     L.O = prop->O;
@@ -1572,7 +1573,26 @@ extern "C" int rbmg_chain_learned_async(rbmg_chain* c, const rbmg_psi* psi, cons
         RBMG_CK(launch_learned(0, P, L, st));
     }
     RBMG_CK(launch_fused<false>(prop, L, L.spins, B, L.logits_cur, st));
-    int r = RBMG_OK;
+    *state = S;
+    return RBMG_OK;
+}
+
+extern "C" int rbmg_chain_learned_async(rbmg_chain* c, const rbmg_psi* psi, const rbmg_operator* op,
+                                        rbmg_proposal* prop, int n_steps, int train, int measure_every,
+                                        void* d_eloc_out, void* stream_ptr) {
+    if (!c || !psi || !prop || n_steps < 0 || train < 0) return fail(RBMG_EINVAL, "learned steps: bad arguments");
+    if (psi->kind != 0 || psi->N != c->N) return fail(RBMG_EINVAL, "learned steps: psi does not match the chain");
+    if (prop->N != c->N) return fail(RBMG_EINVAL, "learned steps: proposal does not match the chain");
+    if (d_eloc_out && (!op || measure_every <= 0)) return fail(RBMG_EINVAL, "learned steps: measurement needs op");
+    if (op && op->max_site >= psi->N) return fail(RBMG_EINVAL, "learned steps: operator acts on a site >= N");
+    if (n_steps == 0) return RBMG_OK;
+    cudaStream_t st = stream_ptr ? static_cast<cudaStream_t>(stream_ptr) : stream();
+    const RbmDev P = psi->rbm_dev();
+    const int B = static_cast<int>(c->walkers);
+    LearnedState* S = nullptr;
+    LearnedLaunch L{};
+    int r = learned_prepare(c, psi, prop, train, st, &S, L);
+    if (r != RBMG_OK) return r;
     const int nt = std::min(train, B);
     OpDev od;
     if (op) od = op->dev();
@@ -1688,5 +1708,107 @@ extern "C" int rbmg_chain_learned_async(rbmg_chain* c, const rbmg_psi* psi, cons
         }
         if (measured(step)) RBMG_CK(measure(step, st));
     }
+    return RBMG_OK;
+}
+
+// Test hook: the locally balanced training target of lb_target_kernel for `count`
+// configurations with the given logits [count][N+8]: dl = (q - p*) / count, the angles of
+// the configurations from scratch by the scalar angles kernel.
+extern "C" int rbmg_proposal_lb_target(rbmg_proposal* prop, const rbmg_psi* psi, int count, const uint64_t* spins,
+                                       const float* logits, float* dl) {
+    if (!prop || !psi || count < 1 || !spins || !logits || !dl) return fail(RBMG_EINVAL, "lb target: bad arguments");
+    if (psi->kind != 0 || psi->N != prop->N) return fail(RBMG_EINVAL, "lb target: psi does not match the proposal");
+    cudaStream_t st = stream();
+    const RbmDev P = psi->rbm_dev();
+    const size_t n = static_cast<size_t>(count), nw = static_cast<size_t>(nwords_of(P.N)),
+                 O = static_cast<size_t>(prop->O), per = static_cast<size_t>((P.Mpad / 32 + 1) / 2) * 32;
+    DevBuf d_spins, d_theta, d_re, d_logits, d_dl;
+    RBMG_CK(d_spins.ensure(sizeof(uint64_t) * n * nw));
+    RBMG_CK(d_theta.ensure(sizeof(float4) * n * per));
+    RBMG_CK(d_re.ensure(sizeof(float2) * n * per));
+    RBMG_CK(d_logits.ensure(sizeof(float) * n * O));
+    RBMG_CK(d_dl.ensure(sizeof(float) * n * O));
+    RBMG_CK(cudaMemcpyAsync(d_spins.p, spins, sizeof(uint64_t) * n * nw, cudaMemcpyHostToDevice, st));
+    RBMG_CK(cudaMemcpyAsync(d_logits.p, logits, sizeof(float) * n * O, cudaMemcpyHostToDevice, st));
+    LearnedLaunch L{};
+    L.B = count;
+    L.N = P.N;
+    L.O = prop->O;
+    L.spins = d_spins.as<uint64_t>();
+    L.theta = d_theta.as<float4>();
+    L.re = d_re.as<float2>();
+    RBMG_CK(launch_learned(0, P, L, st));
+    RBMG_CK(launch_lb_target(P, count, L.spins, L.theta, L.re, d_logits.as<float>(), prop->O, d_dl.as<float>(), st));
+    RBMG_CK(cudaMemcpyAsync(dl, d_dl.p, sizeof(float) * n * O, cudaMemcpyDeviceToHost, st));
+    RBMG_CK(cudaStreamSynchronize(st));
+    return RBMG_OK;
+}
+
+// Test hook: n_steps frozen learned steps of every walker (the single-stream sequence of
+// rbmg_chain_learned_async with train = 0: the first move drawn by its own pass, the
+// network on the proposed states, the accept pass drawing the next move), with the state
+// copied to the host around every launch, so that a CPU replay fed the same logits can
+// check every draw, acceptance ratio and decision.
+extern "C" int rbmg_chain_learned_trace(rbmg_chain* c, const rbmg_psi* psi, rbmg_proposal* prop, int n_steps,
+                                        uint64_t* spins0, uint64_t* rng0, float* theta0, float* re0, float* logits0,
+                                        float* logits_prop, int* site, int* len, float* logq, uint64_t* spins,
+                                        uint64_t* accepts, uint64_t* rng_end) {
+    if (!c || !psi || !prop || n_steps < 1 || !spins0 || !rng0 || !theta0 || !re0 || !logits0 || !logits_prop ||
+        !site || !len || !logq || !spins || !accepts || !rng_end)
+        return fail(RBMG_EINVAL, "learned trace: bad arguments");
+    if (psi->kind != 0 || psi->N != c->N || prop->N != c->N)
+        return fail(RBMG_EINVAL, "learned trace: psi or proposal does not match the chain");
+    if (prop->O > 128) return fail(RBMG_EUNSUPPORTED, "learned trace: networks with N + 8 <= 128");
+    cudaStream_t st = stream();
+    const RbmDev P = psi->rbm_dev();
+    LearnedState* S = nullptr;
+    LearnedLaunch L{};
+    int r = learned_prepare(c, psi, prop, 0, st, &S, L);
+    if (r != RBMG_OK) return r;
+    const size_t B = static_cast<size_t>(c->walkers), nw = static_cast<size_t>(c->nw), O = static_cast<size_t>(prop->O);
+    const int KP = (P.Mpad / 32 + 1) / 2;
+    std::vector<float4> th(B * KP * 32);
+    std::vector<float2> rf(B * KP * 32);
+    RBMG_CK(cudaMemcpyAsync(spins0, L.spins, sizeof(uint64_t) * B * nw, cudaMemcpyDeviceToHost, st));
+    RBMG_CK(cudaMemcpyAsync(rng0, L.rng_index, sizeof(uint64_t) * B, cudaMemcpyDeviceToHost, st));
+    RBMG_CK(cudaMemcpyAsync(th.data(), L.theta, sizeof(float4) * th.size(), cudaMemcpyDeviceToHost, st));
+    RBMG_CK(cudaMemcpyAsync(rf.data(), L.re, sizeof(float2) * rf.size(), cudaMemcpyDeviceToHost, st));
+    RBMG_CK(cudaMemcpyAsync(logits0, L.logits_cur, sizeof(float) * B * O, cudaMemcpyDeviceToHost, st));
+    RBMG_CK(cudaStreamSynchronize(st));
+    // paired layout -> unit order: lane l, pair kk holds units l + 32 (2 kk) and l + 32 (2 kk + 1)
+    for (size_t w = 0; w < B; w++)
+        for (int kk = 0; kk < KP; kk++)
+            for (int l = 0; l < 32; l++) {
+                const float4 t = th[(w * KP + kk) * 32 + l];
+                const float2 f = rf[(w * KP + kk) * 32 + l];
+                const int j0 = l + 64 * kk, j1 = j0 + 32;
+                if (j0 < P.Mpad) {
+                    theta0[(w * P.Mpad + j0) * 2] = t.x;
+                    theta0[(w * P.Mpad + j0) * 2 + 1] = t.z;
+                    re0[w * P.Mpad + j0] = f.x;
+                }
+                if (j1 < P.Mpad) {
+                    theta0[(w * P.Mpad + j1) * 2] = t.y;
+                    theta0[(w * P.Mpad + j1) * 2 + 1] = t.w;
+                    re0[w * P.Mpad + j1] = f.y;
+                }
+            }
+    for (int step = 0; step < n_steps; step++) {
+        if (step == 0) RBMG_CK(launch_draw(L, st));
+        RBMG_CK(launch_fused<false>(prop, L, L.spins_prop, static_cast<int>(B), S->logits_prop.as<float>(), st));
+        const size_t t = static_cast<size_t>(step);
+        RBMG_CK(cudaMemcpyAsync(logits_prop + t * B * O, L.logits_prop, sizeof(float) * B * O, cudaMemcpyDeviceToHost,
+                                st));
+        RBMG_CK(cudaMemcpyAsync(site + t * B, L.site, sizeof(int) * B, cudaMemcpyDeviceToHost, st));
+        RBMG_CK(cudaMemcpyAsync(len + t * B, L.len, sizeof(int) * B, cudaMemcpyDeviceToHost, st));
+        RBMG_CK(cudaMemcpyAsync(logq + t * B, L.logq_fwd, sizeof(float) * B, cudaMemcpyDeviceToHost, st));
+        L.propose_next = step + 1 < n_steps ? 1 : 0;
+        RBMG_CK(launch_learned(1, P, L, st));
+        RBMG_CK(cudaMemcpyAsync(spins + t * B * nw, L.spins, sizeof(uint64_t) * B * nw, cudaMemcpyDeviceToHost, st));
+        RBMG_CK(cudaMemcpyAsync(accepts + t * B, L.accepts, sizeof(uint64_t) * B, cudaMemcpyDeviceToHost, st));
+        RBMG_CK(cudaStreamSynchronize(st));
+    }
+    RBMG_CK(cudaMemcpyAsync(rng_end, L.rng_index, sizeof(uint64_t) * B, cudaMemcpyDeviceToHost, st));
+    RBMG_CK(cudaStreamSynchronize(st));
     return RBMG_OK;
 }

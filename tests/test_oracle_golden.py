@@ -137,3 +137,12 @@ def test_expf_det_error_bound():
     got = np.array([po.expf_det(float(x)) for x in xs], np.float64)
     ref = np.exp(xs.astype(np.float64))
     assert np.max(np.abs(got - ref) / ref) < 4e-7
+
+
+def test_deterministic_log_of_the_restatement():
+    """or_logf_det (the learned proposal's softmax log, replayed bit for bit on the device)
+    is within 2e-7 relative of log over the range the softmax normalisers take."""
+    xs = np.concatenate([np.linspace(1.0, 300.0, 5000), np.exp(np.linspace(-30, 30, 500))]).astype(np.float32)
+    got = np.array([po.logf_det(float(x)) for x in xs], np.float64)
+    ref = np.log(xs.astype(np.float64))
+    assert np.all(np.abs(got - ref) <= 2e-7 * np.maximum(np.abs(ref), 1.0))
