@@ -254,13 +254,26 @@ static inline lc_den32 lc_den_f32(float x, float y) {
     return d;
 }
 
+/* num / den by FMAs (device_math.cuh::div_pos): integer reciprocal estimate
+ * 0x7EF311C2 - bits(den), two Newton steps, one residual correction of the quotient */
+static inline float div_pos_f32(float num, float den) {
+    union { uint32_t u; float f; } b;
+    b.f = den;
+    b.u = 0x7EF311C2u - b.u;
+    float r = b.f;
+    r = fmaf(r, fmaf(-den, r, 1.0f), r);
+    r = fmaf(r, fmaf(-den, r, 1.0f), r);
+    const float q = num * r;
+    return fmaf(r, fmaf(-den, q, num), q);
+}
+
 float or_lc_re_f32(float x, float y) {
     const lc_den32 d = lc_den_f32(x, y);
     const float nr = fmaf(-F_LC_NB, d.p, F_LC_NA);
     const float ni = -F_LC_NB * d.q;
     const float num = fmaf(nr, d.dr, ni * d.di);
     const float den = fmaf(d.dr, d.dr, d.di * d.di);
-    return fmaf(F_LC_A, d.p, num / den) - F_LC_C;
+    return fmaf(F_LC_A, d.p, div_pos_f32(num, den)) - F_LC_C;
 }
 
 void or_lc_f32(float x, float y, float* out) {
