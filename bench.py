@@ -1,35 +1,39 @@
 #!/usr/bin/env python
 """Benchmark: learned-proposal vs plain Metropolis chains of the N=100 complex RBM.
 
-Workload (the configuration the headline metric is quoted on): complex RBM with
-N=100 visible and M=400 hidden units, parameters complex Normal(0, 0.1^2) drawn from
-PCG64(104); periodic 1D transverse-field Ising chain with h=1.0 (200 Pauli strings);
-16384 walkers per GPU.  Two chains run on the same GPU:
+Workload: complex RBM with N=100 visible and M=400 hidden units, parameters complex
+Normal(0, sigma^2) drawn from PCG64(104); periodic 1D transverse-field Ising chain with
+h=1.0 (200 Pauli strings); 16384 walkers per GPU.  Two chains run on the same GPU from the
+same equilibrated configurations:
 
 * plain: single-spin-flip Metropolis (the reference's method); one step = one row =
   `--sweeps-per-row` sweeps of N proposals per walker, then the local energy of every
   walker;
-* learned: after the same thermalisation and `--train-steps` steps of online training
-  (cross-entropy to the locally balanced proposal + Adam on the first `--train-walkers`
-  walkers), the frozen proposal network's cluster-flip Metropolis-Hastings steps; one
-  row = `--learned-steps-per-row` steps (a row of about the plain row's duration), then
-  the local energy of every walker.
+* learned: after `--train-steps` steps of online training (cross-entropy to the locally
+  balanced proposal + Adam on the first `--train-walkers` walkers), the frozen proposal
+  network's cluster-flip Metropolis-Hastings steps; one row = `--learned-steps-per-row`
+  steps (about the plain row's duration), then the local energy of every walker.
 
-The headline metric is effective samples per second of the learned chain: walkers x
-rows / tau_int(E_loc) per second of its timed rows, tau_int (in rows) from Sokal's
-automatic windowing (c = 5) of the walkers' E_loc series; the plain chain's figures sit
-beside it ("plain"), with E_loc/s, the energy standard error per spin, and a flag where
-the window did not converge (tau_int is then a lower bound).
+The headline is effective samples per second of the learned chain: walkers /
+tau_int(E_loc) per second of a timed row, tau_int (in rows) from Sokal's automatic
+windowing (c = 5) of the E_loc series formed by the K timed rows and the `--tau-rows`
+rows that follow them, so that the measurement does not depend on K.  At sigma = 0.1
+the RBM's |psi|^2 is a spin glass: neither chain equilibrates within 2e5 sweeps (the
+E_loc autocorrelation decays logarithmically), so tau_int has no finite estimate there.
+The headline therefore runs the same network at sigma = 0.05 (`--mix-sigma`), where both
+chains mix and tau_int converges, and reports the sigma = 0.1 rows beside it
+("glass_sigma0.1", tau_int lower bounds, energy drift by quarter of the series).
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--workload serving|s_matrix]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+                    [--workload serving|s_matrix|deep]
 
 `--workload serving` times the batched serving of 64 uneven RBMs instead (one line of
 its own); `--workload s_matrix` times get_S_matrix of the N=64, M=128 RBM over 16384
-Monte Carlo samples (P = 8448).
+Monte Carlo samples (P = 8448); `--workload deep` the PsiDeep 100-200-100-50 gradient.
 
 For N > 1 run under torchrun: every rank samples its own replica of the walker sets
-(Philox keys offset by rank), no data-path collective; value = all ranks' effective
-samples / max over ranks of the timed region.
+(Philox keys offset by rank), no data-path collective; value = the sum over ranks of
+walkers / tau_int over the maximum over ranks of the seconds per row.
 """
 import argparse
 import json
@@ -57,6 +61,11 @@ L2_FLUSH_BYTES = 256 << 20
 # DRAM bytes of one sampler launch: dram__bytes_read.sum + dram__bytes_write.sum of an ncu
 # capture of rbm_mc_kernel<13,2> on these 16384 walkers
 SAMPLER_DRAM_BYTES = 1.059e6
+# DRAM bytes of one learned_accept_kernel<13,2> launch of 16384 walkers (ncu, sigma 0.05, mean
+# of three launches: 100.3 MB read, 4.1 MB written -- accepted angles stay in L2 within a launch)
+ACCEPT_DRAM_BYTES = 104.4e6
+# rows of the sigma 0.1 measurement: 10 sweeps, or 150 learned steps (about as long)
+GLASS_SWEEPS_PER_ROW, GLASS_STEPS_PER_ROW = 10, 150
 
 # algorithmic FP32 flops of the sampler, from the operation list of
 # rbmongpu_gb300/csrc/device_math.cuh and rbm_impl.cuh (FMA = 2, mul/add/div = 1)
@@ -66,10 +75,11 @@ FLOPS_PROPOSAL_ANGLE = FLOPS_LC_RE + 4 + 2     # theta update (2 FMA) + differen
 FLOPS_ELOC_ANGLE = FLOPS_LC_C + 4 + 4          # theta'' update + complex difference and sum
 
 
-def workload():
+def workload(sigma=SIGMA):
+    """The N=100, M=400 complex RBM: b and W complex Normal(0, sigma^2) from PCG64(104)."""
     rng = np.random.Generator(np.random.PCG64(PARAM_SEED))
-    b = rng.normal(0, SIGMA, M_HIDDEN) + 1j * rng.normal(0, SIGMA, M_HIDDEN)
-    W = rng.normal(0, SIGMA, (N_SPINS, M_HIDDEN)) + 1j * rng.normal(0, SIGMA, (N_SPINS, M_HIDDEN))
+    b = rng.normal(0, sigma, M_HIDDEN) + 1j * rng.normal(0, sigma, M_HIDDEN)
+    W = rng.normal(0, sigma, (N_SPINS, M_HIDDEN)) + 1j * rng.normal(0, sigma, (N_SPINS, M_HIDDEN))
     return b, W
 
 
@@ -88,11 +98,15 @@ def tau_int(series, c=5.0):
     walkers, each series centred on the all-walker mean.  series: [K, walkers].
     Returns (tau, window, converged); not converged means no window W < K satisfied the
     rule, and tau is then a lower bound."""
-    x = np.asarray(series.real, np.float64)
-    x = x - x.mean()
-    K = x.shape[0]
-    f = np.fft.rfft(x, n=2 * K, axis=0)
-    ac = np.fft.irfft(f * np.conj(f), n=2 * K, axis=0)[:K].mean(axis=1) / np.arange(K, 0, -1)
+    x = np.asarray(series.real)
+    mean = float(x.mean(dtype=np.float64))
+    K, B = x.shape
+    ac = np.zeros(K)
+    for j in range(0, B, 1024):           # walkers in blocks (bounded memory)
+        y = x[:, j:j + 1024].astype(np.float64) - mean
+        f = np.fft.rfft(y, n=2 * K, axis=0)
+        ac += np.fft.irfft(f * np.conj(f), n=2 * K, axis=0)[:K].sum(axis=1)
+    ac /= B * np.arange(K, 0, -1)
     if ac[0] <= 0:
         return 1.0, 1, True
     rho = ac / ac[0]
@@ -168,9 +182,9 @@ class ClockSampler:
 def _cpu_worker(args):
     """One CPU chain of the same workload with the CPU restatement (FP64, the reference's
     arithmetic), persistent across calls; returns (seconds, E_loc series)."""
-    chain, sweeps, state_path = args
+    chain, sweeps, state_path, sigma = args
     from oracle import pyoracle as po
-    b, W = workload()
+    b, W = workload(sigma)
     psi = po.RBM(b, W)
     from rbmongpu_gb300.operators import tfim_chain
     op = po.Op(*tfim_chain(N_SPINS, 1.0, FIELD))
@@ -179,7 +193,7 @@ def _cpu_worker(args):
         state = (st["spins"].copy(), st["rng"].copy(), [1])
     else:
         state = (np.zeros((1, po.nwords(N_SPINS)), np.uint64), np.zeros(1, np.uint64), [0])
-    therm = 0 if state[2][0] else 2
+    therm = 0 if state[2][0] else 50
     t0 = time.perf_counter()
     _, _, el, _, _ = po.mc_run(psi, op, 1, sweeps, 1, therm, rng=po.OR_RNG_PHILOX, seed=7000, prec=po.OR_PREC_REF64,
                                chain_begin=chain, total_chains=4096, state=state)
@@ -188,16 +202,18 @@ def _cpu_worker(args):
     return dt, el[:, 0]
 
 
-def cpu_chains(steps, seconds_per_step, workers, tmpdir):
+def cpu_chains(steps, seconds_per_step, workers, tmpdir, sigma):
     """Runs `workers` persistent CPU chains for `steps` steps of about seconds_per_step."""
     ctx = mp.get_context("spawn")
     with ctx.Pool(workers) as pool:
-        dt, _ = pool.map(_cpu_worker, [(w, 1, os.path.join(tmpdir, f"calib{w}.npz")) for w in range(workers)])[0]
+        dt, _ = pool.map(_cpu_worker, [(w, 1, os.path.join(tmpdir, f"calib{w}.npz"), sigma)
+                                       for w in range(workers)])[0]
         sweeps = max(1, int(seconds_per_step / max(dt, 1e-3)))
         series, wall = [], 0.0
         for k in range(steps):
             t0 = time.perf_counter()
-            out = pool.map(_cpu_worker, [(w, sweeps, os.path.join(tmpdir, f"s{w}.npz")) for w in range(workers)])
+            out = pool.map(_cpu_worker, [(w, sweeps, os.path.join(tmpdir, f"s{w}.npz"), sigma)
+                                         for w in range(workers)])
             wall += time.perf_counter() - t0
             series.append(np.stack([o[1] for o in out], axis=1))
     return np.concatenate(series, axis=0), wall, sweeps
@@ -228,22 +244,139 @@ def replica_seeds(rank):
 
 
 # --------------------------------------------------------------------- GPU arms
+class GpuChains:
+    """The plain and learned chains of one RBM on this GPU, with the row runners the
+    benchmark times.  A plain row is `sweeps` single-flip sweeps, a learned row `steps`
+    frozen learned Metropolis-Hastings steps; both end with the local energy of every
+    walker, written to an E_loc row on the device."""
+
+    def __init__(self, rg, torch, psi, op, B, seeds, chunk_rows=250):
+        self.rg, self.torch, self.psi, self.op, self.B = rg, torch, psi, op, B
+        self.sp = rg.library_stream()
+        self.stream = torch.cuda.ExternalStream(self.sp)
+        self.seed_plain, self.seed_learned, self.seed_net = seeds
+        self.plain = rg.Chain(psi, B, seed=self.seed_plain)
+        self.learned = None
+        self.prop = None
+        self.chunk = chunk_rows
+        self.eloc = torch.empty((chunk_rows, B, 2), dtype=torch.float64, device="cuda")
+        self.scratch = torch.empty((B, 2), dtype=torch.float64, device="cuda")
+        self.flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+        self.train_s = 0.0
+
+    def equilibrate(self, sweeps):
+        with self.torch.cuda.stream(self.stream):
+            self.plain.sweep_async(self.psi, None, sweeps, 1, 0, self.sp)
+        self.torch.cuda.synchronize()
+
+    def start_learned(self, args, train_steps):
+        """The learned chain starts from the plain chain's configurations (its own Philox
+        streams); its network is trained online from there, then frozen."""
+        rg = self.rg
+        self.prop = rg.Proposal(self.psi.N, seed=self.seed_net, lr=1e-3)
+        self.learned = rg.Chain(self.psi, self.B, seed=self.seed_learned)
+        self.learned.set_learned_streams(args.learned_streams)
+        zero = np.zeros(self.B, np.uint64)
+        self.learned.restore(dict(spins=self.plain.checkpoint()["spins"], rng_index=zero, accepts=zero,
+                                  proposals=zero))
+        self.torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        with self.torch.cuda.stream(self.stream):
+            self.learned.learned_async(self.psi, None, self.prop, train_steps, args.train_walkers, 1, 0, self.sp)
+        self.torch.cuda.synchronize()
+        self.train_s = time.perf_counter() - t0
+
+    def row_fn(self, kind, per_row):
+        if kind == "plain":
+            return lambda ptr: self.plain.sweep_async(self.psi, self.op, per_row, per_row, ptr, self.sp)
+        return lambda ptr: self.learned.learned_async(self.psi, self.op, self.prop, per_row, 0, per_row, ptr, self.sp)
+
+    def warm(self, kind, per_row, n):
+        row = self.row_fn(kind, per_row)
+        with self.torch.cuda.stream(self.stream):
+            for _ in range(n):
+                row(self.scratch.data_ptr())
+        self.torch.cuda.synchronize()
+
+    def timed_rows(self, kind, per_row, n, sync):
+        """n rows, each timed by CUDA events on the library stream with L2 flushed in
+        between (outside the events); returns (ms per row [n], E_loc real parts [n, B])."""
+        torch = self.torch
+        row = self.row_fn(kind, per_row)
+        ms, series = [], []
+        for c0 in range(0, n, self.chunk):
+            m = min(self.chunk, n - c0)
+            starts = [torch.cuda.Event(enable_timing=True) for _ in range(m)]
+            ends = [torch.cuda.Event(enable_timing=True) for _ in range(m)]
+            sync()
+            with torch.cuda.stream(self.stream):
+                for k in range(m):
+                    self.flush.fill_(k & 0xFF)
+                    starts[k].record(self.stream)
+                    row(self.eloc[k].data_ptr())
+                    ends[k].record(self.stream)
+            sync()
+            ms += [a.elapsed_time(e) for a, e in zip(starts, ends)]
+            series.append(self.eloc[:m, :, 0].float().cpu().numpy())
+        return np.array(ms), np.concatenate(series, axis=0)
+
+    def more_rows(self, kind, per_row, n):
+        """n further rows, untimed (the series that fixes tau_int)."""
+        row = self.row_fn(kind, per_row)
+        out = []
+        for c0 in range(0, n, self.chunk):
+            m = min(self.chunk, n - c0)
+            with self.torch.cuda.stream(self.stream):
+                for k in range(m):
+                    row(self.eloc[k].data_ptr())
+            self.torch.cuda.synchronize()
+            out.append(self.eloc[:m, :, 0].float().cpu().numpy())
+        return np.concatenate(out, axis=0) if out else np.zeros((0, self.B), np.float32)
+
+    def acceptance(self, chain):
+        _, a, p = chain.state()
+        return a, p
+
+
+def acf_lags(series, lags):
+    """Walker-averaged normalised autocorrelation of E_loc at the given lags (rows)."""
+    x = np.asarray(series, np.float64)
+    x = x - x.mean()
+    v = (x * x).mean()
+    return {int(t): float((x[t:] * x[:len(x) - t]).mean() / v) for t in lags if t < len(x)}
+
+
+def chain_stats(series, timed_ms, B, N=N_SPINS, train_s=0.0):
+    """ESS figures of one chain: tau_int (rows) from the whole series (timed rows and the
+    rows that follow them), the rate from the timed rows alone."""
+    x = np.asarray(series, np.float64)
+    tau, window, ok = tau_int(x)
+    row_s = float(np.mean(timed_ms)) / 1e3
+    sigma = x.std()
+    ess_per_s = B / tau / row_s
+    se = sigma * np.sqrt(tau / x.size)
+    h = len(x) // 2
+    m1, m2 = x[:h].mean(axis=0), x[h:].mean(axis=0)
+    drift = (m2.mean() - m1.mean()) / np.sqrt((m1.var(ddof=1) + m2.var(ddof=1)) / B)
+    # rows to a standard error of 1e-4 per spin: sigma^2 tau / (B rows) = (1e-4 N)^2
+    rows_needed = (sigma / (1e-4 * N)) ** 2 * tau / B
+    return {"tau_int_rows": tau, "tau_window": window, "tau_converged": ok, "series_rows": len(x),
+            "series_over_tau": len(x) / tau, "timed_rows": len(timed_ms), "ms_per_row": row_s * 1e3,
+            "ess_per_s": ess_per_s, "eloc_per_s": B / row_s, "energy_per_spin": x.mean() / N,
+            "sigma_eloc": sigma, "se_per_spin": se / N, "half_drift_in_se": float(drift),
+            "seconds_to_se_1e-4_per_spin": rows_needed * row_s + train_s,
+            "acf": acf_lags(x, (1, 2, 5, 10, 20, 50, 100, 200, 400))}
+
+
 def run_gpu(args, rank, world, local_rank):
+    """The learned-vs-plain comparison on this rank (see the module docstring)."""
     import torch
     import rbmongpu_gb300 as rg
 
     torch.cuda.set_device(local_rank)
     rg.setDevice(local_rank)
-    b, W = workload()
-    psi = rg.Psi(np.zeros(N_SPINS), np.zeros(N_SPINS), b, W, 1.0, False, True)
-    op = rg.Operator(*rg.operators.tfim_chain(N_SPINS, 1.0, FIELD))
     B, K, Wm = args.walkers, args.steps, args.warmup
-    S, L = args.sweeps_per_row, args.learned_steps_per_row
-    sp = rg.library_stream()
-    stream = torch.cuda.ExternalStream(sp)
-    eloc = torch.empty((K, B, 2), dtype=torch.float64, device="cuda")
-    scratch = torch.empty((B, 2), dtype=torch.float64, device="cuda")
-    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    op = rg.Operator(*rg.operators.tfim_chain(N_SPINS, 1.0, FIELD))
 
     def sync():
         torch.cuda.synchronize()
@@ -251,104 +384,99 @@ def run_gpu(args, rank, world, local_rank):
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
-    def timed_rows(n, row):
-        """per-row milliseconds (CUDA events on the library stream), L2 flushed between rows"""
-        starts = [torch.cuda.Event(enable_timing=True) for _ in range(n)]
-        ends = [torch.cuda.Event(enable_timing=True) for _ in range(n)]
-        with torch.cuda.stream(stream):
-            for k in range(n):
-                flush.fill_(k & 0xFF)
-                starts[k].record(stream)
-                row(k)
-                ends[k].record(stream)
-        torch.cuda.synchronize()
-        return np.array([a.elapsed_time(e) for a, e in zip(starts, ends)])
-
-    def series_of(n):
-        return eloc[:n].cpu().numpy().view(np.complex128)[..., 0]
-
     clocks = ClockSampler(local_rank)
-    # ---- plain single-flip chain
-    seed_plain, seed_learned, seed_net = replica_seeds(rank)
-    plain = rg.Chain(psi, B, seed=seed_plain)
-    with torch.cuda.stream(stream):
-        plain.sweep_async(psi, None, THERM_SWEEPS, 1, 0, sp)
-    sync()
-    start = plain.checkpoint()["spins"]   # the learned chain starts here too
-    with torch.cuda.stream(stream):
-        for _ in range(Wm):
-            plain.sweep_async(psi, op, S, S, scratch.data_ptr(), sp)
-    sync()
+    out = {}
+    # ---------------------------------------------------------------- headline: sigma 0.05
+    b, W = workload(args.mix_sigma)
+    psi = rg.Psi(np.zeros(N_SPINS), np.zeros(N_SPINS), b, W, 1.0, False, True)
+    g = GpuChains(rg, torch, psi, op, B, replica_seeds(rank))
+    S, L = args.sweeps_per_row, args.learned_steps_per_row
+    g.equilibrate(args.therm_sweeps)
+    g.start_learned(args, args.train_steps)
+    g.warm("plain", S, Wm)
+    g.warm("learned", L, Wm)
     clocks.start()
-    _, a0, p0 = plain.state()
-    plain_ms = timed_rows(K, lambda k: plain.sweep_async(psi, op, S, S, eloc[k].data_ptr(), sp))
-    _, a1, p1 = plain.state()
-    plain_series = series_of(K)
-    # the sampler kernel alone (one launch of S sweeps), for its roofline
-    kernel_ms = timed_rows(max(3, K // 20), lambda k: plain.sweep_async(psi, None, S, 1, 0, sp))
-    plain_accept = (a1 - a0) / max(p1 - p0, 1)
-
-    # ---- learned-proposal chain
-    prop = rg.Proposal(N_SPINS, seed=seed_net, lr=1e-3)
-    lc = rg.Chain(psi, B, seed=seed_learned)
-    lc.set_learned_streams(args.learned_streams)
-    zero = np.zeros(B, np.uint64)
-    lc.restore(dict(spins=start, rng_index=zero, accepts=zero, proposals=zero))
-    sync()
-    t0 = time.perf_counter()
-    with torch.cuda.stream(stream):
-        lc.learned_async(psi, None, prop, args.train_steps, args.train_walkers, 1, 0, sp)
+    a0 = g.acceptance(g.plain)
+    plain_ms, plain_timed = g.timed_rows("plain", S, K, sync)
+    a1 = g.acceptance(g.plain)
+    l0 = g.acceptance(g.learned)
+    learned_ms, learned_timed = g.timed_rows("learned", L, K, sync)
+    l1 = g.acceptance(g.learned)
+    # the sampler kernel alone (one launch of 10 sweeps, no local energies), its roofline
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+    with torch.cuda.stream(g.stream):
+        for k in range(5):
+            g.flush.fill_(k)
+            starts[k].record(g.stream)
+            g.plain.sweep_async(psi, None, 10, 1, 0, g.sp)
+            ends[k].record(g.stream)
     torch.cuda.synchronize()
-    train_s = time.perf_counter() - t0
-    with torch.cuda.stream(stream):
-        for _ in range(Wm):
-            lc.learned_async(psi, op, prop, L, 0, L, scratch.data_ptr(), sp)
-    sync()
-    _, a0, p0 = lc.state()
-    learned_ms = timed_rows(K, lambda k: lc.learned_async(psi, op, prop, L, 0, L, eloc[k].data_ptr(), sp))
-    _, a1, p1 = lc.state()
+    kernel_ms = np.array([a.elapsed_time(e) for a, e in zip(starts, ends)])
+    # per-kernel durations of a learned step (network pass, accept pass), one stream
+    ms_net, ms_acc = g.learned.learned_kernel_times(psi, g.prop, 20)
     clk = clocks.stop()
-    learned_series = series_of(K)
-    learned_accept = (a1 - a0) / max(p1 - p0, 1)
-
-    plain_stats = series_stats(plain_series, float(plain_ms.sum()) / 1e3)
-    learned_stats = series_stats(learned_series, float(learned_ms.sum()) / 1e3)
+    # the series that fixes tau_int: the timed rows and the rows after them
+    plain_series = np.concatenate([plain_timed, g.more_rows("plain", S, args.tau_rows)])
+    learned_series = np.concatenate([learned_timed, g.more_rows("learned", L, args.tau_rows)])
+    out["plain"] = dict(chain_stats(plain_series, plain_ms, B), acceptance=(a1[0] - a0[0]) / max(a1[1] - a0[1], 1))
+    out["learned"] = dict(chain_stats(learned_series, learned_ms, B, train_s=g.train_s),
+                          acceptance=(l1[0] - l0[0]) / max(l1[1] - l0[1], 1), train_seconds=g.train_s)
+    out.update(plain_ms=plain_ms, learned_ms=learned_ms, kernel_ms=kernel_ms, ms_net=ms_net, ms_acc=ms_acc,
+               clocks=clk, learned_accept=out["learned"]["acceptance"])
 
     # end to end through the public API with host buffers: per row the RBM parameters go
     # host -> device (psi.params) and the row's local energies device -> host (pinned)
-    e2e_K = max(4, K // 10)
+    e2e_K = max(4, K // 4)
     p_host = psi.params
     pinned = torch.empty((B, 2), dtype=torch.float64, pin_memory=True)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for k in range(e2e_K):
         psi.params = p_host
-        with torch.cuda.stream(stream):
-            lc.learned_async(psi, op, prop, L, 0, L, scratch.data_ptr(), sp)
-            pinned.copy_(scratch, non_blocking=True)
-        stream.synchronize()
+        with torch.cuda.stream(g.stream):
+            g.learned.learned_async(psi, op, g.prop, L, 0, L, g.scratch.data_ptr(), g.sp)
+            pinned.copy_(g.scratch, non_blocking=True)
+        g.stream.synchronize()
         _ = pinned.numpy().view(np.complex128)[:, 0].mean()
-    e2e_s = time.perf_counter() - t0
-    h2d = (N_SPINS + 1) * ((M_HIDDEN + 31) // 32 * 32) * 8     # complex64 W and b, padded rows
-    d2h = B * 16
+    out["e2e_s"] = (time.perf_counter() - t0) / e2e_K
+    out["h2d"] = (N_SPINS + 1) * ((M_HIDDEN + 31) // 32 * 32) * 8     # complex64 W and b, padded rows
+    out["d2h"] = B * 16
+    del g
+
+    # ---------------------------------------------------------------- the glassy target (sigma 0.1)
+    if args.glass_rows > 0:
+        b, W = workload(SIGMA)
+        psi = rg.Psi(np.zeros(N_SPINS), np.zeros(N_SPINS), b, W, 1.0, False, True)
+        g = GpuChains(rg, torch, psi, op, B, replica_seeds(rank))
+        g.equilibrate(THERM_SWEEPS)
+        g.start_learned(args, args.train_steps)
+        gl = {}
+        for kind, per in (("plain", GLASS_SWEEPS_PER_ROW), ("learned", GLASS_STEPS_PER_ROW)):
+            ms, x0 = g.timed_rows(kind, per, min(K, args.glass_rows), sync)
+            x = np.concatenate([x0, g.more_rows(kind, per, args.glass_rows - len(x0))])
+            st = chain_stats(x, ms, B)
+            rm = x.mean(axis=1) / N_SPINS
+            q = max(1, len(rm) // 4)
+            st["energy_per_spin_by_quarter"] = [float(rm[i * q:(i + 1) * q].mean()) for i in range(4)]
+            st["walker_mean_spread_per_spin"] = float(x.mean(axis=0).std() / N_SPINS)
+            gl[kind] = st
+        out["glass"] = gl
+        del g
 
     fp32_peak = None
     if rank == 0:
-        import ctypes
-        from rbmongpu_gb300._lib import call
-        v = ctypes.c_double()
-        call("rbmg_probe_fp32_tflops", 20000, ctypes.byref(v))
-        fp32_peak = v.value
-
+        fp32_peak = max(ctypes_probe_fp32(), ctypes_probe_fp32(pairs=True))
+    out["fp32_peak"] = fp32_peak
     # whole-job sums over ranks (walker sets are independent replicas); times are maxima
-    tot = np.array([learned_stats["ess"], plain_stats["ess"], B * e2e_K / learned_stats["tau_int_rows"],
-                    learned_series.size, plain_series.size], np.float64)
-    tmax = np.array([learned_stats["seconds"], plain_stats["seconds"], e2e_s], np.float64)
+    pl, le = out["plain"], out["learned"]
+    tot = np.array([B / le["tau_int_rows"], B / pl["tau_int_rows"], learned_series.size, plain_series.size],
+                   np.float64)
+    tmax = np.array([le["ms_per_row"] / 1e3, pl["ms_per_row"] / 1e3, out["e2e_s"]], np.float64)
     if world > 1:
         tot, tmax = combine_ranks(tot, tmax, "cuda")
-    return dict(tot=tot, tmax=tmax, plain=plain_stats, learned=learned_stats, plain_ms=plain_ms,
-                learned_ms=learned_ms, kernel_ms=kernel_ms, plain_accept=plain_accept, learned_accept=learned_accept,
-                train_s=train_s, e2e_K=e2e_K, h2d=h2d, d2h=d2h, clocks=clk, fp32_peak=fp32_peak)
+    out.update(tot=tot, tmax=tmax)
+    return out
 
 
 # --------------------------------------------------------------------- serving workload
@@ -416,12 +544,7 @@ def run_serving(args):
     for psi, _, w, _ in inst:
         N, M = psi.N, psi.M
         flops += w * (flops_per_sweep(N, M) + flops_per_eloc(N, M, N) + 8 * (N + 1) * M)
-    peak = None
-    import ctypes
-    from rbmongpu_gb300._lib import call
-    v = ctypes.c_double()
-    call("rbmg_probe_fp32_tflops", 20000, ctypes.byref(v))
-    peak = v.value
+    peak = max(ctypes_probe_fp32(), ctypes_probe_fp32(pairs=True))
     sec = float(ms.mean()) / 1e3
     w_shape, rows, blocks = batch.shape
     line = {
@@ -441,7 +564,7 @@ def run_serving(args):
         "gpu_launches": K,
         "roofline": {"bound": "fp32", "achieved": flops / sec / 1e12, "peak": peak, "unit": "TFLOP/s",
                      "frac": flops / sec / 1e12 / peak, "traffic": None,
-                     "peak_source": "measured in this run by the library's FP32 FMA probe kernel",
+                     "peak_source": "measured in this run: the larger of the library's scalar and packed-pair FP32 FMA probes",
                      "kernel": "serve_kernel (persistent)", "flops_per_launch": flops},
         "cpu_baseline": None,
         "clocks": clk,
@@ -524,11 +647,10 @@ def run_smatrix(args):
     acc_s = float(np.mean(ms_acc)) / 1e3
     flops = 8.0 * L * (L + 1) / 2 * n          # 4 FMA per upper-triangle entry and sample
     if simt:
-        v = ctypes.c_double()
-        call("rbmg_probe_fp32_tflops", 20000, ctypes.byref(v))
-        roof = {"bound": "fp32", "achieved": flops / acc_s / 1e12, "peak": v.value, "unit": "TFLOP/s",
-                "frac": flops / acc_s / 1e12 / v.value, "traffic": None,
-                "peak_source": "measured in this run by the library's FP32 FMA probe kernel",
+        peak = max(ctypes_probe_fp32(), ctypes_probe_fp32(pairs=True))
+        roof = {"bound": "fp32", "achieved": flops / acc_s / 1e12, "peak": peak, "unit": "TFLOP/s",
+                "frac": flops / acc_s / 1e12 / peak, "traffic": None,
+                "peak_source": "measured in this run: the larger of the library's scalar and packed-pair FP32 FMA probes",
                 "kernel": "sm_herk_kernel"}
     else:
         # six BF16 part products for each of the four real products of a complex one
@@ -662,7 +784,7 @@ def run_deep(args):
     fwd, proposal, adj = deep_flops()
     # per sweep: layer 0 and log psi from the spins (one full pass), then N proposals
     flops = DEEP_WALKERS * ((therm + 1) * (fwd + N * proposal) + adj)
-    v = ctypes_probe_fp32()
+    v = max(ctypes_probe_fp32(), ctypes_probe_fp32(pairs=True))
     cpu = None
     if args.cpu_seconds > 0:
         from oracle import pyoracle as po
@@ -693,7 +815,7 @@ def run_deep(args):
         "gpu_launches": 177 * K,
         "roofline": {"bound": "fp32", "achieved": flops / sec / 1e12, "peak": v, "unit": "TFLOP/s",
                      "frac": flops / sec / 1e12 / v if v else None, "traffic": None,
-                     "peak_source": "measured in this run by the library's FP32 FMA probe kernel",
+                     "peak_source": "measured in this run: the larger of the library's scalar and packed-pair FP32 FMA probes",
                      "kernel": "deep_mc_multi_kernel + deep_adjoint_multi_kernel + adj_cgemm_kernel (the whole step)",
                      "flops_per_step": flops},
         "cpu_baseline": cpu,
@@ -702,11 +824,12 @@ def run_deep(args):
     print(json.dumps(line))
 
 
-def ctypes_probe_fp32():
+def ctypes_probe_fp32(pairs=False):
+    """FP32 FMA rate of this GPU from the library's probe kernel (scalar or packed pairs)."""
     import ctypes
     from rbmongpu_gb300._lib import call
     v = ctypes.c_double()
-    call("rbmg_probe_fp32_tflops", 20000, ctypes.byref(v))
+    call("rbmg_probe_fp32x2_tflops" if pairs else "rbmg_probe_fp32_tflops", 20000, ctypes.byref(v))
     return v.value
 
 
@@ -716,9 +839,16 @@ def main():
     ap.add_argument("--steps", type=int, default=400, help="timed rows of each chain")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--walkers", type=int, default=WALKERS)
-    ap.add_argument("--sweeps-per-row", type=int, default=10)
-    ap.add_argument("--learned-steps-per-row", type=int, default=150,
-                    help="learned steps per row; 150 makes a learned row last about as long as a plain row")
+    ap.add_argument("--sweeps-per-row", type=int, default=2)
+    ap.add_argument("--learned-steps-per-row", type=int, default=30,
+                    help="learned steps per row; 30 makes a learned row last about as long as a plain row")
+    ap.add_argument("--tau-rows", type=int, default=3000,
+                    help="rows of each chain after the timed ones: the series tau_int is taken from")
+    ap.add_argument("--therm-sweeps", type=int, default=2000, help="shared equilibration sweeps (headline)")
+    ap.add_argument("--mix-sigma", type=float, default=0.05,
+                    help="weight scale of the headline's RBM (both chains mix at 0.05; not at 0.07 or 0.1)")
+    ap.add_argument("--glass-rows", type=int, default=300,
+                    help="rows of each chain on the sigma 0.1 RBM (0: skip that part)")
     ap.add_argument("--learned-streams", type=int, default=0,
                     help="streams of the frozen learned steps (0: automatic, 2 slices from 8192 walkers)")
     ap.add_argument("--train-steps", type=int, default=2000)
@@ -758,9 +888,9 @@ def main():
         if rank != 0:
             return
         with tempfile.TemporaryDirectory() as td:
-            series, wall, sweeps = cpu_chains(args.warmup + args.steps, 1.0, workers, td)
+            series, wall, sweeps = cpu_chains(args.warmup + args.steps, 1.0, workers, td, args.mix_sigma)
         series = series[args.warmup * sweeps:]
-        tau, _, ok = tau_int(series)
+        tau, window, ok = tau_int(series)
         n = series.size
         timed = wall * args.steps / (args.warmup + args.steps)
         value = n / tau / timed
@@ -768,12 +898,13 @@ def main():
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * timed / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic (seeded PCG64 parameters)",
-                "config": {"workload": "rbm_n100_m400_tfim_chain", "method": "plain single-flip Metropolis",
-                           "walkers": workers, "sweeps_per_step": sweeps},
+                "config": {"workload": f"rbm_n100_m400_tfim_chain_sigma{args.mix_sigma:g}",
+                           "method": "plain single-flip Metropolis", "walkers": workers, "sweeps_per_step": sweeps},
                 "cpu_baseline": {"value": value, "unit": UNIT, "cores": workers, "kind": "port",
                                  "sample": f"{workers} FP64 chains x {args.steps * sweeps} sweeps with E_loc each"},
                 "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-                "eloc_per_s": n / timed, "tau_int_sweeps": tau, "tau_converged": ok}
+                "eloc_per_s": n / timed, "tau_int_sweeps": tau, "tau_window": window, "tau_converged": ok,
+                "series_over_tau": series.shape[0] / tau}
         print(json.dumps(line))
         return
 
@@ -787,61 +918,91 @@ def main():
             torch.distributed.destroy_process_group()
         return
     S, L, B = args.sweeps_per_row, args.learned_steps_per_row, args.walkers
-    ess_l, ess_p, ess_e2e, n_l, n_p = r["tot"]
+    inv_tau_l, inv_tau_p, n_l, n_p = r["tot"]
     sec_l, sec_p, sec_e2e = r["tmax"]
-    fl = flops_per_sweep() * S * B
-    avg_launch = float(np.mean(r["kernel_ms"])) / 1e3
-    achieved = fl / avg_launch / 1e12
-    peak = r["fp32_peak"]
+    ess_l, ess_p = inv_tau_l / sec_l, inv_tau_p / sec_p
     pl, le = r["plain"], r["learned"]
+    # the dominant kernel of a learned row: the accept pass (HBM), one launch of all walkers
+    KP = ((M_HIDDEN + 31) // 32 + 1) // 2
+    O = N_SPINS + 8
+    state_b = KP * 32 * (16 + 8)             # angles (paired float4) and Re f (paired float2)
+    acc = le["acceptance"]
+    accept_bytes = B * (state_b + 4 * O + 52 + 40 + acc * (state_b + 4 * O + 16))
+    hbm = measured_peak("hbm_gbs")
+    accept_gbs = accept_bytes / (r["ms_acc"] / 1e3) / 1e9
+    mlp_flops = B * 2.0 * (N_SPINS * 256 + 256 * 256 + 256 * O)
+    bf16 = measured_peak("bf16_tflops")
+    mlp_tfs = mlp_flops / (r["ms_net"] / 1e3) / 1e12
+    fl = flops_per_sweep() * 10 * B
+    avg_launch = float(np.mean(r["kernel_ms"])) / 1e3
+    peak = r["fp32_peak"]
     # CPU baseline on the host cores: the plain method, FP64 restatement, bounded sample
     cpu = None
     if args.cpu_seconds > 0:
         with tempfile.TemporaryDirectory() as td:
-            cs, cwall, csweeps = cpu_chains(max(1, int(args.cpu_seconds)), 1.0, workers, td)
-        cpu_eloc_s = cs.size / cwall
-        tau_sweeps = pl["tau_int_rows"] * S
-        cpu = {"value": cpu_eloc_s / tau_sweeps, "unit": UNIT, "cores": workers, "kind": "port",
-               "sample": f"{workers} FP64 restatement chains x {cs.shape[0]} sweeps with E_loc each; ESS/s "
-                         f"divides their E_loc/s by the GPU plain chain's tau_int in sweeps",
-               "eloc_per_s": cpu_eloc_s}
+            cs, cwall, csweeps = cpu_chains(max(3, int(args.cpu_seconds)), 1.0, workers, td, args.mix_sigma)
+        n_cpu = cs.shape[0]
+        cs = cs[2 * csweeps:]
+        cwall = cwall * cs.shape[0] / n_cpu
+        ctau, _, cok = tau_int(cs)
+        cpu = {"value": cs.size / ctau / cwall, "unit": UNIT, "cores": workers, "kind": "port",
+               "sample": f"{workers} FP64 restatement chains (sigma {args.mix_sigma:g}) x {cs.shape[0]} sweeps with "
+                         f"E_loc each; ESS/s from their own tau_int", "tau_int_sweeps": ctau, "tau_converged": cok,
+               "eloc_per_s": cs.size / cwall}
     gap = (le["energy_per_spin"] - pl["energy_per_spin"]) / np.hypot(le["se_per_spin"], pl["se_per_spin"])
     line = {
-        "metric": METRIC, "value": ess_l / sec_l, "unit": UNIT, "n_gpus": world,
+        "metric": METRIC, "value": ess_l, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(r["learned_ms"])),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 (complex64 RBM), bf16 MLP with f32 accumulation",
-        "data": f"synthetic (seeded PCG64 parameters; random +-1 starts, {THERM_SWEEPS} single-flip sweeps "
+        "data": f"synthetic (seeded PCG64 parameters; random +-1 starts, {args.therm_sweeps} single-flip sweeps "
                 "shared by both chains)",
-        "config": {"workload": "rbm_n100_m400_tfim_chain_learned_vs_plain", "N": N_SPINS, "M": M_HIDDEN,
-                   "walkers_per_gpu": B, "sigma": SIGMA, "h": FIELD, "therm_sweeps": THERM_SWEEPS,
-                   "step": f"learned: {L} frozen MH steps + E_loc; plain: {S} sweeps + E_loc",
-                   "train_steps": args.train_steps, "train_walkers": args.train_walkers,
-                   "learned_streams": learned_slices(args, B),
+        "config": {"workload": f"rbm_n100_m400_tfim_chain_sigma{args.mix_sigma:g}_learned_vs_plain", "N": N_SPINS,
+                   "M": M_HIDDEN, "walkers_per_gpu": B, "sigma": args.mix_sigma, "h": FIELD,
+                   "therm_sweeps": args.therm_sweeps,
+                   "step": f"one row: learned {L} frozen MH steps + E_loc; plain {S} sweeps + E_loc",
+                   "tau_series_rows": args.steps + args.tau_rows, "train_steps": args.train_steps,
+                   "train_walkers": args.train_walkers, "learned_streams": learned_slices(args, B),
                    "l2": "flushed between timed rows"},
-        "learned": dict(le, ess_per_s=ess_l / sec_l, acceptance=r["learned_accept"], train_seconds=r["train_s"],
-                        ms_per_row=float(np.mean(r["learned_ms"]))),
-        "plain": dict(pl, ess_per_s=ess_p / sec_p, acceptance=r["plain_accept"],
-                      ms_per_row=float(np.mean(r["plain_ms"]))),
-        "learned_over_plain_ess_per_s": (ess_l / sec_l) / (ess_p / sec_p),
-        "note": "both chains start from the same equilibrated configurations; where tau_converged is false "
-                "the window reached the series length, tau_int is a lower bound and ESS/s an upper bound; "
-                "half_drift_in_se compares the series' two halves (stationarity)",
+        "learned": le,
+        "plain": pl,
+        "learned_over_plain_ess_per_s": ess_l / ess_p,
         "energy_gap_in_se": gap,
-        "eloc_per_s": n_l / sec_l,
-        "e2e": {"value": ess_e2e / sec_e2e, "unit": UNIT, "h2d_bytes_per_step": int(r["h2d"]),
+        "note": ("ESS/s = walkers / tau_int(E_loc, rows) / seconds per timed row; tau_int by Sokal's windowing "
+                 "(c = 5) of the timed rows and the tau_rows that follow them; seconds_to_se_1e-4_per_spin = "
+                 "rows needed at that tau x seconds per row (+ the online training for the learned chain). "
+                 "The headline runs the configuration's network at sigma 0.05, where both chains mix; "
+                 "glass_sigma0.1 holds the same measurement at sigma 0.1, where neither chain equilibrates "
+                 "within the run (tau_int lower bounds)"),
+        "eloc_per_s": B * world / sec_l,
+        "e2e": {"value": inv_tau_l / sec_e2e, "unit": UNIT, "h2d_bytes_per_step": int(r["h2d"]),
                 "d2h_bytes_per_step": int(r["d2h"])},
         # per learned row and walker slice: the first step's draw, then L x (tensor-core
         # network on the proposed states, accept + next draw); per row: the angles from
         # scratch, the current states' network pass and the local-energy pass
         "gpu_launches": args.steps * (learned_slices(args, B) * (2 * L + 1) + 3),
-        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak if peak else None, "traffic": SAMPLER_DRAM_BYTES,
-                     "traffic_source": "ncu dram__bytes_read + write of one launch (W and walker state are "
-                                       "read once per launch whatever its sweep count)",
-                     "peak_source": "measured in this run by the library's FP32 FMA probe kernel",
-                     "kernel": f"rbm_mc_kernel<13,2> (plain sampler, {S} sweeps per launch)",
-                     "flops_per_launch": fl, "ms_per_launch": avg_launch * 1e3},
+        "roofline": {"bound": "hbm", "achieved": accept_gbs, "peak": hbm, "unit": "GB/s",
+                     "frac": accept_gbs / hbm if hbm else None, "traffic": ACCEPT_DRAM_BYTES,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one learned_accept_kernel "
+                                       "launch of 16384 walkers",
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs, of measured",
+                     "kernel": "learned_accept_kernel<13,2> (accept + next draw; one launch of all walkers, one stream)",
+                     "bytes_per_launch": accept_bytes, "ms_per_launch": r["ms_acc"],
+                     "algorithmic": "per walker: angles and Re f read (24 B per hidden unit pair slot), the proposed "
+                                    "logits row, move and stream words; the same written back on accept"},
+        "network_roofline": {"bound": "tensor", "achieved": mlp_tfs, "peak": bf16, "unit": "TFLOP/s",
+                             "frac": mlp_tfs / bf16 if bf16 else None,
+                             "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst), of measured",
+                             "kernel": "mlp_tc_kernel (tcgen05, the proposed states' logits)",
+                             "flops_per_launch": mlp_flops, "ms_per_launch": r["ms_net"]},
+        "plain_sampler_roofline": {"bound": "fp32", "achieved": fl / avg_launch / 1e12, "peak": peak,
+                                   "unit": "TFLOP/s", "frac": fl / avg_launch / 1e12 / peak if peak else None,
+                                   "traffic": SAMPLER_DRAM_BYTES,
+                                   "peak_source": "measured in this run: the larger of the library's scalar and "
+                                                  "packed-pair FP32 FMA probes",
+                                   "kernel": "rbm_mc_kernel<13,2> (plain sampler, 10 sweeps per launch, sigma 0.05)",
+                                   "flops_per_launch": fl, "ms_per_launch": avg_launch * 1e3},
+        "glass_sigma0.1": r.get("glass"),
         "cpu_baseline": cpu,
         "clocks": r["clocks"],
     }

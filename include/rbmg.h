@@ -331,6 +331,11 @@ RBMG_API int rbmg_proposal_set_state(rbmg_proposal* proposal, const float* param
 RBMG_API int rbmg_chain_learned_async(rbmg_chain* chain, const rbmg_psi* psi, const rbmg_operator* op,
                                       rbmg_proposal* proposal, int n_steps, int train, int measure_every,
                                       void* d_eloc_out, void* stream);
+/* Measurement hook (no reference counterpart): n_steps frozen learned steps on one stream
+ * with CUDA events around each tensor-core network pass and each accept pass; mean
+ * durations in ms (the bench's per-kernel roofline of a learned step). */
+RBMG_API int rbmg_chain_learned_kernel_times(rbmg_chain* chain, const rbmg_psi* psi, rbmg_proposal* proposal,
+                                             int n_steps, double* ms_network, double* ms_accept);
 /* Test hook (no reference counterpart): the locally balanced training target of `count`
  * configurations spins [count][nw] with the given logits [count][N+8]:
  * dl [count][N+8] = (q - p*) / count, p*(i, l) propto |psi(s')/psi(s)| over all N x 8 moves

@@ -111,6 +111,7 @@ SIGNATURES = {
     "rbmg_batch_result": [_vp, C.c_int, _dp, _dp, _dp],
     "rbmg_batch_info": [_vp, _ip, _u64p, _dp],
     "rbmg_chain_learned_async": [_vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_int, _vp, _vp],
+    "rbmg_chain_learned_kernel_times": [_vp, _vp, _vp, C.c_int, _dp, _dp],
     "rbmg_proposal_lb_target": [_vp, _vp, C.c_int, _u64p, _fp, _fp],
     "rbmg_chain_learned_trace": [_vp, _vp, _vp, C.c_int, _u64p, _u64p, _fp, _fp, _fp, _fp, _ip, _ip, _fp, _u64p,
                                  _u64p, _u64p],

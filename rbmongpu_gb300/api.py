@@ -783,6 +783,13 @@ class Chain:
              proposal._h, int(n_steps), int(train), int(measure_every), C.c_void_p(d_eloc) if d_eloc else None,
              C.c_void_p(stream) if stream else None)
 
+    def learned_kernel_times(self, psi, proposal, n_steps):
+        """Measurement hook: mean (network pass, accept pass) durations in ms over n_steps
+        frozen learned steps on one stream."""
+        a, b = C.c_double(), C.c_double()
+        call("rbmg_chain_learned_kernel_times", self._h, psi._h, proposal._h, int(n_steps), C.byref(a), C.byref(b))
+        return a.value, b.value
+
     def learned_trace(self, psi, proposal, n_steps):
         """Test hook: n_steps frozen learned steps with the state recorded around every
         launch (rbmg_chain_learned_trace); returns a dict of host arrays."""

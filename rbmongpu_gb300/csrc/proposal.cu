@@ -1711,6 +1711,52 @@ extern "C" int rbmg_chain_learned_async(rbmg_chain* c, const rbmg_psi* psi, cons
     return RBMG_OK;
 }
 
+// Measurement hook: n_steps frozen learned steps on one stream (the single-stream sequence
+// of rbmg_chain_learned_async, train = 0) with CUDA events around every network pass and
+// every accept pass; returns their mean durations in milliseconds.
+extern "C" int rbmg_chain_learned_kernel_times(rbmg_chain* c, const rbmg_psi* psi, rbmg_proposal* prop, int n_steps,
+                                               double* ms_network, double* ms_accept) {
+    if (!c || !psi || !prop || n_steps < 1 || !ms_network || !ms_accept)
+        return fail(RBMG_EINVAL, "learned kernel times: bad arguments");
+    if (psi->kind != 0 || psi->N != c->N || prop->N != c->N)
+        return fail(RBMG_EINVAL, "learned kernel times: psi or proposal does not match the chain");
+    if (prop->O > 128) return fail(RBMG_EUNSUPPORTED, "learned kernel times: networks with N + 8 <= 128");
+    cudaStream_t st = stream();
+    const RbmDev P = psi->rbm_dev();
+    LearnedState* S = nullptr;
+    LearnedLaunch L{};
+    int r = learned_prepare(c, psi, prop, 0, st, &S, L);
+    if (r != RBMG_OK) return r;
+    std::vector<cudaEvent_t> ev(4 * static_cast<size_t>(n_steps));
+    for (auto& e : ev) RBMG_CK(cudaEventCreate(&e));
+    cudaError_t err = launch_draw(L, st);
+    for (int step = 0; step < n_steps && err == cudaSuccess; step++) {
+        cudaEvent_t* e = ev.data() + 4 * static_cast<size_t>(step);
+        cudaEventRecord(e[0], st);
+        err = launch_fused<false>(prop, L, L.spins_prop, static_cast<int>(c->walkers), S->logits_prop.as<float>(), st);
+        cudaEventRecord(e[1], st);
+        L.propose_next = step + 1 < n_steps ? 1 : 0;
+        cudaEventRecord(e[2], st);
+        if (err == cudaSuccess) err = launch_learned(1, P, L, st);
+        cudaEventRecord(e[3], st);
+    }
+    if (err == cudaSuccess) err = cudaStreamSynchronize(st);
+    double tn = 0.0, ta = 0.0;
+    for (int step = 0; step < n_steps && err == cudaSuccess; step++) {
+        float a = 0.0f, b = 0.0f;
+        cudaEvent_t* e = ev.data() + 4 * static_cast<size_t>(step);
+        err = cudaEventElapsedTime(&a, e[0], e[1]);
+        if (err == cudaSuccess) err = cudaEventElapsedTime(&b, e[2], e[3]);
+        tn += a;
+        ta += b;
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    if (err != cudaSuccess) return cuda_fail(err, "learned kernel times");
+    *ms_network = tn / n_steps;
+    *ms_accept = ta / n_steps;
+    return RBMG_OK;
+}
+
 // Test hook: the locally balanced training target of lb_target_kernel for `count`
 // configurations with the given logits [count][N+8]: dl = (q - p*) / count, the angles of
 // the configurations from scratch by the scalar angles kernel.
