@@ -479,6 +479,42 @@ def run_gpu(args, rank, world, local_rank):
     return out
 
 
+# --------------------------------------------------------------------- long-chain autocorrelation
+def run_autocorrelation(args):
+    """Both chains of the N=100, M=400 RBM at weight scale --ac-sigma for --ac-rows rows
+    (plain: 10 sweeps, learned: 150 steps per row) after the shared equilibration: the
+    walker-averaged E_loc autocorrelation at lags up to 8000 rows, the mean energy by
+    twentieth of the series (drift) and the spread of the walkers' time averages -- the
+    evidence of whether tau_int can be measured at that weight scale."""
+    import torch
+    import rbmongpu_gb300 as rg
+    torch.cuda.set_device(0)
+    b, W = workload(args.ac_sigma)
+    psi = rg.Psi(np.zeros(N_SPINS), np.zeros(N_SPINS), b, W, 1.0, False, True)
+    op = rg.Operator(*rg.operators.tfim_chain(N_SPINS, 1.0, FIELD))
+    B, R = args.walkers, args.ac_rows
+    g = GpuChains(rg, torch, psi, op, B, replica_seeds(0), chunk_rows=200)
+    g.equilibrate(THERM_SWEEPS)
+    g.start_learned(args, args.train_steps)
+    out = {"workload": f"rbm_n100_m400_tfim_chain_sigma{args.ac_sigma:g}", "walkers": B, "rows": R,
+           "therm_sweeps": THERM_SWEEPS, "row": "plain 10 sweeps / learned 150 frozen steps, + E_loc"}
+    lags = [t for t in (1, 2, 5, 10, 20, 50, 100, 200, 500, 1000, 2000, 4000, 8000) if t < R]
+    for kind, per in (("plain", 10), ("learned", 150)):
+        t0 = time.perf_counter()
+        x = g.more_rows(kind, per, R)
+        sec = time.perf_counter() - t0
+        tau, window, ok = tau_int(x)
+        rm = x.mean(axis=1, dtype=np.float64) / N_SPINS
+        q = max(1, R // 20)
+        wm = x.mean(axis=0, dtype=np.float64) / N_SPINS
+        out[kind] = {"seconds": sec, "tau_int_rows": tau, "tau_window": window, "tau_converged": ok,
+                     "acf": acf_lags(x, lags), "energy_per_spin_by_twentieth":
+                     [round(float(rm[i * q:(i + 1) * q].mean()), 5) for i in range(20)],
+                     "walker_mean_per_spin_percentiles": [round(float(v), 4) for v in
+                                                          np.percentile(wm, [1, 10, 50, 90, 99])]}
+    print(json.dumps(out))
+
+
 # --------------------------------------------------------------------- serving workload
 def serving_instances(rg):
     """64 complex RBMs: N uniform in {16, 24, ..., 144}, alpha in {1, 2, 4}, parameters complex
@@ -858,7 +894,10 @@ def main():
     ap.add_argument("--sm-n", type=int, default=SM_N, help="s_matrix workload: visible units")
     ap.add_argument("--sm-m", type=int, default=SM_M, help="s_matrix workload: hidden units")
     ap.add_argument("--sm-simt", type=int, default=0, help="s_matrix workload: 1 = FP32 CUDA-core products")
-    ap.add_argument("--workload", default="learned", choices=["learned", "serving", "s_matrix", "deep"],
+    ap.add_argument("--ac-sigma", type=float, default=SIGMA, help="autocorrelation workload: weight scale")
+    ap.add_argument("--ac-rows", type=int, default=20000, help="autocorrelation workload: rows of each chain")
+    ap.add_argument("--workload", default="learned",
+                    choices=["learned", "serving", "s_matrix", "deep", "autocorrelation"],
                     help="learned: the N=100 learned-vs-plain chains (headline); serving: 64 uneven RBMs; "
                          "s_matrix: get_S_matrix of the N=64, M=128 RBM over 16384 MC samples; "
                          "deep: the PsiDeep 100-200-100-50 gradient through the adjoint kernels")
@@ -880,6 +919,10 @@ def main():
     if args.workload == "deep" and args.impl == "ours":
         if rank == 0:
             run_deep(args)
+        return
+    if args.workload == "autocorrelation":
+        if rank == 0 and args.impl == "ours":
+            run_autocorrelation(args)
         return
 
     if args.impl == "reference":

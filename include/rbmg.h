@@ -392,8 +392,12 @@ RBMG_API int rbmg_batch_get_register_cap(const rbmg_batch* batch, int* regs);
  * `sweeps` sweeps each and keeps the fastest; ms [18] (nullable) gets their mean replay
  * times, caps 255, 128, 96 in turn, each in the order (2,8) (2,16) (4,8) (4,16) (8,8) (8,16) */
 RBMG_API int rbmg_batch_autotune(rbmg_batch* batch, int sweeps, int reps, double* ms);
-/* last replay's results of instance i: energy [2], grad [2P] (nullable), eloc [2 walkers] (nullable) */
+/* last replay's results of instance i: energy [2], grad [2P] (nullable) -- the reference's
+ * estimator <E O*> + conj<E_k> - 2 <E> <O*> (source/network_functions/ExpectationValue.cu:243-253)
+ * over the instance's walkers, summed in a fixed order -- and eloc [2 walkers] (nullable) */
 RBMG_API int rbmg_batch_result(const rbmg_batch* batch, int instance, double* energy, double* grad, double* eloc);
+/* the configurations of instance i's walkers after the last replay, spins [walkers][ceil(N/64)] */
+RBMG_API int rbmg_batch_spins(const rbmg_batch* batch, int instance, uint64_t* spins);
 RBMG_API int rbmg_batch_info(const rbmg_batch* batch, int* num_instances, uint64_t* accepts, double* tuned_ms);
 
 /* ---------------------------------------------------------------- optimisers

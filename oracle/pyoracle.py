@@ -484,3 +484,24 @@ def learned_replay(W, trace, seed, walker_base=0):
     if r != 0:
         raise ValueError(f"or_learned_replay failed ({r})")
     return out
+
+
+def _replay_walker(args):
+    b, W, prefactor, w, samples, therm, seed, total = args
+    spins, _, _, acc, rej = mc_run(RBM(b, W, prefactor), None, 1, samples, 1, therm, seed=seed, chain_begin=w,
+                                   total_chains=total, want_eloc=False)
+    return spins[:, 0], int(acc[0]), int(rej[0])
+
+
+def mc_run_walkers(b, W, prefactor, walkers, samples, therm, seed, total_chains, workers=None):
+    """FP32 replays (Philox stream, the CUDA sampler's operation order) of the given walkers
+    of a `total_chains`-walker MonteCarloLoop pass, one sweep per sample, in a process pool
+    (spawn context, so it is safe after CUDA was initialised in the caller).  Returns
+    (spins [samples, len(walkers), nwords], accepts [len(walkers)], rejects)."""
+    import multiprocessing as mp
+    import os
+    jobs = [(np.asarray(b), np.asarray(W), prefactor, int(w), samples, therm, seed, total_chains) for w in walkers]
+    with mp.get_context("spawn").Pool(workers or min(len(jobs), os.cpu_count() or 1)) as pool:
+        out = pool.map(_replay_walker, jobs)
+    spins = np.stack([o[0] for o in out], axis=1)
+    return spins, np.array([o[1] for o in out], np.uint64), np.array([o[2] for o in out], np.uint64)

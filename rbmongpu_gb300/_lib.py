@@ -109,6 +109,7 @@ SIGNATURES = {
     "rbmg_batch_set_wait": [_vp, C.c_double, C.c_uint32],
     "rbmg_batch_get_register_cap": [_vp, _ip],
     "rbmg_batch_result": [_vp, C.c_int, _dp, _dp, _dp],
+    "rbmg_batch_spins": [_vp, C.c_int, _u64p],
     "rbmg_batch_info": [_vp, _ip, _u64p, _dp],
     "rbmg_chain_learned_async": [_vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_int, _vp, _vp],
     "rbmg_chain_learned_kernel_times": [_vp, _vp, _vp, C.c_int, _dp, _dp],

@@ -527,9 +527,11 @@ class MonteCarloLoop(_Ensemble):
         h = _handle()
         if isinstance(num_samples, MonteCarloLoop):   # MonteCarloLoop(MonteCarloLoop&)
             call("rbmg_mc_copy", num_samples._h, C.byref(h))
+            self.num_markov_chains = num_samples.num_markov_chains
         else:
             call("rbmg_mc_create", int(num_samples), int(num_sweeps), int(num_thermalization_sweeps),
                  int(num_markov_chains), int(seed), C.byref(h))
+            self.num_markov_chains = int(num_markov_chains)
         self._h = h
 
     def set_total_z_symmetry(self, sector):
@@ -538,8 +540,14 @@ class MonteCarloLoop(_Ensemble):
     def set_fast_sweep(self, num_tries):
         call("rbmg_mc_set_fast_sweep", self._h, int(num_tries))
 
-    def acceptance(self):
+    def acceptance(self, per_chain=False):
+        """(accepts, proposals) of the last pass, summed over chains; per_chain=True adds the
+        accept counts of every chain (extension: the reference counts globally)."""
         a, p = C.c_uint64(), C.c_uint64()
+        if per_chain:
+            pc = np.zeros(self.num_markov_chains, np.uint64)
+            call("rbmg_mc_acceptance", self._h, C.byref(a), C.byref(p), _p(pc, _u64p))
+            return a.value, p.value, pc
         call("rbmg_mc_acceptance", self._h, C.byref(a), C.byref(p), None)
         return a.value, p.value
 
@@ -997,7 +1005,8 @@ class Batch:
         return dict(zip(shapes, ms.tolist()))
 
     def result(self, i, want_eloc=False):
-        """(<E_loc>, O_k gradient [P], local energies or None) of instance i, last replay."""
+        """(<E_loc>, O_k gradient [P], local energies or None) of instance i, last replay: the
+        reference's estimator <E O*> + conj<E_k> - 2 <E> <O*> over its walkers."""
         N, P, w = self.instances[i]
         e = np.zeros(2)
         g = np.zeros(P, np.complex128)
@@ -1005,6 +1014,13 @@ class Batch:
         call("rbmg_batch_result", self._h, int(i), _p(e), _p(g.view(np.float64)),
              _p(el.view(np.float64)) if want_eloc else None)
         return complex(e[0], e[1]), g, el
+
+    def spins(self, i):
+        """The configurations of instance i's walkers after the last replay (uint64 words)."""
+        N, _, w = self.instances[i]
+        sp = np.zeros((w, nwords(N)), np.uint64)
+        call("rbmg_batch_spins", self._h, int(i), _p(sp, _u64p))
+        return sp
 
     def accepts(self):
         a = C.c_uint64()

@@ -417,7 +417,7 @@ static int op_compile(rbmg_operator* op) {
 }
 
 // per-site lists of off-diagonal slots flipping that site, for the E_k term
-static int op_site_lists(rbmg_operator* op, int N) {
+int op_site_lists(rbmg_operator* op, int N) {
     if (op->site_ptr_N == N) return RBMG_OK;
     std::vector<std::vector<int>> per(N);
     for (int n = 0; n < op->S; n++) {

@@ -165,6 +165,10 @@ struct rbmg_operator {
     }
 };
 
+// per-site lists of the off-diagonal strings flipping each site, built (once per N) on the
+// device for the E_k term (capi.cu)
+int op_site_lists(rbmg_operator* op, int N);
+
 struct rbmg_ensemble {
     int kind = 0;   // 0 MonteCarloLoop, 1 ExactSummation, 2 fixed sample set
     // MonteCarloLoop

@@ -3,20 +3,27 @@
 //
 // One persistent launch serves the whole batch.  Its warps take tasks from a global
 // queue (one atomic counter): first the walker tasks of every instance, longest first
-// (sweeps of single-flip Metropolis, the local energy and tanh(theta) of the final
-// configuration), then the reduction tasks, each a tile of rows by a chunk of walkers
-// of one instance's O_k sums (added with FP32 atomics), which start once that instance's
-// walkers are all done (a per-instance
-// counter; the wait is bounded by a wall-clock limit after which the kernel raises an
-// error flag and returns).  The walker tasks are compiled for each hidden-unit count per
+// (sweeps of single-flip Metropolis, then at the final configuration the local energy,
+// tanh(theta), the angles, U_j = sum_n e_n tanh(theta''_nj) over every string and the
+// terms e_n of the off-diagonal strings), then the reduction tasks, each a tile of rows by
+// a chunk of walkers of one instance's sums, which start once that instance's walkers are
+// all done (a per-instance counter; the wait is bounded by a wall-clock limit after which
+// the kernel raises an error flag and returns).  Each tile writes its chunk's partial sums;
+// a second kernel of the graph adds the chunks in a fixed order, so every replay gives the
+// same sums bit for bit.  The walker tasks are compiled for each hidden-unit count per
 // lane (1, 2, 4, 8, 13, 18: M <= 576) as separate functions of the one kernel.  The
-// launch (counter resets + kernel) is captured once in a CUDA graph and replayed; the
-// warps per block and the reduction tile height come from an autotuner that times the
-// candidates on the batch itself.
+// launch (counter resets + both kernels) is captured once in a CUDA graph and replayed;
+// the warps per block, the reduction tile height and a register cap come from an
+// autotuner that times the candidates on the batch itself.
 //
-// Per instance and replay the result is <E_loc> over its walkers and the O_k gradient
-// 2 (<E O*> - <E> <O*>), the reference's estimator (ExpectationValue.cu:243-253) with
-// conj<E_k> replaced by <E O*>, its expectation for a hermitian operator.
+// Per instance and replay the result is <E_loc> over its walkers and the reference's O_k
+// gradient <E O*> + conj<E_k> - 2 <E> <O*> (source/network_functions/ExpectationValue.cu:
+// 243-253), with E_k(s) = sum_n e_n O_k(s'_n) (include/operator/Operator.hpp:145-179): for
+// W_ij, s_i (U_j - 2 V_ij) with V_ij the terms of the strings flipping site i, their
+// tanh(theta'') recomputed in the reduction tile from the stored angles.  The sums run
+// centred on the instance's mean energy E (the same value in every tile):
+//   gO = sum conj(O),  gE = sum (E_w - E) conj(O),  gK = sum conj(E_k) - conj(E) conj(O),
+//   gradient = (gE + gK) / W + (conj(E) - E) gO / W.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -42,11 +49,18 @@ struct SInst {
     int walkers;
     uint64_t seed;
     double2* eloc;        // [walkers]
-    float2* T;            // [walkers][Mpad]
+    float2* T;            // [walkers][Mpad] tanh(theta)
+    float2* theta;        // [walkers][Mpad] the angles of the final configuration
+    float2* U;            // [walkers][Mpad] sum over every string of e_n tanh(theta''_n)
+    float2* en;           // [walkers][num_offdiag] e_n of the off-diagonal strings
+    const int* site_ptr;  // [N + 1] off-diagonal slots flipping each site (CSR)
+    const int* site_slots;
     uint64_t* spins;      // [walkers][nw]
     uint64_t* rng_index;  // [walkers]
-    float2* gO;           // [N + 1][Mpad]  sum_w conj(O)   (row N: the biases)
-    float2* gEO;          // [N + 1][Mpad]  sum_w E conj(O)
+    int chunks;           // walker chunks of kReduceWalkers
+    float2* part;         // [chunks][3][N + 1][Mpad] a chunk's gO, gE, gK (row N: the biases)
+    double2* g;           // [3][N + 1][Mpad] the sums over all chunks
+    double2* emean;       // [1] the mean local energy the sums are centred on
     unsigned int* done;   // walkers finished in this replay
 };
 
@@ -209,17 +223,27 @@ __device__ __noinline__ void walker_task(const SLaunch& L, const SInst& Ig, int 
     s_refresh(I, s, tr, ti, lane);
     extern __shared__ float2 s_f[];
     float2* myf = s_f + (threadIdx.x >> 5) * kSK * 32 + lane;
+    const long row_w = static_cast<long>(w) * I.Mpad + lane;
 #pragma unroll
     for (int k = 0; k < K; k++) {
         myf[32 * k] = lc_c_approx(tr[k], ti[k]);
-        I.T[static_cast<long>(w) * I.Mpad + lane + 32 * k] = tanh_c(tr[k], ti[k]);
+        I.T[row_w + 32 * k] = tanh_c(tr[k], ti[k]);
+        I.theta[row_w + 32 * k] = make_float2(tr[k], ti[k]);
     }
+    // E_k: U_j = sum_n e_n tanh(theta''_nj); the diagonal strings' part is their summed
+    // coefficient times tanh(theta_j)
+    float2 U[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) U[k] = make_float2(0.0f, 0.0f);
+    float2 dsum = make_float2(0.0f, 0.0f);
     KahanC e;
     for (int n = 0; n < I.op.S; n++) {
         const float2 cf = string_factor(I.op, n, s);
         const int nf = I.op.nflip[n];
         if (nf == 0) {
             e.add(cf.x, cf.y);
+            dsum.x += cf.x;
+            dsum.y += cf.y;
             continue;
         }
         const int off = I.op.flip_off[n];
@@ -257,6 +281,29 @@ __device__ __noinline__ void walker_task(const SLaunch& L, const SInst& Ig, int 
         }
         const float2 t = string_term(cf, warp_sum_xor2(part));
         e.add(t.x, t.y);
+        // the string's theta'' again (the same operations), its tanh into U
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            float nr = tr[k], ni = ti[k];
+            for (int q = 0; q < nf; q++) {
+                const int site = I.op.flip_sites[off + q];
+                const float two_s = s.up(site) ? -2.0f : 2.0f;
+                const float2 wv = __ldg(I.W + static_cast<long>(site) * I.Mpad + lane + 32 * k);
+                nr = fmaf(two_s, wv.x, nr);
+                ni = fmaf(two_s, wv.y, ni);
+            }
+            const float2 h = tanh_c(nr, ni);
+            U[k].x += t.x * h.x - t.y * h.y;
+            U[k].y += t.x * h.y + t.y * h.x;
+        }
+        if (lane == 0) I.en[static_cast<long>(w) * I.op.num_offdiag + I.op.offdiag_slot[n]] = t;
+    }
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        const float2 h = tanh_c(tr[k], ti[k]);
+        U[k].x += dsum.x * h.x - dsum.y * h.y;
+        U[k].y += dsum.x * h.y + dsum.y * h.x;
+        I.U[row_w + 32 * k] = U[k];
     }
     if (lane == 0) {
 #pragma unroll
@@ -271,9 +318,9 @@ __device__ __noinline__ void walker_task(const SLaunch& L, const SInst& Ig, int 
     if (lane == 0) atomicAdd(I.done, 1u);
 }
 
-// rows [r0, r0 + R) of the instance's O_k sums (row N: the biases), every column, over
-// walkers [w0, w0 + kReduceWalkers): added to the sums with FP32 atomics (the sums are
-// zeroed by the replay; their order of addition is not fixed)
+// rows [r0, r0 + R) of the instance's sums (row N: the biases), every column, over the
+// walkers of chunk [w0, w0 + kReduceWalkers): the chunk's partial sums of gO, gE and gK
+// (every partial is written by exactly one tile; serve_finish_kernel adds the chunks)
 template <int R>
 __device__ __noinline__ void reduce_task(const SLaunch& L, const SInst& I, int r0, int w0, int lane) {
     // wait for the instance's walkers (bounded by L.wait_ns of wall clock; a wait that gives
@@ -293,54 +340,122 @@ __device__ __noinline__ void reduce_task(const SLaunch& L, const SInst& I, int r
     __syncwarp();
     if (*reinterpret_cast<volatile int*>(L.error)) return;
     __threadfence();
+    // the instance's mean local energy, in a fixed order (the same value in every tile)
+    double mx = 0.0, my = 0.0;
+    for (int w = lane; w < I.walkers; w += 32) {
+        const double2 ed = __ldcg(I.eloc + w);
+        mx += ed.x;
+        my += ed.y;
+    }
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) {
+        mx += __shfl_xor_sync(0xffffffffu, mx, off);
+        my += __shfl_xor_sync(0xffffffffu, my, off);
+    }
+    mx /= I.walkers;
+    my /= I.walkers;
+    if (r0 == 0 && w0 == 0 && lane == 0) *I.emean = make_double2(mx, my);
+    const float Er = static_cast<float>(mx), Ei = static_cast<float>(my);
+    const int chunk = w0 / kReduceWalkers;
+    const long plane = static_cast<long>(I.N + 1) * I.Mpad;
+    float2* part = I.part + static_cast<long>(chunk) * 3 * plane;
+    const int w1 = min(I.walkers, w0 + kReduceWalkers);
     for (int kc = 0; kc < I.K; kc++) {
-        float2 aO[R], aE[R];
+        float2 aO[R], aE[R], aK[R];
 #pragma unroll
         for (int r = 0; r < R; r++) {
             aO[r] = make_float2(0.0f, 0.0f);
             aE[r] = make_float2(0.0f, 0.0f);
+            aK[r] = make_float2(0.0f, 0.0f);
         }
         const int j = lane + 32 * kc;
-        const int wd0 = r0 >> 6, wd1 = min(r0 + R - 1, I.N - 1) >> 6;   // the rows span at most two words
-        const int w1 = min(I.walkers, w0 + kReduceWalkers);
         for (int w = w0; w < w1; w++) {
             // L2 loads (__ldcg): the walkers' results were written by other SMs
-            const float2 t = __ldcg(I.T + static_cast<long>(w) * I.Mpad + j);
+            const long o = static_cast<long>(w) * I.Mpad + j;
+            const float2 t = __ldcg(I.T + o);
+            const float2 th = __ldcg(I.theta + o);
+            const float2 u = __ldcg(I.U + o);
             const double2 ed = __ldcg(I.eloc + w);
-            const float ex = static_cast<float>(ed.x), ey = static_cast<float>(ed.y);
-            // conj(t) and E conj(t)
+            const float dx = static_cast<float>(ed.x - mx), dy = static_cast<float>(ed.y - my);
+            // conj(t), (E - <E>) conj(t), and U - <E> t (E_k of the biases, centred)
             const float cx = t.x, cy = -t.y;
-            const float ecx = ex * cx - ey * cy, ecy = ex * cy + ey * cx;
-            const unsigned long long* sw = reinterpret_cast<const unsigned long long*>(I.spins) +
-                                           static_cast<long>(w) * I.nw;
-            const uint64_t word0 = wd0 < I.nw ? __ldcg(sw + wd0) : 0ull;
-            const uint64_t word1 = wd1 < I.nw ? __ldcg(sw + wd1) : 0ull;
+            const float ex = dx * cx - dy * cy, ey = dx * cy + dy * cx;
+            const float kx = u.x - (Er * t.x - Ei * t.y), ky = u.y - (Er * t.y + Ei * t.x);
+            uint64_t sw[kSW];
+#pragma unroll
+            for (int q = 0; q < kSW; q++)
+                sw[q] = q < I.nw ? __ldcg(reinterpret_cast<const unsigned long long*>(I.spins) +
+                                          static_cast<long>(w) * I.nw + q)
+                                 : 0ull;
+            auto up = [&](int site) {
+                uint64_t wd = sw[0];
+#pragma unroll
+                for (int q = 1; q < kSW; q++)
+                    if ((site >> 6) == q) wd = sw[q];
+                return ((wd >> (site & 63)) & 1ull) != 0ull;
+            };
 #pragma unroll
             for (int r = 0; r < R; r++) {
                 const int i = r0 + r;
+                if (i > I.N) continue;
                 float sg = 1.0f;
+                float vx = 0.0f, vy = 0.0f;
                 if (i < I.N) {
-                    const uint64_t word = (i >> 6) == wd0 ? word0 : word1;
-                    sg = ((word >> (i & 63)) & 1ull) ? 1.0f : -1.0f;
+                    sg = up(i) ? 1.0f : -1.0f;
+                    // V_ij: the strings flipping site i, e_n tanh(theta''_nj)
+                    for (int q = I.site_ptr[i]; q < I.site_ptr[i + 1]; q++) {
+                        const int slot = I.site_slots[q];
+                        const int n = I.op.offdiag[slot];
+                        const int nf = I.op.nflip[n], fo = I.op.flip_off[n];
+                        float nr = th.x, ni = th.y;
+                        for (int f = 0; f < nf; f++) {
+                            const int site = I.op.flip_sites[fo + f];
+                            const float two_s = up(site) ? -2.0f : 2.0f;
+                            const float2 wv = __ldg(I.W + static_cast<long>(site) * I.Mpad + j);
+                            nr = fmaf(two_s, wv.x, nr);
+                            ni = fmaf(two_s, wv.y, ni);
+                        }
+                        const float2 h = tanh_c(nr, ni);
+                        const float2 en = __ldcg(I.en + static_cast<long>(w) * I.op.num_offdiag + slot);
+                        vx += en.x * h.x - en.y * h.y;
+                        vy += en.x * h.y + en.y * h.x;
+                    }
                 }
                 aO[r].x += sg * cx;
                 aO[r].y += sg * cy;
-                aE[r].x += sg * ecx;
-                aE[r].y += sg * ecy;
+                aE[r].x += sg * ex;
+                aE[r].y += sg * ey;
+                // conj(s_i (U - 2 V) - <E> O) = sg conj(U - <E> t - 2 V)
+                aK[r].x += sg * (kx - 2.0f * vx);
+                aK[r].y -= sg * (ky - 2.0f * vy);
             }
         }
 #pragma unroll
         for (int r = 0; r < R; r++) {
             const int i = r0 + r;
             if (i <= I.N) {
-                float* o = reinterpret_cast<float*>(I.gO + static_cast<long>(i) * I.Mpad + j);
-                float* eo = reinterpret_cast<float*>(I.gEO + static_cast<long>(i) * I.Mpad + j);
-                atomicAdd(o, aO[r].x);
-                atomicAdd(o + 1, aO[r].y);
-                atomicAdd(eo, aE[r].x);
-                atomicAdd(eo + 1, aE[r].y);
+                const long e = static_cast<long>(i) * I.Mpad + j;
+                part[e] = aO[r];
+                part[plane + e] = aE[r];
+                part[2 * plane + e] = aK[r];
             }
         }
+    }
+}
+
+// the sums over the walker chunks, in chunk order (FP64): blockIdx.y is the instance
+__global__ void serve_finish_kernel(const SInst* inst) {
+    const SInst& I = inst[blockIdx.y];
+    const long n = 3L * (I.N + 1) * I.Mpad;
+    for (long e = static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x; e < n;
+         e += static_cast<long>(gridDim.x) * blockDim.x) {
+        double sx = 0.0, sy = 0.0;
+        for (int c = 0; c < I.chunks; c++) {
+            const float2 v = I.part[c * n + e];
+            sx += v.x;
+            sy += v.y;
+        }
+        I.g[e] = make_double2(sx, sy);
     }
 }
 
@@ -382,8 +497,8 @@ struct rbmg_batch {
     std::vector<const rbmg_operator*> ops;
     std::vector<SInst> host_inst;
     std::vector<uint32_t> walkers;
-    DevBuf d_inst, d_tasks, d_next, d_done, d_error, d_accepts, d_sums;
-    size_t sums_bytes = 0;
+    DevBuf d_inst, d_tasks, d_next, d_done, d_error, d_accepts;
+    int max_elems = 0;          // largest instance's 3 (N + 1) Mpad (the finish kernel's grid)
     std::vector<std::unique_ptr<DevBuf>> bufs;
     int ntasks_walk = 0, ntasks = 0;
     int rows = 16;              // reduction tile height
@@ -489,8 +604,12 @@ int batch_capture(rbmg_batch* b) {
     cudaMemsetAsync(b->d_next.p, 0, sizeof(unsigned int), st);
     cudaMemsetAsync(b->d_done.p, 0, sizeof(unsigned int) * b->n, st);
     cudaMemsetAsync(b->d_accepts.p, 0, sizeof(unsigned long long), st);
-    cudaMemsetAsync(b->d_sums.p, 0, b->sums_bytes, st);
-    const cudaError_t le = launch_serve(b, st);
+    cudaError_t le = launch_serve(b, st);
+    if (le == cudaSuccess) {
+        const dim3 grid(std::min(64, (b->max_elems + 255) / 256), b->n);
+        serve_finish_kernel<<<grid, 256, 0, st>>>(b->d_inst.as<SInst>());
+        le = cudaGetLastError();
+    }
     cudaGraph_t g = nullptr;
     const cudaError_t ce = cudaStreamEndCapture(st, &g);
     RBMG_CK(le);
@@ -543,6 +662,13 @@ extern "C" int rbmg_batch_create(int n, const rbmg_psi* const* psis, const rbmg_
         }
         if (p->N > 64 * kSW) return fail(RBMG_EUNSUPPORTED, "batch: N <= 192");
         if (o->max_site >= p->N) return fail(RBMG_EINVAL, "batch: operator acts on a site >= N");
+        for (int q = 0; q < i; q++)
+            if (ops[q] == o && psis[q]->N != p->N)
+                return fail(RBMG_EINVAL, "batch: an operator shared by instances of different N");
+        {
+            const int r = op_site_lists(const_cast<rbmg_operator*>(o), p->N);
+            if (r != RBMG_OK) return r;
+        }
         const int nw = nwords_of(p->N);
         SInst I{};
         I.N = p->N;
@@ -556,6 +682,8 @@ extern "C" int rbmg_batch_create(int n, const rbmg_psi* const* psis, const rbmg_
         I.Wq = d.Wq;
         I.bq = d.bq;
         I.op = o->dev();
+        I.site_ptr = o->d_site_ptr.as<int>();
+        I.site_slots = o->d_site_slots.as<int>();
         I.walkers = static_cast<int>(walkers[i]);
         I.seed = seeds[i];
         auto alloc = [&](size_t bytes) -> void* {
@@ -566,29 +694,24 @@ extern "C" int rbmg_batch_create(int n, const rbmg_psi* const* psis, const rbmg_
         const size_t B = walkers[i];
         I.eloc = static_cast<double2*>(alloc(sizeof(double2) * B));
         I.T = static_cast<float2*>(alloc(sizeof(float2) * B * p->Mpad));
+        I.theta = static_cast<float2*>(alloc(sizeof(float2) * B * p->Mpad));
+        I.U = static_cast<float2*>(alloc(sizeof(float2) * B * p->Mpad));
+        I.en = static_cast<float2*>(alloc(sizeof(float2) * B * std::max(1, o->num_offdiag)));
         I.spins = static_cast<uint64_t*>(alloc(sizeof(uint64_t) * B * nw));
         I.rng_index = static_cast<uint64_t*>(alloc(sizeof(uint64_t) * B));
-        if (!I.eloc || !I.T || !I.spins || !I.rng_index)
+        I.chunks = static_cast<int>((B + kReduceWalkers - 1) / kReduceWalkers);
+        const size_t elems = 3 * static_cast<size_t>(p->N + 1) * p->Mpad;
+        I.part = static_cast<float2*>(alloc(sizeof(float2) * I.chunks * elems));
+        I.g = static_cast<double2*>(alloc(sizeof(double2) * elems));
+        I.emean = static_cast<double2*>(alloc(sizeof(double2)));
+        b->max_elems = std::max(b->max_elems, static_cast<int>(elems));
+        if (!I.eloc || !I.T || !I.theta || !I.U || !I.en || !I.spins || !I.rng_index || !I.part || !I.g || !I.emean)
             return fail(RBMG_ENOMEM, "batch: device allocation failed");
         RBMG_CK(cudaMemset(I.rng_index, 0, sizeof(uint64_t) * B));
         b->psis.push_back(p);
         b->ops.push_back(o);
         b->walkers.push_back(walkers[i]);
         b->host_inst.push_back(I);
-    }
-    // the O_k sums of all instances in one buffer, zeroed by every replay
-    size_t tot = 0;
-    for (const auto& I : b->host_inst) tot += 2 * static_cast<size_t>(I.N + 1) * I.Mpad;
-    b->sums_bytes = sizeof(float2) * tot;
-    RBMG_CK(b->d_sums.ensure(b->sums_bytes));
-    {
-        float2* q = b->d_sums.as<float2>();
-        for (auto& I : b->host_inst) {
-            I.gO = q;
-            q += static_cast<size_t>(I.N + 1) * I.Mpad;
-            I.gEO = q;
-            q += static_cast<size_t>(I.N + 1) * I.Mpad;
-        }
     }
     RBMG_CK(b->d_done.ensure(sizeof(unsigned int) * n));
     for (int i = 0; i < n; i++) b->host_inst[i].done = b->d_done.as<unsigned int>() + i;
@@ -707,37 +830,44 @@ extern "C" int rbmg_batch_autotune(rbmg_batch* b, int sweeps, int reps, double* 
     return r != RBMG_OK ? r : rbmg_batch_set_register_cap(b, bregs);
 }
 
-// results of the last replay for instance i: <E_loc> over its walkers, the O_k gradient
-// 2 (<E O*> - <E> <O*>) in the reference's parameter layout [2P] (alpha and beta entries 0),
-// optionally the walkers' local energies [2 walkers]
+// results of the last replay for instance i: <E_loc> over its walkers, the reference's O_k
+// gradient <E O*> + conj<E_k> - 2 <E> <O*> in the reference's parameter layout [2P] (alpha
+// and beta entries 0), optionally the walkers' local energies [2 walkers]
 extern "C" int rbmg_batch_result(const rbmg_batch* b, int i, double* energy, double* grad, double* eloc) {
     if (!b || i < 0 || i >= b->n || !energy) return fail(RBMG_EINVAL, "batch result: bad arguments");
     const SInst& I = b->host_inst[i];
-    std::vector<double2> e(I.walkers);
-    RBMG_CK(cudaMemcpy(e.data(), I.eloc, sizeof(double2) * I.walkers, cudaMemcpyDeviceToHost));
-    cplx E(0.0, 0.0);
-    for (const auto& v : e) E += cplx(v.x, v.y);
-    E /= static_cast<double>(I.walkers);
+    double2 em;
+    RBMG_CK(cudaMemcpy(&em, I.emean, sizeof(double2), cudaMemcpyDeviceToHost));
+    const cplx E(em.x, em.y);
     energy[0] = E.real();
     energy[1] = E.imag();
-    if (eloc) std::memcpy(eloc, e.data(), sizeof(double2) * I.walkers);
+    if (eloc) RBMG_CK(cudaMemcpy(eloc, I.eloc, sizeof(double2) * I.walkers, cudaMemcpyDeviceToHost));
     if (grad) {
-        const size_t rows = static_cast<size_t>(I.N + 1) * I.Mpad;
-        std::vector<float2> gO(rows), gEO(rows);
-        RBMG_CK(cudaMemcpy(gO.data(), I.gO, sizeof(float2) * rows, cudaMemcpyDeviceToHost));
-        RBMG_CK(cudaMemcpy(gEO.data(), I.gEO, sizeof(float2) * rows, cudaMemcpyDeviceToHost));
-        cplx* g = reinterpret_cast<cplx*>(grad);
+        const size_t plane = static_cast<size_t>(I.N + 1) * I.Mpad;
+        std::vector<double2> g(3 * plane);
+        RBMG_CK(cudaMemcpy(g.data(), I.g, sizeof(double2) * 3 * plane, cudaMemcpyDeviceToHost));
+        cplx* out = reinterpret_cast<cplx*>(grad);
         const int N = I.N, M = I.M;
         const double inv = 1.0 / I.walkers;
-        for (int k = 0; k < 2 * N; k++) g[k] = 0.0;
+        const cplx shift = std::conj(E) - E;
+        for (int k = 0; k < 2 * N; k++) out[k] = 0.0;
         auto val = [&](int row, int j) {
-            const float2 o = gO[static_cast<size_t>(row) * I.Mpad + j], eo = gEO[static_cast<size_t>(row) * I.Mpad + j];
-            return 2.0 * (cplx(eo.x, eo.y) * inv - E * cplx(o.x, o.y) * inv);
+            const size_t e = static_cast<size_t>(row) * I.Mpad + j;
+            const cplx gO(g[e].x, g[e].y), gE(g[plane + e].x, g[plane + e].y), gK(g[2 * plane + e].x, g[2 * plane + e].y);
+            return (gE + gK) * inv + shift * gO * inv;
         };
-        for (int j = 0; j < M; j++) g[2 * N + j] = val(N, j);
+        for (int j = 0; j < M; j++) out[2 * N + j] = val(N, j);
         for (int r = 0; r < N; r++)
-            for (int j = 0; j < M; j++) g[2 * N + M + static_cast<size_t>(r) * M + j] = val(r, j);
+            for (int j = 0; j < M; j++) out[2 * N + M + static_cast<size_t>(r) * M + j] = val(r, j);
     }
+    return RBMG_OK;
+}
+
+// the walkers' configurations of instance i after the last replay [walkers][ceil(N/64)]
+extern "C" int rbmg_batch_spins(const rbmg_batch* b, int i, uint64_t* spins) {
+    if (!b || i < 0 || i >= b->n || !spins) return fail(RBMG_EINVAL, "batch spins: bad arguments");
+    const SInst& I = b->host_inst[i];
+    RBMG_CK(cudaMemcpy(spins, I.spins, sizeof(uint64_t) * I.walkers * I.nw, cudaMemcpyDeviceToHost));
     return RBMG_OK;
 }
 

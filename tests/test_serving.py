@@ -4,8 +4,11 @@ N=16 instances against FP64 exact summation, and the autotuner.
 
 Tolerances: local energies within 1e-6 relative of the single-network pass (the same
 FP32 operation order; the serving kernel only reads the angles from a runtime count of
-hidden units per lane); Monte-Carlo energies within 5 standard errors of exact summation
-and the gradient within 15 % (relative L2 norm) for 4096 walkers x 16 replays.
+hidden units per lane); every instance's gradient -- the reference's estimator
+<E O*> + conj<E_k> - 2 <E> <O*> -- within 1e-5 of its largest entry of the single-network
+gradient on the same configurations, and bit-identical between tile shapes (fixed-order
+sums); Monte-Carlo energies within 5 standard errors of exact summation and the gradient
+within 15 % (relative L2 norm, statistical) for 4096 walkers x 16 replays.
 """
 import numpy as np
 import pytest
@@ -50,6 +53,30 @@ def test_batch_chains_match_single_network_chains(regs):
         assert np.abs(got - ref).max() <= 1e-6 * np.abs(ref).max(), q
         total_acc += chain.state()[1]
     assert batch.accepts() == total_acc
+
+
+def test_served_gradient_is_the_reference_estimator_on_the_same_configurations():
+    import rbmongpu_gb300 as rg
+    specs = [(16, 1, 0.7, 64), (24, 2, 1.3, 96), (40, 4, 1.9, 300), (72, 2, 1.0, 32), (136, 1, 0.5, 520)]
+    results = []
+    for rows in (16, 8):
+        inst = []
+        for q, (N, a, h, B) in enumerate(specs):
+            inst.append((rbm(N, a, 105_200 + q), rg.Operator(*rg.operators.tfim_chain(N, 1.0, h)), B, 300 + q))
+        batch = rg.Batch(inst)
+        batch.set_shape(4, rows)
+        batch.run(20, 2)
+        results.append([batch.result(q) for q in range(len(inst))])
+        if rows == 16:
+            for q, (psi, op, B, _) in enumerate(inst):
+                E, g, _ = results[-1][q]
+                g_ref, E_ref = rg.ExpectationValue().gradient(psi, op, rg.FixedSamples(psi.N, batch.spins(q)))
+                assert abs(E - E_ref) <= 1e-6 * abs(E_ref), (q, E, E_ref)
+                assert np.abs(g - g_ref).max() <= 1e-5 * np.abs(g_ref).max(), (q, np.abs(g - g_ref).max())
+    # the sums are fixed-order: another tile height gives the same bits
+    for (E1, g1, _), (E2, g2, _) in zip(*results):
+        assert E1 == E2
+        np.testing.assert_array_equal(g1, g2)
 
 
 def test_n16_instances_match_exact_summation():
