@@ -61,7 +61,9 @@ RBMG_API int rbmg_activation(double re, double im, double* out /* [2] */);
  * (include/quantum_state/Psi.hpp:220-238, pyRBMonGPU/main.cpp:50-59).
  * alpha, beta: [N] real; b: [M] complex; W: [N, M] complex row-major.
  * Like the reference (include/quantum_state/PsiBase.hpp:168-178, 183-192) beta is
- * initialised from alpha.  free_quantum_axis != 0 returns RBMG_EUNSUPPORTED. */
+ * initialised from alpha.  free_quantum_axis != 0 makes the Hilbert-space distance of this
+ * psi add the alpha / beta rotation terms (source/network_functions/HilbertSpaceDistance.cu:
+ * 47-81, 109-122); the reference uses the flag nowhere else on this path. */
 RBMG_API int rbmg_psi_create(int N, int M, const double* alpha, const double* beta, const double* b, const double* W,
                     double prefactor, int free_quantum_axis, rbmg_psi** out);
 
@@ -82,6 +84,8 @@ RBMG_API int rbmg_psi_deep_create(int N, int num_layers, const int* sizes, const
 RBMG_API int rbmg_psi_copy(const rbmg_psi* psi, rbmg_psi** out);
 RBMG_API int rbmg_psi_destroy(rbmg_psi* psi);
 
+/* free_quantum_axis (pyRBMonGPU/main.cpp:91, 132, 166) */
+RBMG_API int rbmg_psi_free_quantum_axis(const rbmg_psi* psi, int* on);
 /* psi kind: 0 Psi, 1 PsiDeep, 2 PsiPair */
 RBMG_API int rbmg_psi_kind(const rbmg_psi* psi, int* kind);
 /* N, M (RBM) or width (deep), num_params (include/quantum_state/Psi.hpp:233, PsiDeep.cu:34-66) */

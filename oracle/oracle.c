@@ -731,7 +731,14 @@ void or_samples_gradient(const or_psi* psi, const or_op* op, int num_samples, co
 /* ------------------------------------------------------------------------- */
 typedef struct { cd omega; double pr; double nn; double* omega_O; double* pr_O; } hsd_acc;
 
-/* part: -1 general complex O_k of psi_prime; 0/1 PsiPair real/imag net O_k (real) */
+static inline double qa_at(const double* a, int i) { return a ? a[i] : 0.0; }
+
+/* part: -1 general complex O_k of psi_prime; 0/1 PsiPair real/imag net O_k (real).
+ * With psi's free quantum axis (HilbertSpaceDistance.cu:47-81, 109-122; part -1 only, the
+ * PsiPair gradient of HilbertSpaceDistance_PsiPair.cu has no such branch): r_i =
+ * psi'(s with spin i flipped) / psi'(s), log psi'(s) += sum_i [da_i s_i r_i +
+ * i db_i (r_i cos(sa_i) - s_i sin(sa_i))] with da = alpha' - alpha, db = beta' - beta,
+ * sa = alpha' + alpha, and the O_k of alpha_i, beta_i are s_i r_i, i (r_i cos - s_i sin). */
 static void hsd_add(hsd_acc* h, const or_psi* psi, const or_psi* pp, const or_op* op, int is_unitary,
                     const uint64_t* s, double w, int want_grad, int part, double* ok) {
     const cd lp = log_psi_cd(psi, s);
@@ -739,7 +746,30 @@ static void hsd_add(hsd_acc* h, const or_psi* psi, const or_psi* pp, const or_op
     const double lpa[2] = {lp.re, lp.im};
     or_local_energy(psi, op, s, lpa, el);
     const cd e = C(el[0], el[1]);
-    const cd lpp = log_psi_cd(pp, s);
+    cd lpp = log_psi_cd(pp, s);
+    const int fqa = psi->free_quantum_axis && part < 0;
+    const int N = psi->N;
+    cd* qa_o = NULL;   /* [2N] the alpha / beta O_k of this sample */
+    if (fqa) {
+        qa_o = (cd*)malloc(sizeof(cd) * 2 * (size_t)N);
+        cd corr = C(0.0, 0.0);
+        for (int i = 0; i < N; i++) {
+            uint64_t si[OR_MAX_WORDS];
+            memcpy(si, s, sizeof(uint64_t) * nwords_of(N));
+            spin_flip(si, i);
+            const cd r = cexp_(csub(log_psi_cd(pp, si), lpp));
+            const double sg = spin_at(s, i);
+            const double da = qa_at(pp->alpha, i) - qa_at(psi->alpha, i);
+            const double db = qa_at(pp->beta, i) - qa_at(psi->beta, i);
+            const double sa = qa_at(pp->alpha, i) + qa_at(psi->alpha, i);
+            const cd oa = cscale(sg, r);
+            const cd ob = cmul(C(0.0, 1.0), csub(cscale(cos(sa), r), C(sg * sin(sa), 0.0)));
+            qa_o[i] = oa;
+            qa_o[N + i] = ob;
+            corr = cadd(corr, cadd(cscale(da, oa), cscale(db, ob)));
+        }
+        lpp = cadd(lpp, corr);
+    }
     cd omega;
     if (is_unitary) {
         omega = cmul(cexp_(cconj(csub(lpp, lp))), e);
@@ -751,10 +781,13 @@ static void hsd_add(hsd_acc* h, const or_psi* psi, const or_psi* pp, const or_op
     const double pr = exp(2.0 * (lpp.re - lp.re));
     h->omega = cadd(h->omega, cscale(w, omega));
     h->pr += w * pr;
-    if (!want_grad) return;
+    if (!want_grad) { free(qa_o); return; }
     const int P = or_num_params(pp);
     if (part < 0) {
         or_O_k(pp, s, ok);
+        if (fqa)
+            for (int k = 0; k < 2 * N; k++) cstore(ok, k, qa_o[k]);
+        free(qa_o);
         for (int k = 0; k < P; k++) {
             const cd oc = cconj(cload(ok, k));
             cacc(h->omega_O, k, cmul(cscale(w, omega), oc));

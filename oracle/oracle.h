@@ -61,6 +61,12 @@ typedef struct {
     const double* bias_im[OR_MAX_LAYERS];
     const double* final_w_im;
     int translational_invariance;
+    /* free quantum axis (PsiBase.hpp:164): the Hilbert-space distance of a psi with it set
+     * adds the alpha / beta rotation terms (HilbertSpaceDistance.cu:47-81); alpha, beta [N]
+     * real, NULL = zeros */
+    int free_quantum_axis;
+    const double* alpha;
+    const double* beta;
 } or_psi;
 
 /* ---- random streams ---- */

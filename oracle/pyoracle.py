@@ -35,6 +35,7 @@ class _Psi(C.Structure):
         ("lhs_conn", _up * 3), ("lhs_w", _dp * 3), ("bias", _dp * 3), ("final_w", _dp),
         ("lhs_w_im", _dp * 3), ("bias_im", _dp * 3), ("final_w_im", _dp),
         ("translational_invariance", C.c_int),
+        ("free_quantum_axis", C.c_int), ("alpha", _dp), ("beta", _dp),
     ]
 
 
@@ -97,7 +98,7 @@ class Op:
 
 
 class RBM:
-    def __init__(self, b, W, prefactor=1.0):
+    def __init__(self, b, W, prefactor=1.0, alpha=None, beta=None, free_quantum_axis=False):
         self.b = _c128(b)
         self.W = _c128(W)
         self.N, self.M = self.W.shape
@@ -108,17 +109,28 @@ class RBM:
         self.c.prefactor = prefactor
         self.c.b = _ptr(self.b.view(np.float64))
         self.c.W = _ptr(self.W.view(np.float64))
+        _set_quaxis(self, alpha, beta, free_quantum_axis)
 
     @property
     def num_params(self):
         return 2 * self.N + self.M + self.N * self.M
 
 
+def _set_quaxis(obj, alpha, beta, free_quantum_axis):
+    """alpha / beta rotation angles [N] (real) and the free-quantum-axis flag of a psi."""
+    obj.alpha = np.ascontiguousarray(np.zeros(obj.N) if alpha is None else np.real(alpha), np.float64)
+    obj.beta = np.ascontiguousarray(obj.alpha if beta is None else np.real(beta), np.float64)
+    obj.c.alpha = _ptr(obj.alpha)
+    obj.c.beta = _ptr(obj.beta)
+    obj.c.free_quantum_axis = int(bool(free_quantum_axis))
+    return obj
+
+
 class Deep:
     """PsiDeep (pair=False) or PsiPair (pair=True) from complex per-layer arrays."""
 
     def __init__(self, N, biases, connections, weights, final_weights, prefactor=1.0, pair=False,
-                 translational_invariance=False):
+                 translational_invariance=False, alpha=None, beta=None, free_quantum_axis=False):
         self.N = N
         self.keep = []
         self.c = _Psi()
@@ -127,6 +139,7 @@ class Deep:
         self.c.prefactor = prefactor
         self.c.num_layers = len(biases)
         self.c.translational_invariance = int(translational_invariance)
+        _set_quaxis(self, alpha, beta, free_quantum_axis)
 
         def hold(a):
             self.keep.append(a)

@@ -83,11 +83,17 @@ static Operator load_operator(const std::string& prefix) {
     return Operator(tensor<cplx, 1>(coef, {S}), tensor<int, 2>(types, {S, L}), tensor<int, 2>(idx, {S, L}), false);
 }
 
+// the alpha angles of a free-quantum-axis case (meta fqa = 1), zeros otherwise
+static std::vector<double> load_alpha(const std::string& prefix, long N) {
+    return meta_i("fqa", 0) ? load<double>(prefix + "alpha.bin") : std::vector<double>(N, 0.0);
+}
+
 static Psi load_rbm(const std::string& prefix, long N, long M) {
-    std::vector<double> zeros(N, 0.0);
-    return Psi(tensor<double, 1>(zeros, {N}), tensor<double, 1>(zeros, {N}),
+    const auto alpha = load_alpha(prefix, N);
+    return Psi(tensor<double, 1>(alpha, {N}), tensor<double, 1>(alpha, {N}),
                tensor<cplx, 1>(load<cplx>(prefix + "b.bin"), {M}),
-               tensor<cplx, 2>(load<cplx>(prefix + "W.bin"), {N, M}), meta_d("prefactor", 1.0), false, false);
+               tensor<cplx, 2>(load<cplx>(prefix + "W.bin"), {N, M}), meta_d("prefactor", 1.0),
+               meta_i("fqa", 0) != 0, false);
 }
 
 template <typename Deep>
@@ -104,9 +110,10 @@ static Deep load_deep(const std::string& prefix, long N) {
         W.push_back(tensor<cplx, 2>(load<cplx>(prefix + "W" + std::to_string(l) + ".bin"), {c, size}));
     }
     const long last = meta_i("size" + std::to_string(L - 1));
-    std::vector<double> zeros(N, 0.0);
-    return Deep(tensor<double, 1>(zeros, {N}), tensor<double, 1>(zeros, {N}), b, conn, W,
-                tensor<cplx, 1>(load<cplx>(prefix + "fw.bin"), {last}), meta_d("prefactor", 1.0), false, false);
+    const auto alpha = load_alpha(prefix, N);
+    return Deep(tensor<double, 1>(alpha, {N}), tensor<double, 1>(alpha, {N}), b, conn, W,
+                tensor<cplx, 1>(load<cplx>(prefix + "fw.bin"), {last}), meta_d("prefactor", 1.0),
+                meta_i("fqa", 0) != 0, false);
 }
 
 template <typename P>

@@ -41,6 +41,7 @@ SIGNATURES = {
     "rbmg_psi_copy": [_vp, _vpp],
     "rbmg_psi_destroy": [_vp],
     "rbmg_psi_kind": [_vp, _ip],
+    "rbmg_psi_free_quantum_axis": [_vp, _ip],
     "rbmg_psi_shape": [_vp, _ip, _ip, _ip],
     "rbmg_psi_get_params": [_vp, _dp],
     "rbmg_psi_set_params": [_vp, _dp],

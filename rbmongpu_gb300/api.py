@@ -185,7 +185,9 @@ class _PsiBase:
 
     @property
     def free_quantum_axis(self):
-        return False
+        v = C.c_int()
+        call("rbmg_psi_free_quantum_axis", self._h, C.byref(v))
+        return bool(v.value)
 
     def _vector(self):
         out = np.zeros(1 << self.N, np.complex128)
@@ -194,8 +196,8 @@ class _PsiBase:
 
     @property
     def vector(self):
-        # alpha / beta rotations of pyRBMonGPU/Psi.py:62-74 need QuantumExpression; with the
-        # free quantum axis unsupported they are zero and the vector is the plain amplitude list
+        # the alpha / beta rotations of pyRBMonGPU/Psi.py:62-74 are built with QuantumExpression
+        # (not bundled); the vector is the plain amplitude list, exact where alpha = beta = 0
         return self._vector()
 
     def norm(self, exact_summation):

@@ -57,6 +57,7 @@ struct Workspace {
     DevBuf partial, block_scratch, sums, acc_O, acc_EO, acc_Ek, acc_wO, acc_pO, block_max, zsum;
     DevBuf smat, smean, okrows, sshift, splanes, serror, sout;
     DevBuf acc_B, eabs2, lsums, rw, rwc, acc_C2, acc_C3;
+    DevBuf fqa_qa, fqa_r, fqa_flip, fqa_lpf, fqa_lp, fqa_out;   // free-quantum-axis terms of the HSD
 };
 
 static Workspace& ws() {
@@ -170,7 +171,6 @@ extern "C" int rbmg_psi_create(int N, int M, const double* alpha, const double* 
     (void)beta;
     if (!out || N <= 0 || M <= 0 || !b || !W) return fail(RBMG_EINVAL, "Psi: bad arguments");
     if (N > 64 * kMaxWords) return fail(RBMG_EINVAL, "Psi: N exceeds 256 spins");
-    if (free_quantum_axis) return fail(RBMG_EUNSUPPORTED, "Psi: free_quantum_axis is not provided");
     const int K = rbm_lanes_k(M);
     if (K < 0) return fail(RBMG_EINVAL, "Psi: M exceeds the largest instantiated hidden layer (576)");
     auto p = std::make_unique<rbmg_psi>();
@@ -179,6 +179,7 @@ extern "C" int rbmg_psi_create(int N, int M, const double* alpha, const double* 
     p->M = M;
     p->Mpad = 32 * K;
     p->prefactor = prefactor;
+    p->free_quantum_axis = free_quantum_axis ? 1 : 0;
     p->alpha.assign(N, 0.0);
     if (alpha) p->alpha.assign(alpha, alpha + N);
     p->beta = p->alpha;   // include/quantum_state/PsiBase.hpp:176, 190: beta_array(alpha)
@@ -202,11 +203,11 @@ extern "C" int rbmg_psi_deep_create(int N, int num_layers, const int* sizes, con
         !weights || !final_weights)
         return fail(RBMG_EINVAL, "PsiDeep: bad arguments");
     if (N > 64 * kMaxWords) return fail(RBMG_EINVAL, "PsiDeep: N exceeds 256 spins");
-    if (free_quantum_axis) return fail(RBMG_EUNSUPPORTED, "PsiDeep: free_quantum_axis is not provided");
     auto p = std::make_unique<rbmg_psi>();
     p->kind = pair ? 2 : 1;
     p->N = N;
     p->prefactor = prefactor;
+    p->free_quantum_axis = free_quantum_axis ? 1 : 0;
     p->alpha.assign(N, 0.0);
     if (alpha) p->alpha.assign(alpha, alpha + N);
     p->beta = p->alpha;
@@ -246,6 +247,7 @@ extern "C" int rbmg_psi_copy(const rbmg_psi* psi, rbmg_psi** out) {
     p->prefactor = psi->prefactor;
     p->alpha = psi->alpha;
     p->beta = psi->beta;
+    p->free_quantum_axis = psi->free_quantum_axis;
     p->M = psi->M;
     p->Mpad = psi->Mpad;
     p->b = psi->b;
@@ -328,6 +330,12 @@ extern "C" int rbmg_psi_set_params(rbmg_psi* psi, const double* params) {
     }
     for (auto& v : psi->final_weights) v = in[k++];
     return deep_upload(psi);
+}
+
+extern "C" int rbmg_psi_free_quantum_axis(const rbmg_psi* psi, int* on) {
+    if (!psi || !on) return fail(RBMG_EINVAL, "free_quantum_axis: null");
+    *on = psi->free_quantum_axis;
+    return RBMG_OK;
 }
 
 extern "C" int rbmg_psi_get_prefactor(const rbmg_psi* psi, double* prefactor) {
@@ -1641,6 +1649,45 @@ extern "C" int rbmg_hsd_gradient(const rbmg_psi* psi, const rbmg_psi* pp, const 
         if (r == RBMG_OK) r = rbm_upload64(pp);
         if (r != RBMG_OK) return r;
     }
+    // free quantum axis of psi (HilbertSpaceDistance.cu:47-81, 109-122): log psi' of every
+    // sample gains sum_i [da_i s_i r_i + i db_i (r_i cos_i - s_i sin_i)], r_i = psi'(s with
+    // spin i flipped) / psi'(s), and the gradient its alpha / beta entries; the PsiPair
+    // gradient (HilbertSpaceDistance_PsiPair.cu) has no such branch
+    const bool fqa = psi->free_quantum_axis && !(pp->kind == 2 && want_grad);
+    if (fqa) {
+        std::vector<double> qa(4 * static_cast<size_t>(N));
+        for (int i = 0; i < N; i++) {
+            qa[i] = pp->alpha[i] - psi->alpha[i];
+            qa[N + i] = pp->beta[i] - psi->beta[i];
+            qa[2 * N + i] = std::cos(pp->alpha[i] + psi->alpha[i]);
+            qa[3 * N + i] = std::sin(pp->alpha[i] + psi->alpha[i]);
+        }
+        RBMG_CK(W.fqa_qa.ensure(sizeof(double) * qa.size()));
+        RBMG_CK(cudaMemcpyAsync(W.fqa_qa.p, qa.data(), sizeof(double) * qa.size(), cudaMemcpyHostToDevice, stream()));
+        if (want_grad) RBMG_CK(W.fqa_r.ensure(sizeof(double2) * total * N));
+    }
+    // the free-quantum-axis terms of one chunk of samples, in sub-chunks of <= 2^20 flips
+    auto fqa_chunk = [&](const Chunk& c, uint64_t offset) -> int {
+        const int per = std::max(1, (1 << 20) / N);
+        RBMG_CK(W.fqa_flip.ensure(sizeof(uint64_t) * static_cast<size_t>(per) * N * nw));
+        RBMG_CK(W.fqa_lpf.ensure(sizeof(double2) * static_cast<size_t>(per) * N));
+        RBMG_CK(W.fqa_lp.ensure(sizeof(double2) * per));
+        if (!want_grad) RBMG_CK(W.fqa_r.ensure(sizeof(double2) * static_cast<size_t>(per) * N));
+        for (int b0 = 0; b0 < c.count; b0 += per) {
+            const int n = std::min(per, c.count - b0);
+            const uint64_t* sp = c.spins ? c.spins + static_cast<size_t>(b0) * nw : nullptr;
+            const uint64_t eb = c.enum_base + static_cast<uint64_t>(b0);
+            RBMG_CK(launch_flip_each(n, N, sp, eb, c.enumerate, W.fqa_flip.as<uint64_t>(), stream()));
+            int rr = psi_log_psi_dev(pp, n * N, W.fqa_flip.as<uint64_t>(), 0, 0, W.fqa_lpf.as<double2>());
+            if (rr == RBMG_OK) rr = psi_log_psi_dev(pp, n, sp, eb, c.enumerate, W.fqa_lp.as<double2>());
+            if (rr != RBMG_OK) return rr;
+            double2* rout = want_grad ? W.fqa_r.as<double2>() + (offset + b0) * static_cast<size_t>(N)
+                                      : W.fqa_r.as<double2>();
+            RBMG_CK(launch_fqa_terms(n, N, sp, eb, c.enumerate, W.fqa_lp.as<double2>(), W.fqa_lpf.as<double2>(),
+                                     W.fqa_qa.as<double>(), W.logpsi_p.as<double2>() + b0, rout, stream()));
+        }
+        return RBMG_OK;
+    };
     for (int pass = 0; pass < passes; pass++) {
         // ---- stage 1
         RBMG_CK(W.omega.ensure(sizeof(double2) * total));
@@ -1671,6 +1718,10 @@ extern "C" int rbmg_hsd_gradient(const rbmg_psi* psi, const rbmg_psi* pp, const 
             } else {
                 const int rr = deep_hsd64_chunk(psi, pp, op, c, W.eloc.as<double2>(), W.logpsi_p.as<double2>(),
                                                 stream());
+                if (rr != RBMG_OK) return rr;
+            }
+            if (fqa) {
+                const int rr = fqa_chunk(c, offset);
                 if (rr != RBMG_OK) return rr;
             }
             RBMG_CK(launch_hsd_terms64(c.count, W.eloc.as<double2>(), W.logpsi_p.as<double2>(), is_unitary,
@@ -1748,7 +1799,16 @@ extern "C" int rbmg_hsd_gradient(const rbmg_psi* psi, const rbmg_psi* pp, const 
         }
         std::vector<double2> acc(ok_len);
         RBMG_CK(cudaMemcpyAsync(acc.data(), W.acc_wO.p, sizeof(double2) * ok_len, cudaMemcpyDeviceToHost, stream()));
+        std::vector<double2> acc_qa(fqa ? 2 * static_cast<size_t>(N) : 0);
+        if (fqa) {   // the alpha / beta entries (mode 0 only: fqa is off for the PsiPair gradient)
+            RBMG_CK(W.fqa_out.ensure(sizeof(double2) * 2 * N));
+            RBMG_CK(launch_fqa_grad(count, N, sp, 0, enumerate, W.coef1.as<double2>(), W.fqa_r.as<double2>(),
+                                    W.fqa_qa.as<double>(), W.fqa_out.as<double2>(), stream()));
+            RBMG_CK(cudaMemcpyAsync(acc_qa.data(), W.fqa_out.p, sizeof(double2) * 2 * N, cudaMemcpyDeviceToHost,
+                                    stream()));
+        }
         RBMG_CK(cudaStreamSynchronize(stream()));
+        for (size_t k = 0; k < acc_qa.size(); k++) gout[k] = -(cplx(acc_qa[k].x, acc_qa[k].y) * f);
         // the coefficients already carry 1/v^2/d^nu (mode 0), 1/v^2/d (mode 1), 1/v/d (mode 2)
         if (mode == 0) {          // HilbertSpaceDistance.cu:253-263
             for (size_t k = 0; k < ok_len; k++) gout[2 * N + k] = -(cplx(acc[k].x, acc[k].y) * f);

@@ -74,6 +74,7 @@ struct rbmg_psi {
     int N = 0;
     double prefactor = 1.0;
     std::vector<double> alpha, beta;
+    int free_quantum_axis = 0;   // the Hilbert-space distance's alpha / beta terms (PsiBase.hpp:164)
     // RBM
     int M = 0, Mpad = 0;
     std::vector<rbmg::cplx> b, W;

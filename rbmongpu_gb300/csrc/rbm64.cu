@@ -182,7 +182,109 @@ __global__ void hsd_coef_kernel(int count, const double* __restrict__ w, const d
     }
 }
 
+__device__ __forceinline__ double spin_of(const uint64_t* spins, uint64_t enum_base, int enumerate, long t, int N,
+                                          int i) {
+    const int nw = (N + 63) / 64;
+    const uint64_t word = enumerate ? ((i >> 6) == 0 ? enum_base + static_cast<uint64_t>(t) : 0ull)
+                                    : spins[t * nw + (i >> 6)];
+    return ((word >> (i & 63)) & 1ull) ? 1.0 : -1.0;
+}
+
+__global__ void flip_each_kernel(int count, int N, const uint64_t* spins, uint64_t enum_base, int enumerate,
+                                 uint64_t* out) {
+    const int nw = (N + 63) / 64;
+    const long total = static_cast<long>(count) * N;
+    for (long q = blockIdx.x * 256L + threadIdx.x; q < total; q += static_cast<long>(gridDim.x) * 256) {
+        const long t = q / N;
+        const int i = static_cast<int>(q - t * N);
+        for (int k = 0; k < nw; k++) {
+            uint64_t w = enumerate ? (k == 0 ? enum_base + static_cast<uint64_t>(t) : 0ull) : spins[t * nw + k];
+            if ((i >> 6) == k) w ^= 1ull << (i & 63);
+            out[q * nw + k] = w;
+        }
+    }
+}
+
+__global__ void fqa_terms_kernel(int count, int N, const uint64_t* spins, uint64_t enum_base, int enumerate,
+                                 const double2* lp, const double2* lpf, const double* qa, double2* dl, double2* r) {
+    for (long t = blockIdx.x * 256L + threadIdx.x; t < count; t += static_cast<long>(gridDim.x) * 256) {
+        const double2 l0 = lp[t];
+        double cx = 0.0, cy = 0.0;
+        for (int i = 0; i < N; i++) {
+            const double2 li = lpf[t * N + i];
+            const double m = exp(li.x - l0.x);
+            const double rx = m * cos(li.y - l0.y), ry = m * sin(li.y - l0.y);
+            if (r) r[t * N + i] = make_double2(rx, ry);
+            const double sg = spin_of(spins, enum_base, enumerate, t, N, i);
+            const double da = qa[i], db = qa[N + i], cs = qa[2 * N + i], sn = qa[3 * N + i];
+            // da s_i r_i + i db (r_i cos - s_i sin)
+            cx += da * sg * rx - db * (ry * cs);
+            cy += da * sg * ry + db * (rx * cs - sg * sn);
+        }
+        dl[t] = make_double2(dl[t].x + cx, dl[t].y + cy);
+    }
+}
+
+// one block per angle k (alpha_i: k = i, beta_i: k = N + i)
+__global__ void fqa_grad_kernel(int count, int N, const uint64_t* spins, uint64_t enum_base, int enumerate,
+                                const double2* c, const double2* r, const double* qa, double2* out) {
+    __shared__ double2 red[256];
+    const int k = blockIdx.x, i = k % N;
+    const bool beta = k >= N;
+    double ax = 0.0, ay = 0.0;
+    for (long t = threadIdx.x; t < count; t += 256) {
+        const double2 rv = r[t * N + i];
+        const double sg = spin_of(spins, enum_base, enumerate, t, N, i);
+        double ox, oy;
+        if (beta) {   // i (r cos - s sin)
+            ox = -(rv.y * qa[2 * N + i]);
+            oy = rv.x * qa[2 * N + i] - sg * qa[3 * N + i];
+        } else {      // s r
+            ox = sg * rv.x;
+            oy = sg * rv.y;
+        }
+        const double2 cv = c[t];
+        // c conj(O)
+        ax += cv.x * ox + cv.y * oy;
+        ay += cv.y * ox - cv.x * oy;
+    }
+    red[threadIdx.x] = make_double2(ax, ay);
+    __syncthreads();
+    for (int h = 128; h >= 1; h >>= 1) {
+        if (threadIdx.x < h)
+            red[threadIdx.x] = make_double2(red[threadIdx.x].x + red[threadIdx.x + h].x,
+                                            red[threadIdx.x].y + red[threadIdx.x + h].y);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[k] = red[0];
+}
+
 }  // namespace
+
+cudaError_t launch_flip_each(int count, int N, const uint64_t* spins, uint64_t enum_base, int enumerate,
+                             uint64_t* out, cudaStream_t st) {
+    if (count <= 0) return cudaSuccess;
+    const long total = static_cast<long>(count) * N;
+    flip_each_kernel<<<static_cast<int>(std::min(4096L, (total + 255) / 256)), 256, 0, st>>>(count, N, spins, enum_base,
+                                                                                           enumerate, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fqa_terms(int count, int N, const uint64_t* spins, uint64_t enum_base, int enumerate,
+                             const double2* lp, const double2* lpf, const double* qa, double2* dl, double2* r,
+                             cudaStream_t st) {
+    if (count <= 0) return cudaSuccess;
+    fqa_terms_kernel<<<static_cast<int>(std::min(1024L, (count + 255L) / 256)), 256, 0, st>>>(
+        count, N, spins, enum_base, enumerate, lp, lpf, qa, dl, r);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fqa_grad(int count, int N, const uint64_t* spins, uint64_t enum_base, int enumerate,
+                            const double2* c, const double2* r, const double* qa, double2* out, cudaStream_t st) {
+    if (count <= 0) return cudaSuccess;
+    fqa_grad_kernel<<<2 * N, 256, 0, st>>>(count, N, spins, enum_base, enumerate, c, r, qa, out);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_rbm_hsd64(const Rbm64& P, const Rbm64& PP, const OpDev& op, const Hsd64Launch& L,
                              cudaStream_t st) {

@@ -141,8 +141,17 @@ def act_points(rng):
     return np.asarray(z, np.complex128)
 
 
+def quaxis(meta, arrays, rng, N):
+    """free quantum axis: alpha angles of psi and of psi' (alpha' = alpha + N(0, 0.05^2));
+    the reference sets beta = alpha (include/quantum_state/PsiBase.hpp:176)."""
+    alpha = rng.normal(0, 0.3, N)
+    meta["fqa"] = 1
+    arrays["alpha.bin"] = alpha
+    arrays["pp_alpha.bin"] = alpha + rng.normal(0, 0.05, N)
+
+
 def rbm_case(name, N, M, sigma, seed, op, hop, unitary, nu, mc=None, normalize=True, ok_count=4, smatrix=False,
-             kl=False, ev_extra=False):
+             kl=False, ev_extra=False, fqa=False):
     rng = np.random.Generator(np.random.PCG64(seed))
     b = cnormal(rng, M, sigma)
     W = cnormal(rng, (N, M), sigma)
@@ -158,13 +167,15 @@ def rbm_case(name, N, M, sigma, seed, op, hop, unitary, nu, mc=None, normalize=T
         meta["ev_extra"] = 1
     arrays = {"b.bin": b, "W.bin": W, "pp_b.bin": pb, "pp_W.bin": pW, "ok_spins.bin": ok_spins,
               "act_in.bin": act_points(rng)}
+    if fqa:
+        quaxis(meta, arrays, rng, N)
     arrays.update(op_arrays("op_", op))
     arrays.update(op_arrays("hop_", hop))
     run_case(name, meta, arrays, keep={k.replace(".bin", "") for k in arrays})
 
 
 def deep_case(name, kind, N, sizes, conns, sigma, seed, op, hop, unitary, nu, mc=None, dense=False, hsd2=None,
-              diag_density=0, ev_extra=False):
+              diag_density=0, ev_extra=False, fqa=False):
     rng = np.random.Generator(np.random.PCG64(seed))
     if dense:
         conn = [np.tile(np.arange(c, dtype=np.uint32)[:, None], (1, m)) for c, m in zip(conns, sizes)]
@@ -192,6 +203,8 @@ def deep_case(name, kind, N, sizes, conns, sigma, seed, op, hop, unitary, nu, mc
         meta.update(mc)
     if ev_extra:   # fluctuation_gradient, the operator list [op, hop] and corrected(op, hop)
         meta["ev_extra"] = 1
+    if fqa:
+        quaxis(meta, arrays, rng, N)
     arrays.update(op_arrays("op_", op))
     arrays.update(op_arrays("hop_", hop))
     if diag_density:
@@ -250,6 +263,13 @@ def main():
     cf, ty, ix = tfim_chain(6, 1.0, 1.0)
     deep_case("deep6_hsd2", "deep", 6, [12, 6], [3, 4], 0.2, 106, tfim_chain(6), identity_op(), True, 1.0,
               hsd2=(-0.02j * cf, ty, ix), diag_density=3)
+    # free quantum axis (alpha / beta rotations in the Hilbert-space distance): a small RBM and
+    # a small PsiDeep with random alpha, psi' alpha perturbed, the non-unitary step operator
+    cf, ty, ix = tfim_chain(6, 1.0, 0.7)
+    rbm_case("rbm6_hsd_fqa", 6, 12, 0.1, 17, tfim_chain(6, 1.0, 0.7), (1j * 1e-2 * cf, ty, ix), False, 1.0,
+             fqa=True)
+    deep_case("deep6_hsd_fqa", "deep", 6, [12, 6], [3, 4], 0.2, 18, tfim_chain(6), (1j * 1e-2 * cf, ty, ix),
+              False, 1.0, fqa=True)
     # PsiPair 3 -> [9, 6] connectivity [1, 3] (the reference's test fixture)
     deep_case("pair3", "pair", 3, [9, 6], [1, 3], 0.3, 105, tfim_chain(3), identity_op(), True, 1.0)
 

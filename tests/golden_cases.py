@@ -36,6 +36,12 @@ class Case:
     def prefactor(self):
         return self.s("prefactor") if self.has("s_prefactor") else 1.0
 
+    # free quantum axis: (alpha angles [N], flag); the reference sets beta = alpha
+    def quaxis(self, prefix=""):
+        if self.meta("fqa", 0):
+            return self.i(prefix + "alpha"), True
+        return np.zeros(self.N), False
+
     # RBM parameters
     def rbm(self, prefix=""):
         N, M = self.N, int(self.meta("M"))
@@ -54,4 +60,4 @@ class Case:
 
 
 ALL = ["c1_rbm_exact", "rbm6_hsd_nonunitary", "rbm8_mixed_operator", "c2_rbm_mc", "deep8_sparse",
-       "deep10_dense", "pair3"]
+       "deep10_dense", "pair3", "rbm6_hsd_fqa", "deep6_hsd_fqa"]

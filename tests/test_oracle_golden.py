@@ -13,12 +13,15 @@ def close(a, b, rtol, atol):
 
 def rbm_of(case, prefix=""):
     b, W = case.rbm(prefix)
-    return po.RBM(b, W, case.prefactor if prefix == "" else 1.0)
+    alpha, fqa = case.quaxis(prefix)
+    return po.RBM(b, W, case.prefactor if prefix == "" else 1.0, alpha=alpha, beta=alpha, free_quantum_axis=fqa)
 
 
 def deep_of(case, prefix=""):
     b, c, w, fw = case.deep(prefix)
-    return po.Deep(case.N, b, c, w, fw, case.prefactor if prefix == "" else 1.0, pair=case.kind == "pair")
+    alpha, fqa = case.quaxis(prefix)
+    return po.Deep(case.N, b, c, w, fw, case.prefactor if prefix == "" else 1.0, pair=case.kind == "pair",
+                   alpha=alpha, beta=alpha, free_quantum_axis=fqa)
 
 
 def psi_of(case, prefix=""):
@@ -57,7 +60,7 @@ def test_exact_summation_matches_reference(name):
 
 
 @pytest.mark.parametrize("name", ["c1_rbm_exact", "rbm6_hsd_nonunitary", "rbm8_mixed_operator",
-                                  "deep8_sparse", "deep10_dense", "pair3"])
+                                  "deep8_sparse", "deep10_dense", "pair3", "rbm6_hsd_fqa", "deep6_hsd_fqa"])
 def test_hilbert_space_distance_matches_reference(name):
     c = Case(name)
     psi, pp = psi_of(c), psi_of(c, "pp_")
