@@ -1063,21 +1063,33 @@ def new_neural_network(N, M, initial_value=(0.01 + 1j * math.pi / 4), alpha=0, b
 def new_deep_neural_network(N, M, C_, initial_value=(0.01 + 1j * math.pi / 4), alpha=0, beta=0,
                             free_quantum_axis=False, noise=1e-4, gpu=True, pair=False, noise_modulation="auto",
                             final_weights=10):
-    """pyRBMonGPU/new_neural_network.py:53-153 (1D networks)."""
+    """pyRBMonGPU/new_neural_network.py:53-153.  1D: N spins, layer sizes M [l], connections
+    per unit C_ [l].  2D: N = (rows, cols), M and C_ lists of (rows, cols) pairs; unit (j1, j2)
+    of a layer connects to the units ((j1 d1 + i1) % n0, (j2 d2 + i2) % n1) of the layer below,
+    numbered row * n0 + col as the reference numbers them.  numpy's global random state is
+    consumed in the reference's order, so a seeded caller gets the reference's network."""
+    dim = len(N) if isinstance(N, (list, tuple)) else 1
+    N_lin = N if dim == 1 else N[0] * N[1]
+    M_lin = M if dim == 1 else [m[0] * m[1] for m in M]
+    C_lin = C_ if dim == 1 else [c[0] * c[1] for c in C_]
     for n, m, c in zip([N] + M[:-1], M, C_):
-        assert (m * c) % n == 0
-        assert c <= n
+        if dim == 1:
+            assert (m * c) % n == 0
+            assert c <= n
+        else:
+            assert (m[0] * c[0]) % n[0] == 0 and (m[1] * c[1]) % n[1] == 0
+            assert c[0] <= n[0] and c[1] <= n[1]
     if isinstance(alpha, (float, int)):
-        alpha = alpha * np.ones(N)
+        alpha = alpha * np.ones(N_lin)
     if isinstance(beta, (float, int)):
-        beta = beta * np.ones(N)
-    b = [noise * complex_noise(m) for m in M]
-    w = noise * complex_noise((C_[0], M[0]))
-    w[C_[0] // 2, :] += initial_value
+        beta = beta * np.ones(N_lin)
+    b = [noise * complex_noise(m) for m in M_lin]
+    w = noise * complex_noise((C_lin[0], M_lin[0]))
+    w[C_lin[0] // 2, :] += initial_value
     W = [w]
     if noise_modulation == "auto":
-        noise_modulation = [math.sqrt(6 / (c + next_c)) for c, next_c in zip(C_[1:], C_[2:] + [1])]
-    for c, m, next_c, nm in zip(C_[1:], M[1:], C_[2:] + [1], noise_modulation):
+        noise_modulation = [math.sqrt(6 / (c + next_c)) for c, next_c in zip(C_lin[1:], C_lin[2:] + [1])]
+    for c, m, next_c, nm in zip(C_lin[1:], M_lin[1:], C_lin[2:] + [1], noise_modulation):
         W.append(nm * math.sqrt(6 / (c + next_c)) * real_noise((c, m)) + noise * complex_noise((c, m)))
 
     def delta_func(n, m, c):
@@ -1089,10 +1101,18 @@ def new_deep_neural_network(N, M, C_, initial_value=(0.01 + 1j * math.pi / 4), a
 
     connections = []
     for n, m, c in zip([N] + M[:-1], M, C_):
-        d = delta_func(n, m, c)
-        connections.append(np.array([[(j * d + i) % n for j in range(m)] for i in range(c)]))
+        if dim == 1:
+            d = delta_func(n, m, c)
+            connections.append(np.array([[(j * d + i) % n for j in range(m)] for i in range(c)]))
+        else:
+            d1, d2 = delta_func(n[0], m[0], c[0]), delta_func(n[1], m[1], c[1])
+            units = [(j1, j2) for j1 in range(m[0]) for j2 in range(m[1])]
+            inputs = [(i1, i2) for i1 in range(c[0]) for i2 in range(c[1])]
+            connections.append(np.array([[((j1 * d1 + i1) % n[0]) * n[0] + (j2 * d2 + i2) % n[1]
+                                          for j1, j2 in units] for i1, i2 in inputs]))
     if isinstance(final_weights, (float, int)):
-        final_weights = final_weights * np.ones(M[-1])
+        final_weights = final_weights * np.ones(M_lin[-1])
+    assert len(final_weights) == M_lin[-1]
     cls = PsiPair if pair else PsiDeep
     return cls(alpha, beta, b, connections, W, final_weights, 1.0, free_quantum_axis, gpu)
 
