@@ -249,6 +249,48 @@ __device__ __forceinline__ bool rbm_mh_step2(const RbmDev& P, Spins<NW>& s, pair
     return accept;
 }
 
+// The single-flip proposal of rbm_mh_step2 with the walker's angles and Re f in this
+// warp's shared-memory slice st [3][KP][32] pairs (theta re, theta im, Re f) instead of
+// registers: the same operations in the same order, so the same chain bit for bit.  It
+// frees ~3 KP registers per lane, which for the large hidden layers lets more warps stay
+// resident to hide the dependent chain of each proposal.
+template <int K, int KP, int NW>
+__device__ __forceinline__ bool rbm_flip_step_s(const RbmDev& P, Spins<NW>& s, pair_t* st, WarpRng& rng, int lane,
+                                                uint64_t nmagic) {
+    const int site = static_cast<int>(fastmod(rng.next(), nmagic, static_cast<uint32_t>(P.N)));
+    const pair_t two_s = splat2(s.up(site) ? -2.0f : 2.0f);   // 2 x the new spin
+    const float4* row = P.Wq + static_cast<long>(site) * KP * 32 + lane;
+    float4 w[KP];
+#pragma unroll
+    for (int kk = 0; kk < KP; kk++) w[kk] = __ldg(row + 32 * kk);
+    float part = 0.0f;
+#pragma unroll
+    for (int kk = 0; kk < KP; kk++) {
+        const pair_t nr = fma2(two_s, pk2(w[kk].x, w[kk].y), st[kk * 32 + lane]);
+        const pair_t ni = fma2(two_s, pk2(w[kk].z, w[kk].w), st[(KP + kk) * 32 + lane]);
+        float d0, d1;
+        up2(sub2(lc_re2(nr, ni), st[(2 * KP + kk) * 32 + lane]), d0, d1);
+        part = __fadd_rn(part, d0);
+        if (2 * kk + 1 < K) part = __fadd_rn(part, d1);
+    }
+    const float delta = warp_sum_xor(part);
+    bool accept = delta > 0.0f;
+    if (!accept) accept = rng.uniform() <= expf_det(__fmul_rn(2.0f, delta));
+    if (accept) {
+        s.flip(site);
+#pragma unroll
+        for (int kk = 0; kk < KP; kk++) {
+            const float4 ww = __ldg(row + 32 * kk);
+            const pair_t tr = fma2(two_s, pk2(ww.x, ww.y), st[kk * 32 + lane]);
+            const pair_t ti = fma2(two_s, pk2(ww.z, ww.w), st[(KP + kk) * 32 + lane]);
+            st[kk * 32 + lane] = tr;
+            st[(KP + kk) * 32 + lane] = ti;
+            st[(2 * KP + kk) * 32 + lane] = lc_re2(tr, ti);
+        }
+    }
+    return accept;
+}
+
 // One update of the fast sweep (MonteCarloLoop.hpp:162-171): the proposal flips the spins
 // of a mask that is the AND of `tries` random configurations (each spin flips with
 // probability 2^-tries; the mask is warp-uniform).  Unlike the reference, whose Psi keeps
@@ -473,6 +515,64 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, K > 13 ? 3 : 4) rbm_mc_ke
         for (int kk = 0; kk < KP; kk++) re[kk] = lc_re2(tr[kk], ti[kk]);
         for (int p = 0; p < P.N; p++)
             acc += rbm_mh_step2<K>(P, s, tr, ti, re, rng, lane, L.total_z, nmagic);
+        props += P.N;
+        const int done = sw + 1 - L.n_therm;
+        if (done > 0 && done % L.sweeps_per_sample == 0) {
+            const long row = static_cast<long>(L.sample_base + sample) * L.B + w;
+            if (L.sample_spins && lane == 0) {
+#pragma unroll
+                for (int k = 0; k < NW; k++) L.sample_spins[row * NW + k] = s.w[k];
+            }
+            sample++;
+        }
+    }
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < NW; k++) L.spins[static_cast<long>(w) * NW + k] = s.w[k];
+        L.rng_index[w] = rng.index;
+        L.accepts[w] += acc;
+        L.proposals[w] += props;
+    }
+}
+
+// The sampler for large hidden layers (K >= 13) without the S_z constraint: the walker
+// state in shared memory (rbm_flip_step_s), 6 blocks of 4 warps per SM instead of 4 (3).
+// Chains, samples and counters are those of rbm_mc_kernel.
+template <int K, int NW>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock, 6) rbm_mc_smem_kernel(RbmDev P, McLaunch L) {
+    const int lane = threadIdx.x & 31;
+    const int w = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+    if (w >= L.B) return;
+    constexpr int KP = (K + 1) / 2;
+    extern __shared__ pair_t s_state[];
+    pair_t* st = s_state + (threadIdx.x >> 5) * 3 * KP * 32;
+    WarpRng rng;
+    rng.init(L.seed, L.walker_base + static_cast<uint32_t>(w), L.rng_index[w], lane);
+    const uint64_t nmagic = fastmod_magic(static_cast<uint32_t>(P.N));
+    Spins<NW> s;
+    if (L.init) {
+#pragma unroll
+        for (int k = 0; k < NW; k++) s.w[k] = 0;
+        draw_spins(rng, P.N, s);
+    } else {
+#pragma unroll
+        for (int k = 0; k < NW; k++) s.w[k] = L.spins[static_cast<long>(w) * NW + k];
+    }
+    unsigned long long acc = 0, props = 0;
+    const int total_sweeps = L.n_therm + L.n_samples * L.sweeps_per_sample;
+    int sample = 0;
+    for (int sw = 0; sw < total_sweeps; sw++) {
+        {
+            pair_t tr[KP], ti[KP];
+            rbm_refresh2(P, s, tr, ti, lane);
+#pragma unroll
+            for (int kk = 0; kk < KP; kk++) {
+                st[kk * 32 + lane] = tr[kk];
+                st[(KP + kk) * 32 + lane] = ti[kk];
+                st[(2 * KP + kk) * 32 + lane] = lc_re2(tr[kk], ti[kk]);
+            }
+        }
+        for (int p = 0; p < P.N; p++) acc += rbm_flip_step_s<K, KP>(P, s, st, rng, lane, nmagic);
         props += P.N;
         const int done = sw + 1 - L.n_therm;
         if (done > 0 && done % L.sweeps_per_sample == 0) {
@@ -757,6 +857,18 @@ cudaError_t rbm_mc_launch_k(const RbmDev& P, const OpDev* op, const McLaunch& L,
             case 2: rbm_mc_fast_kernel<K, 2><<<grid, block, 0, st>>>(P, L); break;
             case 3: rbm_mc_fast_kernel<K, 3><<<grid, block, 0, st>>>(P, L); break;
             case 4: rbm_mc_fast_kernel<K, 4><<<grid, block, 0, st>>>(P, L); break;
+            default: return cudaErrorInvalidValue;
+        }
+        return cudaGetLastError();
+    }
+    if (K >= 13 && !L.total_z) {
+        constexpr int KP = (K + 1) / 2;
+        const size_t sm = sizeof(pair_t) * 3 * KP * 32 * kWarpsPerBlock;
+        switch (nw) {
+            case 1: rbm_mc_smem_kernel<K, 1><<<grid, block, sm, st>>>(P, L); break;
+            case 2: rbm_mc_smem_kernel<K, 2><<<grid, block, sm, st>>>(P, L); break;
+            case 3: rbm_mc_smem_kernel<K, 3><<<grid, block, sm, st>>>(P, L); break;
+            case 4: rbm_mc_smem_kernel<K, 4><<<grid, block, sm, st>>>(P, L); break;
             default: return cudaErrorInvalidValue;
         }
         return cudaGetLastError();
