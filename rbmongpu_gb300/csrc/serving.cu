@@ -5,23 +5,24 @@
 // queue (one atomic counter): first the walker tasks of every instance, longest first
 // (sweeps of single-flip Metropolis, then at the final configuration the local energy,
 // tanh(theta), the angles, U_j = sum_n e_n tanh(theta''_nj) over every string and the
-// terms e_n of the off-diagonal strings), then the reduction tasks, each a tile of rows by
-// a chunk of walkers of one instance's sums, which start once that instance's walkers are
-// all done (a per-instance counter; the wait is bounded by a wall-clock limit after which
-// the kernel raises an error flag and returns).  Each tile writes its chunk's partial sums;
-// a second kernel of the graph adds the chunks in a fixed order, so every replay gives the
-// same sums bit for bit.  The walker tasks are compiled for each hidden-unit count per
-// lane (1, 2, 4, 8, 13, 18: M <= 576) as separate functions of the one kernel.  The
-// launch (counter resets + both kernels) is captured once in a CUDA graph and replayed;
-// the warps per block, the reduction tile height and a register cap come from an
-// autotuner that times the candidates on the batch itself.
+// terms e_n of the off-diagonal strings), then the reduction tasks,
+// each a tile of rows by a chunk of walkers of one instance's sums, which start once that
+// instance's walkers are all done (a per-instance counter; the wait is bounded by a
+// wall-clock limit after which the kernel raises an error flag and returns).  Each tile
+// writes its chunk's partial sums; a second kernel of the graph adds the chunks in a fixed
+// order, so every replay gives the same sums bit for bit.  The walker tasks are compiled
+// for each hidden-unit count per lane (1, 2, 4, 8, 13, 18: M <= 576) as separate functions
+// of the one kernel.  The launch (counter resets + both kernels) is captured once in a
+// CUDA graph and replayed; the warps per block, the reduction tile height and a register
+// cap come from an autotuner that times the candidates on the batch itself.
 //
 // Per instance and replay the result is <E_loc> over its walkers and the reference's O_k
 // gradient <E O*> + conj<E_k> - 2 <E> <O*> (source/network_functions/ExpectationValue.cu:
 // 243-253), with E_k(s) = sum_n e_n O_k(s'_n) (include/operator/Operator.hpp:145-179): for
-// W_ij, s_i (U_j - 2 V_ij) with V_ij the terms of the strings flipping site i, their
-// tanh(theta'') recomputed in the reduction tile from the stored angles.  The sums run
-// centred on the instance's mean energy E (the same value in every tile):
+// W_ij, s_i (U_j - 2 V_ij) with V_ij = sum of e_n tanh(theta''_nj) over the strings n
+// flipping site i, recomputed in the tiles from the stored angles (storing these terms
+// per walker and string would move O(N^2 M) bytes per walker through HBM).
+// The sums run centred on the instance's mean energy E (the same value in every tile):
 //   gO = sum conj(O),  gE = sum (E_w - E) conj(O),  gK = sum conj(E_k) - conj(E) conj(O),
 //   gradient = (gE + gK) / W + (conj(E) - E) gO / W.
 #include <algorithm>
@@ -50,8 +51,8 @@ struct SInst {
     uint64_t seed;
     double2* eloc;        // [walkers]
     float2* T;            // [walkers][Mpad] tanh(theta)
-    float2* theta;        // [walkers][Mpad] the angles of the final configuration
     float2* U;            // [walkers][Mpad] sum over every string of e_n tanh(theta''_n)
+    float2* theta;        // [walkers][Mpad] the angles of the final configuration
     float2* en;           // [walkers][num_offdiag] e_n of the off-diagonal strings
     const int* site_ptr;  // [N + 1] off-diagonal slots flipping each site (CSR)
     const int* site_slots;
@@ -69,6 +70,8 @@ struct STask {
     int inst;
     int index;   // walker within the instance, or first row of the tile
     int w0;      // reduction tile: first walker of its walker chunk
+    int general; // reduction tile: 1 if a row's site is not flipped by exactly one string
+                 // that flips that site alone
 };
 
 constexpr int kReduceWalkers = 256;   // walkers per reduction tile
@@ -215,27 +218,29 @@ __device__ __noinline__ void walker_task(const SLaunch& L, const SInst& Ig, int 
             for (int p = 0; p < I.N; p++) acc += s_mh_step2<K>(I, s, tp, tq, rp, rng, lane, nmagic);
         }
     }
-    // measurement: local energy and tanh(theta) of the final configuration; f(theta) in
-    // this warp's shared-memory slice [kSK][32] keeps the register footprint of the sweeps;
-    // f(theta) and f(theta'') both with the approximate reciprocal (the local-energy
-    // differences, as rbm_eloc_t_kernel takes them)
+    // measurement at the final configuration: the local energy, tanh(theta), and for the
+    // E_k term the angles, U_j = sum_n e_n tanh(theta''_nj) and the e_n.  Three
+    // shared-memory slices [kSK][32] of this warp hold f(theta), the current string's
+    // tanh(theta'') and U, keeping the register footprint of the sweeps; f and tanh of an
+    // angle come from one evaluation with the approximate reciprocal (lc_tanh_approx; the
+    // local-energy differences, as rbm_eloc_t_kernel takes them)
     float tr[K], ti[K];
     s_refresh(I, s, tr, ti, lane);
     extern __shared__ float2 s_f[];
-    float2* myf = s_f + (threadIdx.x >> 5) * kSK * 32 + lane;
+    float2* myf = s_f + (threadIdx.x >> 5) * 3 * kSK * 32 + lane;
+    float2* myt = myf + kSK * 32;
+    float2* myu = myt + kSK * 32;
     const long row_w = static_cast<long>(w) * I.Mpad + lane;
 #pragma unroll
     for (int k = 0; k < K; k++) {
-        myf[32 * k] = lc_c_approx(tr[k], ti[k]);
-        I.T[row_w + 32 * k] = tanh_c(tr[k], ti[k]);
+        float2 f, t;
+        lc_tanh_approx(tr[k], ti[k], f, t);
+        myf[32 * k] = f;
+        I.T[row_w + 32 * k] = t;
         I.theta[row_w + 32 * k] = make_float2(tr[k], ti[k]);
+        myu[32 * k] = make_float2(0.0f, 0.0f);
     }
-    // E_k: U_j = sum_n e_n tanh(theta''_nj); the diagonal strings' part is their summed
-    // coefficient times tanh(theta_j)
-    float2 U[K];
-#pragma unroll
-    for (int k = 0; k < K; k++) U[k] = make_float2(0.0f, 0.0f);
-    float2 dsum = make_float2(0.0f, 0.0f);
+    float2 dsum = make_float2(0.0f, 0.0f);   // the diagonal strings' summed coefficient
     KahanC e;
     for (int n = 0; n < I.op.S; n++) {
         const float2 cf = string_factor(I.op, n, s);
@@ -257,53 +262,52 @@ __device__ __noinline__ void walker_task(const SLaunch& L, const SInst& Ig, int 
             for (int k = 0; k < K; k++) wv[k] = __ldg(row + 32 * k);
 #pragma unroll
             for (int k = 0; k < K; k++) {
-                const float2 g = lc_c_approx(fmaf(two_s, wv[k].x, tr[k]), fmaf(two_s, wv[k].y, ti[k]));
+                float2 g, h;
+                lc_tanh_approx(fmaf(two_s, wv[k].x, tr[k]), fmaf(two_s, wv[k].y, ti[k]), g, h);
                 const float2 f0 = myf[32 * k];
                 part.x += g.x - f0.x;
                 part.y += g.y - f0.y;
+                myt[32 * k] = h;
             }
         } else {
 #pragma unroll
             for (int k = 0; k < K; k++) {
-                    float nr = tr[k], ni = ti[k];
-                    for (int q = 0; q < nf; q++) {
-                        const int site = I.op.flip_sites[off + q];
-                        const float two_s = s.up(site) ? -2.0f : 2.0f;
-                        const float2 wv = __ldg(I.W + static_cast<long>(site) * I.Mpad + lane + 32 * k);
-                        nr = fmaf(two_s, wv.x, nr);
-                        ni = fmaf(two_s, wv.y, ni);
-                    }
-                    const float2 g = lc_c_approx(nr, ni);
-                    const float2 f0 = myf[32 * k];
-                    part.x += g.x - f0.x;
-                    part.y += g.y - f0.y;
+                float nr = tr[k], ni = ti[k];
+                for (int q = 0; q < nf; q++) {
+                    const int site = I.op.flip_sites[off + q];
+                    const float two_s = s.up(site) ? -2.0f : 2.0f;
+                    const float2 wv = __ldg(I.W + static_cast<long>(site) * I.Mpad + lane + 32 * k);
+                    nr = fmaf(two_s, wv.x, nr);
+                    ni = fmaf(two_s, wv.y, ni);
                 }
+                float2 g, h;
+                lc_tanh_approx(nr, ni, g, h);
+                const float2 f0 = myf[32 * k];
+                part.x += g.x - f0.x;
+                part.y += g.y - f0.y;
+                myt[32 * k] = h;
+            }
         }
         const float2 t = string_term(cf, warp_sum_xor2(part));
         e.add(t.x, t.y);
-        // the string's theta'' again (the same operations), its tanh into U
+        if (lane == 0) I.en[static_cast<long>(w) * I.op.num_offdiag + I.op.offdiag_slot[n]] = t;
 #pragma unroll
         for (int k = 0; k < K; k++) {
-            float nr = tr[k], ni = ti[k];
-            for (int q = 0; q < nf; q++) {
-                const int site = I.op.flip_sites[off + q];
-                const float two_s = s.up(site) ? -2.0f : 2.0f;
-                const float2 wv = __ldg(I.W + static_cast<long>(site) * I.Mpad + lane + 32 * k);
-                nr = fmaf(two_s, wv.x, nr);
-                ni = fmaf(two_s, wv.y, ni);
-            }
-            const float2 h = tanh_c(nr, ni);
-            U[k].x += t.x * h.x - t.y * h.y;
-            U[k].y += t.x * h.y + t.y * h.x;
+            const float2 h = myt[32 * k];
+            const float2 x = make_float2(t.x * h.x - t.y * h.y, t.x * h.y + t.y * h.x);
+            float2 u = myu[32 * k];
+            u.x += x.x;
+            u.y += x.y;
+            myu[32 * k] = u;
         }
-        if (lane == 0) I.en[static_cast<long>(w) * I.op.num_offdiag + I.op.offdiag_slot[n]] = t;
     }
 #pragma unroll
     for (int k = 0; k < K; k++) {
-        const float2 h = tanh_c(tr[k], ti[k]);
-        U[k].x += dsum.x * h.x - dsum.y * h.y;
-        U[k].y += dsum.x * h.y + dsum.y * h.x;
-        I.U[row_w + 32 * k] = U[k];
+        const float2 h = I.T[row_w + 32 * k];
+        float2 u = myu[32 * k];
+        u.x += dsum.x * h.x - dsum.y * h.y;
+        u.y += dsum.x * h.y + dsum.y * h.x;
+        I.U[row_w + 32 * k] = u;
     }
     if (lane == 0) {
 #pragma unroll
@@ -321,8 +325,9 @@ __device__ __noinline__ void walker_task(const SLaunch& L, const SInst& Ig, int 
 // rows [r0, r0 + R) of the instance's sums (row N: the biases), every column, over the
 // walkers of chunk [w0, w0 + kReduceWalkers): the chunk's partial sums of gO, gE and gK
 // (every partial is written by exactly one tile; serve_finish_kernel adds the chunks)
-template <int R>
-__device__ __noinline__ void reduce_task(const SLaunch& L, const SInst& I, int r0, int w0, int lane) {
+template <int R, bool GENERAL>
+__device__ __noinline__ void reduce_task(const SLaunch& L, const SInst& Ig, int r0, int w0, int lane) {
+    const SInst I = Ig;   // the descriptor in registers: loop-invariant, not re-read per walker
     // wait for the instance's walkers (bounded by L.wait_ns of wall clock; a wait that gives
     // up raises the error flag, and every other waiter leaves as soon as it sees the flag)
     if (lane == 0) {
@@ -360,6 +365,26 @@ __device__ __noinline__ void reduce_task(const SLaunch& L, const SInst& I, int r
     const long plane = static_cast<long>(I.N + 1) * I.Mpad;
     float2* part = I.part + static_cast<long>(chunk) * 3 * plane;
     const int w1 = min(I.walkers, w0 + kReduceWalkers);
+    // per row, fetched once: the off-diagonal slots flipping its site; in the common case
+    // of one slot whose string flips that one site, the slot and the site
+    int sb[R], se[R], fslot[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        const int i = r0 + r;
+        sb[r] = i < I.N ? I.site_ptr[i] : 0;
+        se[r] = i < I.N ? I.site_ptr[i + 1] : 0;
+        fslot[r] = -1;
+        if (se[r] - sb[r] == 1) {
+            const int slot = I.site_slots[sb[r]];
+            const int n = I.op.offdiag[slot];
+            if (I.op.nflip[n] == 1) fslot[r] = slot;
+        }
+    }
+    // the e_n of a block of 32 walkers, [R][32], in this warp's shared-memory slice
+    extern __shared__ float2 s_f[];
+    float2* sen = s_f + (threadIdx.x >> 5) * 3 * kSK * 32;
+    const long estride = I.op.num_offdiag;
+    const uint64_t* spins = reinterpret_cast<const uint64_t*>(I.spins);
     for (int kc = 0; kc < I.K; kc++) {
         float2 aO[R], aE[R], aK[R];
 #pragma unroll
@@ -369,65 +394,110 @@ __device__ __noinline__ void reduce_task(const SLaunch& L, const SInst& I, int r
             aK[r] = make_float2(0.0f, 0.0f);
         }
         const int j = lane + 32 * kc;
-        for (int w = w0; w < w1; w++) {
-            // L2 loads (__ldcg): the walkers' results were written by other SMs
-            const long o = static_cast<long>(w) * I.Mpad + j;
-            const float2 t = __ldcg(I.T + o);
-            const float2 th = __ldcg(I.theta + o);
-            const float2 u = __ldcg(I.U + o);
-            const double2 ed = __ldcg(I.eloc + w);
-            const float dx = static_cast<float>(ed.x - mx), dy = static_cast<float>(ed.y - my);
-            // conj(t), (E - <E>) conj(t), and U - <E> t (E_k of the biases, centred)
-            const float cx = t.x, cy = -t.y;
-            const float ex = dx * cx - dy * cy, ey = dx * cy + dy * cx;
-            const float kx = u.x - (Er * t.x - Ei * t.y), ky = u.y - (Er * t.y + Ei * t.x);
-            uint64_t sw[kSW];
+        float2 wr[R];   // W[i][j] of each row's site (the single-flip case)
 #pragma unroll
-            for (int q = 0; q < kSW; q++)
-                sw[q] = q < I.nw ? __ldcg(reinterpret_cast<const unsigned long long*>(I.spins) +
-                                          static_cast<long>(w) * I.nw + q)
-                                 : 0ull;
-            auto up = [&](int site) {
-                uint64_t wd = sw[0];
+        for (int r = 0; r < R; r++)
+            wr[r] = (r0 + r < I.N) ? __ldg(I.W + static_cast<long>(r0 + r) * I.Mpad + j) : make_float2(0.0f, 0.0f);
+        for (int wb = w0; wb < w1; wb += 32) {
+            // a block of 32 walkers: lane b fetches walker wb + b's centred energy, the spins
+            // of the tile's rows (bit r: row r0 + r up) and the e_n of the rows' single-flip
+            // strings, all at once; the walker loop below takes them by shuffles.  L2 loads
+            // (__ldcg): the walkers' results were written by other SMs
+            const int nb = min(32, w1 - wb);
+            float sdx = 0.0f, sdy = 0.0f;
+            unsigned int sbits = 0u;
+            __syncwarp();   // the previous block's reads of the slice are done
+            if (lane < nb) {
+                const int ws = wb + lane;
+                const double2 ed = __ldcg(I.eloc + ws);
+                sdx = static_cast<float>(ed.x - mx);
+                sdy = static_cast<float>(ed.y - my);
+                // rows r0 .. r0 + R - 1 (R <= 64) lie in at most two spin words
+                const int q0 = min(r0, I.N - 1) >> 6, q1 = min(r0 + R - 1, I.N - 1) >> 6;
+                const uint64_t lo = __ldcg(spins + static_cast<long>(ws) * I.nw + q0);
+                const uint64_t hi = q1 != q0 ? __ldcg(spins + static_cast<long>(ws) * I.nw + q1) : lo;
 #pragma unroll
-                for (int q = 1; q < kSW; q++)
-                    if ((site >> 6) == q) wd = sw[q];
-                return ((wd >> (site & 63)) & 1ull) != 0ull;
-            };
-#pragma unroll
-            for (int r = 0; r < R; r++) {
-                const int i = r0 + r;
-                if (i > I.N) continue;
-                float sg = 1.0f;
-                float vx = 0.0f, vy = 0.0f;
-                if (i < I.N) {
-                    sg = up(i) ? 1.0f : -1.0f;
-                    // V_ij: the strings flipping site i, e_n tanh(theta''_nj)
-                    for (int q = I.site_ptr[i]; q < I.site_ptr[i + 1]; q++) {
-                        const int slot = I.site_slots[q];
-                        const int n = I.op.offdiag[slot];
-                        const int nf = I.op.nflip[n], fo = I.op.flip_off[n];
-                        float nr = th.x, ni = th.y;
-                        for (int f = 0; f < nf; f++) {
-                            const int site = I.op.flip_sites[fo + f];
-                            const float two_s = up(site) ? -2.0f : 2.0f;
-                            const float2 wv = __ldg(I.W + static_cast<long>(site) * I.Mpad + j);
-                            nr = fmaf(two_s, wv.x, nr);
-                            ni = fmaf(two_s, wv.y, ni);
-                        }
-                        const float2 h = tanh_c(nr, ni);
-                        const float2 en = __ldcg(I.en + static_cast<long>(w) * I.op.num_offdiag + slot);
-                        vx += en.x * h.x - en.y * h.y;
-                        vy += en.x * h.y + en.y * h.x;
+                for (int r = 0; r < R; r++) {
+                    const int i = r0 + r;
+                    if (i < I.N) {
+                        const uint64_t wd = (i >> 6) == q0 ? lo : hi;
+                        sbits |= static_cast<unsigned int>((wd >> (i & 63)) & 1ull) << r;
+                        if (fslot[r] >= 0) sen[r * 32 + lane] = __ldcg(I.en + ws * estride + fslot[r]);
                     }
                 }
-                aO[r].x += sg * cx;
-                aO[r].y += sg * cy;
-                aE[r].x += sg * ex;
-                aE[r].y += sg * ey;
-                // conj(s_i (U - 2 V) - <E> O) = sg conj(U - <E> t - 2 V)
-                aK[r].x += sg * (kx - 2.0f * vx);
-                aK[r].y -= sg * (ky - 2.0f * vy);
+            }
+            __syncwarp();
+            for (int bw = 0; bw < nb; bw++) {
+                const int w = wb + bw;
+                const long o = static_cast<long>(w) * I.Mpad + j;
+                const float2 t = __ldcg(I.T + o);
+                const float2 u = __ldcg(I.U + o);
+                const float2 th = __ldcg(I.theta + o);
+                const float dx = __shfl_sync(0xffffffffu, sdx, bw);
+                const float dy = __shfl_sync(0xffffffffu, sdy, bw);
+                const unsigned int bits = __shfl_sync(0xffffffffu, sbits, bw);
+                // conj(t), (E - <E>) conj(t), and U - <E> t (E_k of the biases, centred)
+                const float cx = t.x, cy = -t.y;
+                const float ex = dx * cx - dy * cy, ey = dx * cy + dy * cx;
+                const float kx = u.x - (Er * t.x - Ei * t.y), ky = u.y - (Er * t.y + Ei * t.x);
+                uint64_t sw[kSW];
+#pragma unroll
+                for (int q = 0; q < kSW; q++)
+                    sw[q] = GENERAL && q < I.nw ? __ldcg(spins + static_cast<long>(w) * I.nw + q) : 0ull;
+                auto up = [&](int site) {
+                    uint64_t wd = sw[0];
+#pragma unroll
+                    for (int q = 1; q < kSW; q++)
+                        if ((site >> 6) == q) wd = sw[q];
+                    return ((wd >> (site & 63)) & 1ull) != 0ull;
+                };
+#pragma unroll
+                for (int r = 0; r < R; r++) {
+                    const int i = r0 + r;
+                    if (i > I.N) continue;
+                    float sg = 1.0f;
+                    float vx = 0.0f, vy = 0.0f;
+                    if (i < I.N) {
+                        sg = (bits >> r) & 1u ? 1.0f : -1.0f;
+                        // V_ij = sum over the strings n flipping site i of e_n tanh(theta''_nj),
+                        // the angles theta'' formed as the walker task formed them
+                        if (fslot[r] >= 0) {
+                            const float two_s = sg > 0.0f ? -2.0f : 2.0f;
+                            float2 g, h;
+                            lc_tanh_approx(fmaf(two_s, wr[r].x, th.x), fmaf(two_s, wr[r].y, th.y), g, h);
+                            const float2 en = sen[r * 32 + bw];
+                            vx = en.x * h.x - en.y * h.y;
+                            vy = en.x * h.y + en.y * h.x;
+                        } else if (GENERAL) {
+                            const float2* enw = I.en + w * estride;
+                            for (int q = sb[r]; q < se[r]; q++) {
+                                const int slot = I.site_slots[q];
+                                const int n = I.op.offdiag[slot];
+                                const int nf = I.op.nflip[n], fo = I.op.flip_off[n];
+                                float nr = th.x, ni = th.y;
+                                for (int f = 0; f < nf; f++) {
+                                    const int site = I.op.flip_sites[fo + f];
+                                    const float ts = up(site) ? -2.0f : 2.0f;
+                                    const float2 wv = __ldg(I.W + static_cast<long>(site) * I.Mpad + j);
+                                    nr = fmaf(ts, wv.x, nr);
+                                    ni = fmaf(ts, wv.y, ni);
+                                }
+                                float2 g, h;
+                                lc_tanh_approx(nr, ni, g, h);
+                                const float2 en = __ldcg(enw + slot);
+                                vx += en.x * h.x - en.y * h.y;
+                                vy += en.x * h.y + en.y * h.x;
+                            }
+                        }
+                    }
+                    aO[r].x += sg * cx;
+                    aO[r].y += sg * cy;
+                    aE[r].x += sg * ex;
+                    aE[r].y += sg * ey;
+                    // conj(s_i (U - 2 V) - <E> O) = sg conj(U - <E> t - 2 V)
+                    aK[r].x += sg * (kx - 2.0f * vx);
+                    aK[r].y -= sg * (ky - 2.0f * vy);
+                }
             }
         }
 #pragma unroll
@@ -481,7 +551,10 @@ __global__ void __maxnreg__(REGS) serve_kernel(SLaunch L) {
                 default: walker_task<18>(L, I, task.index, lane); break;
             }
         } else {
-            reduce_task<R>(L, I, task.index, task.w0, lane);
+            // rows whose sites are all flipped by one single-flip string each take the
+            // specialised tile (task.general: some row is not)
+            if (task.general) reduce_task<R, true>(L, I, task.index, task.w0, lane);
+            else reduce_task<R, false>(L, I, task.index, task.w0, lane);
         }
     }
 }
@@ -496,6 +569,7 @@ struct rbmg_batch {
     std::vector<const rbmg_psi*> psis;
     std::vector<const rbmg_operator*> ops;
     std::vector<SInst> host_inst;
+    std::vector<std::vector<char>> single_flip;   // [instance][site]: the single-flip tile serves the site
     std::vector<uint32_t> walkers;
     DevBuf d_inst, d_tasks, d_next, d_done, d_error, d_accepts;
     int max_elems = 0;          // largest instance's 3 (N + 1) Mpad (the finish kernel's grid)
@@ -533,18 +607,24 @@ int batch_tasks(rbmg_batch* b) {
     });
     std::vector<STask> tasks;
     for (int i : order)
-        for (int w = 0; w < b->host_inst[i].walkers; w++) tasks.push_back(STask{0, i, w, 0});
+        for (int w = 0; w < b->host_inst[i].walkers; w++) tasks.push_back(STask{0, i, w, 0, 0});
     b->ntasks_walk = static_cast<int>(tasks.size());
-    for (int i : order)
-        for (int r0 = 0; r0 <= b->host_inst[i].N; r0 += b->rows)
-            for (int w0 = 0; w0 < b->host_inst[i].walkers; w0 += kReduceWalkers) tasks.push_back(STask{1, i, r0, w0});
+    for (int i : order) {
+        const int N = b->host_inst[i].N;
+        for (int r0 = 0; r0 <= N; r0 += b->rows) {
+            int general = 0;
+            for (int r = r0; r < std::min(N, r0 + b->rows); r++) general |= !b->single_flip[i][r];
+            for (int w0 = 0; w0 < b->host_inst[i].walkers; w0 += kReduceWalkers)
+                tasks.push_back(STask{1, i, r0, w0, general});
+        }
+    }
     b->ntasks = static_cast<int>(tasks.size());
     RBMG_CK(b->d_tasks.ensure(sizeof(STask) * tasks.size()));
     RBMG_CK(cudaMemcpy(b->d_tasks.p, tasks.data(), sizeof(STask) * tasks.size(), cudaMemcpyHostToDevice));
     return RBMG_OK;
 }
 
-size_t serve_smem(int warps_per_block) { return sizeof(float2) * kSK * 32 * warps_per_block; }
+size_t serve_smem(int warps_per_block) { return sizeof(float2) * 3 * kSK * 32 * warps_per_block; }
 
 // calls f with the kernel instantiation of (reduction rows, register cap)
 template <class F>
@@ -558,6 +638,16 @@ void with_serve_kernel(int rows, int regs, F f) {
         else if (regs == 96) f(serve_kernel<16, 96>);
         else f(serve_kernel<16, 255>);
     }
+}
+
+// the kernel instantiation's dynamic shared-memory limit (above the 48 KB default for 4 and
+// 8 warps per block); the attribute belongs to the current device's context
+cudaError_t serve_smem_attr(int rows, int regs, size_t sm) {
+    cudaError_t e = cudaSuccess;
+    with_serve_kernel(rows, regs, [&](auto kern) {
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
+    });
+    return e;
 }
 
 cudaError_t launch_serve(rbmg_batch* b, cudaStream_t st) {
@@ -575,6 +665,8 @@ cudaError_t launch_serve(rbmg_batch* b, cudaStream_t st) {
     L.wait_extra = b->wait_extra;
     const int threads = 32 * b->warps_per_block;
     const size_t sm = serve_smem(b->warps_per_block);
+    const cudaError_t e = serve_smem_attr(b->rows, b->regs, sm);
+    if (e != cudaSuccess) return e;
     with_serve_kernel(b->rows, b->regs, [&](auto kern) { kern<<<b->blocks, threads, sm, st>>>(L); });
     return cudaGetLastError();
 }
@@ -594,6 +686,7 @@ int batch_capture(rbmg_batch* b) {
     RBMG_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const int threads = 32 * b->warps_per_block;
     const size_t sm = serve_smem(b->warps_per_block);
+    RBMG_CK(serve_smem_attr(b->rows, b->regs, sm));
     cudaError_t oe = cudaSuccess;
     with_serve_kernel(b->rows, b->regs,
                       [&](auto kern) { oe = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, sm); });
@@ -682,8 +775,6 @@ extern "C" int rbmg_batch_create(int n, const rbmg_psi* const* psis, const rbmg_
         I.Wq = d.Wq;
         I.bq = d.bq;
         I.op = o->dev();
-        I.site_ptr = o->d_site_ptr.as<int>();
-        I.site_slots = o->d_site_slots.as<int>();
         I.walkers = static_cast<int>(walkers[i]);
         I.seed = seeds[i];
         auto alloc = [&](size_t bytes) -> void* {
@@ -694,8 +785,8 @@ extern "C" int rbmg_batch_create(int n, const rbmg_psi* const* psis, const rbmg_
         const size_t B = walkers[i];
         I.eloc = static_cast<double2*>(alloc(sizeof(double2) * B));
         I.T = static_cast<float2*>(alloc(sizeof(float2) * B * p->Mpad));
-        I.theta = static_cast<float2*>(alloc(sizeof(float2) * B * p->Mpad));
         I.U = static_cast<float2*>(alloc(sizeof(float2) * B * p->Mpad));
+        I.theta = static_cast<float2*>(alloc(sizeof(float2) * B * p->Mpad));
         I.en = static_cast<float2*>(alloc(sizeof(float2) * B * std::max(1, o->num_offdiag)));
         I.spins = static_cast<uint64_t*>(alloc(sizeof(uint64_t) * B * nw));
         I.rng_index = static_cast<uint64_t*>(alloc(sizeof(uint64_t) * B));
@@ -704,8 +795,31 @@ extern "C" int rbmg_batch_create(int n, const rbmg_psi* const* psis, const rbmg_
         I.part = static_cast<float2*>(alloc(sizeof(float2) * I.chunks * elems));
         I.g = static_cast<double2*>(alloc(sizeof(double2) * elems));
         I.emean = static_cast<double2*>(alloc(sizeof(double2)));
+        // the batch's own copy of the site lists (the operator's are rebuilt when it is used
+        // with another N), and per site whether the single-flip tile serves it: exactly one
+        // off-diagonal string flips the site and flips it alone (reduce_task's test)
+        int* site_ptr = static_cast<int*>(alloc(sizeof(int) * o->site_ptr.size()));
+        int* site_slots = static_cast<int*>(alloc(sizeof(int) * o->site_slots.size()));
+        if (!site_ptr || !site_slots) return fail(RBMG_ENOMEM, "batch: device allocation failed");
+        RBMG_CK(cudaMemcpy(site_ptr, o->site_ptr.data(), sizeof(int) * o->site_ptr.size(), cudaMemcpyHostToDevice));
+        RBMG_CK(cudaMemcpy(site_slots, o->site_slots.data(), sizeof(int) * o->site_slots.size(),
+                           cudaMemcpyHostToDevice));
+        I.site_ptr = site_ptr;
+        I.site_slots = site_slots;
+        {
+            std::vector<int> string_of(std::max(1, o->num_offdiag), 0);
+            for (int n = 0; n < o->S; n++)
+                if (o->offdiag_slot[n] >= 0) string_of[o->offdiag_slot[n]] = n;
+            std::vector<char> single(p->N);
+            for (int site = 0; site < p->N; site++) {
+                const int sb = o->site_ptr[site], se = o->site_ptr[site + 1];
+                single[site] = se - sb == 1 && o->nflip[string_of[o->site_slots[sb]]] == 1;
+            }
+            b->single_flip.push_back(std::move(single));
+        }
         b->max_elems = std::max(b->max_elems, static_cast<int>(elems));
-        if (!I.eloc || !I.T || !I.theta || !I.U || !I.en || !I.spins || !I.rng_index || !I.part || !I.g || !I.emean)
+        if (!I.eloc || !I.T || !I.U || !I.theta || !I.en || !I.spins || !I.rng_index || !I.part || !I.g ||
+            !I.emean)
             return fail(RBMG_ENOMEM, "batch: device allocation failed");
         RBMG_CK(cudaMemset(I.rng_index, 0, sizeof(uint64_t) * B));
         b->psis.push_back(p);
