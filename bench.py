@@ -273,7 +273,8 @@ class GpuChains:
         """The learned chain starts from the plain chain's configurations (its own Philox
         streams); its network is trained online from there, then frozen."""
         rg = self.rg
-        self.prop = rg.Proposal(self.psi.N, seed=self.seed_net, lr=1e-3)
+        objective = rg.Proposal.REINFORCE if args.objective == "reinforce" else rg.Proposal.LOCALLY_BALANCED
+        self.prop = rg.Proposal(self.psi.N, seed=self.seed_net, lr=1e-3, objective=objective)
         self.learned = rg.Chain(self.psi, self.B, seed=self.seed_learned)
         self.learned.set_learned_streams(args.learned_streams)
         zero = np.zeros(self.B, np.uint64)
@@ -889,6 +890,9 @@ def main():
                     help="streams of the frozen learned steps (0: automatic, 2 slices from 8192 walkers)")
     ap.add_argument("--train-steps", type=int, default=2000)
     ap.add_argument("--train-walkers", type=int, default=4096)
+    ap.add_argument("--objective", default="balanced", choices=["balanced", "reinforce"],
+                    help="training objective of the proposal: cross-entropy to the locally balanced proposal, or "
+                         "REINFORCE on the acceptance (the accept-rate objective)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=16.0, help="budget of the CPU baseline leg")
     ap.add_argument("--sm-n", type=int, default=SM_N, help="s_matrix workload: visible units")
@@ -1005,7 +1009,8 @@ def main():
                    "therm_sweeps": args.therm_sweeps,
                    "step": f"one row: learned {L} frozen MH steps + E_loc; plain {S} sweeps + E_loc",
                    "tau_series_rows": args.steps + args.tau_rows, "train_steps": args.train_steps,
-                   "train_walkers": args.train_walkers, "learned_streams": learned_slices(args, B),
+                   "train_walkers": args.train_walkers, "objective": args.objective,
+                   "learned_streams": learned_slices(args, B),
                    "l2": "flushed between timed rows"},
         "learned": le,
         "plain": pl,
