@@ -59,7 +59,7 @@ METRIC = "effective samples/s (ESS of E_loc) at N=100: learned-proposal MCMC (pl
 UNIT = "samples/s"
 L2_FLUSH_BYTES = 256 << 20
 # DRAM bytes of one sampler launch: dram__bytes_read.sum + dram__bytes_write.sum of an ncu
-# capture of rbm_mc_kernel<13,2> on these 16384 walkers
+# capture of rbm_mc_smem_kernel<13,2> on these 16384 walkers
 SAMPLER_DRAM_BYTES = 1.059e6
 # DRAM bytes of one learned_accept_kernel<13,2> launch of 16384 walkers (ncu, sigma 0.05, mean
 # of three launches: 100.3 MB read, 4.1 MB written -- accepted angles stay in L2 within a launch)
@@ -577,10 +577,15 @@ def run_serving(args):
             E, g, _ = batch.result(q)
             d2h += 16 * inst[q][2] + 2 * 8 * (inst[q][0].N + 1) * ((inst[q][0].M + 31) // 32 * 32)
     e2e_s = time.perf_counter() - t0
+    # algorithmic flops per walker: the sweep, E_loc, and the reference estimator's E_k term
+    # at its minimum -- tanh(theta'') of every off-diagonal string from the denominator its
+    # f(theta'') already formed (44 flops), U_j += e_n tanh (8), and per (row, unit) of the
+    # sums V = e_n tanh (6) and the three centred accumulations (16); the tiles' recomputation
+    # of tanh(theta'') (stored nowhere, to keep O(N^2 M) bytes per walker off HBM) is not counted
     flops = 0
     for psi, _, w, _ in inst:
         N, M = psi.N, psi.M
-        flops += w * (flops_per_sweep(N, M) + flops_per_eloc(N, M, N) + 8 * (N + 1) * M)
+        flops += w * (flops_per_sweep(N, M) + flops_per_eloc(N, M, N) + N * M * (44 + 8) + (N + 1) * M * (6 + 16))
     peak = max(ctypes_probe_fp32(), ctypes_probe_fp32(pairs=True))
     sec = float(ms.mean()) / 1e3
     w_shape, rows, blocks = batch.shape
@@ -861,6 +866,63 @@ def run_deep(args):
     print(json.dumps(line))
 
 
+def run_plain(args):
+    """One step = one 10-sweep launch of the plain single-flip sampler on the N=100, M=400
+    RBM (sigma --mix-sigma), all walkers, the L2 flushed before each launch: the sampler
+    kernel alone, for its roofline and for profiling (no other kernel of the library runs)."""
+    import torch
+    import rbmongpu_gb300 as rg
+    torch.cuda.set_device(0)
+    b, W = workload(args.mix_sigma)
+    N = N_SPINS
+    psi = rg.Psi(np.zeros(N), np.zeros(N), b, W, 1.0, False, True)
+    sp = rg.library_stream()
+    stream = torch.cuda.ExternalStream(sp)
+    B = args.walkers
+    ch = rg.Chain(psi, B, seed=1000)
+    ch.sweep_async(psi, None, 200, 1, 0, sp)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    sweeps = 10
+    for k in range(args.warmup):
+        ch.sweep_async(psi, None, sweeps, 1, 0, sp)
+    torch.cuda.synchronize()
+    K = args.steps
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    clocks = ClockSampler(0)
+    clocks.start()
+    with torch.cuda.stream(stream):
+        for k in range(K):
+            flush.fill_(k & 255)
+            starts[k].record(stream)
+            ch.sweep_async(psi, None, sweeps, 1, 0, sp)
+            ends[k].record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = np.array([a.elapsed_time(e) for a, e in zip(starts, ends)])
+    sec = float(ms.mean()) / 1e3
+    _, acc, props = ch.state()
+    flops = flops_per_sweep() * sweeps * B
+    peak = max(ctypes_probe_fp32(), ctypes_probe_fp32(pairs=True))
+    line = {
+        "metric": "plain single-flip sampler: walker-sweeps/s at N=100, M=400",
+        "value": B * sweeps / sec, "unit": "walker-sweeps/s", "n_gpus": 1, "steps": K, "warmup": args.warmup,
+        "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (complex64)", "data": "synthetic (seeded PCG64 parameters)",
+        "config": {"workload": "rbm_n100_m400_plain_sampler_sigma%g" % args.mix_sigma, "N": N, "M": M_HIDDEN,
+                   "walkers": B, "sweeps_per_step": sweeps, "l2": "flushed before each launch"},
+        "acceptance": float(acc) / float(props) if props else None,
+        "gpu_launches": K,
+        "roofline": {"bound": "fp32", "achieved": flops / sec / 1e12, "peak": peak, "unit": "TFLOP/s",
+                     "frac": flops / sec / 1e12 / peak, "traffic": SAMPLER_DRAM_BYTES,
+                     "peak_source": "measured in this run: the larger of the library's scalar and packed-pair FP32 "
+                                    "FMA probes",
+                     "kernel": "rbm_mc_smem_kernel<13,2>", "flops_per_launch": flops},
+        "clocks": clk,
+    }
+    print(json.dumps(line))
+
+
 def ctypes_probe_fp32(pairs=False):
     """FP32 FMA rate of this GPU from the library's probe kernel (scalar or packed pairs)."""
     import ctypes
@@ -901,10 +963,11 @@ def main():
     ap.add_argument("--ac-sigma", type=float, default=SIGMA, help="autocorrelation workload: weight scale")
     ap.add_argument("--ac-rows", type=int, default=20000, help="autocorrelation workload: rows of each chain")
     ap.add_argument("--workload", default="learned",
-                    choices=["learned", "serving", "s_matrix", "deep", "autocorrelation"],
+                    choices=["learned", "serving", "s_matrix", "deep", "autocorrelation", "plain"],
                     help="learned: the N=100 learned-vs-plain chains (headline); serving: 64 uneven RBMs; "
                          "s_matrix: get_S_matrix of the N=64, M=128 RBM over 16384 MC samples; "
-                         "deep: the PsiDeep 100-200-100-50 gradient through the adjoint kernels")
+                         "deep: the PsiDeep 100-200-100-50 gradient through the adjoint kernels; "
+                         "plain: 10-sweep launches of the plain sampler alone (its roofline, profiling)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -923,6 +986,10 @@ def main():
     if args.workload == "deep" and args.impl == "ours":
         if rank == 0:
             run_deep(args)
+        return
+    if args.workload == "plain" and args.impl == "ours":
+        if rank == 0:
+            run_plain(args)
         return
     if args.workload == "autocorrelation":
         if rank == 0 and args.impl == "ours":
@@ -1048,7 +1115,7 @@ def main():
                                    "traffic": SAMPLER_DRAM_BYTES,
                                    "peak_source": "measured in this run: the larger of the library's scalar and "
                                                   "packed-pair FP32 FMA probes",
-                                   "kernel": "rbm_mc_kernel<13,2> (plain sampler, 10 sweeps per launch, sigma 0.05)",
+                                   "kernel": "rbm_mc_smem_kernel<13,2> (plain sampler, 10 sweeps per launch, sigma 0.05)",
                                    "flops_per_launch": fl, "ms_per_launch": avg_launch * 1e3},
         "glass_sigma0.1": r.get("glass"),
         "cpu_baseline": cpu,

@@ -202,6 +202,7 @@ __device__ __forceinline__ bool rbm_mh_step2(const RbmDev& P, Spins<NW>& s, pair
         rows[q] = P.Wq + static_cast<long>(site) * KP * 32 + lane;
     }
     float part = 0.0f;
+    pair_t fnew[KP];   // Re f of the proposed angles
     if (ns == 1) {
         // single flip: the KP loads of the paired W row are issued together
         float4 w[KP];
@@ -211,8 +212,9 @@ __device__ __forceinline__ bool rbm_mh_step2(const RbmDev& P, Spins<NW>& s, pair
         for (int kk = 0; kk < KP; kk++) {
             const pair_t nr = fma2(two_s[0], pk2(w[kk].x, w[kk].y), tr[kk]);
             const pair_t ni = fma2(two_s[0], pk2(w[kk].z, w[kk].w), ti[kk]);
+            fnew[kk] = lc_re2(nr, ni);
             float d0, d1;
-            up2(sub2(lc_re2(nr, ni), re[kk]), d0, d1);
+            up2(sub2(fnew[kk], re[kk]), d0, d1);
             part = __fadd_rn(part, d0);
             if (2 * kk + 1 < K) part = __fadd_rn(part, d1);
         }
@@ -225,8 +227,9 @@ __device__ __forceinline__ bool rbm_mh_step2(const RbmDev& P, Spins<NW>& s, pair
                 nr = fma2(two_s[q], pk2(w.x, w.y), nr);
                 ni = fma2(two_s[q], pk2(w.z, w.w), ni);
             }
+            fnew[kk] = lc_re2(nr, ni);
             float d0, d1;
-            up2(sub2(lc_re2(nr, ni), re[kk]), d0, d1);
+            up2(sub2(fnew[kk], re[kk]), d0, d1);
             part = __fadd_rn(part, d0);
             if (2 * kk + 1 < K) part = __fadd_rn(part, d1);
         }
@@ -243,23 +246,35 @@ __device__ __forceinline__ bool rbm_mh_step2(const RbmDev& P, Spins<NW>& s, pair
                 tr[kk] = fma2(two_s[q], pk2(w.x, w.y), tr[kk]);
                 ti[kk] = fma2(two_s[q], pk2(w.z, w.w), ti[kk]);
             }
-            re[kk] = lc_re2(tr[kk], ti[kk]);
+            // lc_re2 of the new angles, formed by the same operations: kept from the proposal
+            // where the registers allow (the larger layers take rbm_mc_smem_kernel's buffers)
+            re[kk] = K <= 8 ? fnew[kk] : lc_re2(tr[kk], ti[kk]);
         }
     }
     return accept;
 }
 
 // The single-flip proposal of rbm_mh_step2 with the walker's angles and Re f in this
-// warp's shared-memory slice st [3][KP][32] pairs (theta re, theta im, Re f) instead of
-// registers: the same operations in the same order, so the same chain bit for bit.  It
-// frees ~3 KP registers per lane, which for the large hidden layers lets more warps stay
-// resident to hide the dependent chain of each proposal.
-template <int K, int KP, int NW>
-__device__ __forceinline__ bool rbm_flip_step_s(const RbmDev& P, Spins<NW>& s, pair_t* st, WarpRng& rng, int lane,
-                                                uint64_t nmagic) {
+// warp's shared-memory slice st [4][KP][32] pairs (theta re, theta im, Re f in two buffers)
+// instead of registers: the same operations in the same order, so the same chain bit for
+// bit.  It frees ~3 KP registers per lane, which for the large hidden layers lets more warps
+// stay resident to hide the dependent chain of each proposal.  Buffer cur holds the walker's
+// Re f.  KEEP: the proposal writes its Re f(theta') into the other buffer, and an accepted
+// move takes that buffer as is (the values that recomputing from the new angles gives, bit
+// for bit) and only advances the angles; otherwise an accepted move recomputes Re f in
+// place.  Keeping costs KP stores per proposal and a quarter more shared memory (less L1 for
+// the W rows), and saves KP activations per acceptance: measured on N = 100, M = 416 and
+// 16384 walkers, 10 sweeps take 12.60 ms kept against 13.26 ms recomputed at an acceptance
+// of 0.235 (sigma 0.05 weights), but 12.44 against 11.79 ms at 0.026 (sigma 0.1).  The
+// sampler keeps; a per-warp switch on the running acceptance measured worse in both cases.
+template <int K, int KP, bool KEEP, int NW>
+__device__ __forceinline__ bool rbm_flip_step_s(const RbmDev& P, Spins<NW>& s, pair_t* st, int& cur, WarpRng& rng,
+                                                int lane, uint64_t nmagic) {
     const int site = static_cast<int>(fastmod(rng.next(), nmagic, static_cast<uint32_t>(P.N)));
     const pair_t two_s = splat2(s.up(site) ? -2.0f : 2.0f);   // 2 x the new spin
     const float4* row = P.Wq + static_cast<long>(site) * KP * 32 + lane;
+    pair_t* re = st + (2 + cur) * KP * 32 + lane;
+    pair_t* re_new = st + (3 - cur) * KP * 32 + lane;
     float4 w[KP];
 #pragma unroll
     for (int kk = 0; kk < KP; kk++) w[kk] = __ldg(row + 32 * kk);
@@ -268,8 +283,10 @@ __device__ __forceinline__ bool rbm_flip_step_s(const RbmDev& P, Spins<NW>& s, p
     for (int kk = 0; kk < KP; kk++) {
         const pair_t nr = fma2(two_s, pk2(w[kk].x, w[kk].y), st[kk * 32 + lane]);
         const pair_t ni = fma2(two_s, pk2(w[kk].z, w[kk].w), st[(KP + kk) * 32 + lane]);
+        const pair_t f = lc_re2(nr, ni);
+        if (KEEP) re_new[kk * 32] = f;
         float d0, d1;
-        up2(sub2(lc_re2(nr, ni), st[(2 * KP + kk) * 32 + lane]), d0, d1);
+        up2(sub2(f, re[kk * 32]), d0, d1);
         part = __fadd_rn(part, d0);
         if (2 * kk + 1 < K) part = __fadd_rn(part, d1);
     }
@@ -278,6 +295,7 @@ __device__ __forceinline__ bool rbm_flip_step_s(const RbmDev& P, Spins<NW>& s, p
     if (!accept) accept = rng.uniform() <= expf_det(__fmul_rn(2.0f, delta));
     if (accept) {
         s.flip(site);
+        if (KEEP) cur ^= 1;
 #pragma unroll
         for (int kk = 0; kk < KP; kk++) {
             const float4 ww = __ldg(row + 32 * kk);
@@ -285,7 +303,7 @@ __device__ __forceinline__ bool rbm_flip_step_s(const RbmDev& P, Spins<NW>& s, p
             const pair_t ti = fma2(two_s, pk2(ww.z, ww.w), st[(KP + kk) * 32 + lane]);
             st[kk * 32 + lane] = tr;
             st[(KP + kk) * 32 + lane] = ti;
-            st[(2 * KP + kk) * 32 + lane] = lc_re2(tr, ti);
+            if (!KEEP) re[kk * 32] = lc_re2(tr, ti);
         }
     }
     return accept;
@@ -545,7 +563,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, 6) rbm_mc_smem_kernel(Rbm
     if (w >= L.B) return;
     constexpr int KP = (K + 1) / 2;
     extern __shared__ pair_t s_state[];
-    pair_t* st = s_state + (threadIdx.x >> 5) * 3 * KP * 32;
+    pair_t* st = s_state + (threadIdx.x >> 5) * 4 * KP * 32;
+    int cur = 0;
     WarpRng rng;
     rng.init(L.seed, L.walker_base + static_cast<uint32_t>(w), L.rng_index[w], lane);
     const uint64_t nmagic = fastmod_magic(static_cast<uint32_t>(P.N));
@@ -565,6 +584,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, 6) rbm_mc_smem_kernel(Rbm
         {
             pair_t tr[KP], ti[KP];
             rbm_refresh2(P, s, tr, ti, lane);
+            cur = 0;
 #pragma unroll
             for (int kk = 0; kk < KP; kk++) {
                 st[kk * 32 + lane] = tr[kk];
@@ -572,7 +592,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, 6) rbm_mc_smem_kernel(Rbm
                 st[(2 * KP + kk) * 32 + lane] = lc_re2(tr[kk], ti[kk]);
             }
         }
-        for (int p = 0; p < P.N; p++) acc += rbm_flip_step_s<K, KP>(P, s, st, rng, lane, nmagic);
+        for (int p = 0; p < P.N; p++) acc += rbm_flip_step_s<K, KP, true>(P, s, st, cur, rng, lane, nmagic);
         props += P.N;
         const int done = sw + 1 - L.n_therm;
         if (done > 0 && done % L.sweeps_per_sample == 0) {
@@ -863,7 +883,7 @@ cudaError_t rbm_mc_launch_k(const RbmDev& P, const OpDev* op, const McLaunch& L,
     }
     if (K >= 13 && !L.total_z) {
         constexpr int KP = (K + 1) / 2;
-        const size_t sm = sizeof(pair_t) * 3 * KP * 32 * kWarpsPerBlock;
+        const size_t sm = sizeof(pair_t) * 4 * KP * 32 * kWarpsPerBlock;
         switch (nw) {
             case 1: rbm_mc_smem_kernel<K, 1><<<grid, block, sm, st>>>(P, L); break;
             case 2: rbm_mc_smem_kernel<K, 2><<<grid, block, sm, st>>>(P, L); break;

@@ -152,12 +152,14 @@ __device__ __forceinline__ bool s_mh_step2(const SInst& I, Spins<NW>& s, pair_t 
 #pragma unroll
     for (int kk = 0; kk < KP; kk++) w[kk] = __ldg(row + 32 * kk);
     float part = 0.0f;
+    pair_t fnew[KP];   // Re f of the proposed angles
 #pragma unroll
     for (int kk = 0; kk < KP; kk++) {
         const pair_t nr = fma2(two_s, pk2(w[kk].x, w[kk].y), tr[kk]);
         const pair_t ni = fma2(two_s, pk2(w[kk].z, w[kk].w), ti[kk]);
+        fnew[kk] = lc_re2(nr, ni);
         float d0, d1;
-        up2(sub2(lc_re2(nr, ni), re[kk]), d0, d1);
+        up2(sub2(fnew[kk], re[kk]), d0, d1);
         part = __fadd_rn(part, d0);
         if (2 * kk + 1 < K) part = __fadd_rn(part, d1);
     }
@@ -171,7 +173,8 @@ __device__ __forceinline__ bool s_mh_step2(const SInst& I, Spins<NW>& s, pair_t 
             const float4 ww = __ldg(row + 32 * kk);
             tr[kk] = fma2(two_s, pk2(ww.x, ww.y), tr[kk]);
             ti[kk] = fma2(two_s, pk2(ww.z, ww.w), ti[kk]);
-            re[kk] = lc_re2(tr[kk], ti[kk]);
+            // lc_re2 of the new angles: kept from the proposal where the registers allow
+            re[kk] = K <= 8 ? fnew[kk] : lc_re2(tr[kk], ti[kk]);
         }
     }
     return accept;
