@@ -79,6 +79,50 @@ def test_served_gradient_is_the_reference_estimator_on_the_same_configurations()
         np.testing.assert_array_equal(g1, g2)
 
 
+def mixed_chain(N, h):
+    """TFIM chain plus an X X bond on sites 2, 3 and a Y field on site 5: sites flipped by
+    one single-site string (the single-flip tiles) beside sites flipped by several strings
+    or by a two-site string (the general tiles)."""
+    import rbmongpu_gb300 as rg
+    X, Y, Z = rg.operators.X, rg.operators.Y, rg.operators.Z
+    strings = [[(Z, i), (Z, (i + 1) % N)] for i in range(N)] + [[(X, i)] for i in range(N)]
+    strings += [[(X, 2), (X, 3)], [(Y, 5)]]
+    return rg.operators.table(strings, [-1.0] * N + [-h] * N + [0.3, 0.2])
+
+
+def test_served_gradient_with_multi_flip_strings():
+    """Operators whose strings flip several sites, or several strings per site (Heisenberg
+    chain; TFIM with an extra bond and a Y field): the general reduction tiles, alone and
+    beside single-flip tiles of the same instance, give the reference estimator on the same
+    configurations, and the same bits for both tile heights."""
+    import rbmongpu_gb300 as rg
+    specs = [(16, 2, "heis", 64), (24, 1, "mixed", 96), (40, 2, "mixed", 130), (20, 4, "tfim", 48)]
+    results = []
+    for rows in (16, 8):
+        inst = []
+        for q, (N, a, kind, B) in enumerate(specs):
+            if kind == "heis":
+                op = rg.operators.heisenberg_chain(N, 1.0)
+            elif kind == "mixed":
+                op = mixed_chain(N, 0.9 + 0.1 * q)
+            else:
+                op = rg.operators.tfim_chain(N, 1.0, 1.2)
+            inst.append((rbm(N, a, 105_400 + q), rg.Operator(*op), B, 700 + q))
+        batch = rg.Batch(inst)
+        batch.set_shape(4, rows)
+        batch.run(15, 2)
+        results.append([batch.result(q) for q in range(len(inst))])
+        if rows == 16:
+            for q, (psi, op, B, _) in enumerate(inst):
+                E, g, _ = results[-1][q]
+                g_ref, E_ref = rg.ExpectationValue().gradient(psi, op, rg.FixedSamples(psi.N, batch.spins(q)))
+                assert abs(E - E_ref) <= 1e-6 * abs(E_ref), (q, E, E_ref)
+                assert np.abs(g - g_ref).max() <= 1e-5 * np.abs(g_ref).max(), (q, np.abs(g - g_ref).max())
+    for (E1, g1, _), (E2, g2, _) in zip(*results):
+        assert E1 == E2
+        np.testing.assert_array_equal(g1, g2)
+
+
 def test_n16_instances_match_exact_summation():
     import rbmongpu_gb300 as rg
     N, B, reps = 16, 4096, 16
