@@ -138,7 +138,7 @@ static int rbm_upload(rbmg_psi* p) {
     RBMG_CK(p->dbq.ensure(sizeof(float4) * kp));
     RBMG_CK(p->dWt.ensure(sizeof(float2) * static_cast<size_t>(p->Mpad) * p->N));
     RBMG_CK(launch_rbm_pairs(p->N, p->Mpad, p->dW.as<float2>(), p->db.as<float2>(), p->dWq.as<float4>(),
-                             p->dbq.as<float4>(), p->dWt.as<float2>(), stream()));
+                             p->dbq.as<float4>(), p->dWt.as<float4>(), stream()));
     if (rbm_tc_supported(p->N, p->Mpad)) {
         RBMG_CK(p->dWtc.ensure(sizeof(__nv_bfloat16) * rbm_tc_pack_elems(p->Mpad, rbm_tc_kp(p->N))));
         RBMG_CK(launch_rbm_tc_pack(p->N, p->M, p->Mpad, p->dW.as<float2>(), p->dWtc.as<__nv_bfloat16>(), stream()));

@@ -79,7 +79,7 @@ struct rbmg_psi {
     int M = 0, Mpad = 0;
     std::vector<rbmg::cplx> b, W;
     rbmg::DevBuf dW, db, dWq, dbq;     // complex64 rows, and the sampler's paired copies (kernels.h)
-    rbmg::DevBuf dWt;                  // W transposed [Mpad][N] (the local-energy kernel)
+    rbmg::DevBuf dWt;                  // W transposed, units paired [Mpad / 2][N] (RbmDev::Wt4)
     rbmg::DevBuf dWtc;                 // W as BF16 hi / mid / lo tensor-core operands (angles_tc.cu), if supported
     rbmg::DevBuf tc_error;             // set when a tensor-core pass of this psi gave up waiting
     mutable rbmg::DevBuf dW64, db64;   // FP64 copies for the Hilbert-space distance pass, uploaded on use
@@ -103,7 +103,7 @@ struct rbmg_psi {
     rbmg::RbmDev rbm_dev() const {
         return rbmg::RbmDev{N, M, Mpad, static_cast<const float2*>(dW.p), static_cast<const float2*>(db.p),
                             static_cast<const float4*>(dWq.p), static_cast<const float4*>(dbq.p),
-                            static_cast<const float2*>(dWt.p)};
+                            static_cast<const float4*>(dWt.p)};
     }
 };
 

@@ -22,13 +22,15 @@ struct RbmDev {
     // Wq [N][ceil(K / 2)][32], bq [ceil(K / 2)][32]; the unit beyond an odd K is zero
     const float4* Wq;
     const float4* bq;
-    const float2* Wt;    // W transposed, [Mpad][N] (rows of unit j across the spins)
+    // W transposed with units j and j + 4 side by side (the local-energy kernel's pairs):
+    // Wt4 [Mpad / 2][N], entry (p, i) = (x_j, x_j+4, y_j, y_j+4) of spin i's row,
+    // j = 8 (p / 4) + p % 4
+    const float4* Wt4;
 };
 
-// build Wq, bq from W [N][Mpad], b [Mpad] (K = Mpad / 32 hidden units per lane), and
-// Wt [Mpad][N] = W transposed
+// build Wq, bq from W [N][Mpad], b [Mpad] (K = Mpad / 32 hidden units per lane), and Wt4
 cudaError_t launch_rbm_pairs(int N, int Mpad, const float2* W, const float2* b, float4* Wq, float4* bq,
-                             float2* Wt, cudaStream_t st);
+                             float4* Wt4, cudaStream_t st);
 
 // Pauli-string operator in compact form (built from the reference's padded
 // table, include/operator/Operator.hpp:30-88).

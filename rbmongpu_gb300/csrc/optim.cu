@@ -249,7 +249,7 @@ int psi_scatter(rbmg_psi* psi, const double2* packed) {
                                                                          psi->db.as<float2>(), psi->dW.as<float2>());
         RBMG_CK(cudaGetLastError());
         RBMG_CK(launch_rbm_pairs(psi->N, psi->Mpad, psi->dW.as<float2>(), psi->db.as<float2>(), psi->dWq.as<float4>(),
-                                 psi->dbq.as<float4>(), psi->dWt.as<float2>(), stream()));
+                                 psi->dbq.as<float4>(), psi->dWt.as<float4>(), stream()));
         if (psi->dWtc.p)
             RBMG_CK(launch_rbm_tc_pack(psi->N, psi->M, psi->Mpad, psi->dW.as<float2>(),
                                        psi->dWtc.as<__nv_bfloat16>(), stream()));

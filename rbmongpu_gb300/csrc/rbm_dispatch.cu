@@ -45,22 +45,24 @@ __global__ void rbm_pairs_kernel(int N, int Mpad, int KP, const float2* W, const
     (row < N ? Wq[idx] : bq[rem]) = make_float4(a.x, c.x, a.y, c.y);
 }
 
-// Wt [Mpad][N] = W [N][Mpad] transposed
-__global__ void rbm_transpose_kernel(int N, int Mpad, const float2* W, float2* Wt) {
+// Wt4 [Mpad / 2][N]: entry (p, i) = (x_j, x_j+4, y_j, y_j+4) of W[i], j = 8 (p / 4) + p % 4
+__global__ void rbm_transpose_kernel(int N, int Mpad, const float2* W, float4* Wt4) {
     const long idx = static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (idx >= static_cast<long>(N) * Mpad) return;
-    const int j = static_cast<int>(idx / N), i = static_cast<int>(idx - static_cast<long>(j) * N);
-    Wt[idx] = W[static_cast<long>(i) * Mpad + j];
+    if (idx >= static_cast<long>(N) * (Mpad / 2)) return;
+    const int p = static_cast<int>(idx / N), i = static_cast<int>(idx - static_cast<long>(p) * N);
+    const int j = 8 * (p / 4) + p % 4;
+    const float2 a = W[static_cast<long>(i) * Mpad + j], c = W[static_cast<long>(i) * Mpad + j + 4];
+    Wt4[idx] = make_float4(a.x, c.x, a.y, c.y);
 }
 
 cudaError_t launch_rbm_pairs(int N, int Mpad, const float2* W, const float2* b, float4* Wq, float4* bq,
-                             float2* Wt, cudaStream_t st) {
+                             float4* Wt, cudaStream_t st) {
     const int KP = (Mpad / 32 + 1) / 2;
     const long n = static_cast<long>(N + 1) * KP * 32;
     rbm_pairs_kernel<<<static_cast<int>((n + 255) / 256), 256, 0, st>>>(N, Mpad, KP, W, b, Wq, bq);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || !Wt) return e;
-    const long m = static_cast<long>(N) * Mpad;
+    const long m = static_cast<long>(N) * (Mpad / 2);
     rbm_transpose_kernel<<<static_cast<int>((m + 255) / 256), 256, 0, st>>>(N, Mpad, W, Wt);
     return cudaGetLastError();
 }

@@ -765,13 +765,26 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) rbm_eloc_t_kernel(RbmDev 
     }
     constexpr int KP = (K + 1) / 2;
     constexpr int MP = 32 * K;
-    // (theta.re, theta.im, f.re, f.im) of every unit, in the warp's slice
+    // the angles and f of every unit in the warp's slice, units j and j + 4 side by side
+    // (the pairs the loops below evaluate): pair p = 4 (j / 8) + j % 4 holds
+    // tA[p] = (theta.re_j, theta.re_j+4, theta.im_j, theta.im_j+4) and
+    // tB[p] = (f.re_j, f.re_j+4, f.im_j, f.im_j+4)
     __shared__ float4 tf_sm[kWarpsPerBlock][MP];
-    float4* tf = tf_sm[wib];
+    float4* tA = tf_sm[wib];
+    float4* tB = tA + MP / 2;
     {
         // a lane's pair kk holds units lane + 64 kk and lane + 64 kk + 32
         pair_t tr[KP], ti[KP];
         rbm_refresh2(P, s, tr, ti, lane);
+        float* fa = reinterpret_cast<float*>(tA);
+        float* fb = reinterpret_cast<float*>(tB);
+        auto put = [&](int j, float a, float b, float r, float i) {
+            const int p = 4 * (j >> 3) + (j & 3), h = (j >> 2) & 1;
+            fa[4 * p + h] = a;
+            fa[4 * p + 2 + h] = b;
+            fb[4 * p + h] = r;
+            fb[4 * p + 2 + h] = i;
+        };
 #pragma unroll
         for (int kk = 0; kk < KP; kk++) {
             // f(theta) with the same approximate reciprocal as f(theta'') below
@@ -782,8 +795,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) rbm_eloc_t_kernel(RbmDev 
             up2(v.re, r0, r1);
             up2(v.im, i0, i1);
             const int j0 = lane + 64 * kk;
-            tf[j0] = make_float4(a0, b0, r0, i0);
-            if (2 * kk + 1 < K) tf[j0 + 32] = make_float4(a1, b1, r1, i1);
+            put(j0, a0, b0, r0, i0);
+            if (2 * kk + 1 < K) put(j0 + 32, a1, b1, r1, i1);
         }
     }
     __syncwarp();
@@ -807,35 +820,34 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) rbm_eloc_t_kernel(RbmDev 
         if (live) {
             const int nf = op.nflip[n];
             const int off = op.flip_off[n];
+            // pairs p = q, q + 4, ...: units (j, j + 4), j = q, q + 8, ...
             if (nf == 1) {
                 const int site = op.flip_sites[off];
                 const pair_t two_s = splat2(s.up(site) ? -2.0f : 2.0f);
-                const float2* wcol = P.Wt + site;
+                const float4* wcol = P.Wt4 + site;
 #pragma unroll 2
-                for (int j = q; j < MP; j += 8) {
-                    const float2 w0 = __ldg(wcol + static_cast<long>(j) * N);
-                    const float2 w1 = __ldg(wcol + static_cast<long>(j + 4) * N);
-                    const float4 a0 = tf[j], a1 = tf[j + 4];
-                    const Pair2 g = lc_c2_approx(fma2(two_s, pk2(w0.x, w1.x), pk2(a0.x, a1.x)),
-                                                 fma2(two_s, pk2(w0.y, w1.y), pk2(a0.y, a1.y)));
-                    sr = add2(sr, sub2(g.re, pk2(a0.z, a1.z)));
-                    si = add2(si, sub2(g.im, pk2(a0.w, a1.w)));
+                for (int p = q; p < MP / 2; p += 4) {
+                    const float4 w = __ldg(wcol + static_cast<long>(p) * N);
+                    const float4 a = tA[p], f = tB[p];
+                    const Pair2 g = lc_c2_approx(fma2(two_s, pk2(w.x, w.y), pk2(a.x, a.y)),
+                                                 fma2(two_s, pk2(w.z, w.w), pk2(a.z, a.w)));
+                    sr = add2(sr, sub2(g.re, pk2(f.x, f.y)));
+                    si = add2(si, sub2(g.im, pk2(f.z, f.w)));
                 }
             } else {
-                for (int j = q; j < MP; j += 8) {
-                    const float4 a0 = tf[j], a1 = tf[j + 4];
-                    pair_t xr = pk2(a0.x, a1.x), xi = pk2(a0.y, a1.y);
+                for (int p = q; p < MP / 2; p += 4) {
+                    const float4 a = tA[p], f = tB[p];
+                    pair_t xr = pk2(a.x, a.y), xi = pk2(a.z, a.w);
                     for (int u = 0; u < nf; u++) {
                         const int site = op.flip_sites[off + u];
                         const pair_t two_s = splat2(s.up(site) ? -2.0f : 2.0f);
-                        const float2 w0 = __ldg(P.Wt + static_cast<long>(j) * N + site);
-                        const float2 w1 = __ldg(P.Wt + static_cast<long>(j + 4) * N + site);
-                        xr = fma2(two_s, pk2(w0.x, w1.x), xr);
-                        xi = fma2(two_s, pk2(w0.y, w1.y), xi);
+                        const float4 w = __ldg(P.Wt4 + static_cast<long>(p) * N + site);
+                        xr = fma2(two_s, pk2(w.x, w.y), xr);
+                        xi = fma2(two_s, pk2(w.z, w.w), xi);
                     }
                     const Pair2 g = lc_c2_approx(xr, xi);
-                    sr = add2(sr, sub2(g.re, pk2(a0.z, a1.z)));
-                    si = add2(si, sub2(g.im, pk2(a0.w, a1.w)));
+                    sr = add2(sr, sub2(g.re, pk2(f.x, f.y)));
+                    si = add2(si, sub2(g.im, pk2(f.z, f.w)));
                 }
             }
         }
