@@ -928,6 +928,94 @@ def run_plain(args):
     print(json.dumps(line))
 
 
+MCG_CHAINS, MCG_SWEEPS, MCG_THERM = 4096, 1000, 200
+
+
+def run_mc_gradient(args):
+    """One step = ExpectationValue.gradient over a MonteCarloLoop pass of the plain
+    Metropolis configuration: 4096 walkers of the N=64, M=128 complex RBM (sigma 0.05,
+    PCG64(102)) on the periodic 8x8 transverse-field Ising model (J = 1, h = 3), random
+    +-1 starts, 200 thermalisation sweeps, then 1000 sweeps of 64 single-flip proposals
+    with E_loc and O_k of every walker after every sweep: <E> and the reference gradient
+    <E O_k*> + conj<E_k> - 2 <E><O_k*> over 4 096 000 samples (the call a user makes; its
+    results come back to the host)."""
+    import torch
+    import rbmongpu_gb300 as rg
+    torch.cuda.set_device(0)
+    b, W = sm_workload()
+    N, M = SM_N, SM_M
+    psi = rg.Psi(np.zeros(N), np.zeros(N), b, W, 1.0, False, True)
+    op_t = rg.operators.tfim_square(8, 1.0, 3.0)
+    op = rg.Operator(*op_t)
+    ev = rg.ExpectationValue()
+    mk = lambda k: rg.MonteCarloLoop(MCG_CHAINS * MCG_SWEEPS, 1, MCG_THERM, MCG_CHAINS, seed=2024 + k)   # noqa: E731
+    for k in range(args.warmup):
+        ev.gradient(psi, op, mk(k))
+    sp = rg.library_stream()
+    stream = torch.cuda.ExternalStream(sp)
+    K = args.steps
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    walls = []
+    clocks = ClockSampler(0)
+    clocks.start()
+    for k in range(K):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        starts[k].record(stream)
+        g, E = ev.gradient(psi, op, mk(100 + k))
+        ends[k].record(stream)
+        walls.append(time.perf_counter() - t0)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = np.array([a.elapsed_time(e) for a, e in zip(starts, ends)])
+    assert np.isfinite(E) and np.all(np.isfinite(g))
+    samples = MCG_CHAINS * MCG_SWEEPS
+    sec = float(ms.mean()) / 1e3
+    e2e_s = float(np.mean(walls))
+    n_off = N   # one X string per site
+    per_sample = (flops_per_sweep(N, M) + flops_per_eloc(N, M, n_off) + n_off * M * (44 + 8) + (N + 1) * M * (6 + 16))
+    flops = MCG_CHAINS * (MCG_THERM + MCG_SWEEPS) * flops_per_sweep(N, M) + samples * (per_sample - flops_per_sweep(N, M))
+    peak = max(ctypes_probe_fp32(), ctypes_probe_fp32(pairs=True))
+    cpu = None
+    if args.cpu_seconds > 0:
+        # the reference's arithmetic (FP64) of the same method: 4 chains, 5 thermalisation
+        # sweeps, then sweeps with E_loc, and the gradient estimator on their samples
+        from oracle import pyoracle as po
+        opsi, oop = po.RBM(b, W, 1.0), po.Op(*op_t)
+        n_s = 48
+        t0 = time.perf_counter()
+        ospins, _, _, _, _ = po.mc_run(opsi, oop, 4, n_s, 1, 5, seed=5, prec=po.OR_PREC_REF64, want_eloc=True)
+        po.samples_gradient(opsi, oop, ospins.reshape(-1, ospins.shape[-1]))
+        dt = time.perf_counter() - t0
+        cpu = {"value": 4 * n_s / dt, "unit": "samples/s", "cores": 1, "kind": "port",
+               "sample": "4 chains x (5 thermalisation + 48 measured sweeps) with E_loc, then the O_k gradient "
+                         "estimator (E_k term included) on their 192 samples, FP64 restatement, one core"}
+    P = psi.num_params
+    line = {
+        "metric": "plain MCMC with E_loc and the O_k gradient every sweep: samples/s (N=64, M=128, 8x8 TFIM)",
+        "value": samples / sec, "unit": "samples/s", "n_gpus": 1, "steps": K, "warmup": args.warmup,
+        "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (complex64), f64 sums", "data": "synthetic (seeded PCG64 parameters)",
+        "config": {"workload": "rbm_n64_m128_tfim8x8_h3_mc_gradient", "N": N, "M": M, "walkers": MCG_CHAINS,
+                   "therm_sweeps": MCG_THERM, "measured_sweeps": MCG_SWEEPS,
+                   "step": "MonteCarloLoop pass + E_loc + O_k gradient sums of every sample (one gradient call)",
+                   "l2": "inputs larger than L2 are not involved: the pass reads W (64 KB) and writes sums"},
+        "eloc_per_s": samples / sec,
+        "e2e": {"value": samples / e2e_s, "unit": "samples/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 16 * P + 16},
+        "roofline": {"bound": "fp32", "achieved": flops / sec / 1e12, "peak": peak, "unit": "TFLOP/s",
+                     "frac": flops / sec / 1e12 / peak, "traffic": None,
+                     "peak_source": "measured in this run: the larger of the library's scalar and packed-pair FP32 "
+                                    "FMA probes",
+                     "kernel": "the whole call (sampler sweeps, local energies, estimator sums)",
+                     "flops_per_step": flops},
+        "cpu_baseline": cpu,
+        "clocks": clk,
+    }
+    print(json.dumps(line))
+
+
 def ctypes_probe_fp32(pairs=False):
     """FP32 FMA rate of this GPU from the library's probe kernel (scalar or packed pairs)."""
     import ctypes
@@ -968,11 +1056,12 @@ def main():
     ap.add_argument("--ac-sigma", type=float, default=SIGMA, help="autocorrelation workload: weight scale")
     ap.add_argument("--ac-rows", type=int, default=20000, help="autocorrelation workload: rows of each chain")
     ap.add_argument("--workload", default="learned",
-                    choices=["learned", "serving", "s_matrix", "deep", "autocorrelation", "plain"],
+                    choices=["learned", "serving", "s_matrix", "deep", "autocorrelation", "plain", "mc_gradient"],
                     help="learned: the N=100 learned-vs-plain chains (headline); serving: 64 uneven RBMs; "
                          "s_matrix: get_S_matrix of the N=64, M=128 RBM over 16384 MC samples; "
                          "deep: the PsiDeep 100-200-100-50 gradient through the adjoint kernels; "
-                         "plain: 10-sweep launches of the plain sampler alone (its roofline, profiling)")
+                         "plain: 10-sweep launches of the plain sampler alone (its roofline, profiling); "
+                         "mc_gradient: the N=64, M=128 8x8-TFIM gradient over 4096 walkers x 1000 sweeps")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -995,6 +1084,10 @@ def main():
     if args.workload == "plain" and args.impl == "ours":
         if rank == 0:
             run_plain(args)
+        return
+    if args.workload == "mc_gradient" and args.impl == "ours":
+        if rank == 0:
+            run_mc_gradient(args)
         return
     if args.workload == "autocorrelation":
         if rank == 0 and args.impl == "ours":
