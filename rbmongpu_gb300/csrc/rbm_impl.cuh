@@ -464,9 +464,16 @@ __device__ __forceinline__ double2 rbm_local_energy(const RbmDev& P, const OpDev
             }
         }
         float2 part = make_float2(0.0f, 0.0f);
+        float2 th[GRAD ? K : 1];
 #pragma unroll
         for (int k = 0; k < K; k++) {
-            const float2 g = lc_c(nr[k], ni[k]);
+            float2 g;
+            if (GRAD) {
+                // f and tanh of the flipped angle from one denominator (lc_tanh_approx)
+                lc_tanh_approx(nr[k], ni[k], g, th[k]);
+            } else {
+                g = lc_c(nr[k], ni[k]);
+            }
             part.x += g.x - f[k].x;
             part.y += g.y - f[k].y;
         }
@@ -477,7 +484,7 @@ __device__ __forceinline__ double2 rbm_local_energy(const RbmDev& P, const OpDev
             float2* xrow = X + static_cast<long>(op.offdiag_slot[n]) * P.Mpad + lane;
 #pragma unroll
             for (int k = 0; k < K; k++) {
-                const float2 t2 = tanh_c(nr[k], ni[k]);
+                const float2 t2 = th[k];
                 const float2 v = make_float2(ex * t2.x - ey * t2.y, ex * t2.y + ey * t2.x);
                 U[k].x += v.x;
                 U[k].y += v.y;
@@ -692,18 +699,21 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) rbm_est_kernel(RbmDev P, 
         float tr[K], ti[K];
         rbm_refresh(P, s, tr, ti, lane);
         float2 f[K], T[K], U[K];
+        const bool grad = (L.flags & EST_GRADVEC) != 0;
 #pragma unroll
-        for (int k = 0; k < K; k++) f[k] = lc_c(tr[k], ti[k]);
+        for (int k = 0; k < K; k++) {
+            // with the O_k vectors: f and tanh from one denominator, the same evaluation as
+            // the flipped angles' in rbm_local_energy<true> (so that unchanged units cancel)
+            if (grad) lc_tanh_approx(tr[k], ti[k], f[k], T[k]);
+            else f[k] = lc_c(tr[k], ti[k]);
+        }
         if (L.flags & EST_LOGPSI) {
             const double2 lp = warp_log_psi(f);
             if (lane == 0) L.logpsi[t] = lp;
         }
-        if (L.flags & EST_GRADVEC) {
+        if (grad) {
 #pragma unroll
-            for (int k = 0; k < K; k++) {
-                T[k] = tanh_c(tr[k], ti[k]);
-                L.T[t * P.Mpad + lane + 32 * k] = T[k];
-            }
+            for (int k = 0; k < K; k++) L.T[t * P.Mpad + lane + 32 * k] = T[k];
             const double2 e = rbm_local_energy<true>(P, op, s, tr, ti, f, T, U,
                                                      L.X + t * op.num_offdiag * P.Mpad, lane);
             const float shx = static_cast<float>(L.e_shift.x), shy = static_cast<float>(L.e_shift.y);
