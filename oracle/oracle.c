@@ -267,6 +267,11 @@ static inline float div_pos_f32(float num, float den) {
     return fmaf(r, fmaf(-den, q, num), q);
 }
 
+/* div_pos_f32 over arrays (a test hook: the reciprocal's error bound) */
+void or_div_pos_f32_n(const float* num, const float* den, float* out, long n) {
+    for (long i = 0; i < n; i++) out[i] = div_pos_f32(num[i], den[i]);
+}
+
 float or_lc_re_f32(float x, float y) {
     const lc_den32 d = lc_den_f32(x, y);
     const float nr = fmaf(-F_LC_NB, d.p, F_LC_NA);

@@ -78,6 +78,7 @@ void or_mt_words(uint32_t seed, int count, uint32_t* out);
 void or_logcosh(double re, double im, double* out);   /* out[2] */
 void or_tanh(double re, double im, double* out);
 float or_lc_re_f32(float x, float y);
+void or_div_pos_f32_n(const float* num, const float* den, float* out, long n);
 void or_lc_f32(float x, float y, float* out);
 void or_tanh_f32(float x, float y, float* out);
 float or_expf_det(float x);

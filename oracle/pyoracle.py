@@ -463,6 +463,17 @@ def lc_re_f32(x, y):
     return lib().or_lc_re_f32(C.c_float(x), C.c_float(y))
 
 
+def div_pos_f32(num, den):
+    """The FMA-only quotient of the Metropolis test (device_math.cuh::div_pos), elementwise."""
+    num = np.ascontiguousarray(num, np.float32)
+    den = np.ascontiguousarray(den, np.float32)
+    out = np.empty_like(num)
+    fp = C.POINTER(C.c_float)
+    lib().or_div_pos_f32_n(num.ctypes.data_as(fp), den.ctypes.data_as(fp), out.ctypes.data_as(fp),
+                           C.c_long(num.size))
+    return out
+
+
 def logf_det(x):
     """The deterministic FP32 log of the proposal's softmax (device_math.cuh::logf_det)."""
     return lib().or_logf_det(C.c_float(x))

@@ -149,3 +149,20 @@ def test_deterministic_log_of_the_restatement():
     got = np.array([po.logf_det(float(x)) for x in xs], np.float64)
     ref = np.log(xs.astype(np.float64))
     assert np.all(np.abs(got - ref) <= 2e-7 * np.maximum(np.abs(ref), 1.0))
+
+
+def test_div_pos_is_within_an_ulp_of_the_ieee_quotient():
+    """div_pos (device_math.cuh; the Metropolis test's quotient, replayed here by the
+    oracle bit for bit): within one ulp of the correctly rounded quotient for every
+    denominator the activation produces (|D(u)|^2 >= 84) and numerators of any sign, and
+    equal to it for all but a small fraction of inputs."""
+    rng = np.random.default_rng(21)
+    n = 1_000_000
+    den = np.float32(84.0) * np.exp2(rng.uniform(0.0, 40.0, n)).astype(np.float32)
+    num = (rng.normal(size=n) * np.exp2(rng.uniform(-20.0, 60.0, n))).astype(np.float32)
+    got = po.div_pos_f32(num, den)
+    ref = (num / den).astype(np.float32)       # IEEE division, correctly rounded
+    ulp = np.spacing(np.abs(ref)).astype(np.float64)
+    err = np.abs(got.astype(np.float64) - ref.astype(np.float64))
+    assert np.all(err <= ulp), float((err / ulp).max())
+    assert np.mean(got != ref) < 1e-3, float(np.mean(got != ref))
